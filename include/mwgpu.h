@@ -1,0 +1,174 @@
+/*
+ * mwgpu.h -- C-ABI of the GB300 operator-application library.
+ *
+ * This is the boundary MRCPP's host code binds to.  The host keeps its
+ * FunctionTree / OperatorTree objects (src/trees/FunctionTree.h,
+ * src/trees/OperatorTree.h) and hands flat copies of them to the device:
+ * operator node caches once per (operator, apply precision), the input tree
+ * once per apply, and the output tree level by level.  The GPU side replaces
+ * ConvolutionCalculator::calcNodeVector (src/treebuilders/TreeCalculator.h:39-50
+ * via ConvolutionCalculator.cpp:224-382) and the two whole-tree transforms of
+ * apply (src/treebuilders/apply.cpp:82-84).  Only D = 3, T = double is
+ * accelerated.  There is no CPU fallback: every entry point needs a CUDA
+ * device and returns MWGPU_ERR_NO_DEVICE without one.
+ *
+ * Conventions
+ *   - plain pointers and sizes, host memory unless stated otherwise;
+ *   - a node index is 4 ints (scale, l0, l1, l2) like mrcpp::NodeIndex<3>
+ *     (src/trees/NodeIndex.h:39-97);
+ *   - a node's coefficients are 8*(k+1)^3 doubles, component c (bit d set =
+ *     wavelet in direction d) at c*(k+1)^3, x fastest inside a component, the
+ *     layout of MWNode::coefs (src/trees/MWNode.h:183, FunctionNode.cpp:77-83);
+ *   - an operator node is 4*(k+1)^2 doubles (T, C, B, A; each (k+1)x(k+1)
+ *     column-major) plus 4 component norms, the layout of OperatorNode::coefs
+ *     (src/trees/OperatorNode.cpp:96-104);
+ *   - every call returns an mwgpu_status; MWGPU_OK = 0.  The reference aborts on
+ *     errors (MSG_ABORT, src/utils/Printer.h:159-170); here the caller gets a
+ *     code and mwgpu_last_error() gives the message.
+ */
+#ifndef MWGPU_H
+#define MWGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int mwgpu_status;
+#define MWGPU_OK 0
+#define MWGPU_ERR_BAD_ARG 1
+#define MWGPU_ERR_OOM 2
+#define MWGPU_ERR_DEVICE 3
+#define MWGPU_ERR_TIMEOUT 4
+#define MWGPU_ERR_NO_DEVICE 5
+#define MWGPU_ERR_INTERNAL 6
+
+#define MWGPU_PREC_FP64 0  /* plain form: FP64 throughout */
+#define MWGPU_PREC_MIXED 1 /* mixed form: FP32 contractions, FP64 accumulation */
+
+#define MWGPU_TOPDOWN 0
+#define MWGPU_BOTTOMUP 1
+
+typedef struct mwgpu_ctx mwgpu_ctx;
+typedef struct mwgpu_oper mwgpu_oper;
+typedef struct mwgpu_tree mwgpu_tree;
+
+typedef struct {
+    int device;         /* CUDA device ordinal */
+    int precision;      /* MWGPU_PREC_FP64 or MWGPU_PREC_MIXED */
+    int reserved[6];
+} mwgpu_config;
+
+/* World box + basis: mrcpp::MultiResolutionAnalysis<3>
+ * (src/trees/MultiResolutionAnalysis.h:59-65, BoundingBox.cpp:47-80). */
+typedef struct {
+    int order;          /* k; K = k+1 */
+    int root_scale;
+    int corner[3];
+    int nbox[3];
+    int max_scale;      /* root_scale + max depth */
+    double sf;          /* uniform scaling factor */
+    /* 8 (k+1)x(k+1) column-major filters: compression H0t,H1t,G0t,G1t then
+     * reconstruction H0,G0,H1,G1 (MWFilter::getSubFilter, MWFilter.cpp:100-133) */
+    const double *filters;
+} mwgpu_mra_desc;
+
+/* Operator node caches of a ConvolutionOperator<3> (MWOperator::oper_exp,
+ * isotropic; OperatorTree::setupOperNodeCache, OperatorTree.cpp:200-238).
+ * For term t and depth d < depth[t] the nodes for l = -L..L, L =
+ * max_transl[sum(depth[0..t-1]) + d], are stored consecutively. */
+typedef struct {
+    int n_terms;
+    int order;
+    const int *depth;        /* [n_terms] number of operator scales per term */
+    const int *max_transl;   /* [sum depth] */
+    const double *blocks;    /* [nodes * 4 * K*K] */
+    const double *norms;     /* [nodes * 4], OperatorNode::calcComponentNorm */
+    double build_prec;       /* norm precision of the operator trees */
+} mwgpu_oper_desc;
+
+/* Flat FunctionTree<3>.  child0[i] = index of the first of the 8 contiguous
+ * children of node i, or -1 for a leaf. */
+typedef struct {
+    int n_nodes;
+    const int *idx;          /* [n_nodes * 4] */
+    const int *child0;       /* [n_nodes] */
+    const double *coefs;     /* [n_nodes * 8K^3] or NULL (zeros) */
+    const double *norms;     /* [n_nodes * 8] or NULL (computed on the device) */
+} mwgpu_tree_desc;
+
+/* Counters of one level (OperatorStatistics, OperatorStatistics.cpp:84-105). */
+typedef struct {
+    unsigned long long node_terms;   /* (g, f, term) triples with >= 1 contracted component */
+    unsigned long long components;   /* contracted (g, f, term, ft, gt) component products */
+    unsigned long long band_nodes;   /* (g, f) pairs inside the operator band */
+    unsigned long long gen_nodes;    /* input GenNodes created */
+    double device_ms;                /* device time of the level (CUDA events) */
+    double contract_ms;              /* device time of the contraction kernel */
+} mwgpu_level_stats;
+
+/* Context on one device.  Replaces nothing in the reference (MRCPP has no
+ * device state); owns the stream and scratch buffers. */
+mwgpu_status mwgpu_init(mwgpu_ctx **ctx, const mwgpu_config *cfg);
+mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx);
+/* Message of the last failed call on this context (or of the last failed
+ * mwgpu_init when ctx is NULL). */
+const char *mwgpu_last_error(const mwgpu_ctx *ctx);
+mwgpu_status mwgpu_set_precision(mwgpu_ctx *ctx, int precision);
+
+/* Uploads the operator node caches and derives, for apply precision `prec`,
+ * the band widths (MWOperator::calcBandWidths, MWOperator.cpp:78-108 and
+ * OperatorTree::calcBandWidth, OperatorTree.cpp:109-134) and the band-size
+ * factors (ConvolutionCalculator::initBandSizes, ConvolutionCalculator.cpp:105-139).
+ * prec < 0 uses build_prec. */
+mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_oper_desc *oper, double prec,
+                                   mwgpu_oper **out);
+mwgpu_status mwgpu_free_operator(mwgpu_ctx *ctx, mwgpu_oper *oper);
+/* Band widths at the uploaded precision: widths[t * (rows) * 5 + d * 5 + c]
+ * (c = T,C,B,A,max), rows = *n_rows, and band_max[rows]. Either pointer may be
+ * NULL to query n_rows only. */
+mwgpu_status mwgpu_operator_bandwidths(mwgpu_ctx *ctx, const mwgpu_oper *oper, int *n_rows, int *widths, int *band_max);
+
+/* Input tree (the `inp` of apply, compressed s+d form, all nodes).  GenNodes
+ * the operator band needs are created on the device from these nodes, like
+ * MWTree::getNode (MWTree.cpp:340-352); the host never sees them, matching
+ * inp.deleteGenerated() at the end of apply (apply.cpp:86-87). */
+mwgpu_status mwgpu_upload_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *tree, mwgpu_tree **out);
+/* Output tree with the given topology and zero coefficients. */
+mwgpu_status mwgpu_create_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *tree, mwgpu_tree **out);
+/* Appends nodes (e.g. the children made by TreeAdaptor::splitNodeVector,
+ * TreeAdaptor.h:41-52) and sets child0 of their parents. The new nodes get
+ * indices n_nodes .. n_nodes+n-1 in order. */
+mwgpu_status mwgpu_tree_add_nodes(mwgpu_ctx *ctx, mwgpu_tree *tree, int n, const int *idx, int n_parents, const int *parent_ids,
+                                  const int *parent_child0);
+mwgpu_status mwgpu_tree_size(const mwgpu_tree *tree, int *n_nodes);
+mwgpu_status mwgpu_free_tree(mwgpu_ctx *ctx, mwgpu_tree *tree);
+
+/* One TreeBuilder iteration of apply: computes the nodes out[node_ix[0..n)]
+ * (ConvolutionCalculator::calcNode for each, ConvolutionCalculator.cpp:224-274)
+ * with the screening threshold that calcNode derives from out_sqnorm
+ * (:241-248; out_sqnorm <= 0 disables norm screening exactly like the
+ * reference).  Coefficients stay on the device; norms_out (n*8 doubles, may be
+ * NULL) receives the component norms the split test needs. */
+mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n,
+                               double prec, double out_sqnorm, double *norms_out, mwgpu_level_stats *stats);
+
+/* Whole-tree transform of the output tree: MWGPU_TOPDOWN with overwrite = 0
+ * adds the coarse-scale contributions downwards (MWTree::mwTransformDown,
+ * MWTree.cpp:194-216); MWGPU_BOTTOMUP recompresses (MWTree::mwTransformUp,
+ * MWTree.cpp:166-181). */
+mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tree, int direction, int overwrite);
+
+/* Copies coefficients and/or norms of all real nodes back (either may be NULL). */
+mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tree, double *coefs, double *norms);
+
+/* Synchronises the context stream; returns device errors. */
+mwgpu_status mwgpu_sync(mwgpu_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MWGPU_H */

@@ -1,0 +1,94 @@
+/*
+ * mwhost.h -- C interface of the host-side mirror of MRCPP used to drive the
+ * GPU path without MRCPP itself: MultiResolutionAnalysis<3>, FunctionTree<3>,
+ * GaussFunc/GaussExp projection, PoissonOperator/HelmholtzOperator
+ * construction and mrcpp::apply.  Names and argument meaning follow the
+ * reference API:
+ *   mwh_apply          mrcpp::apply(prec, out, oper, inp, maxIter, absPrec)   src/treebuilders/apply.h:41
+ *   mwh_poisson        mrcpp::PoissonOperator(MRA, prec)                       src/operators/PoissonOperator.h:44
+ *   mwh_helmholtz      mrcpp::HelmholtzOperator(MRA, mu, prec)                 src/operators/HelmholtzOperator.h:44
+ *   mwh_project_gauss  mrcpp::build_grid + mrcpp::project                      src/treebuilders/grid.h, project.h
+ *   mwh_copy_grid      mrcpp::copy_grid                                         src/treebuilders/grid.h
+ *   mwh_dot            mrcpp::dot(FunctionTree, FunctionTree)                  src/treebuilders/multiply.h
+ * Every function returns 0 on success, a nonzero mwgpu_status-like code on
+ * error; mwh_last_error() gives the message (the reference aborts instead).
+ */
+#ifndef MWHOST_H
+#define MWHOST_H
+
+#include "mwgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mwh_mra mwh_mra;
+typedef struct mwh_tree mwh_tree;
+typedef struct mwh_oper mwh_oper;
+
+typedef struct {
+    unsigned long long node_terms; /* summed over levels */
+    unsigned long long components;
+    unsigned long long band_nodes;
+    unsigned long long gen_nodes;
+    int iterations;                /* TreeBuilder iterations */
+    int out_nodes;                 /* nodes of the output tree */
+    double device_ms;              /* device time of all levels */
+    double contract_ms;            /* device time of the contraction kernels */
+    double transform_ms;           /* wall time of the TopDown + BottomUp transforms */
+    double wall_ms;                /* wall time of the whole apply */
+} mwh_apply_stats;
+
+const char *mwh_last_error(void);
+/* Path of the MW table file (filters, cross correlation); default: found next to the library. */
+int mwh_set_table_path(const char *path);
+
+/* MultiResolutionAnalysis<3>(BoundingBox<3>(n, corner, nbox, {sf,sf,sf}), basis(type, order), max_depth);
+ * type 0 = Legendre, 1 = Interpolating. */
+int mwh_mra_create(int type, int order, int root_scale, const int *corner, const int *nbox, double sf, int max_depth, mwh_mra **out);
+/* MultiResolutionAnalysis<3>({lb, ub}, ...) (BoundingBox.cpp:47-80) */
+int mwh_mra_from_bounds(int type, int order, int lb, int ub, int max_depth, mwh_mra **out);
+void mwh_mra_free(mwh_mra *mra);
+/* MRA descriptor for the C-ABI; filters must hold 8*(k+1)^2 doubles. */
+int mwh_mra_desc(const mwh_mra *mra, mwgpu_mra_desc *desc, double *filters);
+
+int mwh_tree_create(const mwh_mra *mra, mwh_tree **out);
+void mwh_tree_free(mwh_tree *tree);
+/* n Gaussians coef * exp(-exp * |r - pos|^2) (pos: 3n doubles). */
+int mwh_build_grid_gauss(mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos);
+int mwh_project_gauss(double prec, mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos, int max_iter,
+                      int abs_prec);
+int mwh_copy_grid(mwh_tree *out, const mwh_tree *inp);
+/* node count (non-generated nodes) and tree square norm */
+int mwh_tree_info(const mwh_tree *tree, int *n_nodes, double *square_norm);
+/* flat copy: idx[4n], child0[n] (local numbering), coefs[n*8K^3], norms[n*8]; any may be NULL */
+int mwh_tree_export(const mwh_tree *tree, int *idx, int *child0, double *coefs, double *norms);
+/* replaces the tree with the given flat tree (same layout as export; roots first) */
+int mwh_tree_import(mwh_tree *tree, int n, const int *idx, const int *child0, const double *coefs, double square_norm);
+double mwh_dot(const mwh_tree *a, const mwh_tree *b);
+double mwh_evalf(const mwh_tree *tree, double x, double y, double z);
+double mwh_integrate(const mwh_tree *tree);
+
+int mwh_poisson(const mwh_mra *mra, double prec, mwh_oper **out);
+int mwh_helmholtz(const mwh_mra *mra, double mu, double prec, mwh_oper **out);
+void mwh_oper_free(mwh_oper *oper);
+/* number of terms, total operator nodes, total (term, depth) rows */
+int mwh_oper_info(const mwh_oper *oper, int *n_terms, int *n_nodes, int *n_rows);
+/* flat node caches: depth[T], max_transl[rows], blocks[nodes*4K^2], norms[nodes*4],
+ * kernel exponents/coefficients[T]; any may be NULL */
+int mwh_oper_export(const mwh_oper *oper, int *depth, int *max_transl, double *blocks, double *norms, double *kexp, double *kcoef);
+/* operator descriptor pointing into the operator's own arrays (valid while oper lives) */
+int mwh_oper_desc(const mwh_oper *oper, mwgpu_oper_desc *desc);
+/* kernel of PoissonKernel/HelmholtzKernel alone (no trees): returns the term count,
+ * fills exps/coefs when non-NULL (cap entries) */
+int mwh_poisson_kernel(double eps, double r_min, double r_max, int cap, double *exps, double *coefs);
+int mwh_helmholtz_kernel(double mu, double eps, double r_min, double r_max, int cap, double *exps, double *coefs);
+
+/* mrcpp::apply on the GPU: precision = MWGPU_PREC_FP64 or MWGPU_PREC_MIXED. */
+int mwh_apply(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int max_iter, int abs_prec, int precision, mwh_apply_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MWHOST_H */

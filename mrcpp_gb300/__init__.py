@@ -1,0 +1,352 @@
+"""mrcpp_gb300: GB300-native multiwavelet operator application.
+
+Python mirror of the MRCPP interface for the operator-application path
+(``mrcpp::apply`` with ``PoissonOperator`` / ``HelmholtzOperator``), bound
+with ctypes to ``libmwgpu.so``.  The library holds the sm_103a CUDA kernels
+behind the C-ABI of ``include/mwgpu.h`` and the C++ host mirror of
+``include/mwhost.h`` (MRA, FunctionTree, projection, operator construction).
+
+There is no CPU implementation of the operator application here: ``apply``
+always runs on the GPU and raises ``MWGPUError`` when no device or no library
+is available.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "MWGPUError", "lib", "MRA", "FunctionTree", "PoissonOperator", "HelmholtzOperator", "ConvolutionOperator",
+    "build_grid", "project", "apply", "copy_grid", "dot", "poisson_kernel", "helmholtz_kernel",
+    "LEGENDRE", "INTERPOLATING", "FP64", "MIXED",
+]
+
+LEGENDRE = 0
+INTERPOLATING = 1
+FP64 = 0
+MIXED = 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmwgpu.so")
+
+
+class MWGPUError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("mwgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class MwgpuMraDesc(C.Structure):
+    _fields_ = [("order", C.c_int), ("root_scale", C.c_int), ("corner", C.c_int * 3), ("nbox", C.c_int * 3),
+                ("max_scale", C.c_int), ("sf", C.c_double), ("filters", C.POINTER(C.c_double))]
+
+
+class MwgpuOperDesc(C.Structure):
+    _fields_ = [("n_terms", C.c_int), ("order", C.c_int), ("depth", C.POINTER(C.c_int)), ("max_transl", C.POINTER(C.c_int)),
+                ("blocks", C.POINTER(C.c_double)), ("norms", C.POINTER(C.c_double)), ("build_prec", C.c_double)]
+
+
+class MwgpuTreeDesc(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("idx", C.POINTER(C.c_int)), ("child0", C.POINTER(C.c_int)),
+                ("coefs", C.POINTER(C.c_double)), ("norms", C.POINTER(C.c_double))]
+
+
+class MwgpuConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("reserved", C.c_int * 6)]
+
+
+class MwgpuLevelStats(C.Structure):
+    _fields_ = [("node_terms", C.c_ulonglong), ("components", C.c_ulonglong), ("band_nodes", C.c_ulonglong),
+                ("gen_nodes", C.c_ulonglong), ("device_ms", C.c_double), ("contract_ms", C.c_double)]
+
+
+class MwhApplyStats(C.Structure):
+    _fields_ = [("node_terms", C.c_ulonglong), ("components", C.c_ulonglong), ("band_nodes", C.c_ulonglong),
+                ("gen_nodes", C.c_ulonglong), ("iterations", C.c_int), ("out_nodes", C.c_int), ("device_ms", C.c_double),
+                ("contract_ms", C.c_double), ("transform_ms", C.c_double), ("wall_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_P = C.c_void_p
+_PI = C.POINTER(C.c_int)
+_PD = C.POINTER(C.c_double)
+_SIGS = {
+    # device C-ABI (include/mwgpu.h)
+    "mwgpu_init": (C.c_int, [C.POINTER(_P), C.POINTER(MwgpuConfig)]),
+    "mwgpu_destroy": (C.c_int, [_P]),
+    "mwgpu_last_error": (C.c_char_p, [_P]),
+    "mwgpu_set_precision": (C.c_int, [_P, C.c_int]),
+    "mwgpu_upload_operator": (C.c_int, [_P, C.POINTER(MwgpuMraDesc), C.POINTER(MwgpuOperDesc), C.c_double, C.POINTER(_P)]),
+    "mwgpu_free_operator": (C.c_int, [_P, _P]),
+    "mwgpu_operator_bandwidths": (C.c_int, [_P, _P, _PI, _PI, _PI]),
+    "mwgpu_upload_tree": (C.c_int, [_P, C.POINTER(MwgpuMraDesc), C.POINTER(MwgpuTreeDesc), C.POINTER(_P)]),
+    "mwgpu_create_tree": (C.c_int, [_P, C.POINTER(MwgpuMraDesc), C.POINTER(MwgpuTreeDesc), C.POINTER(_P)]),
+    "mwgpu_tree_add_nodes": (C.c_int, [_P, _P, C.c_int, _PI, C.c_int, _PI, _PI]),
+    "mwgpu_tree_size": (C.c_int, [_P, _PI]),
+    "mwgpu_free_tree": (C.c_int, [_P, _P]),
+    "mwgpu_apply_level": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_double, C.c_double, _PD, C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_transform": (C.c_int, [_P, _P, C.c_int, C.c_int]),
+    "mwgpu_download_tree": (C.c_int, [_P, _P, _PD, _PD]),
+    "mwgpu_sync": (C.c_int, [_P]),
+    # host mirror (include/mwhost.h)
+    "mwh_last_error": (C.c_char_p, []),
+    "mwh_set_table_path": (C.c_int, [C.c_char_p]),
+    "mwh_mra_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _PI, _PI, C.c_double, C.c_int, C.POINTER(_P)]),
+    "mwh_mra_from_bounds": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_P)]),
+    "mwh_mra_free": (None, [_P]),
+    "mwh_mra_desc": (C.c_int, [_P, C.POINTER(MwgpuMraDesc), _PD]),
+    "mwh_tree_create": (C.c_int, [_P, C.POINTER(_P)]),
+    "mwh_tree_free": (None, [_P]),
+    "mwh_build_grid_gauss": (C.c_int, [_P, C.c_int, _PD, _PD, _PD]),
+    "mwh_project_gauss": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int]),
+    "mwh_copy_grid": (C.c_int, [_P, _P]),
+    "mwh_tree_info": (C.c_int, [_P, _PI, _PD]),
+    "mwh_tree_export": (C.c_int, [_P, _PI, _PI, _PD, _PD]),
+    "mwh_tree_import": (C.c_int, [_P, C.c_int, _PI, _PI, _PD, C.c_double]),
+    "mwh_dot": (C.c_double, [_P, _P]),
+    "mwh_evalf": (C.c_double, [_P, C.c_double, C.c_double, C.c_double]),
+    "mwh_integrate": (C.c_double, [_P]),
+    "mwh_poisson": (C.c_int, [_P, C.c_double, C.POINTER(_P)]),
+    "mwh_helmholtz": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(_P)]),
+    "mwh_oper_free": (None, [_P]),
+    "mwh_oper_info": (C.c_int, [_P, _PI, _PI, _PI]),
+    "mwh_oper_export": (C.c_int, [_P, _PI, _PI, _PD, _PD, _PD, _PD]),
+    "mwh_oper_desc": (C.c_int, [_P, C.POINTER(MwgpuOperDesc)]),
+    "mwh_poisson_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
+    "mwh_helmholtz_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
+    "mwh_apply": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded libmwgpu.so (raises MWGPUError if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MWGPUError(6, "libmwgpu.so not built (%s); run python -m mrcpp_gb300.build" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ck(code):
+    if code != 0:
+        raise MWGPUError(code, lib().mwh_last_error().decode())
+
+
+def _pi(a):
+    return a.ctypes.data_as(_PI)
+
+
+def _pd(a):
+    return a.ctypes.data_as(_PD)
+
+
+class MRA:
+    """MultiResolutionAnalysis<3>: world box + scaling basis (src/trees/MultiResolutionAnalysis.h)."""
+
+    def __init__(self, box=(-20, 20), order=5, basis=INTERPOLATING, max_depth=30, scale=None, corner=None, nbox=None, sf=None):
+        h = _P()
+        if scale is not None:
+            c = np.ascontiguousarray(corner, dtype=np.int32)
+            nb = np.ascontiguousarray(nbox, dtype=np.int32)
+            _ck(lib().mwh_mra_create(basis, order, scale, _pi(c), _pi(nb), float(sf if sf else 1.0), max_depth, C.byref(h)))
+        else:
+            _ck(lib().mwh_mra_from_bounds(basis, order, int(box[0]), int(box[1]), max_depth, C.byref(h)))
+        self._h = h
+        self.order = order
+        self.kp1 = order + 1
+        self.basis = basis
+        self._desc = MwgpuMraDesc()
+        self._filters = np.zeros(8 * self.kp1 * self.kp1)
+        _ck(lib().mwh_mra_desc(self._h, C.byref(self._desc), _pd(self._filters)))
+        self.root_scale = self._desc.root_scale
+        self.corner = tuple(self._desc.corner)
+        self.nbox = tuple(self._desc.nbox)
+        self.sf = self._desc.sf
+        self.max_scale = self._desc.max_scale
+
+    @property
+    def filters(self):
+        """8 (k+1)x(k+1) column-major filters: compression H0t,H1t,G0t,G1t, reconstruction H0,G0,H1,G1."""
+        K = self.kp1
+        return self._filters.reshape(8, K, K).transpose(0, 2, 1).copy()  # [f][row][col]
+
+    def desc(self):
+        return self._desc
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mwh_mra_free(self._h)
+            self._h = None
+
+
+class FunctionTree:
+    """FunctionTree<3>: adaptive tree of compressed s+d node coefficients."""
+
+    def __init__(self, mra):
+        self.mra = mra
+        h = _P()
+        _ck(lib().mwh_tree_create(mra._h, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mwh_tree_free(self._h)
+            self._h = None
+
+    @property
+    def n_nodes(self):
+        n = C.c_int()
+        _ck(lib().mwh_tree_info(self._h, C.byref(n), None))
+        return n.value
+
+    @property
+    def square_norm(self):
+        s = C.c_double()
+        _ck(lib().mwh_tree_info(self._h, None, C.byref(s)))
+        return s.value
+
+    def export(self):
+        """Flat breadth-first copy: idx [n,4], child0 [n], coefs [n, 8K^3], norms [n, 8]."""
+        n = self.n_nodes
+        K3 = self.mra.kp1 ** 3
+        idx = np.zeros((n, 4), dtype=np.int32)
+        c0 = np.zeros(n, dtype=np.int32)
+        coefs = np.zeros((n, 8 * K3))
+        norms = np.zeros((n, 8))
+        _ck(lib().mwh_tree_export(self._h, _pi(idx), _pi(c0), _pd(coefs), _pd(norms)))
+        return {"idx": idx, "child0": c0, "coefs": coefs, "norms": norms}
+
+    def load_flat(self, idx, child0, coefs, square_norm=-1.0):
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        c0 = np.ascontiguousarray(child0, dtype=np.int32)
+        coefs = np.ascontiguousarray(coefs, dtype=np.float64)
+        _ck(lib().mwh_tree_import(self._h, len(c0), _pi(idx), _pi(c0), _pd(coefs), float(square_norm)))
+
+    def evalf(self, r):
+        return lib().mwh_evalf(self._h, float(r[0]), float(r[1]), float(r[2]))
+
+    def integrate(self):
+        return lib().mwh_integrate(self._h)
+
+
+def _gauss_arrays(gaussians):
+    coef = np.ascontiguousarray([g[0] for g in gaussians], dtype=np.float64)
+    ex = np.ascontiguousarray([g[1] for g in gaussians], dtype=np.float64)
+    pos = np.ascontiguousarray([list(g[2]) for g in gaussians], dtype=np.float64).reshape(-1)
+    return coef, ex, pos
+
+
+def build_grid(tree, gaussians):
+    """build_grid(tree, GaussExp): gaussians = [(coef, exponent, (x,y,z)), ...]."""
+    coef, ex, pos = _gauss_arrays(gaussians)
+    _ck(lib().mwh_build_grid_gauss(tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos)))
+
+
+def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True):
+    """build_grid (optional) + project(prec, tree, GaussExp) (src/treebuilders/project.cpp:41-66)."""
+    if grid:
+        build_grid(tree, gaussians)
+    coef, ex, pos = _gauss_arrays(gaussians)
+    _ck(lib().mwh_project_gauss(float(prec), tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos), int(max_iter), int(bool(abs_prec))))
+
+
+def copy_grid(out, inp):
+    _ck(lib().mwh_copy_grid(out._h, inp._h))
+
+
+def dot(a, b):
+    return lib().mwh_dot(a._h, b._h)
+
+
+class ConvolutionOperator:
+    """Separated Gaussian convolution operator (src/operators/ConvolutionOperator.h)."""
+
+    def __init__(self, mra, handle):
+        self.mra = mra
+        self._h = handle
+        nt, nn, nr = C.c_int(), C.c_int(), C.c_int()
+        _ck(lib().mwh_oper_info(self._h, C.byref(nt), C.byref(nn), C.byref(nr)))
+        self.n_terms, self.n_nodes, self.n_rows = nt.value, nn.value, nr.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mwh_oper_free(self._h)
+            self._h = None
+
+    def size(self):
+        return self.n_terms
+
+    def export(self):
+        """Node caches: depth[T], max_transl[rows], blocks[nodes,4,K,K] (column-major blocks), norms[nodes,4], kernel."""
+        K = self.mra.kp1
+        depth = np.zeros(self.n_terms, dtype=np.int32)
+        mt = np.zeros(self.n_rows, dtype=np.int32)
+        blocks = np.zeros(self.n_nodes * 4 * K * K)
+        norms = np.zeros(self.n_nodes * 4)
+        kexp = np.zeros(self.n_terms)
+        kcoef = np.zeros(self.n_terms)
+        _ck(lib().mwh_oper_export(self._h, _pi(depth), _pi(mt), _pd(blocks), _pd(norms), _pd(kexp), _pd(kcoef)))
+        return {"depth": depth, "max_transl": mt, "blocks": blocks, "norms": norms, "kernel_exp": kexp, "kernel_coef": kcoef}
+
+    def desc(self):
+        d = MwgpuOperDesc()
+        _ck(lib().mwh_oper_desc(self._h, C.byref(d)))
+        return d
+
+
+class PoissonOperator(ConvolutionOperator):
+    """PoissonOperator(MRA, prec): 1/r as a sum of Gaussians (src/operators/PoissonOperator.cpp:40-55)."""
+
+    def __init__(self, mra, prec):
+        h = _P()
+        _ck(lib().mwh_poisson(mra._h, float(prec), C.byref(h)))
+        super().__init__(mra, h)
+        self.prec = prec
+
+
+class HelmholtzOperator(ConvolutionOperator):
+    """HelmholtzOperator(MRA, mu, prec): exp(-mu r)/r (src/operators/HelmholtzOperator.cpp:41-56)."""
+
+    def __init__(self, mra, mu, prec):
+        h = _P()
+        _ck(lib().mwh_helmholtz(mra._h, float(mu), float(prec), C.byref(h)))
+        super().__init__(mra, h)
+        self.prec = prec
+        self.mu = mu
+
+
+def _kernel(fn, *args):
+    n = fn(*args, 0, None, None)
+    if n < 0:
+        _ck(n)
+    ex = np.zeros(n)
+    co = np.zeros(n)
+    fn(*args, n, _pd(ex), _pd(co))
+    return ex, co
+
+
+def poisson_kernel(eps, r_min, r_max):
+    """PoissonKernel(eps, r_min, r_max): (exponents, coefficients)."""
+    return _kernel(lib().mwh_poisson_kernel, float(eps), float(r_min), float(r_max))
+
+
+def helmholtz_kernel(mu, eps, r_min, r_max):
+    """HelmholtzKernel(mu, eps, r_min, r_max): (exponents, coefficients)."""
+    return _kernel(lib().mwh_helmholtz_kernel, float(mu), float(eps), float(r_min), float(r_max))
+
+
+def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64):
+    """mrcpp::apply(prec, out, oper, inp, maxIter, absPrec) on the GPU; returns the apply statistics."""
+    st = MwhApplyStats()
+    _ck(lib().mwh_apply(float(prec), out._h, oper._h, inp._h, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
+    return st.as_dict()

@@ -1,0 +1,240 @@
+// Operator application kernels: band lookup pre-pass and the FP64 per-node
+// contraction.
+//
+// The contraction restates ConvolutionCalculator (src/treebuilders/
+// ConvolutionCalculator.cpp) for one output node g per CTA:
+//   band box          makeOperBand/fillOperBand            :142-222
+//   f/g components    calcNode loop over ft, gt            :252-265  (ft=gt=0 only at depth 0)
+//   term skip         applyOperComp maxDeltaL > bw.max     :277-288
+//   screening         applyOperator band + norm test       :297-329
+//   contraction       tensorApplyOperComp, 3 x g = f^T O   :333-382
+// Work per (f, term) is re-associated: for each f component ft the
+// direction-x and direction-y intermediates are shared between the g
+// components that need them; the arithmetic of each component product is
+// the same three 1D applications.
+#include "mwgpu_internal.cuh"
+
+namespace mwgpu {
+
+namespace {
+
+// out[c + K2*j] (+)= sum_i in[i + K*c] * F[i + K*j], products and sums in TC;
+// the result is converted to TO (accumulated in TO when ADD).
+template <bool ADD, typename TC, typename TI, typename TO>
+__device__ __forceinline__ void tapply(TO *out, const TI *in, const double *F, int K, int tid, int nthr) {
+    const int K2 = K * K, K3 = K2 * K;
+    for (int e = tid; e < K3; e += nthr) {
+        int c = e % K2, j = e / K2;
+        const TI *a = in + K * c;
+        const double *b = F + K * j;
+        TC s = (TC)0;
+        for (int i = 0; i < K; i++) s = fma((TC)a[i], (TC)__ldg(b + i), s);
+        if (ADD) out[c + K2 * j] += (TO)s;
+        else out[c + K2 * j] = (TO)s;
+    }
+}
+
+struct Box {
+    int s[3], e[3];
+    int total;
+};
+
+__device__ inline bool band_box(const DevMRA &m, const DevOper &op, int4 g, int &depth, Box &b) {
+    depth = g.x - m.root_scale;
+    int w = (depth >= 0 && depth < op.n_band_max) ? op.band_max[depth] : -1;
+    if (w < 0) return false;
+    int gl[3] = {g.y, g.z, g.w};
+    b.total = 1;
+    for (int d = 0; d < 3; d++) {
+        int nboxes = m.nbox[d] * (1 << depth);
+        int c = m.corner[d] * (1 << depth);
+        b.s[d] = max(gl[d] - w, c);
+        b.e[d] = min(gl[d] + w, c + nboxes - 1);
+        b.total *= (b.e[d] - b.s[d] + 1);
+    }
+    return b.total > 0;
+}
+
+__device__ inline void box_cell(const Box &b, int q, int &x, int &y, int &z) {
+    int nx = b.e[0] - b.s[0] + 1, ny = b.e[1] - b.s[1] + 1;
+    x = b.s[0] + q % nx;
+    y = b.s[1] + (q / nx) % ny;
+    z = b.s[2] + q / (nx * ny);
+}
+
+__global__ void k_band_missing(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work, uint64_t *pkeys,
+                               int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err) {
+    int gi = work[blockIdx.x];
+    int4 gx = g.idx[gi];
+    int depth;
+    Box b;
+    if (!band_box(m, op, gx, depth, b)) return;
+    for (int q = threadIdx.x; q < b.total; q += blockDim.x) {
+        int x, y, z;
+        box_cell(b, q, x, y, z);
+        uint64_t key;
+        if (!pack_key(m, gx.x, x, y, z, key)) { atomicOr(err, DE_RANGE); continue; }
+        if (hash_find(f.hkeys, f.hvals, f.hcap, key) >= 0) continue;
+        bool full = false;
+        if (hash_insert(pkeys, pvals, phcap, key, 0, &full)) {
+            int pos = atomicAdd(pcount, 1);
+            if (pos < pcap) plist[pos] = key;
+        }
+        if (full) atomicOr(err, DE_HASH_FULL);
+    }
+}
+
+// One CTA per output node.  Shared memory: g accumulator 8K^3, x-intermediates
+// 2K^3, xy-intermediates 4K^3.
+// TC is the type of the 1D products and of the x / xy intermediates: double
+// for the plain form, float for the mixed form.  The g accumulator is FP64 in
+// both forms (the compensation that keeps the mixed form at FP32 product
+// accuracy instead of FP32 summation accuracy).
+template <typename TC>
+__global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work,
+                                                  double gthr, LevelStats *stats, int *err) {
+    extern __shared__ double sm[];
+    const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    double *gacc = sm;
+    TC *X0 = (TC *)(gacc + 8 * K3);
+    TC *X1 = X0 + 2 * K3;
+    __shared__ int s_fid;
+    __shared__ double s_fn[8];
+    __shared__ unsigned s_mask[2];
+    __shared__ unsigned long long s_nt, s_nc;
+    const int gi = work[blockIdx.x];
+    const int4 gx = g.idx[gi];
+    for (int e = tid; e < 8 * K3; e += nthr) gacc[e] = 0.0;
+    if (tid == 0) { s_nt = 0; s_nc = 0; }
+    __syncthreads();
+    int depth;
+    Box b;
+    unsigned long long nband = 0;
+    if (band_box(m, op, gx, depth, b)) {
+        const int T = op.n_terms;
+        for (int q = 0; q < b.total; q++) {
+            int fx, fy, fz;
+            box_cell(b, q, fx, fy, fz);
+            if (tid == 0) {
+                uint64_t key;
+                int id = -1;
+                if (pack_key(m, gx.x, fx, fy, fz, key)) id = hash_find(f.hkeys, f.hvals, f.hcap, key);
+                if (id < 0) atomicOr(err, DE_LOOKUP);
+                s_fid = id;
+                if (id >= 0)
+                    for (int c = 0; c < 8; c++) s_fn[c] = f.norms[(size_t)id * 8 + c];
+            }
+            __syncthreads();
+            const int fid = s_fid;
+            if (fid < 0) { __syncthreads(); continue; }
+            nband++;
+            const int tl[3] = {fx - gx.y, fy - gx.z, fz - gx.w};
+            const int maxdl = max(abs(tl[0]), max(abs(tl[1]), abs(tl[2])));
+            const bool gen = fid >= f.cap_real;
+            const double *fc = gen ? f.gcoefs + (size_t)(fid - f.cap_real) * K3 : f.coefs + (size_t)fid * 8 * K3;
+            for (int ti = 0; ti < T; ti++) {
+                const int i = op.term_order[depth * T + ti];
+                const int *bwi = op.bw + ((size_t)i * op.max_rows + depth) * 5;
+                if (maxdl > bwi[4]) break;  // terms sorted by descending max width at this depth
+                if (tid < 64) {
+                    const int ft = tid >> 3, gt = tid & 7;
+                    bool pass = true;
+                    const double fNorm = s_fn[ft];
+                    if (fNorm < kMachineZero) pass = false;
+                    if (depth != 0 && ft == 0 && gt == 0) pass = false;
+                    double oNorm = 1.0;
+                    if (pass) {
+                        for (int d = 0; d < 3; d++) {
+                            const int a = (gt >> d) & 1, bb = (ft >> d) & 1, idx = 2 * a + bb;
+                            if (abs(tl[d]) > bwi[idx]) { pass = false; break; }
+                            const int node = op.dep_off[i * op.max_rows + depth] + tl[d] + op.dep_L[i * op.max_rows + depth];
+                            oNorm *= op.norms[(size_t)node * 4 + idx];
+                        }
+                    }
+                    if (pass) {
+                        const double fThr = (double)op.band_size[((size_t)i * kMaxDepthRows + depth) * 64 + gt * 8 + ft] * fNorm;
+                        const double upper = oNorm * fThr;
+                        pass = upper > gthr;
+                    }
+                    unsigned bal = __ballot_sync(0xffffffffu, pass);
+                    if ((tid & 31) == 0) s_mask[tid >> 5] = bal;
+                }
+                __syncthreads();
+                const unsigned long long mask = (unsigned long long)s_mask[0] | ((unsigned long long)s_mask[1] << 32);
+                if (mask == 0ull) { __syncthreads(); continue; }
+                if (tid == 0) { s_nt++; s_nc += __popcll(mask); }
+                const int L0 = op.dep_L[i * op.max_rows + depth];
+                const int off = op.dep_off[i * op.max_rows + depth];
+                const double *ob[3];
+                for (int d = 0; d < 3; d++) ob[d] = op.blocks + (size_t)(off + tl[d] + L0) * 4 * K2;
+                for (int ft = 0; ft < 8; ft++) {
+                    const unsigned gm = (unsigned)((mask >> (8 * ft)) & 0xffull);
+                    if (gm == 0) continue;
+                    const double *fin = fc + (size_t)ft * K3;
+                    const int b0 = ft & 1, b1 = (ft >> 1) & 1, b2 = (ft >> 2) & 1;
+                    unsigned need0 = 0, need1 = 0;
+                    for (int gt = 0; gt < 8; gt++)
+                        if (gm & (1u << gt)) { need0 |= 1u << (gt & 1); need1 |= 1u << (gt & 3); }
+                    for (int a0 = 0; a0 < 2; a0++)
+                        if (need0 & (1u << a0)) tapply<false, TC>(X0 + a0 * K3, fin, ob[0] + (2 * a0 + b0) * K2, K, tid, nthr);
+                    __syncthreads();
+                    for (int s = 0; s < 4; s++)
+                        if (need1 & (1u << s)) tapply<false, TC>(X1 + s * K3, X0 + (s & 1) * K3, ob[1] + (2 * (s >> 1) + b1) * K2, K, tid, nthr);
+                    __syncthreads();
+                    for (int gt = 0; gt < 8; gt++)
+                        if (gm & (1u << gt)) tapply<true, TC>(gacc + gt * K3, X1 + (gt & 3) * K3, ob[2] + (2 * (gt >> 2) + b2) * K2, K, tid, nthr);
+                    __syncthreads();
+                }
+            }
+            __syncthreads();  // s_fid / s_fn are rewritten for the next band cell
+        }
+    }
+    __syncthreads();
+    double *go = g.coefs + (size_t)gi * 8 * K3;
+    for (int e = tid; e < 8 * K3; e += nthr) go[e] = gacc[e];
+    // node norms (MWNode::calcNorms)
+    __shared__ double red[8][8];
+    for (int comp = 0; comp < 8; comp++) {
+        double s = 0.0;
+        for (int e = tid; e < K3; e += nthr) { double v = gacc[comp * K3 + e]; s += v * v; }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) red[comp][tid >> 5] = s;
+    }
+    __syncthreads();
+    if (tid < 8) {
+        double t = 0.0;
+        for (int w = 0; w < nthr / 32; w++) t += red[tid][w];
+        g.norms[(size_t)gi * 8 + tid] = sqrt(t);
+    }
+    if (tid == 0) {
+        atomicAdd(&stats->node_terms, s_nt);
+        atomicAdd(&stats->components, s_nc);
+        atomicAdd(&stats->band_nodes, nband);
+    }
+}
+
+}  // namespace
+
+void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
+                         uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s) {
+    if (n_work <= 0) return;
+    k_band_missing<<<n_work, 256, 0, s>>>(m, op, f, g, work, n_work, pkeys, pvals, phcap, plist, pcount, pcap, err);
+}
+
+void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
+                          double gthr, LevelStats *stats, int *err, cudaStream_t s) {
+    if (n_work <= 0) return;
+    size_t smem = sizeof(double) * 14 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err);
+}
+
+void launch_contract_mixed(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
+                           double gthr, LevelStats *stats, int *err, cudaStream_t s) {
+    if (n_work <= 0) return;
+    size_t smem = sizeof(double) * 8 * m.kp1_d + sizeof(float) * 6 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_contract<float><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err);
+}
+
+}  // namespace mwgpu

@@ -1,0 +1,300 @@
+// Tree kernels: node lookup table, GenNode generation, node norms and the
+// whole-tree multiwavelet transforms.
+//
+// Reference behaviour restated here:
+//   GenNodes        MWTree::getNode -> MWNode::retrieveNode -> threadSafeGenChildren
+//                   -> tree_utils::mw_transform(readOnlyScaling)  (src/trees/MWTree.cpp:340-352,
+//                   src/trees/MWNode.cpp:410-418, 1097-1120, src/utils/tree_utils.cpp:113-216)
+//   node norms      MWNode::calcNorms / calcComponentNorm (src/trees/MWNode.cpp:609-655)
+//   TopDown (add)   MWTree::mwTransformDown -> MWNode::giveChildrenCoefs(false) (MWTree.cpp:194-216)
+//   BottomUp        MWTree::mwTransformUp -> FunctionNode<3>::reCompress -> mw_transform_back
+//                   (MWTree.cpp:166-181, FunctionNode.cpp:391-409, tree_utils.cpp:229-301)
+// The 1D step everywhere is math_utils::apply_filter: out(K^2 x K) = in^T (K^2 x K) * F.
+#include "mwgpu_internal.cuh"
+
+namespace mwgpu {
+
+namespace {
+
+// out[c + K2*j] (+)= sum_i in[i + K*c] * F[i + K*j]
+template <bool ADD>
+__device__ __forceinline__ void dapply(double *out, const double *in, const double *F, int K, int tid, int nthr) {
+    const int K2 = K * K, K3 = K2 * K;
+    for (int e = tid; e < K3; e += nthr) {
+        int c = e % K2, j = e / K2;
+        const double *a = in + K * c;
+        const double *b = F + K * j;
+        double s = 0.0;
+        for (int i = 0; i < K; i++) s = fma(a[i], b[i], s);
+        if (ADD) out[c + K2 * j] += s;
+        else out[c + K2 * j] = s;
+    }
+}
+
+__device__ inline void unpack_key(const DevMRA &m, uint64_t key, int &n, int &l0, int &l1, int &l2) {
+    int d = (int)(key & 31);
+    n = m.root_scale + d;
+    int l[3];
+    for (int i = 0; i < 3; i++) l[i] = (int)((key >> (5 + 19 * i)) & ((1u << 19) - 1)) + m.corner[i] * (1 << d);
+    l0 = l[0];
+    l1 = l[1];
+    l2 = l[2];
+}
+
+__device__ inline const double *filt(const DevMRA &m, int op, int fidx) { return m.filt + ((size_t)op * 4 + fidx) * m.K * m.K; }
+
+__global__ void k_hash_build(DevMRA m, DevTree t, int first, int count, int *err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    int id = first + i;
+    int4 x = t.idx[id];
+    uint64_t key;
+    if (!pack_key(m, x.x, x.y, x.z, x.w, key)) { atomicOr(err, DE_RANGE); return; }
+    bool full = false;
+    hash_insert(t.hkeys, t.hvals, t.hcap, key, id, &full);
+    if (full) atomicOr(err, DE_HASH_FULL);
+}
+
+// One CTA per pending GenNode: walk up to the nearest node present in the
+// lookup table, then reconstruct down along the path to the requested child.
+__global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err) {
+    extern __shared__ double sm[];
+    const int K = m.K, K3 = m.kp1_d;
+    double *b0 = sm;           // 4 K^3
+    double *b1 = sm + 4 * K3;  // 4 K^3
+    __shared__ int s_anc, s_ancn;
+    int p = blockIdx.x;
+    if (p >= n_pend) return;
+    int n, l0, l1, l2;
+    unpack_key(m, plist[p], n, l0, l1, l2);
+    if (threadIdx.x == 0) {
+        s_anc = -1;
+        s_ancn = 0;
+        for (int a = n - 1; a >= m.root_scale; a--) {
+            int sh = n - a;
+            uint64_t key;
+            if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
+            int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
+            if (id >= 0) { s_anc = id; s_ancn = a; break; }
+        }
+    }
+    __syncthreads();
+    int anc = s_anc, an = s_ancn;
+    if (anc < 0) {
+        if (threadIdx.x == 0) atomicOr(err, DE_LOOKUP);
+        return;
+    }
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const double *src;
+    bool real = anc < f.cap_real;
+    // first step
+    {
+        int sh = n - an - 1;
+        int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
+        if (real) {
+            const double *in = f.coefs + (size_t)anc * 8 * K3;
+            // stage 0: tmp[(c0,b1,b2)] for the 4 (b1,b2), slot q = b1 + 2*b2
+            for (int q = 0; q < 4; q++) {
+                int ftlo = 2 * q;  // b0 = 0, bits b1,b2 from q
+                dapply<false>(b0 + q * K3, in + (size_t)ftlo * K3, filt(m, 1, 2 * c0 + 0), K, tid, nthr);
+            }
+            __syncthreads();
+            for (int q = 0; q < 4; q++) dapply<true>(b0 + q * K3, in + (size_t)(2 * q + 1) * K3, filt(m, 1, 2 * c0 + 1), K, tid, nthr);
+            __syncthreads();
+            // stage 1: tmp2[(c0,c1,b2)], slot b2
+            for (int b2 = 0; b2 < 2; b2++) dapply<false>(b1 + b2 * K3, b0 + (0 + 2 * b2) * K3, filt(m, 1, 2 * c1 + 0), K, tid, nthr);
+            __syncthreads();
+            for (int b2 = 0; b2 < 2; b2++) dapply<true>(b1 + b2 * K3, b0 + (1 + 2 * b2) * K3, filt(m, 1, 2 * c1 + 1), K, tid, nthr);
+            __syncthreads();
+            // stage 2
+            dapply<false>(b0, b1, filt(m, 1, 2 * c2 + 0), K, tid, nthr);
+            __syncthreads();
+            dapply<true>(b0, b1 + K3, filt(m, 1, 2 * c2 + 1), K, tid, nthr);
+            __syncthreads();
+        } else {
+            const double *in = f.gcoefs + (size_t)(anc - f.cap_real) * K3;
+            dapply<false>(b1, in, filt(m, 1, 2 * c0), K, tid, nthr);
+            __syncthreads();
+            dapply<false>(b1 + K3, b1, filt(m, 1, 2 * c1), K, tid, nthr);
+            __syncthreads();
+            dapply<false>(b0, b1 + K3, filt(m, 1, 2 * c2), K, tid, nthr);
+            __syncthreads();
+        }
+        src = b0;
+    }
+    // remaining steps from scaling-only parents
+    for (int a = an + 1; a < n; a++) {
+        int sh = n - a - 1;
+        int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
+        dapply<false>(b1, src, filt(m, 1, 2 * c0), K, tid, nthr);
+        __syncthreads();
+        dapply<false>(b1 + K3, b1, filt(m, 1, 2 * c1), K, tid, nthr);
+        __syncthreads();
+        dapply<false>(b0, b1 + K3, filt(m, 1, 2 * c2), K, tid, nthr);
+        __syncthreads();
+        src = b0;
+    }
+    int slot = gen_base + p;
+    if (slot >= f.cap_gen) {
+        if (tid == 0) atomicOr(err, DE_POOL_FULL);
+        return;
+    }
+    double *out = f.gcoefs + (size_t)slot * K3;
+    for (int e = tid; e < K3; e += nthr) out[e] = src[e];
+    // scaling norm (GenNode wavelet norms are zero)
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int e = tid; e < K3; e += nthr) s += src[e] * src[e];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((tid & 31) == 0) red[tid >> 5] = s;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) t += red[w];
+        double *nr = f.norms + (size_t)(f.cap_real + slot) * 8;
+        nr[0] = sqrt(t);
+        for (int c = 1; c < 8; c++) nr[c] = 0.0;
+        f.idx[f.cap_real + slot] = make_int4(n, l0, l1, l2);
+    }
+}
+
+__global__ void k_gen_insert(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_pend) return;
+    bool full = false;
+    hash_insert(f.hkeys, f.hvals, f.hcap, plist[p], f.cap_real + gen_base + p, &full);
+    if (full) atomicOr(err, DE_HASH_FULL);
+}
+
+__device__ void block_norms(const double *c, int K3, double *nr, int tid, int nthr) {
+    __shared__ double red[8][32];
+    for (int comp = 0; comp < 8; comp++) {
+        double s = 0.0;
+        for (int e = tid; e < K3; e += nthr) { double v = c[comp * K3 + e]; s += v * v; }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((tid & 31) == 0) red[comp][tid >> 5] = s;
+    }
+    __syncthreads();
+    if (tid < 8) {
+        double t = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) t += red[tid][w];
+        nr[tid] = sqrt(t);
+    }
+    __syncthreads();
+}
+
+__global__ void k_node_norms(DevMRA m, DevTree t, const int *nodes, int n) {
+    int i = nodes[blockIdx.x];
+    block_norms(t.coefs + (size_t)i * 8 * m.kp1_d, m.kp1_d, t.norms + (size_t)i * 8, threadIdx.x, blockDim.x);
+}
+
+// TopDown: parent (s,d) -> children scaling, added (overwrite=false) or assigned.
+__global__ void k_mw_down(DevMRA m, DevTree t, const int *parents, int n, bool overwrite) {
+    extern __shared__ double sm[];
+    const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    double *t1 = sm, *t2 = sm + 8 * K3;
+    int p = parents[blockIdx.x];
+    int c0 = t.child0[p];
+    if (c0 < 0) return;
+    const double *in = t.coefs + (size_t)p * 8 * K3;
+    // stage 0 (direction x)
+    for (int gt = 0; gt < 8; gt++) {
+        dapply<false>(t1 + gt * K3, in + (size_t)(gt & ~1) * K3, filt(m, 1, 2 * (gt & 1) + 0), K, tid, nthr);
+    }
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) dapply<true>(t1 + gt * K3, in + (size_t)(gt | 1) * K3, filt(m, 1, 2 * (gt & 1) + 1), K, tid, nthr);
+    __syncthreads();
+    // stage 1 (direction y)
+    for (int gt = 0; gt < 8; gt++) dapply<false>(t2 + gt * K3, t1 + (gt & ~2) * K3, filt(m, 1, 2 * ((gt >> 1) & 1) + 0), K, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) dapply<true>(t2 + gt * K3, t1 + (gt | 2) * K3, filt(m, 1, 2 * ((gt >> 1) & 1) + 1), K, tid, nthr);
+    __syncthreads();
+    // stage 2 (direction z) straight into the children scaling blocks
+    for (int gt = 0; gt < 8; gt++) {
+        double *o = t.coefs + (size_t)(c0 + gt) * 8 * K3;
+        if (overwrite) {
+            for (int e = tid; e < 8 * K3; e += nthr) o[e] = 0.0;
+            __syncthreads();
+            dapply<false>(o, t2 + (gt & ~4) * K3, filt(m, 1, 2 * ((gt >> 2) & 1) + 0), K, tid, nthr);
+        } else {
+            dapply<true>(o, t2 + (gt & ~4) * K3, filt(m, 1, 2 * ((gt >> 2) & 1) + 0), K, tid, nthr);
+        }
+    }
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) {
+        double *o = t.coefs + (size_t)(c0 + gt) * 8 * K3;
+        dapply<true>(o, t2 + (gt | 4) * K3, filt(m, 1, 2 * ((gt >> 2) & 1) + 1), K, tid, nthr);
+    }
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) block_norms(t.coefs + (size_t)(c0 + gt) * 8 * K3, K3, t.norms + (size_t)(c0 + gt) * 8, tid, nthr);
+}
+
+// BottomUp: 8 children scaling blocks -> parent (s,d), then parent norms.
+__global__ void k_mw_up(DevMRA m, DevTree t, const int *parents, int n) {
+    extern __shared__ double sm[];
+    const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    double *t1 = sm, *t2 = sm + 8 * K3;
+    int p = parents[blockIdx.x];
+    int c0 = t.child0[p];
+    if (c0 < 0) return;
+    for (int ct = 0; ct < 8; ct++) {
+        const double *cs = t.coefs + (size_t)(c0 + ct) * 8 * K3;
+        for (int e = tid; e < K3; e += nthr) t1[ct * K3 + e] = cs[e];
+    }
+    __syncthreads();
+    double *bufs[2] = {t1, t2};
+    for (int d = 0; d < 3; d++) {
+        double *in = bufs[d & 1], *out = bufs[(d + 1) & 1];
+        int mask = 1 << d;
+        for (int gt = 0; gt < 8; gt++)
+            dapply<false>(out + gt * K3, in + (gt & ~mask) * K3, filt(m, 0, 2 * ((gt >> d) & 1) + 0), K, tid, nthr);
+        __syncthreads();
+        for (int gt = 0; gt < 8; gt++)
+            dapply<true>(out + gt * K3, in + (gt | mask) * K3, filt(m, 0, 2 * ((gt >> d) & 1) + 1), K, tid, nthr);
+        __syncthreads();
+    }
+    double *pc = t.coefs + (size_t)p * 8 * K3;
+    for (int e = tid; e < 8 * K3; e += nthr) pc[e] = t2[e];
+    __syncthreads();
+    block_norms(pc, K3, t.norms + (size_t)p * 8, tid, nthr);
+}
+
+}  // namespace
+
+void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *err, cudaStream_t s) {
+    if (count <= 0) return;
+    k_hash_build<<<(count + 255) / 256, 256, 0, s>>>(m, t, first, count, err);
+}
+
+void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {
+    if (n_pend <= 0) return;
+    size_t smem = sizeof(double) * 8 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_nodes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err);
+}
+
+void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {
+    if (n_pend <= 0) return;
+    k_gen_insert<<<(n_pend + 255) / 256, 256, 0, s>>>(m, f, plist, n_pend, gen_base, err);
+}
+
+void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_node_norms<<<n, 128, 0, s>>>(m, t, nodes, n);
+}
+
+void launch_mw_down(const DevMRA &m, DevTree t, const int *parents, int n, bool overwrite, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = sizeof(double) * 16 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mw_down<<<n, 256, smem, s>>>(m, t, parents, n, overwrite);
+}
+
+void launch_mw_up(const DevMRA &m, DevTree t, const int *parents, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = sizeof(double) * 16 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_up, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mw_up<<<n, 256, smem, s>>>(m, t, parents, n);
+}
+
+}  // namespace mwgpu

@@ -1,0 +1,126 @@
+// Internal device-side structures of the mwgpu library (not part of the C-ABI).
+//
+// HBM layout
+//   operator tables: one array of operator nodes for all terms; node = 4 K*K
+//     blocks (T,C,B,A; column-major K x K) + 4 component norms; per
+//     (term, depth) the offset of translation l = -L and L.
+//   trees: node index (scale, l0, l1, l2) as int4, 8 K^3 doubles per real
+//     node (compressed s+d form, component c at c*K^3, x fastest), 8 norms per
+//     node; GenNodes (scaling-only nodes made by reconstruction) live in a
+//     separate pool of K^3 doubles per node, ids >= capacity_real.
+//   lookup: open-addressing hash keyed by (depth, translation offsets).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mwgpu {
+
+constexpr int kMaxDepthRows = 30;   // ConvolutionCalculator band-size rows (MaxDepth)
+constexpr double kMachineZero = 1.0e-14;
+constexpr uint64_t kEmptyKey = ~0ull;
+
+struct DevMRA {
+    int K, kp1_d, root_scale, max_scale;
+    int corner[3], nbox[3];
+    double sf;
+    const double *filt;  // [2 ops][4 filters][K*K] column-major; op 0 = compression, 1 = reconstruction
+};
+
+struct DevOper {
+    int n_terms, K;
+    int max_rows;               // rows of per-term tables (= kMaxDepthRows + 1)
+    const int *term_depth;      // [T]
+    const int *dep_off;         // [T * max_rows] node offset of l = -L, -1 beyond term depth
+    const int *dep_L;           // [T * max_rows]
+    const double *blocks;       // [nodes * 4 * K * K]
+    const double *norms;        // [nodes * 4]
+    const int *bw;              // [T * max_rows * 5] band widths at the apply precision (-1 beyond)
+    const int *band_size;       // [T * kMaxDepthRows * 64] ConvolutionCalculator band-size factors
+    const int *band_max;        // [max_rows]
+    const int *term_order;      // [max_rows * T] terms sorted by descending bw max at depth
+    int n_band_max;
+};
+
+struct DevTree {
+    int n_real, cap_real;        // real nodes
+    int n_gen, cap_gen;          // generated scaling-only nodes
+    int4 *idx;                   // [cap_real + cap_gen] (scale, l0, l1, l2)
+    double *coefs;               // [cap_real * 8 K^3]
+    double *gcoefs;              // [cap_gen * K^3]
+    double *norms;               // [(cap_real + cap_gen) * 8]
+    int *child0;                 // [cap_real] first child id or -1
+    uint64_t *hkeys;             // [hcap]
+    int *hvals;                  // [hcap]
+    int hcap;                    // power of two
+};
+
+__host__ __device__ inline bool pack_key(const DevMRA &m, int n, int l0, int l1, int l2, uint64_t &key) {
+    int d = n - m.root_scale;
+    if (d < 0 || d > 30) return false;
+    int l[3] = {l0, l1, l2};
+    uint64_t k = (uint64_t)d;
+    for (int i = 0; i < 3; i++) {
+        long long t = (long long)l[i] - (long long)m.corner[i] * (1ll << d);
+        if (t < 0 || t >= (long long)m.nbox[i] * (1ll << d) || t >= (1ll << 19)) return false;
+        k |= (uint64_t)t << (5 + 19 * i);
+    }
+    key = k;
+    return true;
+}
+
+__host__ __device__ inline uint32_t hash_slot(uint64_t key, int hcap) {
+    uint64_t h = key * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 29;
+    return (uint32_t)(h & (uint64_t)(hcap - 1));
+}
+
+__device__ inline int hash_find(const uint64_t *keys, const int *vals, int hcap, uint64_t key) {
+    uint32_t s = hash_slot(key, hcap);
+    for (int probe = 0; probe < hcap; probe++) {
+        uint64_t k = keys[s];
+        if (k == key) return vals[s];
+        if (k == kEmptyKey) return -1;
+        s = (s + 1) & (hcap - 1);
+    }
+    return -1;
+}
+
+// Inserts key; returns true if this call inserted it. Bounded probing.
+__device__ inline bool hash_insert(uint64_t *keys, int *vals, int hcap, uint64_t key, int val, bool *full) {
+    uint32_t s = hash_slot(key, hcap);
+    for (int probe = 0; probe < hcap; probe++) {
+        unsigned long long prev = atomicCAS((unsigned long long *)&keys[s], (unsigned long long)kEmptyKey, (unsigned long long)key);
+        if (prev == kEmptyKey) { vals[s] = val; return true; }
+        if (prev == key) return false;
+        s = (s + 1) & (hcap - 1);
+    }
+    *full = true;
+    return false;
+}
+
+// error flags written by kernels (host reads them after each phase)
+enum DevError { DE_LOOKUP = 1, DE_HASH_FULL = 2, DE_POOL_FULL = 4, DE_RANGE = 8 };
+
+struct LevelStats {
+    unsigned long long node_terms;   // (g, f, term) triples with >= 1 contracted component
+    unsigned long long components;   // contracted (g, f, term, ft, gt) components
+    unsigned long long band_nodes;   // (g, f) pairs visited
+    unsigned long long gen_nodes;    // GenNodes created
+};
+
+// kernel launchers (k_apply.cu / k_tree.cu)
+void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
+                         uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s);
+void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
+void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
+void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
+                          double gthr, LevelStats *stats, int *err, cudaStream_t s);
+void launch_contract_mixed(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
+                           double gthr, LevelStats *stats, int *err, cudaStream_t s);
+void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cudaStream_t s);
+void launch_mw_down(const DevMRA &m, DevTree t, const int *parents, int n, bool overwrite, cudaStream_t s);
+void launch_mw_up(const DevMRA &m, DevTree t, const int *parents, int n, cudaStream_t s);
+void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *err, cudaStream_t s);
+
+}  // namespace mwgpu

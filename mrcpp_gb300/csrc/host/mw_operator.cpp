@@ -1,0 +1,273 @@
+// Construction of the separated convolution operators (host, one-time).
+//
+// Follows src/operators/PoissonKernel.cpp:48-86, HelmholtzKernel.cpp:47-80,
+// PoissonOperator.cpp:40-55, HelmholtzOperator.cpp:41-56,
+// ConvolutionOperator.cpp:51-142, MWOperator.cpp:35-129,
+// src/treebuilders/CrossCorrelationCalculator.cpp:36-96, OperatorAdaptor.h:32-49,
+// src/trees/OperatorNode.cpp:56-80 (component norms),
+// src/trees/OperatorTree.cpp:109-134 (band width), :200-238 (node cache).
+#include "mw_host.h"
+
+namespace mwh {
+
+namespace {
+constexpr double root_pi = 1.7724538509055160273;  // api/constants.h
+}  // namespace
+
+std::vector<GaussFunc<1>> poisson_kernel(double epsilon, double r_min, double r_max) {
+    std::vector<GaussFunc<1>> out;
+    double r0 = r_min / r_max;
+    double r1 = r_max;
+    double t1 = 1.0L;
+    while ((2.0 * t1 * std::exp(-t1)) > epsilon) t1 *= 1.1L;
+    double t2 = 1.0L;
+    while ((std::sqrt(t2) * std::exp(-t2) / r0) > epsilon) t2 *= 1.1L;
+    double s1 = -std::log(2.0 * t1);
+    double s2 = std::log(t2 / (r0 * r0)) / 2.0;
+    double h = 1.0 / (0.2L - 0.47L * std::log10(epsilon));
+    int n_exp = static_cast<int>(std::ceil((s2 - s1) / h) + 1);
+    if (n_exp > MaxSepRank) throw Error(1, "Maximum separation rank exceeded.");
+    for (int i = 0; i < n_exp; i++) {
+        double arg = s1 + h * i;
+        double sinharg = std::sinh(arg);
+        double cosharg = std::cosh(arg);
+        double onepexp = 1.0 + std::exp(-sinharg);
+        double expo = 4.0L * (sinharg + std::log(onepexp)) * (sinharg + std::log(onepexp));
+        double coef = h * (4.0L / root_pi) * cosharg / onepexp;
+        expo *= 1.0 / (r1 * r1);
+        coef *= 1.0 / r1;
+        if (i == 0 || i == (n_exp - 1)) coef *= 1.0 / 2.0;
+        out.push_back(GaussFunc<1>(expo, coef));
+    }
+    return out;
+}
+
+std::vector<GaussFunc<1>> helmholtz_kernel(double mu, double epsilon, double r_min, double r_max) {
+    std::vector<GaussFunc<1>> out;
+    double r0 = r_min / r_max;
+    double r1 = r_max;
+    double mu_tilde = mu * r1;
+    double t = std::max((-2.5L * std::log(epsilon)), 5.0L);
+    double s1 = -std::log(4 * t / (mu_tilde * mu_tilde)) / 2;
+    double s2 = std::log(t / (r0 * r0)) / 2;
+    double h = 1.0 / (0.20L - 0.47L * std::log10(epsilon));
+    int n_exp = static_cast<int>(std::ceil((s2 - s1) / h) + 1);
+    if (n_exp > MaxSepRank) throw Error(1, "Maximum separation rank exceeded.");
+    for (int i = 0; i < n_exp; i++) {
+        double arg = s1 + h * i;
+        double temp = -arg * 2.0;
+        double temp2 = -mu_tilde * mu_tilde * std::exp(temp) / 4.0 + arg;
+        double beta = (h * (2.0 / root_pi) * std::exp(temp2));
+        double temp3 = 2.0L * arg;
+        double alpha = std::exp(temp3);
+        alpha *= 1.0 / (r1 * r1);
+        beta *= 1.0 / r1;
+        if (i == 0 || i == (n_exp - 1)) beta *= 1.0 / 2.0;
+        out.push_back(GaussFunc<1>(alpha, beta));
+    }
+    return out;
+}
+
+// OperatorNode::calcComponentNorm
+static double oper_component_norm(const Tree<2> &t, int node, int comp, double normPrec) {
+    int depth = t.depth(node);
+    double thrs = std::max(MachinePrec, normPrec / (8.0 * (1 << depth)));
+    const int K = t.K;
+    const double *m = t.c(node) + (size_t)comp * K * K;
+    double sq = 0.0;
+    for (int j = 0; j < K * K; j++) sq += m[j] * m[j];
+    double vecNorm = std::sqrt(sq);
+    double norm = 0.0;
+    if (vecNorm > thrs) {
+        double infNorm = 0.0, oneNorm = 0.0;
+        for (int r = 0; r < K; r++) {
+            double s = 0.0;
+            for (int c = 0; c < K; c++) s += std::fabs(m[r + K * c]);
+            infNorm = std::max(infNorm, s);
+        }
+        for (int c = 0; c < K; c++) {
+            double s = 0.0;
+            for (int r = 0; r < K; r++) s += std::fabs(m[r + K * c]);
+            oneNorm = std::max(oneNorm, s);
+        }
+        if (std::sqrt(infNorm * oneNorm) > thrs) {
+            double twoNorm = vecNorm;
+            if (twoNorm > thrs) norm = twoNorm;
+        }
+    }
+    return norm;
+}
+
+void build_operator_terms(ConvolutionOperator &op, double k_prec, double o_prec) {
+    const MRA<3> &mra = op.mra;
+    const auto &box = mra.world;
+    const int type = mra.basis->type;
+    const int k = mra.order();
+    int reach = op.operReach + 1;
+    if (reach < 0)
+        for (int d = 0; d < 3; d++)
+            if (box.size(d) > reach) reach = box.size(d);
+    double sf = box.sf[0];
+    // kernel MRA (ConvolutionOperator::getKernelMRA) and operator MRA (MWOperator::getOperatorMRA)
+    MRA<1> kmra(BoundingBox<1>(op.operRoot, {-reach}, {2 * reach}, {sf}), type, 2 * k + 1);
+    MRA<2> omra(BoundingBox<2>(op.operRoot, {0, 0}, {reach, reach}, {sf, sf}), type, k);
+    const int K = k + 1, Kp = 2 * K;
+    Mat Lm = table(2, type, k), Rm = table(3, type, k);
+    for (auto *M : {&Lm, &Rm})
+        for (auto &x : M->a)
+            if (std::fabs(x) < MachinePrec) x = 0.0;
+
+    op.terms.clear();
+    for (const auto &g : op.kernel) {
+        GaussFunc<1> kf = g;
+        kf.coef = std::copysign(std::pow(std::fabs(g.coef), 1.0 / 3.0), g.coef);
+        Tree<1> ktree(kmra);
+        build_grid(ktree, kf);
+        project<1>(k_prec, ktree, [&kf](const double *r) { return kf.evalf(r); });
+
+        Tree<2> otree(omra);
+        otree.componentNorm = [o_prec](const Tree<2> &t, int i, int c) { return oper_component_norm(t, i, c, o_prec); };
+        auto calc = [&](Tree<2> &t, const std::vector<int> &work) {
+            for (int node : work) {
+                double *coefs = t.c(node);
+                std::fill(coefs, coefs + t.nCoefs, 0.0);
+                int scale = t.nodes[node].n + 1;
+                for (int i = 0; i < 4; i++) {
+                    int l0 = 2 * t.nodes[node].l[0] + (i & 1);
+                    int l1 = 2 * t.nodes[node].l[1] + ((i >> 1) & 1);
+                    int la[1] = {l1 - l0 - 1}, lb[1] = {l1 - l0};
+                    int na = ktree.getNode(scale, la, true);
+                    int nb = ktree.getNode(scale, lb, true);
+                    const double *sa = ktree.c(na), *sb = ktree.c(nb);
+                    for (int r = 0; r < K * K; r++) {
+                        double va = 0.0, vb = 0.0;
+                        for (int p = 0; p < Kp; p++) va += Lm(r, p) * sa[p];
+                        for (int p = 0; p < Kp; p++) vb += Rm(r, p) * sb[p];
+                        coefs[i * K * K + r] = va + vb;
+                    }
+                }
+                double two_n = std::pow(2.0, -scale / 2.0);
+                for (int j = 0; j < t.nCoefs; j++) coefs[j] = std::sqrt(sf) * two_n * coefs[j];
+                t.mwTransformNode(node, Compression);
+                t.nodes[node].flags |= F_HASCOEFS;
+                t.calcNorms(node);
+            }
+        };
+        auto split = [](const Tree<2> &t, int i) {
+            const auto &n = t.nodes[i];
+            bool chkTransl = (n.l[0] == 0 || n.l[1] == 0);
+            bool chkCompNorm = false;
+            for (int c = 1; c < 4; c++)
+                if (n.norms[c] > 0.0) chkCompNorm = true;
+            return chkTransl && chkCompNorm;
+        };
+        tree_build<2>(otree, otree.endNodes(), calc, split, -1, omra.maxScale());
+        otree.mwTransformUp();
+
+        // setupOperNodeCache
+        OperatorTerm term;
+        auto levels = otree.nodesByDepth(false);
+        int nScales = (int)levels.size();
+        term.depth = nScales;
+        term.maxTransl.assign(nScales, 0);
+        for (int n = 0; n < nScales; n++)
+            for (int i : levels[n]) {
+                term.maxTransl[n] = std::max(term.maxTransl[n], std::abs(otree.nodes[i].l[0]));
+                term.maxTransl[n] = std::max(term.maxTransl[n], std::abs(otree.nodes[i].l[1]));
+            }
+        std::vector<std::vector<int>> cache(nScales);
+        for (int n = 0; n < nScales; n++) {
+            int scale = op.operRoot + n;
+            int L = term.maxTransl[n];
+            cache[n].assign(2 * L + 1, -1);
+            for (int i = L; i >= 0; i--) {
+                int l[2] = {0, i};
+                cache[n][L - i] = otree.getNode(scale, l, false);
+            }
+            for (int i = 1; i <= L; i++) {
+                int l[2] = {i, 0};
+                cache[n][L + i] = otree.getNode(scale, l, false);
+            }
+        }
+        size_t total = 0;
+        term.offset.resize(nScales);
+        for (int n = 0; n < nScales; n++) { term.offset[n] = total; total += cache[n].size(); }
+        term.blocks.assign(total * 4 * K * K, 0.0);
+        term.norms.assign(total * 4, 0.0);
+        for (int n = 0; n < nScales; n++)
+            for (size_t j = 0; j < cache[n].size(); j++) {
+                int node = cache[n][j];
+                size_t idx = term.offset[n] + j;
+                std::memcpy(&term.blocks[idx * 4 * K * K], otree.c(node), sizeof(double) * 4 * K * K);
+                for (int c = 0; c < 4; c++) term.norms[idx * 4 + c] = otree.nodes[node].norms[c];
+            }
+        op.terms.push_back(std::move(term));
+    }
+    op.bandPrec = -2.0;
+}
+
+void ConvolutionOperator::calcBandWidths(double prec) {
+    if (prec == bandPrec && !bandMax.empty()) return;
+    int maxDepth = 0;
+    for (auto &t : terms) {
+        double p = prec < 0.0 ? buildPrec : prec;
+        t.bw.w.assign(t.depth + 1, {-1, -1, -1, -1, -1});
+        for (int depth = 0; depth < t.depth; depth++) {
+            int l = 0;
+            bool done = false;
+            while (!done) {
+                done = true;
+                size_t idx = t.nodeIndex(depth, l);
+                double thrs = std::max(MachinePrec, p / (8.0 * (1 << depth)));
+                for (int c = 0; c < 4; c++)
+                    if (t.norms[idx * 4 + c] > thrs) {
+                        t.bw.setWidth(depth, c, l);
+                        done = false;
+                    }
+                if (++l > t.maxTransl[depth]) break;
+            }
+        }
+        if (t.bw.depth() > maxDepth) maxDepth = t.bw.depth();
+    }
+    bandMax.assign(maxDepth + 1, -1);
+    for (auto &t : terms)
+        for (int n = 0; n <= t.bw.depth(); n++)
+            for (int j = 0; j < 4; j++) bandMax[n] = std::max(bandMax[n], t.bw.getWidth(n, j));
+    bandPrec = prec;
+}
+
+int ConvolutionOperator::getMaxBandWidth(int depth) const {
+    if (depth < 0) {
+        int m = -1;
+        for (int w : bandMax) m = std::max(m, w);
+        return m;
+    }
+    if (depth < (int)bandMax.size()) return bandMax[depth];
+    return -1;
+}
+
+std::unique_ptr<ConvolutionOperator> make_convolution(const MRA<3> &mra, const std::vector<GaussFunc<1>> &kernel, double prec) {
+    auto op = std::make_unique<ConvolutionOperator>();
+    op->mra = mra;
+    op->operRoot = mra.rootScale();
+    op->buildPrec = prec;
+    op->kernel = kernel;
+    build_operator_terms(*op, prec / 10.0, prec);
+    return op;
+}
+
+std::unique_ptr<ConvolutionOperator> make_poisson(const MRA<3> &mra, double prec) {
+    double k_prec = prec / 10.0;
+    double r_min = mra.calcMinDistance(k_prec);
+    double r_max = mra.calcMaxDistance();
+    return make_convolution(mra, poisson_kernel(k_prec, r_min, r_max), prec);
+}
+
+std::unique_ptr<ConvolutionOperator> make_helmholtz(const MRA<3> &mra, double mu, double prec) {
+    double k_prec = prec / 10.0;
+    double r_min = mra.calcMinDistance(k_prec);
+    double r_max = mra.calcMaxDistance();
+    return make_convolution(mra, helmholtz_kernel(mu, k_prec, r_min, r_max), prec);
+}
+
+}  // namespace mwh

@@ -1,0 +1,847 @@
+/*
+ * CPU oracle for the operator-application path (TEST INFRASTRUCTURE ONLY).
+ *
+ * A plain-C restatement of MRCPP's mrcpp::apply(prec, out, oper, inp, maxIter,
+ * absPrec) for D = 3, T = double.  Only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline legs of bench.py use it, as the checker or as the timed CPU
+ * stand-in for the reference; the product (libmwgpu.so) never links or calls it.
+ *
+ * Followed line by line (paths inside MRChemSoft/mrcpp):
+ *   apply                     src/treebuilders/apply.cpp:68-93
+ *   band widths               src/operators/MWOperator.cpp:78-108, src/trees/OperatorTree.cpp:109-134
+ *   band-size factors         src/treebuilders/ConvolutionCalculator.cpp:105-139
+ *   band box + node lookup    ConvolutionCalculator.cpp:142-222, src/trees/MWTree.cpp:340-352
+ *   GenNodes                  src/trees/MWNode.cpp:410-418, 1097-1120, FunctionNode.cpp:293-328,
+ *                             src/utils/tree_utils.cpp:113-216 (readOnlyScaling)
+ *   calcNode                  ConvolutionCalculator.cpp:224-274
+ *   applyOperComp/Operator    ConvolutionCalculator.cpp:277-329
+ *   tensorApplyOperComp       ConvolutionCalculator.cpp:333-382 with OperatorState.h:45-127
+ *   node norms                src/trees/MWNode.cpp:609-655
+ *   TreeBuilder loop          src/treebuilders/TreeBuilder.cpp:38-87, 150-166
+ *   split                     src/treebuilders/TreeAdaptor.h:41-52, src/utils/tree_utils.cpp:47-65
+ *   TopDown / BottomUp        src/trees/MWTree.cpp:166-216, MWNode.cpp:312-335,
+ *                             FunctionNode.cpp:391-409, tree_utils.cpp:229-301
+ * Differences from the reference that do not change results: GenNodes needed
+ * by a level are created serially before the parallel node loop (the
+ * reference creates them inside the loop under per-node locks); the work list
+ * is in breadth-first rather than Hilbert order (only the summation order of
+ * the level norm sums changes).
+ *
+ * Parity pin: the reference ships no golden coefficients for this path.  The
+ * oracle is pinned by the reference's own known-answer tests re-run through
+ * it (tests/test_oracle_pins.py): Poisson Coulomb self-energy of a unit
+ * Gaussian (tests/operators/poisson_operator.cpp:129-154), the hydrogen
+ * Helmholtz fixed point (tests/operators/helmholtz_operator.cpp:131-198) and
+ * the analytic erf potential.
+ */
+#include "oracle_apply.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MACHINE_ZERO 1.0e-14
+#define MACHINE_PREC 1.0e-15
+#define MAX_DEPTH_ROWS 30
+
+/* ---------------------------------------------------------------- trees */
+typedef struct {
+    int n, l[3];
+} okey;
+
+typedef struct {
+    okey *keys;
+    int *vals;
+    size_t cap, count;
+} omap;
+
+typedef struct {
+    int K, K3, nc; /* nc = 8K^3 */
+    int root_scale, corner[3], nbox[3];
+    size_t n, cap;
+    okey *idx;
+    int *child0; /* first of 8 contiguous children or -1 */
+    int *parent;
+    int *gen;    /* 1 = GenNode (scaling coefficients only) */
+    double *coefs; /* nc per node (GenNodes use the first K^3) */
+    double *norms; /* 8 per node */
+    double *sqn;
+    int *roots;
+    int nroots;
+    omap map;
+    double square_norm;
+} otree;
+
+static uint64_t okey_hash(okey k) {
+    uint64_t h = (uint64_t)(uint32_t)k.n * 0x9E3779B97F4A7C15ull;
+    for (int d = 0; d < 3; d++) h ^= (uint64_t)(uint32_t)k.l[d] + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    return h;
+}
+static int okey_eq(okey a, okey b) { return a.n == b.n && a.l[0] == b.l[0] && a.l[1] == b.l[1] && a.l[2] == b.l[2]; }
+
+static void omap_init(omap *m, size_t cap) {
+    m->cap = 1;
+    while (m->cap < cap) m->cap <<= 1;
+    m->keys = (okey *)malloc(sizeof(okey) * m->cap);
+    m->vals = (int *)malloc(sizeof(int) * m->cap);
+    for (size_t i = 0; i < m->cap; i++) m->vals[i] = -1;
+    m->count = 0;
+}
+static void omap_free(omap *m) {
+    free(m->keys);
+    free(m->vals);
+}
+static int omap_find(const omap *m, okey k) {
+    size_t s = okey_hash(k) & (m->cap - 1);
+    for (;;) {
+        if (m->vals[s] < 0) return -1;
+        if (okey_eq(m->keys[s], k)) return m->vals[s];
+        s = (s + 1) & (m->cap - 1);
+    }
+}
+static void omap_put(omap *m, okey k, int v);
+static void omap_grow(omap *m) {
+    omap n;
+    omap_init(&n, m->cap * 2);
+    for (size_t i = 0; i < m->cap; i++)
+        if (m->vals[i] >= 0) omap_put(&n, m->keys[i], m->vals[i]);
+    omap_free(m);
+    *m = n;
+}
+static void omap_put(omap *m, okey k, int v) {
+    if (2 * (m->count + 1) > m->cap) omap_grow(m);
+    size_t s = okey_hash(k) & (m->cap - 1);
+    for (;;) {
+        if (m->vals[s] < 0) {
+            m->keys[s] = k;
+            m->vals[s] = v;
+            m->count++;
+            return;
+        }
+        if (okey_eq(m->keys[s], k)) {
+            m->vals[s] = v;
+            return;
+        }
+        s = (s + 1) & (m->cap - 1);
+    }
+}
+
+static void tree_reserve(otree *t, size_t need) {
+    if (need <= t->cap) return;
+    size_t cap = t->cap ? t->cap : 64;
+    while (cap < need) cap *= 2;
+    t->idx = (okey *)realloc(t->idx, sizeof(okey) * cap);
+    t->child0 = (int *)realloc(t->child0, sizeof(int) * cap);
+    t->parent = (int *)realloc(t->parent, sizeof(int) * cap);
+    t->gen = (int *)realloc(t->gen, sizeof(int) * cap);
+    t->coefs = (double *)realloc(t->coefs, sizeof(double) * cap * t->nc);
+    t->norms = (double *)realloc(t->norms, sizeof(double) * cap * 8);
+    t->sqn = (double *)realloc(t->sqn, sizeof(double) * cap);
+    t->cap = cap;
+}
+
+static int tree_add(otree *t, okey k, int parent, int gen) {
+    tree_reserve(t, t->n + 1);
+    int id = (int)t->n++;
+    t->idx[id] = k;
+    t->child0[id] = -1;
+    t->parent[id] = parent;
+    t->gen[id] = gen;
+    memset(t->coefs + (size_t)id * t->nc, 0, sizeof(double) * t->nc);
+    for (int c = 0; c < 8; c++) t->norms[(size_t)id * 8 + c] = -1.0;
+    t->sqn[id] = -1.0;
+    omap_put(&t->map, k, id);
+    return id;
+}
+
+static void tree_init(otree *t, const oracle_mra *m) {
+    memset(t, 0, sizeof(*t));
+    t->K = m->order + 1;
+    t->K3 = t->K * t->K * t->K;
+    t->nc = 8 * t->K3;
+    t->root_scale = m->root_scale;
+    for (int d = 0; d < 3; d++) {
+        t->corner[d] = m->corner[d];
+        t->nbox[d] = m->nbox[d];
+    }
+    omap_init(&t->map, 1024);
+    t->square_norm = -1.0;
+}
+
+static void tree_free(otree *t) {
+    free(t->idx);
+    free(t->child0);
+    free(t->parent);
+    free(t->gen);
+    free(t->coefs);
+    free(t->norms);
+    free(t->sqn);
+    free(t->roots);
+    omap_free(&t->map);
+}
+
+/* flat tree, parents before children, roots first */
+static int tree_load(otree *t, const oracle_mra *m, int n, const int *idx, const int *child0, const double *coefs, const double *norms) {
+    tree_init(t, m);
+    tree_reserve(t, (size_t)n);
+    int nr = m->nbox[0] * m->nbox[1] * m->nbox[2];
+    t->roots = (int *)malloc(sizeof(int) * nr);
+    t->nroots = nr;
+    for (int j = 0; j < n; j++) {
+        okey k = {idx[4 * j], {idx[4 * j + 1], idx[4 * j + 2], idx[4 * j + 3]}};
+        tree_add(t, k, -1, 0);
+    }
+    for (int j = 0; j < n; j++) {
+        t->child0[j] = child0[j];
+        if (child0[j] >= 0)
+            for (int c = 0; c < 8; c++) t->parent[child0[j] + c] = j;
+        if (coefs) memcpy(t->coefs + (size_t)j * t->nc, coefs + (size_t)j * t->nc, sizeof(double) * t->nc);
+        if (norms) {
+            double s = 0.0;
+            for (int c = 0; c < 8; c++) {
+                t->norms[(size_t)j * 8 + c] = norms[(size_t)j * 8 + c];
+                s += norms[(size_t)j * 8 + c] * norms[(size_t)j * 8 + c];
+            }
+            t->sqn[j] = s;
+        }
+    }
+    if (n < nr) return -1;
+    for (int r = 0; r < nr; r++) t->roots[r] = r;
+    return 0;
+}
+
+/* ---------------------------------------------------------------- 1D filter step */
+/* math_utils::apply_filter: g(K^2 x K) (=|+=) f^T(K^2 x K) * F(K x K), column-major */
+static void apply_filter(double *out, const double *in, const double *F, int K, int add) {
+    const int K2 = K * K;
+    for (int j = 0; j < K; j++) {
+        const double *Fj = F + (size_t)K * j;
+        for (int c = 0; c < K2; c++) {
+            const double *fc = in + (size_t)K * c;
+            double s = 0.0;
+            for (int i = 0; i < K; i++) s += fc[i] * Fj[i];
+            if (add) out[c + (size_t)K2 * j] += s;
+            else out[c + (size_t)K2 * j] = s;
+        }
+    }
+}
+
+static const double *filt(const oracle_mra *m, int op, int fidx) {
+    int K = m->order + 1;
+    return m->filters + ((size_t)op * 4 + fidx) * K * K;
+}
+
+/* tree_utils::mw_transform (D = 3): parent -> 8 children scaling blocks at stride */
+static void mw_transform(const oracle_mra *m, const double *in, double *out, int readOnlyScaling, int stride, int overwrite, double *tmp1,
+                         double *tmp2) {
+    const int K = m->order + 1, K3 = K * K * K;
+    int ftlim = 8, ftlim2 = 8, ftlim3 = 8;
+    if (readOnlyScaling) {
+        ftlim = 1;
+        ftlim2 = 2;
+        ftlim3 = 4;
+    }
+    int add;
+    for (int gt = 0; gt < 8; gt++) {
+        add = 0;
+        for (int ft = 0; ft < ftlim; ft++)
+            if ((gt | 1) == (ft | 1)) {
+                apply_filter(tmp1 + (size_t)gt * K3, in + (size_t)ft * K3, filt(m, 1, 2 * ((gt >> 0) & 1) + ((ft >> 0) & 1)), K, add);
+                add = 1;
+            }
+    }
+    for (int gt = 0; gt < 8; gt++) {
+        add = 0;
+        for (int ft = 0; ft < ftlim2; ft++)
+            if ((gt | 2) == (ft | 2)) {
+                apply_filter(tmp2 + (size_t)gt * K3, tmp1 + (size_t)ft * K3, filt(m, 1, 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1)), K, add);
+                add = 1;
+            }
+    }
+    for (int gt = 0; gt < 8; gt++) {
+        add = overwrite ? 0 : 1;
+        for (int ft = 0; ft < ftlim3; ft++)
+            if ((gt | 4) == (ft | 4)) {
+                apply_filter(out + (size_t)gt * stride, tmp2 + (size_t)ft * K3, filt(m, 1, 2 * ((gt >> 2) & 1) + ((ft >> 2) & 1)), K, add);
+                add = 1;
+            }
+    }
+}
+
+/* tree_utils::mw_transform_back (D = 3): 8 children scaling at stride -> parent s+d */
+static void mw_transform_back(const oracle_mra *m, const double *in, double *out, int stride, double *tmp) {
+    const int K = m->order + 1, K3 = K * K * K;
+    int add;
+    for (int gt = 0; gt < 8; gt++) {
+        add = 0;
+        for (int ft = 0; ft < 8; ft++)
+            if ((gt | 1) == (ft | 1)) {
+                apply_filter(out + (size_t)gt * K3, in + (size_t)ft * stride, filt(m, 0, 2 * (gt & 1) + (ft & 1)), K, add);
+                add = 1;
+            }
+    }
+    for (int gt = 0; gt < 8; gt++) {
+        add = 0;
+        for (int ft = 0; ft < 8; ft++)
+            if ((gt | 2) == (ft | 2)) {
+                apply_filter(tmp + (size_t)gt * K3, out + (size_t)ft * K3, filt(m, 0, 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1)), K, add);
+                add = 1;
+            }
+    }
+    for (int gt = 0; gt < 8; gt++) {
+        add = 0;
+        for (int ft = 0; ft < 8; ft++)
+            if ((gt | 4) == (ft | 4)) {
+                apply_filter(out + (size_t)gt * K3, tmp + (size_t)ft * K3, filt(m, 0, 2 * ((gt >> 2) & 1) + ((ft >> 2) & 1)), K, add);
+                add = 1;
+            }
+    }
+}
+
+/* MWNode::calcNorms / calcComponentNorm (GenNode wavelet norms are 0) */
+static void calc_norms(otree *t, int i) {
+    double sq = 0.0;
+    for (int c = 0; c < 8; c++) {
+        double nrm = 0.0;
+        if (!(t->gen[i] && c != 0)) {
+            const double *x = t->coefs + (size_t)i * t->nc + (size_t)c * t->K3;
+            double s = 0.0;
+            for (int j = 0; j < t->K3; j++) s += x[j] * x[j];
+            nrm = sqrt(s);
+        }
+        t->norms[(size_t)i * 8 + c] = nrm;
+        sq += nrm * nrm;
+    }
+    t->sqn[i] = sq;
+}
+
+static double scaling_norm(const otree *t, int i) {
+    double s = t->norms[(size_t)i * 8];
+    return s >= 0.0 ? s * s : -1.0;
+}
+static double wavelet_norm(const otree *t, int i) {
+    double w = 0.0;
+    for (int c = 1; c < 8; c++) {
+        double n = t->norms[(size_t)i * 8 + c];
+        if (n >= 0.0) w += n * n;
+        else w = -1.0;
+    }
+    return w;
+}
+
+static int create_children(otree *t, int i, int gen) {
+    int first = -1;
+    for (int c = 0; c < 8; c++) {
+        okey k;
+        k.n = t->idx[i].n + 1;
+        for (int d = 0; d < 3; d++) k.l[d] = 2 * t->idx[i].l[d] + ((c >> d) & 1);
+        int id = tree_add(t, k, i, gen);
+        if (c == 0) first = id;
+    }
+    t->child0[i] = first;
+    return first;
+}
+
+/* MWTree::getNode with generation (MWNode::retrieveNode, threadSafeGenChildren) */
+static int get_node(otree *t, const oracle_mra *m, okey k, double *tmp1, double *tmp2) {
+    int id = omap_find(&t->map, k);
+    if (id >= 0) return id;
+    int shift = k.n - t->root_scale;
+    okey r;
+    r.n = t->root_scale;
+    for (int d = 0; d < 3; d++) r.l[d] = k.l[d] >> shift;
+    int cur = omap_find(&t->map, r);
+    if (cur < 0) return -1;
+    while (t->idx[cur].n < k.n) {
+        if (t->child0[cur] < 0) {
+            int c0 = create_children(t, cur, 1);
+            int ro = t->gen[cur];
+            /* giveChildrenCoefs(overwrite = true): GenNode children hold K^3 coefficients,
+               stride nc in this storage (the first K^3 are used) */
+            for (int c = 0; c < 8; c++) memset(t->coefs + (size_t)(c0 + c) * t->nc, 0, sizeof(double) * t->nc);
+            mw_transform(m, t->coefs + (size_t)cur * t->nc, t->coefs + (size_t)c0 * t->nc, ro, t->nc, 1, tmp1, tmp2);
+            for (int c = 0; c < 8; c++) calc_norms(t, c0 + c);
+        }
+        int sh = k.n - t->idx[cur].n - 1;
+        int c = 0;
+        for (int d = 0; d < 3; d++) c |= ((k.l[d] >> sh) & 1) << d;
+        cur = t->child0[cur] + c;
+    }
+    return cur;
+}
+
+/* ---------------------------------------------------------------- operator */
+typedef struct {
+    int T, K;
+    const int *depth;
+    int *row0;   /* first max_transl row of each term */
+    size_t *off; /* per (term, depth) node offset of l = -L */
+    const int *mt;
+    const double *blocks, *norms;
+    int *bw;     /* [T][rows][5] */
+    int rows;
+    int *band_max; /* [rows] */
+    int n_band_max;
+    int *bsize;  /* [T][30][65] */
+} ooper;
+
+static void oper_setup(ooper *o, const oracle_oper *d, double prec) {
+    o->T = d->n_terms;
+    o->K = d->order + 1;
+    o->depth = d->depth;
+    o->mt = d->max_transl;
+    o->blocks = d->blocks;
+    o->norms = d->norms;
+    int maxDepth = 0;
+    for (int t = 0; t < o->T; t++)
+        if (d->depth[t] > maxDepth) maxDepth = d->depth[t];
+    o->rows = maxDepth + 1;
+    o->row0 = (int *)malloc(sizeof(int) * o->T);
+    o->off = (size_t *)malloc(sizeof(size_t) * o->T * o->rows);
+    o->bw = (int *)malloc(sizeof(int) * o->T * o->rows * 5);
+    for (int i = 0; i < o->T * o->rows * 5; i++) o->bw[i] = -1;
+    if (prec < 0.0) prec = d->build_prec;
+    size_t node = 0;
+    int row = 0;
+    for (int t = 0; t < o->T; t++) {
+        o->row0[t] = row;
+        for (int dd = 0; dd < d->depth[t]; dd++) {
+            int L = d->max_transl[row + dd];
+            o->off[(size_t)t * o->rows + dd] = node;
+            /* OperatorTree::calcBandWidth */
+            int l = 0, done = 0;
+            while (!done) {
+                done = 1;
+                size_t nid = node + (size_t)(l + L);
+                double thrs = fmax(MACHINE_PREC, prec / (8.0 * (1 << dd)));
+                for (int c = 0; c < 4; c++)
+                    if (d->norms[nid * 4 + c] > thrs) {
+                        int *w = &o->bw[((size_t)t * o->rows + dd) * 5];
+                        w[c] = l;
+                        if (l > w[4]) w[4] = l;
+                        done = 0;
+                    }
+                if (++l > L) break;
+            }
+            node += 2 * (size_t)L + 1;
+        }
+        row += d->depth[t];
+    }
+    /* MWOperator::calcBandWidths */
+    o->n_band_max = maxDepth + 1;
+    o->band_max = (int *)malloc(sizeof(int) * o->n_band_max);
+    for (int n = 0; n < o->n_band_max; n++) o->band_max[n] = -1;
+    for (int t = 0; t < o->T; t++)
+        for (int n = 0; n <= d->depth[t]; n++)
+            for (int c = 0; c < 4; c++) {
+                int w = o->bw[((size_t)t * o->rows + n) * 5 + c];
+                if (w > o->band_max[n]) o->band_max[n] = w;
+            }
+    /* ConvolutionCalculator::initBandSizes / calcBandSizeFactor */
+    o->bsize = (int *)calloc((size_t)o->T * MAX_DEPTH_ROWS * 65, sizeof(int));
+    for (int t = 0; t < o->T; t++)
+        for (int dd = 0; dd < MAX_DEPTH_ROWS; dd++) {
+            int *row_ = o->bsize + ((size_t)t * MAX_DEPTH_ROWS + dd) * 65;
+            int mx = 0;
+            for (int gt = 0; gt < 8; gt++)
+                for (int ft = 0; ft < 8; ft++) {
+                    int tot = 1;
+                    for (int i = 0; i < 3; i++) {
+                        int oIdx = 2 * ((gt >> i) & 1) + ((ft >> i) & 1);
+                        int width = (dd > d->depth[t]) ? -1 : o->bw[((size_t)t * o->rows + dd) * 5 + oIdx];
+                        if (width < 0) continue;
+                        tot *= 2 * width + 1;
+                    }
+                    row_[gt * 8 + ft] = tot * 64;
+                    if (tot * 64 > mx) mx = tot * 64;
+                }
+            row_[64] = mx;
+        }
+}
+
+static void oper_free(ooper *o) {
+    free(o->row0);
+    free(o->off);
+    free(o->bw);
+    free(o->band_max);
+    free(o->bsize);
+}
+
+static int bw_get(const ooper *o, int t, int depth, int idx) {
+    if (depth > o->depth[t] || depth < 0 || depth >= o->rows) return -1;
+    return o->bw[((size_t)t * o->rows + depth) * 5 + idx];
+}
+
+/* OperatorTree::getNode(depth, l) via the node cache */
+static size_t oper_node(const ooper *o, int t, int depth, int l) {
+    int L = o->mt[o->row0[t] + depth];
+    return o->off[(size_t)t * o->rows + depth] + (size_t)(l + L);
+}
+
+/* ---------------------------------------------------------------- apply */
+typedef struct {
+    unsigned long long node_terms, components;
+} ostats;
+
+/* band box of g (makeOperBand); returns 0 when the band is empty */
+static int band_box(const ooper *o, const otree *f, okey g, int *s, int *e) {
+    int depth = g.n - f->root_scale;
+    int width = (depth >= 0 && depth < o->n_band_max) ? o->band_max[depth] : -1;
+    if (width < 0) return 0;
+    for (int i = 0; i < 3; i++) {
+        int nboxes = f->nbox[i] * (1 << depth);
+        int c_i = f->corner[i] * (1 << depth);
+        s[i] = g.l[i] - width;
+        e[i] = g.l[i] + width;
+        if (s[i] < c_i) s[i] = c_i;
+        if (e[i] > c_i + nboxes - 1) e[i] = c_i + nboxes - 1;
+        if (e[i] < s[i]) return 0;
+    }
+    return 1;
+}
+
+/* ConvolutionCalculator::calcNode for output node gi */
+static void calc_node(const oracle_mra *m, const ooper *o, const otree *f, otree *g, int gi, double prec, double gsq, double *scr,
+                      ostats *st) {
+    const int K = g->K, K3 = g->K3;
+    double *gc = g->coefs + (size_t)gi * g->nc;
+    memset(gc, 0, sizeof(double) * g->nc);
+    okey gk = g->idx[gi];
+    int o_depth = gk.n - m->root_scale;
+    double gThrs = gsq;
+    if (gThrs > 0.0) {
+        double nTerms = (double)o->T;
+        double precFac = 1.0;
+        gThrs = prec * precFac * sqrt(gThrs / nTerms);
+    }
+    int s[3], e[3];
+    double *scr1 = scr, *scr2 = scr + K3;
+    if (band_box(o, f, gk, s, e)) {
+        int fl[3];
+        for (fl[2] = s[2]; fl[2] <= e[2]; fl[2]++)
+            for (fl[1] = s[1]; fl[1] <= e[1]; fl[1]++)
+                for (fl[0] = s[0]; fl[0] <= e[0]; fl[0]++) {
+                    okey fk = {gk.n, {fl[0], fl[1], fl[2]}};
+                    int fi = omap_find(&f->map, fk);
+                    if (fi < 0) continue; /* cannot happen: GenNodes made beforehand */
+                    const double *fc = f->coefs + (size_t)fi * f->nc;
+                    int maxDeltaL = 0;
+                    for (int d = 0; d < 3; d++) {
+                        int dl = abs(fl[d] - gk.l[d]);
+                        if (dl > maxDeltaL) maxDeltaL = dl;
+                    }
+                    for (int ft = 0; ft < 8; ft++) {
+                        double fNorm = f->norms[(size_t)fi * 8 + ft];
+                        if (fNorm < MACHINE_ZERO) continue;
+                        for (int gt = 0; gt < 8; gt++) {
+                            if (!(o_depth == 0 || gt != 0 || ft != 0)) continue;
+                            /* applyOperComp */
+                            for (int i = 0; i < o->T; i++) {
+                                if (maxDeltaL > bw_get(o, i, o_depth, 4)) continue;
+                                double fThreshold = (double)o->bsize[((size_t)i * MAX_DEPTH_ROWS + o_depth) * 65 + gt * 8 + ft] * fNorm;
+                                /* applyOperator */
+                                double oNorm = 1.0;
+                                const double *oData[3];
+                                int outside = 0;
+                                for (int d = 0; d < 3; d++) {
+                                    int oTransl = fl[d] - gk.l[d];
+                                    int a = (gt >> d) & 1, b = (ft >> d) & 1;
+                                    int idx = (a << 1) + b;
+                                    if (abs(oTransl) > bw_get(o, i, o_depth, idx)) {
+                                        outside = 1;
+                                        break;
+                                    }
+                                    size_t node = oper_node(o, i, o_depth, oTransl);
+                                    oNorm *= o->norms[node * 4 + idx];
+                                    oData[d] = o->blocks + node * 4 * K * K + (size_t)idx * K * K;
+                                }
+                                if (outside) continue;
+                                double upperBound = oNorm * fThreshold;
+                                if (upperBound > gThrs) {
+                                    st->components++;
+                                    /* tensorApplyOperComp */
+                                    apply_filter(scr2, fc + (size_t)ft * K3, oData[0], K, 0);
+                                    apply_filter(scr1, scr2, oData[1], K, 0);
+                                    apply_filter(gc + (size_t)gt * K3, scr1, oData[2], K, 1);
+                                }
+                            }
+                        }
+                    }
+                }
+    }
+    calc_norms(g, gi);
+}
+
+/* node.term count: (g, f, i) triples with >= 1 contracted component.  Counted by
+ * re-running the screening without the contraction (instrumentation only). */
+static unsigned long long count_node_terms(const oracle_mra *m, const ooper *o, const otree *f, const otree *g, int gi, double prec,
+                                           double gsq) {
+    okey gk = g->idx[gi];
+    int o_depth = gk.n - m->root_scale;
+    double gThrs = gsq;
+    if (gThrs > 0.0) gThrs = prec * 1.0 * sqrt(gThrs / (double)o->T);
+    int s[3], e[3];
+    unsigned long long cnt = 0;
+    if (!band_box(o, f, gk, s, e)) return 0;
+    int fl[3];
+    for (fl[2] = s[2]; fl[2] <= e[2]; fl[2]++)
+        for (fl[1] = s[1]; fl[1] <= e[1]; fl[1]++)
+            for (fl[0] = s[0]; fl[0] <= e[0]; fl[0]++) {
+                okey fk = {gk.n, {fl[0], fl[1], fl[2]}};
+                int fi = omap_find(&f->map, fk);
+                if (fi < 0) continue;
+                int maxDeltaL = 0;
+                for (int d = 0; d < 3; d++) {
+                    int dl = abs(fl[d] - gk.l[d]);
+                    if (dl > maxDeltaL) maxDeltaL = dl;
+                }
+                for (int i = 0; i < o->T; i++) {
+                    if (maxDeltaL > bw_get(o, i, o_depth, 4)) continue;
+                    int any = 0;
+                    for (int ft = 0; ft < 8 && !any; ft++) {
+                        double fNorm = f->norms[(size_t)fi * 8 + ft];
+                        if (fNorm < MACHINE_ZERO) continue;
+                        for (int gt = 0; gt < 8 && !any; gt++) {
+                            if (!(o_depth == 0 || gt != 0 || ft != 0)) continue;
+                            double fThreshold = (double)o->bsize[((size_t)i * MAX_DEPTH_ROWS + o_depth) * 65 + gt * 8 + ft] * fNorm;
+                            double oNorm = 1.0;
+                            int outside = 0;
+                            for (int d = 0; d < 3; d++) {
+                                int oTransl = fl[d] - gk.l[d];
+                                int idx = (((gt >> d) & 1) << 1) + ((ft >> d) & 1);
+                                if (abs(oTransl) > bw_get(o, i, o_depth, idx)) {
+                                    outside = 1;
+                                    break;
+                                }
+                                oNorm *= o->norms[oper_node(o, i, o_depth, oTransl) * 4 + idx];
+                            }
+                            if (!outside && oNorm * fThreshold > gThrs) any = 1;
+                        }
+                    }
+                    cnt += (unsigned long long)any;
+                }
+            }
+    return cnt;
+}
+
+/* tree_utils::split_check */
+static int split_check(const otree *t, int i, double prec, double splitFac, int absPrec) {
+    int split = 0;
+    if (prec > 0.0) {
+        double t_norm = 1.0;
+        double sq_norm = t->square_norm;
+        if (sq_norm > 0.0 && !absPrec) t_norm = sqrt(sq_norm);
+        double scale_fac = 1.0;
+        if (splitFac > MACHINE_ZERO) {
+            double expo = 0.5 * splitFac * (t->idx[i].n + 1);
+            scale_fac = pow(2.0, -expo);
+        }
+        double w_thrs = fmax(2.0 * MACHINE_PREC, prec * t_norm * scale_fac);
+        double w_norm = sqrt(wavelet_norm(t, i));
+        if (w_norm > w_thrs) split = 1;
+    }
+    return split;
+}
+
+/* breadth-first list of nodes, optionally only branch nodes, per depth */
+static int *bfs(const otree *t, size_t *count, int **lvl_start, int *nlvl) {
+    int *out = (int *)malloc(sizeof(int) * (t->n + 1));
+    size_t c = 0;
+    int cap_l = 64;
+    *lvl_start = (int *)malloc(sizeof(int) * cap_l);
+    *nlvl = 0;
+    for (int r = 0; r < t->nroots; r++) out[c++] = t->roots[r];
+    size_t head = 0;
+    while (head < c) {
+        size_t end = c;
+        if (*nlvl + 2 > cap_l) {
+            cap_l *= 2;
+            *lvl_start = (int *)realloc(*lvl_start, sizeof(int) * cap_l);
+        }
+        (*lvl_start)[(*nlvl)++] = (int)head;
+        for (; head < end; head++) {
+            int i = out[head];
+            int c0 = t->child0[i];
+            if (c0 >= 0 && !t->gen[c0])
+                for (int k = 0; k < 8; k++) out[c++] = c0 + k;
+        }
+    }
+    (*lvl_start)[*nlvl] = (int)c;
+    *count = c;
+    return out;
+}
+
+struct oracle_result {
+    otree g;
+    ostats st;
+    int iterations;
+};
+
+int oracle_apply(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm, double prec,
+                 int max_iter, int abs_prec, int nthreads, int count_terms, oracle_result **res) {
+    if (!m || !od || !inp || !out0 || !res) return 1;
+    if (od->order != m->order) return 1;
+    ooper o;
+    oper_setup(&o, od, prec); /* MWOperator::calcBandWidths(prec) */
+    otree f;
+    if (tree_load(&f, m, inp->n_nodes, inp->idx, inp->child0, inp->coefs, inp->norms)) return 2;
+    oracle_result *R = (oracle_result *)calloc(1, sizeof(oracle_result));
+    if (tree_load(&R->g, m, out0->n_nodes, out0->idx, out0->child0, NULL, NULL)) return 2;
+    otree *g = &R->g;
+    g->square_norm = out_sqnorm;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    const int K3 = g->K3;
+    double *tmp1 = (double *)malloc(sizeof(double) * 8 * K3), *tmp2 = (double *)malloc(sizeof(double) * 8 * K3);
+    int max_scale = m->max_scale;
+    /* initial work vector: all nodes of the output tree (breadth-first) */
+    size_t nwork;
+    int *lvl, nl;
+    int *work = bfs(g, &nwork, &lvl, &nl);
+    free(lvl);
+    double sNorm = 0.0, wNorm = 0.0;
+    int iter = 0;
+    while (nwork > 0) {
+        /* GenNodes of the bands of this level (serially, before the parallel loop) */
+        for (size_t w = 0; w < nwork; w++) {
+            okey gk = g->idx[work[w]];
+            int s[3], e[3], fl[3];
+            if (!band_box(&o, &f, gk, s, e)) continue;
+            for (fl[2] = s[2]; fl[2] <= e[2]; fl[2]++)
+                for (fl[1] = s[1]; fl[1] <= e[1]; fl[1]++)
+                    for (fl[0] = s[0]; fl[0] <= e[0]; fl[0]++) {
+                        okey fk = {gk.n, {fl[0], fl[1], fl[2]}};
+                        get_node(&f, m, fk, tmp1, tmp2);
+                    }
+        }
+        double gsq = g->square_norm;
+        unsigned long long comps = 0, nts = 0;
+#pragma omp parallel reduction(+ : comps, nts)
+        {
+            double *scr = (double *)malloc(sizeof(double) * 2 * K3);
+            ostats ls = {0, 0};
+#pragma omp for schedule(dynamic, 1)
+            for (long w = 0; w < (long)nwork; w++) {
+                calc_node(m, &o, &f, g, work[w], prec, gsq, scr, &ls);
+                if (count_terms) nts += count_node_terms(m, &o, &f, g, work[w], prec, gsq);
+            }
+            comps += ls.components;
+            free(scr);
+        }
+        R->st.components += comps;
+        R->st.node_terms += nts;
+        /* TreeBuilder norm bookkeeping */
+        if (iter == 0) {
+            sNorm = 0.0;
+            for (size_t w = 0; w < nwork; w++)
+                if (g->idx[work[w]].n - m->root_scale >= 0) sNorm += scaling_norm(g, work[w]);
+        }
+        for (size_t w = 0; w < nwork; w++)
+            if (g->idx[work[w]].n - m->root_scale >= 0) wNorm += wavelet_norm(g, work[w]);
+        g->square_norm = (sNorm < 0.0 || wNorm < 0.0) ? -1.0 : sNorm + wNorm;
+        if (iter >= max_iter && max_iter >= 0) nwork = 0;
+        /* TreeAdaptor::splitNodeVector */
+        int *next = (int *)malloc(sizeof(int) * (8 * nwork + 1));
+        size_t nn = 0;
+        for (size_t w = 0; w < nwork; w++) {
+            int i = work[w];
+            if (g->child0[i] >= 0) continue;
+            if (g->idx[i].n + 2 > max_scale) continue;
+            if (split_check(g, i, prec, 1.0, abs_prec)) {
+                int c0 = create_children(g, i, 0);
+                for (int c = 0; c < 8; c++) next[nn++] = c0 + c;
+            }
+        }
+        free(work);
+        work = next;
+        nwork = nn;
+        iter++;
+    }
+    free(work);
+    R->iterations = iter;
+    /* mwTransform(TopDown, false) */
+    size_t cnt;
+    int *order = bfs(g, &cnt, &lvl, &nl);
+    for (int L = 0; L < nl; L++) {
+#pragma omp parallel
+        {
+            double *t1 = (double *)malloc(sizeof(double) * 8 * K3), *t2 = (double *)malloc(sizeof(double) * 8 * K3);
+#pragma omp for schedule(dynamic, 4)
+            for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+                int i = order[q];
+                int c0 = g->child0[i];
+                if (c0 < 0) continue;
+                mw_transform(m, g->coefs + (size_t)i * g->nc, g->coefs + (size_t)c0 * g->nc, 0, g->nc, 0, t1, t2);
+                for (int c = 0; c < 8; c++) calc_norms(g, c0 + c);
+            }
+            free(t1);
+            free(t2);
+        }
+    }
+    /* mwTransform(BottomUp) */
+    for (int L = nl - 2; L >= 0; L--) {
+#pragma omp parallel
+        {
+            double *t1 = (double *)malloc(sizeof(double) * 8 * K3);
+#pragma omp for schedule(dynamic, 4)
+            for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+                int i = order[q];
+                int c0 = g->child0[i];
+                if (c0 < 0) continue;
+                mw_transform_back(m, g->coefs + (size_t)c0 * g->nc, g->coefs + (size_t)i * g->nc, g->nc, t1);
+                calc_norms(g, i);
+            }
+            free(t1);
+        }
+    }
+    /* calcSquareNorm over end nodes */
+    double sq = 0.0;
+    for (size_t q = 0; q < cnt; q++)
+        if (g->child0[order[q]] < 0) sq += g->sqn[order[q]];
+    g->square_norm = sq;
+    free(order);
+    free(lvl);
+    free(tmp1);
+    free(tmp2);
+    tree_free(&f);
+    oper_free(&o);
+    *res = R;
+    return 0;
+}
+
+int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
+                       unsigned long long *components, int *iterations) {
+    if (!r) return 1;
+    if (n_nodes) *n_nodes = (int)r->g.n;
+    if (square_norm) *square_norm = r->g.square_norm;
+    if (node_terms) *node_terms = r->st.node_terms;
+    if (components) *components = r->st.components;
+    if (iterations) *iterations = r->iterations;
+    return 0;
+}
+
+int oracle_result_export(const oracle_result *r, int *idx, int *child0, double *coefs, double *norms) {
+    if (!r) return 1;
+    const otree *g = &r->g;
+    for (size_t i = 0; i < g->n; i++) {
+        if (idx) {
+            idx[4 * i] = g->idx[i].n;
+            for (int d = 0; d < 3; d++) idx[4 * i + 1 + d] = g->idx[i].l[d];
+        }
+        if (child0) child0[i] = g->child0[i];
+    }
+    if (coefs) memcpy(coefs, g->coefs, sizeof(double) * g->n * g->nc);
+    if (norms) memcpy(norms, g->norms, sizeof(double) * g->n * 8);
+    return 0;
+}
+
+void oracle_result_free(oracle_result *r) {
+    if (!r) return;
+    tree_free(&r->g);
+    free(r);
+}

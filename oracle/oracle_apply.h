@@ -1,0 +1,55 @@
+/*
+ * CPU oracle for mrcpp::apply (test infrastructure only; see oracle_apply.c).
+ */
+#ifndef ORACLE_APPLY_H
+#define ORACLE_APPLY_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int order;          /* k */
+    int root_scale;
+    int corner[3];
+    int nbox[3];
+    int max_scale;
+    double sf;
+    /* 8 (k+1)^2 column-major filters: compression H0t,H1t,G0t,G1t, reconstruction H0,G0,H1,G1 */
+    const double *filters;
+} oracle_mra;
+
+typedef struct {
+    int n_terms;
+    int order;
+    const int *depth;      /* [n_terms] operator scales per term */
+    const int *max_transl; /* [sum depth] */
+    const double *blocks;  /* per node 4 (k+1)^2, nodes l = -L..L per (term, depth) */
+    const double *norms;   /* per node 4 */
+    double build_prec;
+} oracle_oper;
+
+typedef struct {
+    int n_nodes;
+    const int *idx;        /* [n*4] scale, l0, l1, l2; roots first, parents before children */
+    const int *child0;     /* [n] */
+    const double *coefs;   /* [n*8K^3] (input tree) */
+    const double *norms;   /* [n*8] (input tree) */
+} oracle_tree;
+
+typedef struct oracle_result oracle_result;
+
+/* apply(prec, out, oper, inp, max_iter, abs_prec) starting from the topology out0
+ * whose square norm is out_sqnorm (-1 for a fresh or copied grid). */
+int oracle_apply(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
+                 double prec, int max_iter, int abs_prec, int nthreads, int count_terms, oracle_result **res);
+int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
+                       unsigned long long *components, int *iterations);
+int oracle_result_export(const oracle_result *r, int *idx, int *child0, double *coefs, double *norms);
+void oracle_result_free(oracle_result *r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
