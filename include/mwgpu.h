@@ -167,6 +167,21 @@ mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tree, double 
 /* Synchronises the context stream; returns device errors. */
 mwgpu_status mwgpu_sync(mwgpu_ctx *ctx);
 
+/* Drops the GenNodes made by earlier mwgpu_apply_level calls on an input tree
+ * (FunctionTree::deleteGenerated, called by apply at apply.cpp:86-87). */
+mwgpu_status mwgpu_tree_clear_generated(mwgpu_ctx *ctx, mwgpu_tree *tree);
+
+/* Device timers: records CUDA event `slot` (0..15) on the context stream;
+ * elapsed time between two recorded slots. No reference counterpart (MRCPP's
+ * Timer, src/utils/Timer.h:40-58, is host-only). */
+mwgpu_status mwgpu_timer_mark(mwgpu_ctx *ctx, int slot);
+mwgpu_status mwgpu_timer_elapsed(mwgpu_ctx *ctx, int slot0, int slot1, double *ms);
+/* Number of kernels this context has launched so far. */
+mwgpu_status mwgpu_launch_count(const mwgpu_ctx *ctx, unsigned long long *count);
+/* Writes `bytes` of device scratch on the context stream (evicts L2 between
+ * timed repetitions). */
+mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,9 @@ typedef struct {
     double contract_ms;            /* device time of the contraction kernels */
     double transform_ms;           /* wall time of the TopDown + BottomUp transforms */
     double wall_ms;                /* wall time of the whole apply */
+    unsigned long long launches;   /* kernels launched by this apply */
+    unsigned long long h2d_bytes;  /* host-to-device bytes copied by this apply */
+    unsigned long long d2h_bytes;  /* device-to-host bytes copied by this apply */
 } mwh_apply_stats;
 
 const char *mwh_last_error(void);

@@ -63,7 +63,8 @@ class MwgpuLevelStats(C.Structure):
 class MwhApplyStats(C.Structure):
     _fields_ = [("node_terms", C.c_ulonglong), ("components", C.c_ulonglong), ("band_nodes", C.c_ulonglong),
                 ("gen_nodes", C.c_ulonglong), ("iterations", C.c_int), ("out_nodes", C.c_int), ("device_ms", C.c_double),
-                ("contract_ms", C.c_double), ("transform_ms", C.c_double), ("wall_ms", C.c_double)]
+                ("contract_ms", C.c_double), ("transform_ms", C.c_double), ("wall_ms", C.c_double),
+                ("launches", C.c_ulonglong), ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -90,6 +91,11 @@ _SIGS = {
     "mwgpu_transform": (C.c_int, [_P, _P, C.c_int, C.c_int]),
     "mwgpu_download_tree": (C.c_int, [_P, _P, _PD, _PD]),
     "mwgpu_sync": (C.c_int, [_P]),
+    "mwgpu_tree_clear_generated": (C.c_int, [_P, _P]),
+    "mwgpu_timer_mark": (C.c_int, [_P, C.c_int]),
+    "mwgpu_timer_elapsed": (C.c_int, [_P, C.c_int, C.c_int, _PD]),
+    "mwgpu_launch_count": (C.c_int, [_P, C.POINTER(C.c_ulonglong)]),
+    "mwgpu_scrub_l2": (C.c_int, [_P, C.c_size_t]),
     # host mirror (include/mwhost.h)
     "mwh_last_error": (C.c_char_p, []),
     "mwh_set_table_path": (C.c_int, [C.c_char_p]),

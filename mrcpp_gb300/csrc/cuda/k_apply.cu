@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
     int depth;
     Box b;
     unsigned long long nband = 0;
-    if (band_box(m, op, gx, depth, b)) {
+    if (band_box(m, op, gx, depth, b) && depth < kMaxDepthRows) {
         const int T = op.n_terms;
         for (int q = 0; q < b.total; q++) {
             int fx, fy, fz;
@@ -227,14 +227,6 @@ void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, 
     size_t smem = sizeof(double) * 14 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err);
-}
-
-void launch_contract_mixed(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
-                           double gthr, LevelStats *stats, int *err, cudaStream_t s) {
-    if (n_work <= 0) return;
-    size_t smem = sizeof(double) * 8 * m.kp1_d + sizeof(float) * 6 * m.kp1_d;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_contract<float><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err);
 }
 
 }  // namespace mwgpu

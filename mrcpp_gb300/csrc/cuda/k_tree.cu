@@ -10,6 +10,8 @@
 //   BottomUp        MWTree::mwTransformUp -> FunctionNode<3>::reCompress -> mw_transform_back
 //                   (MWTree.cpp:166-181, FunctionNode.cpp:391-409, tree_utils.cpp:229-301)
 // The 1D step everywhere is math_utils::apply_filter: out(K^2 x K) = in^T (K^2 x K) * F.
+#include <algorithm>
+
 #include "mwgpu_internal.cuh"
 
 namespace mwgpu {
@@ -140,7 +142,11 @@ __global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pe
         return;
     }
     double *out = f.gcoefs + (size_t)slot * K3;
-    for (int e = tid; e < K3; e += nthr) out[e] = src[e];
+    float *out32 = f.gcoefs32 + (size_t)slot * K3;
+    for (int e = tid; e < K3; e += nthr) {
+        out[e] = src[e];
+        out32[e] = (float)src[e];
+    }
     // scaling norm (GenNode wavelet norms are zero)
     __shared__ double red[32];
     double s = 0.0;
@@ -259,7 +265,17 @@ __global__ void k_mw_up(DevMRA m, DevTree t, const int *parents, int n) {
     block_norms(pc, K3, t.norms + (size_t)p * 8, tid, nthr);
 }
 
+__global__ void k_to_float(const double *src, float *dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = (float)src[i];
+}
+
 }  // namespace
+
+void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s) {
+    if (n == 0) return;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    k_to_float<<<blocks, 256, 0, s>>>(src, dst, n);
+}
 
 void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *err, cudaStream_t s) {
     if (count <= 0) return;

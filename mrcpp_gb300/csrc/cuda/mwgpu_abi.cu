@@ -39,6 +39,10 @@ struct mwgpu_ctx {
     int *d_pcount = nullptr;
     int *d_list = nullptr;  // parent lists for transforms
     int list_cap = 0;
+    cudaEvent_t marks[16] = {};
+    unsigned long long launches = 0;
+    void *d_scrub = nullptr;
+    size_t scrub_bytes = 0;
 };
 
 struct mwgpu_oper {
@@ -128,7 +132,9 @@ mwgpu_status rebuild_hash(mwgpu_ctx *ctx, mwgpu_tree *tr, long long entries) {
     MW_CK(cudaMemsetAsync(t.hkeys, 0xFF, sizeof(uint64_t) * hcap, ctx->stream));
     MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     launch_hash_build(tr->mra, t, 0, t.n_real, ctx->d_err, ctx->stream);
+    ctx->launches += t.n_real > 0;
     if (t.n_gen > 0) launch_hash_build(tr->mra, t, t.cap_real, t.n_gen, ctx->d_err, ctx->stream);
+    ctx->launches += t.n_gen > 0;
     int herr = 0;
     MW_CK(cudaMemcpyAsync(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MW_CK(cudaStreamSynchronize(ctx->stream));
@@ -181,19 +187,26 @@ mwgpu_status grow_gen(mwgpu_ctx *ctx, mwgpu_tree *tr, int need) {
     int tot = t.cap_real + cap;
     int4 *idx;
     double *g, *norms;
+    float *g32;
     if (auto s = dev_alloc(ctx, &idx, tot)) return s;
     if (auto s = dev_alloc(ctx, &norms, (size_t)tot * 8)) return s;
     if (auto s = dev_alloc(ctx, &g, (size_t)cap * K3)) return s;
+    if (auto s = dev_alloc(ctx, &g32, (size_t)cap * K3)) return s;
     MW_CK(cudaMemcpyAsync(idx, t.idx, sizeof(int4) * (t.cap_real + t.n_gen), cudaMemcpyDeviceToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(norms, t.norms, sizeof(double) * 8 * (t.cap_real + t.n_gen), cudaMemcpyDeviceToDevice, ctx->stream));
-    if (t.n_gen > 0) MW_CK(cudaMemcpyAsync(g, t.gcoefs, sizeof(double) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (t.n_gen > 0) {
+        MW_CK(cudaMemcpyAsync(g, t.gcoefs, sizeof(double) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(g32, t.gcoefs32, sizeof(float) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     MW_CK(cudaStreamSynchronize(ctx->stream));
     cudaFree(t.idx);
     cudaFree(t.norms);
     if (t.gcoefs) cudaFree(t.gcoefs);
+    if (t.gcoefs32) cudaFree(t.gcoefs32);
     t.idx = idx;
     t.norms = norms;
     t.gcoefs = g;
+    t.gcoefs32 = g32;
     t.cap_gen = cap;
     return MWGPU_OK;
 }
@@ -232,6 +245,8 @@ mwgpu_status check_err(mwgpu_ctx *ctx, const char *phase) {
     return MWGPU_OK;
 }
 
+void free_tree(mwgpu_tree *tr);
+
 mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *d, bool input, mwgpu_tree **out) {
     MW_ARG(out && d && d->n_nodes > 0 && d->idx && d->child0, "invalid tree descriptor");
     auto *tr = new mwgpu_tree();
@@ -258,6 +273,12 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     MW_CK(cudaMemcpyAsync(t.child0, d->child0, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
     if (d->coefs) MW_CK(cudaMemcpyAsync(t.coefs, d->coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
     else MW_CK(cudaMemsetAsync(t.coefs, 0, sizeof(double) * tot * nc, ctx->stream));
+    if (input) {
+        // FP32 copy read by the mixed form
+        if ((s = dev_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(tr); return s; }
+        launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
+        ctx->launches++;
+    }
     if (d->norms) {
         MW_CK(cudaMemcpyAsync(t.norms, d->norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
     } else if (d->coefs) {
@@ -266,6 +287,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
         if ((s = ensure_work(ctx, n))) { delete tr; return s; }
         MW_CK(cudaMemcpyAsync(ctx->d_work, all.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
         launch_node_norms(tr->mra, t, ctx->d_work, n, ctx->stream);
+        ctx->launches++;
     } else {
         MW_CK(cudaMemsetAsync(t.norms, 0, sizeof(double) * tot * 8, ctx->stream));
     }
@@ -282,6 +304,8 @@ void free_tree(mwgpu_tree *tr) {
     cudaFree(t.norms);
     cudaFree(t.child0);
     if (t.gcoefs) cudaFree(t.gcoefs);
+    if (t.coefs32) cudaFree(t.coefs32);
+    if (t.gcoefs32) cudaFree(t.gcoefs32);
     if (t.hkeys) cudaFree(t.hkeys);
     if (t.hvals) cudaFree(t.hvals);
     if (tr->d_filt) cudaFree(tr->d_filt);
@@ -329,6 +353,9 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
                     (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list})
         if (p) cudaFree(p);
+    for (auto &e : ctx->marks)
+        if (e) cudaEventDestroy(e);
+    if (ctx->d_scrub) cudaFree(ctx->d_scrub);
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev2);
@@ -430,10 +457,14 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     };
     int *p_td, *p_off, *p_L, *p_bw, *p_bsz, *p_bm, *p_ord;
     double *p_blk, *p_nrm;
+    std::vector<float> blk32(node * 4 * K2);
+    for (size_t q = 0; q < blk32.size(); q++) blk32[q] = (float)d->blocks[q];
+    float *p_blk32;
     mwgpu_status s;
     if ((s = up(&p_td, d->depth, T)) || (s = up(&p_off, dep_off.data(), dep_off.size())) || (s = up(&p_L, dep_L.data(), dep_L.size())) ||
         (s = up(&p_bw, bw.data(), bw.size())) || (s = up(&p_bsz, bsz.data(), bsz.size())) || (s = up(&p_bm, band_max.data(), band_max.size())) ||
-        (s = up(&p_ord, order.data(), order.size())) || (s = up(&p_blk, d->blocks, node * 4 * K2)) || (s = up(&p_nrm, d->norms, node * 4))) {
+        (s = up(&p_ord, order.data(), order.size())) || (s = up(&p_blk, d->blocks, node * 4 * K2)) || (s = up(&p_nrm, d->norms, node * 4)) ||
+        (s = up(&p_blk32, blk32.data(), blk32.size()))) {
         for (void *p : o->allocs) cudaFree(p);
         delete o;
         return s;
@@ -451,6 +482,7 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.band_max = p_bm;
     o->op.term_order = p_ord;
     o->op.n_band_max = maxDepth + 1;
+    o->op.blocks32 = p_blk32;
     *out = o;
     return MWGPU_OK;
 }
@@ -508,6 +540,7 @@ mwgpu_status mwgpu_tree_add_nodes(mwgpu_ctx *ctx, mwgpu_tree *tr, int n, const i
     if (n > 0) {
         MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
         launch_hash_build(tr->mra, t, old, n, ctx->d_err, ctx->stream);
+        ctx->launches++;
         return check_err(ctx, "tree_add_nodes");
     }
     return MWGPU_OK;
@@ -550,6 +583,7 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
         MW_CK(cudaMemsetAsync(ctx->d_pcount, 0, sizeof(int), ctx->stream));
         launch_band_missing(o->mra, o->op, inp->t, out->t, ctx->d_work, n, ctx->d_pkeys, ctx->d_pvals, ctx->phcap, ctx->d_plist,
                             ctx->d_pcount, ctx->pcap, ctx->d_err, ctx->stream);
+        ctx->launches++;
         int herr = 0;
         MW_CK(cudaMemcpyAsync(&pcount, ctx->d_pcount, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         MW_CK(cudaMemcpyAsync(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -568,15 +602,21 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
             if (auto s = rebuild_hash(ctx, inp, (long long)f.n_real + f.n_gen + pcount)) return s;
         launch_gen_nodes(inp->mra, f, ctx->d_plist, pcount, f.n_gen, ctx->d_err, ctx->stream);
         launch_gen_insert(inp->mra, f, ctx->d_plist, pcount, f.n_gen, ctx->d_err, ctx->stream);
+        ctx->launches += 2;
         f.n_gen += pcount;
     }
     double gthr = out_sqnorm;
     if (gthr > 0.0) gthr = prec * 1.0 * std::sqrt(gthr / (double)o->op.n_terms);
+    if (ctx->precision == MWGPU_PREC_MIXED && !mixed_supported(o->op.K)) {
+        ctx->err = "mixed form supports orders k = 1..11";
+        return MWGPU_ERR_BAD_ARG;
+    }
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (ctx->precision == MWGPU_PREC_MIXED)
         launch_contract_mixed(o->mra, o->op, inp->t, out->t, ctx->d_work, n, gthr, ctx->d_stats, ctx->d_err, ctx->stream);
     else
         launch_contract_fp64(o->mra, o->op, inp->t, out->t, ctx->d_work, n, gthr, ctx->d_stats, ctx->d_err, ctx->stream);
+    ctx->launches++;
     MW_CK(cudaGetLastError());
     MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
     LevelStats hs{};
@@ -630,9 +670,15 @@ mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tr, int direction, int 
     }
     MW_CK(cudaMemcpyAsync(ctx->d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, ctx->stream));
     if (direction == MWGPU_TOPDOWN) {
-        for (auto &r : ranges) launch_mw_down(tr->mra, tr->t, ctx->d_list + r.first, r.second, overwrite != 0, ctx->stream);
+        for (auto &r : ranges) {
+            launch_mw_down(tr->mra, tr->t, ctx->d_list + r.first, r.second, overwrite != 0, ctx->stream);
+            ctx->launches += r.second > 0;
+        }
     } else {
-        for (int l = (int)ranges.size() - 1; l >= 0; l--) launch_mw_up(tr->mra, tr->t, ctx->d_list + ranges[l].first, ranges[l].second, ctx->stream);
+        for (int l = (int)ranges.size() - 1; l >= 0; l--) {
+            launch_mw_up(tr->mra, tr->t, ctx->d_list + ranges[l].first, ranges[l].second, ctx->stream);
+            ctx->launches += ranges[l].second > 0;
+        }
     }
     MW_CK(cudaGetLastError());
     MW_CK(cudaStreamSynchronize(ctx->stream));
@@ -652,6 +698,53 @@ mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tr, double *c
 mwgpu_status mwgpu_sync(mwgpu_ctx *ctx) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     MW_CK(cudaStreamSynchronize(ctx->stream));
+    return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_tree_clear_generated(mwgpu_ctx *ctx, mwgpu_tree *tr) {
+    if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(tr->is_input, "only input trees hold GenNodes");
+    cudaSetDevice(ctx->device);
+    if (tr->t.n_gen == 0) return MWGPU_OK;
+    tr->t.n_gen = 0;
+    return rebuild_hash(ctx, tr, tr->t.n_real);
+}
+
+mwgpu_status mwgpu_timer_mark(mwgpu_ctx *ctx, int slot) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(slot >= 0 && slot < 16, "timer slot out of range");
+    cudaSetDevice(ctx->device);
+    if (!ctx->marks[slot]) MW_CK(cudaEventCreate(&ctx->marks[slot]));
+    MW_CK(cudaEventRecord(ctx->marks[slot], ctx->stream));
+    return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_timer_elapsed(mwgpu_ctx *ctx, int a, int b, double *ms) {
+    if (!ctx || !ms) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(a >= 0 && a < 16 && b >= 0 && b < 16 && ctx->marks[a] && ctx->marks[b], "timer slot not recorded");
+    MW_CK(cudaEventSynchronize(ctx->marks[b]));
+    float f = 0.f;
+    MW_CK(cudaEventElapsedTime(&f, ctx->marks[a], ctx->marks[b]));
+    *ms = f;
+    return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_launch_count(const mwgpu_ctx *ctx, unsigned long long *count) {
+    if (!ctx || !count) return MWGPU_ERR_BAD_ARG;
+    *count = ctx->launches;
+    return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    if (bytes > ctx->scrub_bytes) {
+        if (ctx->d_scrub) cudaFree(ctx->d_scrub);
+        ctx->d_scrub = nullptr;
+        MW_CK(cudaMalloc(&ctx->d_scrub, bytes));
+        ctx->scrub_bytes = bytes;
+    }
+    MW_CK(cudaMemsetAsync(ctx->d_scrub, (int)(ctx->launches & 0xff), bytes, ctx->stream));
     return MWGPU_OK;
 }
 

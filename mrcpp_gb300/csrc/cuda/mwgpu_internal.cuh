@@ -40,6 +40,7 @@ struct DevOper {
     const int *band_max;        // [max_rows]
     const int *term_order;      // [max_rows * T] terms sorted by descending bw max at depth
     int n_band_max;
+    const float *blocks32;      // FP32 copy of blocks (mixed form)
 };
 
 struct DevTree {
@@ -50,6 +51,8 @@ struct DevTree {
     double *gcoefs;              // [cap_gen * K^3]
     double *norms;               // [(cap_real + cap_gen) * 8]
     int *child0;                 // [cap_real] first child id or -1
+    float *coefs32;              // input trees: FP32 copy of coefs (mixed form)
+    float *gcoefs32;             // input trees: FP32 copy of gcoefs
     uint64_t *hkeys;             // [hcap]
     int *hvals;                  // [hcap]
     int hcap;                    // power of two
@@ -116,11 +119,13 @@ void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_p
 void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
                           double gthr, LevelStats *stats, int *err, cudaStream_t s);
+bool mixed_supported(int K);
 void launch_contract_mixed(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
                            double gthr, LevelStats *stats, int *err, cudaStream_t s);
 void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cudaStream_t s);
 void launch_mw_down(const DevMRA &m, DevTree t, const int *parents, int n, bool overwrite, cudaStream_t s);
 void launch_mw_up(const DevMRA &m, DevTree t, const int *parents, int n, cudaStream_t s);
+void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s);
 void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *err, cudaStream_t s);
 
 }  // namespace mwgpu

@@ -92,7 +92,8 @@ void export_tree(const Tree<3> &t, std::vector<int> &order, std::vector<int> &id
 mwgpu_ctx *gpu_ctx(int precision) {
     if (!g_ctx) {
         mwgpu_config cfg{};
-        cfg.device = 0;
+        const char *dev = std::getenv("MWGPU_DEVICE");
+        cfg.device = dev ? std::atoi(dev) : 0;
         cfg.precision = precision;
         if (int s = mwgpu_init(&g_ctx, &cfg)) throw Error(s, std::string("GPU initialisation failed: ") + mwgpu_last_error(nullptr));
     }
@@ -406,6 +407,10 @@ int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int 
             ck(st, "create output tree");
         }
         mwh_apply_stats acc{};
+        unsigned long long l0 = 0, l1 = 0;
+        mwgpu_launch_count(ctx, &l0);
+        acc.h2d_bytes = (unsigned long long)(coefs.size() + norms.size()) * 8 + (idx.size() + child0.size()) * 4 +
+                        (oidx.size() + oc0.size()) * 4;
         try {
             // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
             std::vector<int> work;
@@ -416,6 +421,8 @@ int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int 
                 nbuf.resize(w.size() * 8);
                 mwgpu_level_stats ls{};
                 ck(mwgpu_apply_level(ctx, dop, dinp, dout, w.data(), (int)w.size(), prec, t.squareNorm, nbuf.data(), &ls), "apply level");
+                acc.h2d_bytes += w.size() * 4;
+                acc.d2h_bytes += (unsigned long long)t.nodes.size() * 8 * 8;
                 for (size_t j = 0; j < w.size(); j++) {
                     double sq = 0.0;
                     for (int c = 0; c < 8; c++) {
@@ -451,6 +458,7 @@ int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int 
                     }
                 }
                 ck(mwgpu_tree_add_nodes(ctx, dout, n, nidx.data(), (int)pids.size(), pids.data(), pc0.data()), "add output nodes");
+                acc.h2d_bytes += (nidx.size() + pids.size() + pc0.size()) * 4 + t.nodes.size() * 4;
                 synced = t.nodes.size();
             };
             auto calc_sync = [&](Tree<3> &t, const std::vector<int> &w) {
@@ -464,6 +472,7 @@ int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int 
             ck(mwgpu_transform(ctx, dout, MWGPU_BOTTOMUP, 1), "BottomUp transform");
             std::vector<double> nn(out.nodes.size() * 8);
             ck(mwgpu_download_tree(ctx, dout, out.coefs.data(), nn.data()), "download output tree");
+            acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
             auto t2 = std::chrono::steady_clock::now();
             acc.transform_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
             for (size_t i = 0; i < out.nodes.size(); i++) {
@@ -481,6 +490,8 @@ int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int 
             mwgpu_free_tree(ctx, dinp);
             throw;
         }
+        mwgpu_launch_count(ctx, &l1);
+        acc.launches = l1 - l0;
         mwgpu_free_tree(ctx, dout);
         mwgpu_free_tree(ctx, dinp);
         acc.out_nodes = (int)out.nodes.size();

@@ -13,6 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+FAST_PATH = os.path.join(HERE, "_build", "liboracle_fast.so")
 
 _PI = C.POINTER(C.c_int)
 _PD = C.POINTER(C.c_double)
@@ -32,7 +33,7 @@ class OracleTree(C.Structure):
     _fields_ = [("n_nodes", C.c_int), ("idx", _PI), ("child0", _PI), ("coefs", _PD), ("norms", _PD)]
 
 
-_lib = None
+_libs = {}
 
 
 def build():
@@ -41,23 +42,27 @@ def build():
     return LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "oracle_apply.c")):
+def lib(fast=False):
+    """The checker library, or (fast=True) the same source built with
+    -ffast-math, used only to time the CPU baseline."""
+    path = FAST_PATH if fast else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(os.path.join(HERE, "oracle_apply.c")):
             build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         L.oracle_apply.restype = C.c_int
         L.oracle_apply.argtypes = [C.POINTER(OracleMra), C.POINTER(OracleOper), C.POINTER(OracleTree), C.POINTER(OracleTree), C.c_double,
                                    C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        L.oracle_apply_sampled.restype = C.c_int
+        L.oracle_apply_sampled.argtypes = L.oracle_apply.argtypes[:10] + [C.c_int, C.POINTER(C.c_void_p)]
         L.oracle_result_info.restype = C.c_int
         L.oracle_result_info.argtypes = [C.c_void_p, _PI, _PD, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), _PI]
         L.oracle_result_export.restype = C.c_int
         L.oracle_result_export.argtypes = [C.c_void_p, _PI, _PI, _PD, _PD]
         L.oracle_result_free.restype = None
         L.oracle_result_free.argtypes = [C.c_void_p]
-        _lib = L
-    return _lib
+        _libs[path] = L
+    return _libs[path]
 
 
 def _pi(a):
@@ -68,50 +73,65 @@ def _pd(a):
     return a.ctypes.data_as(_PD)
 
 
-def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, nthreads=0, count_terms=True):
+class Prepared:
+    """Marshalled inputs of one oracle apply; run() calls the C oracle only
+    (so a timing of run() covers the restated reference path alone)."""
+
+    def __init__(self, prec, out, oper, inp, max_iter=-1, abs_prec=False):
+        mra = inp.mra
+        self.mra = mra
+        self.prec, self.max_iter, self.abs_prec = float(prec), int(max_iter), int(bool(abs_prec))
+        d = mra.desc()
+        self.keep = []
+        m = OracleMra()
+        m.order, m.root_scale, m.max_scale, m.sf = d.order, d.root_scale, d.max_scale, d.sf
+        for i in range(3):
+            m.corner[i] = d.corner[i]
+            m.nbox[i] = d.nbox[i]
+        filt = np.ascontiguousarray(mra._filters)
+        self.keep.append(filt)
+        m.filters = _pd(filt)
+        ex = oper.export()
+        o = OracleOper()
+        o.n_terms, o.order, o.build_prec = oper.n_terms, mra.order, float(oper.prec)
+        self.keep.append(ex)
+        o.depth, o.max_transl = _pi(ex["depth"]), _pi(ex["max_transl"])
+        o.blocks, o.norms = _pd(ex["blocks"]), _pd(ex["norms"])
+        fi = inp.export()
+        self.keep.append(fi)
+        ft = OracleTree(len(fi["child0"]), _pi(fi["idx"]), _pi(fi["child0"]), _pd(fi["coefs"]), _pd(fi["norms"]))
+        go = out.export()
+        self.keep.append(go)
+        gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
+        self.m, self.o, self.ft, self.gt = m, o, ft, gt
+        self.out_sqnorm = float(out.square_norm)
+
+    def run(self, nthreads=0, count_terms=True, sample=1, export=True, fast=False):
+        L = lib(fast)
+        res = C.c_void_p()
+        rc = L.oracle_apply_sampled(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), self.out_sqnorm, self.prec,
+                                        self.max_iter, self.abs_prec, int(nthreads), int(bool(count_terms)), int(sample), C.byref(res))
+        if rc != 0:
+            raise RuntimeError("oracle_apply failed with code %d" % rc)
+        n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()
+        L.oracle_result_info(res, C.byref(n), C.byref(sq), C.byref(nt), C.byref(nc), C.byref(it))
+        out = {"square_norm": sq.value, "node_terms": nt.value, "components": nc.value, "iterations": it.value, "n_nodes": n.value}
+        if export:
+            K3 = self.mra.kp1 ** 3
+            out["idx"] = np.zeros((n.value, 4), dtype=np.int32)
+            out["child0"] = np.zeros(n.value, dtype=np.int32)
+            out["coefs"] = np.zeros((n.value, 8 * K3))
+            out["norms"] = np.zeros((n.value, 8))
+            L.oracle_result_export(res, _pi(out["idx"]), _pi(out["child0"]), _pd(out["coefs"]), _pd(out["norms"]))
+        L.oracle_result_free(res)
+        return out
+
+
+def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, nthreads=0, count_terms=True, sample=1):
     """Oracle apply.  `out` (FunctionTree) gives the starting topology and square
     norm; `oper` a mrcpp_gb300 ConvolutionOperator; `inp` the input FunctionTree.
     Returns a dict with the flat output tree and the counters."""
-    mra = inp.mra
-    d = mra.desc()
-    keep = []
-    m = OracleMra()
-    m.order, m.root_scale, m.max_scale, m.sf = d.order, d.root_scale, d.max_scale, d.sf
-    for i in range(3):
-        m.corner[i] = d.corner[i]
-        m.nbox[i] = d.nbox[i]
-    filt = np.ascontiguousarray(mra._filters)
-    keep.append(filt)
-    m.filters = _pd(filt)
-    ex = oper.export()
-    o = OracleOper()
-    o.n_terms, o.order, o.build_prec = oper.n_terms, mra.order, float(oper.prec)
-    for k in ("depth", "max_transl", "blocks", "norms"):
-        keep.append(ex[k])
-    o.depth, o.max_transl = _pi(ex["depth"]), _pi(ex["max_transl"])
-    o.blocks, o.norms = _pd(ex["blocks"]), _pd(ex["norms"])
-    fi = inp.export()
-    keep.append(fi)
-    ft = OracleTree(len(fi["child0"]), _pi(fi["idx"]), _pi(fi["child0"]), _pd(fi["coefs"]), _pd(fi["norms"]))
-    go = out.export()
-    keep.append(go)
-    gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
-    res = C.c_void_p()
-    rc = lib().oracle_apply(C.byref(m), C.byref(o), C.byref(ft), C.byref(gt), float(out.square_norm), float(prec), int(max_iter),
-                            int(bool(abs_prec)), int(nthreads), int(bool(count_terms)), C.byref(res))
-    if rc != 0:
-        raise RuntimeError("oracle_apply failed with code %d" % rc)
-    n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()
-    lib().oracle_result_info(res, C.byref(n), C.byref(sq), C.byref(nt), C.byref(nc), C.byref(it))
-    K3 = mra.kp1 ** 3
-    idx = np.zeros((n.value, 4), dtype=np.int32)
-    c0 = np.zeros(n.value, dtype=np.int32)
-    coefs = np.zeros((n.value, 8 * K3))
-    norms = np.zeros((n.value, 8))
-    lib().oracle_result_export(res, _pi(idx), _pi(c0), _pd(coefs), _pd(norms))
-    lib().oracle_result_free(res)
-    return {"idx": idx, "child0": c0, "coefs": coefs, "norms": norms, "square_norm": sq.value, "node_terms": nt.value,
-            "components": nc.value, "iterations": it.value}
+    return Prepared(prec, out, oper, inp, max_iter, abs_prec).run(nthreads, count_terms, sample)
 
 
 def to_tree(result, mra):

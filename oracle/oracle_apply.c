@@ -683,6 +683,14 @@ struct oracle_result {
 
 int oracle_apply(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm, double prec,
                  int max_iter, int abs_prec, int nthreads, int count_terms, oracle_result **res) {
+    return oracle_apply_sampled(m, od, inp, out0, out_sqnorm, prec, max_iter, abs_prec, nthreads, count_terms, 1, res);
+}
+
+/* sample > 1 computes only every sample-th node of each work list (a bounded
+ * timing sample for the CPU baseline; the tree is then incomplete). */
+int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
+                         double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, oracle_result **res) {
+    if (sample < 1) sample = 1;
     if (!m || !od || !inp || !out0 || !res) return 1;
     if (od->order != m->order) return 1;
     ooper o;
@@ -708,7 +716,7 @@ int oracle_apply(const oracle_mra *m, const oracle_oper *od, const oracle_tree *
     int iter = 0;
     while (nwork > 0) {
         /* GenNodes of the bands of this level (serially, before the parallel loop) */
-        for (size_t w = 0; w < nwork; w++) {
+        for (size_t w = 0; w < nwork; w += (size_t)sample) {
             okey gk = g->idx[work[w]];
             int s[3], e[3], fl[3];
             if (!band_box(&o, &f, gk, s, e)) continue;
@@ -726,7 +734,7 @@ int oracle_apply(const oracle_mra *m, const oracle_oper *od, const oracle_tree *
             double *scr = (double *)malloc(sizeof(double) * 2 * K3);
             ostats ls = {0, 0};
 #pragma omp for schedule(dynamic, 1)
-            for (long w = 0; w < (long)nwork; w++) {
+            for (long w = 0; w < (long)nwork; w += sample) {
                 calc_node(m, &o, &f, g, work[w], prec, gsq, scr, &ls);
                 if (count_terms) nts += count_node_terms(m, &o, &f, g, work[w], prec, gsq);
             }

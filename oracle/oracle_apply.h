@@ -43,6 +43,8 @@ typedef struct oracle_result oracle_result;
  * whose square norm is out_sqnorm (-1 for a fresh or copied grid). */
 int oracle_apply(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
                  double prec, int max_iter, int abs_prec, int nthreads, int count_terms, oracle_result **res);
+int oracle_apply_sampled(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
+                         double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, oracle_result **res);
 int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
                        unsigned long long *components, int *iterations);
 int oracle_result_export(const oracle_result *r, int *idx, int *child0, double *coefs, double *norms);

@@ -85,3 +85,30 @@ def test_mixed_precision_error(gpu):
     mx, l2 = rel_errors(gx["coefs"], ref["coefs"][perm])
     assert l2 <= MIXED_TOL, l2
     assert st["node_terms"] == ref["node_terms"]
+
+
+def test_mixed_adaptive_interpolating_k5(gpu):
+    mra = mw.MRA(box=(-20, 20), order=5, basis=mw.INTERPOLATING)
+    P = mw.PoissonOperator(mra, 1e-3)
+    f = project(mra, 1e-3, unit_gaussian(10.0, (0.1, 0.2, -0.3)))
+    st, gx, ref = run_pair(1e-3, mra, P, f, mw.FunctionTree(mra), mw.FunctionTree(mra), precision=mw.MIXED)
+    same, perm = match(gx, ref)
+    assert same, "mixed-form adaptive topology differs from the oracle"
+    mx, l2 = rel_errors(gx["coefs"], ref["coefs"][perm])
+    assert l2 <= MIXED_TOL, l2
+
+
+def test_mixed_k7_fixed_grid(gpu):
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, 1e-4)
+    f = project(mra, 1e-4, gaussian_sum(5, 3, (1.0, 30.0), (-3.0, 3.0)))
+    grid = mw.FunctionTree(mra)
+    mw.apply(1e-4, grid, P, f, precision=mw.FP64)
+    g1, g2 = mw.FunctionTree(mra), mw.FunctionTree(mra)
+    mw.copy_grid(g1, grid)
+    mw.copy_grid(g2, grid)
+    s1 = mw.apply(1e-4, g1, P, f, max_iter=0, precision=mw.MIXED)
+    s2 = mw.apply(1e-4, g2, P, f, max_iter=0, precision=mw.FP64)
+    a, b = g1.export()["coefs"], g2.export()["coefs"]
+    assert s1["node_terms"] == s2["node_terms"]
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= MIXED_TOL
