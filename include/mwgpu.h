@@ -182,6 +182,28 @@ mwgpu_status mwgpu_launch_count(const mwgpu_ctx *ctx, unsigned long long *count)
  * timed repetitions). */
 mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes);
 
+/* Allocation-free variant of mwgpu_apply_level.  No counterpart in the
+ * reference (MRCPP allocates on the host as it goes).  For callers that must
+ * not allocate device memory while a level runs -- code inside a framework
+ * whose caching allocator owns the device memory, or a latency-critical loop
+ * where cudaMalloc/cudaFree would synchronise the device.  Its work list,
+ * error flag, counters and norm staging live in a fixed 4.5 MiB device array
+ * that every GPU loading the library holds until exit; it calls no cudaMalloc,
+ * cudaFree or other allocating routine.
+ *   - n <= 65536 nodes, else MWGPU_ERR_BAD_ARG;
+ *   - it creates no GenNodes: every node of the operator bands must already be
+ *     in the input tree (run mwgpu_apply_level once on the same nodes first),
+ *     else MWGPU_ERR_BAD_ARG;
+ *   - the first call on a device looks up the array's device address; make
+ *     that first call before any stream capture;
+ *   - all calls share the one array: calls that overlap on the GPU (other host
+ *     threads, other contexts on the same device) race.  Each call clears the
+ *     counters and the error flag it uses before its kernels run.
+ * Same arguments and results as mwgpu_apply_level otherwise. */
+mwgpu_status mwgpu_apply_level_static(mwgpu_ctx *ctx, const mwgpu_oper *oper, const mwgpu_tree *inp, mwgpu_tree *out,
+                                      const int *node_ix, int n, double prec, double out_sqnorm, double *norms_out,
+                                      mwgpu_level_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -749,3 +750,125 @@ mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free level computation.
+//
+// For callers that must not allocate device memory while they run a level:
+// code inside a framework whose caching allocator owns the device memory (a
+// stray cudaMalloc outside it fragments the pool and can fail once the pool
+// has claimed the free memory), and latency-critical loops where cudaMalloc /
+// cudaFree would synchronise the device.  mwgpu_apply_level keeps its work
+// list, error flag and counters in context buffers that it grows with
+// cudaMalloc when a level is larger than any before; this variant keeps them
+// in one file-scope device array of fixed size instead.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kStaticMaxNodes = 65536;  // largest node list one call accepts
+constexpr int kStaticMaxDevices = 64;
+
+struct StaticScratch {
+    int work[kStaticMaxNodes];              // node indices of the level
+    double norms[(size_t)kStaticMaxNodes * 8];  // component norms staged for the host
+    LevelStats stats;                       // counters, zeroed by every call
+    int err;                                // device error flags, zeroed by every call
+};
+
+// 4.5 MiB per device, held from library load until process exit.  Host code
+// must not pass `g_static_scratch` itself to a kernel: on the host that name
+// is only a stand-in for the device symbol; its device address comes from
+// cudaGetSymbolAddress below.
+static __device__ __align__(256) StaticScratch g_static_scratch;
+
+std::mutex g_static_mu;
+StaticScratch *g_static_addr[kStaticMaxDevices] = {};
+
+__global__ void k_gather_norms(const double *norms, const int *work, int n, double *dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * 8) return;
+    dst[i] = norms[(size_t)work[i / 8] * 8 + (i % 8)];
+}
+
+}  // namespace
+
+extern "C" mwgpu_status mwgpu_apply_level_static(mwgpu_ctx *ctx, const mwgpu_oper *o, const mwgpu_tree *inp, mwgpu_tree *out,
+                                                 const int *node_ix, int n, double prec, double out_sqnorm, double *norms_out,
+                                                 mwgpu_level_stats *stats) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(o && inp && out && inp->is_input && !out->is_input, "invalid operator or trees");
+    MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
+    MW_ARG(n <= kStaticMaxNodes, "mwgpu_apply_level_static accepts at most 65536 nodes per call");
+    MW_ARG(inp->mra.K == o->op.K && out->mra.K == o->op.K, "order mismatch");
+    MW_ARG(ctx->device >= 0 && ctx->device < kStaticMaxDevices, "device ordinal beyond the static scratch table");
+    if (ctx->precision == MWGPU_PREC_MIXED && !mixed_supported(o->op.K)) {
+        ctx->err = "mixed form supports orders k = 1..11";
+        return MWGPU_ERR_BAD_ARG;
+    }
+    for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < out->t.n_real, "node index out of range");
+    MW_CK(cudaSetDevice(ctx->device));
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return MWGPU_OK;
+    // once per device, with the device current: the device address of the array
+    StaticScratch *sc = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_static_mu);
+        if (!g_static_addr[ctx->device]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess || !p) {
+                ctx->err = std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e);
+                return MWGPU_ERR_DEVICE;
+            }
+            g_static_addr[ctx->device] = (StaticScratch *)p;
+        }
+        sc = g_static_addr[ctx->device];
+    }
+    MW_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    MW_CK(cudaMemcpyAsync(sc->work, node_ix, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemsetAsync(&sc->err, 0, sizeof(int), ctx->stream));
+    MW_CK(cudaMemsetAsync(&sc->stats, 0, sizeof(LevelStats), ctx->stream));
+    double gthr = out_sqnorm;
+    if (gthr > 0.0) gthr = prec * 1.0 * std::sqrt(gthr / (double)o->op.n_terms);
+    MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    // GenNodes are not made here: every band node must already be in the input
+    // tree's lookup table (a band node that is missing sets DE_LOOKUP)
+    if (ctx->precision == MWGPU_PREC_MIXED)
+        launch_contract_mixed(o->mra, o->op, inp->t, out->t, sc->work, n, gthr, &sc->stats, &sc->err, ctx->stream);
+    else
+        launch_contract_fp64(o->mra, o->op, inp->t, out->t, sc->work, n, gthr, &sc->stats, &sc->err, ctx->stream);
+    ctx->launches++;
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
+    if (norms_out) {
+        k_gather_norms<<<(n * 8 + 255) / 256, 256, 0, ctx->stream>>>(out->t.norms, sc->work, n, sc->norms);
+        ctx->launches++;
+        MW_CK(cudaGetLastError());
+        MW_CK(cudaMemcpyAsync(norms_out, sc->norms, sizeof(double) * 8 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    LevelStats hs{};
+    int herr = 0;
+    MW_CK(cudaMemcpyAsync(&hs, &sc->stats, sizeof(LevelStats), cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaMemcpyAsync(&herr, &sc->err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaStreamSynchronize(ctx->stream));
+    if (herr & DE_LOOKUP) {
+        ctx->err = "apply_level_static: a band node is missing from the input tree (run mwgpu_apply_level once on these nodes first)";
+        return MWGPU_ERR_BAD_ARG;
+    }
+    if (herr) {
+        ctx->err = "apply_level_static: device error flags " + std::to_string(herr);
+        return MWGPU_ERR_INTERNAL;
+    }
+    if (stats) {
+        stats->node_terms = hs.node_terms;
+        stats->components = hs.components;
+        stats->band_nodes = hs.band_nodes;
+        stats->gen_nodes = 0;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev2);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2);
+        stats->contract_ms = ms;
+    }
+    return MWGPU_OK;
+}
