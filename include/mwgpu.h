@@ -190,6 +190,7 @@ mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes);
  * error flag, counters and norm staging live in a fixed 4.5 MiB device array
  * that every GPU loading the library holds until exit; it calls no cudaMalloc,
  * cudaFree or other allocating routine.
+ *   - FP64 form only (the context precision must be MWGPU_PREC_FP64);
  *   - n <= 65536 nodes, else MWGPU_ERR_BAD_ARG;
  *   - it creates no GenNodes: every node of the operator bands must already be
  *     in the input tree (run mwgpu_apply_level once on the same nodes first),

@@ -1,19 +1,30 @@
-// Mixed-precision contraction (FP32 products, FP32 partial sums per band
-// cell group, FP64 accumulation of the partial sums).
+// Mixed-precision contraction over a work list (FP32 products and FP32 partial
+// sums, FP64 accumulation of the partial sums every 16 work items).
 //
-// Same screening and term/band selection as the FP64 kernel (k_apply.cu),
-// restating ConvolutionCalculator.cpp:224-382; only the arithmetic of the
-// component products changes.  One CTA per output node g, 256 threads.
+// One CTA (256 threads = 8 warps) per chunk of the work items of one output
+// node g (k_worklist.cu makes the items; the screening of
+// ConvolutionCalculator.cpp:224-329 is already in each item's (ft, gt)
+// mask).  Two schedules produce the same sum of component products as
+// tensorApplyOperComp (ConvolutionCalculator.cpp:333-382):
 //
-// Work of one (f, term) pair is done in two groups of four f components:
-//   stage 0  X0[ft][a0]     = O^x_{a0 b0}  applied along x to f_ft
-//   stage 1  X1[ft][a0 a1]  = O^y_{a1 b1}  applied along y to X0[ft][a0]
-//   stage 2  g[gt]         += O^z_{a2 b2}  applied along z to X1[ft][gt & 3]
-// where only the (ft, gt) pairs the screening keeps are formed.  Each 1D
-// application is MRCPP's out(K^2 x K) = in^T (K^2 x K) * O (K x K) step; the
-// intermediates live in shared memory with rows padded to an odd number of
-// 16-byte words (conflict-free float4 row loads), the g accumulators live in
-// registers: thread t owns coefficients t + 256 m of the output node.
+// * block schedule (the mask is the full structural set: every component the
+//   band and zero-norm rules allow): the three 1D applications are summed over
+//   the input bit of each direction,
+//     Y0[a0 b1 b2] = sum_b0 O^x_{a0 b0} f[b0 b1 b2]
+//     Y1[a0 a1 b2] = sum_b1 O^y_{a1 b1} Y0[a0 b1 b2]
+//     g [a0 a1 a2] += sum_b2 O^z_{a2 b2} Y1[a0 a1 b2]
+//   (48 K^4 FMA for a full node instead of 3 K^4 per component), with the
+//   s->s product that the reference leaves out at depth > 0 (ft = gt = 0,
+//   :261) carried in a separate channel U -> P and dropped at the end;
+// * component schedule (a partial mask, from the norm screening): per group of
+//   four f components the x and xy intermediates the kept (ft, gt) pairs need.
+//
+// Every step is one output block out(K^2 x K) = sum_p in_p^T (K^2 x K) O_p (K x K)
+// (MRCPP's 1D application).  A warp computes one output block: lane l owns the
+// rows c = l + 32 r, keeps a group of JG operator columns in registers and
+// reads its rows with vector loads.  Intermediates live in shared memory with
+// rows padded to an odd number of 16-byte words.  Warp w accumulates output
+// component gt = w of g in registers (lane l: rows l + 32 r, all K columns).
 #pragma once
 
 #include "mwgpu_internal.cuh"
@@ -32,209 +43,352 @@ struct Shape {
     static constexpr int K2 = K * K;
     static constexpr int K3 = K * K * K;
     static constexpr int P = padded_row(K);
-    static constexpr int BLK = P * K2;                  // one padded K^3 block
-    static constexpr int NOUT = (8 * K3 + 255) / 256;    // accumulators per thread
-    static constexpr int SMEM_FLOATS = 4 * 2 * BLK + 4 * 4 * BLK + 12 * K2;
+    static constexpr int BLK = P * K2;                   // one padded K^3 block
+    static constexpr int R = (K2 + 31) / 32;             // rows per lane
+    static constexpr int JG = K <= 8 ? (K % 4 == 0 ? 4 : (K % 2 == 0 ? K / 2 : K)) : 2;  // operator columns held in registers
+    static constexpr int NBUF = 24;                      // padded blocks in shared memory
+    static constexpr int SMEM_FLOATS = NBUF * BLK + 12 * K2 + 2 * 8 * K3;  // + FP64 accumulators
+    static constexpr int MIN_BLOCKS = K <= 8 ? 2 : 1;
 };
 
-// out (padded) = apply O along the row axis of `in` (row stride IS), for the
-// applies listed in `list` (count n, each entry: in block ptr, out block, O ptr).
+// one output block: out = sum_p O_p applied along the row axis of in_p
+struct StageOut {
+    float *out;
+    const float *in[4];
+    const float *o[4];
+    int np;
+};
+
+// loads K consecutive floats
 template <int K, int IS>
-__device__ __forceinline__ void apply_rows(float *__restrict__ out, const float *__restrict__ in, const float *__restrict__ O, int e) {
-    using S = Shape<K>;
-    // element e of the output block: c = e % K2 (row of in), j = e / K2
-    const int c = e % S::K2, j = e / S::K2;
-    const float *a = in + IS * c;
-    const float *b = O + K * j;
-    float s = 0.f;
+__device__ __forceinline__ void load_row(float (&a)[K], const float *base) {
+    if constexpr (K % 4 == 0 && IS % 4 == 0) {
 #pragma unroll
-    for (int i = 0; i < K; i++) s = fmaf(a[i], b[i], s);
-    // next layout: row (c_hi + K j), position c_lo, row stride P
-    const int c_lo = c % K, c_hi = c / K;
-    out[c_lo + S::P * (c_hi + K * j)] = s;
+        for (int i = 0; i < K; i += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(base + i);
+            a[i] = v.x;
+            a[i + 1] = v.y;
+            a[i + 2] = v.z;
+            a[i + 3] = v.w;
+        }
+    } else if constexpr (K % 2 == 0 && IS % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < K; i += 2) {
+            const float2 v = *reinterpret_cast<const float2 *>(base + i);
+            a[i] = v.x;
+            a[i + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < K; i++) a[i] = base[i];
+    }
 }
 
-template <int K>
-__global__ void __launch_bounds__(256) k_contract_mixed(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work,
-                                                        double gthr, LevelStats *stats, int *err) {
+// warp-level block step: s[r][j] = sum_p sum_i in_p[i + IS c_r] O_p[i + K j]
+template <int K, int IS>
+__device__ __forceinline__ void warp_block(const StageOut &x, int lane, float (&s)[Shape<K>::R][K]) {
     using S = Shape<K>;
-    constexpr int K2 = S::K2, K3 = S::K3, P = S::P, BLK = S::BLK, NOUT = S::NOUT;
-    extern __shared__ float smf[];
-    float *X0 = smf;                  // [4 ft][2 a0] padded blocks
-    float *X1 = X0 + 8 * BLK;         // [4 ft][4 (a0,a1)] padded blocks
-    float *OB = X1 + 16 * BLK;        // [3 dirs][4 comps] K*K
-    __shared__ int s_fid;
-    __shared__ double s_fn[8];
-    __shared__ unsigned s_mask[2];
-    __shared__ unsigned long long s_nt, s_nc;
-    const int tid = threadIdx.x;
-    const int gi = work[blockIdx.x];
-    const int4 gx = g.idx[gi];
-    float acc[NOUT];
-    double acc64[NOUT];
+    constexpr int R = S::R, JG = S::JG;
 #pragma unroll
-    for (int q = 0; q < NOUT; q++) { acc[q] = 0.f; acc64[q] = 0.0; }
-    if (tid == 0) { s_nt = 0; s_nc = 0; }
-    __syncthreads();
-    const int depth = gx.x - m.root_scale;
-    const int w = (depth >= 0 && depth < op.n_band_max) ? op.band_max[depth] : -1;
-    unsigned long long nband = 0;
-    if (w >= 0 && depth < kMaxDepthRows) {
-        int bs[3], be[3], tot = 1;
-        const int gl[3] = {gx.y, gx.z, gx.w};
-        for (int d = 0; d < 3; d++) {
-            int nboxes = m.nbox[d] * (1 << depth), c = m.corner[d] * (1 << depth);
-            bs[d] = max(gl[d] - w, c);
-            be[d] = min(gl[d] + w, c + nboxes - 1);
-            tot *= max(0, be[d] - bs[d] + 1);
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int j = 0; j < K; j++) s[r][j] = 0.f;
+    for (int p = 0; p < x.np; p++) {
+        const float *in = x.in[p];
+        const float *O = x.o[p];
+#pragma unroll
+        for (int j0 = 0; j0 < K; j0 += JG) {
+            float w[JG][K];
+#pragma unroll
+            for (int jj = 0; jj < JG; jj++) load_row<K, K>(w[jj], O + K * (j0 + jj));
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int c = lane + 32 * r;
+                if (c < S::K2) {
+                    float a[K];
+                    load_row<K, IS>(a, in + IS * c);
+#pragma unroll
+                    for (int jj = 0; jj < JG; jj++)
+#pragma unroll
+                        for (int i = 0; i < K; i++) s[r][j0 + jj] = fmaf(a[i], w[jj][i], s[r][j0 + jj]);
+                }
+            }
         }
-        const int nx = be[0] - bs[0] + 1, ny = be[1] - bs[1] + 1;
-        const int T = op.n_terms;
-        int since_flush = 0;
-        for (int q = 0; q < tot; q++) {
-            const int fx = bs[0] + q % nx, fy = bs[1] + (q / nx) % ny, fz = bs[2] + q / (nx * ny);
+    }
+}
+
+template <int K, int IS>
+__device__ __forceinline__ void run_stage(const StageOut *so, int nso, int warp, int lane) {
+    using S = Shape<K>;
+    for (int b = warp; b < nso; b += 8) {
+        float s[S::R][K];
+        warp_block<K, IS>(so[b], lane, s);
+        float *out = so[b].out;
+#pragma unroll
+        for (int r = 0; r < S::R; r++) {
+            const int c = lane + 32 * r;
+            if (c < S::K2)
+#pragma unroll
+                for (int j = 0; j < K; j++) out[(c % K) + S::P * (c / K + K * j)] = s[r][j];
+        }
+    }
+}
+
+// One CTA per chunk of the work items of one output node: chunk = (position of
+// g in the work list, first item, end item).  The FP64 partial sum of the chunk
+// goes to partial[blockIdx.x]; k_reduce_chunks adds the chunks of each g in
+// order (deterministic) and computes the node norms.
+template <int K>
+__global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work,
+                                                                              const int4 *chunks, const WorkItem *items, double *partial,
+                                                                              int *err) {
+    using S = Shape<K>;
+    constexpr int K2 = S::K2, K3 = S::K3, BLK = S::BLK, R = S::R;
+    extern __shared__ __align__(16) float smf[];
+    float *BUF = smf;                  // NBUF padded blocks
+    float *OB = BUF + S::NBUF * BLK;   // [3 dirs][4 comps] K*K, out-of-band blocks zero
+    double *G64 = (double *)(OB + 12 * K2);  // FP64 accumulators (thread-owned elements)
+    __shared__ StageOut s_so0[9], s_so1[17], s_g[8];
+    __shared__ int s_n0, s_n1;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int4 ch = chunks[blockIdx.x];
+    const int gi = work[ch.x];
+    const int depth = g.idx[gi].x - m.root_scale;
+    // warp `warp` owns component gt = warp of g: rows lane + 32 r, all columns
+    float acc[R][K];
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int j = 0; j < K; j++) acc[r][j] = 0.f;
+    for (int e = tid; e < 8 * K3; e += 256) G64[e] = 0.0;
+    const long long it0 = ch.y, it1 = ch.z;
+    int since = 0;
+    for (long long it = it0; it < it1; it++) {
+        const WorkItem item = items[it];
+        const int i = item.term;
+        const int *bwi = op.bw + ((size_t)i * op.max_rows + depth) * 5;
+        const int L0 = op.dep_L[i * op.max_rows + depth], off = op.dep_off[i * op.max_rows + depth];
+        for (int e = tid; e < 12 * K2; e += 256) {
+            const int d = e / (4 * K2), r = e % (4 * K2), c = r / K2;
+            const int l = item.tl[d];
+            float v = 0.f;
+            if (off >= 0 && abs(l) <= bwi[c] && abs(l) <= L0) v = op.blocks32[(size_t)(off + l + L0) * 4 * K2 + r];
+            OB[e] = v;
+        }
+        const bool gen = item.fid >= f.cap_real;
+        const float *fc = gen ? f.gcoefs32 + (size_t)(item.fid - f.cap_real) * K3 : f.coefs32 + (size_t)item.fid * 8 * K3;
+        const bool block = item.flags & 1;
+        const float *OX = OB, *OY = OB + 4 * K2, *OZ = OB + 8 * K2;
+        if (block) {
             if (tid == 0) {
-                uint64_t key;
-                int id = -1;
-                if (pack_key(m, gx.x, fx, fy, fz, key)) id = hash_find(f.hkeys, f.hvals, f.hcap, key);
-                if (id < 0) atomicOr(err, DE_LOOKUP);
-                s_fid = id;
-                if (id >= 0)
-                    for (int c = 0; c < 8; c++) s_fn[c] = f.norms[(size_t)id * 8 + c];
+                bool nz[8], ib[3][4];
+                for (int b = 0; b < 8; b++) nz[b] = ((item.mask >> (8 * b)) & 0xffull) != 0ull;
+                for (int d = 0; d < 3; d++)
+                    for (int c = 0; c < 4; c++) ib[d][c] = abs((int)item.tl[d]) <= bwi[c];
+                const bool pure = depth != 0 && nz[0];
+                float *Y0 = BUF, *U = BUF + 8 * BLK, *Y1 = BUF + 9 * BLK, *PP = BUF + 17 * BLK;
+                bool y0[9], y1[9];
+                int n0 = 0, n1 = 0;
+                for (int o = 0; o < 8; o++) {
+                    const int a0 = o & 1, b1 = (o >> 1) & 1, b2 = o >> 2;
+                    StageOut x;
+                    x.np = 0;
+                    x.out = Y0 + o * BLK;
+                    for (int b0 = 0; b0 < 2; b0++) {
+                        const int src = b0 + 2 * b1 + 4 * b2;
+                        if (!nz[src] || !ib[0][2 * a0 + b0]) continue;
+                        if (pure && src == 0 && a0 == 0) continue;  // the s->s path goes through U
+                        x.in[x.np] = fc + (size_t)src * K3;
+                        x.o[x.np] = OX + (2 * a0 + b0) * K2;
+                        x.np++;
+                    }
+                    y0[o] = x.np > 0;
+                    if (x.np) s_so0[n0++] = x;
+                }
+                y0[8] = pure && ib[0][0];
+                if (y0[8]) {
+                    StageOut x;
+                    x.out = U;
+                    x.in[0] = fc;
+                    x.o[0] = OX;
+                    x.np = 1;
+                    s_so0[n0++] = x;
+                }
+                for (int p = 0; p < 8; p++) {
+                    const int a0 = p & 1, a1 = (p >> 1) & 1, b2 = p >> 2;
+                    StageOut x;
+                    x.np = 0;
+                    x.out = Y1 + p * BLK;
+                    for (int b1 = 0; b1 < 2; b1++) {
+                        const int src = a0 + 2 * b1 + 4 * b2;
+                        if (!y0[src] || !ib[1][2 * a1 + b1]) continue;
+                        x.in[x.np] = Y0 + src * BLK;
+                        x.o[x.np] = OY + (2 * a1 + b1) * K2;
+                        x.np++;
+                    }
+                    if (y0[8] && p == 2 && ib[1][2]) {  // U -> (a0, a1, b2) = (0, 1, 0)
+                        x.in[x.np] = U;
+                        x.o[x.np] = OY + 2 * K2;
+                        x.np++;
+                    }
+                    y1[p] = x.np > 0;
+                    if (x.np) s_so1[n1++] = x;
+                }
+                y1[8] = y0[8] && ib[1][0];
+                if (y1[8]) {
+                    StageOut x;
+                    x.out = PP;
+                    x.in[0] = U;
+                    x.o[0] = OY;
+                    x.np = 1;
+                    s_so1[n1++] = x;
+                }
+                for (int gt = 0; gt < 8; gt++) {
+                    const int a2 = gt >> 2;
+                    StageOut x;
+                    x.np = 0;
+                    x.out = nullptr;
+                    for (int b2 = 0; b2 < 2; b2++) {
+                        const int src = (gt & 3) + 4 * b2;
+                        if (!y1[src] || !ib[2][2 * a2 + b2]) continue;
+                        x.in[x.np] = Y1 + src * BLK;
+                        x.o[x.np] = OZ + (2 * a2 + b2) * K2;
+                        x.np++;
+                    }
+                    if (y1[8] && gt == 4 && ib[2][2]) {  // P -> (0, 0, 1); P -> (0, 0, 0) is the dropped s->s product
+                        x.in[x.np] = PP;
+                        x.o[x.np] = OZ + 2 * K2;
+                        x.np++;
+                    }
+                    s_g[gt] = x;
+                }
+                s_n0 = n0;
+                s_n1 = n1;
             }
             __syncthreads();
-            const int fid = s_fid;
-            if (fid >= 0) {
-                nband++;
-                const int tl[3] = {fx - gx.y, fy - gx.z, fz - gx.w};
-                const int maxdl = max(abs(tl[0]), max(abs(tl[1]), abs(tl[2])));
-                const bool gen = fid >= f.cap_real;
-                const float *fc = gen ? f.gcoefs32 + (size_t)(fid - f.cap_real) * K3 : f.coefs32 + (size_t)fid * 8 * K3;
-                for (int ti = 0; ti < T; ti++) {
-                    const int i = op.term_order[depth * T + ti];
-                    const int *bwi = op.bw + ((size_t)i * op.max_rows + depth) * 5;
-                    if (maxdl > bwi[4]) break;
-                    if (tid < 64) {
-                        const int ft = tid >> 3, gt = tid & 7;
-                        bool pass = true;
-                        const double fNorm = s_fn[ft];
-                        if (fNorm < kMachineZero) pass = false;
-                        if (depth != 0 && ft == 0 && gt == 0) pass = false;
-                        double oNorm = 1.0;
-                        if (pass) {
-                            for (int d = 0; d < 3; d++) {
-                                const int a = (gt >> d) & 1, bb = (ft >> d) & 1, idx = 2 * a + bb;
-                                if (abs(tl[d]) > bwi[idx]) { pass = false; break; }
-                                const int node = op.dep_off[i * op.max_rows + depth] + tl[d] + op.dep_L[i * op.max_rows + depth];
-                                oNorm *= op.norms[(size_t)node * 4 + idx];
-                            }
+            run_stage<K, K>(s_so0, s_n0, warp, lane);
+            __syncthreads();
+            run_stage<K, S::P>(s_so1, s_n1, warp, lane);
+            __syncthreads();
+            float s[R][K];
+            warp_block<K, S::P>(s_g[warp], lane, s);
+#pragma unroll
+            for (int r = 0; r < R; r++)
+#pragma unroll
+                for (int j = 0; j < K; j++) acc[r][j] += s[r][j];
+        } else {
+            for (int grp = 0; grp < 2; grp++) {
+                const unsigned gmask = (unsigned)((item.mask >> (32 * grp)) & 0xffffffffull);
+                if (gmask == 0) continue;
+                if (tid == 0) {
+                    float *X0 = BUF, *X1 = BUF + 8 * BLK;
+                    int n0 = 0, n1 = 0;
+                    for (int lft = 0; lft < 4; lft++) {
+                        const int ft = 4 * grp + lft;
+                        const unsigned col = (gmask >> (8 * lft)) & 0xffu;
+                        for (int a0 = 0; a0 < 2; a0++) {
+                            if (!(col & (a0 ? 0xAAu : 0x55u))) continue;
+                            StageOut x;
+                            x.out = X0 + (lft * 2 + a0) * BLK;
+                            x.in[0] = fc + (size_t)ft * K3;
+                            x.o[0] = OX + (2 * a0 + (ft & 1)) * K2;
+                            x.np = 1;
+                            s_so0[n0++] = x;
                         }
-                        if (pass) {
-                            const double fThr = (double)op.band_size[((size_t)i * kMaxDepthRows + depth) * 64 + gt * 8 + ft] * fNorm;
-                            pass = oNorm * fThr > gthr;
-                        }
-                        unsigned bal = __ballot_sync(0xffffffffu, pass);
-                        if ((tid & 31) == 0) s_mask[tid >> 5] = bal;
-                    }
-                    // operator blocks of the three directions
-                    {
-                        const int L0 = op.dep_L[i * op.max_rows + depth], off = op.dep_off[i * op.max_rows + depth];
-                        for (int e = tid; e < 12 * K2; e += 256) {
-                            const int d = e / (4 * K2), r = e % (4 * K2);
-                            const int l = tl[d];
-                            float v = 0.f;
-                            if (off >= 0 && abs(l) <= L0) v = op.blocks32[(size_t)(off + l + L0) * 4 * K2 + r];
-                            OB[e] = v;
+                        for (int sidx = 0; sidx < 4; sidx++) {
+                            if (!(col & ((1u << sidx) | (1u << (sidx + 4))))) continue;
+                            StageOut x;
+                            x.out = X1 + (lft * 4 + sidx) * BLK;
+                            x.in[0] = X0 + (lft * 2 + (sidx & 1)) * BLK;
+                            x.o[0] = OY + (2 * (sidx >> 1) + ((ft >> 1) & 1)) * K2;
+                            x.np = 1;
+                            s_so1[n1++] = x;
                         }
                     }
-                    __syncthreads();
-                    const unsigned long long mask = (unsigned long long)s_mask[0] | ((unsigned long long)s_mask[1] << 32);
-                    if (mask != 0ull) {
-                        if (tid == 0) { s_nt++; s_nc += __popcll(mask); }
-                        for (int grp = 0; grp < 2; grp++) {
-                            const unsigned gmask = (unsigned)((mask >> (32 * grp)) & 0xffffffffull);
-                            if (gmask == 0) continue;
-                            // stage 0: X0[lft][a0] for needed (ft, a0)
-                            // needed bit sets per local ft
-                            for (int e = tid; e < 8 * K3; e += 256) {
-                                const int ap = e / K3, el = e % K3;
-                                const int lft = ap >> 1, a0 = ap & 1, ft = 4 * grp + lft;
-                                const unsigned col = (gmask >> (8 * lft)) & 0xffu;
-                                const unsigned need = (a0 ? 0xAAu : 0x55u);  // gt with gt&1 == a0
-                                if (!(col & need)) continue;
-                                apply_rows<K, K>(X0 + ap * BLK, fc + (size_t)ft * K3, OB + 0 * 4 * K2 + (2 * a0 + (ft & 1)) * K2, el);
-                            }
-                            __syncthreads();
-                            // stage 1: X1[lft][s], s = a0 + 2 a1
-                            for (int e = tid; e < 16 * K3; e += 256) {
-                                const int ap = e / K3, el = e % K3;
-                                const int lft = ap >> 2, s = ap & 3, ft = 4 * grp + lft;
-                                const unsigned col = (gmask >> (8 * lft)) & 0xffu;
-                                const unsigned need = (1u << s) | (1u << (s + 4));
-                                if (!(col & need)) continue;
-                                apply_rows<K, P>(X1 + ap * BLK, X0 + (lft * 2 + (s & 1)) * BLK, OB + 1 * 4 * K2 + (2 * (s >> 1) + ((ft >> 1) & 1)) * K2, el);
-                            }
-                            __syncthreads();
-                            // stage 2: thread-owned g coefficients e = tid + 256 q
-#pragma unroll
-                            for (int qq = 0; qq < NOUT; qq++) {
-                                const int e = tid + 256 * qq;
-                                if (e >= 8 * K3) break;
-                                const int gt = e / K3, el = e % K3;
-                                const int c = el % K2, j = el / K2;
-                                float s = 0.f;
-#pragma unroll
-                                for (int lft = 0; lft < 4; lft++) {
-                                    const int ft = 4 * grp + lft;
-                                    if (!((gmask >> (8 * lft + gt)) & 1u)) continue;
-                                    const float *a = X1 + (lft * 4 + (gt & 3)) * BLK + P * c;
-                                    const float *b = OB + 2 * 4 * K2 + (2 * (gt >> 2) + (ft >> 2)) * K2 + K * j;
-#pragma unroll
-                                    for (int ii = 0; ii < K; ii++) s = fmaf(a[ii], b[ii], s);
-                                }
-                                acc[qq] += s;
-                            }
-                            __syncthreads();
+                    for (int gt = 0; gt < 8; gt++) {
+                        StageOut x;
+                        x.np = 0;
+                        x.out = nullptr;
+                        for (int lft = 0; lft < 4; lft++) {
+                            const int ft = 4 * grp + lft;
+                            if (!((gmask >> (8 * lft + gt)) & 1u)) continue;
+                            x.in[x.np] = X1 + (lft * 4 + (gt & 3)) * BLK;
+                            x.o[x.np] = OZ + (2 * (gt >> 2) + (ft >> 2)) * K2;
+                            x.np++;
                         }
-                    } else {
-                        __syncthreads();
+                        s_g[gt] = x;
                     }
+                    s_n0 = n0;
+                    s_n1 = n1;
                 }
-                if (++since_flush >= 8) {
+                __syncthreads();
+                run_stage<K, K>(s_so0, s_n0, warp, lane);
+                __syncthreads();
+                run_stage<K, S::P>(s_so1, s_n1, warp, lane);
+                __syncthreads();
+                float s[R][K];
+                warp_block<K, S::P>(s_g[warp], lane, s);
 #pragma unroll
-                    for (int qq = 0; qq < NOUT; qq++) { acc64[qq] += (double)acc[qq]; acc[qq] = 0.f; }
-                    since_flush = 0;
-                }
+                for (int r = 0; r < R; r++)
+#pragma unroll
+                    for (int j = 0; j < K; j++) acc[r][j] += s[r][j];
+                __syncthreads();
             }
-            __syncthreads();  // s_fid / s_fn rewritten next cell
+        }
+        __syncthreads();  // OB, BUF and the stage lists are rewritten by the next item
+        if (++since >= 16) {
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const int c = lane + 32 * r;
+                if (c < K2)
+#pragma unroll
+                    for (int j = 0; j < K; j++) {
+                        G64[warp * K3 + c + K2 * j] += (double)acc[r][j];
+                        acc[r][j] = 0.f;
+                    }
+            }
+            since = 0;
         }
     }
-    double *go = g.coefs + (size_t)gi * 8 * K3;
+    double *go = partial + (size_t)blockIdx.x * 8 * K3;
 #pragma unroll
-    for (int qq = 0; qq < NOUT; qq++) {
-        const int e = tid + 256 * qq;
-        if (e >= 8 * K3) break;
-        go[e] = acc64[qq] + (double)acc[qq];
+    for (int r = 0; r < R; r++) {
+        const int c = lane + 32 * r;
+        if (c < K2)
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                const int e = warp * K3 + c + K2 * j;
+                go[e] = G64[e] + (double)acc[r][j];
+            }
     }
-    __syncthreads();
-    // node norms (MWNode::calcNorms) from the stored FP64 coefficients
+}
+
+// g coefficients = sum of the chunk partials of g in chunk order; node norms.
+__global__ void __launch_bounds__(256) k_reduce_chunks(DevTree g, const int *work, const int *chunk_begin, const double *partial, int nc) {
+    const int tid = threadIdx.x;
+    const int wi = blockIdx.x;
+    const int gi = work[wi];
+    const int c0 = chunk_begin[wi], c1 = chunk_begin[wi + 1];
+    double *go = g.coefs + (size_t)gi * nc;
+    const int K3 = nc / 8;
     __shared__ double red[8][8];
+    double part[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int e = tid; e < nc; e += 256) {
+        double v = 0.0;
+        for (int c = c0; c < c1; c++) v += partial[(size_t)c * nc + e];
+        go[e] = v;
+        part[e / K3] += v * v;
+    }
     for (int comp = 0; comp < 8; comp++) {
-        double s = 0.0;
-        for (int e = tid; e < K3; e += 256) { double v = go[comp * K3 + e]; s += v * v; }
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((tid & 31) == 0) red[comp][tid >> 5] = s;
+        double v = part[comp];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) red[comp][tid >> 5] = v;
     }
     __syncthreads();
     if (tid < 8) {
         double t = 0.0;
         for (int wv = 0; wv < 8; wv++) t += red[tid][wv];
         g.norms[(size_t)gi * 8 + tid] = sqrt(t);
-    }
-    if (tid == 0) {
-        atomicAdd(&stats->node_terms, s_nt);
-        atomicAdd(&stats->components, s_nc);
-        atomicAdd(&stats->band_nodes, nband);
     }
 }
 

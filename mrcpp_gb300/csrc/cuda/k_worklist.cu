@@ -1,0 +1,235 @@
+// Work-list builder: the band traversal and screening of ConvolutionCalculator
+// (src/treebuilders/ConvolutionCalculator.cpp:142-329) for a whole level at
+// once, one thread per (output node g, band cell f) pair.
+//
+// For every term whose band reaches f (applyOperComp :277-288) the thread forms
+// the 64-bit (ft, gt) component mask from the per-direction band check and the
+// norm test of applyOperator (:297-329), in FP64 and in the reference's
+// expression order; the band-size factor of :105-139 is rebuilt from the
+// direction-0 widths.  Triples with a non-empty mask become work items; their
+// number is the node-term count.
+//
+// COUNT writes the item count of every pair, an exclusive scan gives the write
+// positions, FILL writes the items.  Items are ordered by (g, cell, term), the
+// order of the reference's loops (cells x fastest, terms by descending width).
+#include "mwgpu_internal.cuh"
+
+namespace mwgpu {
+
+namespace {
+
+struct PairCtx {
+    int wi, fid, depth;
+    int tl[3];
+};
+
+// locate pair p: g position wi (binary search in pair_off), its band cell and f
+__device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work,
+                                   const long long *pair_off, int n_work, long long p, PairCtx &pc) {
+    int lo = 0, hi = n_work - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pair_off[mid] <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    const int wi = lo;
+    const int4 gx = g.idx[work[wi]];
+    const int depth = gx.x - m.root_scale;
+    const int w = op.band_max[depth];
+    const int gl[3] = {gx.y, gx.z, gx.w};
+    int bs[3], be[3];
+    for (int d = 0; d < 3; d++) {
+        int nboxes = m.nbox[d] * (1 << depth), c = m.corner[d] * (1 << depth);
+        bs[d] = max(gl[d] - w, c);
+        be[d] = min(gl[d] + w, c + nboxes - 1);
+    }
+    const long long q = p - pair_off[wi];
+    const int nx = be[0] - bs[0] + 1, ny = be[1] - bs[1] + 1;
+    const int fx = bs[0] + (int)(q % nx), fy = bs[1] + (int)((q / nx) % ny), fz = bs[2] + (int)(q / ((long long)nx * ny));
+    pc.wi = wi;
+    pc.depth = depth;
+    pc.tl[0] = fx - gl[0];
+    pc.tl[1] = fy - gl[1];
+    pc.tl[2] = fz - gl[2];
+    uint64_t key;
+    pc.fid = -1;
+    if (pack_key(m, gx.x, fx, fy, fz, key)) pc.fid = hash_find(f.hkeys, f.hvals, f.hcap, key);
+    return pc.fid >= 0;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, const long long *pair_off, int n_work,
+                                               long long n_pairs, double gthr, int *counts, const long long *item_off, WorkItem *items,
+                                               unsigned long long *ncomp, unsigned long long *nband, int *err) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int cnt = 0;
+    unsigned long long comp = 0, band = 0;
+    if (p < n_pairs) {
+        PairCtx pc;
+        if (!locate_pair(m, op, f, g, work, pair_off, n_work, p, pc)) {
+            atomicOr(err, DE_LOOKUP);
+        } else {
+            band = 1;
+            double fn[8];
+            bool any = false;
+            for (int c = 0; c < 8; c++) {
+                fn[c] = f.norms[(size_t)pc.fid * 8 + c];
+                any |= !(fn[c] < kMachineZero);
+            }
+            const int maxdl = max(abs(pc.tl[0]), max(abs(pc.tl[1]), abs(pc.tl[2])));
+            const int T = op.n_terms, depth = pc.depth;
+            long long wpos = FILL ? item_off[p] : 0;
+            for (int ti = 0; any && ti < T; ti++) {
+                const int i = op.term_order[depth * T + ti];
+                const int *bwi = op.bw + ((size_t)i * op.max_rows + depth) * 5;
+                if (maxdl > bwi[4]) break;
+                const int L0 = op.dep_L[i * op.max_rows + depth], off = op.dep_off[i * op.max_rows + depth];
+                int wd[4];
+                for (int c = 0; c < 4; c++) wd[c] = bwi[c];
+                bool inb[3][4];
+                double nrm[3][4];
+                for (int d = 0; d < 3; d++)
+                    for (int c = 0; c < 4; c++) {
+                        inb[d][c] = abs(pc.tl[d]) <= wd[c];
+                        nrm[d][c] = inb[d][c] ? op.norms[(size_t)(off + pc.tl[d] + L0) * 4 + c] : 0.0;
+                    }
+                // band-size factor 64 * prod_d (2 w(2 a_d + b_d) + 1) over directions with w >= 0
+                int fac[4];
+                for (int c = 0; c < 4; c++) fac[c] = wd[c] < 0 ? 1 : 2 * wd[c] + 1;
+                unsigned long long mask = 0, smask = 0;
+                for (int ft = 0; ft < 8; ft++) {
+                    const double fNorm = fn[ft];
+                    if (fNorm < kMachineZero) continue;
+                    for (int gt = 0; gt < 8; gt++) {
+                        if (depth != 0 && ft == 0 && gt == 0) continue;
+                        const int i0 = 2 * (gt & 1) + (ft & 1), i1 = 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1), i2 = 2 * (gt >> 2) + (ft >> 2);
+                        if (!(inb[0][i0] && inb[1][i1] && inb[2][i2])) continue;
+                        const unsigned long long bit = 1ull << (ft * 8 + gt);
+                        smask |= bit;
+                        double oNorm = 1.0;
+                        oNorm *= nrm[0][i0];
+                        oNorm *= nrm[1][i1];
+                        oNorm *= nrm[2][i2];
+                        const int bsz = fac[i0] * fac[i1] * fac[i2] * 64;
+                        const double fThr = (double)bsz * fNorm;
+                        if (oNorm * fThr > gthr) mask |= bit;
+                    }
+                }
+                if (mask == 0ull) continue;
+                if (FILL) {
+                    WorkItem it;
+                    it.mask = mask;
+                    it.fid = pc.fid;
+                    it.term = (short)i;
+                    it.tl[0] = (short)pc.tl[0];
+                    it.tl[1] = (short)pc.tl[1];
+                    it.tl[2] = (short)pc.tl[2];
+                    it.flags = (mask == smask) ? 1 : 0;
+                    it.pad = 0;
+                    items[wpos++] = it;
+                } else {
+                    comp += __popcll(mask);
+                }
+                cnt++;
+            }
+        }
+        if (!FILL) counts[p] = cnt;
+    }
+    if (!FILL) {
+        for (int o = 16; o > 0; o >>= 1) {
+            comp += __shfl_down_sync(0xffffffffu, comp, o);
+            band += __shfl_down_sync(0xffffffffu, band, o);
+        }
+        if ((threadIdx.x & 31) == 0 && (comp || band)) {
+            atomicAdd(ncomp, comp);
+            atomicAdd(nband, band);
+        }
+    }
+}
+
+// exclusive scan of int counts into long long offsets: per-block scan, scan of
+// the block sums (one block), add.
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_local(const int *in, long long *out, long long n, long long *block_sums) {
+    __shared__ long long s[kScanBlock];
+    const long long base = blockIdx.x * (long long)kScanBlock;
+    const int t = threadIdx.x;
+    long long v = (base + t < n) ? in[base + t] : 0;
+    s[t] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+        long long x = t >= o ? s[t - o] : 0;
+        __syncthreads();
+        s[t] += x;
+        __syncthreads();
+    }
+    if (base + t < n) out[base + t] = s[t] - v;
+    if (t == kScanBlock - 1) block_sums[blockIdx.x] = s[t];
+}
+
+__global__ void k_scan_sums(long long *block_sums, int nb, long long *total) {
+    __shared__ long long s[kScanBlock];
+    long long carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += kScanBlock) {
+        const int t = threadIdx.x;
+        long long v = (b0 + t < nb) ? block_sums[b0 + t] : 0;
+        s[t] = v;
+        __syncthreads();
+        for (int o = 1; o < kScanBlock; o <<= 1) {
+            long long x = t >= o ? s[t - o] : 0;
+            __syncthreads();
+            s[t] += x;
+            __syncthreads();
+        }
+        if (b0 + t < nb) block_sums[b0 + t] = carry + s[t] - v;
+        long long last = s[kScanBlock - 1];
+        __syncthreads();
+        carry += last;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(long long *out, long long n, const long long *block_sums, const long long *total) {
+    const long long i = blockIdx.x * (long long)kScanBlock + threadIdx.x;
+    if (i < n) out[i] += block_sums[blockIdx.x];
+    if (i == n) out[n] = *total;
+}
+
+// per-g item offsets: g_off[wi] = item_off[pair_off[wi]]
+__global__ void k_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off) {
+    const int wi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (wi <= n_work) g_off[wi] = item_off[pair_off[wi]];
+}
+
+}  // namespace
+
+void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
+                        int n_work, long long n_pairs, double gthr, int *counts, unsigned long long *ncomp, unsigned long long *nband, int *err,
+                        cudaStream_t s) {
+    if (n_pairs <= 0) return;
+    k_pairs<false><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, f, g, work, pair_off, n_work, n_pairs, gthr, counts, nullptr, nullptr,
+                                                                    ncomp, nband, err);
+}
+
+void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
+                       int n_work, long long n_pairs, double gthr, const long long *item_off, WorkItem *items, int *err, cudaStream_t s) {
+    if (n_pairs <= 0) return;
+    k_pairs<true><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, f, g, work, pair_off, n_work, n_pairs, gthr, nullptr, item_off, items,
+                                                                   nullptr, nullptr, err);
+}
+
+long long scan_blocks(long long n) { return (n + kScanBlock - 1) / kScanBlock; }
+
+void launch_scan(const int *in, long long *out, long long n, long long *block_sums, long long *total, cudaStream_t s) {
+    const long long nb = scan_blocks(n + 1);
+    k_scan_local<<<(unsigned)nb, kScanBlock, 0, s>>>(in, out, n, block_sums);
+    k_scan_sums<<<1, kScanBlock, 0, s>>>(block_sums, (int)nb, total);
+    k_scan_add<<<(unsigned)nb, kScanBlock, 0, s>>>(out, n, block_sums, total);
+}
+
+void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s) {
+    k_gather_goff<<<(n_work + 1 + 255) / 256, 256, 0, s>>>(item_off, pair_off, n_work, g_off);
+}
+
+}  // namespace mwgpu

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -41,6 +42,20 @@ struct mwgpu_ctx {
     int *d_list = nullptr;  // parent lists for transforms
     int list_cap = 0;
     cudaEvent_t marks[16] = {};
+    // work list of the mixed form
+    WorkItem *d_items = nullptr;
+    long long items_cap = 0;
+    long long *d_pair_off = nullptr, pair_off_cap = 0;
+    int *d_pcounts = nullptr;
+    long long pcounts_cap = 0;
+    long long *d_item_off = nullptr, item_off_cap = 0;
+    long long *d_scan = nullptr, scan_cap = 0;
+    long long *d_goff = nullptr, goff_cap = 0;
+    int4 *d_chunks = nullptr;
+    int *d_chunk_begin = nullptr;
+    int chunks_cap = 0;
+    double *d_partial = nullptr;
+    size_t partial_cap = 0;  // doubles
     unsigned long long launches = 0;
     void *d_scrub = nullptr;
     size_t scrub_bytes = 0;
@@ -248,6 +263,108 @@ mwgpu_status check_err(mwgpu_ctx *ctx, const char *phase) {
 
 void free_tree(mwgpu_tree *tr);
 
+// grows a device buffer of T to at least n elements (contents not kept)
+template <class T> mwgpu_status grow_buf(mwgpu_ctx *ctx, T **p, long long *cap, long long n) {
+    if (n <= *cap) return MWGPU_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = std::max(n, 2 * *cap);
+    return dev_alloc(ctx, p, (size_t)*cap);
+}
+
+// Mixed form: work list (pair counts, scan, fill) then the contraction over
+// chunks of items and the per-node reduction.  node_terms is returned in *hs.
+mwgpu_status run_mixed(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *d_work, const int *node_ix, int n,
+                       double gthr, LevelStats *hs) {
+    // (g, band cell) pairs: the band boxes of makeOperBand, clipped to the world
+    std::vector<long long> poff(n + 1, 0);
+    const DevMRA &m = o->mra;
+    for (int wi = 0; wi < n; wi++) {
+        const int4 gx = out->h_idx[node_ix[wi]];
+        const int depth = gx.x - m.root_scale;
+        long long cells = 0;
+        if (depth >= 0 && depth < o->op.n_band_max && depth < kMaxDepthRows && o->band_max[depth] >= 0) {
+            const int w = o->band_max[depth];
+            const int gl[3] = {gx.y, gx.z, gx.w};
+            cells = 1;
+            for (int d = 0; d < 3; d++) {
+                long long nboxes = (long long)m.nbox[d] << depth, c = (long long)m.corner[d] << depth;
+                long long s0 = std::max<long long>(gl[d] - w, c), e0 = std::min<long long>(gl[d] + w, c + nboxes - 1);
+                cells *= std::max<long long>(0, e0 - s0 + 1);
+            }
+        }
+        poff[wi + 1] = poff[wi] + cells;
+    }
+    const long long np = poff[n];
+    if (auto s = grow_buf(ctx, &ctx->d_pair_off, &ctx->pair_off_cap, n + 1)) return s;
+    if (auto s = grow_buf(ctx, &ctx->d_pcounts, &ctx->pcounts_cap, np + 1)) return s;
+    if (auto s = grow_buf(ctx, &ctx->d_item_off, &ctx->item_off_cap, np + 1)) return s;
+    if (auto s = grow_buf(ctx, &ctx->d_scan, &ctx->scan_cap, scan_blocks(np + 1) + 2)) return s;
+    if (auto s = grow_buf(ctx, &ctx->d_goff, &ctx->goff_cap, n + 1)) return s;
+    MW_CK(cudaMemcpyAsync(ctx->d_pair_off, poff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    LevelStats *dst = ctx->d_stats;
+    launch_pairs_count(m, o->op, inp->t, out->t, d_work, ctx->d_pair_off, n, np, gthr, ctx->d_pcounts, &dst->components, &dst->band_nodes,
+                       ctx->d_err, ctx->stream);
+    long long *d_total = ctx->d_scan + (ctx->scan_cap - 1);
+    launch_scan(ctx->d_pcounts, ctx->d_item_off, np, ctx->d_scan, d_total, ctx->stream);
+    launch_gather_goff(ctx->d_item_off, ctx->d_pair_off, n, ctx->d_goff, ctx->stream);
+    ctx->launches += 5;
+    std::vector<long long> offs(n + 1);
+    MW_CK(cudaMemcpyAsync(offs.data(), ctx->d_goff, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaStreamSynchronize(ctx->stream));
+    const long long total = offs[n];
+    if (total > 0x7fffffffLL) {
+        ctx->err = "work list of more than 2^31 items";
+        return MWGPU_ERR_BAD_ARG;
+    }
+    if (total > ctx->items_cap) {
+        if (ctx->d_items) cudaFree(ctx->d_items);
+        ctx->d_items = nullptr;
+        ctx->items_cap = std::max(total, 2 * ctx->items_cap);
+        if (auto s = dev_alloc(ctx, &ctx->d_items, (size_t)ctx->items_cap)) return s;
+    }
+    launch_pairs_fill(m, o->op, inp->t, out->t, d_work, ctx->d_pair_off, n, np, gthr, ctx->d_item_off, ctx->d_items, ctx->d_err, ctx->stream);
+    ctx->launches++;
+    // chunks of about the same number of items, several waves of CTAs
+    long long per = std::max<long long>(8, (total + 8 * 304 - 1) / (8 * 304));
+    if (const char *e = std::getenv("MWGPU_CHUNK_ITEMS")) per = std::max<long long>(1, std::atoll(e));
+    std::vector<int4> chunks;
+    std::vector<int> cbeg(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        cbeg[i] = (int)chunks.size();
+        long long b = offs[i], e = offs[i + 1];
+        if (b == e) chunks.push_back(make_int4(i, (int)b, (int)e, 0));
+        for (long long c = b; c < e; c += per) chunks.push_back(make_int4(i, (int)c, (int)std::min(e, c + per), 0));
+    }
+    cbeg[n] = (int)chunks.size();
+    const int nch = (int)chunks.size();
+    if (nch > ctx->chunks_cap || n + 1 > ctx->chunks_cap) {
+        if (ctx->d_chunks) cudaFree(ctx->d_chunks);
+        if (ctx->d_chunk_begin) cudaFree(ctx->d_chunk_begin);
+        ctx->d_chunks = nullptr;
+        ctx->d_chunk_begin = nullptr;
+        ctx->chunks_cap = std::max(std::max(nch, n + 1), 2 * ctx->chunks_cap);
+        if (auto s = dev_alloc(ctx, &ctx->d_chunks, ctx->chunks_cap)) return s;
+        if (auto s = dev_alloc(ctx, &ctx->d_chunk_begin, ctx->chunks_cap)) return s;
+    }
+    const size_t need = (size_t)nch * 8 * (size_t)o->mra.kp1_d;  // doubles
+    if (need > ctx->partial_cap) {
+        if (ctx->d_partial) cudaFree(ctx->d_partial);
+        ctx->d_partial = nullptr;
+        ctx->partial_cap = std::max(need, 2 * ctx->partial_cap);
+        if (auto s = dev_alloc(ctx, &ctx->d_partial, ctx->partial_cap)) return s;
+    }
+    MW_CK(cudaMemcpyAsync(ctx->d_chunks, chunks.data(), sizeof(int4) * nch, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_chunk_begin, cbeg.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    launch_contract_items(o->mra, o->op, inp->t, out->t, d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items, ctx->d_partial,
+                          ctx->d_err, ctx->stream);
+    ctx->launches += 3;
+    MW_CK(cudaStreamSynchronize(ctx->stream));  // host vectors above must outlive the copies
+    hs->node_terms = (unsigned long long)total;
+    return MWGPU_OK;
+}
+
 mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *d, bool input, mwgpu_tree **out) {
     MW_ARG(out && d && d->n_nodes > 0 && d->idx && d->child0, "invalid tree descriptor");
     auto *tr = new mwgpu_tree();
@@ -352,7 +469,9 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
-                    (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list})
+                    (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_chunks,
+                    (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
+                    (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff})
         if (p) cudaFree(p);
     for (auto &e : ctx->marks)
         if (e) cudaEventDestroy(e);
@@ -612,12 +731,14 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
         ctx->err = "mixed form supports orders k = 1..11";
         return MWGPU_ERR_BAD_ARG;
     }
-    MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    if (ctx->precision == MWGPU_PREC_MIXED)
-        launch_contract_mixed(o->mra, o->op, inp->t, out->t, ctx->d_work, n, gthr, ctx->d_stats, ctx->d_err, ctx->stream);
-    else
+    LevelStats mixed_nt{};
+    if (ctx->precision == MWGPU_PREC_MIXED) {
+        if (auto s = run_mixed(ctx, o, inp, out, ctx->d_work, node_ix, n, gthr, &mixed_nt)) return s;
+    } else {
+        MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
         launch_contract_fp64(o->mra, o->op, inp->t, out->t, ctx->d_work, n, gthr, ctx->d_stats, ctx->d_err, ctx->stream);
-    ctx->launches++;
+        ctx->launches++;
+    }
     MW_CK(cudaGetLastError());
     MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
     LevelStats hs{};
@@ -631,6 +752,7 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
     } else if (auto s = check_err(ctx, "apply_level")) {
         return s;
     }
+    if (ctx->precision == MWGPU_PREC_MIXED) hs.node_terms = mixed_nt.node_terms;
     if (stats) {
         stats->node_terms = hs.node_terms;
         stats->components = hs.components;
@@ -801,10 +923,7 @@ extern "C" mwgpu_status mwgpu_apply_level_static(mwgpu_ctx *ctx, const mwgpu_ope
     MW_ARG(n <= kStaticMaxNodes, "mwgpu_apply_level_static accepts at most 65536 nodes per call");
     MW_ARG(inp->mra.K == o->op.K && out->mra.K == o->op.K, "order mismatch");
     MW_ARG(ctx->device >= 0 && ctx->device < kStaticMaxDevices, "device ordinal beyond the static scratch table");
-    if (ctx->precision == MWGPU_PREC_MIXED && !mixed_supported(o->op.K)) {
-        ctx->err = "mixed form supports orders k = 1..11";
-        return MWGPU_ERR_BAD_ARG;
-    }
+    MW_ARG(ctx->precision == MWGPU_PREC_FP64, "mwgpu_apply_level_static computes the FP64 form only");
     for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < out->t.n_real, "node index out of range");
     MW_CK(cudaSetDevice(ctx->device));
     if (stats) std::memset(stats, 0, sizeof(*stats));
@@ -833,10 +952,7 @@ extern "C" mwgpu_status mwgpu_apply_level_static(mwgpu_ctx *ctx, const mwgpu_ope
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
     // GenNodes are not made here: every band node must already be in the input
     // tree's lookup table (a band node that is missing sets DE_LOOKUP)
-    if (ctx->precision == MWGPU_PREC_MIXED)
-        launch_contract_mixed(o->mra, o->op, inp->t, out->t, sc->work, n, gthr, &sc->stats, &sc->err, ctx->stream);
-    else
-        launch_contract_fp64(o->mra, o->op, inp->t, out->t, sc->work, n, gthr, &sc->stats, &sc->err, ctx->stream);
+    launch_contract_fp64(o->mra, o->op, inp->t, out->t, sc->work, n, gthr, &sc->stats, &sc->err, ctx->stream);
     ctx->launches++;
     MW_CK(cudaGetLastError());
     MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));

@@ -105,6 +105,19 @@ __device__ inline bool hash_insert(uint64_t *keys, int *vals, int hcap, uint64_t
 // error flags written by kernels (host reads them after each phase)
 enum DevError { DE_LOOKUP = 1, DE_HASH_FULL = 2, DE_POOL_FULL = 4, DE_RANGE = 8 };
 
+// One (output node, input node, term) triple with its contracted (ft, gt)
+// components: bit ft*8+gt of mask.  flags bit 0: the mask equals the
+// structural set (every component the band and zero-norm rules allow), so
+// the components may be summed blockwise.
+struct WorkItem {
+    unsigned long long mask;
+    int fid;
+    short term;
+    short tl[3];
+    short flags;
+    short pad;
+};
+
 struct LevelStats {
     unsigned long long node_terms;   // (g, f, term) triples with >= 1 contracted component
     unsigned long long components;   // contracted (g, f, term, ft, gt) components
@@ -120,8 +133,16 @@ void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
                           double gthr, LevelStats *stats, int *err, cudaStream_t s);
 bool mixed_supported(int K);
-void launch_contract_mixed(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
-                           double gthr, LevelStats *stats, int *err, cudaStream_t s);
+void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
+                        int n_work, long long n_pairs, double gthr, int *counts, unsigned long long *ncomp, unsigned long long *nband, int *err,
+                        cudaStream_t s);
+void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
+                       int n_work, long long n_pairs, double gthr, const long long *item_off, WorkItem *items, int *err, cudaStream_t s);
+long long scan_blocks(long long n);
+void launch_scan(const int *in, long long *out, long long n, long long *block_sums, long long *total, cudaStream_t s);
+void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s);
+void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work, const int4 *chunks,
+                           int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err, cudaStream_t s);
 void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cudaStream_t s);
 void launch_mw_down(const DevMRA &m, DevTree t, const int *parents, int n, bool overwrite, cudaStream_t s);
 void launch_mw_up(const DevMRA &m, DevTree t, const int *parents, int n, cudaStream_t s);

@@ -112,3 +112,22 @@ def test_mixed_k7_fixed_grid(gpu):
     a, b = g1.export()["coefs"], g2.export()["coefs"]
     assert s1["node_terms"] == s2["node_terms"]
     assert np.linalg.norm(a - b) / np.linalg.norm(b) <= MIXED_TOL
+
+
+def test_mixed_orders_in_sequence(gpu):
+    # one context serves levels of different orders one after the other; its
+    # work buffers must follow the larger coefficient blocks
+    for order in (4, 7, 5, 9):
+        mra = mw.MRA(box=(-20, 20), order=order, basis=mw.LEGENDRE)
+        P = mw.PoissonOperator(mra, 1e-3)
+        f = project(mra, 1e-3, gaussian_sum(order, 2, (2.0, 20.0), (-1.0, 1.0)))
+        g1, g2 = mw.FunctionTree(mra), mw.FunctionTree(mra)
+        s1 = mw.apply(1e-3, g1, P, f, precision=mw.FP64)
+        mw.copy_grid(g2, g1)
+        s2 = mw.apply(1e-3, g2, P, f, max_iter=0, precision=mw.MIXED)
+        g3 = mw.FunctionTree(mra)
+        mw.copy_grid(g3, g1)
+        mw.apply(1e-3, g3, P, f, max_iter=0, precision=mw.FP64)
+        a, b = g2.export()["coefs"], g3.export()["coefs"]
+        assert np.isfinite(a).all()
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) <= MIXED_TOL, order
