@@ -46,6 +46,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 METRIC = "Poisson apply node·terms/s on 1 GB300, mixed vs FP64 form at ≤1e-5 rel error"
 UNIT = "node-terms/s"
 ORDER, PREC, NGAUSS, SEED = 7, 1e-5, 16, 2026
+EXP_RANGE, CENTRE_RANGE, MU = (1.0, 100.0), (-5.0, 5.0), None
 WORKLOAD = "poisson-apply legendre k=7 box [-32,32]^3, 16 gaussians (exp 1..100, centres [-5,5]^3), prec 1e-5, fixed output grid (maxIter=0)"
 
 
@@ -57,11 +58,19 @@ def parse():
     p.add_argument("--impl", default="mw", choices=["mw", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true", help="6 Gaussians at 1e-4 (a short launch for ncu captures)")
+    p.add_argument("--workload", default="poisson", choices=["poisson", "helmholtz"],
+                   help="poisson: the FP64-GPU Poisson configuration (default); helmholtz: the mixed-precision Helmholtz "
+                        "configuration (mu=1, k=9, 32 Gaussians with exponents 0.5..500 in [-6,6]^3, prec 1e-6)")
     a = p.parse_args()
+    global PREC, NGAUSS, WORKLOAD, ORDER, EXP_RANGE, CENTRE_RANGE, MU, METRIC
+    if a.workload == "helmholtz":
+        ORDER, PREC, NGAUSS, EXP_RANGE, CENTRE_RANGE, MU = 9, 1e-6, 32, (0.5, 500.0), (-6.0, 6.0), 1.0
+        METRIC = "Helmholtz (mu=1) apply node·terms/s on 1 GB300, mixed vs FP64 form"
+        WORKLOAD = "helmholtz-apply mu=1 legendre k=9 box [-32,32]^3, 32 gaussians (exp 0.5..500, centres [-6,6]^3), prec 1e-6, fixed output grid (maxIter=0)"
     if a.small:
-        global PREC, NGAUSS, WORKLOAD
-        PREC, NGAUSS = 1e-4, 6
-        WORKLOAD = WORKLOAD.replace("16 gaussians", "6 gaussians").replace("prec 1e-5", "prec 1e-4")
+        PREC, NGAUSS = PREC * 10, 6
+        WORKLOAD = WORKLOAD.replace("16 gaussians", "6 gaussians").replace("32 gaussians", "6 gaussians").replace(
+            "prec 1e-5", "prec 1e-4").replace("prec 1e-6", "prec 1e-5")
     a.warm = max(a.warmup, 3)
     return a
 
@@ -109,9 +118,9 @@ def make_input():
     from cases import gaussian_sum
 
     mra = mw.MRA(box=(-32, 32), order=ORDER, basis=mw.LEGENDRE)
-    P = mw.PoissonOperator(mra, PREC)
+    P = mw.PoissonOperator(mra, PREC) if MU is None else mw.HelmholtzOperator(mra, MU, PREC)
     f = mw.FunctionTree(mra)
-    mw.project(PREC, f, gaussian_sum(SEED, NGAUSS, (1.0, 100.0), (-5.0, 5.0)))
+    mw.project(PREC, f, gaussian_sum(SEED, NGAUSS, EXP_RANGE, CENTRE_RANGE))
     return mra, P, f
 
 
@@ -318,6 +327,7 @@ def main():
     out_fp64 = np.zeros((n_out, 8 * K ** 3))
     ck(L.mwgpu_download_tree(ctx, dout, mw._pd(out_fp64), None))
     rel_l2 = float(np.linalg.norm(out_mixed - out_fp64) / np.linalg.norm(out_fp64))
+    node_err = float((np.linalg.norm(out_mixed - out_fp64, axis=1) / np.linalg.norm(out_fp64, axis=1).max()).max())
 
     node_terms = st_mixed.node_terms
     t_mixed = reduce_max(pg, statistics.mean(ms_mixed))
@@ -344,7 +354,7 @@ def main():
     # roofline of the contraction kernel (mixed form, last timed launch)
     bf16_peak, hbm_peak, peak_kind = load_peaks()
     achieved = node_terms * flop_per_nt / (st_mixed.contract_ms / 1e3) / 1e12
-    tr = load_traffic()
+    tr = load_traffic() if (args.workload == "poisson" and not args.small) else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
             "traffic": (tr or {}).get("dram_bytes_per_launch"), "peak_kind": peak_kind + " bf16 dense burst",
             "kernel": "k_contract<float> (mixed form)", "kernel_ms": st_mixed.contract_ms,
@@ -367,7 +377,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "ms_per_step": t_e2e * 1e3},
                 "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": t_fp64, "contract_ms": st_fp64.contract_ms},
-                "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error": rel_l2},
+                "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error": rel_l2, "max_node_error": node_err},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     barrier(pg)

@@ -131,3 +131,26 @@ def test_mixed_orders_in_sequence(gpu):
         a, b = g2.export()["coefs"], g3.export()["coefs"]
         assert np.isfinite(a).all()
         assert np.linalg.norm(a - b) / np.linalg.norm(b) <= MIXED_TOL, order
+
+
+def test_helmholtz_k9_mixed_vs_fp64_and_oracle(gpu):
+    # Helmholtz (mu = 1), Legendre k=9: the mixed form against the FP64 form
+    # (global and per-node error) and the FP64 form against the oracle
+    mra = mw.MRA(box=(-32, 32), order=9, basis=mw.LEGENDRE)
+    H = mw.HelmholtzOperator(mra, 1.0, 1e-4)
+    f = project(mra, 1e-4, gaussian_sum(31, 3, (0.5, 20.0), (-2.0, 2.0)))
+    g64 = mw.FunctionTree(mra)
+    st = mw.apply(1e-4, g64, H, f, precision=mw.FP64)
+    ref = oracle.apply(1e-4, mw.FunctionTree(mra), H, f)
+    check_fp64(st, g64.export(), ref)
+    gm = mw.FunctionTree(mra)
+    mw.copy_grid(gm, g64)
+    mw.apply(1e-4, gm, H, f, max_iter=0, precision=mw.MIXED)
+    g2 = mw.FunctionTree(mra)
+    mw.copy_grid(g2, g64)
+    mw.apply(1e-4, g2, H, f, max_iter=0, precision=mw.FP64)
+    a, b = gm.export(), g2.export()
+    assert np.linalg.norm(a["coefs"] - b["coefs"]) / np.linalg.norm(b["coefs"]) <= MIXED_TOL
+    # per node, relative to the largest node norm
+    per_node = np.linalg.norm(a["coefs"] - b["coefs"], axis=1) / np.linalg.norm(b["coefs"], axis=1).max()
+    assert per_node.max() <= MIXED_TOL
