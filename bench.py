@@ -58,15 +58,23 @@ def parse():
     p.add_argument("--impl", default="mw", choices=["mw", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true", help="6 Gaussians at 1e-4 (a short launch for ncu captures)")
-    p.add_argument("--workload", default="poisson", choices=["poisson", "helmholtz"],
+    p.add_argument("--workload", default="poisson", choices=["poisson", "helmholtz", "batch"],
                    help="poisson: the FP64-GPU Poisson configuration (default); helmholtz: the mixed-precision Helmholtz "
-                        "configuration (mu=1, k=9, 32 Gaussians with exponents 0.5..500 in [-6,6]^3, prec 1e-6)")
+                        "configuration (mu=1, k=9, 32 Gaussians with exponents 0.5..500 in [-6,6]^3, prec 1e-6); batch: 64 "
+                        "functions of 1..32 Gaussians (exponents 0.1..1000, centres [-8,8]^3), k=7, prec 1e-5, one planned "
+                        "level (CUDA graph, persistent contraction, autotuned chunks) against separate FP64 applies")
+    p.add_argument("--batch-n", type=int, default=64, help="functions in the batch workload")
+    p.add_argument("--fp64-sample", type=int, default=8, help="batch workload: separate FP64 applies timed (every n/s-th function)")
     a = p.parse_args()
     global PREC, NGAUSS, WORKLOAD, ORDER, EXP_RANGE, CENTRE_RANGE, MU, METRIC
     if a.workload == "helmholtz":
         ORDER, PREC, NGAUSS, EXP_RANGE, CENTRE_RANGE, MU = 9, 1e-6, 32, (0.5, 500.0), (-6.0, 6.0), 1.0
         METRIC = "Helmholtz (mu=1) apply node·terms/s on 1 GB300, mixed vs FP64 form"
         WORKLOAD = "helmholtz-apply mu=1 legendre k=9 box [-32,32]^3, 32 gaussians (exp 0.5..500, centres [-6,6]^3), prec 1e-6, fixed output grid (maxIter=0)"
+    if a.workload == "batch":
+        METRIC = "Batched Poisson apply node·terms/s on 1 GB300, mixed (one graph) vs separate FP64 applies"
+        WORKLOAD = ("batched poisson-apply legendre k=7 box [-32,32]^3, %d functions of 1..32 gaussians (exp 0.1..1000, centres "
+                    "[-8,8]^3), prec 1e-5, fixed output grids (maxIter=0)" % a.batch_n)
     if a.small:
         PREC, NGAUSS = PREC * 10, 6
         WORKLOAD = WORKLOAD.replace("16 gaussians", "6 gaussians").replace("32 gaussians", "6 gaussians").replace(
@@ -244,12 +252,187 @@ def load_traffic():
     return None
 
 
+def make_batch(n):
+    """n seeded functions, each a sum of 1..32 Gaussians (count uniform,
+    exponents log-uniform in [0.1, 1000], centres uniform in [-8, 8]^3,
+    coefficients uniform in [-1, 1]), projected at 1e-5 with k = 7."""
+    import mrcpp_gb300 as mw
+    from cases import gaussian_sum
+
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, PREC)
+    counts = np.random.default_rng(4044).integers(1, 33, n)
+    fs = []
+    for i in range(n):
+        f = mw.FunctionTree(mra)
+        mw.project(PREC, f, gaussian_sum(5000 + i, int(counts[i]), (0.1, 1000.0), (-8.0, 8.0)))
+        fs.append(f)
+    return mra, P, fs, counts
+
+
+def main_batch(args, rank, world, local, pg):
+    import ctypes as C
+
+    import mrcpp_gb300 as mw
+
+    t_setup = time.perf_counter()
+    mra, P, fs, counts = make_batch(args.batch_n)
+    nb = len(fs)
+    # fixed output grids: the adaptive applies (mixed batch; topology equals FP64's)
+    grids = [mw.FunctionTree(mra) for _ in fs]
+    mw.apply_batch(PREC, grids, P, fs, precision=mw.MIXED)
+    L = mw.lib()
+    ctx = C.c_void_p()
+    cfg = mw.MwgpuConfig()
+    cfg.device = local
+    cfg.precision = mw.MIXED
+    if L.mwgpu_init(C.byref(ctx), C.byref(cfg)) != 0:
+        raise SystemExit("mwgpu_init failed: %s" % L.mwgpu_last_error(None).decode())
+
+    def ck(rc):
+        if rc != 0:
+            raise SystemExit("mwgpu error %d: %s" % (rc, L.mwgpu_last_error(ctx).decode()))
+
+    dop = C.c_void_p()
+    ck(L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), PREC, C.byref(dop)))
+    keep, dins, douts, sizes = [], [], [], []
+    for f, g in zip(fs, grids):
+        fx = f.export()
+        fd = mw.MwgpuTreeDesc(len(fx["child0"]), mw._pi(fx["idx"]), mw._pi(fx["child0"]), mw._pd(fx["coefs"]), mw._pd(fx["norms"]))
+        t = C.c_void_p()
+        ck(L.mwgpu_upload_tree(ctx, C.byref(mra.desc()), C.byref(fd), C.byref(t)))
+        gx = g.export()
+        gd = mw.MwgpuTreeDesc(len(gx["child0"]), mw._pi(gx["idx"]), mw._pi(gx["child0"]), None, None)
+        o = C.c_void_p()
+        ck(L.mwgpu_create_tree(ctx, C.byref(mra.desc()), C.byref(gd), C.byref(o)))
+        keep.append((fx, gx))
+        dins.append(t)
+        douts.append(o)
+        sizes.append(len(gx["child0"]))
+    K = ORDER + 1
+    K8 = 8 * K ** 3
+    flop_per_nt = 96.0 * K ** 4
+    PA = C.c_void_p * nb
+    wt = np.concatenate([np.full(s, t, dtype=np.int32) for t, s in enumerate(sizes)])
+    wn = np.concatenate([np.arange(s, dtype=np.int32) for s in sizes])
+    sq = np.full(nb, -1.0)
+    plan = C.c_void_p()
+    t0 = time.perf_counter()
+    ck(L.mwgpu_plan_create(ctx, dop, nb, PA(*dins), PA(*douts), mw._pi(wt), mw._pi(wn), len(wt), PREC, mw._pd(sq), 3, C.byref(plan)))
+    t_plan = time.perf_counter() - t0
+    per, grid, ncand, lpe = C.c_longlong(), C.c_int(), C.c_int(8), C.c_ulonglong()
+    cand_items, cand_ms = (C.c_longlong * 8)(), (C.c_double * 8)()
+    ck(L.mwgpu_plan_info(plan, C.byref(per), C.byref(grid), C.byref(ncand), cand_items, cand_ms, C.byref(lpe)))
+    scrub = 256 << 20
+
+    def step():
+        ck(L.mwgpu_scrub_l2(ctx, scrub))
+        ck(L.mwgpu_timer_mark(ctx, 0))
+        ck(L.mwgpu_plan_execute(ctx, plan, None))
+        ck(L.mwgpu_timer_mark(ctx, 1))
+        ms = C.c_double()
+        ck(L.mwgpu_timer_elapsed(ctx, 0, 1, C.byref(ms)))
+        return ms.value
+
+    for _ in range(args.warm):
+        step()
+    st = mw.MwgpuLevelStats()
+    ck(L.mwgpu_plan_check(ctx, plan, C.byref(st)))
+    barrier(pg)
+    with ClockSampler(local) as cs:
+        ms = [step() for _ in range(args.steps)]
+    st = mw.MwgpuLevelStats()
+    ck(L.mwgpu_plan_check(ctx, plan, C.byref(st)))
+    barrier(pg)
+    clk = cs.summary()
+    node_terms = st.node_terms
+    t_step = reduce_max(pg, statistics.mean(ms))
+    value = reduce_sum(pg, node_terms) / (t_step / 1e3)
+    outs_mixed = []
+    # separate plain-form applies on a sample of the functions
+    sample = list(range(0, nb, max(1, nb // max(1, args.fp64_sample))))[:args.fp64_sample]
+    for t in sample:
+        c = np.zeros((sizes[t], K8))
+        ck(L.mwgpu_download_tree(ctx, douts[t], mw._pd(c), None))
+        outs_mixed.append(c)
+    ck(L.mwgpu_plan_destroy(ctx, plan))
+    ck(L.mwgpu_set_precision(ctx, mw.FP64))
+    fp_nt, fp_ms, errs = 0, 0.0, []
+    for j, t in enumerate([sample[0]] + sample):   # the first one is an untimed warm-up
+        work = np.arange(sizes[t], dtype=np.int32)
+        ck(L.mwgpu_tree_clear_generated(ctx, dins[t]))
+        ck(L.mwgpu_scrub_l2(ctx, scrub))
+        ck(L.mwgpu_timer_mark(ctx, 2))
+        s64 = mw.MwgpuLevelStats()
+        ck(L.mwgpu_apply_level(ctx, dop, dins[t], douts[t], mw._pi(work), sizes[t], PREC, -1.0, None, C.byref(s64)))
+        ck(L.mwgpu_transform(ctx, douts[t], 0, 0))
+        ck(L.mwgpu_transform(ctx, douts[t], 1, 1))
+        ck(L.mwgpu_timer_mark(ctx, 3))
+        m64 = C.c_double()
+        ck(L.mwgpu_timer_elapsed(ctx, 2, 3, C.byref(m64)))
+        if j == 0:
+            continue
+        fp_nt += s64.node_terms
+        fp_ms += m64.value
+        c = np.zeros((sizes[t], K8))
+        ck(L.mwgpu_download_tree(ctx, douts[t], mw._pd(c), None))
+        errs.append(float(np.linalg.norm(outs_mixed[j - 1] - c) / np.linalg.norm(c)))
+    value_fp64 = fp_nt / (fp_ms / 1e3)
+    # end to end through the public batched apply (host trees in and out)
+    e2e_times, h2d, d2h = [], 0, 0
+    for i in range(2):
+        gs = []
+        for g in grids:
+            x = mw.FunctionTree(mra)
+            mw.copy_grid(x, g)
+            gs.append(x)
+        barrier(pg)
+        t0 = time.perf_counter()
+        s = mw.apply_batch(PREC, gs, P, fs, max_iter=0, precision=mw.MIXED)
+        dt = time.perf_counter() - t0
+        if i >= 1:
+            e2e_times.append(dt)
+            h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+    t_e2e = reduce_max(pg, statistics.mean(e2e_times))
+    e2e_value = reduce_sum(pg, node_terms) / t_e2e
+    bf16_peak, hbm_peak, peak_kind = load_peaks()
+    achieved = node_terms * flop_per_nt / (st.contract_ms / 1e3) / 1e12
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": None,
+            "peak_kind": peak_kind + " bf16 dense burst", "kernel": "k_contract_items (persistent, all functions)",
+            "kernel_ms": st.contract_ms, "flop_per_node_term": flop_per_nt}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warm,
+                "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 products, f64 accumulation", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "functions": nb, "gaussians_per_function": [int(c) for c in counts],
+                           "out_nodes": int(sum(sizes)), "out_nodes_min_max": [int(min(sizes)), int(max(sizes))],
+                           "in_nodes_total": int(sum(len(k[0]["child0"]) for k in keep)),
+                           "node_terms_per_step": int(node_terms), "components_per_step": int(st.components),
+                           "l2": "256 MiB scrub between steps", "parallelism": "replicas" if world > 1 else "single",
+                           "plan": {"chunk_items": per.value, "persistent_grid": grid.value, "create_s": t_plan,
+                                    "autotune": [[int(cand_items[i]), float(cand_ms[i])] for i in range(ncand.value)],
+                                    "launches_per_step": int(lpe.value)},
+                           "setup_s": time.perf_counter() - t_setup},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                        "ms_per_step": t_e2e * 1e3},
+                "fp64_separate": {"value": value_fp64, "unit": UNIT, "functions_timed": sample, "node_terms": int(fp_nt),
+                                  "ms": fp_ms},
+                "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error_max": max(errs), "rel_l2_errors": errs},
+                "roofline": roof, "cpu_baseline": None, "clocks": clk, "gpu_launches": int(lpe.value) * args.steps}
+        print(json.dumps(line), flush=True)
+    barrier(pg)
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
         barrier(pg)
+        return
+    if args.workload == "batch":
+        os.environ["MWGPU_DEVICE"] = str(local)
+        main_batch(args, rank, world, local, pg)
         return
     os.environ["MWGPU_DEVICE"] = str(local)
     import ctypes as C

@@ -161,6 +161,66 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tre
  * MWTree.cpp:166-181). */
 mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tree, int direction, int overwrite);
 
+/* Batched level: one TreeBuilder iteration of n_trees independent applies of
+ * the same operator (the loop over functions that calls mrcpp::apply once per
+ * function, apply.cpp:68-93), computed by one work list and one contraction
+ * launch.  Entry i computes node node_ix[i] of outs[work_tree[i]] from
+ * inps[work_tree[i]] with the screening threshold of out_sqnorms[work_tree[i]];
+ * norms_out (n*8, may be NULL) is in entry order.  Input and output trees of a
+ * batch must be distinct.  Results equal n_trees calls of mwgpu_apply_level. */
+mwgpu_status mwgpu_apply_level_batch(mwgpu_ctx *ctx, const mwgpu_oper *oper, int n_trees, mwgpu_tree *const *inps, mwgpu_tree *const *outs,
+                                     const int *work_tree, const int *node_ix, int n, double prec, const double *out_sqnorms,
+                                     double *norms_out, mwgpu_level_stats *stats);
+/* mwgpu_transform of several distinct trees with the same MRA, one launch per
+ * depth for all of them. */
+mwgpu_status mwgpu_transform_batch(mwgpu_ctx *ctx, int n_trees, mwgpu_tree *const *trees, int direction, int overwrite);
+
+/* Level plans.  No counterpart in the reference (each mrcpp::apply rebuilds
+ * its bands, apply.cpp:68-93).  For levels whose node lists stay fixed: apply
+ * with maxIter = 0 onto given output grids (the fixed-grid apply of
+ * apply.cpp:68-93 with copy_grid), over one or many functions, possibly
+ * repeated as input values change (a fixed-grid SCF loop).
+ *
+ * mwgpu_plan_create computes the level once (same arguments and results as
+ * mwgpu_apply_level_batch, in the context precision) and keeps what depends
+ * only on the topology: the input trees' GenNode keys and slots (earlier
+ * GenNodes of the input trees are dropped first), the band pair offsets,
+ * buffer capacities (work list: 1.25x the planned size) and, with
+ * MWGPU_PLAN_AUTOTUNE, the chunk length of the persistent contraction launch,
+ * chosen by timing candidates on this level.  The level is then captured as
+ * one CUDA graph: GenNode values from the current input coefficients,
+ * screening and work list, contraction (one persistent launch for all trees),
+ * chunk reduction and norms, and with MWGPU_PLAN_TRANSFORMS the TopDown(add)
+ * and BottomUp transforms of all output trees (the node list must then hold
+ * every node of every output tree once).
+ *
+ * mwgpu_plan_execute replays the graph on the context stream.  With stats it
+ * waits and returns them (and the device status); without, it returns at once
+ * and mwgpu_plan_check later waits and reports.  While a plan exists its trees
+ * may not be changed structurally: level calls, mwgpu_tree_add_nodes,
+ * mwgpu_tree_clear_generated and mwgpu_free_tree on them return
+ * MWGPU_ERR_BAD_ARG.  New input coefficients for the same topology go in with
+ * mwgpu_tree_update_coefs.  If they change the screening so much that the work
+ * list outgrows its capacity, execute/check return MWGPU_ERR_OOM: create a new
+ * plan. */
+typedef struct mwgpu_plan mwgpu_plan;
+#define MWGPU_PLAN_TRANSFORMS 1
+#define MWGPU_PLAN_AUTOTUNE 2
+mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *oper, int n_trees, mwgpu_tree *const *inps, mwgpu_tree *const *outs,
+                               const int *work_tree, const int *node_ix, int n, double prec, const double *out_sqnorms, int flags,
+                               mwgpu_plan **plan);
+mwgpu_status mwgpu_plan_execute(mwgpu_ctx *ctx, mwgpu_plan *plan, mwgpu_level_stats *stats);
+mwgpu_status mwgpu_plan_check(mwgpu_ctx *ctx, mwgpu_plan *plan, mwgpu_level_stats *stats);
+/* Chunk length and persistent grid in use, the timed candidates (n_candidates:
+ * in = room in the arrays, out = number tried) and kernel launches per execution. */
+mwgpu_status mwgpu_plan_info(const mwgpu_plan *plan, long long *chunk_items, int *grid, int *n_candidates, long long *cand_items,
+                             double *cand_ms, unsigned long long *launches);
+mwgpu_status mwgpu_plan_destroy(mwgpu_ctx *ctx, mwgpu_plan *plan);
+/* New coefficients (and norms, or NULL to compute them) of all nodes of an
+ * input tree with unchanged topology; refreshes the FP32 copy.  GenNodes are
+ * recomputed by the next level call or plan execution. */
+mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tree, const double *coefs, const double *norms);
+
 /* Copies coefficients and/or norms of all real nodes back (either may be NULL). */
 mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tree, double *coefs, double *norms);
 
@@ -181,6 +241,62 @@ mwgpu_status mwgpu_launch_count(const mwgpu_ctx *ctx, unsigned long long *count)
 /* Writes `bytes` of device scratch on the context stream (evicts L2 between
  * timed repetitions). */
 mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes);
+
+/* Learned output grid.  No counterpart in the reference.  A 3-layer, 64-wide
+ * network (BF16 weights, FP32 arithmetic) that predicts for an output node of
+ * apply whether the wavelet-norm split test (tree_utils::split_check,
+ * tree_utils.cpp:47-65) will refine it; mwgpu_apply_judged runs the split test
+ * itself, so the prediction changes how many host round trips the apply
+ * needs, never its result.
+ * Parameters: MWGPU_MLP_PARAMS floats, W1[64][8], b1[64], W2[64][64], b2[64],
+ * W3[64], b3 (W[out][in], row-major).  Features: MWGPU_MLP_FEATURES floats per
+ * node (depth/16; log10 of the input norm at the node relative to f_norm /8;
+ * the same summed over the operator band box /8; operator terms reaching the
+ * depth /100; translation parities; 1 if the input has a node there). */
+typedef struct mwgpu_mlp mwgpu_mlp;
+#define MWGPU_MLP_FEATURES 8
+#define MWGPU_MLP_PARAMS 4801
+mwgpu_status mwgpu_mlp_create(mwgpu_ctx *ctx, const float *params, mwgpu_mlp **mlp);
+mwgpu_status mwgpu_mlp_destroy(mwgpu_ctx *ctx, mwgpu_mlp *mlp);
+/* FP32 master parameters and/or their BF16 copy (either may be NULL). */
+mwgpu_status mwgpu_mlp_get(mwgpu_ctx *ctx, const mwgpu_mlp *mlp, float *params, uint16_t *bf16);
+/* Features of n nodes (idx: n*4 ints) against input tree inp; x: n*8 floats. */
+mwgpu_status mwgpu_mlp_features(mwgpu_ctx *ctx, const mwgpu_oper *oper, const mwgpu_tree *inp, double f_norm, const int *idx, int n,
+                                float *x);
+/* P(split) of n feature rows. */
+mwgpu_status mwgpu_mlp_infer(mwgpu_ctx *ctx, const mwgpu_mlp *mlp, const float *x, int n, float *prob);
+/* Gradient (MWGPU_MLP_PARAMS floats) and value of the weighted binary cross
+ * entropy over n samples (labels 0/1, weight pos_weight for label 1). */
+mwgpu_status mwgpu_mlp_grad(mwgpu_ctx *ctx, const mwgpu_mlp *mlp, const float *x, const float *y, int n, float pos_weight, float *grad,
+                            float *loss);
+/* Adam training on the device: `epochs` passes over the n samples in seeded
+ * random order, mini-batches of `batch`; epoch_loss (may be NULL) gets the
+ * mean batch loss of every epoch. */
+mwgpu_status mwgpu_mlp_train(mwgpu_ctx *ctx, mwgpu_mlp *mlp, const float *x, const float *y, int n, int epochs, int batch, float lr,
+                             float pos_weight, unsigned seed, float *epoch_loss);
+
+/* Adaptive apply over a proposed output grid, judged on the device.  No
+ * counterpart in the reference; it runs the TreeBuilder loop of apply
+ * (TreeBuilder.cpp:38-87 with WaveletAdaptor, tree_utils.cpp:47-65) for all
+ * levels without returning to the host.  `out` holds the proposal: level 0 =
+ * the root nodes of a fresh output tree, every proposed split has its 8
+ * children (child0) in the next level, and the nodes are ordered by level,
+ * each level in the order of its parents (the order TreeBuilder creates
+ * nodes): nodes level_begin[j] .. level_begin[j+1]-1 form level j.
+ * Level j computes the nodes the split test kept (the roots, then the
+ * children of refined nodes) with the screening threshold of the tree norm of
+ * the levels before (out_sqnorm at the start), adds their norms to the tree
+ * norm in TreeBuilder's order and judges them with split_check (prec,
+ * abs_prec, splitFac 1).  flags_out[i]: bit 0 = node of the judged tree,
+ * bit 1 = refined.  first_miss = the first level where a refined node had no
+ * proposed children (-1: none); the result is then exact up to that level
+ * only.  With `transforms` and no miss, TopDown(add) and BottomUp run over the
+ * judged tree.  sq_levels (n_levels, may be NULL) gets the tree norm after
+ * each level.  Equal to mwgpu_apply_level driven by the host TreeBuilder on
+ * the judged tree whenever first_miss is -1. */
+mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, int n_levels,
+                                const int *level_begin, double prec, int abs_prec, double out_sqnorm, int transforms, int *flags_out,
+                                int *first_miss, double *sq_levels, mwgpu_level_stats *stats);
 
 /* Allocation-free variant of mwgpu_apply_level.  No counterpart in the
  * reference (MRCPP allocates on the host as it goes).  For callers that must

@@ -5,6 +5,7 @@
  * construction and mrcpp::apply.  Names and argument meaning follow the
  * reference API:
  *   mwh_apply          mrcpp::apply(prec, out, oper, inp, maxIter, absPrec)   src/treebuilders/apply.h:41
+ *   mwh_apply_batch    a loop of mrcpp::apply over functions, one device pass
  *   mwh_poisson        mrcpp::PoissonOperator(MRA, prec)                       src/operators/PoissonOperator.h:44
  *   mwh_helmholtz      mrcpp::HelmholtzOperator(MRA, mu, prec)                 src/operators/HelmholtzOperator.h:44
  *   mwh_project_gauss  mrcpp::build_grid + mrcpp::project                      src/treebuilders/grid.h, project.h
@@ -89,6 +90,35 @@ int mwh_helmholtz_kernel(double mu, double eps, double r_min, double r_max, int 
 
 /* mrcpp::apply on the GPU: precision = MWGPU_PREC_FP64 or MWGPU_PREC_MIXED. */
 int mwh_apply(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int max_iter, int abs_prec, int precision, mwh_apply_stats *stats);
+/* n independent applies of one operator, outs[t] = oper(inps[t]) (the loop over
+ * functions around mrcpp::apply, apply.h:41), advanced in lockstep: each
+ * TreeBuilder iteration of all trees is one mwgpu_apply_level_batch call and
+ * the transforms of all trees share their launches.  Every output equals the
+ * one mwh_apply gives for its pair.  Trees must be distinct; stats are summed. */
+int mwh_apply_batch(double prec, int n, mwh_tree **outs, mwh_oper *oper, mwh_tree **inps, int max_iter, int abs_prec, int precision,
+                    mwh_apply_stats *stats);
+
+/* Learned output grid (no reference counterpart): the network proposes the
+ * output grid level by level (features + inference on the GPU), then one
+ * mwgpu_apply_judged pass computes and judges it with the split test.  The
+ * result equals mwh_apply(prec, out, oper, inp, -1, abs_prec, precision):
+ * when the judge refines a node the proposal did not, the apply is redone
+ * the plain way (fallback = 1).  `out` must be a fresh tree (root nodes
+ * only), else the plain apply runs. */
+typedef struct mwh_mlp mwh_mlp;
+typedef struct {
+    mwh_apply_stats apply;   /* of the judged pass (or of the plain fallback) */
+    int proposal_nodes, proposal_levels, kept_nodes, first_miss, fallback, host_round_trips;
+    double predict_ms, judged_ms;
+} mwh_learned_stats;
+int mwh_mlp_create(const float *params, mwh_mlp **out);
+void mwh_mlp_free(mwh_mlp *mlp);
+int mwh_apply_learned(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, const mwh_mlp *mlp, double threshold, int abs_prec,
+                      int precision, mwh_learned_stats *stats);
+/* Training data: features (n*8) of every node of `grid` (e.g. the output of a
+ * plain apply of oper on inp, in node order) and labels (1 = the node has
+ * children).  n = number of nodes of grid. */
+int mwh_grid_features(double prec, mwh_tree *grid, mwh_oper *oper, mwh_tree *inp, float *x, float *y);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = [
     "MWGPUError", "lib", "MRA", "FunctionTree", "PoissonOperator", "HelmholtzOperator", "ConvolutionOperator",
-    "build_grid", "project", "apply", "copy_grid", "dot", "poisson_kernel", "helmholtz_kernel",
+    "build_grid", "project", "apply", "apply_batch", "copy_grid", "dot", "poisson_kernel", "helmholtz_kernel",
     "LEGENDRE", "INTERPOLATING", "FP64", "MIXED",
 ]
 
@@ -89,6 +89,16 @@ _SIGS = {
     "mwgpu_free_tree": (C.c_int, [_P, _P]),
     "mwgpu_apply_level": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_double, C.c_double, _PD, C.POINTER(MwgpuLevelStats)]),
     "mwgpu_transform": (C.c_int, [_P, _P, C.c_int, C.c_int]),
+    "mwgpu_apply_level_batch": (C.c_int, [_P, _P, C.c_int, C.POINTER(_P), C.POINTER(_P), _PI, _PI, C.c_int, C.c_double, _PD, _PD,
+                                          C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_transform_batch": (C.c_int, [_P, C.c_int, C.POINTER(_P), C.c_int, C.c_int]),
+    "mwgpu_plan_create": (C.c_int, [_P, _P, C.c_int, C.POINTER(_P), C.POINTER(_P), _PI, _PI, C.c_int, C.c_double, _PD, C.c_int,
+                                    C.POINTER(_P)]),
+    "mwgpu_plan_execute": (C.c_int, [_P, _P, C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_plan_check": (C.c_int, [_P, _P, C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_plan_info": (C.c_int, [_P, C.POINTER(C.c_longlong), _PI, _PI, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_ulonglong)]),
+    "mwgpu_plan_destroy": (C.c_int, [_P, _P]),
+    "mwgpu_tree_update_coefs": (C.c_int, [_P, _P, _PD, _PD]),
     "mwgpu_download_tree": (C.c_int, [_P, _P, _PD, _PD]),
     "mwgpu_sync": (C.c_int, [_P]),
     "mwgpu_tree_clear_generated": (C.c_int, [_P, _P]),
@@ -123,6 +133,8 @@ _SIGS = {
     "mwh_poisson_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
     "mwh_helmholtz_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
     "mwh_apply": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwh_apply_batch": (C.c_int, [C.c_double, C.c_int, C.POINTER(_P), _P, C.POINTER(_P), C.c_int, C.c_int, C.c_int,
+                                  C.POINTER(MwhApplyStats)]),
 }
 
 _lib = None
@@ -355,4 +367,20 @@ def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64):
     """mrcpp::apply(prec, out, oper, inp, maxIter, absPrec) on the GPU; returns the apply statistics."""
     st = MwhApplyStats()
     _ck(lib().mwh_apply(float(prec), out._h, oper._h, inp._h, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
+    return st.as_dict()
+
+
+def apply_batch(prec, outs, oper, inps, max_iter=-1, abs_prec=False, precision=FP64):
+    """outs[t] = oper(inps[t]) for every t: the loop of mrcpp::apply calls over a
+    set of functions, computed in lockstep so that every TreeBuilder iteration
+    of all functions is one device pass.  Each result equals apply() of its
+    pair.  Returns the summed statistics."""
+    outs, inps = list(outs), list(inps)
+    if len(outs) != len(inps) or not outs:
+        raise ValueError("apply_batch needs as many outputs as inputs")
+    n = len(outs)
+    po = (_P * n)(*[o._h for o in outs])
+    pi = (_P * n)(*[i._h for i in inps])
+    st = MwhApplyStats()
+    _ck(lib().mwh_apply_batch(float(prec), n, po, oper._h, pi, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
     return st.as_dict()

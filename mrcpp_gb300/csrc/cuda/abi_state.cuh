@@ -1,0 +1,115 @@
+// Host-side state behind the C-ABI handles (mwgpu_ctx, mwgpu_oper, mwgpu_tree)
+// shared by the translation units that implement include/mwgpu.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../../include/mwgpu.h"
+#include "mwgpu_internal.cuh"
+
+using mwgpu::DevMRA;
+using mwgpu::DevOper;
+using mwgpu::DevTree;
+using mwgpu::LevelStats;
+using mwgpu::WorkItem;
+
+struct mwgpu_ctx {
+    int device = 0;
+    int precision = MWGPU_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    std::string err;
+    int *d_err = nullptr;
+    LevelStats *d_stats = nullptr;
+    int *d_work = nullptr;
+    int *d_wtree = nullptr;  // tree of every work entry (batched levels)
+    int work_cap = 0;
+    // per-tree arrays of a batched level
+    DevTree *d_fs = nullptr, *d_gs = nullptr;
+    double *d_gthr = nullptr;
+    int trees_cap = 0;
+    double *d_nstage = nullptr;  // norms of the computed nodes, staged for the host
+    long long nstage_cap = 0;
+    // pending GenNode set
+    uint64_t *d_pkeys = nullptr;
+    int *d_pvals = nullptr;
+    int phcap = 0;
+    uint64_t *d_plist = nullptr;
+    int pcap = 0;
+    long long ph_total = 0, pl_total = 0;
+    int *d_pcount = nullptr;  // one pending count per tree
+    int pcount_cap = 0;
+    int *d_list = nullptr;  // parent lists for transforms
+    int *d_ltree = nullptr;  // tree of every parent (batched transforms)
+    int list_cap = 0;
+    cudaEvent_t marks[16] = {};
+    // work list of the mixed form
+    WorkItem *d_items = nullptr;
+    long long items_cap = 0;
+    long long *d_pair_off = nullptr, pair_off_cap = 0;
+    int *d_pcounts = nullptr;
+    long long pcounts_cap = 0;
+    long long *d_item_off = nullptr, item_off_cap = 0;
+    long long *d_scan = nullptr, scan_cap = 0;
+    long long *d_goff = nullptr, goff_cap = 0;
+    int4 *d_chunks = nullptr;
+    int *d_chunk_begin = nullptr;
+    int chunks_cap = 0;
+    double *d_partial = nullptr;
+    size_t partial_cap = 0;  // doubles
+    unsigned long long launches = 0;
+    void *d_arena = nullptr;  // scratch of the judged apply, carved per call
+    size_t arena_bytes = 0;
+    void *d_scrub = nullptr;
+    size_t scrub_bytes = 0;
+};
+
+struct mwgpu_oper {
+    DevMRA mra{};
+    double *d_filt = nullptr;
+    DevOper op{};
+    std::vector<void *> allocs;
+    int n_rows = 0;
+    std::vector<int> widths;    // [T * n_rows * 5]
+    std::vector<int> band_max;  // [n_rows]
+};
+
+struct mwgpu_tree {
+    DevMRA mra{};
+    double *d_filt = nullptr;
+    std::vector<double> h_filt;  // host copy of the filters (batch compatibility check)
+    int plans = 0;               // plans that hold this tree (its device arrays must not move)
+    DevTree t{};
+    std::vector<int4> h_idx;
+    std::vector<int> h_child0;
+    bool is_input = false;
+};
+
+#define MW_CK(call)                                                                                 \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                          \
+            return (e_ == cudaErrorMemoryAllocation) ? MWGPU_ERR_OOM : MWGPU_ERR_DEVICE;            \
+        }                                                                                           \
+    } while (0)
+
+#define MW_ARG(cond, msg)                     \
+    do {                                      \
+        if (!(cond)) {                        \
+            ctx->err = msg;                   \
+            return MWGPU_ERR_BAD_ARG;         \
+        }                                     \
+    } while (0)
+
+
+template <class T> inline mwgpu_status dev_alloc(mwgpu_ctx *ctx, T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    MW_CK(cudaMalloc((void **)p, sizeof(T) * n));
+    return MWGPU_OK;
+}
+

@@ -5,42 +5,75 @@ namespace mwgpu {
 
 namespace {
 template <int K>
-void launch_k(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, const int4 *chunks, int n_chunks,
-              const WorkItem *items, double *partial, int *err, cudaStream_t s) {
+void launch_k(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, const int4 *chunks,
+              int n_chunks, const WorkItem *items, double *partial, int *err, const int *n_chunks_dev, int *counter, cudaStream_t s) {
     size_t smem = sizeof(float) * mixed::Shape<K>::SMEM_FLOATS;
     auto kern = mixed::k_contract_items<K>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<n_chunks, 256, smem, s>>>(m, op, f, g, work, chunks, items, partial, err);
+    kern<<<n_chunks, 256, smem, s>>>(m, op, fs, gs, work_tree, work, chunks, items, partial, err, n_chunks_dev, counter);
+}
+
+template <int K>
+int resident_k() {
+    size_t smem = sizeof(float) * mixed::Shape<K>::SMEM_FLOATS;
+    auto kern = mixed::k_contract_items<K>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem) != cudaSuccess) return 0;
+    return nb;
 }
 }  // namespace
 
 bool mixed_supported(int K) { return K >= 2 && K <= 12; }
 
-void launch_items(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, const int4 *chunks, int n_chunks,
-                  const WorkItem *items, double *partial, int *err, cudaStream_t s);
 
-void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work, const int4 *chunks,
-                           int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err, cudaStream_t s) {
+void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                           int n_work, const int4 *chunks, int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err,
+                           cudaStream_t s) {
     if (n_work <= 0) return;
-    launch_items(m, op, f, g, work, chunks, n_chunks, items, partial, err, s);
-    mixed::k_reduce_chunks<<<n_work, 256, 0, s>>>(g, work, chunk_begin, partial, 8 * m.kp1_d);
+    launch_items(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, nullptr, nullptr, s);
+    mixed::k_reduce_chunks<<<n_work, 256, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nullptr);
 }
 
-void launch_items(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, const int4 *chunks, int n_chunks,
-                  const WorkItem *items, double *partial, int *err, cudaStream_t s) {
+void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tree, const int *work, int n_work, const int *chunk_begin,
+                          const double *partial, cudaStream_t s, const int *nw_dev) {
+    if (n_work <= 0) return;
+    mixed::k_reduce_chunks<<<n_work, 256, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nw_dev);
+}
+
+int contract_items_resident(int K) {
+    switch (K) {
+        case 2: return resident_k<2>();
+        case 3: return resident_k<3>();
+        case 4: return resident_k<4>();
+        case 5: return resident_k<5>();
+        case 6: return resident_k<6>();
+        case 7: return resident_k<7>();
+        case 8: return resident_k<8>();
+        case 9: return resident_k<9>();
+        case 10: return resident_k<10>();
+        case 11: return resident_k<11>();
+        case 12: return resident_k<12>();
+        default: return 0;
+    }
+}
+
+void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                  const int4 *chunks, int n_chunks, const WorkItem *items, double *partial, int *err, const int *n_chunks_dev, int *counter,
+                  cudaStream_t s) {
     if (n_chunks <= 0) return;
     switch (m.K) {
-        case 2: launch_k<2>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 3: launch_k<3>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 4: launch_k<4>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 5: launch_k<5>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 6: launch_k<6>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 7: launch_k<7>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 8: launch_k<8>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 9: launch_k<9>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 10: launch_k<10>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 11: launch_k<11>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
-        case 12: launch_k<12>(m, op, f, g, work, chunks, n_chunks, items, partial, err, s); break;
+        case 2: launch_k<2>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 3: launch_k<3>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 4: launch_k<4>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 5: launch_k<5>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 6: launch_k<6>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 7: launch_k<7>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 8: launch_k<8>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 9: launch_k<9>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 10: launch_k<10>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 11: launch_k<11>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
+        case 12: launch_k<12>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
         default: break;
     }
 }

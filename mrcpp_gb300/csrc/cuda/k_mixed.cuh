@@ -134,14 +134,21 @@ __device__ __forceinline__ void run_stage(const StageOut *so, int nso, int warp,
     }
 }
 
-// One CTA per chunk of the work items of one output node: chunk = (position of
-// g in the work list, first item, end item).  The FP64 partial sum of the chunk
-// goes to partial[blockIdx.x]; k_reduce_chunks adds the chunks of each g in
-// order (deterministic) and computes the node norms.
+// Chunks of the work items of one output node: chunk = (position of g in the
+// work list, first item, end item).  The FP64 partial sum of chunk c goes to
+// partial[c]; k_reduce_chunks adds the chunks of each g in order
+// (deterministic) and computes the node norms.
+//
+// Without a chunk counter every CTA computes chunk blockIdx.x.  With one, the
+// launch is persistent: CTA b starts with chunk b and then takes chunks
+// gridDim.x + atomicAdd(counter, 1) until *n_chunks_dev is reached (the
+// counter must be 0 at launch), so the grid size does not depend on the work
+// list and the number of chunks can be produced on the device.
 template <int K>
-__global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work,
-                                                                              const int4 *chunks, const WorkItem *items, double *partial,
-                                                                              int *err) {
+__global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(DevMRA m, DevOper op, const DevTree *fs, const DevTree *gs,
+                                                                              const int *work_tree, const int *work, const int4 *chunks,
+                                                                              const WorkItem *items, double *partial, int *err,
+                                                                              const int *n_chunks_dev, int *counter) {
     using S = Shape<K>;
     constexpr int K2 = S::K2, K3 = S::K3, BLK = S::BLK, R = S::R;
     extern __shared__ __align__(16) float smf[];
@@ -149,11 +156,16 @@ __global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(De
     float *OB = BUF + S::NBUF * BLK;   // [3 dirs][4 comps] K*K, out-of-band blocks zero
     double *G64 = (double *)(OB + 12 * K2);  // FP64 accumulators (thread-owned elements)
     __shared__ StageOut s_so0[9], s_so1[17], s_g[8];
-    __shared__ int s_n0, s_n1;
+    __shared__ int s_n0, s_n1, s_next;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int4 ch = chunks[blockIdx.x];
+    const int n_chunks = n_chunks_dev ? *n_chunks_dev : (int)gridDim.x;
+    for (int cix = blockIdx.x; cix < n_chunks;) {
+    const int4 ch = chunks[cix];
     const int gi = work[ch.x];
-    const int depth = g.idx[gi].x - m.root_scale;
+    const int tree = work_tree[ch.x];
+    const int depth = gs[tree].idx[gi].x - m.root_scale;
+    const int f_cap_real = fs[tree].cap_real;
+    const float *f_coefs32 = fs[tree].coefs32, *f_gcoefs32 = fs[tree].gcoefs32;
     // warp `warp` owns component gt = warp of g: rows lane + 32 r, all columns
     float acc[R][K];
 #pragma unroll
@@ -175,8 +187,8 @@ __global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(De
             if (off >= 0 && abs(l) <= bwi[c] && abs(l) <= L0) v = op.blocks32[(size_t)(off + l + L0) * 4 * K2 + r];
             OB[e] = v;
         }
-        const bool gen = item.fid >= f.cap_real;
-        const float *fc = gen ? f.gcoefs32 + (size_t)(item.fid - f.cap_real) * K3 : f.coefs32 + (size_t)item.fid * 8 * K3;
+        const bool gen = item.fid >= f_cap_real;
+        const float *fc = gen ? f_gcoefs32 + (size_t)(item.fid - f_cap_real) * K3 : f_coefs32 + (size_t)item.fid * 8 * K3;
         const bool block = item.flags & 1;
         const float *OX = OB, *OY = OB + 4 * K2, *OZ = OB + 8 * K2;
         if (block) {
@@ -350,7 +362,7 @@ __global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(De
             since = 0;
         }
     }
-    double *go = partial + (size_t)blockIdx.x * 8 * K3;
+    double *go = partial + (size_t)cix * 8 * K3;
 #pragma unroll
     for (int r = 0; r < R; r++) {
         const int c = lane + 32 * r;
@@ -361,13 +373,22 @@ __global__ void __launch_bounds__(256, Shape<K>::MIN_BLOCKS) k_contract_items(De
                 go[e] = G64[e] + (double)acc[r][j];
             }
     }
+    if (!counter) break;
+    __syncthreads();  // G64 is cleared with another thread mapping by the next chunk
+    if (tid == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);
+    __syncthreads();
+    cix = s_next;
+    }
 }
 
 // g coefficients = sum of the chunk partials of g in chunk order; node norms.
-__global__ void __launch_bounds__(256) k_reduce_chunks(DevTree g, const int *work, const int *chunk_begin, const double *partial, int nc) {
+__global__ void __launch_bounds__(256) k_reduce_chunks(const DevTree *gs, const int *work_tree, const int *work, const int *chunk_begin,
+                                                       const double *partial, int nc, const int *nw_dev) {
     const int tid = threadIdx.x;
     const int wi = blockIdx.x;
+    if (nw_dev && wi >= *nw_dev) return;
     const int gi = work[wi];
+    const DevTree &g = gs[work_tree[wi]];
     const int c0 = chunk_begin[wi], c1 = chunk_begin[wi + 1];
     double *go = g.coefs + (size_t)gi * nc;
     const int K3 = nc / 8;

@@ -59,7 +59,7 @@ __global__ void k_hash_build(DevMRA m, DevTree t, int first, int count, int *err
 
 // One CTA per pending GenNode: walk up to the nearest node present in the
 // lookup table, then reconstruct down along the path to the requested child.
-__global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err) {
+__global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, bool real_only) {
     extern __shared__ double sm[];
     const int K = m.K, K3 = m.kp1_d;
     double *b0 = sm;           // 4 K^3
@@ -77,7 +77,7 @@ __global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pe
             uint64_t key;
             if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
             int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
-            if (id >= 0) { s_anc = id; s_ancn = a; break; }
+            if (id >= 0 && (!real_only || id < f.cap_real)) { s_anc = id; s_ancn = a; break; }
         }
     }
     __syncthreads();
@@ -195,8 +195,10 @@ __global__ void k_node_norms(DevMRA m, DevTree t, const int *nodes, int n) {
 }
 
 // TopDown: parent (s,d) -> children scaling, added (overwrite=false) or assigned.
-__global__ void k_mw_down(DevMRA m, DevTree t, const int *parents, int n, bool overwrite) {
+// With ptree set, parent j belongs to tree ts[ptree[j]] (several trees per launch).
+__global__ void k_mw_down(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite) {
     extern __shared__ double sm[];
+    const DevTree t = ptree ? ts[ptree[blockIdx.x]] : t0;
     const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
     double *t1 = sm, *t2 = sm + 8 * K3;
     int p = parents[blockIdx.x];
@@ -236,8 +238,9 @@ __global__ void k_mw_down(DevMRA m, DevTree t, const int *parents, int n, bool o
 }
 
 // BottomUp: 8 children scaling blocks -> parent (s,d), then parent norms.
-__global__ void k_mw_up(DevMRA m, DevTree t, const int *parents, int n) {
+__global__ void k_mw_up(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n) {
     extern __shared__ double sm[];
+    const DevTree t = ptree ? ts[ptree[blockIdx.x]] : t0;
     const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
     double *t1 = sm, *t2 = sm + 8 * K3;
     int p = parents[blockIdx.x];
@@ -269,7 +272,28 @@ __global__ void k_to_float(const double *src, float *dst, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = (float)src[i];
 }
 
+__global__ void k_gather_norms_multi(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * 8) return;
+    const int w = i / 8;
+    dst[i] = gs[work_tree[w]].norms[(size_t)work[w] * 8 + (i % 8)];
+}
+
+// device time stamp (PTX %globaltimer, nanoseconds)
+__global__ void k_stamp(unsigned long long *t) {
+    unsigned long long v;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+    *t = v;
+}
+
 }  // namespace
+
+void launch_stamp(unsigned long long *t, cudaStream_t s) { k_stamp<<<1, 1, 0, s>>>(t); }
+
+void launch_gather_norms(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst, cudaStream_t s) {
+    if (n <= 0) return;
+    k_gather_norms_multi<<<(n * 8 + 255) / 256, 256, 0, s>>>(gs, work_tree, work, n, dst);
+}
 
 void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s) {
     if (n == 0) return;
@@ -282,11 +306,11 @@ void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *er
     k_hash_build<<<(count + 255) / 256, 256, 0, s>>>(m, t, first, count, err);
 }
 
-void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {
+void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s, bool real_only) {
     if (n_pend <= 0) return;
     size_t smem = sizeof(double) * 8 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_nodes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err);
+    k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
 }
 
 void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {
@@ -299,18 +323,18 @@ void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cuda
     k_node_norms<<<n, 128, 0, s>>>(m, t, nodes, n);
 }
 
-void launch_mw_down(const DevMRA &m, DevTree t, const int *parents, int n, bool overwrite, cudaStream_t s) {
+void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite, cudaStream_t s) {
     if (n <= 0) return;
     size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_mw_down<<<n, 256, smem, s>>>(m, t, parents, n, overwrite);
+    k_mw_down<<<n, 256, smem, s>>>(m, t, ts, ptree, parents, n, overwrite);
 }
 
-void launch_mw_up(const DevMRA &m, DevTree t, const int *parents, int n, cudaStream_t s) {
+void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s) {
     if (n <= 0) return;
     size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_up, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_mw_up<<<n, 256, smem, s>>>(m, t, parents, n);
+    k_mw_up<<<n, 256, smem, s>>>(m, t, ts, ptree, parents, n);
 }
 
 }  // namespace mwgpu

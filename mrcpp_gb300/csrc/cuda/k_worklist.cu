@@ -19,13 +19,13 @@ namespace mwgpu {
 namespace {
 
 struct PairCtx {
-    int wi, fid, depth;
+    int wi, fid, depth, tree;
     int tl[3];
 };
 
-// locate pair p: g position wi (binary search in pair_off), its band cell and f
-__device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work,
-                                   const long long *pair_off, int n_work, long long p, PairCtx &pc) {
+// locate pair p: work position wi (binary search in pair_off), its tree, band cell and f
+__device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree,
+                                   const int *work, const long long *pair_off, int n_work, long long p, PairCtx &pc) {
     int lo = 0, hi = n_work - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -33,7 +33,9 @@ __device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const Dev
         else hi = mid - 1;
     }
     const int wi = lo;
-    const int4 gx = g.idx[work[wi]];
+    const int t = work_tree[wi];
+    const DevTree &f = fs[t];
+    const int4 gx = gs[t].idx[work[wi]];
     const int depth = gx.x - m.root_scale;
     const int w = op.band_max[depth];
     const int gl[3] = {gx.y, gx.z, gx.w};
@@ -47,6 +49,7 @@ __device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const Dev
     const int nx = be[0] - bs[0] + 1, ny = be[1] - bs[1] + 1;
     const int fx = bs[0] + (int)(q % nx), fy = bs[1] + (int)((q / nx) % ny), fz = bs[2] + (int)(q / ((long long)nx * ny));
     pc.wi = wi;
+    pc.tree = t;
     pc.depth = depth;
     pc.tl[0] = fx - gl[0];
     pc.tl[1] = fy - gl[1];
@@ -58,18 +61,28 @@ __device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const Dev
 }
 
 template <bool FILL>
-__global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, const long long *pair_off, int n_work,
-                                               long long n_pairs, double gthr, int *counts, const long long *item_off, WorkItem *items,
-                                               unsigned long long *ncomp, unsigned long long *nband, int *err) {
+// n_pairs / n_work are the launch capacity; with np_dev / nw_dev the actual
+// counts come from the device (levels whose work list is made on the device),
+// and COUNT writes zero counts for the pairs in [*np_dev, n_pairs).
+__global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                                               const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts,
+                                               const long long *item_off, WorkItem *items, long long items_cap, unsigned long long *ncomp,
+                                               unsigned long long *nband, int *err, const long long *np_dev, const int *nw_dev) {
     const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int cnt = 0;
     unsigned long long comp = 0, band = 0;
+    const long long n_cap = n_pairs;
+    if (np_dev) n_pairs = *np_dev;
+    if (nw_dev) n_work = *nw_dev;
+    if (!FILL && p >= n_pairs && p < n_cap) counts[p] = 0;
     if (p < n_pairs) {
         PairCtx pc;
-        if (!locate_pair(m, op, f, g, work, pair_off, n_work, p, pc)) {
+        if (!locate_pair(m, op, fs, gs, work_tree, work, pair_off, n_work, p, pc)) {
             atomicOr(err, DE_LOOKUP);
         } else {
             band = 1;
+            const DevTree &f = fs[pc.tree];
+            const double gthr = gthrs[pc.tree];
             double fn[8];
             bool any = false;
             for (int c = 0; c < 8; c++) {
@@ -126,7 +139,9 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, DevTree f, 
                     it.tl[2] = (short)pc.tl[2];
                     it.flags = (mask == smask) ? 1 : 0;
                     it.pad = 0;
-                    items[wpos++] = it;
+                    if (wpos < items_cap) items[wpos] = it;
+                    else atomicOr(err, DE_POOL_FULL);
+                    wpos++;
                 } else {
                     comp += __popcll(mask);
                 }
@@ -197,26 +212,84 @@ __global__ void k_scan_add(long long *out, long long n, const long long *block_s
 }
 
 // per-g item offsets: g_off[wi] = item_off[pair_off[wi]]
-__global__ void k_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off) {
+__global__ void k_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, const int *nw_dev) {
     const int wi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nw_dev) n_work = *nw_dev;
     if (wi <= n_work) g_off[wi] = item_off[pair_off[wi]];
+}
+
+// chunks of at most `per` items per work entry (at least one, so that every
+// output node gets its reduction input)
+__device__ inline long long chunk_len(const long long *g_off, int n_work, long long per) {
+    if (per > 0) return per;
+    const long long total = g_off[n_work];
+    return max(8LL, (total + kChunkTarget - 1) / kChunkTarget);
+}
+
+__global__ void k_chunk_count(const long long *g_off, int n_work, long long per, int *counts, const int *nw_dev) {
+    const int wi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (wi >= n_work) return;
+    if (nw_dev && wi >= *nw_dev) {
+        counts[wi] = 0;
+        return;
+    }
+    per = chunk_len(g_off, nw_dev ? *nw_dev : n_work, per);
+    const long long len = g_off[wi + 1] - g_off[wi];
+    counts[wi] = len == 0 ? 1 : (int)((len + per - 1) / per);
+}
+
+__global__ void k_chunk_fill(const long long *g_off, const long long *c_off, int n_work, long long per, int4 *chunks, int *chunk_begin,
+                             int cap, int *n_chunks, int *err, const int *nw_dev) {
+    const int wi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nw_dev) n_work = *nw_dev;
+    if (n_work == 0 && wi == 0) {
+        chunk_begin[0] = 0;
+        *n_chunks = 0;
+    }
+    if (wi >= n_work) return;
+    per = chunk_len(g_off, n_work, per);
+    const long long b = g_off[wi], e = g_off[wi + 1];
+    long long c = c_off[wi];
+    chunk_begin[wi] = (int)c;
+    if (wi == n_work - 1) {
+        const long long tot = c_off[n_work];
+        chunk_begin[n_work] = (int)tot;
+        *n_chunks = (int)(tot < (long long)cap ? tot : (long long)cap);
+        if (tot > cap) atomicOr(err, DE_POOL_FULL);
+    }
+    if (b == e) {
+        if (c < cap) chunks[c] = make_int4(wi, (int)b, (int)e, 0);
+        return;
+    }
+    for (long long x = b; x < e; x += per, c++)
+        if (c < cap) chunks[c] = make_int4(wi, (int)x, (int)min(e, x + per), 0);
 }
 
 }  // namespace
 
-void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
-                        int n_work, long long n_pairs, double gthr, int *counts, unsigned long long *ncomp, unsigned long long *nband, int *err,
-                        cudaStream_t s) {
+void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                        const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts, unsigned long long *ncomp,
+                        unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
     if (n_pairs <= 0) return;
-    k_pairs<false><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, f, g, work, pair_off, n_work, n_pairs, gthr, counts, nullptr, nullptr,
-                                                                    ncomp, nband, err);
+    k_pairs<false><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts,
+                                                                    nullptr, nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
 }
 
-void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
-                       int n_work, long long n_pairs, double gthr, const long long *item_off, WorkItem *items, int *err, cudaStream_t s) {
+void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                       const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const long long *item_off, WorkItem *items,
+                       long long items_cap, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
     if (n_pairs <= 0) return;
-    k_pairs<true><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, f, g, work, pair_off, n_work, n_pairs, gthr, nullptr, item_off, items,
-                                                                   nullptr, nullptr, err);
+    k_pairs<true><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr,
+                                                                   item_off, items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
+}
+
+void launch_chunk_count(const long long *g_off, int n_work, long long per, int *counts, cudaStream_t s, const int *nw_dev) {
+    k_chunk_count<<<(n_work + 255) / 256, 256, 0, s>>>(g_off, n_work, per, counts, nw_dev);
+}
+
+void launch_chunk_fill(const long long *g_off, const long long *c_off, int n_work, long long per, int4 *chunks, int *chunk_begin, int cap,
+                       int *n_chunks, int *err, cudaStream_t s, const int *nw_dev) {
+    k_chunk_fill<<<(n_work + 255) / 256, 256, 0, s>>>(g_off, c_off, n_work, per, chunks, chunk_begin, cap, n_chunks, err, nw_dev);
 }
 
 long long scan_blocks(long long n) { return (n + kScanBlock - 1) / kScanBlock; }
@@ -228,8 +301,8 @@ void launch_scan(const int *in, long long *out, long long n, long long *block_su
     k_scan_add<<<(unsigned)nb, kScanBlock, 0, s>>>(out, n, block_sums, total);
 }
 
-void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s) {
-    k_gather_goff<<<(n_work + 1 + 255) / 256, 256, 0, s>>>(item_off, pair_off, n_work, g_off);
+void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev) {
+    k_gather_goff<<<(n_work + 1 + 255) / 256, 256, 0, s>>>(item_off, pair_off, n_work, g_off, nw_dev);
 }
 
 }  // namespace mwgpu

@@ -22,80 +22,7 @@ thread_local std::string g_init_error;
 constexpr double kMachinePrec = 1.0e-15;
 }  // namespace
 
-struct mwgpu_ctx {
-    int device = 0;
-    int precision = MWGPU_PREC_FP64;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-    std::string err;
-    int *d_err = nullptr;
-    LevelStats *d_stats = nullptr;
-    int *d_work = nullptr;
-    int work_cap = 0;
-    // pending GenNode set
-    uint64_t *d_pkeys = nullptr;
-    int *d_pvals = nullptr;
-    int phcap = 0;
-    uint64_t *d_plist = nullptr;
-    int pcap = 0;
-    int *d_pcount = nullptr;
-    int *d_list = nullptr;  // parent lists for transforms
-    int list_cap = 0;
-    cudaEvent_t marks[16] = {};
-    // work list of the mixed form
-    WorkItem *d_items = nullptr;
-    long long items_cap = 0;
-    long long *d_pair_off = nullptr, pair_off_cap = 0;
-    int *d_pcounts = nullptr;
-    long long pcounts_cap = 0;
-    long long *d_item_off = nullptr, item_off_cap = 0;
-    long long *d_scan = nullptr, scan_cap = 0;
-    long long *d_goff = nullptr, goff_cap = 0;
-    int4 *d_chunks = nullptr;
-    int *d_chunk_begin = nullptr;
-    int chunks_cap = 0;
-    double *d_partial = nullptr;
-    size_t partial_cap = 0;  // doubles
-    unsigned long long launches = 0;
-    void *d_scrub = nullptr;
-    size_t scrub_bytes = 0;
-};
-
-struct mwgpu_oper {
-    DevMRA mra{};
-    double *d_filt = nullptr;
-    DevOper op{};
-    std::vector<void *> allocs;
-    int n_rows = 0;
-    std::vector<int> widths;    // [T * n_rows * 5]
-    std::vector<int> band_max;  // [n_rows]
-};
-
-struct mwgpu_tree {
-    DevMRA mra{};
-    double *d_filt = nullptr;
-    DevTree t{};
-    std::vector<int4> h_idx;
-    std::vector<int> h_child0;
-    bool is_input = false;
-};
-
-#define MW_CK(call)                                                                                 \
-    do {                                                                                            \
-        cudaError_t e_ = (call);                                                                    \
-        if (e_ != cudaSuccess) {                                                                    \
-            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                          \
-            return (e_ == cudaErrorMemoryAllocation) ? MWGPU_ERR_OOM : MWGPU_ERR_DEVICE;            \
-        }                                                                                           \
-    } while (0)
-
-#define MW_ARG(cond, msg)                     \
-    do {                                      \
-        if (!(cond)) {                        \
-            ctx->err = msg;                   \
-            return MWGPU_ERR_BAD_ARG;         \
-        }                                     \
-    } while (0)
+#include "abi_state.cuh"
 
 namespace {
 
@@ -119,12 +46,6 @@ mwgpu_status make_mra(mwgpu_ctx *ctx, const mwgpu_mra_desc *d, DevMRA &m, double
     return MWGPU_OK;
 }
 
-template <class T> mwgpu_status dev_alloc(mwgpu_ctx *ctx, T **p, size_t n) {
-    *p = nullptr;
-    if (n == 0) n = 1;
-    MW_CK(cudaMalloc((void **)p, sizeof(T) * n));
-    return MWGPU_OK;
-}
 
 int next_pow2(long long x) {
     int p = 1;
@@ -230,22 +151,48 @@ mwgpu_status grow_gen(mwgpu_ctx *ctx, mwgpu_tree *tr, int need) {
 mwgpu_status ensure_work(mwgpu_ctx *ctx, int n) {
     if (n <= ctx->work_cap) return MWGPU_OK;
     if (ctx->d_work) cudaFree(ctx->d_work);
+    if (ctx->d_wtree) cudaFree(ctx->d_wtree);
+    ctx->d_work = ctx->d_wtree = nullptr;
     ctx->work_cap = std::max(n, 2 * ctx->work_cap);
-    return dev_alloc(ctx, &ctx->d_work, ctx->work_cap);
+    if (auto s = dev_alloc(ctx, &ctx->d_work, ctx->work_cap)) return s;
+    return dev_alloc(ctx, &ctx->d_wtree, ctx->work_cap);
 }
 
-mwgpu_status ensure_pending(mwgpu_ctx *ctx, int phcap, int pcap) {
-    if (phcap > ctx->phcap) {
+mwgpu_status ensure_trees(mwgpu_ctx *ctx, int nt) {
+    if (nt <= ctx->trees_cap) return MWGPU_OK;
+    for (void *p : {(void *)ctx->d_fs, (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_pcount})
+        if (p) cudaFree(p);
+    ctx->d_fs = ctx->d_gs = nullptr;
+    ctx->d_gthr = nullptr;
+    ctx->d_pcount = nullptr;
+    ctx->trees_cap = std::max(nt, 2 * ctx->trees_cap);
+    if (auto s = dev_alloc(ctx, &ctx->d_fs, ctx->trees_cap)) return s;
+    if (auto s = dev_alloc(ctx, &ctx->d_gs, ctx->trees_cap)) return s;
+    if (auto s = dev_alloc(ctx, &ctx->d_gthr, ctx->trees_cap)) return s;
+    if (auto s = dev_alloc(ctx, &ctx->d_pcount, ctx->trees_cap)) return s;
+    ctx->pcount_cap = ctx->trees_cap;
+    return MWGPU_OK;
+}
+
+// pending GenNode sets of nt trees: tree t uses hash slots [t phcap, (t+1) phcap)
+// and list slots [t pcap, (t+1) pcap)
+mwgpu_status ensure_pending(mwgpu_ctx *ctx, int phcap, int pcap, int nt) {
+    if (phcap > ctx->phcap || (long long)phcap * nt > ctx->ph_total) {
         if (ctx->d_pkeys) cudaFree(ctx->d_pkeys);
         if (ctx->d_pvals) cudaFree(ctx->d_pvals);
-        if (auto s = dev_alloc(ctx, &ctx->d_pkeys, phcap)) return s;
-        if (auto s = dev_alloc(ctx, &ctx->d_pvals, phcap)) return s;
-        ctx->phcap = phcap;
+        ctx->d_pkeys = nullptr;
+        ctx->d_pvals = nullptr;
+        ctx->phcap = std::max(phcap, ctx->phcap);
+        ctx->ph_total = (long long)ctx->phcap * nt;
+        if (auto s = dev_alloc(ctx, &ctx->d_pkeys, (size_t)ctx->ph_total)) return s;
+        if (auto s = dev_alloc(ctx, &ctx->d_pvals, (size_t)ctx->ph_total)) return s;
     }
-    if (pcap > ctx->pcap) {
+    if (pcap > ctx->pcap || (long long)pcap * nt > ctx->pl_total) {
         if (ctx->d_plist) cudaFree(ctx->d_plist);
-        if (auto s = dev_alloc(ctx, &ctx->d_plist, pcap)) return s;
-        ctx->pcap = pcap;
+        ctx->d_plist = nullptr;
+        ctx->pcap = std::max(pcap, ctx->pcap);
+        ctx->pl_total = (long long)ctx->pcap * nt;
+        if (auto s = dev_alloc(ctx, &ctx->d_plist, (size_t)ctx->pl_total)) return s;
     }
     return MWGPU_OK;
 }
@@ -272,15 +219,30 @@ template <class T> mwgpu_status grow_buf(mwgpu_ctx *ctx, T **p, long long *cap, 
     return dev_alloc(ctx, p, (size_t)*cap);
 }
 
-// Mixed form: work list (pair counts, scan, fill) then the contraction over
-// chunks of items and the per-node reduction.  node_terms is returned in *hs.
-mwgpu_status run_mixed(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *d_work, const int *node_ix, int n,
-                       double gthr, LevelStats *hs) {
-    // (g, band cell) pairs: the band boxes of makeOperBand, clipped to the world
-    std::vector<long long> poff(n + 1, 0);
+// One level over nt (input, output) tree pairs that share an operator.  The
+// work entries are grouped by tree: entries seg[t] .. seg[t+1]-1 are nodes of
+// output tree t.
+struct Level {
+    const mwgpu_oper *o = nullptr;
+    int nt = 0;
+    mwgpu_tree *const *inps = nullptr;
+    mwgpu_tree *const *outs = nullptr;
+    int n = 0;
+    std::vector<int> node, tree, order;  // grouped entries; order[j] = caller position of entry j
+    std::vector<int> seg;
+    std::vector<double> gthr;
+    std::vector<DevTree> fs, gs;
+};
+
+// (g, band cell) pairs of every work entry: the band boxes of makeOperBand
+// (ConvolutionCalculator.cpp:142-222), clipped to the world; poff[n] = total
+void pair_offsets(const Level &lv, std::vector<long long> &poff) {
+    const mwgpu_oper *o = lv.o;
     const DevMRA &m = o->mra;
+    const int n = lv.n;
+    poff.assign(n + 1, 0);
     for (int wi = 0; wi < n; wi++) {
-        const int4 gx = out->h_idx[node_ix[wi]];
+        const int4 gx = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]];
         const int depth = gx.x - m.root_scale;
         long long cells = 0;
         if (depth >= 0 && depth < o->op.n_band_max && depth < kMaxDepthRows && o->band_max[depth] >= 0) {
@@ -295,6 +257,16 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwg
         }
         poff[wi + 1] = poff[wi] + cells;
     }
+}
+
+// Mixed form: work list (pair counts, scan, fill) then the contraction over
+// chunks of items and the per-node reduction.  node_terms is returned in *hs.
+mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
+    const mwgpu_oper *o = lv.o;
+    const int n = lv.n;
+    const DevMRA &m = o->mra;
+    std::vector<long long> poff;
+    pair_offsets(lv, poff);
     const long long np = poff[n];
     if (auto s = grow_buf(ctx, &ctx->d_pair_off, &ctx->pair_off_cap, n + 1)) return s;
     if (auto s = grow_buf(ctx, &ctx->d_pcounts, &ctx->pcounts_cap, np + 1)) return s;
@@ -303,8 +275,8 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwg
     if (auto s = grow_buf(ctx, &ctx->d_goff, &ctx->goff_cap, n + 1)) return s;
     MW_CK(cudaMemcpyAsync(ctx->d_pair_off, poff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
     LevelStats *dst = ctx->d_stats;
-    launch_pairs_count(m, o->op, inp->t, out->t, d_work, ctx->d_pair_off, n, np, gthr, ctx->d_pcounts, &dst->components, &dst->band_nodes,
-                       ctx->d_err, ctx->stream);
+    launch_pairs_count(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_pcounts,
+                       &dst->components, &dst->band_nodes, ctx->d_err, ctx->stream);
     long long *d_total = ctx->d_scan + (ctx->scan_cap - 1);
     launch_scan(ctx->d_pcounts, ctx->d_item_off, np, ctx->d_scan, d_total, ctx->stream);
     launch_gather_goff(ctx->d_item_off, ctx->d_pair_off, n, ctx->d_goff, ctx->stream);
@@ -323,10 +295,11 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwg
         ctx->items_cap = std::max(total, 2 * ctx->items_cap);
         if (auto s = dev_alloc(ctx, &ctx->d_items, (size_t)ctx->items_cap)) return s;
     }
-    launch_pairs_fill(m, o->op, inp->t, out->t, d_work, ctx->d_pair_off, n, np, gthr, ctx->d_item_off, ctx->d_items, ctx->d_err, ctx->stream);
+    launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_item_off,
+                      ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream);
     ctx->launches++;
     // chunks of about the same number of items, several waves of CTAs
-    long long per = std::max<long long>(8, (total + 8 * 304 - 1) / (8 * 304));
+    long long per = std::max<long long>(8, (total + kChunkTarget - 1) / kChunkTarget);
     if (const char *e = std::getenv("MWGPU_CHUNK_ITEMS")) per = std::max<long long>(1, std::atoll(e));
     std::vector<int4> chunks;
     std::vector<int> cbeg(n + 1, 0);
@@ -357,9 +330,9 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwg
     MW_CK(cudaMemcpyAsync(ctx->d_chunks, chunks.data(), sizeof(int4) * nch, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(ctx->d_chunk_begin, cbeg.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
-    launch_contract_items(o->mra, o->op, inp->t, out->t, d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items, ctx->d_partial,
-                          ctx->d_err, ctx->stream);
-    ctx->launches += 3;
+    launch_contract_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items,
+                          ctx->d_partial, ctx->d_err, ctx->stream);
+    ctx->launches += 2;
     MW_CK(cudaStreamSynchronize(ctx->stream));  // host vectors above must outlive the copies
     hs->node_terms = (unsigned long long)total;
     return MWGPU_OK;
@@ -370,6 +343,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     auto *tr = new mwgpu_tree();
     tr->is_input = input;
     if (auto s = make_mra(ctx, mra, tr->mra, &tr->d_filt)) { delete tr; return s; }
+    tr->h_filt.assign(mra->filters, mra->filters + 8 * tr->mra.K * tr->mra.K);
     DevTree &t = tr->t;
     const int n = d->n_nodes;
     const size_t nc = 8 * (size_t)tr->mra.kp1_d;
@@ -432,6 +406,258 @@ void free_tree(mwgpu_tree *tr) {
 
 }  // namespace
 
+namespace {
+
+// GenNodes the operator bands of the work entries need, every tree at once
+// (MWTree::getNode, MWTree.cpp:340-352); ctx->d_work / d_wtree hold the entries.
+mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount, unsigned long long &gen_total) {
+    const mwgpu_oper *o = lv.o;
+    const int nt = lv.nt;
+    pcount.assign(nt, 0);
+    for (int attempt = 0; attempt < 8; attempt++) {
+        if (auto s = ensure_pending(ctx, std::max(ctx->phcap, 1 << 16), std::max(ctx->pcap, 1 << 15), nt)) return s;
+        MW_CK(cudaMemsetAsync(ctx->d_pkeys, 0xFF, sizeof(uint64_t) * ctx->phcap * nt, ctx->stream));
+        MW_CK(cudaMemsetAsync(ctx->d_pcount, 0, sizeof(int) * nt, ctx->stream));
+        for (int t = 0; t < nt; t++) {
+            const int b = lv.seg[t], e = lv.seg[t + 1];
+            if (b == e) continue;
+            launch_band_missing(o->mra, o->op, lv.inps[t]->t, lv.outs[t]->t, ctx->d_work + b, e - b, ctx->d_pkeys + (size_t)t * ctx->phcap,
+                                ctx->d_pvals + (size_t)t * ctx->phcap, ctx->phcap, ctx->d_plist + (size_t)t * ctx->pcap, ctx->d_pcount + t,
+                                ctx->pcap, ctx->d_err, ctx->stream);
+            ctx->launches++;
+        }
+        int herr = 0;
+        MW_CK(cudaMemcpyAsync(pcount.data(), ctx->d_pcount, sizeof(int) * nt, cudaMemcpyDeviceToHost, ctx->stream));
+        MW_CK(cudaMemcpyAsync(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        if (herr & DE_RANGE) { ctx->err = "band index outside the lookup range"; return MWGPU_ERR_INTERNAL; }
+        const bool hfull = herr & DE_HASH_FULL;
+        const int pmax = *std::max_element(pcount.begin(), pcount.end());
+        if (!hfull && pmax <= ctx->pcap) break;
+        MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        if (auto s = ensure_pending(ctx, hfull ? ctx->phcap * 4 : next_pow2(4LL * pmax), std::max(pmax + 1024, ctx->pcap), nt)) return s;
+        if (attempt == 7) { ctx->err = "pending GenNode set did not fit"; return MWGPU_ERR_OOM; }
+    }
+    gen_total = 0;
+    for (int t = 0; t < nt; t++) {
+        if (pcount[t] == 0) continue;
+        mwgpu_tree *inp = lv.inps[t];
+        DevTree &f = inp->t;
+        if (auto s = grow_gen(ctx, inp, f.n_gen + pcount[t])) return s;
+        if (2LL * (f.n_real + f.n_gen + pcount[t]) + 16 > f.hcap)
+            if (auto s = rebuild_hash(ctx, inp, (long long)f.n_real + f.n_gen + pcount[t])) return s;
+        const uint64_t *pl = ctx->d_plist + (size_t)t * ctx->pcap;
+        launch_gen_nodes(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream);
+        launch_gen_insert(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream);
+        ctx->launches += 2;
+        f.n_gen += pcount[t];
+        gen_total += pcount[t];
+    }
+    return MWGPU_OK;
+}
+
+// Everything of one level after validation: GenNodes of every input tree,
+// per-tree thresholds, the contraction and the norm gather.
+mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double prec, double *norms_out, mwgpu_level_stats *stats,
+                       std::vector<int> *pcount_out = nullptr) {
+    const mwgpu_oper *o = lv.o;
+    const int n = lv.n, nt = lv.nt;
+    if (auto s = ensure_work(ctx, n)) return s;
+    if (auto s = ensure_trees(ctx, nt)) return s;
+    MW_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_work, lv.node.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_wtree, lv.tree.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
+    std::vector<int> pcount;
+    unsigned long long gen_total = 0;
+    if (auto s = gen_pass(ctx, lv, pcount, gen_total)) return s;
+    if (pcount_out) *pcount_out = pcount;
+    // per-tree screening threshold (ConvolutionCalculator.cpp:297-305)
+    lv.gthr.assign(nt, 0.0);
+    for (int t = 0; t < nt; t++) {
+        double g = sqnorms[t];
+        if (g > 0.0) g = prec * 1.0 * std::sqrt(g / (double)o->op.n_terms);
+        lv.gthr[t] = g;
+    }
+    lv.fs.resize(nt);
+    lv.gs.resize(nt);
+    for (int t = 0; t < nt; t++) {
+        lv.fs[t] = lv.inps[t]->t;
+        lv.gs[t] = lv.outs[t]->t;
+    }
+    MW_CK(cudaMemcpyAsync(ctx->d_fs, lv.fs.data(), sizeof(DevTree) * nt, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_gs, lv.gs.data(), sizeof(DevTree) * nt, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_gthr, lv.gthr.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->stream));
+    LevelStats mixed_nt{};
+    if (ctx->precision == MWGPU_PREC_MIXED) {
+        if (auto s = run_mixed(ctx, lv, &mixed_nt)) return s;
+    } else {
+        MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        for (int t = 0; t < nt; t++) {
+            const int b = lv.seg[t], e = lv.seg[t + 1];
+            if (b == e) continue;
+            launch_contract_fp64(o->mra, o->op, lv.inps[t]->t, lv.outs[t]->t, ctx->d_work + b, e - b, lv.gthr[t], ctx->d_stats, ctx->d_err,
+                                 ctx->stream);
+            ctx->launches++;
+        }
+    }
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
+    LevelStats hs{};
+    MW_CK(cudaMemcpyAsync(&hs, ctx->d_stats, sizeof(LevelStats), cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> staged;
+    if (norms_out) {
+        if (auto s = grow_buf(ctx, &ctx->d_nstage, &ctx->nstage_cap, 8LL * n)) return s;
+        launch_gather_norms(ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_nstage, ctx->stream);
+        ctx->launches++;
+        staged.resize((size_t)8 * n);
+        MW_CK(cudaMemcpyAsync(staged.data(), ctx->d_nstage, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (auto s = check_err(ctx, "apply_level")) return s;
+    if (norms_out)
+        for (int j = 0; j < n; j++) std::memcpy(norms_out + 8 * (size_t)lv.order[j], &staged[8 * (size_t)j], sizeof(double) * 8);
+    if (ctx->precision == MWGPU_PREC_MIXED) hs.node_terms = mixed_nt.node_terms;
+    if (stats) {
+        stats->node_terms = hs.node_terms;
+        stats->components = hs.components;
+        stats->band_nodes = hs.band_nodes;
+        stats->gen_nodes = gen_total;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev2);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2);
+        stats->contract_ms = ms;
+    }
+    return MWGPU_OK;
+}
+
+// TopDown / BottomUp of nt trees with the same MRA: one launch per depth for
+// all trees (MWTree.cpp:166-216).
+mwgpu_status transform_impl(mwgpu_ctx *ctx, int nt, mwgpu_tree *const *trees, int direction, int overwrite) {
+    MW_ARG(direction == MWGPU_TOPDOWN || direction == MWGPU_BOTTOMUP, "invalid transform direction");
+    MW_ARG(!(direction == MWGPU_BOTTOMUP && !overwrite), "BottomUp transform always overwrites");
+    for (int t = 0; t < nt; t++) {
+        MW_ARG(trees[t], "null tree");
+        MW_ARG(trees[t]->h_filt == trees[0]->h_filt && trees[t]->mra.root_scale == trees[0]->mra.root_scale, "trees of a batch need the same MRA");
+        for (int u = 0; u < t; u++) MW_ARG(trees[u] != trees[t], "trees of a batch must be distinct");
+    }
+    cudaSetDevice(ctx->device);
+    // parents per depth (breadth-first order from the roots), all trees
+    std::vector<std::vector<int2>> levels;
+    for (int t = 0; t < nt; t++) {
+        const mwgpu_tree *tr = trees[t];
+        const int n = tr->t.n_real;
+        for (int i = 0; i < n; i++) {
+            const int depth = tr->h_idx[i].x - tr->mra.root_scale;
+            if (tr->h_child0[i] < 0 || depth < 0) continue;
+            if ((int)levels.size() <= depth) levels.resize(depth + 1);
+            levels[depth].push_back(make_int2(t, i));
+        }
+    }
+    std::vector<int> flat, ftree;
+    std::vector<std::pair<int, int>> ranges;
+    for (auto &l : levels) {
+        ranges.push_back({(int)flat.size(), (int)l.size()});
+        for (auto &e : l) {
+            ftree.push_back(e.x);
+            flat.push_back(e.y);
+        }
+    }
+    if (flat.empty()) return MWGPU_OK;
+    if ((int)flat.size() > ctx->list_cap) {
+        if (ctx->d_list) cudaFree(ctx->d_list);
+        if (ctx->d_ltree) cudaFree(ctx->d_ltree);
+        ctx->d_list = ctx->d_ltree = nullptr;
+        ctx->list_cap = (int)flat.size() * 2;
+        if (auto s = dev_alloc(ctx, &ctx->d_list, ctx->list_cap)) return s;
+        if (auto s = dev_alloc(ctx, &ctx->d_ltree, ctx->list_cap)) return s;
+    }
+    MW_CK(cudaMemcpyAsync(ctx->d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, ctx->stream));
+    const DevTree *ts = nullptr;
+    const int *ptree = nullptr;
+    std::vector<DevTree> h_ts;
+    if (nt > 1) {
+        if (auto s = ensure_trees(ctx, nt)) return s;
+        for (int t = 0; t < nt; t++) h_ts.push_back(trees[t]->t);
+        MW_CK(cudaMemcpyAsync(ctx->d_gs, h_ts.data(), sizeof(DevTree) * nt, cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_ltree, ftree.data(), sizeof(int) * ftree.size(), cudaMemcpyHostToDevice, ctx->stream));
+        ts = ctx->d_gs;
+        ptree = ctx->d_ltree;
+    }
+    const DevMRA &m = trees[0]->mra;
+    const DevTree &t0 = trees[0]->t;
+    if (direction == MWGPU_TOPDOWN) {
+        for (auto &r : ranges) {
+            launch_mw_down(m, t0, ts, ptree ? ptree + r.first : nullptr, ctx->d_list + r.first, r.second, overwrite != 0, ctx->stream);
+            ctx->launches += r.second > 0;
+        }
+    } else {
+        for (int l = (int)ranges.size() - 1; l >= 0; l--) {
+            launch_mw_up(m, t0, ts, ptree ? ptree + ranges[l].first : nullptr, ctx->d_list + ranges[l].first, ranges[l].second, ctx->stream);
+            ctx->launches += ranges[l].second > 0;
+        }
+    }
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaStreamSynchronize(ctx->stream));
+    return MWGPU_OK;
+}
+
+// Validation shared by the single-tree, batched and planned level calls;
+// groups the work entries by tree (stable).
+mwgpu_status make_level(mwgpu_ctx *ctx, const mwgpu_oper *o, int nt, mwgpu_tree *const *inps, mwgpu_tree *const *outs, const int *work_tree,
+                        const int *node_ix, int n, Level &lv) {
+    MW_ARG(o, "invalid operator or trees");
+    for (int t = 0; t < nt; t++) {
+        MW_ARG(inps[t] && outs[t] && inps[t]->is_input && !outs[t]->is_input, "invalid operator or trees");
+        MW_ARG(inps[t]->mra.K == o->op.K && outs[t]->mra.K == o->op.K, "order mismatch");
+        for (int u = 0; u < t; u++) MW_ARG(inps[u] != inps[t] && outs[u] != outs[t], "trees of a batch must be distinct");
+        MW_ARG(inps[t]->plans == 0 && outs[t]->plans == 0, "tree is held by a plan (destroy the plan first)");
+    }
+    MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
+    if (ctx->precision == MWGPU_PREC_MIXED && !mixed_supported(o->op.K)) {
+        ctx->err = "mixed form supports orders k = 1..11";
+        return MWGPU_ERR_BAD_ARG;
+    }
+    lv.o = o;
+    lv.nt = nt;
+    lv.inps = inps;
+    lv.outs = outs;
+    lv.n = n;
+    lv.seg.assign(nt + 1, 0);
+    for (int i = 0; i < n; i++) {
+        const int t = work_tree ? work_tree[i] : 0;
+        MW_ARG(t >= 0 && t < nt, "work tree index out of range");
+        MW_ARG(node_ix[i] >= 0 && node_ix[i] < outs[t]->t.n_real, "node index out of range");
+        lv.seg[t + 1]++;
+    }
+    for (int t = 0; t < nt; t++) lv.seg[t + 1] += lv.seg[t];
+    lv.node.resize(n);
+    lv.tree.resize(n);
+    lv.order.resize(n);
+    std::vector<int> pos(lv.seg.begin(), lv.seg.end() - 1);
+    for (int i = 0; i < n; i++) {
+        const int t = work_tree ? work_tree[i] : 0;
+        const int j = pos[t]++;
+        lv.node[j] = node_ix[i];
+        lv.tree[j] = t;
+        lv.order[j] = i;
+    }
+    return MWGPU_OK;
+}
+
+mwgpu_status level_entry(mwgpu_ctx *ctx, const mwgpu_oper *o, int nt, mwgpu_tree *const *inps, mwgpu_tree *const *outs, const int *work_tree,
+                         const int *node_ix, int n, double prec, const double *sqnorms, double *norms_out, mwgpu_level_stats *stats) {
+    Level lv;
+    if (auto s = make_level(ctx, o, nt, inps, outs, work_tree, node_ix, n, lv)) return s;
+    cudaSetDevice(ctx->device);
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (n == 0) return MWGPU_OK;
+    return level_run(ctx, lv, sqnorms, prec, norms_out, stats);
+}
+
+}  // namespace
+
 extern "C" {
 
 mwgpu_status mwgpu_init(mwgpu_ctx **out, const mwgpu_config *cfg) {
@@ -453,8 +679,7 @@ mwgpu_status mwgpu_init(mwgpu_ctx **out, const mwgpu_config *cfg) {
     }
     if (cudaSetDevice(ctx->device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess || cudaEventCreate(&ctx->ev2) != cudaSuccess ||
-        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, sizeof(LevelStats)) != cudaSuccess ||
-        cudaMalloc(&ctx->d_pcount, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, sizeof(LevelStats)) != cudaSuccess) {
         g_init_error = std::string("device initialisation failed: ") + cudaGetErrorString(cudaGetLastError());
         delete ctx;
         return MWGPU_ERR_DEVICE;
@@ -471,11 +696,13 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
                     (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_chunks,
                     (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
-                    (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff})
+                    (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
+                    (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_nstage, (void *)ctx->d_ltree})
         if (p) cudaFree(p);
     for (auto &e : ctx->marks)
         if (e) cudaEventDestroy(e);
     if (ctx->d_scrub) cudaFree(ctx->d_scrub);
+    if (ctx->d_arena) cudaFree(ctx->d_arena);
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev2);
@@ -640,6 +867,7 @@ mwgpu_status mwgpu_tree_add_nodes(mwgpu_ctx *ctx, mwgpu_tree *tr, int n, const i
                                   const int *parent_child0) {
     if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
     MW_ARG(!tr->is_input, "cannot add nodes to an input tree");
+    MW_ARG(tr->plans == 0, "tree is held by a plan (destroy the plan first)");
     MW_ARG(n >= 0 && (n == 0 || idx), "invalid node list");
     cudaSetDevice(ctx->device);
     DevTree &t = tr->t;
@@ -674,6 +902,7 @@ mwgpu_status mwgpu_tree_size(const mwgpu_tree *tr, int *n) {
 
 mwgpu_status mwgpu_free_tree(mwgpu_ctx *ctx, mwgpu_tree *tr) {
     if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(tr->plans == 0, "tree is held by a plan (destroy the plan first)");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     free_tree(tr);
@@ -683,129 +912,29 @@ mwgpu_status mwgpu_free_tree(mwgpu_ctx *ctx, mwgpu_tree *tr) {
 mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n,
                                double prec, double out_sqnorm, double *norms_out, mwgpu_level_stats *stats) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
-    MW_ARG(o && inp && out && inp->is_input && !out->is_input, "invalid operator or trees");
-    MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
-    MW_ARG(inp->mra.K == o->op.K && out->mra.K == o->op.K, "order mismatch");
-    cudaSetDevice(ctx->device);
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    if (n == 0) return MWGPU_OK;
-    for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < out->t.n_real, "node index out of range");
-    if (auto s = ensure_work(ctx, n)) return s;
-    MW_CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    MW_CK(cudaMemcpyAsync(ctx->d_work, node_ix, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
-    MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
-    MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
-    // GenNodes needed by the operator bands of this level
-    int pcount = 0;
-    for (int attempt = 0; attempt < 8; attempt++) {
-        if (auto s = ensure_pending(ctx, std::max(ctx->phcap, 1 << 16), std::max(ctx->pcap, 1 << 15))) return s;
-        MW_CK(cudaMemsetAsync(ctx->d_pkeys, 0xFF, sizeof(uint64_t) * ctx->phcap, ctx->stream));
-        MW_CK(cudaMemsetAsync(ctx->d_pcount, 0, sizeof(int), ctx->stream));
-        launch_band_missing(o->mra, o->op, inp->t, out->t, ctx->d_work, n, ctx->d_pkeys, ctx->d_pvals, ctx->phcap, ctx->d_plist,
-                            ctx->d_pcount, ctx->pcap, ctx->d_err, ctx->stream);
-        ctx->launches++;
-        int herr = 0;
-        MW_CK(cudaMemcpyAsync(&pcount, ctx->d_pcount, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        MW_CK(cudaMemcpyAsync(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        MW_CK(cudaStreamSynchronize(ctx->stream));
-        if (herr & DE_RANGE) { ctx->err = "band index outside the lookup range"; return MWGPU_ERR_INTERNAL; }
-        bool hfull = herr & DE_HASH_FULL;
-        if (!hfull && pcount <= ctx->pcap) break;
-        MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
-        if (auto s = ensure_pending(ctx, hfull ? ctx->phcap * 4 : next_pow2(4LL * pcount), std::max(pcount + 1024, ctx->pcap))) return s;
-        if (attempt == 7) { ctx->err = "pending GenNode set did not fit"; return MWGPU_ERR_OOM; }
-    }
-    if (pcount > 0) {
-        DevTree &f = inp->t;
-        if (auto s = grow_gen(ctx, inp, f.n_gen + pcount)) return s;
-        if (2LL * (f.n_real + f.n_gen + pcount) + 16 > f.hcap)
-            if (auto s = rebuild_hash(ctx, inp, (long long)f.n_real + f.n_gen + pcount)) return s;
-        launch_gen_nodes(inp->mra, f, ctx->d_plist, pcount, f.n_gen, ctx->d_err, ctx->stream);
-        launch_gen_insert(inp->mra, f, ctx->d_plist, pcount, f.n_gen, ctx->d_err, ctx->stream);
-        ctx->launches += 2;
-        f.n_gen += pcount;
-    }
-    double gthr = out_sqnorm;
-    if (gthr > 0.0) gthr = prec * 1.0 * std::sqrt(gthr / (double)o->op.n_terms);
-    if (ctx->precision == MWGPU_PREC_MIXED && !mixed_supported(o->op.K)) {
-        ctx->err = "mixed form supports orders k = 1..11";
-        return MWGPU_ERR_BAD_ARG;
-    }
-    LevelStats mixed_nt{};
-    if (ctx->precision == MWGPU_PREC_MIXED) {
-        if (auto s = run_mixed(ctx, o, inp, out, ctx->d_work, node_ix, n, gthr, &mixed_nt)) return s;
-    } else {
-        MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
-        launch_contract_fp64(o->mra, o->op, inp->t, out->t, ctx->d_work, n, gthr, ctx->d_stats, ctx->d_err, ctx->stream);
-        ctx->launches++;
-    }
-    MW_CK(cudaGetLastError());
-    MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
-    LevelStats hs{};
-    MW_CK(cudaMemcpyAsync(&hs, ctx->d_stats, sizeof(LevelStats), cudaMemcpyDeviceToHost, ctx->stream));
-    if (norms_out) {
-        // gather the norms of the computed nodes
-        std::vector<double> all((size_t)out->t.n_real * 8);
-        MW_CK(cudaMemcpyAsync(all.data(), out->t.norms, sizeof(double) * all.size(), cudaMemcpyDeviceToHost, ctx->stream));
-        if (auto s = check_err(ctx, "apply_level")) return s;
-        for (int i = 0; i < n; i++) std::memcpy(norms_out + 8 * (size_t)i, &all[(size_t)node_ix[i] * 8], sizeof(double) * 8);
-    } else if (auto s = check_err(ctx, "apply_level")) {
-        return s;
-    }
-    if (ctx->precision == MWGPU_PREC_MIXED) hs.node_terms = mixed_nt.node_terms;
-    if (stats) {
-        stats->node_terms = hs.node_terms;
-        stats->components = hs.components;
-        stats->band_nodes = hs.band_nodes;
-        stats->gen_nodes = (unsigned long long)pcount;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev2);
-        stats->device_ms = ms;
-        cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2);
-        stats->contract_ms = ms;
-    }
-    return MWGPU_OK;
+    mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
+    return level_entry(ctx, o, 1, inps, outs, nullptr, node_ix, n, prec, &out_sqnorm, norms_out, stats);
+}
+
+mwgpu_status mwgpu_apply_level_batch(mwgpu_ctx *ctx, const mwgpu_oper *o, int n_trees, mwgpu_tree *const *inps, mwgpu_tree *const *outs,
+                                     const int *work_tree, const int *node_ix, int n, double prec, const double *out_sqnorms,
+                                     double *norms_out, mwgpu_level_stats *stats) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n_trees >= 1 && inps && outs && out_sqnorms, "invalid tree arrays");
+    MW_ARG(n == 0 || work_tree, "null work_tree");
+    return level_entry(ctx, o, n_trees, inps, outs, work_tree, node_ix, n, prec, out_sqnorms, norms_out, stats);
 }
 
 mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tr, int direction, int overwrite) {
     if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
-    MW_ARG(direction == MWGPU_TOPDOWN || direction == MWGPU_BOTTOMUP, "invalid transform direction");
-    MW_ARG(!(direction == MWGPU_BOTTOMUP && !overwrite), "BottomUp transform always overwrites");
-    cudaSetDevice(ctx->device);
-    const int n = tr->t.n_real;
-    // parents per depth (breadth-first order from the roots)
-    std::vector<int> depth(n, -1);
-    std::vector<std::vector<int>> levels;
-    for (int i = 0; i < n; i++) depth[i] = tr->h_idx[i].x - tr->mra.root_scale;
-    int maxd = 0;
-    for (int i = 0; i < n; i++) maxd = std::max(maxd, depth[i]);
-    levels.resize(maxd + 1);
-    for (int i = 0; i < n; i++)
-        if (tr->h_child0[i] >= 0 && depth[i] >= 0) levels[depth[i]].push_back(i);
-    std::vector<int> flat;
-    std::vector<std::pair<int, int>> ranges;
-    for (auto &l : levels) { ranges.push_back({(int)flat.size(), (int)l.size()}); flat.insert(flat.end(), l.begin(), l.end()); }
-    if (flat.empty()) return MWGPU_OK;
-    if ((int)flat.size() > ctx->list_cap) {
-        if (ctx->d_list) cudaFree(ctx->d_list);
-        ctx->list_cap = (int)flat.size() * 2;
-        if (auto s = dev_alloc(ctx, &ctx->d_list, ctx->list_cap)) return s;
-    }
-    MW_CK(cudaMemcpyAsync(ctx->d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, ctx->stream));
-    if (direction == MWGPU_TOPDOWN) {
-        for (auto &r : ranges) {
-            launch_mw_down(tr->mra, tr->t, ctx->d_list + r.first, r.second, overwrite != 0, ctx->stream);
-            ctx->launches += r.second > 0;
-        }
-    } else {
-        for (int l = (int)ranges.size() - 1; l >= 0; l--) {
-            launch_mw_up(tr->mra, tr->t, ctx->d_list + ranges[l].first, ranges[l].second, ctx->stream);
-            ctx->launches += ranges[l].second > 0;
-        }
-    }
-    MW_CK(cudaGetLastError());
-    MW_CK(cudaStreamSynchronize(ctx->stream));
-    return MWGPU_OK;
+    mwgpu_tree *trees[1] = {tr};
+    return transform_impl(ctx, 1, trees, direction, overwrite);
+}
+
+mwgpu_status mwgpu_transform_batch(mwgpu_ctx *ctx, int n_trees, mwgpu_tree *const *trees, int direction, int overwrite) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n_trees >= 1 && trees, "invalid tree array");
+    return transform_impl(ctx, n_trees, trees, direction, overwrite);
 }
 
 mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tr, double *coefs, double *norms) {
@@ -824,9 +953,40 @@ mwgpu_status mwgpu_sync(mwgpu_ctx *ctx) {
     return MWGPU_OK;
 }
 
+mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tr, const double *coefs, const double *norms) {
+    if (!ctx || !tr || !coefs) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(tr->is_input, "only input trees take new coefficients");
+    cudaSetDevice(ctx->device);
+    DevTree &t = tr->t;
+    const int n = t.n_real;
+    const size_t nc = 8 * (size_t)tr->mra.kp1_d;
+    MW_CK(cudaMemcpyAsync(t.coefs, coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
+    launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
+    ctx->launches++;
+    if (norms) {
+        MW_CK(cudaMemcpyAsync(t.norms, norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        std::vector<int> all(n);
+        for (int i = 0; i < n; i++) all[i] = i;
+        if (auto s = ensure_work(ctx, n)) return s;
+        MW_CK(cudaMemcpyAsync(ctx->d_work, all.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+        launch_node_norms(tr->mra, t, ctx->d_work, n, ctx->stream);
+        ctx->launches++;
+    }
+    MW_CK(cudaStreamSynchronize(ctx->stream));
+    // GenNodes hold values of the old coefficients: a plan recomputes its own,
+    // otherwise they are dropped and made again by the next level
+    if (tr->plans == 0 && t.n_gen > 0) {
+        t.n_gen = 0;
+        return rebuild_hash(ctx, tr, n);
+    }
+    return MWGPU_OK;
+}
+
 mwgpu_status mwgpu_tree_clear_generated(mwgpu_ctx *ctx, mwgpu_tree *tr) {
     if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
     MW_ARG(tr->is_input, "only input trees hold GenNodes");
+    MW_ARG(tr->plans == 0, "tree is held by a plan (destroy the plan first)");
     cudaSetDevice(ctx->device);
     if (tr->t.n_gen == 0) return MWGPU_OK;
     tr->t.n_gen = 0;
@@ -985,6 +1145,680 @@ extern "C" mwgpu_status mwgpu_apply_level_static(mwgpu_ctx *ctx, const mwgpu_ope
         stats->device_ms = ms;
         cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2);
         stats->contract_ms = ms;
+    }
+    return MWGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Level plans: one level over a batch of trees whose node lists stay fixed
+// (apply with maxIter = 0 onto given output grids, or the repeated applies of
+// a fixed-grid SCF loop).  What depends only on the topology is prepared once:
+// the GenNode keys and slots, the band pair offsets, buffer capacities and the
+// chunk length (chosen by timing candidates).  What depends on values -- the
+// GenNode coefficients, screening and work list, contraction, reduction,
+// norms and the transforms -- is captured as one CUDA graph and recomputed on
+// every execution.
+// ---------------------------------------------------------------------------
+struct mwgpu_plan {
+    const mwgpu_oper *o = nullptr;
+    int nt = 0, n = 0, precision = 0, flags = 0;
+    std::vector<mwgpu_tree *> inps, outs;
+    std::vector<int> seg;
+    std::vector<double> gthr;
+    std::vector<void *> allocs;
+    int *d_work = nullptr, *d_wtree = nullptr;
+    DevTree *d_fs = nullptr, *d_gs = nullptr;
+    double *d_gthr = nullptr;
+    long long np = 0;
+    long long *d_pair_off = nullptr, *d_item_off = nullptr, *d_scan = nullptr, *d_goff = nullptr, *d_coff = nullptr, *d_cscan = nullptr;
+    long long scan_n = 0, cscan_n = 0;
+    int *d_pcounts = nullptr, *d_ccount = nullptr;
+    WorkItem *d_items = nullptr;
+    long long items_cap = 0;
+    int4 *d_chunks = nullptr;
+    int *d_chunk_begin = nullptr, *d_nchunks = nullptr, *d_counter = nullptr;
+    int chunks_cap = 0;
+    double *d_partial = nullptr;
+    LevelStats *d_stats = nullptr;
+    int *d_err = nullptr;
+    unsigned long long *d_stamps = nullptr;  // level start, contraction start / end, level end (ns)
+    std::vector<uint64_t *> d_gkeys;
+    std::vector<int> gcount;
+    int *d_list = nullptr, *d_ltree = nullptr;
+    std::vector<std::pair<int, int>> ranges;
+    long long per = 0;
+    int grid = 0;
+    cudaEvent_t e1 = nullptr, e2 = nullptr;  // autotuning timers (outside the graph)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long launches_per_exec = 0;
+    std::vector<double> tune_ms;  // per candidate, ms per million items
+    std::vector<long long> tune_per;
+};
+
+namespace {
+
+template <class T> mwgpu_status plan_alloc(mwgpu_ctx *ctx, mwgpu_plan *pl, T **p, size_t n) {
+    if (auto s = dev_alloc(ctx, p, n)) return s;
+    pl->allocs.push_back((void *)*p);
+    return MWGPU_OK;
+}
+
+void plan_free(mwgpu_plan *pl) {
+    if (!pl) return;
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    for (cudaEvent_t e : {pl->e1, pl->e2})
+        if (e) cudaEventDestroy(e);
+    for (void *p : pl->allocs) cudaFree(p);
+    delete pl;
+}
+
+// chunking + contraction + reduction of a planned mixed level (no host sync)
+void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
+    const mwgpu_oper *o = pl->o;
+    cudaStream_t st = ctx->stream;
+    launch_chunk_count(pl->d_goff, pl->n, per, pl->d_ccount, st);
+    launch_scan(pl->d_ccount, pl->d_coff, pl->n, pl->d_cscan, pl->d_cscan + (pl->cscan_n - 1), st);
+    launch_chunk_fill(pl->d_goff, pl->d_coff, pl->n, per, pl->d_chunks, pl->d_chunk_begin, pl->chunks_cap, pl->d_nchunks, pl->d_err, st);
+    cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st);
+    if (reduce) launch_stamp(pl->d_stamps + 1, st);
+    else cudaEventRecord(pl->e1, st);
+    launch_items(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_chunks, pl->grid, pl->d_items, pl->d_partial, pl->d_err,
+                 pl->d_nchunks, pl->d_counter, st);
+    if (reduce) launch_reduce_chunks(o->mra, pl->d_gs, pl->d_wtree, pl->d_work, pl->n, pl->d_chunk_begin, pl->d_partial, st);
+    ctx->launches += 6 + (reduce ? 2 : 0);
+}
+
+// the whole level on the context stream, without host synchronisation
+void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
+    const mwgpu_oper *o = pl->o;
+    cudaStream_t st = ctx->stream;
+    launch_stamp(pl->d_stamps + 0, st);
+    ctx->launches++;
+    cudaMemsetAsync(pl->d_err, 0, sizeof(int), st);
+    cudaMemsetAsync(pl->d_stats, 0, sizeof(LevelStats), st);
+    // GenNode values from the current input coefficients (slots fixed at plan time)
+    for (int t = 0; t < pl->nt; t++) {
+        if (pl->gcount[t] == 0) continue;
+        launch_gen_nodes(pl->inps[t]->mra, pl->inps[t]->t, pl->d_gkeys[t], pl->gcount[t], 0, pl->d_err, st, true);
+        ctx->launches++;
+    }
+    if (pl->precision == MWGPU_PREC_MIXED) {
+        LevelStats *dst = pl->d_stats;
+        launch_pairs_count(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
+                           &dst->components, &dst->band_nodes, pl->d_err, st);
+        launch_scan(pl->d_pcounts, pl->d_item_off, pl->np, pl->d_scan, pl->d_scan + (pl->scan_n - 1), st);
+        launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st);
+        launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_item_off,
+                          pl->d_items, pl->items_cap, pl->d_err, st);
+        ctx->launches += 6;
+        plan_contract(ctx, pl, pl->per, true);
+    } else {
+        launch_stamp(pl->d_stamps + 1, st);
+        ctx->launches++;
+        for (int t = 0; t < pl->nt; t++) {
+            const int b = pl->seg[t], e = pl->seg[t + 1];
+            if (b == e) continue;
+            launch_contract_fp64(o->mra, o->op, pl->inps[t]->t, pl->outs[t]->t, pl->d_work + b, e - b, pl->gthr[t], pl->d_stats, pl->d_err, st);
+            ctx->launches++;
+        }
+    }
+    launch_stamp(pl->d_stamps + 2, st);
+    ctx->launches++;
+    if (pl->flags & MWGPU_PLAN_TRANSFORMS) {
+        const mwgpu_tree *t0 = pl->outs[0];
+        for (auto &r : pl->ranges) {
+            launch_mw_down(t0->mra, t0->t, pl->d_gs, pl->d_ltree + r.first, pl->d_list + r.first, r.second, false, st);
+            ctx->launches += r.second > 0;
+        }
+        for (int l = (int)pl->ranges.size() - 1; l >= 0; l--) {
+            launch_mw_up(t0->mra, t0->t, pl->d_gs, pl->d_ltree + pl->ranges[l].first, pl->d_list + pl->ranges[l].first, pl->ranges[l].second, st);
+            ctx->launches += pl->ranges[l].second > 0;
+        }
+    }
+    launch_stamp(pl->d_stamps + 3, st);
+    ctx->launches++;
+}
+
+mwgpu_status plan_check(mwgpu_ctx *ctx, mwgpu_plan *pl, mwgpu_level_stats *stats) {
+    int herr = 0;
+    LevelStats hs{};
+    long long total = 0;
+    unsigned long long stamps[4] = {0, 0, 0, 0};
+    MW_CK(cudaMemcpyAsync(stamps, pl->d_stamps, sizeof(stamps), cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaMemcpyAsync(&herr, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaMemcpyAsync(&hs, pl->d_stats, sizeof(LevelStats), cudaMemcpyDeviceToHost, ctx->stream));
+    if (pl->precision == MWGPU_PREC_MIXED)
+        MW_CK(cudaMemcpyAsync(&total, pl->d_goff + pl->n, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaStreamSynchronize(ctx->stream));
+    if (herr & DE_POOL_FULL) {
+        ctx->err = "plan: the work list outgrew the planned capacity (input values changed the screening); create a new plan";
+        return MWGPU_ERR_OOM;
+    }
+    if (herr) {
+        ctx->err = "plan: device error flags " + std::to_string(herr);
+        return MWGPU_ERR_INTERNAL;
+    }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->node_terms = pl->precision == MWGPU_PREC_MIXED ? (unsigned long long)total : hs.node_terms;
+        stats->components = hs.components;
+        stats->band_nodes = hs.band_nodes;
+        unsigned long long g = 0;
+        for (int c : pl->gcount) g += c;
+        stats->gen_nodes = g;
+        stats->device_ms = (double)(stamps[3] - stamps[0]) * 1e-6;
+        stats->contract_ms = (double)(stamps[2] - stamps[1]) * 1e-6;
+    }
+    return MWGPU_OK;
+}
+
+}  // namespace
+
+extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, int n_trees, mwgpu_tree *const *inps, mwgpu_tree *const *outs,
+                                          const int *work_tree, const int *node_ix, int n, double prec, const double *out_sqnorms, int flags,
+                                          mwgpu_plan **out) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(out && n_trees >= 1 && inps && outs && out_sqnorms, "invalid plan arguments");
+    MW_ARG(n > 0, "a plan needs at least one node");
+    *out = nullptr;
+    Level lv;
+    if (auto s = make_level(ctx, o, n_trees, inps, outs, work_tree, node_ix, n, lv)) return s;
+    cudaSetDevice(ctx->device);
+    if (flags & MWGPU_PLAN_TRANSFORMS) {
+        // the transforms rewrite every node: the plan must compute all of them
+        for (int t = 0; t < n_trees; t++) {
+            const int cnt = lv.seg[t + 1] - lv.seg[t];
+            MW_ARG(cnt == outs[t]->t.n_real, "a plan with transforms must compute every node of its output trees");
+            std::vector<char> seen(outs[t]->t.n_real, 0);
+            for (int j = lv.seg[t]; j < lv.seg[t + 1]; j++) {
+                MW_ARG(!seen[lv.node[j]], "a node appears twice in the plan");
+                seen[lv.node[j]] = 1;
+            }
+        }
+    }
+    for (int t = 0; t < n_trees; t++)
+        MW_ARG(outs[t]->h_filt == outs[0]->h_filt && outs[t]->mra.root_scale == outs[0]->mra.root_scale, "trees of a plan need the same MRA");
+    // a fresh GenNode set that belongs to the plan
+    for (int t = 0; t < n_trees; t++)
+        if (inps[t]->t.n_gen > 0) {
+            inps[t]->t.n_gen = 0;
+            if (auto s = rebuild_hash(ctx, inps[t], inps[t]->t.n_real)) return s;
+        }
+    // eager level: makes the GenNodes, gives the work-list size and the result
+    std::vector<int> pcount;
+    mwgpu_level_stats st0{};
+    if (auto s = level_run(ctx, lv, out_sqnorms, prec, nullptr, &st0, &pcount)) return s;
+
+    auto *pl = new mwgpu_plan();
+    pl->o = o;
+    pl->nt = n_trees;
+    pl->n = n;
+    pl->precision = ctx->precision;
+    pl->flags = flags;
+    pl->inps.assign(inps, inps + n_trees);
+    pl->outs.assign(outs, outs + n_trees);
+    pl->seg = lv.seg;
+    pl->gthr = lv.gthr;
+    auto fail = [&](mwgpu_status s) {
+        plan_free(pl);
+        return s;
+    };
+    mwgpu_status s;
+    if ((s = plan_alloc(ctx, pl, &pl->d_work, n)) || (s = plan_alloc(ctx, pl, &pl->d_wtree, n)) || (s = plan_alloc(ctx, pl, &pl->d_fs, n_trees)) ||
+        (s = plan_alloc(ctx, pl, &pl->d_gs, n_trees)) || (s = plan_alloc(ctx, pl, &pl->d_gthr, n_trees)) ||
+        (s = plan_alloc(ctx, pl, &pl->d_stats, 1)) || (s = plan_alloc(ctx, pl, &pl->d_err, 1)) || (s = plan_alloc(ctx, pl, &pl->d_stamps, 4)))
+        return fail(s);
+    if (cudaEventCreate(&pl->e1) != cudaSuccess || cudaEventCreate(&pl->e2) != cudaSuccess) {
+        ctx->err = "plan: event creation failed";
+        return fail(MWGPU_ERR_DEVICE);
+    }
+    MW_CK(cudaMemcpyAsync(pl->d_work, lv.node.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(pl->d_wtree, lv.tree.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(pl->d_fs, lv.fs.data(), sizeof(DevTree) * n_trees, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(pl->d_gs, lv.gs.data(), sizeof(DevTree) * n_trees, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(pl->d_gthr, lv.gthr.data(), sizeof(double) * n_trees, cudaMemcpyHostToDevice, ctx->stream));
+    // GenNode keys of every input tree (slots 0 .. count-1 after the reset above)
+    pl->gcount = pcount;
+    pl->d_gkeys.assign(n_trees, nullptr);
+    for (int t = 0; t < n_trees; t++) {
+        if (pcount[t] == 0) continue;
+        if ((s = plan_alloc(ctx, pl, &pl->d_gkeys[t], pcount[t]))) return fail(s);
+        MW_CK(cudaMemcpyAsync(pl->d_gkeys[t], ctx->d_plist + (size_t)t * ctx->pcap, sizeof(uint64_t) * pcount[t], cudaMemcpyDeviceToDevice,
+                              ctx->stream));
+    }
+    // transforms: parents per depth over all output trees
+    if (flags & MWGPU_PLAN_TRANSFORMS) {
+        std::vector<std::vector<int2>> levels;
+        for (int t = 0; t < n_trees; t++) {
+            const mwgpu_tree *tr = outs[t];
+            for (int i = 0; i < tr->t.n_real; i++) {
+                const int depth = tr->h_idx[i].x - tr->mra.root_scale;
+                if (tr->h_child0[i] < 0 || depth < 0) continue;
+                if ((int)levels.size() <= depth) levels.resize(depth + 1);
+                levels[depth].push_back(make_int2(t, i));
+            }
+        }
+        std::vector<int> flat, ftree;
+        for (auto &l : levels) {
+            pl->ranges.push_back({(int)flat.size(), (int)l.size()});
+            for (auto &e : l) {
+                ftree.push_back(e.x);
+                flat.push_back(e.y);
+            }
+        }
+        if ((s = plan_alloc(ctx, pl, &pl->d_list, flat.size())) || (s = plan_alloc(ctx, pl, &pl->d_ltree, flat.size()))) return fail(s);
+        if (!flat.empty()) {
+            MW_CK(cudaMemcpyAsync(pl->d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, ctx->stream));
+            MW_CK(cudaMemcpyAsync(pl->d_ltree, ftree.data(), sizeof(int) * ftree.size(), cudaMemcpyHostToDevice, ctx->stream));
+        }
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (pl->precision == MWGPU_PREC_MIXED) {
+        std::vector<long long> poff;
+        pair_offsets(lv, poff);
+        pl->np = poff[n];
+        const long long total = (long long)st0.node_terms;
+        pl->items_cap = total + total / 4 + 1024;
+        pl->scan_n = scan_blocks(pl->np + 1) + 2;
+        pl->cscan_n = scan_blocks(n + 1) + 2;
+        int dev_sm = 0;
+        cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, ctx->device);
+        const int res = std::max(1, contract_items_resident(o->op.K));
+        pl->grid = std::max(1, dev_sm) * res;
+        const long long per_min = std::max<long long>(4, pl->items_cap / (16LL * pl->grid) / 2);
+        const long long ccap = (long long)n + pl->items_cap / per_min + 1;
+        if (ccap > 0x7fffffffLL || pl->items_cap > 0x7fffffffLL) {
+            ctx->err = "plan: work list too large";
+            return fail(MWGPU_ERR_BAD_ARG);
+        }
+        pl->chunks_cap = (int)ccap;
+        if ((s = plan_alloc(ctx, pl, &pl->d_pair_off, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_pcounts, pl->np + 1)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_item_off, pl->np + 1)) || (s = plan_alloc(ctx, pl, &pl->d_scan, pl->scan_n)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_goff, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_ccount, n + 1)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_coff, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_cscan, pl->cscan_n)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_items, pl->items_cap)) || (s = plan_alloc(ctx, pl, &pl->d_chunks, pl->chunks_cap)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_chunk_begin, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_nchunks, 1)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_counter, 1)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_partial, (size_t)pl->chunks_cap * 8 * o->mra.kp1_d)))
+            return fail(s);
+        MW_CK(cudaMemcpyAsync(pl->d_pair_off, poff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        // chunk length: candidates around the default, each timed on the full
+        // contraction of this level (after one untimed work-list pass)
+        pl->per = std::max<long long>(8, (total + 8LL * pl->grid - 1) / (8LL * pl->grid));
+        plan_sequence(ctx, pl);
+        if ((s = plan_check(ctx, pl, nullptr))) return fail(s);
+        const bool tune = (flags & MWGPU_PLAN_AUTOTUNE) != 0 && total > 0;
+        if (tune) {
+            double best = 1e300;
+            long long best_per = pl->per;
+            for (int waves : {2, 4, 8, 16}) {
+                const long long per = std::max<long long>(per_min, (total + (long long)waves * pl->grid - 1) / ((long long)waves * pl->grid));
+                float ms = 0.f;
+                for (int rep = 0; rep < 2; rep++) {
+                    plan_contract(ctx, pl, per, false);
+                    MW_CK(cudaEventRecord(pl->e2, ctx->stream));
+                    MW_CK(cudaEventSynchronize(pl->e2));
+                    float m1 = 0.f;
+                    MW_CK(cudaEventElapsedTime(&m1, pl->e1, pl->e2));
+                    ms = rep == 0 ? m1 : std::min(ms, m1);
+                    if (m1 > 250.f) break;  // long launches: one timing is enough
+                }
+                pl->tune_per.push_back(per);
+                pl->tune_ms.push_back(ms);
+                if (ms < best) {
+                    best = ms;
+                    best_per = per;
+                }
+            }
+            pl->per = best_per;
+            // the trees hold what every execution leaves (same chunking)
+            plan_sequence(ctx, pl);
+            if ((s = plan_check(ctx, pl, nullptr))) return fail(s);
+        }
+    } else {
+        // one eager pass: the trees hold what every execution leaves (with the transforms)
+        plan_sequence(ctx, pl);
+        if ((s = plan_check(ctx, pl, nullptr))) return fail(s);
+    }
+    // capture the level as one graph
+    unsigned long long l0 = ctx->launches;
+    MW_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+    plan_sequence(ctx, pl);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &pl->graph);
+    pl->launches_per_exec = ctx->launches - l0;
+    ctx->launches = l0;
+    if (ce != cudaSuccess) {
+        ctx->err = std::string("plan: graph capture failed: ") + cudaGetErrorString(ce);
+        return fail(MWGPU_ERR_DEVICE);
+    }
+    ce = cudaGraphInstantiate(&pl->exec, pl->graph, 0);
+    if (ce != cudaSuccess) {
+        ctx->err = std::string("plan: graph instantiation failed: ") + cudaGetErrorString(ce);
+        return fail(MWGPU_ERR_DEVICE);
+    }
+    for (auto *t : pl->inps) t->plans++;
+    for (auto *t : pl->outs) t->plans++;
+    *out = pl;
+    return MWGPU_OK;
+}
+
+extern "C" mwgpu_status mwgpu_plan_execute(mwgpu_ctx *ctx, mwgpu_plan *pl, mwgpu_level_stats *stats) {
+    if (!ctx || !pl) return MWGPU_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    MW_CK(cudaGraphLaunch(pl->exec, ctx->stream));
+    ctx->launches += pl->launches_per_exec;
+    if (!stats) return MWGPU_OK;
+    return plan_check(ctx, pl, stats);
+}
+
+extern "C" mwgpu_status mwgpu_plan_check(mwgpu_ctx *ctx, mwgpu_plan *pl, mwgpu_level_stats *stats) {
+    if (!ctx || !pl) return MWGPU_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    return plan_check(ctx, pl, stats);
+}
+
+extern "C" mwgpu_status mwgpu_plan_info(const mwgpu_plan *pl, long long *chunk_items, int *grid, int *n_candidates, long long *cand_items,
+                                        double *cand_ms, unsigned long long *launches) {
+    if (!pl) return MWGPU_ERR_BAD_ARG;
+    if (chunk_items) *chunk_items = pl->per;
+    if (grid) *grid = pl->grid;
+    if (launches) *launches = pl->launches_per_exec;
+    if (n_candidates) {
+        const int nc = (int)pl->tune_per.size();
+        if (cand_items)
+            for (int i = 0; i < std::min(nc, *n_candidates); i++) cand_items[i] = pl->tune_per[i];
+        if (cand_ms)
+            for (int i = 0; i < std::min(nc, *n_candidates); i++) cand_ms[i] = pl->tune_ms[i];
+        *n_candidates = nc;
+    }
+    return MWGPU_OK;
+}
+
+extern "C" mwgpu_status mwgpu_plan_destroy(mwgpu_ctx *ctx, mwgpu_plan *pl) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    if (!pl) return MWGPU_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto *t : pl->inps) t->plans--;
+    for (auto *t : pl->outs) t->plans--;
+    plan_free(pl);
+    return MWGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Judged adaptive apply over a proposed output grid (mwgpu_apply_judged).
+// ---------------------------------------------------------------------------
+namespace {
+
+// bump allocator over ctx->d_arena: first a sizing pass (base == nullptr),
+// then the carving pass
+struct Carver {
+    char *base = nullptr;
+    size_t off = 0;
+    template <class T> T *take(size_t n) {
+        off = (off + 255) & ~(size_t)255;
+        T *p = base ? (T *)(base + off) : nullptr;
+        off += sizeof(T) * std::max<size_t>(n, 1);
+        return p;
+    }
+};
+
+}  // namespace
+
+extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, int n_levels,
+                                           const int *level_begin, double prec, int abs_prec, double out_sqnorm, int transforms,
+                                           int *flags_out, int *first_miss_out, double *sq_levels, mwgpu_level_stats *stats) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(o && inp && out && level_begin && flags_out && first_miss_out, "null argument");
+    MW_ARG(n_levels >= 1 && level_begin[0] == 0 && level_begin[n_levels] == out->t.n_real, "level ranges must cover the output tree");
+    for (int j = 0; j < n_levels; j++) MW_ARG(level_begin[j + 1] > level_begin[j], "empty proposal level");
+    const int N = out->t.n_real;
+    // levels and children: children of level j are consecutive in level j+1
+    for (int j = 0; j < n_levels; j++)
+        for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
+            const int c0 = out->h_child0[i];
+            MW_ARG(c0 < 0 || (c0 >= level_begin[j + 1] && j + 1 < n_levels && c0 + 8 <= level_begin[j + 2]),
+                   "proposed children must lie in the next level");
+        }
+    std::vector<int> all(N);
+    for (int i = 0; i < N; i++) all[i] = i;
+    mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
+    Level lv;
+    if (auto s = make_level(ctx, o, 1, inps, outs, nullptr, all.data(), N, lv)) return s;
+    cudaSetDevice(ctx->device);
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const bool mixed = ctx->precision == MWGPU_PREC_MIXED;
+    const DevMRA &m = o->mra;
+    if (auto s = ensure_work(ctx, N)) return s;
+    if (auto s = ensure_trees(ctx, 1)) return s;
+    MW_CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_work, all.data(), sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemsetAsync(ctx->d_wtree, 0, sizeof(int) * N, ctx->stream));
+    MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
+    // GenNodes for every proposed node (a superset of what the judged tree needs)
+    std::vector<int> pcount;
+    unsigned long long gen_total = 0;
+    if (auto s = gen_pass(ctx, lv, pcount, gen_total)) return s;
+    lv.fs.assign(1, inp->t);
+    lv.gs.assign(1, out->t);
+    MW_CK(cudaMemcpyAsync(ctx->d_fs, lv.fs.data(), sizeof(DevTree), cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_gs, lv.gs.data(), sizeof(DevTree), cudaMemcpyHostToDevice, ctx->stream));
+    // band pairs per proposed node; per level the largest counts any judged subset can reach
+    std::vector<long long> poff;
+    pair_offsets(lv, poff);
+    std::vector<int> cells(N);
+    for (int i = 0; i < N; i++) cells[i] = (int)(poff[i + 1] - poff[i]);
+    std::vector<long long> lvl_pairs(n_levels, 0), lvl_items(n_levels, 0);
+    for (int j = 0; j < n_levels; j++) lvl_pairs[j] = poff[level_begin[j + 1]] - poff[level_begin[j]];
+    int grid = 0, dev_sm = 0;
+    long long max_pairs = 0, max_items = 0, max_chunks = 0;
+    int max_level = 0;
+    for (int j = 0; j < n_levels; j++) max_level = std::max(max_level, level_begin[j + 1] - level_begin[j]);
+    for (auto v : lvl_pairs) max_pairs = std::max(max_pairs, v);
+    std::vector<long long> lvl_per(n_levels, 8);
+    if (mixed) {
+        // items per proposed node without norm screening (an upper bound of every level's work list)
+        if (auto s = grow_buf(ctx, &ctx->d_pair_off, &ctx->pair_off_cap, N + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_pcounts, &ctx->pcounts_cap, poff[N] + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_item_off, &ctx->item_off_cap, poff[N] + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_scan, &ctx->scan_cap, scan_blocks(poff[N] + 1) + 2)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_goff, &ctx->goff_cap, N + 1)) return s;
+        const double neg = -HUGE_VAL;
+        MW_CK(cudaMemcpyAsync(ctx->d_gthr, &neg, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_pair_off, poff.data(), sizeof(long long) * (N + 1), cudaMemcpyHostToDevice, ctx->stream));
+        LevelStats *dst = ctx->d_stats;
+        launch_pairs_count(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, N, poff[N], ctx->d_gthr, ctx->d_pcounts,
+                           &dst->components, &dst->band_nodes, ctx->d_err, ctx->stream);
+        launch_scan(ctx->d_pcounts, ctx->d_item_off, poff[N], ctx->d_scan, ctx->d_scan + (ctx->scan_cap - 1), ctx->stream);
+        launch_gather_goff(ctx->d_item_off, ctx->d_pair_off, N, ctx->d_goff, ctx->stream);
+        ctx->launches += 5;
+        std::vector<long long> ub(N + 1);
+        MW_CK(cudaMemcpyAsync(ub.data(), ctx->d_goff, sizeof(long long) * (N + 1), cudaMemcpyDeviceToHost, ctx->stream));
+        MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
+        if (auto s = check_err(ctx, "judged apply (work-list bound)")) return s;
+        cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, ctx->device);
+        grid = std::max(1, dev_sm) * std::max(1, contract_items_resident(o->op.K));
+        // chunk length from the level's item count on the device (the rule of
+        // the host-driven levels, so that both give the same sums): at most
+        // n + kChunkTarget + 1 chunks
+        for (int j = 0; j < n_levels; j++) {
+            lvl_items[j] = ub[level_begin[j + 1]] - ub[level_begin[j]];
+            lvl_per[j] = 0;
+            max_items = std::max(max_items, lvl_items[j]);
+            max_chunks = std::max(max_chunks, (long long)(level_begin[j + 1] - level_begin[j]) + kChunkTarget + 1);
+        }
+        if (max_items > 0x7fffffffLL || max_chunks > 0x7fffffffLL) {
+            ctx->err = "judged apply: work list too large";
+            return MWGPU_ERR_BAD_ARG;
+        }
+    }
+    // scratch, sized then carved
+    const int rows = std::max(m.max_scale - m.root_scale + 2, 1);
+    auto carve = [&](Carver &c) {
+        struct B {
+            int *flags, *kcnt, *work, *nwork, *ccnt, *pcounts, *chunk_begin, *nchunks, *counter, *first_miss, *cells;
+            long long *koff, *kscan, *pair_off, *pscan, *item_off, *iscan, *goff, *coff, *cscan;
+            int4 *chunks;
+            WorkItem *items;
+            double *partial, *state, *sq, *scale_fac;
+            unsigned long long *node_terms;
+        } b{};
+        b.flags = c.take<int>(N);
+        b.cells = c.take<int>(N);
+        b.kcnt = c.take<int>(max_level + 1);
+        b.koff = c.take<long long>(max_level + 1);
+        b.kscan = c.take<long long>(scan_blocks(max_level + 1) + 2);
+        b.work = c.take<int>(max_level + 1);
+        b.nwork = c.take<int>(1);
+        b.ccnt = c.take<int>(max_level + 1);
+        b.pair_off = c.take<long long>(max_level + 1);
+        b.pscan = c.take<long long>(scan_blocks(max_level + 1) + 2);
+        b.pcounts = c.take<int>(max_pairs + 1);
+        b.item_off = c.take<long long>(max_pairs + 1);
+        b.iscan = c.take<long long>(scan_blocks(max_pairs + 1) + 2);
+        b.goff = c.take<long long>(max_level + 1);
+        b.coff = c.take<long long>(max_level + 1);
+        b.cscan = c.take<long long>(scan_blocks(max_level + 1) + 2);
+        b.chunks = c.take<int4>(mixed ? max_chunks : 1);
+        b.chunk_begin = c.take<int>(max_level + 1);
+        b.nchunks = c.take<int>(1);
+        b.counter = c.take<int>(1);
+        b.items = c.take<WorkItem>(mixed ? max_items : 1);
+        b.partial = c.take<double>(mixed ? (size_t)max_chunks * 8 * m.kp1_d : 1);
+        b.state = c.take<double>(3);
+        b.sq = c.take<double>(n_levels);
+        b.scale_fac = c.take<double>(rows);
+        b.first_miss = c.take<int>(1);
+        b.node_terms = c.take<unsigned long long>(1);
+        return b;
+    };
+    Carver sizing;
+    carve(sizing);
+    if (sizing.off > ctx->arena_bytes) {
+        if (ctx->d_arena) cudaFree(ctx->d_arena);
+        ctx->d_arena = nullptr;
+        ctx->arena_bytes = 0;
+        MW_CK(cudaMalloc(&ctx->d_arena, sizing.off));
+        ctx->arena_bytes = sizing.off;
+    }
+    Carver cv;
+    cv.base = (char *)ctx->d_arena;
+    auto b = carve(cv);
+    // initial state: the roots are kept; tree norm of the fresh output tree
+    std::vector<int> h_flags(N, 0);
+    for (int i = level_begin[0]; i < level_begin[1]; i++) h_flags[i] = 1;
+    std::vector<double> fac(rows);
+    for (int d = 0; d < rows; d++) fac[d] = std::pow(2.0, -(0.5 * 1.0 * (m.root_scale + d + 1)));
+    const double state0[3] = {0.0, 0.0, out_sqnorm};
+    const int big = 0x7fffffff;
+    MW_CK(cudaMemcpyAsync(b.flags, h_flags.data(), sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(b.cells, cells.data(), sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(b.scale_fac, fac.data(), sizeof(double) * rows, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(b.state, state0, sizeof(state0), cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(b.first_miss, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemsetAsync(b.node_terms, 0, sizeof(unsigned long long), ctx->stream));
+    MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    cudaStream_t st = ctx->stream;
+    const int T = o->op.n_terms;
+    for (int j = 0; j < n_levels; j++) {
+        const int lb = level_begin[j], nl = level_begin[j + 1] - lb;
+        launch_keep_counts(b.flags, lb, nl, b.kcnt, st);
+        launch_scan(b.kcnt, b.koff, nl, b.kscan, b.kscan + (scan_blocks(max_level + 1) + 1), st);
+        launch_compact(b.flags, lb, nl, b.koff, b.work, b.nwork, st);
+        launch_threshold(b.state + 2, prec, T, ctx->d_gthr, st);
+        ctx->launches += 6;
+        if (mixed) {
+            const long long pc = lvl_pairs[j];
+            launch_cells(b.work, b.nwork, nl, b.cells, b.ccnt, st);
+            launch_scan(b.ccnt, b.pair_off, nl, b.pscan, b.pscan + (scan_blocks(max_level + 1) + 1), st);
+            const long long *np_dev = b.pair_off + nl;
+            LevelStats *dst = ctx->d_stats;
+            launch_pairs_count(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.pcounts, &dst->components,
+                               &dst->band_nodes, ctx->d_err, st, np_dev, b.nwork);
+            launch_scan(b.pcounts, b.item_off, pc, b.iscan, b.iscan + (scan_blocks(max_pairs + 1) + 1), st);
+            launch_gather_goff(b.item_off, b.pair_off, nl, b.goff, st, b.nwork);
+            launch_chunk_count(b.goff, nl, lvl_per[j], b.ccnt, st, b.nwork);
+            launch_scan(b.ccnt, b.coff, nl, b.cscan, b.cscan + (scan_blocks(max_level + 1) + 1), st);
+            const int ccap = (int)((long long)nl + kChunkTarget + 1);
+            launch_chunk_fill(b.goff, b.coff, nl, lvl_per[j], b.chunks, b.chunk_begin, ccap, b.nchunks, ctx->d_err, st, b.nwork);
+            launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.item_off, b.items,
+                              lvl_items[j], ctx->d_err, st, np_dev, b.nwork);
+            MW_CK(cudaMemsetAsync(b.counter, 0, sizeof(int), st));
+            launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,
+                         st);
+            launch_reduce_chunks(m, ctx->d_gs, ctx->d_wtree, b.work, nl, b.chunk_begin, b.partial, st, b.nwork);
+            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + j, b.goff, b.node_terms, st);
+            ctx->launches += 17;
+        } else {
+            launch_contract_fp64(m, o->op, inp->t, out->t, b.work, nl, 0.0, ctx->d_stats, ctx->d_err, st, b.nwork, ctx->d_gthr);
+            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + j, nullptr, nullptr, st);
+            ctx->launches += 2;
+        }
+        launch_judge(m, out->t, b.work, b.nwork, nl, b.state, prec, abs_prec, b.scale_fac, m.max_scale, b.flags, j, b.first_miss, st);
+        ctx->launches++;
+    }
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
+    int first_miss = big;
+    unsigned long long nt_mixed = 0;
+    LevelStats hs{};
+    MW_CK(cudaMemcpyAsync(flags_out, b.flags, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+    MW_CK(cudaMemcpyAsync(&first_miss, b.first_miss, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MW_CK(cudaMemcpyAsync(&nt_mixed, b.node_terms, sizeof(nt_mixed), cudaMemcpyDeviceToHost, st));
+    MW_CK(cudaMemcpyAsync(&hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    std::vector<double> sqv(n_levels);
+    MW_CK(cudaMemcpyAsync(sqv.data(), b.sq, sizeof(double) * n_levels, cudaMemcpyDeviceToHost, st));
+    if (auto s = check_err(ctx, "judged apply")) return s;
+    if (sq_levels) std::memcpy(sq_levels, sqv.data(), sizeof(double) * n_levels);
+    *first_miss_out = first_miss == big ? -1 : first_miss;
+    if (stats) {
+        stats->node_terms = mixed ? nt_mixed : hs.node_terms;
+        stats->components = hs.components;
+        stats->band_nodes = hs.band_nodes;
+        stats->gen_nodes = gen_total;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev2);
+        stats->device_ms = ms;
+        cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2);
+        stats->contract_ms = ms;
+    }
+    if (transforms && first_miss == big) {
+        // TopDown(add) and BottomUp over the judged tree: its parents are the refined nodes
+        std::vector<std::vector<int>> levels(n_levels);
+        for (int j = 0; j < n_levels; j++)
+            for (int i = level_begin[j]; i < level_begin[j + 1]; i++)
+                if ((flags_out[i] & 3) == 3) levels[j].push_back(i);
+        std::vector<int> flat;
+        std::vector<std::pair<int, int>> ranges;
+        for (auto &l : levels) {
+            ranges.push_back({(int)flat.size(), (int)l.size()});
+            flat.insert(flat.end(), l.begin(), l.end());
+        }
+        if (!flat.empty()) {
+            if ((int)flat.size() > ctx->list_cap) {
+                if (ctx->d_list) cudaFree(ctx->d_list);
+                if (ctx->d_ltree) cudaFree(ctx->d_ltree);
+                ctx->d_list = ctx->d_ltree = nullptr;
+                ctx->list_cap = (int)flat.size() * 2;
+                if (auto s = dev_alloc(ctx, &ctx->d_list, ctx->list_cap)) return s;
+                if (auto s = dev_alloc(ctx, &ctx->d_ltree, ctx->list_cap)) return s;
+            }
+            MW_CK(cudaMemcpyAsync(ctx->d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, st));
+            for (auto &r : ranges) {
+                launch_mw_down(out->mra, out->t, nullptr, nullptr, ctx->d_list + r.first, r.second, false, st);
+                ctx->launches += r.second > 0;
+            }
+            for (int l = (int)ranges.size() - 1; l >= 0; l--) {
+                launch_mw_up(out->mra, out->t, nullptr, nullptr, ctx->d_list + ranges[l].first, ranges[l].second, st);
+                ctx->launches += ranges[l].second > 0;
+            }
+            MW_CK(cudaGetLastError());
+            MW_CK(cudaStreamSynchronize(st));
+        }
     }
     return MWGPU_OK;
 }

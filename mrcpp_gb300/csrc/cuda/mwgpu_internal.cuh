@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace mwgpu {
@@ -19,6 +20,11 @@ namespace mwgpu {
 constexpr int kMaxDepthRows = 30;   // ConvolutionCalculator band-size rows (MaxDepth)
 constexpr double kMachineZero = 1.0e-14;
 constexpr uint64_t kEmptyKey = ~0ull;
+// chunk length of the mixed contraction: max(8, ceil(items / kChunkTarget))
+constexpr long long kChunkTarget = 8 * 304;
+// learned-grid network: features, hidden width, parameter count
+constexpr int kMlpFeatures = 8, kMlpHidden = 64;
+constexpr int kMlpParams = kMlpHidden * kMlpFeatures + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
 
 struct DevMRA {
     int K, kp1_d, root_scale, max_scale;
@@ -128,25 +134,68 @@ struct LevelStats {
 // kernel launchers (k_apply.cu / k_tree.cu)
 void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
                          uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s);
-void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
+// real_only: reconstruct from the nearest real ancestor even where a GenNode
+// ancestor exists (GenNodes that are rewritten by the same launch)
+void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s,
+                      bool real_only = false);
 void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
-                          double gthr, LevelStats *stats, int *err, cudaStream_t s);
+                          double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev = nullptr,
+                          const double *gthr_dev = nullptr);
 bool mixed_supported(int K);
-void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
-                        int n_work, long long n_pairs, double gthr, int *counts, unsigned long long *ncomp, unsigned long long *nband, int *err,
-                        cudaStream_t s);
-void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, const long long *pair_off,
-                       int n_work, long long n_pairs, double gthr, const long long *item_off, WorkItem *items, int *err, cudaStream_t s);
+void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                        const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts, unsigned long long *ncomp,
+                        unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
+void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                       const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const long long *item_off, WorkItem *items,
+                       long long items_cap, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
+// chunking of the work list on the device (graph-capturable levels); per <= 0:
+// the chunk length follows from the item count on the device (kChunkTarget)
+void launch_chunk_count(const long long *g_off, int n_work, long long per, int *counts, cudaStream_t s, const int *nw_dev = nullptr);
+void launch_chunk_fill(const long long *g_off, const long long *c_off, int n_work, long long per, int4 *chunks, int *chunk_begin, int cap,
+                       int *n_chunks, int *err, cudaStream_t s, const int *nw_dev = nullptr);
+void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                  const int4 *chunks, int n_chunks, const WorkItem *items, double *partial, int *err, const int *n_chunks_dev, int *counter,
+                  cudaStream_t s);
+void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tree, const int *work, int n_work, const int *chunk_begin,
+                          const double *partial, cudaStream_t s, const int *nw_dev = nullptr);
+// CTAs of the contraction kernel of order K resident on one SM (0 if unknown)
+int contract_items_resident(int K);
 long long scan_blocks(long long n);
 void launch_scan(const int *in, long long *out, long long n, long long *block_sums, long long *total, cudaStream_t s);
-void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s);
-void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work, const int4 *chunks,
-                           int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err, cudaStream_t s);
+void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev = nullptr);
+void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                           int n_work, const int4 *chunks, int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err,
+                           cudaStream_t s);
+// writes the device's nanosecond timer (usable inside CUDA graphs)
+void launch_stamp(unsigned long long *t, cudaStream_t s);
+void launch_gather_norms(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst, cudaStream_t s);
 void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cudaStream_t s);
-void launch_mw_down(const DevMRA &m, DevTree t, const int *parents, int n, bool overwrite, cudaStream_t s);
-void launch_mw_up(const DevMRA &m, DevTree t, const int *parents, int n, cudaStream_t s);
+void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite, cudaStream_t s);
+void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s);
 void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s);
 void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *err, cudaStream_t s);
+
+// learned grid (k_mlp.cu)
+size_t mlp_train_smem();
+void launch_mlp_infer(const float *X, int n, const __nv_bfloat16 *wb, float *prob, cudaStream_t s);
+void launch_mlp_train_tile(const float *X, const float *Y, const int *idx, int base, int count, const __nv_bfloat16 *wb, float pos_weight,
+                           float inv_wsum, float *partial, float *loss_partial, cudaStream_t s);
+void launch_mlp_reduce(const float *partial, const float *loss_partial, int tiles, float *grad, float *loss, cudaStream_t s);
+void launch_mlp_adam(float *master, float *m1, float *m2, const float *grad, __nv_bfloat16 *wb, float lr, float beta1, float beta2, float eps,
+                     float c1, float c2, cudaStream_t s);
+void launch_mlp_to_bf16(const float *src, __nv_bfloat16 *dst, int n, cudaStream_t s);
+void launch_mlp_features(const DevMRA &m, const DevTree &f, const int4 *nodes, int n, const int *band_w, const int *terms, int rows, double ftot,
+                         float *X, cudaStream_t s);
+
+// judged adaptive apply (k_judged.cu)
+void launch_keep_counts(const int *flags, int begin, int n, int *cnt, cudaStream_t s);
+void launch_compact(const int *flags, int begin, int n, const long long *koff, int *work, int *n_work, cudaStream_t s);
+void launch_cells(const int *work, const int *n_work, int cap, const int *cells, int *cnt, cudaStream_t s);
+void launch_threshold(const double *sq, double prec, int n_terms, double *gthr, cudaStream_t s);
+void launch_level_norm(const DevTree &g, const int *work, const int *n_work, int first_level, double *state, double *sq_level,
+                       const long long *g_off, unsigned long long *node_terms, cudaStream_t s);
+void launch_judge(const DevMRA &m, const DevTree &g, const int *work, const int *n_work, int cap, const double *state, double prec, int abs_prec,
+                  const double *scale_fac, int max_scale, int *flags, int level, int *first_miss, cudaStream_t s);
 
 }  // namespace mwgpu

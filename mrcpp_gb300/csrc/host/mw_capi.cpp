@@ -104,6 +104,244 @@ mwgpu_ctx *gpu_ctx(int precision) {
 void ck(int s, const char *what) {
     if (s) throw Error(s, std::string(what) + ": " + mwgpu_last_error(g_ctx));
 }
+
+// operator tables on the device, cached per (operator, apply precision)
+mwgpu_oper *device_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwh_oper *operp, double prec) {
+    auto it = g_oper_cache.find({operp, prec});
+    if (it != g_oper_cache.end()) return it->second;
+    mwgpu_oper *dop = nullptr;
+    mwgpu_oper_desc od{};
+    mwh_oper_desc(operp, &od);
+    ck(mwgpu_upload_operator(ctx, &md, &od, prec, &dop), "upload operator");
+    g_oper_cache[{operp, prec}] = dop;
+    return dop;
+}
+
+// State of one output tree inside apply: the TreeBuilder loop of
+// TreeBuilder.cpp:38-87 (sNorm from the first iteration, cumulative wNorm,
+// maxIter, WaveletAdaptor split), advanced one iteration at a time so that
+// several trees can share every device level call.
+struct BuildState {
+    Tree<3> *tree = nullptr;
+    mwgpu_tree *dinp = nullptr, *dout = nullptr;
+    std::vector<int> work;
+    double sNorm = 0.0, wNorm = 0.0;
+    int iter = 0;
+    size_t synced = 0;
+};
+
+mwgpu_tree *upload_input(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, const Tree<3> &inp, mwh_apply_stats &acc) {
+    std::vector<int> order, idx, child0;
+    export_tree(inp, order, idx, child0);
+    std::vector<double> coefs(order.size() * (size_t)inp.nCoefs), norms(order.size() * 8);
+    for (size_t j = 0; j < order.size(); j++) {
+        std::memcpy(&coefs[j * inp.nCoefs], inp.c(order[j]), sizeof(double) * inp.nCoefs);
+        std::memcpy(&norms[j * 8], inp.nodes[order[j]].norms, sizeof(double) * 8);
+    }
+    mwgpu_tree_desc fd{(int)order.size(), idx.data(), child0.data(), coefs.data(), norms.data()};
+    mwgpu_tree *dinp = nullptr;
+    ck(mwgpu_upload_tree(ctx, &md, &fd, &dinp), "upload input tree");
+    acc.h2d_bytes += (unsigned long long)(coefs.size() + norms.size()) * 8 + (idx.size() + child0.size()) * 4;
+    return dinp;
+}
+
+// output tree: the host ids are the device ids (nodes are only appended)
+mwgpu_tree *create_output(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, Tree<3> &out, mwh_apply_stats &acc) {
+    out.clearGenerated();
+    std::vector<int> oidx(out.nodes.size() * 4), oc0(out.nodes.size(), -1);
+    for (size_t i = 0; i < out.nodes.size(); i++) {
+        oidx[4 * i] = out.nodes[i].n;
+        for (int d = 0; d < 3; d++) oidx[4 * i + 1 + d] = out.nodes[i].l[d];
+        oc0[i] = out.nodes[i].child0;
+    }
+    mwgpu_tree_desc gd{(int)out.nodes.size(), oidx.data(), oc0.data(), nullptr, nullptr};
+    mwgpu_tree *dout = nullptr;
+    ck(mwgpu_create_tree(ctx, &md, &gd, &dout), "create output tree");
+    acc.h2d_bytes += (oidx.size() + oc0.size()) * 4;
+    return dout;
+}
+
+// children made by the split step are mirrored to the device before the next
+// iteration computes them
+void sync_new(mwgpu_ctx *ctx, BuildState &b, mwh_apply_stats &acc) {
+    const Tree<3> &t = *b.tree;
+    if (t.nodes.size() <= b.synced) return;
+    int n = (int)(t.nodes.size() - b.synced);
+    std::vector<int> nidx(4 * (size_t)n), pids, pc0;
+    for (int j = 0; j < n; j++) {
+        const auto &nd = t.nodes[b.synced + j];
+        nidx[4 * j] = nd.n;
+        for (int d = 0; d < 3; d++) nidx[4 * j + 1 + d] = nd.l[d];
+        if (nd.parent >= 0 && t.nodes[nd.parent].child0 == (int)(b.synced + j)) {
+            pids.push_back(nd.parent);
+            pc0.push_back(t.nodes[nd.parent].child0);
+        }
+    }
+    ck(mwgpu_tree_add_nodes(ctx, b.dout, n, nidx.data(), (int)pids.size(), pids.data(), pc0.data()), "add output nodes");
+    acc.h2d_bytes += (nidx.size() + pids.size() + pc0.size()) * 4 + t.nodes.size() * 4;
+    b.synced = t.nodes.size();
+}
+
+// mrcpp::apply (apply.cpp:68-93) for nt independent (out, inp) pairs with one
+// operator.  Each TreeBuilder iteration of all trees still building is one
+// device level call; the transforms of all trees share their launches.
+int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree **inps, int max_iter, int abs_prec, int precision,
+               mwh_apply_stats *stats) {
+    ConvolutionOperator &op = *operp->op;
+    for (int t = 0; t < nt; t++) {
+        if (!(*outs[t]->t->mra == *inps[t]->t->mra)) return fail(1, "Incompatible MRA");
+        if (!(*outs[t]->t->mra == op.mra)) return fail(1, "Operator MRA differs from the function MRA");
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lk(g_gpu_mu);
+    mwgpu_ctx *ctx = gpu_ctx(precision);
+    const MRA<3> &mra = *outs[0]->t->mra;
+    std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
+    mwgpu_mra_desc md{};
+    fill_desc(mra, &md, filters.data());
+
+    mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
+    mwh_apply_stats acc{};
+    unsigned long long l0 = 0, l1 = 0;
+    mwgpu_launch_count(ctx, &l0);
+    std::vector<BuildState> bs(nt);
+    auto release = [&] {
+        for (auto &b : bs) {
+            if (b.dout) mwgpu_free_tree(ctx, b.dout);
+            if (b.dinp) mwgpu_free_tree(ctx, b.dinp);
+            b.dout = b.dinp = nullptr;
+        }
+    };
+    try {
+        for (int t = 0; t < nt; t++) {
+            BuildState &b = bs[t];
+            b.tree = outs[t]->t.get();
+            b.dinp = upload_input(ctx, md, *inps[t]->t, acc);
+            b.dout = create_output(ctx, md, *b.tree, acc);
+            b.synced = b.tree->nodes.size();
+            // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
+            for (auto &lvl : b.tree->nodesByDepth(false))
+                for (int i : lvl) b.work.push_back(i);
+        }
+        std::vector<int> wtree, wnode;
+        std::vector<double> sq(nt), nbuf;
+        std::vector<mwgpu_tree *> dins(nt), douts(nt);
+        for (int t = 0; t < nt; t++) {
+            dins[t] = bs[t].dinp;
+            douts[t] = bs[t].dout;
+        }
+        while (true) {
+            wtree.clear();
+            wnode.clear();
+            for (int t = 0; t < nt; t++) {
+                BuildState &b = bs[t];
+                if (b.work.empty()) continue;
+                sync_new(ctx, b, acc);
+                for (int i : b.work) {
+                    wtree.push_back(t);
+                    wnode.push_back(i);
+                }
+            }
+            if (wnode.empty()) break;
+            for (int t = 0; t < nt; t++) sq[t] = bs[t].tree->squareNorm;
+            const int n = (int)wnode.size();
+            nbuf.resize((size_t)n * 8);
+            mwgpu_level_stats ls{};
+            if (nt == 1)
+                ck(mwgpu_apply_level(ctx, dop, dins[0], douts[0], wnode.data(), n, prec, sq[0], nbuf.data(), &ls), "apply level");
+            else
+                ck(mwgpu_apply_level_batch(ctx, dop, nt, dins.data(), douts.data(), wtree.data(), wnode.data(), n, prec, sq.data(), nbuf.data(),
+                                           &ls),
+                   "apply level");
+            acc.h2d_bytes += (unsigned long long)n * (nt == 1 ? 4 : 8);
+            acc.d2h_bytes += (unsigned long long)n * 8 * 8;
+            for (int j = 0; j < n; j++) {
+                Tree<3> &t = *bs[wtree[j]].tree;
+                auto &nd = t.nodes[wnode[j]];
+                double s2 = 0.0;
+                for (int c = 0; c < 8; c++) {
+                    nd.norms[c] = nbuf[(size_t)j * 8 + c];
+                    s2 += nd.norms[c] * nd.norms[c];
+                }
+                nd.squareNorm = s2;
+                nd.flags |= F_HASCOEFS;
+            }
+            acc.node_terms += ls.node_terms;
+            acc.components += ls.components;
+            acc.band_nodes += ls.band_nodes;
+            acc.gen_nodes += ls.gen_nodes;
+            acc.device_ms += ls.device_ms;
+            acc.contract_ms += ls.contract_ms;
+            acc.iterations++;
+            // TreeBuilder::build bookkeeping and split, per tree (TreeBuilder.cpp:49-80)
+            for (int t = 0; t < nt; t++) {
+                BuildState &b = bs[t];
+                if (b.work.empty()) continue;
+                Tree<3> &tree = *b.tree;
+                if (b.iter == 0) {
+                    b.sNorm = 0.0;
+                    for (int i : b.work)
+                        if (tree.depth(i) >= 0) b.sNorm += tree.scalingNorm(i);
+                }
+                for (int i : b.work)
+                    if (tree.depth(i) >= 0) b.wNorm += tree.waveletNorm(i);
+                tree.squareNorm = (b.sNorm < 0.0 || b.wNorm < 0.0) ? -1.0 : b.sNorm + b.wNorm;
+                if (b.iter >= max_iter && max_iter >= 0) b.work.clear();
+                std::vector<int> next;
+                for (int i : b.work) {
+                    if (tree.isBranch(i)) continue;
+                    if (tree.nodes[i].n + 2 > mra.maxScale()) continue;
+                    if (split_check(tree, i, prec, 1.0, abs_prec != 0)) {
+                        tree.createChildren(i, false);
+                        int c0 = tree.nodes[i].child0;
+                        for (int c = 0; c < Tree<3>::tDim; c++) next.push_back(c0 + c);
+                    }
+                }
+                b.work.swap(next);
+                b.iter++;
+            }
+        }
+        for (auto &b : bs) sync_new(ctx, b, acc);
+        auto t1 = std::chrono::steady_clock::now();
+        if (nt == 1) {
+            ck(mwgpu_transform(ctx, douts[0], MWGPU_TOPDOWN, 0), "TopDown transform");
+            ck(mwgpu_transform(ctx, douts[0], MWGPU_BOTTOMUP, 1), "BottomUp transform");
+        } else {
+            ck(mwgpu_transform_batch(ctx, nt, douts.data(), MWGPU_TOPDOWN, 0), "TopDown transform");
+            ck(mwgpu_transform_batch(ctx, nt, douts.data(), MWGPU_BOTTOMUP, 1), "BottomUp transform");
+        }
+        int out_nodes = 0;
+        for (auto &b : bs) {
+            Tree<3> &out = *b.tree;
+            std::vector<double> nn(out.nodes.size() * 8);
+            ck(mwgpu_download_tree(ctx, b.dout, out.coefs.data(), nn.data()), "download output tree");
+            acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
+            for (size_t i = 0; i < out.nodes.size(); i++) {
+                double s2 = 0.0;
+                for (int c = 0; c < 8; c++) {
+                    out.nodes[i].norms[c] = nn[i * 8 + c];
+                    s2 += nn[i * 8 + c] * nn[i * 8 + c];
+                }
+                out.nodes[i].squareNorm = s2;
+                out.nodes[i].flags |= F_HASCOEFS;
+            }
+            out.calcSquareNorm();
+            out_nodes += (int)out.nodes.size();
+        }
+        auto t2 = std::chrono::steady_clock::now();
+        acc.transform_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+        acc.out_nodes = out_nodes;
+    } catch (...) {
+        release();
+        throw;
+    }
+    mwgpu_launch_count(ctx, &l1);
+    acc.launches = l1 - l0;
+    release();
+    acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = acc;
+    return 0;
+}
 }  // namespace
 
 extern "C" {
@@ -355,148 +593,239 @@ int mwh_helmholtz_kernel(double mu, double eps, double r_min, double r_max, int 
 int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int max_iter, int abs_prec, int precision, mwh_apply_stats *stats) {
     return guard([&] {
         if (!outp || !operp || !inpp) return fail(1, "null argument");
-        Tree<3> &out = *outp->t;
-        Tree<3> &inp = *inpp->t;
-        ConvolutionOperator &op = *operp->op;
-        if (!(*out.mra == *inp.mra)) return fail(1, "Incompatible MRA");
-        if (!(*out.mra == op.mra)) return fail(1, "Operator MRA differs from the function MRA");
-        auto t0 = std::chrono::steady_clock::now();
+        mwh_tree *outs[1] = {outp}, *inps[1] = {inpp};
+        return apply_impl(prec, 1, outs, operp, inps, max_iter, abs_prec, precision, stats);
+    });
+}
+
+int mwh_apply_batch(double prec, int n, mwh_tree **outs, mwh_oper *operp, mwh_tree **inps, int max_iter, int abs_prec, int precision,
+                    mwh_apply_stats *stats) {
+    return guard([&] {
+        if (n < 1 || !outs || !inps || !operp) return fail(1, "null argument");
+        for (int t = 0; t < n; t++) {
+            if (!outs[t] || !inps[t]) return fail(1, "null argument");
+            for (int u = 0; u < t; u++)
+                if (outs[u] == outs[t] || inps[u] == inps[t] || outs[u] == inps[t]) return fail(1, "trees of a batch must be distinct");
+        }
+        return apply_impl(prec, n, outs, operp, inps, max_iter, abs_prec, precision, stats);
+    });
+}
+
+
+struct mwh_mlp {
+    std::vector<float> params;
+    mwgpu_mlp *dev = nullptr;
+};
+
+int mwh_mlp_create(const float *params, mwh_mlp **out) {
+    return guard([&] {
+        if (!params || !out) return fail(1, "null argument");
+        *out = new mwh_mlp{std::vector<float>(params, params + MWGPU_MLP_PARAMS), nullptr};
+        return 0;
+    });
+}
+
+void mwh_mlp_free(mwh_mlp *m) {
+    if (!m) return;
+    if (m->dev && g_ctx) {
         std::lock_guard<std::mutex> lk(g_gpu_mu);
-        mwgpu_ctx *ctx = gpu_ctx(precision);
-        const MRA<3> &mra = *out.mra;
+        mwgpu_mlp_destroy(g_ctx, m->dev);
+    }
+    delete m;
+}
+
+int mwh_grid_features(double prec, mwh_tree *gridp, mwh_oper *operp, mwh_tree *inpp, float *x, float *y) {
+    return guard([&] {
+        if (!gridp || !operp || !inpp || !x) return fail(1, "null argument");
+        Tree<3> &grid = *gridp->t;
+        Tree<3> &inp = *inpp->t;
+        std::lock_guard<std::mutex> lk(g_gpu_mu);
+        mwgpu_ctx *ctx = gpu_ctx(MWGPU_PREC_FP64);
+        const MRA<3> &mra = *inp.mra;
         std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
         mwgpu_mra_desc md{};
         fill_desc(mra, &md, filters.data());
-
-        // operator tables on the device, cached per (operator, apply precision)
-        mwgpu_oper *dop = nullptr;
-        auto it = g_oper_cache.find({operp, prec});
-        if (it != g_oper_cache.end()) {
-            dop = it->second;
-        } else {
-            mwgpu_oper_desc od{};
-            mwh_oper_desc(operp, &od);
-            ck(mwgpu_upload_operator(ctx, &md, &od, prec, &dop), "upload operator");
-            g_oper_cache[{operp, prec}] = dop;
-        }
-
-        // input tree
-        std::vector<int> order, idx, child0;
-        export_tree(inp, order, idx, child0);
-        std::vector<double> coefs(order.size() * (size_t)inp.nCoefs), norms(order.size() * 8);
-        for (size_t j = 0; j < order.size(); j++) {
-            std::memcpy(&coefs[j * inp.nCoefs], inp.c(order[j]), sizeof(double) * inp.nCoefs);
-            std::memcpy(&norms[j * 8], inp.nodes[order[j]].norms, sizeof(double) * 8);
-        }
-        mwgpu_tree_desc fd{(int)order.size(), idx.data(), child0.data(), coefs.data(), norms.data()};
-        mwgpu_tree *dinp = nullptr, *dout = nullptr;
-        ck(mwgpu_upload_tree(ctx, &md, &fd, &dinp), "upload input tree");
-
-        // output tree: the host ids are the device ids (nodes are only appended)
-        out.clearGenerated();
-        std::vector<int> oidx(out.nodes.size() * 4), oc0(out.nodes.size(), -1);
-        for (size_t i = 0; i < out.nodes.size(); i++) {
-            oidx[4 * i] = out.nodes[i].n;
-            for (int d = 0; d < 3; d++) oidx[4 * i + 1 + d] = out.nodes[i].l[d];
-            oc0[i] = out.nodes[i].child0;
-        }
-        mwgpu_tree_desc gd{(int)out.nodes.size(), oidx.data(), oc0.data(), nullptr, nullptr};
-        int st = mwgpu_create_tree(ctx, &md, &gd, &dout);
-        if (st) {
-            mwgpu_free_tree(ctx, dinp);
-            ck(st, "create output tree");
-        }
+        mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
         mwh_apply_stats acc{};
-        unsigned long long l0 = 0, l1 = 0;
-        mwgpu_launch_count(ctx, &l0);
-        acc.h2d_bytes = (unsigned long long)(coefs.size() + norms.size()) * 8 + (idx.size() + child0.size()) * 4 +
-                        (oidx.size() + oc0.size()) * 4;
-        try {
-            // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
-            std::vector<int> work;
-            for (auto &lvl : out.nodesByDepth(false))
-                for (int i : lvl) work.push_back(i);
-            std::vector<double> nbuf;
-            auto calc = [&](Tree<3> &t, const std::vector<int> &w) {
-                nbuf.resize(w.size() * 8);
-                mwgpu_level_stats ls{};
-                ck(mwgpu_apply_level(ctx, dop, dinp, dout, w.data(), (int)w.size(), prec, t.squareNorm, nbuf.data(), &ls), "apply level");
-                acc.h2d_bytes += w.size() * 4;
-                acc.d2h_bytes += (unsigned long long)t.nodes.size() * 8 * 8;
-                for (size_t j = 0; j < w.size(); j++) {
-                    double sq = 0.0;
-                    for (int c = 0; c < 8; c++) {
-                        t.nodes[w[j]].norms[c] = nbuf[j * 8 + c];
-                        sq += nbuf[j * 8 + c] * nbuf[j * 8 + c];
-                    }
-                    t.nodes[w[j]].squareNorm = sq;
-                    t.nodes[w[j]].flags |= F_HASCOEFS;
-                }
-                acc.node_terms += ls.node_terms;
-                acc.components += ls.components;
-                acc.band_nodes += ls.band_nodes;
-                acc.gen_nodes += ls.gen_nodes;
-                acc.device_ms += ls.device_ms;
-                acc.contract_ms += ls.contract_ms;
-                acc.iterations++;
-            };
-            size_t synced = out.nodes.size();
-            auto split = [&](const Tree<3> &t, int i) { return split_check(t, i, prec, 1.0, abs_prec != 0); };
-            // children made by the split step are mirrored to the device before
-            // the next iteration computes them (host ids == device ids)
-            auto sync_new = [&](const Tree<3> &t) {
-                if (t.nodes.size() <= synced) return;
-                int n = (int)(t.nodes.size() - synced);
-                std::vector<int> nidx(4 * (size_t)n), pids, pc0;
-                for (int j = 0; j < n; j++) {
-                    const auto &nd = t.nodes[synced + j];
-                    nidx[4 * j] = nd.n;
-                    for (int d = 0; d < 3; d++) nidx[4 * j + 1 + d] = nd.l[d];
-                    if (nd.parent >= 0 && t.nodes[nd.parent].child0 == (int)(synced + j)) {
-                        pids.push_back(nd.parent);
-                        pc0.push_back(t.nodes[nd.parent].child0);
-                    }
-                }
-                ck(mwgpu_tree_add_nodes(ctx, dout, n, nidx.data(), (int)pids.size(), pids.data(), pc0.data()), "add output nodes");
-                acc.h2d_bytes += (nidx.size() + pids.size() + pc0.size()) * 4 + t.nodes.size() * 4;
-                synced = t.nodes.size();
-            };
-            auto calc_sync = [&](Tree<3> &t, const std::vector<int> &w) {
-                sync_new(t);
-                calc(t, w);
-            };
-            tree_build<3>(out, work, calc_sync, split, max_iter, mra.maxScale());
-            sync_new(out);
-            auto t1 = std::chrono::steady_clock::now();
-            ck(mwgpu_transform(ctx, dout, MWGPU_TOPDOWN, 0), "TopDown transform");
-            ck(mwgpu_transform(ctx, dout, MWGPU_BOTTOMUP, 1), "BottomUp transform");
-            std::vector<double> nn(out.nodes.size() * 8);
-            ck(mwgpu_download_tree(ctx, dout, out.coefs.data(), nn.data()), "download output tree");
-            acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
-            auto t2 = std::chrono::steady_clock::now();
-            acc.transform_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
-            for (size_t i = 0; i < out.nodes.size(); i++) {
-                double sq = 0.0;
-                for (int c = 0; c < 8; c++) {
-                    out.nodes[i].norms[c] = nn[i * 8 + c];
-                    sq += nn[i * 8 + c] * nn[i * 8 + c];
-                }
-                out.nodes[i].squareNorm = sq;
-                out.nodes[i].flags |= F_HASCOEFS;
-            }
-            out.calcSquareNorm();
-        } catch (...) {
-            mwgpu_free_tree(ctx, dout);
-            mwgpu_free_tree(ctx, dinp);
-            throw;
+        mwgpu_tree *dinp = upload_input(ctx, md, inp, acc);
+        const int n = (int)grid.nodes.size();
+        std::vector<int> idx(4 * (size_t)n);
+        for (int i = 0; i < n; i++) {
+            idx[4 * i] = grid.nodes[i].n;
+            for (int d = 0; d < 3; d++) idx[4 * i + 1 + d] = grid.nodes[i].l[d];
+            if (y) y[i] = grid.nodes[i].child0 >= 0 ? 1.f : 0.f;
         }
-        mwgpu_launch_count(ctx, &l1);
-        acc.launches = l1 - l0;
-        mwgpu_free_tree(ctx, dout);
+        int st = mwgpu_mlp_features(ctx, dop, dinp, std::sqrt(std::max(inp.squareNorm, 0.0)), idx.data(), n, x);
         mwgpu_free_tree(ctx, dinp);
-        acc.out_nodes = (int)out.nodes.size();
-        acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        if (stats) *stats = acc;
+        ck(st, "grid features");
+        return 0;
+    });
+}
+
+int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, const mwh_mlp *mlpc, double threshold, int abs_prec,
+                      int precision, mwh_learned_stats *stats) {
+    return guard([&] {
+        if (!outp || !operp || !inpp || !mlpc) return fail(1, "null argument");
+        mwh_mlp *mlp = const_cast<mwh_mlp *>(mlpc);
+        Tree<3> &out = *outp->t;
+        Tree<3> &inp = *inpp->t;
+        mwh_learned_stats ls{};
+        ls.first_miss = -1;
+        // only a fresh output tree (the roots) can take a proposal
+        bool fresh = true;
+        for (auto &nd : out.nodes) fresh = fresh && nd.child0 < 0 && nd.n == out.mra->rootScale();
+        if (!fresh) {
+            mwh_tree *o1[1] = {outp}, *i1[1] = {inpp};
+            int rc = apply_impl(prec, 1, o1, operp, i1, -1, abs_prec, precision, &ls.apply);
+            ls.fallback = 1;
+            if (stats) *stats = ls;
+            return rc;
+        }
+        auto t0 = std::chrono::steady_clock::now();
+        mwgpu_ctx *ctx = nullptr;
+        mwgpu_tree *dinp = nullptr, *dprop = nullptr;
+        int first_miss = -1;
+        std::vector<int> flags, level_begin;
+        std::vector<double> coefs, norms;
+        Tree<3> prop(*out.mra);
+        {
+            std::lock_guard<std::mutex> lk(g_gpu_mu);
+            ctx = gpu_ctx(precision);
+            const MRA<3> &mra = *out.mra;
+            std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
+            mwgpu_mra_desc md{};
+            fill_desc(mra, &md, filters.data());
+            mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
+            if (!mlp->dev) ck(mwgpu_mlp_create(ctx, mlp->params.data(), &mlp->dev), "network upload");
+            mwh_apply_stats acc{};
+            unsigned long long l0 = 0, l1 = 0;
+            mwgpu_launch_count(ctx, &l0);
+            try {
+                dinp = upload_input(ctx, md, inp, acc);
+                const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
+                // proposal, level by level: children of the nodes the network refines
+                std::vector<int> cur;
+                for (size_t i = 0; i < prop.nodes.size(); i++) cur.push_back((int)i);
+                level_begin.push_back(0);
+                std::vector<int> idx;
+                std::vector<float> x, pr;
+                while (!cur.empty()) {
+                    level_begin.push_back(level_begin.back() + (int)cur.size());
+                    const int n = (int)cur.size();
+                    idx.resize(4 * (size_t)n);
+                    for (int j = 0; j < n; j++) {
+                        const auto &nd = prop.nodes[cur[j]];
+                        idx[4 * j] = nd.n;
+                        for (int d = 0; d < 3; d++) idx[4 * j + 1 + d] = nd.l[d];
+                    }
+                    x.resize((size_t)n * MWGPU_MLP_FEATURES);
+                    pr.resize(n);
+                    ck(mwgpu_mlp_features(ctx, dop, dinp, f_norm, idx.data(), n, x.data()), "grid features");
+                    ck(mwgpu_mlp_infer(ctx, mlp->dev, x.data(), n, pr.data()), "grid inference");
+                    ls.host_round_trips += 2;
+                    std::vector<int> next;
+                    for (int j = 0; j < n; j++) {
+                        const int i = cur[j];
+                        if (pr[j] <= threshold || prop.nodes[i].n + 2 > mra.maxScale()) continue;
+                        prop.createChildren(i, false);
+                        const int c0 = prop.nodes[i].child0;
+                        for (int c = 0; c < Tree<3>::tDim; c++) next.push_back(c0 + c);
+                    }
+                    cur.swap(next);
+                    ls.proposal_levels++;
+                }
+                ls.proposal_nodes = (int)prop.nodes.size();
+                auto t1 = std::chrono::steady_clock::now();
+                ls.predict_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+                // the proposal as the device output tree, judged in one pass
+                std::vector<int> pidx(prop.nodes.size() * 4), pc0(prop.nodes.size(), -1);
+                for (size_t i = 0; i < prop.nodes.size(); i++) {
+                    pidx[4 * i] = prop.nodes[i].n;
+                    for (int d = 0; d < 3; d++) pidx[4 * i + 1 + d] = prop.nodes[i].l[d];
+                    pc0[i] = prop.nodes[i].child0;
+                }
+                mwgpu_tree_desc gd{(int)prop.nodes.size(), pidx.data(), pc0.data(), nullptr, nullptr};
+                ck(mwgpu_create_tree(ctx, &md, &gd, &dprop), "create proposal tree");
+                acc.h2d_bytes += (pidx.size() + pc0.size()) * 4;
+                flags.assign(prop.nodes.size(), 0);
+                mwgpu_level_stats st{};
+                const int nlev = (int)level_begin.size() - 1;
+                ck(mwgpu_apply_judged(ctx, dop, dinp, dprop, nlev, level_begin.data(), prec, abs_prec, out.squareNorm, 1, flags.data(),
+                                      &first_miss, nullptr, &st),
+                   "judged apply");
+                ls.host_round_trips += 1;
+                acc.d2h_bytes += flags.size() * 4;
+                if (first_miss < 0) {
+                    coefs.resize(prop.nodes.size() * (size_t)prop.nCoefs);
+                    norms.resize(prop.nodes.size() * 8);
+                    ck(mwgpu_download_tree(ctx, dprop, coefs.data(), norms.data()), "download output tree");
+                    acc.d2h_bytes += (coefs.size() + norms.size()) * 8;
+                    ls.host_round_trips += 1;
+                }
+                acc.node_terms = st.node_terms;
+                acc.components = st.components;
+                acc.band_nodes = st.band_nodes;
+                acc.gen_nodes = st.gen_nodes;
+                acc.device_ms = st.device_ms;
+                acc.contract_ms = st.contract_ms;
+                acc.iterations = 1;
+                ls.judged_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+            } catch (...) {
+                if (dprop) mwgpu_free_tree(ctx, dprop);
+                if (dinp) mwgpu_free_tree(ctx, dinp);
+                throw;
+            }
+            mwgpu_free_tree(ctx, dprop);
+            mwgpu_free_tree(ctx, dinp);
+            mwgpu_launch_count(ctx, &l1);
+            acc.launches = l1 - l0;
+            ls.apply = acc;
+        }
+        ls.first_miss = first_miss;
+        if (first_miss >= 0) {
+            // the judge refined a node the proposal left out: the plain apply decides
+            mwh_tree *o1[1] = {outp}, *i1[1] = {inpp};
+            mwh_apply_stats pa{};
+            int rc = apply_impl(prec, 1, o1, operp, i1, -1, abs_prec, precision, &pa);
+            if (rc) return rc;
+            pa.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            ls.apply = pa;
+            ls.fallback = 1;
+            if (stats) *stats = ls;
+            return 0;
+        }
+        // the judged tree, created in TreeBuilder's order (the host ids of the plain apply)
+        std::vector<int> map(prop.nodes.size(), -1);
+        for (size_t i = 0; i < out.nodes.size(); i++) map[i] = (int)i;
+        const int nlev = (int)level_begin.size() - 1;
+        int kept = 0;
+        for (int j = 0; j < nlev; j++)
+            for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
+                if (!(flags[i] & 1)) continue;
+                kept++;
+                if ((flags[i] & 3) != 3) continue;
+                const int oi = map[i];
+                out.createChildren(oi, false);
+                const int c0 = out.nodes[oi].child0, p0 = prop.nodes[i].child0;
+                for (int c = 0; c < Tree<3>::tDim; c++) map[p0 + c] = c0 + c;
+            }
+        ls.kept_nodes = kept;
+        for (size_t i = 0; i < prop.nodes.size(); i++) {
+            const int oi = map[i];
+            if (oi < 0 || !(flags[i] & 1)) continue;
+            std::memcpy(out.c(oi), &coefs[i * (size_t)prop.nCoefs], sizeof(double) * prop.nCoefs);
+            double s2 = 0.0;
+            for (int c = 0; c < 8; c++) {
+                out.nodes[oi].norms[c] = norms[i * 8 + c];
+                s2 += norms[i * 8 + c] * norms[i * 8 + c];
+            }
+            out.nodes[oi].squareNorm = s2;
+            out.nodes[oi].flags |= F_HASCOEFS;
+        }
+        out.calcSquareNorm();
+        ls.apply.out_nodes = (int)out.nodes.size();
+        ls.apply.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = ls;
         return 0;
     });
 }
