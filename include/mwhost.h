@@ -116,8 +116,8 @@ void mwh_mlp_free(mwh_mlp *mlp);
 int mwh_apply_learned(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, const mwh_mlp *mlp, double threshold, int abs_prec,
                       int precision, mwh_learned_stats *stats);
 /* Training data: features (n*8) of every node of `grid` (e.g. the output of a
- * plain apply of oper on inp, in node order) and labels (1 = the node has
- * children).  n = number of nodes of grid. */
+ * plain apply of oper on inp) in the order of the tree export (breadth first),
+ * and labels (1 = the node has children).  n = number of nodes of grid. */
 int mwh_grid_features(double prec, mwh_tree *grid, mwh_oper *oper, mwh_tree *inp, float *x, float *y);
 
 #ifdef __cplusplus

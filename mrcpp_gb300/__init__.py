@@ -17,7 +17,7 @@ import numpy as np
 
 __all__ = [
     "MWGPUError", "lib", "MRA", "FunctionTree", "PoissonOperator", "HelmholtzOperator", "ConvolutionOperator",
-    "build_grid", "project", "apply", "apply_batch", "copy_grid", "dot", "poisson_kernel", "helmholtz_kernel",
+    "build_grid", "project", "apply", "apply_batch", "apply_learned", "GridNetwork", "grid_features", "copy_grid", "dot", "poisson_kernel", "helmholtz_kernel",
     "LEGENDRE", "INTERPOLATING", "FP64", "MIXED",
 ]
 
@@ -70,9 +70,21 @@ class MwhApplyStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class MwhLearnedStats(C.Structure):
+    _fields_ = [("apply", MwhApplyStats), ("proposal_nodes", C.c_int), ("proposal_levels", C.c_int), ("kept_nodes", C.c_int),
+                ("first_miss", C.c_int), ("fallback", C.c_int), ("host_round_trips", C.c_int), ("predict_ms", C.c_double),
+                ("judged_ms", C.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "apply"}
+        d["apply"] = self.apply.as_dict()
+        return d
+
+
 _P = C.c_void_p
 _PI = C.POINTER(C.c_int)
 _PD = C.POINTER(C.c_double)
+_PF = C.POINTER(C.c_float)
 _SIGS = {
     # device C-ABI (include/mwgpu.h)
     "mwgpu_init": (C.c_int, [C.POINTER(_P), C.POINTER(MwgpuConfig)]),
@@ -99,6 +111,15 @@ _SIGS = {
     "mwgpu_plan_info": (C.c_int, [_P, C.POINTER(C.c_longlong), _PI, _PI, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_ulonglong)]),
     "mwgpu_plan_destroy": (C.c_int, [_P, _P]),
     "mwgpu_tree_update_coefs": (C.c_int, [_P, _P, _PD, _PD]),
+    "mwgpu_apply_judged": (C.c_int, [_P, _P, _P, _P, C.c_int, _PI, C.c_double, C.c_int, C.c_double, C.c_int, _PI, _PI, _PD,
+                                     C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_mlp_create": (C.c_int, [_P, _PF, C.POINTER(_P)]),
+    "mwgpu_mlp_destroy": (C.c_int, [_P, _P]),
+    "mwgpu_mlp_get": (C.c_int, [_P, _P, _PF, C.POINTER(C.c_uint16)]),
+    "mwgpu_mlp_features": (C.c_int, [_P, _P, _P, C.c_double, _PI, C.c_int, _PF]),
+    "mwgpu_mlp_infer": (C.c_int, [_P, _P, _PF, C.c_int, _PF]),
+    "mwgpu_mlp_grad": (C.c_int, [_P, _P, _PF, _PF, C.c_int, C.c_float, _PF, _PF]),
+    "mwgpu_mlp_train": (C.c_int, [_P, _P, _PF, _PF, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint, _PF]),
     "mwgpu_download_tree": (C.c_int, [_P, _P, _PD, _PD]),
     "mwgpu_sync": (C.c_int, [_P]),
     "mwgpu_tree_clear_generated": (C.c_int, [_P, _P]),
@@ -135,6 +156,10 @@ _SIGS = {
     "mwh_apply": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwh_apply_batch": (C.c_int, [C.c_double, C.c_int, C.POINTER(_P), _P, C.POINTER(_P), C.c_int, C.c_int, C.c_int,
                                   C.POINTER(MwhApplyStats)]),
+    "mwh_mlp_create": (C.c_int, [_PF, C.POINTER(_P)]),
+    "mwh_mlp_free": (None, [_P]),
+    "mwh_apply_learned": (C.c_int, [C.c_double, _P, _P, _P, _P, C.c_double, C.c_int, C.c_int, C.POINTER(MwhLearnedStats)]),
+    "mwh_grid_features": (C.c_int, [C.c_double, _P, _P, _P, _PF, _PF]),
 }
 
 _lib = None
@@ -384,3 +409,59 @@ def apply_batch(prec, outs, oper, inps, max_iter=-1, abs_prec=False, precision=F
     st = MwhApplyStats()
     _ck(lib().mwh_apply_batch(float(prec), n, po, oper._h, pi, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
     return st.as_dict()
+
+
+def _pf(a):
+    return a.ctypes.data_as(_PF)
+
+
+MLP_PARAMS = 4801
+MLP_FEATURES = 8
+DEFAULT_NETWORK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "grid_mlp_k7.npz")
+
+
+class GridNetwork:
+    """The learned output-grid network (3 layers, 64 wide, BF16 weights): its
+    FP32 parameters, W1[64][8], b1, W2[64][64], b2, W3[64], b3."""
+
+    def __init__(self, params):
+        self.params = np.ascontiguousarray(np.asarray(params, dtype=np.float32))
+        if self.params.shape != (MLP_PARAMS,):
+            raise ValueError("expected %d parameters" % MLP_PARAMS)
+        h = _P()
+        _ck(lib().mwh_mlp_create(_pf(self.params), C.byref(h)))
+        self._h = h
+
+    @classmethod
+    def load(cls, path=DEFAULT_NETWORK):
+        with np.load(path) as z:
+            net = cls(z["params"])
+            net.meta = {k: z[k] for k in z.files if k != "params"}
+        return net
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mwh_mlp_free(self._h)
+            self._h = None
+
+
+def apply_learned(prec, out, oper, inp, network, threshold=0.3, abs_prec=False, precision=FP64):
+    """mrcpp::apply(prec, out, oper, inp) with the output grid proposed by the
+    network and judged on the device by the split test: the result equals
+    apply(prec, out, oper, inp, precision=precision).  Returns the statistics
+    (proposal size, first missed level, fallback, round trips, timings)."""
+    st = MwhLearnedStats()
+    _ck(lib().mwh_apply_learned(float(prec), out._h, oper._h, inp._h, network._h, float(threshold), int(bool(abs_prec)), int(precision),
+                                C.byref(st)))
+    return st.as_dict()
+
+
+def grid_features(prec, grid, oper, inp):
+    """Features of every node of `grid` against inp (rows in the order of
+    grid.export()), and labels (1 = the node has children): training data for
+    the network."""
+    n = grid.n_nodes
+    x = np.zeros((n, MLP_FEATURES), dtype=np.float32)
+    y = np.zeros(n, dtype=np.float32)
+    _ck(lib().mwh_grid_features(float(prec), grid._h, oper._h, inp._h, _pf(x), _pf(y)))
+    return x, y

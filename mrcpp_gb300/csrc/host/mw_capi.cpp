@@ -648,12 +648,16 @@ int mwh_grid_features(double prec, mwh_tree *gridp, mwh_oper *operp, mwh_tree *i
         mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
         mwh_apply_stats acc{};
         mwgpu_tree *dinp = upload_input(ctx, md, inp, acc);
-        const int n = (int)grid.nodes.size();
+        // rows in the order of the tree export (breadth first)
+        std::vector<int> order, gidx, gc0;
+        export_tree(grid, order, gidx, gc0);
+        const int n = (int)order.size();
         std::vector<int> idx(4 * (size_t)n);
-        for (int i = 0; i < n; i++) {
-            idx[4 * i] = grid.nodes[i].n;
-            for (int d = 0; d < 3; d++) idx[4 * i + 1 + d] = grid.nodes[i].l[d];
-            if (y) y[i] = grid.nodes[i].child0 >= 0 ? 1.f : 0.f;
+        for (int j = 0; j < n; j++) {
+            const auto &nd = grid.nodes[order[j]];
+            idx[4 * j] = nd.n;
+            for (int d = 0; d < 3; d++) idx[4 * j + 1 + d] = nd.l[d];
+            if (y) y[j] = gc0[j] >= 0 ? 1.f : 0.f;
         }
         int st = mwgpu_mlp_features(ctx, dop, dinp, std::sqrt(std::max(inp.squareNorm, 0.0)), idx.data(), n, x);
         mwgpu_free_tree(ctx, dinp);
@@ -703,6 +707,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
             try {
                 dinp = upload_input(ctx, md, inp, acc);
                 const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
+                const size_t max_nodes = std::max<size_t>(4096, 4 * inp.nodes.size());
                 // proposal, level by level: children of the nodes the network refines
                 std::vector<int> cur;
                 for (size_t i = 0; i < prop.nodes.size(); i++) cur.push_back((int)i);
@@ -723,16 +728,19 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     ck(mwgpu_mlp_features(ctx, dop, dinp, f_norm, idx.data(), n, x.data()), "grid features");
                     ck(mwgpu_mlp_infer(ctx, mlp->dev, x.data(), n, pr.data()), "grid inference");
                     ls.host_round_trips += 2;
-                    std::vector<int> next;
-                    for (int j = 0; j < n; j++) {
-                        const int i = cur[j];
-                        if (pr[j] <= threshold || prop.nodes[i].n + 2 > mra.maxScale()) continue;
+                    std::vector<int> next, refine;
+                    for (int j = 0; j < n; j++)
+                        if (pr[j] > threshold && prop.nodes[cur[j]].n + 2 <= mra.maxScale()) refine.push_back(cur[j]);
+                    ls.proposal_levels++;
+                    // a proposal larger than the budget stops here (the judge then
+                    // reports the first level it would have needed)
+                    if (prop.nodes.size() + Tree<3>::tDim * refine.size() > max_nodes) break;
+                    for (int i : refine) {
                         prop.createChildren(i, false);
                         const int c0 = prop.nodes[i].child0;
                         for (int c = 0; c < Tree<3>::tDim; c++) next.push_back(c0 + c);
                     }
                     cur.swap(next);
-                    ls.proposal_levels++;
                 }
                 ls.proposal_nodes = (int)prop.nodes.size();
                 auto t1 = std::chrono::steady_clock::now();

@@ -1,0 +1,219 @@
+"""Trains the learned output-grid network on grids that the method itself
+generates, and evaluates it on held-out densities.
+
+    python -m mrcpp_gb300.learned.train_grid --out mrcpp_gb300/data/grid_mlp_k7.npz
+
+Data: seeded Gaussian-sum densities (n ~ U{1..6} Gaussians, exponents
+log-uniform in [1, 100], centres uniform in [-5, 5]^3, coefficients uniform in
+[-1, 1]) projected at 1e-5 with Legendre k = 7 in [-32, 32]^3; for each, the
+plain adaptive Poisson apply at 1e-5 (mixed form) on the GPU gives the output
+tree, and every output node becomes one sample: its features against the input
+tree and the label "the split test refined it".  Seeds 10000.. train
+(the last tenth of them chooses the decision threshold), seeds 20000.. are held
+out.  Training runs on the GPU with the library's own kernels (Adam on the
+weighted binary cross entropy).  The evaluation compares the learned apply with
+the plain adaptive apply on every held-out density: host round trips of the
+TreeBuilder loop, wall time, fallbacks, topology and coefficient identity.
+"""
+import argparse
+import ctypes as C
+import json
+import multiprocessing as mp
+import os
+import time
+
+import numpy as np
+
+ORDER, PREC, BOX = 7, 1e-5, (-32, 32)
+TRAIN_SEED0, HELD_SEED0 = 10000, 20000
+
+_state = {}
+
+
+def density(seed):
+    """n ~ U{1..6} Gaussians c exp(-a |r - R|^2): a log-uniform [1, 100], R in [-5, 5]^3, c in [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(1, 7))
+    out = []
+    for _ in range(n):
+        a = float(np.exp(rng.uniform(np.log(1.0), np.log(100.0))))
+        c = float(rng.uniform(-1.0, 1.0))
+        r = tuple(float(v) for v in rng.uniform(-5.0, 5.0, 3))
+        out.append((c, a, r))
+    return out
+
+
+def _setup():
+    import mrcpp_gb300 as mw
+    if "mra" not in _state:
+        _state["mra"] = mw.MRA(box=BOX, order=ORDER, basis=mw.LEGENDRE)
+        _state["P"] = mw.PoissonOperator(_state["mra"], PREC)
+    return mw, _state["mra"], _state["P"]
+
+
+def sample(seed):
+    """Features and labels of the plain output tree of one density."""
+    mw, mra, P = _setup()
+    f = mw.FunctionTree(mra)
+    mw.project(PREC, f, density(seed))
+    g = mw.FunctionTree(mra)
+    st = mw.apply(PREC, g, P, f, precision=mw.MIXED)
+    x, y = mw.grid_features(PREC, g, P, f)
+    return seed, x, y, st["iterations"], g.n_nodes, f.n_nodes
+
+
+def _worker_init():
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+
+
+def generate(seeds, workers):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers, initializer=_worker_init) as pool:
+        return pool.map(sample, seeds, chunksize=4)
+
+
+def he_init(seed):
+    """He initialisation of the weights, zero biases (parameter layout of
+    include/mwgpu.h)."""
+    F, H = 8, 64
+    rng = np.random.default_rng(seed)
+    p = np.zeros(4801, dtype=np.float32)
+    p[0:H * F] = rng.normal(0.0, np.sqrt(2.0 / F), H * F)
+    o2 = H * F + H
+    p[o2:o2 + H * H] = rng.normal(0.0, np.sqrt(2.0 / H), H * H)
+    o3 = o2 + H * H + H
+    p[o3:o3 + H] = rng.normal(0.0, np.sqrt(1.0 / H), H)
+    return p
+
+
+def gpu_train(X, Y, epochs, batch, lr, pos_weight, seed):
+    import mrcpp_gb300 as mw
+    L = mw.lib()
+    ctx = C.c_void_p()
+    if L.mwgpu_init(C.byref(ctx), C.byref(mw.MwgpuConfig())) != 0:
+        raise SystemExit("no GPU: " + L.mwgpu_last_error(None).decode())
+    try:
+        p = he_init(seed)
+        net = C.c_void_p()
+        assert L.mwgpu_mlp_create(ctx, mw._pf(p), C.byref(net)) == 0
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        curve = np.zeros(epochs, dtype=np.float32)
+        t0 = time.perf_counter()
+        rc = L.mwgpu_mlp_train(ctx, net, mw._pf(X), mw._pf(Y), len(Y), epochs, batch, lr, pos_weight, seed, mw._pf(curve))
+        if rc:
+            raise SystemExit(L.mwgpu_last_error(ctx).decode())
+        t_train = time.perf_counter() - t0
+        out = np.zeros(4801, dtype=np.float32)
+        assert L.mwgpu_mlp_get(ctx, net, mw._pf(out), None) == 0
+        L.mwgpu_mlp_destroy(ctx, net)
+        return out, curve, t_train
+    finally:
+        L.mwgpu_destroy(ctx)
+
+
+def gpu_prob(params, X):
+    import mrcpp_gb300 as mw
+    L = mw.lib()
+    ctx = C.c_void_p()
+    assert L.mwgpu_init(C.byref(ctx), C.byref(mw.MwgpuConfig())) == 0
+    try:
+        net = C.c_void_p()
+        assert L.mwgpu_mlp_create(ctx, mw._pf(np.ascontiguousarray(params)), C.byref(net)) == 0
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        pr = np.zeros(len(X), dtype=np.float32)
+        assert L.mwgpu_mlp_infer(ctx, net, mw._pf(X), len(X), mw._pf(pr)) == 0
+        L.mwgpu_mlp_destroy(ctx, net)
+        return pr
+    finally:
+        L.mwgpu_destroy(ctx)
+
+
+def evaluate(params, threshold, seeds, precision):
+    """Plain adaptive apply vs learned apply on each density (same process, sequential)."""
+    mw, mra, P = _setup()
+    from mrcpp_gb300 import GridNetwork
+    net = GridNetwork(params)
+    rows = []
+    for s in seeds:
+        f = mw.FunctionTree(mra)
+        mw.project(PREC, f, density(s))
+        g0 = mw.FunctionTree(mra)
+        t0 = time.perf_counter()
+        sp = mw.apply(PREC, g0, P, f, precision=precision)
+        t_plain = time.perf_counter() - t0
+        g1 = mw.FunctionTree(mra)
+        t0 = time.perf_counter()
+        sl = mw.apply_learned(PREC, g1, P, f, net, threshold=threshold, precision=precision)
+        t_learned = time.perf_counter() - t0
+        a, b = g0.export(), g1.export()
+        ka = {tuple(r): i for i, r in enumerate(a["idx"].reshape(-1, 4).tolist())}
+        kb = [tuple(r) for r in b["idx"].reshape(-1, 4).tolist()]
+        same = len(ka) == len(kb) and all(k in ka for k in kb)
+        diff = None
+        if same:
+            perm = np.array([ka[k] for k in kb])
+            diff = float(np.abs(a["coefs"][perm] - b["coefs"]).max() / max(np.abs(a["coefs"]).max(), 1e-300))
+        rows.append({"seed": s, "out_nodes": g0.n_nodes, "plain_iterations": sp["iterations"], "plain_ms": 1e3 * t_plain,
+                     "learned_ms": 1e3 * t_learned, "fallback": sl["fallback"], "first_miss": sl["first_miss"],
+                     "proposal_nodes": sl["proposal_nodes"], "kept_nodes": sl["kept_nodes"], "round_trips": sl["host_round_trips"],
+                     "same_topology": bool(same), "max_rel_diff": diff})
+    return rows
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "data", "grid_mlp_k7.npz"))
+    ap.add_argument("--train", type=int, default=2000)
+    ap.add_argument("--held", type=int, default=200)
+    ap.add_argument("--workers", type=int, default=max(1, (os.cpu_count() or 2) - 1))
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--success", type=float, default=0.97, help="share of validation densities the threshold must propose completely")
+    ap.add_argument("--report", default=None, help="JSON file for the evaluation")
+    a = ap.parse_args()
+    t0 = time.perf_counter()
+    res = generate(list(range(TRAIN_SEED0, TRAIN_SEED0 + a.train)), a.workers)
+    t_gen = time.perf_counter() - t0
+    n_val = max(1, a.train // 10)
+    tr, va = res[:-n_val], res[-n_val:]
+    X = np.concatenate([r[1] for r in tr])
+    Y = np.concatenate([r[2] for r in tr])
+    pos = float(Y.sum())
+    pos_weight = float(min(50.0, 4.0 * (len(Y) - pos) / max(pos, 1.0)))
+    params, curve, t_train = gpu_train(X, Y, a.epochs, a.batch, a.lr, pos_weight, 1234)
+    # threshold: below the smallest P(split) of the refined nodes of `success` of the validation grids
+    mins = []
+    for r in va:
+        pr = gpu_prob(params, r[1])
+        sp = pr[r[2] > 0.5]
+        mins.append(float(sp.min()) if len(sp) else 1.0)
+    threshold = float(np.quantile(np.array(mins), 1.0 - a.success)) * 0.999
+    import mrcpp_gb300 as mw
+    rows = evaluate(params, threshold, list(range(HELD_SEED0, HELD_SEED0 + a.held)), mw.MIXED)
+    summ = {
+        "train_densities": len(tr), "validation_densities": len(va), "held_out_densities": len(rows), "samples": int(len(Y)),
+        "positives": int(pos), "pos_weight": pos_weight, "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "threshold": threshold,
+        "loss_first_last": [float(curve[0]), float(curve[-1])], "train_s": t_train, "generate_s": t_gen,
+        "held_out": {
+            "fallback_rate": float(np.mean([r["fallback"] for r in rows])),
+            "same_topology": int(sum(r["same_topology"] for r in rows)),
+            "max_rel_diff": max((r["max_rel_diff"] or 0.0) for r in rows),
+            "plain_ms_total": float(sum(r["plain_ms"] for r in rows)),
+            "learned_ms_total": float(sum(r["learned_ms"] for r in rows)),
+            "plain_iterations_mean": float(np.mean([r["plain_iterations"] for r in rows])),
+            "learned_round_trips_mean": float(np.mean([r["round_trips"] for r in rows])),
+            "proposal_over_kept": float(np.sum([r["proposal_nodes"] for r in rows]) / max(1, np.sum([r["kept_nodes"] or 0 for r in rows]))),
+        },
+    }
+    os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+    np.savez(a.out, params=params, threshold=np.float64(threshold), loss_curve=curve, summary=json.dumps(summ))
+    if a.report:
+        with open(a.report, "w") as fh:
+            json.dump({"summary": summ, "held_out": rows}, fh, indent=1)
+    print(json.dumps(summ))
+
+
+if __name__ == "__main__":
+    main()
