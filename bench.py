@@ -58,12 +58,13 @@ def parse():
     p.add_argument("--impl", default="mw", choices=["mw", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--small", action="store_true", help="6 Gaussians at 1e-4 (a short launch for ncu captures)")
-    p.add_argument("--workload", default="poisson", choices=["poisson", "helmholtz", "batch"],
+    p.add_argument("--workload", default="poisson", choices=["poisson", "helmholtz", "batch", "learned"],
                    help="poisson: the FP64-GPU Poisson configuration (default); helmholtz: the mixed-precision Helmholtz "
                         "configuration (mu=1, k=9, 32 Gaussians with exponents 0.5..500 in [-6,6]^3, prec 1e-6); batch: 64 "
                         "functions of 1..32 Gaussians (exponents 0.1..1000, centres [-8,8]^3), k=7, prec 1e-5, one planned "
                         "level (CUDA graph, persistent contraction, autotuned chunks) against separate FP64 applies")
     p.add_argument("--batch-n", type=int, default=64, help="functions in the batch workload")
+    p.add_argument("--learned-n", type=int, default=20, help="held-out densities in the learned-grid workload")
     p.add_argument("--fp64-sample", type=int, default=8, help="batch workload: separate FP64 applies timed (every n/s-th function)")
     a = p.parse_args()
     global PREC, NGAUSS, WORKLOAD, ORDER, EXP_RANGE, CENTRE_RANGE, MU, METRIC
@@ -75,6 +76,10 @@ def parse():
         METRIC = "Batched Poisson apply node·terms/s on 1 GB300, mixed (one graph) vs separate FP64 applies"
         WORKLOAD = ("batched poisson-apply legendre k=7 box [-32,32]^3, %d functions of 1..32 gaussians (exp 0.1..1000, centres "
                     "[-8,8]^3), prec 1e-5, fixed output grids (maxIter=0)" % a.batch_n)
+    if a.workload == "learned":
+        METRIC = "Adaptive Poisson apply node·terms/s on 1 GB300, learned grid vs plain refinement (mixed form)"
+        WORKLOAD = ("adaptive poisson-apply legendre k=7 box [-32,32]^3, %d held-out densities of 1..6 gaussians (exp 1..100, centres "
+                    "[-5,5]^3), prec 1e-5, learned output grid judged by the split test vs plain TreeBuilder refinement" % a.learned_n)
     if a.small:
         PREC, NGAUSS = PREC * 10, 6
         WORKLOAD = WORKLOAD.replace("16 gaussians", "6 gaussians").replace("32 gaussians", "6 gaussians").replace(
@@ -423,6 +428,71 @@ def main_batch(args, rank, world, local, pg):
     barrier(pg)
 
 
+def main_learned(args, rank, world, local, pg):
+    import mrcpp_gb300 as mw
+    from mrcpp_gb300.learned import train_grid as tg
+
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, PREC)
+    net = mw.GridNetwork.load()
+    thr = float(net.meta["threshold"])
+    seeds = list(range(tg.HELD_SEED0, tg.HELD_SEED0 + args.learned_n))
+    fs = []
+    for sd in seeds:
+        f = mw.FunctionTree(mra)
+        mw.project(PREC, f, tg.density(sd))
+        fs.append(f)
+    # warm-up: operator upload, network upload, first contexts
+    for _ in range(max(1, args.warm)):
+        mw.apply(PREC, mw.FunctionTree(mra), P, fs[0], precision=mw.MIXED)
+        mw.apply_learned(PREC, mw.FunctionTree(mra), P, fs[0], net, threshold=thr, precision=mw.MIXED)
+    plain_t, learned_t, nt_p, nt_l, it_p, it_l, rt_l, cont, same, diffs, contract, launches = [], [], 0, 0, [], [], [], 0, 0, [], 0.0, 0
+    with ClockSampler(local) as cs:
+        for f in fs:
+            g0 = mw.FunctionTree(mra)
+            t0 = time.perf_counter()
+            sp = mw.apply(PREC, g0, P, f, precision=mw.MIXED)
+            plain_t.append(time.perf_counter() - t0)
+            g1 = mw.FunctionTree(mra)
+            t0 = time.perf_counter()
+            sl = mw.apply_learned(PREC, g1, P, f, net, threshold=thr, precision=mw.MIXED)
+            learned_t.append(time.perf_counter() - t0)
+            nt_p += sp["node_terms"]
+            nt_l += sl["apply"]["node_terms"]
+            it_p.append(sp["iterations"])
+            it_l.append(sl["apply"]["iterations"])
+            rt_l.append(sl["host_round_trips"])
+            cont += sl["fallback"]
+            contract += sl["apply"]["contract_ms"]
+            launches += sl["apply"]["launches"]
+            a, b = g0.export(), g1.export()
+            if a["idx"].shape == b["idx"].shape and np.array_equal(a["idx"], b["idx"]):
+                same += 1
+                diffs.append(float(np.abs(a["coefs"] - b["coefs"]).max() / max(np.abs(a["coefs"]).max(), 1e-300)))
+    t_l, t_p = sum(learned_t), sum(plain_t)
+    value = nt_l / t_l
+    bf16_peak, hbm_peak, peak_kind = load_peaks()
+    achieved = nt_l * 96.0 * 8 ** 4 / (contract / 1e3) / 1e12 if contract > 0 else None
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(fs), "warmup": max(1, args.warm),
+                "ms_per_step": 1e3 * t_l / len(fs), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 products, f64 accumulation", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "densities": len(fs), "threshold": thr, "network": "mrcpp_gb300/data/grid_mlp_k7.npz",
+                           "step": "one adaptive apply of one density (host trees in and out)", "parallelism": "single"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                        "note": "the adaptive apply is end to end by construction (host FunctionTrees)"},
+                "plain": {"value": nt_p / t_p, "unit": UNIT, "ms_per_step": 1e3 * t_p / len(fs), "iterations_mean": float(np.mean(it_p))},
+                "learned": {"compute_iterations_mean": float(np.mean(it_l)), "host_round_trips_mean": float(np.mean(rt_l)),
+                            "continued_after_miss": cont, "same_topology": same, "max_rel_diff": max(diffs) if diffs else None,
+                            "speedup_wall": t_p / t_l},
+                "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                             "frac": (achieved / bf16_peak) if achieved else None, "traffic": None, "peak_kind": peak_kind + " bf16 dense burst",
+                             "kernel": "k_contract_items (judged levels)"},
+                "cpu_baseline": None, "clocks": cs.summary(), "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    barrier(pg)
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args.gpus)
@@ -433,6 +503,10 @@ def main():
     if args.workload == "batch":
         os.environ["MWGPU_DEVICE"] = str(local)
         main_batch(args, rank, world, local, pg)
+        return
+    if args.workload == "learned":
+        os.environ["MWGPU_DEVICE"] = str(local)
+        main_learned(args, rank, world, local, pg)
         return
     os.environ["MWGPU_DEVICE"] = str(local)
     import ctypes as C

@@ -250,9 +250,10 @@ mwgpu_status mwgpu_scrub_l2(mwgpu_ctx *ctx, size_t bytes);
  * needs, never its result.
  * Parameters: MWGPU_MLP_PARAMS floats, W1[64][8], b1[64], W2[64][64], b2[64],
  * W3[64], b3 (W[out][in], row-major).  Features: MWGPU_MLP_FEATURES floats per
- * node (depth/16; log10 of the input norm at the node relative to f_norm /8;
- * the same summed over the operator band box /8; operator terms reaching the
- * depth /100; translation parities; 1 if the input has a node there). */
+ * node (depth/16; log10 of the input's wavelet norm at the node relative to
+ * f_norm /8; log10 of the input norm summed over the operator band box /8;
+ * operator terms reaching the depth /100; translation parities; 1 / 0.5 / 0
+ * if the input has a branch node / a leaf / no node there). */
 typedef struct mwgpu_mlp mwgpu_mlp;
 #define MWGPU_MLP_FEATURES 8
 #define MWGPU_MLP_PARAMS 4801
@@ -263,6 +264,10 @@ mwgpu_status mwgpu_mlp_get(mwgpu_ctx *ctx, const mwgpu_mlp *mlp, float *params, 
 /* Features of n nodes (idx: n*4 ints) against input tree inp; x: n*8 floats. */
 mwgpu_status mwgpu_mlp_features(mwgpu_ctx *ctx, const mwgpu_oper *oper, const mwgpu_tree *inp, double f_norm, const int *idx, int n,
                                 float *x);
+/* Features + inference in one call (device buffers kept in the network):
+ * P(split) of n nodes (idx: n*4 ints) against input tree inp. */
+mwgpu_status mwgpu_mlp_predict(mwgpu_ctx *ctx, mwgpu_mlp *mlp, const mwgpu_oper *oper, const mwgpu_tree *inp, double f_norm, const int *idx,
+                               int n, float *prob);
 /* P(split) of n feature rows. */
 mwgpu_status mwgpu_mlp_infer(mwgpu_ctx *ctx, const mwgpu_mlp *mlp, const float *x, int n, float *prob);
 /* Gradient (MWGPU_MLP_PARAMS floats) and value of the weighted binary cross
@@ -291,12 +296,15 @@ mwgpu_status mwgpu_mlp_train(mwgpu_ctx *ctx, mwgpu_mlp *mlp, const float *x, con
  * bit 1 = refined.  first_miss = the first level where a refined node had no
  * proposed children (-1: none); the result is then exact up to that level
  * only.  With `transforms` and no miss, TopDown(add) and BottomUp run over the
- * judged tree.  sq_levels (n_levels, may be NULL) gets the tree norm after
- * each level.  Equal to mwgpu_apply_level driven by the host TreeBuilder on
- * the judged tree whenever first_miss is -1. */
+ * judged tree.  norm_levels (3*n_levels, may be NULL) gets TreeBuilder's
+ * sNorm, wNorm and tree norm after each level (to continue the loop on the
+ * host after a miss).  Equal to mwgpu_apply_level driven by the host
+ * TreeBuilder on the judged tree whenever first_miss is -1. */
 mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, int n_levels,
                                 const int *level_begin, double prec, int abs_prec, double out_sqnorm, int transforms, int *flags_out,
-                                int *first_miss, double *sq_levels, mwgpu_level_stats *stats);
+                                int *first_miss, double *norm_levels, mwgpu_level_stats *stats);
+/* Copies coefficients and norms of nodes src_ids[j] of src to dst_ids[j] of dst. */
+mwgpu_status mwgpu_tree_copy_nodes(mwgpu_ctx *ctx, const mwgpu_tree *src, mwgpu_tree *dst, int n, const int *src_ids, const int *dst_ids);
 
 /* Allocation-free variant of mwgpu_apply_level.  No counterpart in the
  * reference (MRCPP allocates on the host as it goes).  For callers that must

@@ -101,10 +101,11 @@ int mwh_apply_batch(double prec, int n, mwh_tree **outs, mwh_oper *oper, mwh_tre
 /* Learned output grid (no reference counterpart): the network proposes the
  * output grid level by level (features + inference on the GPU), then one
  * mwgpu_apply_judged pass computes and judges it with the split test.  The
- * result equals mwh_apply(prec, out, oper, inp, -1, abs_prec, precision):
- * when the judge refines a node the proposal did not, the apply is redone
- * the plain way (fallback = 1).  `out` must be a fresh tree (root nodes
- * only), else the plain apply runs. */
+ * result equals mwh_apply(prec, out, oper, inp, -1, abs_prec, precision).
+ * When the judge refines a node of level j that the proposal did not, levels
+ * 0..j are kept and the host TreeBuilder loop continues from level j+1 with
+ * the missed children appended (fallback = 1, first_miss = j).  `out` must be
+ * a fresh tree (root nodes only), else the plain apply runs. */
 typedef struct mwh_mlp mwh_mlp;
 typedef struct {
     mwh_apply_stats apply;   /* of the judged pass (or of the plain fallback) */

@@ -118,6 +118,8 @@ _SIGS = {
     "mwgpu_mlp_get": (C.c_int, [_P, _P, _PF, C.POINTER(C.c_uint16)]),
     "mwgpu_mlp_features": (C.c_int, [_P, _P, _P, C.c_double, _PI, C.c_int, _PF]),
     "mwgpu_mlp_infer": (C.c_int, [_P, _P, _PF, C.c_int, _PF]),
+    "mwgpu_mlp_predict": (C.c_int, [_P, _P, _P, _P, C.c_double, _PI, C.c_int, _PF]),
+    "mwgpu_tree_copy_nodes": (C.c_int, [_P, _P, _P, C.c_int, _PI, _PI]),
     "mwgpu_mlp_grad": (C.c_int, [_P, _P, _PF, _PF, C.c_int, C.c_float, _PF, _PF]),
     "mwgpu_mlp_train": (C.c_int, [_P, _P, _PF, _PF, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint, _PF]),
     "mwgpu_download_tree": (C.c_int, [_P, _P, _PD, _PD]),
@@ -432,9 +434,14 @@ class GridNetwork:
         _ck(lib().mwh_mlp_create(_pf(self.params), C.byref(h)))
         self._h = h
 
+    FEATURES = 2  # feature set of include/mwgpu.h (wavelet norm, branch / leaf / absent)
+
     @classmethod
     def load(cls, path=DEFAULT_NETWORK):
         with np.load(path) as z:
+            version = int(z["features"]) if "features" in z.files else 1
+            if version != cls.FEATURES:
+                raise ValueError("%s was trained on another feature set; retrain it" % path)
             net = cls(z["params"])
             net.meta = {k: z[k] for k in z.files if k != "params"}
         return net

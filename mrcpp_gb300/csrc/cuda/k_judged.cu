@@ -65,7 +65,8 @@ __device__ inline double wavelet_norm(const double *nrm) {
     return w;
 }
 
-// state[0] sNorm, state[1] wNorm, state[2] tree norm; node_terms += items of the level
+// state[0] sNorm, state[1] wNorm, state[2] tree norm (also copied to
+// sq_level[0..3) of the level); node_terms += items of the level
 constexpr int kNormBlock = 1024;
 __global__ void __launch_bounds__(kNormBlock) k_level_norm(DevTree g, const int *work, const int *n_work, int first_level, double *state,
                                                            double *sq_level, const long long *g_off, unsigned long long *node_terms) {
@@ -94,7 +95,9 @@ __global__ void __launch_bounds__(kNormBlock) k_level_norm(DevTree g, const int 
         state[1] = wNorm;
         const double sq = (sNorm < 0.0 || wNorm < 0.0) ? -1.0 : __dadd_rn(sNorm, wNorm);
         state[2] = sq;
-        *sq_level = sq;
+        sq_level[0] = sNorm;
+        sq_level[1] = wNorm;
+        sq_level[2] = sq;
         if (node_terms && g_off) *node_terms += (unsigned long long)g_off[n];
     }
 }

@@ -10,7 +10,7 @@ void launch_k(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTr
     size_t smem = sizeof(float) * mixed::Shape<K>::SMEM_FLOATS;
     auto kern = mixed::k_contract_items<K>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<n_chunks, 256, smem, s>>>(m, op, fs, gs, work_tree, work, chunks, items, partial, err, n_chunks_dev, counter);
+    kern<<<n_chunks, mixed::Shape<K>::NT, smem, s>>>(m, op, fs, gs, work_tree, work, chunks, items, partial, err, n_chunks_dev, counter);
 }
 
 template <int K>
@@ -19,12 +19,13 @@ int resident_k() {
     auto kern = mixed::k_contract_items<K>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, mixed::Shape<K>::NT, smem) != cudaSuccess) return 0;
     return nb;
 }
 }  // namespace
 
-bool mixed_supported(int K) { return K >= 2 && K <= 12; }
+// the staged blocks of K >= 11 do not fit the 227 KB of shared memory of a CTA
+bool mixed_supported(int K) { return K >= 2 && K <= 10; }
 
 
 void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
@@ -52,8 +53,6 @@ int contract_items_resident(int K) {
         case 8: return resident_k<8>();
         case 9: return resident_k<9>();
         case 10: return resident_k<10>();
-        case 11: return resident_k<11>();
-        case 12: return resident_k<12>();
         default: return 0;
     }
 }
@@ -72,8 +71,6 @@ void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const D
         case 8: launch_k<8>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
         case 9: launch_k<9>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
         case 10: launch_k<10>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
-        case 11: launch_k<11>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
-        case 12: launch_k<12>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
         default: break;
     }
 }

@@ -14,14 +14,14 @@
 // Features of a node (n, l) against the input tree f (relative to the total
 // norm |f| of f, base-10 logarithms):
 //   0  depth / 16
-//   1  log10 |f(n,l)| / 8: the node's norm, or, where f has no node there, the
-//      nearest stored ancestor's norm times 2^(-3(n-a)/2) (its norm spread over
-//      the 8^(n-a) descendants)
-//   2  log10 of the same estimate summed over the operator band box at this
-//      depth (half width min(band_max, 3), clipped to the world) / 8
+//   1  log10 |f(n,l)| / 8: the wavelet norm of f's node, or, where f has no
+//      node there, the nearest stored ancestor's norm times 2^(-3(n-a)/2) (its
+//      norm spread over the 8^(n-a) descendants)
+//   2  log10 of the total-norm estimate summed over the operator band box at
+//      this depth (half width min(band_max, 3), clipped to the world) / 8
 //   3  operator terms whose band reaches this depth / 100
 //   4-6  translation parity l_d mod 2
-//   7  1 if f has a node at (n, l), else 0
+//   7  f at (n, l): 1 = a node with children, 0.5 = a leaf, 0 = no node
 #include <cuda_bf16.h>
 
 #include "mwgpu_internal.cuh"
@@ -184,10 +184,11 @@ __global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, int n) {
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) dst[p] = __float2bfloat16_rn(src[p]);
 }
 
-// norm of f around (n, l): the stored node, else the nearest stored ancestor
-// spread over its descendants; 0 outside the world
-__device__ inline double norm_estimate(const DevMRA &m, const DevTree &f, int n, int l0, int l1, int l2, bool *exists) {
-    *exists = false;
+// norm of f around (n, l): the stored node (wavelet part only if `wavelet`),
+// else the nearest stored ancestor's total norm spread over its descendants;
+// 0 outside the world.  *stored: 0 none, 1 leaf, 2 node with children.
+__device__ inline double norm_estimate(const DevMRA &m, const DevTree &f, int n, int l0, int l1, int l2, bool wavelet, int *stored) {
+    *stored = 0;
     for (int a = n; a >= m.root_scale; a--) {
         const int sh = n - a;
         uint64_t key;
@@ -195,11 +196,11 @@ __device__ inline double norm_estimate(const DevMRA &m, const DevTree &f, int n,
         const int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
         if (id >= 0 && id < f.cap_real) {
             double s = 0.0;
-            for (int c = 0; c < 8; c++) {
+            for (int c = (wavelet && sh == 0) ? 1 : 0; c < 8; c++) {
                 const double v = f.norms[(size_t)id * 8 + c];
                 s += v * v;
             }
-            *exists = sh == 0;
+            if (sh == 0) *stored = f.child0[id] >= 0 ? 2 : 1;
             return sqrt(s) * exp2(-1.5 * sh);
         }
     }
@@ -225,13 +226,13 @@ __global__ void k_features(DevMRA m, DevTree f, const int4 *nodes, int n, const 
     const int cells = max(nx, 0) * max(ny, 0) * max(nz, 0);
     double band = 0.0;
     for (int q = lane; q < cells; q += 32) {
-        bool ex;
-        band += norm_estimate(m, f, g.x, bs[0] + q % nx, bs[1] + (q / nx) % ny, bs[2] + q / (nx * ny), &ex);
+        int st;
+        band += norm_estimate(m, f, g.x, bs[0] + q % nx, bs[1] + (q / nx) % ny, bs[2] + q / (nx * ny), false, &st);
     }
     for (int o = 16; o > 0; o >>= 1) band += __shfl_down_sync(0xffffffffu, band, o);
     if (lane == 0) {
-        bool ex;
-        const double own = norm_estimate(m, f, g.x, g.y, g.z, g.w, &ex);
+        int st;
+        const double own = norm_estimate(m, f, g.x, g.y, g.z, g.w, true, &st);
         const double inv = ftot > 0.0 ? 1.0 / ftot : 1.0;
         float *x = X + (size_t)warp * F;
         x[0] = (float)depth / 16.f;
@@ -241,7 +242,7 @@ __global__ void k_features(DevMRA m, DevTree f, const int4 *nodes, int n, const 
         x[4] = (float)(g.y & 1);
         x[5] = (float)(g.z & 1);
         x[6] = (float)(g.w & 1);
-        x[7] = ex ? 1.f : 0.f;
+        x[7] = 0.5f * (float)st;
     }
 }
 

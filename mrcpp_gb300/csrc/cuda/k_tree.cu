@@ -286,7 +286,20 @@ __global__ void k_stamp(unsigned long long *t) {
     *t = v;
 }
 
+__global__ void k_copy_nodes(DevTree src, DevTree dst, const int *sid, const int *did, int n, int nc) {
+    const int j = blockIdx.x;
+    if (j >= n) return;
+    const double *a = src.coefs + (size_t)sid[j] * nc;
+    double *b = dst.coefs + (size_t)did[j] * nc;
+    for (int e = threadIdx.x; e < nc; e += blockDim.x) b[e] = a[e];
+    if (threadIdx.x < 8) dst.norms[(size_t)did[j] * 8 + threadIdx.x] = src.norms[(size_t)sid[j] * 8 + threadIdx.x];
+}
+
 }  // namespace
+
+void launch_copy_nodes(const DevTree &src, const DevTree &dst, const int *sid, const int *did, int n, int nc, cudaStream_t s) {
+    if (n > 0) k_copy_nodes<<<n, 256, 0, s>>>(src, dst, sid, did, n, nc);
+}
 
 void launch_stamp(unsigned long long *t, cudaStream_t s) { k_stamp<<<1, 1, 0, s>>>(t); }
 

@@ -19,6 +19,12 @@ struct mwgpu_mlp {
     float *m1 = nullptr, *m2 = nullptr;  // Adam moments
     __nv_bfloat16 *wb = nullptr;      // BF16 copy used by the forward passes
     long long steps = 0;              // Adam steps taken
+    // buffers of mwgpu_mlp_predict, grown as needed
+    int4 *p_nodes = nullptr;
+    float *p_x = nullptr, *p_prob = nullptr;
+    int p_cap = 0;
+    int *p_tab = nullptr;  // band widths and term counts per depth
+    int p_rows = 0;
 };
 
 namespace {
@@ -73,7 +79,8 @@ mwgpu_status mwgpu_mlp_destroy(mwgpu_ctx *ctx, mwgpu_mlp *m) {
     if (!m) return MWGPU_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (void *p : {(void *)m->master, (void *)m->m1, (void *)m->m2, (void *)m->wb})
+    for (void *p : {(void *)m->master, (void *)m->m1, (void *)m->m2, (void *)m->wb, (void *)m->p_nodes, (void *)m->p_x, (void *)m->p_prob,
+                    (void *)m->p_tab})
         if (p) cudaFree(p);
     delete m;
     return MWGPU_OK;
@@ -207,6 +214,52 @@ mwgpu_status mwgpu_mlp_train(mwgpu_ctx *ctx, mwgpu_mlp *m, const float *x, const
             epoch_loss[e] = (float)(a / nbatch);
         }
     }
+    return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_mlp_predict(mwgpu_ctx *ctx, mwgpu_mlp *m, const mwgpu_oper *o, const mwgpu_tree *inp, double f_norm, const int *idx, int n,
+                               float *prob) {
+    if (!ctx || !m || !o || !inp || !prob) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n >= 0 && (n == 0 || idx), "invalid node list");
+    MW_ARG(inp->is_input, "features are computed against an input tree");
+    if (n == 0) return MWGPU_OK;
+    cudaSetDevice(ctx->device);
+    const int rows = o->n_rows, T = o->op.n_terms;
+    std::vector<int> tab(2 * (size_t)rows, 0);
+    for (int d = 0; d < rows; d++) {
+        tab[d] = o->band_max[d];
+        for (int t = 0; t < T; t++) tab[rows + d] += o->widths[((size_t)t * rows + d) * 5 + 4] >= 0;
+    }
+    if (n > m->p_cap) {
+        for (void *p : {(void *)m->p_nodes, (void *)m->p_x, (void *)m->p_prob})
+            if (p) cudaFree(p);
+        m->p_nodes = nullptr;
+        m->p_x = m->p_prob = nullptr;
+        m->p_cap = 0;
+        const int cap = std::max(n, 1024);
+        mwgpu_status st;
+        if ((st = dev_alloc(ctx, &m->p_nodes, cap)) || (st = dev_alloc(ctx, &m->p_x, (size_t)cap * kMlpFeatures)) ||
+            (st = dev_alloc(ctx, &m->p_prob, cap)))
+            return st;
+        m->p_cap = cap;
+    }
+    if (rows > m->p_rows) {
+        if (m->p_tab) cudaFree(m->p_tab);
+        m->p_tab = nullptr;
+        m->p_rows = 0;
+        if (auto st = dev_alloc(ctx, &m->p_tab, 2 * (size_t)rows)) return st;
+        m->p_rows = rows;
+    }
+    std::vector<int4> nodes(n);
+    for (int i = 0; i < n; i++) nodes[i] = make_int4(idx[4 * i], idx[4 * i + 1], idx[4 * i + 2], idx[4 * i + 3]);
+    MW_CK(cudaMemcpyAsync(m->p_nodes, nodes.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(m->p_tab, tab.data(), sizeof(int) * 2 * rows, cudaMemcpyHostToDevice, ctx->stream));
+    launch_mlp_features(inp->mra, inp->t, m->p_nodes, n, m->p_tab, m->p_tab + rows, rows, f_norm, m->p_x, ctx->stream);
+    launch_mlp_infer(m->p_x, n, m->wb, m->p_prob, ctx->stream);
+    ctx->launches += 2;
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaMemcpyAsync(prob, m->p_prob, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    MW_CK(cudaStreamSynchronize(ctx->stream));
     return MWGPU_OK;
 }
 

@@ -616,7 +616,7 @@ mwgpu_status make_level(mwgpu_ctx *ctx, const mwgpu_oper *o, int nt, mwgpu_tree 
     }
     MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
     if (ctx->precision == MWGPU_PREC_MIXED && !mixed_supported(o->op.K)) {
-        ctx->err = "mixed form supports orders k = 1..11";
+        ctx->err = "mixed form supports orders k = 1..9";
         return MWGPU_ERR_BAD_ARG;
     }
     lv.o = o;
@@ -1690,7 +1690,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
         b.items = c.take<WorkItem>(mixed ? max_items : 1);
         b.partial = c.take<double>(mixed ? (size_t)max_chunks * 8 * m.kp1_d : 1);
         b.state = c.take<double>(3);
-        b.sq = c.take<double>(n_levels);
+        b.sq = c.take<double>(3 * (size_t)n_levels);
         b.scale_fac = c.take<double>(rows);
         b.first_miss = c.take<int>(1);
         b.node_terms = c.take<unsigned long long>(1);
@@ -1751,11 +1751,11 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,
                          st);
             launch_reduce_chunks(m, ctx->d_gs, ctx->d_wtree, b.work, nl, b.chunk_begin, b.partial, st, b.nwork);
-            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + j, b.goff, b.node_terms, st);
+            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, b.goff, b.node_terms, st);
             ctx->launches += 17;
         } else {
             launch_contract_fp64(m, o->op, inp->t, out->t, b.work, nl, 0.0, ctx->d_stats, ctx->d_err, st, b.nwork, ctx->d_gthr);
-            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + j, nullptr, nullptr, st);
+            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, nullptr, nullptr, st);
             ctx->launches += 2;
         }
         launch_judge(m, out->t, b.work, b.nwork, nl, b.state, prec, abs_prec, b.scale_fac, m.max_scale, b.flags, j, b.first_miss, st);
@@ -1770,10 +1770,10 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     MW_CK(cudaMemcpyAsync(&first_miss, b.first_miss, sizeof(int), cudaMemcpyDeviceToHost, st));
     MW_CK(cudaMemcpyAsync(&nt_mixed, b.node_terms, sizeof(nt_mixed), cudaMemcpyDeviceToHost, st));
     MW_CK(cudaMemcpyAsync(&hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
-    std::vector<double> sqv(n_levels);
-    MW_CK(cudaMemcpyAsync(sqv.data(), b.sq, sizeof(double) * n_levels, cudaMemcpyDeviceToHost, st));
+    std::vector<double> sqv(3 * (size_t)n_levels);
+    MW_CK(cudaMemcpyAsync(sqv.data(), b.sq, sizeof(double) * 3 * n_levels, cudaMemcpyDeviceToHost, st));
     if (auto s = check_err(ctx, "judged apply")) return s;
-    if (sq_levels) std::memcpy(sq_levels, sqv.data(), sizeof(double) * n_levels);
+    if (sq_levels) std::memcpy(sq_levels, sqv.data(), sizeof(double) * 3 * n_levels);
     *first_miss_out = first_miss == big ? -1 : first_miss;
     if (stats) {
         stats->node_terms = mixed ? nt_mixed : hs.node_terms;
@@ -1820,5 +1820,25 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             MW_CK(cudaStreamSynchronize(st));
         }
     }
+    return MWGPU_OK;
+}
+
+extern "C" mwgpu_status mwgpu_tree_copy_nodes(mwgpu_ctx *ctx, const mwgpu_tree *src, mwgpu_tree *dst, int n, const int *src_ids,
+                                              const int *dst_ids) {
+    if (!ctx || !src || !dst) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n >= 0 && (n == 0 || (src_ids && dst_ids)), "invalid node lists");
+    MW_ARG(src->mra.K == dst->mra.K, "order mismatch");
+    MW_ARG(dst->plans == 0, "tree is held by a plan (destroy the plan first)");
+    for (int i = 0; i < n; i++)
+        MW_ARG(src_ids[i] >= 0 && src_ids[i] < src->t.n_real && dst_ids[i] >= 0 && dst_ids[i] < dst->t.n_real, "node index out of range");
+    if (n == 0) return MWGPU_OK;
+    cudaSetDevice(ctx->device);
+    if (auto s = ensure_work(ctx, n)) return s;
+    MW_CK(cudaMemcpyAsync(ctx->d_work, src_ids, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_wtree, dst_ids, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    launch_copy_nodes(src->t, dst->t, ctx->d_work, ctx->d_wtree, n, 8 * src->mra.kp1_d, ctx->stream);
+    ctx->launches++;
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaStreamSynchronize(ctx->stream));
     return MWGPU_OK;
 }

@@ -167,6 +167,8 @@ void launch_gather_goff(const long long *item_off, const long long *pair_off, in
 void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                            int n_work, const int4 *chunks, int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err,
                            cudaStream_t s);
+// copies coefficients and norms of nodes sid[j] of src to nodes did[j] of dst
+void launch_copy_nodes(const DevTree &src, const DevTree &dst, const int *sid, const int *did, int n, int nc, cudaStream_t s);
 // writes the device's nanosecond timer (usable inside CUDA graphs)
 void launch_stamp(unsigned long long *t, cudaStream_t s);
 void launch_gather_norms(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst, cudaStream_t s);

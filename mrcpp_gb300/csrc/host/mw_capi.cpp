@@ -185,8 +185,10 @@ void sync_new(mwgpu_ctx *ctx, BuildState &b, mwh_apply_stats &acc) {
 // mrcpp::apply (apply.cpp:68-93) for nt independent (out, inp) pairs with one
 // operator.  Each TreeBuilder iteration of all trees still building is one
 // device level call; the transforms of all trees share their launches.
+// resume (nt = 1 only): continue the TreeBuilder loop of an apply whose
+// earlier iterations ran elsewhere (device trees, work, iteration and norms).
 int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree **inps, int max_iter, int abs_prec, int precision,
-               mwh_apply_stats *stats) {
+               mwh_apply_stats *stats, const BuildState *resume = nullptr) {
     ConvolutionOperator &op = *operp->op;
     for (int t = 0; t < nt; t++) {
         if (!(*outs[t]->t->mra == *inps[t]->t->mra)) return fail(1, "Incompatible MRA");
@@ -215,6 +217,10 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     try {
         for (int t = 0; t < nt; t++) {
             BuildState &b = bs[t];
+            if (resume) {
+                b = *resume;
+                continue;
+            }
             b.tree = outs[t]->t.get();
             b.dinp = upload_input(ctx, md, *inps[t]->t, acc);
             b.dout = create_output(ctx, md, *b.tree, acc);
@@ -690,8 +696,9 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         mwgpu_tree *dinp = nullptr, *dprop = nullptr;
         int first_miss = -1;
         std::vector<int> flags, level_begin;
-        std::vector<double> coefs, norms;
+        std::vector<double> coefs, norms, norm_levels;
         Tree<3> prop(*out.mra);
+        BuildState resume;
         {
             std::lock_guard<std::mutex> lk(g_gpu_mu);
             ctx = gpu_ctx(precision);
@@ -713,7 +720,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 for (size_t i = 0; i < prop.nodes.size(); i++) cur.push_back((int)i);
                 level_begin.push_back(0);
                 std::vector<int> idx;
-                std::vector<float> x, pr;
+                std::vector<float> pr;
                 while (!cur.empty()) {
                     level_begin.push_back(level_begin.back() + (int)cur.size());
                     const int n = (int)cur.size();
@@ -723,11 +730,9 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                         idx[4 * j] = nd.n;
                         for (int d = 0; d < 3; d++) idx[4 * j + 1 + d] = nd.l[d];
                     }
-                    x.resize((size_t)n * MWGPU_MLP_FEATURES);
                     pr.resize(n);
-                    ck(mwgpu_mlp_features(ctx, dop, dinp, f_norm, idx.data(), n, x.data()), "grid features");
-                    ck(mwgpu_mlp_infer(ctx, mlp->dev, x.data(), n, pr.data()), "grid inference");
-                    ls.host_round_trips += 2;
+                    ck(mwgpu_mlp_predict(ctx, mlp->dev, dop, dinp, f_norm, idx.data(), n, pr.data()), "grid prediction");
+                    ls.host_round_trips += 1;
                     std::vector<int> next, refine;
                     for (int j = 0; j < n; j++)
                         if (pr[j] > threshold && prop.nodes[cur[j]].n + 2 <= mra.maxScale()) refine.push_back(cur[j]);
@@ -758,8 +763,9 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 flags.assign(prop.nodes.size(), 0);
                 mwgpu_level_stats st{};
                 const int nlev = (int)level_begin.size() - 1;
+                norm_levels.assign(3 * (size_t)nlev, 0.0);
                 ck(mwgpu_apply_judged(ctx, dop, dinp, dprop, nlev, level_begin.data(), prec, abs_prec, out.squareNorm, 1, flags.data(),
-                                      &first_miss, nullptr, &st),
+                                      &first_miss, norm_levels.data(), &st),
                    "judged apply");
                 ls.host_round_trips += 1;
                 acc.d2h_bytes += flags.size() * 4;
@@ -769,6 +775,38 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     ck(mwgpu_download_tree(ctx, dprop, coefs.data(), norms.data()), "download output tree");
                     acc.d2h_bytes += (coefs.size() + norms.size()) * 8;
                     ls.host_round_trips += 1;
+                } else {
+                    // exact up to level first_miss: that part of the judged tree goes
+                    // into a fresh output tree, with the children of every node the
+                    // judge refined at that level; the host loop continues from there
+                    const int jm = first_miss;
+                    std::vector<int> map(prop.nodes.size(), -1), src, dst;
+                    for (size_t i = 0; i < out.nodes.size(); i++) map[i] = (int)i;
+                    for (int j = 0; j <= jm; j++)
+                        for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
+                            if (!(flags[i] & 1)) continue;
+                            src.push_back(i);
+                            dst.push_back(map[i]);
+                            if ((flags[i] & 3) != 3) continue;
+                            const int oi = map[i];
+                            out.createChildren(oi, false);
+                            const int c0 = out.nodes[oi].child0, p0 = prop.nodes[i].child0;
+                            if (j < jm && p0 >= 0)
+                                for (int c = 0; c < Tree<3>::tDim; c++) map[p0 + c] = c0 + c;
+                            if (j == jm)
+                                for (int c = 0; c < Tree<3>::tDim; c++) resume.work.push_back(c0 + c);
+                        }
+                    resume.tree = &out;
+                    resume.dinp = dinp;
+                    resume.dout = create_output(ctx, md, out, acc);
+                    resume.synced = out.nodes.size();
+                    resume.iter = jm + 1;
+                    resume.sNorm = norm_levels[3 * jm];
+                    resume.wNorm = norm_levels[3 * jm + 1];
+                    out.squareNorm = norm_levels[3 * jm + 2];
+                    ck(mwgpu_tree_copy_nodes(ctx, dprop, resume.dout, (int)src.size(), src.data(), dst.data()), "copy judged levels");
+                    ls.kept_nodes = (int)src.size();
+                    dinp = nullptr;  // owned by the continuation now
                 }
                 acc.node_terms = st.node_terms;
                 acc.components = st.components;
@@ -781,24 +819,39 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
             } catch (...) {
                 if (dprop) mwgpu_free_tree(ctx, dprop);
                 if (dinp) mwgpu_free_tree(ctx, dinp);
+                if (resume.dout) mwgpu_free_tree(ctx, resume.dout);
+                if (resume.dinp) mwgpu_free_tree(ctx, resume.dinp);
                 throw;
             }
             mwgpu_free_tree(ctx, dprop);
-            mwgpu_free_tree(ctx, dinp);
+            if (dinp) mwgpu_free_tree(ctx, dinp);
             mwgpu_launch_count(ctx, &l1);
             acc.launches = l1 - l0;
             ls.apply = acc;
         }
         ls.first_miss = first_miss;
         if (first_miss >= 0) {
-            // the judge refined a node the proposal left out: the plain apply decides
+            // the judge refined a node the proposal left out: the host loop
+            // continues from that level (missed splits appended)
             mwh_tree *o1[1] = {outp}, *i1[1] = {inpp};
             mwh_apply_stats pa{};
-            int rc = apply_impl(prec, 1, o1, operp, i1, -1, abs_prec, precision, &pa);
+            int rc = apply_impl(prec, 1, o1, operp, i1, -1, abs_prec, precision, &pa, &resume);
             if (rc) return rc;
-            pa.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-            ls.apply = pa;
             ls.fallback = 1;
+            ls.host_round_trips += pa.iterations + 1;
+            ls.apply.node_terms += pa.node_terms;
+            ls.apply.components += pa.components;
+            ls.apply.band_nodes += pa.band_nodes;
+            ls.apply.gen_nodes += pa.gen_nodes;
+            ls.apply.iterations += pa.iterations;
+            ls.apply.device_ms += pa.device_ms;
+            ls.apply.contract_ms += pa.contract_ms;
+            ls.apply.transform_ms = pa.transform_ms;
+            ls.apply.launches += pa.launches;
+            ls.apply.h2d_bytes += pa.h2d_bytes;
+            ls.apply.d2h_bytes += pa.d2h_bytes;
+            ls.apply.out_nodes = pa.out_nodes;
+            ls.apply.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             if (stats) *stats = ls;
             return 0;
         }

@@ -157,6 +157,7 @@ def evaluate(params, threshold, seeds, precision):
         rows.append({"seed": s, "out_nodes": g0.n_nodes, "plain_iterations": sp["iterations"], "plain_ms": 1e3 * t_plain,
                      "learned_ms": 1e3 * t_learned, "fallback": sl["fallback"], "first_miss": sl["first_miss"],
                      "proposal_nodes": sl["proposal_nodes"], "kept_nodes": sl["kept_nodes"], "round_trips": sl["host_round_trips"],
+                     "learned_iterations": sl["apply"]["iterations"], "node_terms": sl["apply"]["node_terms"],
                      "same_topology": bool(same), "max_rel_diff": diff})
     return rows
 
@@ -181,7 +182,7 @@ def main():
     X = np.concatenate([r[1] for r in tr])
     Y = np.concatenate([r[2] for r in tr])
     pos = float(Y.sum())
-    pos_weight = float(min(50.0, 4.0 * (len(Y) - pos) / max(pos, 1.0)))
+    pos_weight = float(min(50.0, (len(Y) - pos) / max(pos, 1.0)))
     params, curve, t_train = gpu_train(X, Y, a.epochs, a.batch, a.lr, pos_weight, 1234)
     # threshold: below the smallest P(split) of the refined nodes of `success` of the validation grids
     mins = []
@@ -189,11 +190,24 @@ def main():
         pr = gpu_prob(params, r[1])
         sp = pr[r[2] > 0.5]
         mins.append(float(sp.min()) if len(sp) else 1.0)
-    threshold = float(np.quantile(np.array(mins), 1.0 - a.success)) * 0.999
     import mrcpp_gb300 as mw
+    # candidate thresholds: complete proposals for `success` (and 90 %) of the
+    # validation grids, and 0.5; the one with the least learned-apply time on a
+    # part of the held-out set is kept
+    mins = np.array(mins)
+    cands = sorted({float(np.quantile(mins, 1.0 - a.success)) * 0.999, float(np.quantile(mins, 0.1)) * 0.999, 0.5, 0.7, 0.85})
+    probe = list(range(HELD_SEED0, HELD_SEED0 + min(a.held, 40)))
+    tune = []
+    for c in cands:
+        r = evaluate(params, c, probe, mw.MIXED)
+        tune.append({"threshold": c, "learned_ms": float(sum(x["learned_ms"] for x in r)), "plain_ms": float(sum(x["plain_ms"] for x in r)),
+                     "continued": float(np.mean([x["fallback"] for x in r]))})
+    threshold = min(tune, key=lambda t: t["learned_ms"])["threshold"]
     rows = evaluate(params, threshold, list(range(HELD_SEED0, HELD_SEED0 + a.held)), mw.MIXED)
+    split_in_input = float(X[Y > 0.5, 7].mean()) if pos > 0 else 0.0
     summ = {
         "train_densities": len(tr), "validation_densities": len(va), "held_out_densities": len(rows), "samples": int(len(Y)),
+        "refined_nodes_stored_in_input": split_in_input, "output_nodes_stored_in_input": float(X[:, 7].mean()), "threshold_tuning": tune,
         "positives": int(pos), "pos_weight": pos_weight, "epochs": a.epochs, "batch": a.batch, "lr": a.lr, "threshold": threshold,
         "loss_first_last": [float(curve[0]), float(curve[-1])], "train_s": t_train, "generate_s": t_gen,
         "held_out": {
@@ -204,11 +218,14 @@ def main():
             "learned_ms_total": float(sum(r["learned_ms"] for r in rows)),
             "plain_iterations_mean": float(np.mean([r["plain_iterations"] for r in rows])),
             "learned_round_trips_mean": float(np.mean([r["round_trips"] for r in rows])),
+            "learned_compute_iterations_mean": float(np.mean([r["learned_iterations"] for r in rows])),
+            "continued_after_miss": int(sum(r["fallback"] for r in rows)),
+            "first_miss_histogram": {str(k): int(v) for k, v in zip(*np.unique([r["first_miss"] for r in rows], return_counts=True))},
             "proposal_over_kept": float(np.sum([r["proposal_nodes"] for r in rows]) / max(1, np.sum([r["kept_nodes"] or 0 for r in rows]))),
         },
     }
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
-    np.savez(a.out, params=params, threshold=np.float64(threshold), loss_curve=curve, summary=json.dumps(summ))
+    np.savez(a.out, params=params, threshold=np.float64(threshold), loss_curve=curve, summary=json.dumps(summ), features=np.int32(2))
     if a.report:
         with open(a.report, "w") as fh:
             json.dump({"summary": summ, "held_out": rows}, fh, indent=1)
