@@ -59,6 +59,16 @@ struct Shape {
     static constexpr int MIN_BLOCKS = 2 * (SMEM_FLOATS * 4 + 1024) <= 228 * 1024 ? 2 : 1;
 };
 
+// Row c of a block handled by `lane` in its r-th row slot.  For K = 8 (P = 12)
+// the 8-row groups are interleaved so that the 32 scattered stores of
+// store_block hit disjoint banks (groups {0,2,4,6} then {1,3,5,7}); row loads
+// stay conflict-free (8 consecutive rows per quarter warp).
+template <int K>
+__device__ __forceinline__ int row_of(int lane, int r) {
+    if constexpr (K == 8 && padded_row(K) == 12) return (lane & 7) + 8 * (2 * (lane >> 3) + r);
+    else return lane + 32 * r;
+}
+
 // loads K consecutive floats
 template <int K, int IS>
 __device__ __forceinline__ void load_row(float (&a)[K], const float *base) {
@@ -103,7 +113,7 @@ __device__ __forceinline__ void task_block(const float *const (&in)[NS], const f
         float a[R][K];
 #pragma unroll
         for (int r = 0; r < R; r++) {
-            const int c = lane + 32 * r;
+            const int c = row_of<K>(lane, r);
             if (c < S::K2) load_row<K, S::P>(a[r], in[p] + S::P * c);
             else
 #pragma unroll
@@ -128,7 +138,7 @@ __device__ __forceinline__ void store_block(float *out, int lane, const float (&
     using S = Shape<K>;
 #pragma unroll
     for (int r = 0; r < S::R; r++) {
-        const int c = lane + 32 * r;
+        const int c = row_of<K>(lane, r);
         if (c < S::K2)
 #pragma unroll
             for (int j = 0; j < K; j++) out[(c % K) + S::P * (c / K + K * j)] = s[r][j];
@@ -225,7 +235,7 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
             for (int j = 0; j < K; j++) {
                 acc[r][j] = 0.f;
                 cmp[r][j] = 0.f;
-                const int c = lane + 32 * r;
+                const int c = row_of<K>(lane, r);
                 if (!S::KAHAN && c < K2) G64[warp * K3 + c + K2 * j] = 0.0;
             }
         const int it0 = ch.y, it1 = ch.z;
@@ -405,7 +415,7 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
             if (!S::KAHAN && ++since >= 16) {
 #pragma unroll
                 for (int r = 0; r < R; r++) {
-                    const int c = lane + 32 * r;
+                    const int c = row_of<K>(lane, r);
                     if (c < K2)
 #pragma unroll
                         for (int j = 0; j < K; j++) {
@@ -421,7 +431,7 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
         double *go = partial + (size_t)cix * 8 * K3;
 #pragma unroll
         for (int r = 0; r < R; r++) {
-            const int c = lane + 32 * r;
+            const int c = row_of<K>(lane, r);
             if (c < K2)
 #pragma unroll
                 for (int j = 0; j < K; j++) {

@@ -268,6 +268,96 @@ __global__ void k_mw_up(DevMRA m, DevTree t0, const DevTree *ts, const int *ptre
     block_norms(pc, K3, t.norms + (size_t)p * 8, tid, nthr);
 }
 
+// The transforms of the mixed form: the same three filter stages with FP32
+// products in shared memory, the children / parent coefficients kept in FP64.
+template <bool ADD>
+__device__ __forceinline__ void fapply(float *out, const float *in, const float *F, int K, int tid, int nthr) {
+    const int K2 = K * K, K3 = K2 * K;
+    for (int e = tid; e < K3; e += nthr) {
+        const int c = e % K2, j = e / K2;
+        const float *a = in + K * c;
+        const float *b = F + K * j;
+        float s = 0.f;
+        for (int i = 0; i < K; i++) s = fmaf(a[i], b[i], s);
+        if (ADD) out[c + K2 * j] += s;
+        else out[c + K2 * j] = s;
+    }
+}
+
+// filters of op (0 compression, 1 reconstruction) as floats: F[fidx * K2 + ...]
+__device__ __forceinline__ void load_filters32(float *F, const DevMRA &m, int op, int tid, int nthr) {
+    const int n = 4 * m.K * m.K;
+    const double *src = m.filt + (size_t)op * n;
+    for (int e = tid; e < n; e += nthr) F[e] = (float)src[e];
+}
+
+__global__ void k_mw_down32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite) {
+    extern __shared__ float sm32[];
+    const DevTree t = ptree ? ts[ptree[blockIdx.x]] : t0;
+    const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    float *pin = sm32, *t1 = pin + 8 * K3, *t2 = t1 + 8 * K3, *F = t2 + 8 * K3;
+    const int p = parents[blockIdx.x];
+    const int c0 = t.child0[p];
+    if (c0 < 0) return;
+    const double *in = t.coefs + (size_t)p * 8 * K3;
+    for (int e = tid; e < 8 * K3; e += nthr) pin[e] = (float)in[e];
+    load_filters32(F, m, 1, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) fapply<false>(t1 + gt * K3, pin + (gt & ~1) * K3, F + (2 * (gt & 1) + 0) * K2, K, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) fapply<true>(t1 + gt * K3, pin + (gt | 1) * K3, F + (2 * (gt & 1) + 1) * K2, K, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) fapply<false>(t2 + gt * K3, t1 + (gt & ~2) * K3, F + (2 * ((gt >> 1) & 1) + 0) * K2, K, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) fapply<true>(t2 + gt * K3, t1 + (gt | 2) * K3, F + (2 * ((gt >> 1) & 1) + 1) * K2, K, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) fapply<false>(t1 + gt * K3, t2 + (gt & ~4) * K3, F + (2 * ((gt >> 2) & 1) + 0) * K2, K, tid, nthr);
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) fapply<true>(t1 + gt * K3, t2 + (gt | 4) * K3, F + (2 * ((gt >> 2) & 1) + 1) * K2, K, tid, nthr);
+    __syncthreads();
+    // child gt receives the scaling block t1[gt] (its wavelet blocks are untouched: only the scaling part is passed down)
+    for (int e = tid; e < 8 * K3; e += nthr) {
+        const int gt = e / K3, r = e % K3;
+        double *o = t.coefs + (size_t)(c0 + gt) * 8 * K3;
+        if (overwrite) {
+            // overwrite: the child's whole block is replaced by its scaling part
+            for (int cc = 0; cc < 8; cc++)
+                if (cc == 0) o[r] = (double)t1[e];
+                else o[cc * K3 + r] = 0.0;
+        } else {
+            o[r] += (double)t1[e];
+        }
+    }
+    __syncthreads();
+    for (int gt = 0; gt < 8; gt++) block_norms(t.coefs + (size_t)(c0 + gt) * 8 * K3, K3, t.norms + (size_t)(c0 + gt) * 8, tid, nthr);
+}
+
+__global__ void k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n) {
+    extern __shared__ float sm32[];
+    const DevTree t = ptree ? ts[ptree[blockIdx.x]] : t0;
+    const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    float *t1 = sm32, *t2 = t1 + 8 * K3, *F = t2 + 8 * K3;
+    const int p = parents[blockIdx.x];
+    const int c0 = t.child0[p];
+    if (c0 < 0) return;
+    for (int e = tid; e < 8 * K3; e += nthr) t1[e] = (float)t.coefs[(size_t)(c0 + e / K3) * 8 * K3 + e % K3];
+    load_filters32(F, m, 0, tid, nthr);
+    __syncthreads();
+    float *bufs[2] = {t1, t2};
+    for (int d = 0; d < 3; d++) {
+        float *inb = bufs[d & 1], *outb = bufs[(d + 1) & 1];
+        const int mask = 1 << d;
+        for (int gt = 0; gt < 8; gt++) fapply<false>(outb + gt * K3, inb + (gt & ~mask) * K3, F + (2 * ((gt >> d) & 1) + 0) * K2, K, tid, nthr);
+        __syncthreads();
+        for (int gt = 0; gt < 8; gt++) fapply<true>(outb + gt * K3, inb + (gt | mask) * K3, F + (2 * ((gt >> d) & 1) + 1) * K2, K, tid, nthr);
+        __syncthreads();
+    }
+    double *pc = t.coefs + (size_t)p * 8 * K3;
+    for (int e = tid; e < 8 * K3; e += nthr) pc[e] = (double)t2[e];
+    __syncthreads();
+    block_norms(pc, K3, t.norms + (size_t)p * 8, tid, nthr);
+}
+
 __global__ void k_to_float(const double *src, float *dst, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = (float)src[i];
 }
@@ -336,15 +426,28 @@ void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cuda
     k_node_norms<<<n, 128, 0, s>>>(m, t, nodes, n);
 }
 
-void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite, cudaStream_t s) {
+void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite, cudaStream_t s,
+                    bool fp32) {
     if (n <= 0) return;
+    if (fp32) {
+        const size_t sm = sizeof(float) * (24 * (size_t)m.kp1_d + 4 * m.K * m.K);
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k_mw_down32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_mw_down32<<<n, 256, sm, s>>>(m, t, ts, ptree, parents, n, overwrite);
+        return;
+    }
     size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_mw_down<<<n, 256, smem, s>>>(m, t, ts, ptree, parents, n, overwrite);
 }
 
-void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s) {
+void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s, bool fp32) {
     if (n <= 0) return;
+    if (fp32) {
+        const size_t sm = sizeof(float) * (16 * (size_t)m.kp1_d + 4 * m.K * m.K);
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k_mw_up32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_mw_up32<<<n, 256, sm, s>>>(m, t, ts, ptree, parents, n);
+        return;
+    }
     size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_up, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_mw_up<<<n, 256, smem, s>>>(m, t, ts, ptree, parents, n);

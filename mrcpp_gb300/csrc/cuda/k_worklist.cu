@@ -83,6 +83,16 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
             band = 1;
             const DevTree &f = fs[pc.tree];
             const double gthr = gthrs[pc.tree];
+            // Norm test oNorm * fThr > gThreshold: without screening (gThreshold < 0)
+            // every structural component passes; otherwise an FP32 estimate decides
+            // when it is clear of the threshold by far more than its rounding
+            // error (2^-12 relative against < 2^-20), and the FP64 expression of
+            // the reference decides the rest.  For 1e-20 < gThreshold < 1e20 an
+            // FP32 underflow of one factor can only happen for products far below
+            // the threshold (the other factors are bounded by 1e12).
+            const bool screen = !(gthr < 0.0);
+            const bool fp32 = gthr > 1e-20 && gthr < 1e20;
+            const float thr_hi = (float)(gthr * (1.0 + 1.0 / 4096.0)), thr_lo = (float)(gthr * (1.0 - 1.0 / 4096.0));
             double fn[8];
             bool any = false;
             for (int c = 0; c < 8; c++) {
@@ -101,10 +111,12 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
                 for (int c = 0; c < 4; c++) wd[c] = bwi[c];
                 bool inb[3][4];
                 double nrm[3][4];
+                float nrf[3][4];
                 for (int d = 0; d < 3; d++)
                     for (int c = 0; c < 4; c++) {
                         inb[d][c] = abs(pc.tl[d]) <= wd[c];
-                        nrm[d][c] = inb[d][c] ? op.norms[(size_t)(off + pc.tl[d] + L0) * 4 + c] : 0.0;
+                        nrm[d][c] = (screen && inb[d][c]) ? op.norms[(size_t)(off + pc.tl[d] + L0) * 4 + c] : 0.0;
+                        nrf[d][c] = (float)nrm[d][c];
                     }
                 // band-size factor 64 * prod_d (2 w(2 a_d + b_d) + 1) over directions with w >= 0
                 int fac[4];
@@ -119,11 +131,23 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
                         if (!(inb[0][i0] && inb[1][i1] && inb[2][i2])) continue;
                         const unsigned long long bit = 1ull << (ft * 8 + gt);
                         smask |= bit;
+                        if (!screen) {
+                            mask |= bit;
+                            continue;
+                        }
+                        const int bsz = fac[i0] * fac[i1] * fac[i2] * 64;
+                        if (fp32) {
+                            const float est = nrf[0][i0] * nrf[1][i1] * nrf[2][i2] * ((float)bsz * (float)fNorm);
+                            if (est > thr_hi) {
+                                mask |= bit;
+                                continue;
+                            }
+                            if (est < thr_lo) continue;
+                        }
                         double oNorm = 1.0;
                         oNorm *= nrm[0][i0];
                         oNorm *= nrm[1][i1];
                         oNorm *= nrm[2][i2];
-                        const int bsz = fac[i0] * fac[i1] * fac[i2] * 64;
                         const double fThr = (double)bsz * fNorm;
                         if (oNorm * fThr > gthr) mask |= bit;
                     }

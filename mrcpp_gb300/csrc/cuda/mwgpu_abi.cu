@@ -587,14 +587,15 @@ mwgpu_status transform_impl(mwgpu_ctx *ctx, int nt, mwgpu_tree *const *trees, in
     }
     const DevMRA &m = trees[0]->mra;
     const DevTree &t0 = trees[0]->t;
+    const bool fp32 = ctx->precision == MWGPU_PREC_MIXED;  // FP32 filter products in the mixed form
     if (direction == MWGPU_TOPDOWN) {
         for (auto &r : ranges) {
-            launch_mw_down(m, t0, ts, ptree ? ptree + r.first : nullptr, ctx->d_list + r.first, r.second, overwrite != 0, ctx->stream);
+            launch_mw_down(m, t0, ts, ptree ? ptree + r.first : nullptr, ctx->d_list + r.first, r.second, overwrite != 0, ctx->stream, fp32);
             ctx->launches += r.second > 0;
         }
     } else {
         for (int l = (int)ranges.size() - 1; l >= 0; l--) {
-            launch_mw_up(m, t0, ts, ptree ? ptree + ranges[l].first : nullptr, ctx->d_list + ranges[l].first, ranges[l].second, ctx->stream);
+            launch_mw_up(m, t0, ts, ptree ? ptree + ranges[l].first : nullptr, ctx->d_list + ranges[l].first, ranges[l].second, ctx->stream, fp32);
             ctx->launches += ranges[l].second > 0;
         }
     }
@@ -1269,11 +1270,13 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
     if (pl->flags & MWGPU_PLAN_TRANSFORMS) {
         const mwgpu_tree *t0 = pl->outs[0];
         for (auto &r : pl->ranges) {
-            launch_mw_down(t0->mra, t0->t, pl->d_gs, pl->d_ltree + r.first, pl->d_list + r.first, r.second, false, st);
+            launch_mw_down(t0->mra, t0->t, pl->d_gs, pl->d_ltree + r.first, pl->d_list + r.first, r.second, false, st,
+                           pl->precision == MWGPU_PREC_MIXED);
             ctx->launches += r.second > 0;
         }
         for (int l = (int)pl->ranges.size() - 1; l >= 0; l--) {
-            launch_mw_up(t0->mra, t0->t, pl->d_gs, pl->d_ltree + pl->ranges[l].first, pl->d_list + pl->ranges[l].first, pl->ranges[l].second, st);
+            launch_mw_up(t0->mra, t0->t, pl->d_gs, pl->d_ltree + pl->ranges[l].first, pl->d_list + pl->ranges[l].first, pl->ranges[l].second, st,
+                         pl->precision == MWGPU_PREC_MIXED);
             ctx->launches += pl->ranges[l].second > 0;
         }
     }
@@ -1809,11 +1812,11 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             }
             MW_CK(cudaMemcpyAsync(ctx->d_list, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice, st));
             for (auto &r : ranges) {
-                launch_mw_down(out->mra, out->t, nullptr, nullptr, ctx->d_list + r.first, r.second, false, st);
+                launch_mw_down(out->mra, out->t, nullptr, nullptr, ctx->d_list + r.first, r.second, false, st, mixed);
                 ctx->launches += r.second > 0;
             }
             for (int l = (int)ranges.size() - 1; l >= 0; l--) {
-                launch_mw_up(out->mra, out->t, nullptr, nullptr, ctx->d_list + ranges[l].first, ranges[l].second, st);
+                launch_mw_up(out->mra, out->t, nullptr, nullptr, ctx->d_list + ranges[l].first, ranges[l].second, st, mixed);
                 ctx->launches += ranges[l].second > 0;
             }
             MW_CK(cudaGetLastError());

@@ -173,8 +173,10 @@ void launch_copy_nodes(const DevTree &src, const DevTree &dst, const int *sid, c
 void launch_stamp(unsigned long long *t, cudaStream_t s);
 void launch_gather_norms(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst, cudaStream_t s);
 void launch_node_norms(const DevMRA &m, DevTree t, const int *nodes, int n, cudaStream_t s);
-void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite, cudaStream_t s);
-void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s);
+// fp32: FP32 filter products (the mixed form), coefficients stay FP64
+void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite, cudaStream_t s,
+                    bool fp32 = false);
+void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s, bool fp32 = false);
 void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s);
 void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *err, cudaStream_t s);
 
