@@ -288,21 +288,24 @@ mwgpu_status mwgpu_mlp_train(mwgpu_ctx *ctx, mwgpu_mlp *mlp, const float *x, con
  * children (child0) in the next level, and the nodes are ordered by level,
  * each level in the order of its parents (the order TreeBuilder creates
  * nodes): nodes level_begin[j] .. level_begin[j+1]-1 form level j.
- * Level j computes the nodes the split test kept (the roots, then the
- * children of refined nodes) with the screening threshold of the tree norm of
- * the levels before (out_sqnorm at the start), adds their norms to the tree
- * norm in TreeBuilder's order and judges them with split_check (prec,
- * abs_prec, splitFac 1).  flags_out[i]: bit 0 = node of the judged tree,
- * bit 1 = refined.  first_miss = the first level where a refined node had no
- * proposed children (-1: none); the result is then exact up to that level
- * only.  With `transforms` and no miss, TopDown(add) and BottomUp run over the
- * judged tree.  norm_levels (3*n_levels, may be NULL) gets TreeBuilder's
- * sNorm, wNorm and tree norm after each level (to continue the loop on the
- * host after a miss).  Equal to mwgpu_apply_level driven by the host
- * TreeBuilder on the judged tree whenever first_miss is -1. */
+ * Level j computes the nodes the split test kept (the nodes of first_level,
+ * then the children of refined nodes) with the screening threshold of the tree
+ * norm of the levels before, adds their norms to the tree norm in
+ * TreeBuilder's order and judges them with split_check (prec, abs_prec,
+ * splitFac 1).  Levels before first_level are a judged tree computed earlier
+ * (their coefficients already in `out`; refined = has children); state_in =
+ * TreeBuilder's sNorm, wNorm and tree norm after them ({0, 0, out's tree norm}
+ * for first_level 0).  flags_out[i]: bit 0 = node of the judged tree, bit 1 =
+ * refined.  first_miss = the first level where a refined node had no proposed
+ * children (-1: none); the result is then exact up to that level only.  With
+ * `transforms` and no miss, TopDown(add) and BottomUp run over the judged
+ * tree.  norm_levels (3*n_levels, may be NULL) gets sNorm, wNorm and the tree
+ * norm after each computed level (to continue after a miss).  Equal to
+ * mwgpu_apply_level driven by the host TreeBuilder on the judged tree
+ * whenever first_miss is -1. */
 mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, int n_levels,
-                                const int *level_begin, double prec, int abs_prec, double out_sqnorm, int transforms, int *flags_out,
-                                int *first_miss, double *norm_levels, mwgpu_level_stats *stats);
+                                const int *level_begin, double prec, int abs_prec, int first_level, const double *state_in, int transforms,
+                                int *flags_out, int *first_miss, double *norm_levels, mwgpu_level_stats *stats);
 /* Copies coefficients and norms of nodes src_ids[j] of src to dst_ids[j] of dst. */
 mwgpu_status mwgpu_tree_copy_nodes(mwgpu_ctx *ctx, const mwgpu_tree *src, mwgpu_tree *dst, int n, const int *src_ids, const int *dst_ids);
 

@@ -99,13 +99,15 @@ int mwh_apply_batch(double prec, int n, mwh_tree **outs, mwh_oper *oper, mwh_tre
                     mwh_apply_stats *stats);
 
 /* Learned output grid (no reference counterpart): the network proposes the
- * output grid level by level (features + inference on the GPU), then one
- * mwgpu_apply_judged pass computes and judges it with the split test.  The
- * result equals mwh_apply(prec, out, oper, inp, -1, abs_prec, precision).
- * When the judge refines a node of level j that the proposal did not, levels
- * 0..j are kept and the host TreeBuilder loop continues from level j+1 with
- * the missed children appended (fallback = 1, first_miss = j).  `out` must be
- * a fresh tree (root nodes only), else the plain apply runs. */
+ * output grid level by level (features + inference on the GPU; the first
+ * full_levels levels are refined without asking it), then a
+ * mwgpu_apply_judged pass computes and judges it with the split test.  When
+ * the judge refines a node of level j that the proposal did not, levels 0..j
+ * are kept, all children of the refined nodes of level j are added, the
+ * network proposes below them and another judged pass continues from level
+ * j+1 (fallback = 1, first_miss = j of the first pass).  The result equals
+ * mwh_apply(prec, out, oper, inp, -1, abs_prec, precision).  `out` must be a
+ * fresh tree (root nodes only), else the plain apply runs. */
 typedef struct mwh_mlp mwh_mlp;
 typedef struct {
     mwh_apply_stats apply;   /* of the judged pass (or of the plain fallback) */
@@ -114,8 +116,8 @@ typedef struct {
 } mwh_learned_stats;
 int mwh_mlp_create(const float *params, mwh_mlp **out);
 void mwh_mlp_free(mwh_mlp *mlp);
-int mwh_apply_learned(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, const mwh_mlp *mlp, double threshold, int abs_prec,
-                      int precision, mwh_learned_stats *stats);
+int mwh_apply_learned(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, const mwh_mlp *mlp, double threshold, int full_levels,
+                      int abs_prec, int precision, mwh_learned_stats *stats);
 /* Training data: features (n*8) of every node of `grid` (e.g. the output of a
  * plain apply of oper on inp) in the order of the tree export (breadth first),
  * and labels (1 = the node has children).  n = number of nodes of grid. */

@@ -111,7 +111,7 @@ _SIGS = {
     "mwgpu_plan_info": (C.c_int, [_P, C.POINTER(C.c_longlong), _PI, _PI, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_ulonglong)]),
     "mwgpu_plan_destroy": (C.c_int, [_P, _P]),
     "mwgpu_tree_update_coefs": (C.c_int, [_P, _P, _PD, _PD]),
-    "mwgpu_apply_judged": (C.c_int, [_P, _P, _P, _P, C.c_int, _PI, C.c_double, C.c_int, C.c_double, C.c_int, _PI, _PI, _PD,
+    "mwgpu_apply_judged": (C.c_int, [_P, _P, _P, _P, C.c_int, _PI, C.c_double, C.c_int, C.c_int, _PD, C.c_int, _PI, _PI, _PD,
                                      C.POINTER(MwgpuLevelStats)]),
     "mwgpu_mlp_create": (C.c_int, [_P, _PF, C.POINTER(_P)]),
     "mwgpu_mlp_destroy": (C.c_int, [_P, _P]),
@@ -160,7 +160,7 @@ _SIGS = {
                                   C.POINTER(MwhApplyStats)]),
     "mwh_mlp_create": (C.c_int, [_PF, C.POINTER(_P)]),
     "mwh_mlp_free": (None, [_P]),
-    "mwh_apply_learned": (C.c_int, [C.c_double, _P, _P, _P, _P, C.c_double, C.c_int, C.c_int, C.POINTER(MwhLearnedStats)]),
+    "mwh_apply_learned": (C.c_int, [C.c_double, _P, _P, _P, _P, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(MwhLearnedStats)]),
     "mwh_grid_features": (C.c_int, [C.c_double, _P, _P, _P, _PF, _PF]),
 }
 
@@ -452,14 +452,15 @@ class GridNetwork:
             self._h = None
 
 
-def apply_learned(prec, out, oper, inp, network, threshold=0.3, abs_prec=False, precision=FP64):
+def apply_learned(prec, out, oper, inp, network, threshold=0.3, full_levels=0, abs_prec=False, precision=FP64):
     """mrcpp::apply(prec, out, oper, inp) with the output grid proposed by the
-    network and judged on the device by the split test: the result equals
+    network (the first `full_levels` levels refined without it) and judged on
+    the device by the split test: the result equals
     apply(prec, out, oper, inp, precision=precision).  Returns the statistics
-    (proposal size, first missed level, fallback, round trips, timings)."""
+    (proposal size, first missed level, further passes, round trips, timings)."""
     st = MwhLearnedStats()
-    _ck(lib().mwh_apply_learned(float(prec), out._h, oper._h, inp._h, network._h, float(threshold), int(bool(abs_prec)), int(precision),
-                                C.byref(st)))
+    _ck(lib().mwh_apply_learned(float(prec), out._h, oper._h, inp._h, network._h, float(threshold), int(full_levels), int(bool(abs_prec)),
+                                int(precision), C.byref(st)))
     return st.as_dict()
 
 

@@ -55,7 +55,15 @@ struct Shape {
     static constexpr bool KAHAN = K <= 8;                // compensated FP32 accumulators in registers; else FP64 in shared memory
     static constexpr int CG = K >= 10 ? 2 : 4;           // f components per group (component schedule)
     static constexpr int NBUF = CG == 2 ? 18 : 24;       // work blocks
-    static constexpr int SMEM_FLOATS = 8 * BLK + NBUF * BLK + 3 * 12 * K2 + (KAHAN ? 0 : 2 * 8 * K3);
+    // k = 7: the products run on the tensor cores (mma.sync m16n8k8, TF32 with
+    // a hi/lo split of both operands, 3 products per FP32 product); the
+    // intermediates are then stored column by column, element (c, j) of an
+    // output block at j S1 + (c % 8) + 12 (c / 8), S1 = 100: conflict-free
+    // fragment loads and stores
+    static constexpr bool MMA = K == 8;
+    static constexpr int S1 = 100;
+    static constexpr int IB = MMA ? K * S1 : BLK;        // one intermediate block
+    static constexpr int SMEM_FLOATS = 8 * BLK + NBUF * IB + 3 * 12 * K2 + (KAHAN ? 0 : 2 * 8 * K3);
     static constexpr int MIN_BLOCKS = 2 * (SMEM_FLOATS * 4 + 1024) <= 228 * 1024 ? 2 : 1;
 };
 
@@ -145,6 +153,118 @@ __device__ __forceinline__ void store_block(float *out, int lane, const float (&
     }
 }
 
+// ---- tensor-core path (K = 8) ----
+__device__ __forceinline__ unsigned to_tf32(float x) {
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+// x = hi + lo with hi, lo TF32 (22 significant bits together)
+__device__ __forceinline__ void split_tf32(float x, unsigned &hi, unsigned &lo) {
+    hi = to_tf32(x);
+    lo = to_tf32(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3, unsigned b0, unsigned b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// (c, j) of accumulator element e = 4 mt + v of a lane (C fragment of m-tile mt)
+__device__ __forceinline__ void mma_cj(int lane, int e, int &c, int &j) {
+    const int mt = e >> 2, v = e & 3;
+    c = 16 * mt + (lane >> 2) + 8 * (v >> 1);
+    j = 2 * (lane & 3) + (v & 1);
+}
+
+// One warp task on the tensor cores: the 64 x 8 output block as 4 m-tiles of
+// m16n8k8.  A(c, i): staged f (FIN, row c at P c) or an intermediate block
+// (element (i + K (c % K), c / K) of its producer at (c / K) S1 + i + 12 (c % K));
+// B(i, j) = O(i, j) from the transposed operator block.  s holds the C
+// fragments: d[mt][v] = s[mt >> 1][4 (mt & 1) + v].
+template <int K, int NS, bool FIN>
+__device__ __forceinline__ void task_mma(const float *const (&in)[NS], const float *const (&O)[NS], unsigned valid, int lane,
+                                         float (&s)[Shape<K>::R][K]) {
+    using S = Shape<K>;
+    static_assert(K == 8, "tensor-core path for K = 8");
+    const int g = lane >> 2, t = lane & 3;
+    float d[4][4];
+#pragma unroll
+    for (int mt = 0; mt < 4; mt++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) d[mt][v] = 0.f;
+#pragma unroll
+    for (int p = 0; p < NS; p++) {
+        if (!((valid >> p) & 1u)) continue;
+        unsigned bh0, bl0, bh1, bl1;
+        split_tf32(O[p][g + K * t], bh0, bl0);
+        split_tf32(O[p][g + K * (t + 4)], bh1, bl1);
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) {
+            float x[4];
+            if (FIN) {
+                const float *r0 = in[p] + S::P * (16 * mt + g), *r1 = in[p] + S::P * (16 * mt + g + 8);
+                x[0] = r0[t];
+                x[1] = r1[t];
+                x[2] = r0[t + 4];
+                x[3] = r1[t + 4];
+            } else {
+                const float *r0 = in[p] + (2 * mt) * S::S1 + 12 * g, *r1 = in[p] + (2 * mt + 1) * S::S1 + 12 * g;
+                x[0] = r0[t];
+                x[1] = r1[t];
+                x[2] = r0[t + 4];
+                x[3] = r1[t + 4];
+            }
+            unsigned ah[4], al[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) split_tf32(x[q], ah[q], al[q]);
+            mma_tf32(d[mt], al[0], al[1], al[2], al[3], bh0, bh1);
+            mma_tf32(d[mt], ah[0], ah[1], ah[2], ah[3], bl0, bl1);
+            mma_tf32(d[mt], ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+        }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 4; mt++)
+#pragma unroll
+        for (int v = 0; v < 4; v++) s[mt >> 1][4 * (mt & 1) + v] = d[mt][v];
+}
+
+// stores C fragments into an intermediate block: element (c, j) at j S1 + (c % 8) + 12 (c / 8)
+template <int K>
+__device__ __forceinline__ void store_mma(float *out, int lane, const float (&s)[Shape<K>::R][K]) {
+    using S = Shape<K>;
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        int c, j;
+        mma_cj(lane, e, c, j);
+        out[j * S::S1 + (c & 7) + 12 * (c >> 3)] = s[e >> 3][e & 7];
+    }
+}
+
+// one warp task / store on either path
+template <int K, int NS, bool FIN>
+__device__ __forceinline__ void task(const float *const (&in)[NS], const float *const (&O)[NS], unsigned valid, int lane,
+                                     float (&s)[Shape<K>::R][K]) {
+    if constexpr (Shape<K>::MMA) task_mma<K, NS, FIN>(in, O, valid, lane, s);
+    else task_block<K, NS>(in, O, valid, lane, s);
+}
+template <int K>
+__device__ __forceinline__ void store(float *out, int lane, const float (&s)[Shape<K>::R][K]) {
+    if constexpr (Shape<K>::MMA) store_mma<K>(out, lane, s);
+    else store_block<K>(out, lane, s);
+}
+// (c, j) of accumulator element (r, jj) of a lane
+template <int K>
+__device__ __forceinline__ void acc_cj(int lane, int r, int jj, int &c, int &j) {
+    if constexpr (Shape<K>::MMA) mma_cj(lane, r * K + jj, c, j);
+    else {
+        c = row_of<K>(lane, r);
+        j = jj;
+    }
+}
+
 __device__ __forceinline__ void cp_async16(float *dst, const float *src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
@@ -177,21 +297,27 @@ __device__ __forceinline__ void stage_f(float *fb, const WorkItem &item, int f_c
     }
 }
 
-// the item's operator blocks [x, y, z][T, C, B, A], zero outside the band,
-// each K x K block transposed (row i = O(i, 0..K-1))
+// the item's operator blocks [x, y, z][T, C, B, A] (transposed FP32 copies),
+// zero outside the band: cp.async copies of whole blocks
 template <int K>
 __device__ __forceinline__ void stage_ob(float *ob, const DevOper &op, const WorkItem &item, int depth) {
     using S = Shape<K>;
     const int i = item.term;
     const int *bwi = op.bw + ((size_t)i * op.max_rows + depth) * 5;
     const int L0 = op.dep_L[i * op.max_rows + depth], off = op.dep_off[i * op.max_rows + depth];
-    for (int e = threadIdx.x; e < 12 * S::K2; e += S::NT) {
-        const int d = e / (4 * S::K2), r = e % (4 * S::K2), c = r / S::K2, ij = r % S::K2;
+    constexpr int CH = S::K2 % 4 == 0 ? 4 : 1, PER = S::K2 / CH;
+    for (int e = threadIdx.x; e < 12 * PER; e += S::NT) {
+        const int blk = e / PER, q = e % PER, d = blk >> 2, c = blk & 3;
         const int l = d == 0 ? item.tl[0] : (d == 1 ? item.tl[1] : item.tl[2]);
-        float v = 0.f;
-        if (off >= 0 && abs(l) <= bwi[c] && abs(l) <= L0) v = op.blocks32[(size_t)(off + l + L0) * 4 * S::K2 + r];
-        // column-major O(i, j) at i + K j is stored transposed, at j + K i
-        ob[e - ij + (ij / K) + K * (ij % K)] = v;
+        float *dst = ob + blk * S::K2 + CH * q;
+        if (off >= 0 && abs(l) <= bwi[c] && abs(l) <= L0) {
+            const float *src = op.blocks32 + (size_t)(off + l + L0) * 4 * S::K2 + c * S::K2 + CH * q;
+            if constexpr (CH == 4) cp_async16(dst, src);
+            else cp_async4(dst, src);
+        } else {
+            if constexpr (CH == 4) *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+            else *dst = 0.f;
+        }
     }
 }
 
@@ -211,11 +337,11 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                                                                                      const int4 *chunks, const WorkItem *items, double *partial,
                                                                                      int *err, const int *n_chunks_dev, int *counter) {
     using S = Shape<K>;
-    constexpr int K2 = S::K2, K3 = S::K3, BLK = S::BLK, R = S::R, NW = S::NW, CG = S::CG;
+    constexpr int K2 = S::K2, K3 = S::K3, BLK = S::BLK, IB = S::IB, R = S::R, NW = S::NW, CG = S::CG;
     extern __shared__ __align__(16) float smf[];
     float *FB = smf;                                  // 8 staged f blocks
     float *BUF = FB + 8 * BLK;                        // NBUF work blocks
-    float *OBS = BUF + S::NBUF * BLK;                 // 3 x [3 dirs][4 comps] K x K
+    float *OBS = BUF + S::NBUF * IB;                  // 3 x [3 dirs][4 comps] K x K
     double *G64 = (double *)(OBS + 3 * 12 * K2);      // FP64 accumulators (without KAHAN)
     __shared__ int s_next;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -232,10 +358,11 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
 #pragma unroll
         for (int r = 0; r < R; r++)
 #pragma unroll
-            for (int j = 0; j < K; j++) {
-                acc[r][j] = 0.f;
-                cmp[r][j] = 0.f;
-                const int c = row_of<K>(lane, r);
+            for (int jj = 0; jj < K; jj++) {
+                acc[r][jj] = 0.f;
+                cmp[r][jj] = 0.f;
+                int c, j;
+                acc_cj<K>(lane, r, jj, c, j);
                 if (!S::KAHAN && c < K2) G64[warp * K3 + c + K2 * j] = 0.0;
             }
         const int it0 = ch.y, it1 = ch.z;
@@ -254,14 +381,6 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
             WorkItem nx = item;
             if (has_next) nx = items[it + 1];
             const float *OX = OBS + (k % 3) * 12 * K2, *OY = OX + 4 * K2, *OZ = OX + 8 * K2;
-            const int *bwi = op.bw + ((size_t)item.term * op.max_rows + depth) * 5;
-            int ib[3] = {0, 0, 0};  // bit c of ib[d]: |l_d| within the band of component c
-#pragma unroll
-            for (int d = 0; d < 3; d++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) ib[d] |= (abs((int)item.tl[d]) <= bwi[c]) << c;
-            unsigned nzm = 0;
-            for (int b = 0; b < 8; b++) nzm |= (((item.mask >> (8 * b)) & 0xffull) != 0ull) << b;
             const bool block = item.flags & 1;
             int last = 0, nsub = 1;
             if (!block) {
@@ -277,42 +396,22 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                 }
                 float sv[R][K];
                 if (block) {
-                    const bool pure = depth != 0 && (nzm & 1u);
-                    unsigned y0 = 0, y1 = 0;
-                    for (int o = 0; o < 8; o++) {
-                        const int a0 = o & 1, b12 = o & 6;
-                        for (int b0 = 0; b0 < 2; b0++) {
-                            const int src = b0 + b12;
-                            if (((nzm >> src) & 1u) && ((ib[0] >> (2 * a0 + b0)) & 1) && !(pure && src == 0 && a0 == 0)) y0 |= 1u << o;
-                        }
-                    }
-                    if (pure && (ib[0] & 1)) y0 |= 1u << 8;
-                    for (int q = 0; q < 8; q++) {
-                        const int a0 = q & 1, a1 = (q >> 1) & 1, b2 = q >> 2;
-                        for (int b1 = 0; b1 < 2; b1++)
-                            if (((y0 >> (a0 + 2 * b1 + 4 * b2)) & 1u) && ((ib[1] >> (2 * a1 + b1)) & 1)) y1 |= 1u << q;
-                        if (q == 2 && ((y0 >> 8) & 1u) && ((ib[1] >> 2) & 1)) y1 |= 1u << q;
-                    }
-                    if (((y0 >> 8) & 1u) && (ib[1] & 1)) y1 |= 1u << 8;
-                    float *Y0 = BUF, *U = BUF + 8 * BLK, *Y1 = BUF + 9 * BLK, *PP = BUF + 17 * BLK;
+                    // stage structure from the work-list builder (k_worklist.cu)
+                    const unsigned long long sc = item.sched;
+                    float *Y0 = BUF, *U = BUF + 8 * IB, *Y1 = BUF + 9 * IB, *PP = BUF + 17 * IB;
                     // stage 0: outputs Y0[o] (o < 8) and U (o = 8)
                     for (int o = warp; o < 9; o += NW) {
-                        if (!((y0 >> o) & 1u)) continue;
+                        unsigned valid = o < 8 ? (unsigned)((sc >> (2 * o)) & 3ull) : (unsigned)((sc >> 16) & 1ull);
+                        if (!valid) continue;
                         const int a0 = o & 1, b12 = o & 6;  // src = b0 + b12
                         const float *in[2] = {FB + b12 * BLK, FB + (b12 + 1) * BLK};
                         const float *O[2] = {OX + 2 * a0 * K2, OX + (2 * a0 + 1) * K2};
-                        unsigned valid = 0;
-                        for (int b0 = 0; b0 < 2; b0++) {
-                            const int src = b0 + b12;
-                            if (((nzm >> src) & 1u) && ((ib[0] >> (2 * a0 + b0)) & 1) && !(pure && src == 0 && a0 == 0)) valid |= 1u << b0;
-                        }
                         if (o == 8) {  // U = O^x_T f[0]
                             in[0] = FB;
                             O[0] = OX;
-                            valid = 1u;
                         }
-                        task_block<K, 2>(in, O, valid, lane, sv);
-                        store_block<K>(o < 8 ? Y0 + o * BLK : U, lane, sv);
+                        task<K, 2, true>(in, O, valid, lane, sv);
+                        store<K>(o < 8 ? Y0 + o * IB : U, lane, sv);
                     }
                     __syncthreads();
                     if (has_next) {  // the staged f block is free: the next item's f and operator blocks
@@ -321,37 +420,31 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                     }
                     // stage 1: outputs Y1[q] (q < 8) and PP (q = 8)
                     for (int q = warp; q < 9; q += NW) {
-                        if (!((y1 >> q) & 1u)) continue;
+                        unsigned valid = q < 8 ? (unsigned)((sc >> (17 + 2 * q)) & 3ull) | (q == 2 ? (unsigned)((sc >> 33) & 1ull) << 2 : 0u)
+                                               : (unsigned)((sc >> 34) & 1ull);
+                        if (!valid) continue;
                         const int a0 = q & 1, a1 = (q >> 1) & 1, b2 = q >> 2;
-                        const float *in[3] = {Y0 + (a0 + 4 * b2) * BLK, Y0 + (a0 + 2 + 4 * b2) * BLK, U};
+                        const float *in[3] = {Y0 + (a0 + 4 * b2) * IB, Y0 + (a0 + 2 + 4 * b2) * IB, U};  // U -> (0, 1, 0)
                         const float *O[3] = {OY + 2 * a1 * K2, OY + (2 * a1 + 1) * K2, OY + 2 * K2};
-                        unsigned valid = 0;
-                        for (int b1 = 0; b1 < 2; b1++)
-                            if (((y0 >> (a0 + 2 * b1 + 4 * b2)) & 1u) && ((ib[1] >> (2 * a1 + b1)) & 1)) valid |= 1u << b1;
-                        if (q == 2 && ((y0 >> 8) & 1u) && ((ib[1] >> 2) & 1)) valid |= 4u;  // U -> (a0, a1, b2) = (0, 1, 0)
                         if (q == 8) {  // P = O^y_T U
                             in[0] = U;
                             O[0] = OY;
-                            valid = 1u;
                         }
-                        task_block<K, 3>(in, O, valid, lane, sv);
-                        store_block<K>(q < 8 ? Y1 + q * BLK : PP, lane, sv);
+                        task<K, 3, false>(in, O, valid, lane, sv);
+                        store<K>(q < 8 ? Y1 + q * IB : PP, lane, sv);
                     }
                     __syncthreads();
-                    // stage 2: g component gt = warp
+                    // stage 2: g component gt = warp; P -> (0, 0, 1), while P -> (0, 0, 0) is
+                    // the dropped s->s product
                     {
                         const int gt = warp, a2 = gt >> 2;
-                        const float *in[3] = {Y1 + (gt & 3) * BLK, Y1 + ((gt & 3) + 4) * BLK, PP};
+                        const float *in[3] = {Y1 + (gt & 3) * IB, Y1 + ((gt & 3) + 4) * IB, PP};
                         const float *O[3] = {OZ + 2 * a2 * K2, OZ + (2 * a2 + 1) * K2, OZ + 2 * K2};
-                        unsigned valid = 0;
-                        for (int b2 = 0; b2 < 2; b2++)
-                            if (((y1 >> ((gt & 3) + 4 * b2)) & 1u) && ((ib[2] >> (2 * a2 + b2)) & 1)) valid |= 1u << b2;
-                        // P -> (0, 0, 1); P -> (0, 0, 0) is the dropped s->s product
-                        if (gt == 4 && ((y1 >> 8) & 1u) && ((ib[2] >> 2) & 1)) valid |= 4u;
-                        task_block<K, 3>(in, O, valid, lane, sv);
+                        const unsigned valid = (unsigned)((sc >> (35 + 2 * gt)) & 3ull) | (gt == 4 ? (unsigned)((sc >> 51) & 1ull) << 2 : 0u);
+                        task<K, 3, false>(in, O, valid, lane, sv);
                     }
                 } else {
-                    float *X0 = BUF, *X1 = BUF + 2 * CG * BLK;
+                    float *X0 = BUF, *X1 = BUF + 2 * CG * IB;
                     const int ft0 = CG * sub;
                     // stage 0: X0[(lft, a0)] = O^x_{a0, ft&1} f[ft]
                     for (int jx = warp; jx < 2 * CG; jx += NW) {
@@ -360,8 +453,8 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                         if (!(col & (a0 ? 0xAAu : 0x55u))) continue;
                         const float *in[1] = {FB + ft * BLK};
                         const float *O[1] = {OX + (2 * a0 + (ft & 1)) * K2};
-                        task_block<K, 1>(in, O, 1u, lane, sv);
-                        store_block<K>(X0 + jx * BLK, lane, sv);
+                        task<K, 1, true>(in, O, 1u, lane, sv);
+                        store<K>(X0 + jx * IB, lane, sv);
                     }
                     __syncthreads();
                     if (sub == last && has_next) {
@@ -373,10 +466,10 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                         const int lft = jx >> 2, sidx = jx & 3, ft = ft0 + lft;
                         const unsigned col = (unsigned)((gbits >> (8 * lft)) & 0xffull);
                         if (!(col & ((1u << sidx) | (1u << (sidx + 4))))) continue;
-                        const float *in[1] = {X0 + (2 * lft + (sidx & 1)) * BLK};
+                        const float *in[1] = {X0 + (2 * lft + (sidx & 1)) * IB};
                         const float *O[1] = {OY + (2 * (sidx >> 1) + ((ft >> 1) & 1)) * K2};
-                        task_block<K, 1>(in, O, 1u, lane, sv);
-                        store_block<K>(X1 + jx * BLK, lane, sv);
+                        task<K, 1, false>(in, O, 1u, lane, sv);
+                        store<K>(X1 + jx * IB, lane, sv);
                     }
                     __syncthreads();
                     // stage 2: g[gt] += sum over the group's kept (ft, gt) of O^z_{a2, ft>>2} X1[(lft, gt&3)]
@@ -388,11 +481,11 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
 #pragma unroll
                         for (int lft = 0; lft < CG; lft++) {
                             const int ft = ft0 + lft;
-                            in[lft] = X1 + (4 * lft + (gt & 3)) * BLK;
+                            in[lft] = X1 + (4 * lft + (gt & 3)) * IB;
                             O[lft] = OZ + (2 * (gt >> 2) + (ft >> 2)) * K2;
                             if ((gbits >> (8 * lft + gt)) & 1ull) valid |= 1u << lft;
                         }
-                        task_block<K, CG>(in, O, valid, lane, sv);
+                        task<K, CG, false>(in, O, valid, lane, sv);
                     }
                     // no barrier before the next group: its stage 0 writes X0, which stage 2
                     // does not read, and its stage 1 writes X1 only after the next barrier
@@ -414,15 +507,14 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
             }
             if (!S::KAHAN && ++since >= 16) {
 #pragma unroll
-                for (int r = 0; r < R; r++) {
-                    const int c = row_of<K>(lane, r);
-                    if (c < K2)
+                for (int r = 0; r < R; r++)
 #pragma unroll
-                        for (int j = 0; j < K; j++) {
-                            G64[warp * K3 + c + K2 * j] += (double)acc[r][j];
-                            acc[r][j] = 0.f;
-                        }
-                }
+                    for (int jj = 0; jj < K; jj++) {
+                        int c, j;
+                        acc_cj<K>(lane, r, jj, c, j);
+                        if (c < K2) G64[warp * K3 + c + K2 * j] += (double)acc[r][jj];
+                        acc[r][jj] = 0.f;
+                    }
                 since = 0;
             }
             cp_async_wait_all();
@@ -430,15 +522,16 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
         }
         double *go = partial + (size_t)cix * 8 * K3;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int c = row_of<K>(lane, r);
-            if (c < K2)
+        for (int r = 0; r < R; r++)
 #pragma unroll
-                for (int j = 0; j < K; j++) {
+            for (int jj = 0; jj < K; jj++) {
+                int c, j;
+                acc_cj<K>(lane, r, jj, c, j);
+                if (c < K2) {
                     const int e = warp * K3 + c + K2 * j;
-                    go[e] = S::KAHAN ? (double)acc[r][j] - (double)cmp[r][j] : G64[e] + (double)acc[r][j];
+                    go[e] = S::KAHAN ? (double)acc[r][jj] - (double)cmp[r][jj] : G64[e] + (double)acc[r][jj];
                 }
-        }
+            }
         if (!counter) break;
         __syncthreads();
         if (tid == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);

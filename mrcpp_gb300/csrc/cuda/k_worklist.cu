@@ -12,11 +12,60 @@
 // COUNT writes the item count of every pair, an exclusive scan gives the write
 // positions, FILL writes the items.  Items are ordered by (g, cell, term), the
 // order of the reference's loops (cells x fastest, terms by descending width).
+//
+// Block-schedule items (the mask is the full structural set) carry the input
+// structure of the contraction's three stages (`sched`):
+//   bits  0-15  stage 0, output o = (a0 b1 b2): input b0 valid at bit 2 o + b0
+//   bit  16     the U channel (s->s, x step) exists
+//   bits 17-32  stage 1, output q = (a0 a1 b2): input b1 valid at bit 17 + 2 q + b1
+//   bit  33     U feeds output q = 2 (a0 = 0, a1 = 1, b2 = 0)
+//   bit  34     the P channel (s->s, xy steps) exists
+//   bits 35-50  stage 2, component gt: input b2 valid at bit 35 + 2 gt + b2
+//   bit  51     P feeds gt = 4
 #include "mwgpu_internal.cuh"
 
 namespace mwgpu {
 
 namespace {
+
+// the stage structure of a block-schedule item (bit layout above)
+__device__ inline unsigned long long block_schedule(unsigned nzm, const int (&ib)[3], bool pure) {
+    unsigned long long sc = 0ull;
+    unsigned y0 = 0, y1 = 0;
+    for (int o = 0; o < 8; o++) {
+        const int a0 = o & 1, b12 = o & 6;
+        for (int b0 = 0; b0 < 2; b0++) {
+            const int src = b0 + b12;
+            if (((nzm >> src) & 1u) && ((ib[0] >> (2 * a0 + b0)) & 1) && !(pure && src == 0 && a0 == 0)) {
+                sc |= 1ull << (2 * o + b0);
+                y0 |= 1u << o;
+            }
+        }
+    }
+    const bool u = pure && (ib[0] & 1);
+    if (u) sc |= 1ull << 16;
+    for (int q = 0; q < 8; q++) {
+        const int a0 = q & 1, a1 = (q >> 1) & 1, b2 = q >> 2;
+        for (int b1 = 0; b1 < 2; b1++)
+            if (((y0 >> (a0 + 2 * b1 + 4 * b2)) & 1u) && ((ib[1] >> (2 * a1 + b1)) & 1)) {
+                sc |= 1ull << (17 + 2 * q + b1);
+                y1 |= 1u << q;
+            }
+    }
+    if (u && ((ib[1] >> 2) & 1)) {
+        sc |= 1ull << 33;
+        y1 |= 1u << 2;
+    }
+    const bool pp = u && (ib[1] & 1);
+    if (pp) sc |= 1ull << 34;
+    for (int gt = 0; gt < 8; gt++) {
+        const int a2 = gt >> 2;
+        for (int b2 = 0; b2 < 2; b2++)
+            if (((y1 >> ((gt & 3) + 4 * b2)) & 1u) && ((ib[2] >> (2 * a2 + b2)) & 1)) sc |= 1ull << (35 + 2 * gt + b2);
+    }
+    if (pp && ((ib[2] >> 2) & 1)) sc |= 1ull << 51;
+    return sc;
+}
 
 struct PairCtx {
     int wi, fid, depth, tree;
@@ -163,6 +212,15 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
                     it.tl[2] = (short)pc.tl[2];
                     it.flags = (mask == smask) ? 1 : 0;
                     it.pad = 0;
+                    it.sched = 0ull;
+                    if (it.flags) {
+                        unsigned nzm = 0;
+                        for (int b = 0; b < 8; b++) nzm |= (((mask >> (8 * b)) & 0xffull) != 0ull) << b;
+                        int ib[3] = {0, 0, 0};
+                        for (int d = 0; d < 3; d++)
+                            for (int c = 0; c < 4; c++) ib[d] |= (inb[d][c] ? 1 : 0) << c;
+                        it.sched = block_schedule(nzm, ib, depth != 0 && (nzm & 1u));
+                    }
                     if (wpos < items_cap) items[wpos] = it;
                     else atomicOr(err, DE_POOL_FULL);
                     wpos++;

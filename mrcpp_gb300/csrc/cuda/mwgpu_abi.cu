@@ -805,8 +805,12 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     };
     int *p_td, *p_off, *p_L, *p_bw, *p_bsz, *p_bm, *p_ord;
     double *p_blk, *p_nrm;
+    // FP32 copy for the mixed form, each K x K block transposed (row i = O(i, 0..K-1))
     std::vector<float> blk32(node * 4 * K2);
-    for (size_t q = 0; q < blk32.size(); q++) blk32[q] = (float)d->blocks[q];
+    for (size_t q = 0; q < blk32.size(); q++) {
+        const size_t b = q / K2, ij = q % K2;  // column-major O(i, j) at i + K j
+        blk32[b * K2 + (ij / K) + K * (ij % K)] = (float)d->blocks[q];
+    }
     float *p_blk32;
     mwgpu_status s;
     if ((s = up(&p_td, d->depth, T)) || (s = up(&p_off, dep_off.data(), dep_off.size())) || (s = up(&p_L, dep_L.data(), dep_L.size())) ||
@@ -1572,10 +1576,11 @@ struct Carver {
 }  // namespace
 
 extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, int n_levels,
-                                           const int *level_begin, double prec, int abs_prec, double out_sqnorm, int transforms,
-                                           int *flags_out, int *first_miss_out, double *sq_levels, mwgpu_level_stats *stats) {
+                                           const int *level_begin, double prec, int abs_prec, int first_level, const double *state_in,
+                                           int transforms, int *flags_out, int *first_miss_out, double *sq_levels, mwgpu_level_stats *stats) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
-    MW_ARG(o && inp && out && level_begin && flags_out && first_miss_out, "null argument");
+    MW_ARG(o && inp && out && level_begin && flags_out && first_miss_out && state_in, "null argument");
+    MW_ARG(first_level >= 0 && first_level < n_levels, "first level out of range");
     MW_ARG(n_levels >= 1 && level_begin[0] == 0 && level_begin[n_levels] == out->t.n_real, "level ranges must cover the output tree");
     for (int j = 0; j < n_levels; j++) MW_ARG(level_begin[j + 1] > level_begin[j], "empty proposal level");
     const int N = out->t.n_real;
@@ -1711,12 +1716,16 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     Carver cv;
     cv.base = (char *)ctx->d_arena;
     auto b = carve(cv);
-    // initial state: the roots are kept; tree norm of the fresh output tree
+    // initial state: the levels before first_level are the judged tree already
+    // computed (kept; refined where they have children), first_level is kept;
+    // TreeBuilder's sNorm, wNorm and tree norm after the levels before
     std::vector<int> h_flags(N, 0);
-    for (int i = level_begin[0]; i < level_begin[1]; i++) h_flags[i] = 1;
+    for (int j = 0; j < first_level; j++)
+        for (int i = level_begin[j]; i < level_begin[j + 1]; i++) h_flags[i] = 1 | (out->h_child0[i] >= 0 ? 2 : 0);
+    for (int i = level_begin[first_level]; i < level_begin[first_level + 1]; i++) h_flags[i] = 1;
     std::vector<double> fac(rows);
     for (int d = 0; d < rows; d++) fac[d] = std::pow(2.0, -(0.5 * 1.0 * (m.root_scale + d + 1)));
-    const double state0[3] = {0.0, 0.0, out_sqnorm};
+    const double state0[3] = {state_in[0], state_in[1], state_in[2]};
     const int big = 0x7fffffff;
     MW_CK(cudaMemcpyAsync(b.flags, h_flags.data(), sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(b.cells, cells.data(), sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream));
@@ -1727,7 +1736,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
     cudaStream_t st = ctx->stream;
     const int T = o->op.n_terms;
-    for (int j = 0; j < n_levels; j++) {
+    for (int j = first_level; j < n_levels; j++) {
         const int lb = level_begin[j], nl = level_begin[j + 1] - lb;
         launch_keep_counts(b.flags, lb, nl, b.kcnt, st);
         launch_scan(b.kcnt, b.koff, nl, b.kscan, b.kscan + (scan_blocks(max_level + 1) + 1), st);
@@ -1754,7 +1763,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,
                          st);
             launch_reduce_chunks(m, ctx->d_gs, ctx->d_wtree, b.work, nl, b.chunk_begin, b.partial, st, b.nwork);
-            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, b.goff, b.node_terms, st);
+            launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, b.goff, b.node_terms, st);  // sNorm: level 0 only
             ctx->launches += 17;
         } else {
             launch_contract_fp64(m, o->op, inp->t, out->t, b.work, nl, 0.0, ctx->d_stats, ctx->d_err, st, b.nwork, ctx->d_gthr);

@@ -46,7 +46,7 @@ struct DevOper {
     const int *band_max;        // [max_rows]
     const int *term_order;      // [max_rows * T] terms sorted by descending bw max at depth
     int n_band_max;
-    const float *blocks32;      // FP32 copy of blocks (mixed form)
+    const float *blocks32;      // FP32 copy of blocks (mixed form), each K x K block transposed
 };
 
 struct DevTree {
@@ -116,11 +116,12 @@ enum DevError { DE_LOOKUP = 1, DE_HASH_FULL = 2, DE_POOL_FULL = 4, DE_RANGE = 8 
 // structural set (every component the band and zero-norm rules allow), so
 // the components may be summed blockwise.
 struct WorkItem {
-    unsigned long long mask;
+    unsigned long long mask;   // contracted (ft, gt) components, bit 8 ft + gt
+    unsigned long long sched;  // block schedule: valid inputs of every stage output (see k_worklist.cu)
     int fid;
     short term;
     short tl[3];
-    short flags;
+    short flags;               // bit 0: block schedule
     short pad;
 };
 

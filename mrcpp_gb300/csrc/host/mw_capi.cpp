@@ -672,8 +672,8 @@ int mwh_grid_features(double prec, mwh_tree *gridp, mwh_oper *operp, mwh_tree *i
     });
 }
 
-int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, const mwh_mlp *mlpc, double threshold, int abs_prec,
-                      int precision, mwh_learned_stats *stats) {
+int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, const mwh_mlp *mlpc, double threshold, int full_levels,
+                      int abs_prec, int precision, mwh_learned_stats *stats) {
     return guard([&] {
         if (!outp || !operp || !inpp || !mlpc) return fail(1, "null argument");
         mwh_mlp *mlp = const_cast<mwh_mlp *>(mlpc);
@@ -692,54 +692,58 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
             return rc;
         }
         auto t0 = std::chrono::steady_clock::now();
-        mwgpu_ctx *ctx = nullptr;
-        mwgpu_tree *dinp = nullptr, *dprop = nullptr;
-        int first_miss = -1;
-        std::vector<int> flags, level_begin;
-        std::vector<double> coefs, norms, norm_levels;
-        Tree<3> prop(*out.mra);
-        BuildState resume;
-        {
-            std::lock_guard<std::mutex> lk(g_gpu_mu);
-            ctx = gpu_ctx(precision);
-            const MRA<3> &mra = *out.mra;
-            std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
-            mwgpu_mra_desc md{};
-            fill_desc(mra, &md, filters.data());
-            mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
-            if (!mlp->dev) ck(mwgpu_mlp_create(ctx, mlp->params.data(), &mlp->dev), "network upload");
-            mwh_apply_stats acc{};
-            unsigned long long l0 = 0, l1 = 0;
-            mwgpu_launch_count(ctx, &l0);
-            try {
-                dinp = upload_input(ctx, md, inp, acc);
-                const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
-                const size_t max_nodes = std::max<size_t>(4096, 4 * inp.nodes.size());
-                // proposal, level by level: children of the nodes the network refines
-                std::vector<int> cur;
-                for (size_t i = 0; i < prop.nodes.size(); i++) cur.push_back((int)i);
-                level_begin.push_back(0);
-                std::vector<int> idx;
-                std::vector<float> pr;
+        std::lock_guard<std::mutex> lk(g_gpu_mu);
+        mwgpu_ctx *ctx = gpu_ctx(precision);
+        const MRA<3> &mra = *out.mra;
+        std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
+        mwgpu_mra_desc md{};
+        fill_desc(mra, &md, filters.data());
+        mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
+        if (!mlp->dev) ck(mwgpu_mlp_create(ctx, mlp->params.data(), &mlp->dev), "network upload");
+        mwh_apply_stats acc{};
+        unsigned long long l0 = 0, l1 = 0;
+        mwgpu_launch_count(ctx, &l0);
+        mwgpu_tree *dinp = nullptr, *dprop = nullptr, *dold = nullptr;
+        // The proposal, level by level.  `prop` holds the judged tree of the
+        // levels before `first` (exact) and the proposed levels after it; its
+        // node order is TreeBuilder's (levels, each in the order of the parents).
+        Tree<3> prop(mra);
+        std::vector<int> level_begin, flags;
+        std::vector<double> norm_levels, coefs, norms;
+        try {
+            dinp = upload_input(ctx, md, inp, acc);
+            const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
+            const size_t max_nodes = std::max<size_t>(4096, 4 * inp.nodes.size());
+            std::vector<int> idx;
+            std::vector<float> pr;
+            // extends the proposal below the nodes `cur` (one level), predicting level by level
+            auto propose = [&](std::vector<int> cur) {
                 while (!cur.empty()) {
                     level_begin.push_back(level_begin.back() + (int)cur.size());
+                    const int lvl = (int)level_begin.size() - 2;
                     const int n = (int)cur.size();
-                    idx.resize(4 * (size_t)n);
-                    for (int j = 0; j < n; j++) {
-                        const auto &nd = prop.nodes[cur[j]];
-                        idx[4 * j] = nd.n;
-                        for (int d = 0; d < 3; d++) idx[4 * j + 1 + d] = nd.l[d];
+                    std::vector<int> refine;
+                    if (lvl < full_levels) {
+                        for (int i : cur)
+                            if (prop.nodes[i].n + 2 <= mra.maxScale()) refine.push_back(i);
+                    } else {
+                        idx.resize(4 * (size_t)n);
+                        for (int j = 0; j < n; j++) {
+                            const auto &nd = prop.nodes[cur[j]];
+                            idx[4 * j] = nd.n;
+                            for (int d = 0; d < 3; d++) idx[4 * j + 1 + d] = nd.l[d];
+                        }
+                        pr.resize(n);
+                        ck(mwgpu_mlp_predict(ctx, mlp->dev, dop, dinp, f_norm, idx.data(), n, pr.data()), "grid prediction");
+                        ls.host_round_trips += 1;
+                        for (int j = 0; j < n; j++)
+                            if (pr[j] > threshold && prop.nodes[cur[j]].n + 2 <= mra.maxScale()) refine.push_back(cur[j]);
                     }
-                    pr.resize(n);
-                    ck(mwgpu_mlp_predict(ctx, mlp->dev, dop, dinp, f_norm, idx.data(), n, pr.data()), "grid prediction");
-                    ls.host_round_trips += 1;
-                    std::vector<int> next, refine;
-                    for (int j = 0; j < n; j++)
-                        if (pr[j] > threshold && prop.nodes[cur[j]].n + 2 <= mra.maxScale()) refine.push_back(cur[j]);
                     ls.proposal_levels++;
                     // a proposal larger than the budget stops here (the judge then
                     // reports the first level it would have needed)
                     if (prop.nodes.size() + Tree<3>::tDim * refine.size() > max_nodes) break;
+                    std::vector<int> next;
                     for (int i : refine) {
                         prop.createChildren(i, false);
                         const int c0 = prop.nodes[i].child0;
@@ -747,10 +751,17 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     }
                     cur.swap(next);
                 }
-                ls.proposal_nodes = (int)prop.nodes.size();
-                auto t1 = std::chrono::steady_clock::now();
-                ls.predict_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
-                // the proposal as the device output tree, judged in one pass
+            };
+            std::vector<int> roots;
+            for (size_t i = 0; i < prop.nodes.size(); i++) roots.push_back((int)i);
+            level_begin.push_back(0);
+            propose(roots);
+            ls.proposal_nodes = (int)prop.nodes.size();
+            double state[3] = {0.0, 0.0, out.squareNorm};
+            int first = 0;
+            std::vector<int> src_prev;  // node of the previous device proposal for every node of prop (-1: new)
+            for (int pass = 0;; pass++) {
+                // the proposal as a device tree; the judged levels before `first` are copied over
                 std::vector<int> pidx(prop.nodes.size() * 4), pc0(prop.nodes.size(), -1);
                 for (size_t i = 0; i < prop.nodes.size(); i++) {
                     pidx[4 * i] = prop.nodes[i].n;
@@ -758,103 +769,91 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     pc0[i] = prop.nodes[i].child0;
                 }
                 mwgpu_tree_desc gd{(int)prop.nodes.size(), pidx.data(), pc0.data(), nullptr, nullptr};
+                dold = dprop;
+                dprop = nullptr;
                 ck(mwgpu_create_tree(ctx, &md, &gd, &dprop), "create proposal tree");
                 acc.h2d_bytes += (pidx.size() + pc0.size()) * 4;
-                flags.assign(prop.nodes.size(), 0);
-                mwgpu_level_stats st{};
+                if (dold) {
+                    std::vector<int> a, b;
+                    for (int i = 0; i < level_begin[first]; i++) {
+                        a.push_back(src_prev[i]);
+                        b.push_back(i);
+                    }
+                    ck(mwgpu_tree_copy_nodes(ctx, dold, dprop, (int)a.size(), a.data(), b.data()), "copy judged levels");
+                    mwgpu_free_tree(ctx, dold);
+                    dold = nullptr;
+                }
                 const int nlev = (int)level_begin.size() - 1;
+                flags.assign(prop.nodes.size(), 0);
                 norm_levels.assign(3 * (size_t)nlev, 0.0);
-                ck(mwgpu_apply_judged(ctx, dop, dinp, dprop, nlev, level_begin.data(), prec, abs_prec, out.squareNorm, 1, flags.data(),
-                                      &first_miss, norm_levels.data(), &st),
+                int miss = -1;
+                mwgpu_level_stats st{};
+                ck(mwgpu_apply_judged(ctx, dop, dinp, dprop, nlev, level_begin.data(), prec, abs_prec, first, state, 1, flags.data(), &miss,
+                                      norm_levels.data(), &st),
                    "judged apply");
                 ls.host_round_trips += 1;
+                acc.node_terms += st.node_terms;
+                acc.components += st.components;
+                acc.band_nodes += st.band_nodes;
+                acc.gen_nodes += st.gen_nodes;
+                acc.device_ms += st.device_ms;
+                acc.contract_ms += st.contract_ms;
+                acc.iterations += 1;
                 acc.d2h_bytes += flags.size() * 4;
-                if (first_miss < 0) {
-                    coefs.resize(prop.nodes.size() * (size_t)prop.nCoefs);
-                    norms.resize(prop.nodes.size() * 8);
-                    ck(mwgpu_download_tree(ctx, dprop, coefs.data(), norms.data()), "download output tree");
-                    acc.d2h_bytes += (coefs.size() + norms.size()) * 8;
-                    ls.host_round_trips += 1;
-                } else {
-                    // exact up to level first_miss: that part of the judged tree goes
-                    // into a fresh output tree, with the children of every node the
-                    // judge refined at that level; the host loop continues from there
-                    const int jm = first_miss;
-                    std::vector<int> map(prop.nodes.size(), -1), src, dst;
-                    for (size_t i = 0; i < out.nodes.size(); i++) map[i] = (int)i;
-                    for (int j = 0; j <= jm; j++)
-                        for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
-                            if (!(flags[i] & 1)) continue;
-                            src.push_back(i);
-                            dst.push_back(map[i]);
-                            if ((flags[i] & 3) != 3) continue;
-                            const int oi = map[i];
-                            out.createChildren(oi, false);
-                            const int c0 = out.nodes[oi].child0, p0 = prop.nodes[i].child0;
-                            if (j < jm && p0 >= 0)
-                                for (int c = 0; c < Tree<3>::tDim; c++) map[p0 + c] = c0 + c;
-                            if (j == jm)
-                                for (int c = 0; c < Tree<3>::tDim; c++) resume.work.push_back(c0 + c);
-                        }
-                    resume.tree = &out;
-                    resume.dinp = dinp;
-                    resume.dout = create_output(ctx, md, out, acc);
-                    resume.synced = out.nodes.size();
-                    resume.iter = jm + 1;
-                    resume.sNorm = norm_levels[3 * jm];
-                    resume.wNorm = norm_levels[3 * jm + 1];
-                    out.squareNorm = norm_levels[3 * jm + 2];
-                    ck(mwgpu_tree_copy_nodes(ctx, dprop, resume.dout, (int)src.size(), src.data(), dst.data()), "copy judged levels");
-                    ls.kept_nodes = (int)src.size();
-                    dinp = nullptr;  // owned by the continuation now
+                if (pass == 0) ls.first_miss = miss;
+                if (miss < 0) break;
+                // a refinement the proposal missed at level `miss`: the judged tree
+                // up to there is kept, all children of the refined nodes of that
+                // level are added, the network proposes below them, next pass
+                ls.fallback = 1;
+                Tree<3> next(mra);
+                std::vector<int> map(prop.nodes.size(), -1), nsrc;
+                for (size_t i = 0; i < next.nodes.size(); i++) {
+                    map[i] = (int)i;
+                    nsrc.push_back((int)i);
                 }
-                acc.node_terms = st.node_terms;
-                acc.components = st.components;
-                acc.band_nodes = st.band_nodes;
-                acc.gen_nodes = st.gen_nodes;
-                acc.device_ms = st.device_ms;
-                acc.contract_ms = st.contract_ms;
-                acc.iterations = 1;
-                ls.judged_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
-            } catch (...) {
-                if (dprop) mwgpu_free_tree(ctx, dprop);
-                if (dinp) mwgpu_free_tree(ctx, dinp);
-                if (resume.dout) mwgpu_free_tree(ctx, resume.dout);
-                if (resume.dinp) mwgpu_free_tree(ctx, resume.dinp);
-                throw;
+                // nlb[j + 1] = end of level j of `next` (iteration j creates level j + 1)
+                std::vector<int> nlb{0, (int)next.nodes.size()}, frontier;
+                for (int j = 0; j <= miss; j++) {
+                    for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
+                        if ((flags[i] & 3) != 3) continue;
+                        const int oi = map[i];
+                        next.createChildren(oi, false);
+                        const int c0 = next.nodes[oi].child0, p0 = prop.nodes[i].child0;
+                        for (int c = 0; c < Tree<3>::tDim; c++) {
+                            nsrc.push_back(j < miss && p0 >= 0 ? p0 + c : -1);
+                            if (j < miss && p0 >= 0) map[p0 + c] = c0 + c;
+                            if (j == miss) frontier.push_back(c0 + c);
+                        }
+                    }
+                    nlb.push_back((int)nsrc.size());
+                }
+                // levels 0 .. miss stay; the frontier (level miss + 1) is proposed next
+                level_begin.assign(nlb.begin(), nlb.begin() + (miss + 2));
+                prop = std::move(next);
+                src_prev = nsrc;
+                state[0] = norm_levels[3 * miss];
+                state[1] = norm_levels[3 * miss + 1];
+                state[2] = norm_levels[3 * miss + 2];
+                first = miss + 1;
+                propose(frontier);
+                ls.proposal_nodes += (int)prop.nodes.size() - level_begin[first];
             }
-            mwgpu_free_tree(ctx, dprop);
+            coefs.resize(prop.nodes.size() * (size_t)prop.nCoefs);
+            norms.resize(prop.nodes.size() * 8);
+            ck(mwgpu_download_tree(ctx, dprop, coefs.data(), norms.data()), "download output tree");
+            acc.d2h_bytes += (coefs.size() + norms.size()) * 8;
+            ls.host_round_trips += 1;
+        } catch (...) {
+            if (dprop) mwgpu_free_tree(ctx, dprop);
+            if (dold) mwgpu_free_tree(ctx, dold);
             if (dinp) mwgpu_free_tree(ctx, dinp);
-            mwgpu_launch_count(ctx, &l1);
-            acc.launches = l1 - l0;
-            ls.apply = acc;
+            throw;
         }
-        ls.first_miss = first_miss;
-        if (first_miss >= 0) {
-            // the judge refined a node the proposal left out: the host loop
-            // continues from that level (missed splits appended)
-            mwh_tree *o1[1] = {outp}, *i1[1] = {inpp};
-            mwh_apply_stats pa{};
-            int rc = apply_impl(prec, 1, o1, operp, i1, -1, abs_prec, precision, &pa, &resume);
-            if (rc) return rc;
-            ls.fallback = 1;
-            ls.host_round_trips += pa.iterations + 1;
-            ls.apply.node_terms += pa.node_terms;
-            ls.apply.components += pa.components;
-            ls.apply.band_nodes += pa.band_nodes;
-            ls.apply.gen_nodes += pa.gen_nodes;
-            ls.apply.iterations += pa.iterations;
-            ls.apply.device_ms += pa.device_ms;
-            ls.apply.contract_ms += pa.contract_ms;
-            ls.apply.transform_ms = pa.transform_ms;
-            ls.apply.launches += pa.launches;
-            ls.apply.h2d_bytes += pa.h2d_bytes;
-            ls.apply.d2h_bytes += pa.d2h_bytes;
-            ls.apply.out_nodes = pa.out_nodes;
-            ls.apply.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-            if (stats) *stats = ls;
-            return 0;
-        }
+        mwgpu_free_tree(ctx, dprop);
+        mwgpu_free_tree(ctx, dinp);
+        mwgpu_launch_count(ctx, &l1);
+        acc.launches = l1 - l0;
         // the judged tree, created in TreeBuilder's order (the host ids of the plain apply)
         std::vector<int> map(prop.nodes.size(), -1);
         for (size_t i = 0; i < out.nodes.size(); i++) map[i] = (int)i;
@@ -884,8 +883,9 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
             out.nodes[oi].flags |= F_HASCOEFS;
         }
         out.calcSquareNorm();
-        ls.apply.out_nodes = (int)out.nodes.size();
-        ls.apply.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        acc.out_nodes = (int)out.nodes.size();
+        acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        ls.apply = acc;
         if (stats) *stats = ls;
         return 0;
     });

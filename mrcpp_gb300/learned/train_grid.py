@@ -129,7 +129,7 @@ def gpu_prob(params, X):
         L.mwgpu_destroy(ctx)
 
 
-def evaluate(params, threshold, seeds, precision):
+def evaluate(params, threshold, seeds, precision, full_levels=1):
     """Plain adaptive apply vs learned apply on each density (same process, sequential)."""
     mw, mra, P = _setup()
     from mrcpp_gb300 import GridNetwork
@@ -144,7 +144,7 @@ def evaluate(params, threshold, seeds, precision):
         t_plain = time.perf_counter() - t0
         g1 = mw.FunctionTree(mra)
         t0 = time.perf_counter()
-        sl = mw.apply_learned(PREC, g1, P, f, net, threshold=threshold, precision=precision)
+        sl = mw.apply_learned(PREC, g1, P, f, net, threshold=threshold, full_levels=full_levels, precision=precision)
         t_learned = time.perf_counter() - t0
         a, b = g0.export(), g1.export()
         ka = {tuple(r): i for i, r in enumerate(a["idx"].reshape(-1, 4).tolist())}
@@ -158,6 +158,7 @@ def evaluate(params, threshold, seeds, precision):
                      "learned_ms": 1e3 * t_learned, "fallback": sl["fallback"], "first_miss": sl["first_miss"],
                      "proposal_nodes": sl["proposal_nodes"], "kept_nodes": sl["kept_nodes"], "round_trips": sl["host_round_trips"],
                      "learned_iterations": sl["apply"]["iterations"], "node_terms": sl["apply"]["node_terms"],
+                     "predict_ms": sl["predict_ms"], "judged_ms": sl["judged_ms"],
                      "same_topology": bool(same), "max_rel_diff": diff})
     return rows
 
@@ -173,6 +174,7 @@ def main():
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--success", type=float, default=0.97, help="share of validation densities the threshold must propose completely")
     ap.add_argument("--report", default=None, help="JSON file for the evaluation")
+    ap.add_argument("--full-levels", type=int, default=1, help="proposal levels refined without the network")
     a = ap.parse_args()
     t0 = time.perf_counter()
     res = generate(list(range(TRAIN_SEED0, TRAIN_SEED0 + a.train)), a.workers)
@@ -199,11 +201,11 @@ def main():
     probe = list(range(HELD_SEED0, HELD_SEED0 + min(a.held, 40)))
     tune = []
     for c in cands:
-        r = evaluate(params, c, probe, mw.MIXED)
+        r = evaluate(params, c, probe, mw.MIXED, a.full_levels)
         tune.append({"threshold": c, "learned_ms": float(sum(x["learned_ms"] for x in r)), "plain_ms": float(sum(x["plain_ms"] for x in r)),
                      "continued": float(np.mean([x["fallback"] for x in r]))})
     threshold = min(tune, key=lambda t: t["learned_ms"])["threshold"]
-    rows = evaluate(params, threshold, list(range(HELD_SEED0, HELD_SEED0 + a.held)), mw.MIXED)
+    rows = evaluate(params, threshold, list(range(HELD_SEED0, HELD_SEED0 + a.held)), mw.MIXED, a.full_levels)
     split_in_input = float(X[Y > 0.5, 7].mean()) if pos > 0 else 0.0
     summ = {
         "train_densities": len(tr), "validation_densities": len(va), "held_out_densities": len(rows), "samples": int(len(Y)),
@@ -225,7 +227,8 @@ def main():
         },
     }
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
-    np.savez(a.out, params=params, threshold=np.float64(threshold), loss_curve=curve, summary=json.dumps(summ), features=np.int32(2))
+    np.savez(a.out, params=params, threshold=np.float64(threshold), loss_curve=curve, summary=json.dumps(summ), features=np.int32(2),
+             full_levels=np.int32(a.full_levels))
     if a.report:
         with open(a.report, "w") as fh:
             json.dump({"summary": summ, "held_out": rows}, fh, indent=1)

@@ -85,8 +85,9 @@ class Judged:
         miss = C.c_int()
         st = mw.MwgpuLevelStats()
         lb = np.ascontiguousarray(lb, dtype=np.int32)
-        rc = L.mwgpu_apply_judged(self.ctx, self.dop, self.dinp, t, len(lb) - 1, mw._pi(lb), self.prec, 0, -1.0, 1, mw._pi(flags),
-                                  C.byref(miss), None, C.byref(st))
+        state0 = np.array([0.0, 0.0, -1.0])
+        rc = L.mwgpu_apply_judged(self.ctx, self.dop, self.dinp, t, len(lb) - 1, mw._pi(lb), self.prec, 0, 0, mw._pd(state0), 1,
+                                  mw._pi(flags), C.byref(miss), None, C.byref(st))
         assert rc == 0, L.mwgpu_last_error(self.ctx).decode()
         coefs = np.zeros((n, 8 * self.mra.kp1 ** 3))
         assert L.mwgpu_download_tree(self.ctx, t, mw._pd(coefs), None) == 0
@@ -238,3 +239,32 @@ def test_learned_apply_equals_plain_and_falls_back(gpu):
     assert same
     if len(px["child0"]) > 8:
         assert st2["fallback"] == 1 and st2["first_miss"] == 0
+
+
+def test_trained_network_against_plain_refinement(gpu):
+    """The committed network on held-out densities of its training family: the
+    learned apply gives the plain apply's tree (topology and coefficients) with
+    fewer judged passes than the plain TreeBuilder has iterations."""
+    from mrcpp_gb300.learned import train_grid as tg
+
+    net = mw.GridNetwork.load()
+    thr = float(net.meta["threshold"])
+    full = int(net.meta["full_levels"])
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, tg.PREC)
+    passes, iters = [], []
+    for seed in range(tg.HELD_SEED0, tg.HELD_SEED0 + 6):
+        f = mw.FunctionTree(mra)
+        mw.project(tg.PREC, f, tg.density(seed))
+        g0 = mw.FunctionTree(mra)
+        sp = mw.apply(tg.PREC, g0, P, f, precision=mw.MIXED)
+        g1 = mw.FunctionTree(mra)
+        sl = mw.apply_learned(tg.PREC, g1, P, f, net, threshold=thr, full_levels=full, precision=mw.MIXED)
+        a, b = g0.export(), g1.export()
+        same, perm = match(b, a)
+        assert same, seed
+        mx, _ = rel_errors(b["coefs"], a["coefs"][perm])
+        assert mx <= 1e-12, (seed, mx)
+        passes.append(sl["apply"]["iterations"])
+        iters.append(sp["iterations"])
+    assert np.mean(passes) < np.mean(iters), (passes, iters)
