@@ -201,6 +201,9 @@ __device__ __forceinline__ void task_mma(const float *const (&in)[NS], const flo
         unsigned bh0, bl0, bh1, bl1;
         split_tf32(O[p][g + K * t], bh0, bl0);
         split_tf32(O[p][g + K * (t + 4)], bh1, bl1);
+        // all four m-tiles' A fragments first, then the products m-tile after
+        // m-tile, so that consecutive mma instructions are independent
+        unsigned ah[4][4], al[4][4];
 #pragma unroll
         for (int mt = 0; mt < 4; mt++) {
             float x[4];
@@ -217,13 +220,15 @@ __device__ __forceinline__ void task_mma(const float *const (&in)[NS], const flo
                 x[2] = r0[t + 4];
                 x[3] = r1[t + 4];
             }
-            unsigned ah[4], al[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) split_tf32(x[q], ah[q], al[q]);
-            mma_tf32(d[mt], al[0], al[1], al[2], al[3], bh0, bh1);
-            mma_tf32(d[mt], ah[0], ah[1], ah[2], ah[3], bl0, bl1);
-            mma_tf32(d[mt], ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+            for (int q = 0; q < 4; q++) split_tf32(x[q], ah[mt][q], al[mt][q]);
         }
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) mma_tf32(d[mt], al[mt][0], al[mt][1], al[mt][2], al[mt][3], bh0, bh1);
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) mma_tf32(d[mt], ah[mt][0], ah[mt][1], ah[mt][2], ah[mt][3], bl0, bl1);
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) mma_tf32(d[mt], ah[mt][0], ah[mt][1], ah[mt][2], ah[mt][3], bh0, bh1);
     }
 #pragma unroll
     for (int mt = 0; mt < 4; mt++)

@@ -19,11 +19,13 @@ namespace mwgpu {
 namespace {
 
 // out[c + K2*j] (+)= sum_i in[i + K*c] * F[i + K*j]
+// (consecutive threads take consecutive j of one row c: the row is a broadcast
+// read and the filter columns hit distinct banks)
 template <bool ADD>
 __device__ __forceinline__ void dapply(double *out, const double *in, const double *F, int K, int tid, int nthr) {
     const int K2 = K * K, K3 = K2 * K;
     for (int e = tid; e < K3; e += nthr) {
-        int c = e % K2, j = e / K2;
+        int c = e / K, j = e % K;
         const double *a = in + K * c;
         const double *b = F + K * j;
         double s = 0.0;
@@ -274,7 +276,7 @@ template <bool ADD>
 __device__ __forceinline__ void fapply(float *out, const float *in, const float *F, int K, int tid, int nthr) {
     const int K2 = K * K, K3 = K2 * K;
     for (int e = tid; e < K3; e += nthr) {
-        const int c = e % K2, j = e / K2;
+        const int c = e / K, j = e % K;
         const float *a = in + K * c;
         const float *b = F + K * j;
         float s = 0.f;
