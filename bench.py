@@ -631,7 +631,8 @@ def main():
                 "ms_per_step": t_mixed, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 products, f64 accumulation", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "out_nodes": n_out, "node_terms_per_step": int(node_terms),
-                           "components_per_step": int(st_mixed.components), "l2": "256 MiB scrub between steps",
+                           "components_per_step": int(st_mixed.components), "gen_nodes_per_step": int(st_mixed.gen_nodes),
+                           "band_pairs_per_step": int(st_mixed.band_nodes), "l2": "256 MiB scrub between steps",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "ms_per_step": t_e2e * 1e3},

@@ -333,7 +333,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     launch_contract_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items,
                           ctx->d_partial, ctx->d_err, ctx->stream);
     ctx->launches += 2;
-    MW_CK(cudaStreamSynchronize(ctx->stream));  // host vectors above must outlive the copies
+    // (the chunk arrays came from pageable memory: the copies read them before returning)
     hs->node_terms = (unsigned long long)total;
     return MWGPU_OK;
 }
@@ -348,7 +348,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     const int n = d->n_nodes;
     const size_t nc = 8 * (size_t)tr->mra.kp1_d;
     t.n_real = n;
-    t.cap_real = input ? n : std::max(n, 64);
+    t.cap_real = input ? n : std::max(n, 512);  // output trees grow by the split step: room for a few levels
     t.n_gen = 0;
     t.cap_gen = 0;
     int tot = t.cap_real;
@@ -383,7 +383,9 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     } else {
         MW_CK(cudaMemsetAsync(t.norms, 0, sizeof(double) * tot * 8, ctx->stream));
     }
-    if ((s = rebuild_hash(ctx, tr, n))) { delete tr; return s; }
+    // only input trees are looked up by node index (band cells, GenNode
+    // ancestors); output trees are addressed by position
+    if (input && (s = rebuild_hash(ctx, tr, n))) { delete tr; return s; }
     *out = tr;
     return MWGPU_OK;
 }
@@ -889,13 +891,7 @@ mwgpu_status mwgpu_tree_add_nodes(mwgpu_ctx *ctx, mwgpu_tree *tr, int n, const i
     if (n > 0) MW_CK(cudaMemcpyAsync(t.idx + old, tr->h_idx.data() + old, sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(t.child0, tr->h_child0.data(), sizeof(int) * (old + n), cudaMemcpyHostToDevice, ctx->stream));
     t.n_real = old + n;
-    if (2LL * t.n_real + 16 > t.hcap) return rebuild_hash(ctx, tr, t.n_real);
-    if (n > 0) {
-        MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
-        launch_hash_build(tr->mra, t, old, n, ctx->d_err, ctx->stream);
-        ctx->launches++;
-        return check_err(ctx, "tree_add_nodes");
-    }
+    // (copies from pageable memory read their source before returning)
     return MWGPU_OK;
 }
 

@@ -734,7 +734,9 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                             for (int d = 0; d < 3; d++) idx[4 * j + 1 + d] = nd.l[d];
                         }
                         pr.resize(n);
+                        const auto tp = std::chrono::steady_clock::now();
                         ck(mwgpu_mlp_predict(ctx, mlp->dev, dop, dinp, f_norm, idx.data(), n, pr.data()), "grid prediction");
+                        ls.predict_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tp).count();
                         ls.host_round_trips += 1;
                         for (int j = 0; j < n; j++)
                             if (pr[j] > threshold && prop.nodes[cur[j]].n + 2 <= mra.maxScale()) refine.push_back(cur[j]);
@@ -788,9 +790,11 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 norm_levels.assign(3 * (size_t)nlev, 0.0);
                 int miss = -1;
                 mwgpu_level_stats st{};
+                const auto tj = std::chrono::steady_clock::now();
                 ck(mwgpu_apply_judged(ctx, dop, dinp, dprop, nlev, level_begin.data(), prec, abs_prec, first, state, 1, flags.data(), &miss,
                                       norm_levels.data(), &st),
                    "judged apply");
+                ls.judged_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tj).count();
                 ls.host_round_trips += 1;
                 acc.node_terms += st.node_terms;
                 acc.components += st.components;

@@ -175,7 +175,27 @@ def main():
     ap.add_argument("--success", type=float, default=0.97, help="share of validation densities the threshold must propose completely")
     ap.add_argument("--report", default=None, help="JSON file for the evaluation")
     ap.add_argument("--full-levels", type=int, default=1, help="proposal levels refined without the network")
+    ap.add_argument("--evaluate", default=None, help="only evaluate this trained network (npz) on the held-out densities")
+    ap.add_argument("--thresholds", default=None, help="with --evaluate: comma-separated thresholds to compare")
     a = ap.parse_args()
+    if a.evaluate:
+        import mrcpp_gb300 as mw
+        with np.load(a.evaluate) as z:
+            params = z["params"]
+            thr0 = float(z["threshold"])
+        thrs = [float(x) for x in a.thresholds.split(",")] if a.thresholds else [thr0]
+        seeds = list(range(HELD_SEED0, HELD_SEED0 + a.held))
+        out = []
+        for t in thrs:
+            rows = evaluate(params, t, seeds, mw.MIXED, a.full_levels)
+            out.append({"threshold": t, "full_levels": a.full_levels, "plain_ms": float(sum(r["plain_ms"] for r in rows)),
+                        "learned_ms": float(sum(r["learned_ms"] for r in rows)),
+                        "passes_mean": float(np.mean([r["learned_iterations"] for r in rows])),
+                        "plain_iterations_mean": float(np.mean([r["plain_iterations"] for r in rows])),
+                        "predict_ms": float(sum(r["predict_ms"] for r in rows)), "judged_ms": float(sum(r["judged_ms"] for r in rows)),
+                        "same_topology": int(sum(r["same_topology"] for r in rows)), "n": len(rows)})
+        print(json.dumps(out))
+        return
     t0 = time.perf_counter()
     res = generate(list(range(TRAIN_SEED0, TRAIN_SEED0 + a.train)), a.workers)
     t_gen = time.perf_counter() - t0
