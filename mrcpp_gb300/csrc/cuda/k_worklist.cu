@@ -144,10 +144,13 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
             const float thr_hi = (float)(gthr * (1.0 + 1.0 / 4096.0)), thr_lo = (float)(gthr * (1.0 - 1.0 / 4096.0));
             double fn[8];
             bool any = false;
+            double fmx = 0.0;
             for (int c = 0; c < 8; c++) {
                 fn[c] = f.norms[(size_t)pc.fid * 8 + c];
                 any |= !(fn[c] < kMachineZero);
+                if (!(fn[c] < kMachineZero)) fmx = fmax(fmx, fn[c]);
             }
+            const float fmx_up = nextafterf((float)fmx, INFINITY);
             const int maxdl = max(abs(pc.tl[0]), max(abs(pc.tl[1]), abs(pc.tl[2])));
             const int T = op.n_terms, depth = pc.depth;
             long long wpos = FILL ? item_off[p] : 0;
@@ -158,6 +161,17 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
                 const int L0 = op.dep_L[i * op.max_rows + depth], off = op.dep_off[i * op.max_rows + depth];
                 int wd[4];
                 for (int c = 0; c < 4; c++) wd[c] = bwi[c];
+                if (screen && fp32) {
+                    // bound of every component product of this term: the largest
+                    // operator norm per direction, band size and f norm; clear of the
+                    // threshold by far more than the FP32 rounding -> nothing passes
+                    if (off < 0 || abs(pc.tl[0]) > L0 || abs(pc.tl[1]) > L0 || abs(pc.tl[2]) > L0) continue;
+                    int fm = 1;
+                    for (int c = 0; c < 4; c++) fm = max(fm, wd[c] < 0 ? 1 : 2 * wd[c] + 1);
+                    const float bound = op.norm_max[off + pc.tl[0] + L0] * op.norm_max[off + pc.tl[1] + L0] * op.norm_max[off + pc.tl[2] + L0] *
+                                        ((float)(fm * fm * fm * 64) * fmx_up);
+                    if (bound < thr_lo) continue;
+                }
                 bool inb[3][4];
                 double nrm[3][4];
                 float nrf[3][4];

@@ -813,12 +813,19 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         const size_t b = q / K2, ij = q % K2;  // column-major O(i, j) at i + K j
         blk32[b * K2 + (ij / K) + K * (ij % K)] = (float)d->blocks[q];
     }
-    float *p_blk32;
+    // per operator node an upper bound of its 4 component norms (screening bound)
+    std::vector<float> nmax(node);
+    for (size_t q = 0; q < node; q++) {
+        double mx = 0.0;
+        for (int c = 0; c < 4; c++) mx = std::max(mx, d->norms[q * 4 + c]);
+        nmax[q] = std::nextafter((float)mx, INFINITY);
+    }
+    float *p_blk32, *p_nmax;
     mwgpu_status s;
     if ((s = up(&p_td, d->depth, T)) || (s = up(&p_off, dep_off.data(), dep_off.size())) || (s = up(&p_L, dep_L.data(), dep_L.size())) ||
         (s = up(&p_bw, bw.data(), bw.size())) || (s = up(&p_bsz, bsz.data(), bsz.size())) || (s = up(&p_bm, band_max.data(), band_max.size())) ||
         (s = up(&p_ord, order.data(), order.size())) || (s = up(&p_blk, d->blocks, node * 4 * K2)) || (s = up(&p_nrm, d->norms, node * 4)) ||
-        (s = up(&p_blk32, blk32.data(), blk32.size()))) {
+        (s = up(&p_blk32, blk32.data(), blk32.size())) || (s = up(&p_nmax, nmax.data(), nmax.size()))) {
         for (void *p : o->allocs) cudaFree(p);
         delete o;
         return s;
@@ -837,6 +844,7 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.term_order = p_ord;
     o->op.n_band_max = maxDepth + 1;
     o->op.blocks32 = p_blk32;
+    o->op.norm_max = p_nmax;
     *out = o;
     return MWGPU_OK;
 }

@@ -47,6 +47,7 @@ struct DevOper {
     const int *term_order;      // [max_rows * T] terms sorted by descending bw max at depth
     int n_band_max;
     const float *blocks32;      // FP32 copy of blocks (mixed form), each K x K block transposed
+    const float *norm_max;      // [nodes] upper bound of the 4 component norms (FP32, rounded up)
 };
 
 struct DevTree {

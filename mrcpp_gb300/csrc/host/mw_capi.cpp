@@ -131,6 +131,27 @@ struct BuildState {
 };
 
 mwgpu_tree *upload_input(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, const Tree<3> &inp, mwh_apply_stats &acc) {
+    bool any_gen = false;
+    for (size_t i = 0; i < inp.nodes.size() && !any_gen; i++) any_gen = inp.isGen((int)i);
+    if (!any_gen) {
+        // the device tree takes the host node order: the coefficients go up
+        // straight from the tree's own storage (lookups are by node index key)
+        const size_t n = inp.nodes.size();
+        std::vector<int> idx(4 * n), child0(n);
+        std::vector<double> norms(8 * n);
+        for (size_t i = 0; i < n; i++) {
+            const auto &nd = inp.nodes[i];
+            idx[4 * i] = nd.n;
+            for (int d = 0; d < 3; d++) idx[4 * i + 1 + d] = nd.l[d];
+            child0[i] = nd.child0;
+            std::memcpy(&norms[8 * i], nd.norms, sizeof(double) * 8);
+        }
+        mwgpu_tree_desc fd{(int)n, idx.data(), child0.data(), inp.coefs.data(), norms.data()};
+        mwgpu_tree *dinp = nullptr;
+        ck(mwgpu_upload_tree(ctx, &md, &fd, &dinp), "upload input tree");
+        acc.h2d_bytes += (unsigned long long)(n * inp.nCoefs + norms.size()) * 8 + (idx.size() + child0.size()) * 4;
+        return dinp;
+    }
     std::vector<int> order, idx, child0;
     export_tree(inp, order, idx, child0);
     std::vector<double> coefs(order.size() * (size_t)inp.nCoefs), norms(order.size() * 8);
