@@ -33,13 +33,13 @@ void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs
                            cudaStream_t s) {
     if (n_work <= 0) return;
     launch_items(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, nullptr, nullptr, s);
-    mixed::k_reduce_chunks<<<n_work, 256, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nullptr);
+    mixed::k_reduce_chunks<<<dim3(n_work, 8), mixed::kReduceThreads, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nullptr);
 }
 
 void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tree, const int *work, int n_work, const int *chunk_begin,
                           const double *partial, cudaStream_t s, const int *nw_dev) {
     if (n_work <= 0) return;
-    mixed::k_reduce_chunks<<<n_work, 256, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nw_dev);
+    mixed::k_reduce_chunks<<<dim3(n_work, 8), mixed::kReduceThreads, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nw_dev);
 }
 
 int contract_items_resident(int K) {

@@ -546,34 +546,61 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
 }
 
 // g coefficients = sum of the chunk partials of g in chunk order; node norms.
-__global__ void __launch_bounds__(256) k_reduce_chunks(const DevTree *gs, const int *work_tree, const int *work, const int *chunk_begin,
-                                                       const double *partial, int nc, const int *nw_dev) {
-    const int tid = threadIdx.x;
-    const int wi = blockIdx.x;
+// CTA (wi, comp) handles component comp of work entry wi: each thread sums
+// up to 4 coefficients over the chunks with 4 chunks of loads in flight (the
+// additions per coefficient stay in chunk order), so coarse levels with few
+// g nodes and many chunks each still spread over 8 CTAs per node.
+constexpr int kReduceThreads = 128;
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_chunks(const DevTree *gs, const int *work_tree, const int *work, const int *chunk_begin,
+                                                                  const double *partial, int nc, const int *nw_dev) {
+    constexpr int NT = kReduceThreads, E = 4, U = 4;
+    const int tid = threadIdx.x, wi = blockIdx.x, comp = blockIdx.y;
     if (nw_dev && wi >= *nw_dev) return;
     const int gi = work[wi];
     const DevTree &g = gs[work_tree[wi]];
     const int c0 = chunk_begin[wi], c1 = chunk_begin[wi + 1];
-    double *go = g.coefs + (size_t)gi * nc;
     const int K3 = nc / 8;
-    __shared__ double red[8][8];
-    double part[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int e = tid; e < nc; e += 256) {
-        double v = 0.0;
-        for (int c = c0; c < c1; c++) v += partial[(size_t)c * nc + e];
-        go[e] = v;
-        part[e / K3] += v * v;
+    const double *src = partial + (size_t)comp * K3;
+    double *go = g.coefs + (size_t)gi * nc + (size_t)comp * K3;
+    double ss = 0.0;
+    for (int e0 = tid; e0 < K3; e0 += E * NT) {
+        bool ok[E];
+        double v[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            ok[j] = e0 + j * NT < K3;
+            v[j] = 0.0;
+        }
+        int c = c0;
+        for (; c + U <= c1; c += U) {
+            double q[U][E];
+#pragma unroll
+            for (int u = 0; u < U; u++)
+#pragma unroll
+                for (int j = 0; j < E; j++) q[u][j] = ok[j] ? src[(size_t)(c + u) * nc + e0 + j * NT] : 0.0;
+#pragma unroll
+            for (int u = 0; u < U; u++)
+#pragma unroll
+                for (int j = 0; j < E; j++) v[j] += q[u][j];
+        }
+        for (; c < c1; c++)
+#pragma unroll
+            for (int j = 0; j < E; j++) v[j] += ok[j] ? src[(size_t)c * nc + e0 + j * NT] : 0.0;
+#pragma unroll
+        for (int j = 0; j < E; j++)
+            if (ok[j]) {
+                go[e0 + j * NT] = v[j];
+                ss += v[j] * v[j];
+            }
     }
-    for (int comp = 0; comp < 8; comp++) {
-        double v = part[comp];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if ((tid & 31) == 0) red[comp][tid >> 5] = v;
-    }
+    __shared__ double red[NT / 32];
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, o);
+    if ((tid & 31) == 0) red[tid >> 5] = ss;
     __syncthreads();
-    if (tid < 8) {
+    if (tid == 0) {
         double t = 0.0;
-        for (int wv = 0; wv < 8; wv++) t += red[tid][wv];
-        g.norms[(size_t)gi * 8 + tid] = sqrt(t);
+        for (int wv = 0; wv < NT / 32; wv++) t += red[wv];
+        g.norms[(size_t)gi * 8 + comp] = sqrt(t);
     }
 }
 

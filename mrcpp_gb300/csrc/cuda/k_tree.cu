@@ -191,6 +191,19 @@ __device__ void block_norms(const double *c, int K3, double *nr, int tid, int nt
     __syncthreads();
 }
 
+// Node norms with warp w summing component w (256 threads): FP64 arithmetic is
+// slow on this part, so each lane does K^3/32 products and one shuffle tree.
+__device__ __forceinline__ void block_norms8(const double *c, int K3, double *nr, int tid) {
+    const int w = tid >> 5, lane = tid & 31;
+    double s = 0.0;
+    for (int e = lane; e < K3; e += 32) {
+        const double v = c[(size_t)w * K3 + e];
+        s += v * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) nr[w] = sqrt(s);
+}
+
 __global__ void k_node_norms(DevMRA m, DevTree t, const int *nodes, int n) {
     int i = nodes[blockIdx.x];
     block_norms(t.coefs + (size_t)i * 8 * m.kp1_d, m.kp1_d, t.norms + (size_t)i * 8, threadIdx.x, blockDim.x);
@@ -331,7 +344,18 @@ __global__ void k_mw_down32(DevMRA m, DevTree t0, const DevTree *ts, const int *
         }
     }
     __syncthreads();
-    for (int gt = 0; gt < 8; gt++) block_norms(t.coefs + (size_t)(c0 + gt) * 8 * K3, K3, t.norms + (size_t)(c0 + gt) * 8, tid, nthr);
+    // only the scaling component of a child changed: warp w recomputes the
+    // scaling norm of child w (the wavelet norms stay, or are 0 when overwritten)
+    {
+        const int w = tid >> 5, lane = tid & 31;
+        const double *cc = t.coefs + (size_t)(c0 + w) * 8 * K3;
+        double s = 0.0;
+        for (int e = lane; e < K3; e += 32) s += cc[e] * cc[e];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        double *nr = t.norms + (size_t)(c0 + w) * 8;
+        if (lane == 0) nr[0] = sqrt(s);
+        if (overwrite && lane >= 1 && lane < 8) nr[lane] = 0.0;
+    }
 }
 
 __global__ void k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n) {
@@ -357,7 +381,7 @@ __global__ void k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *pt
     double *pc = t.coefs + (size_t)p * 8 * K3;
     for (int e = tid; e < 8 * K3; e += nthr) pc[e] = (double)t2[e];
     __syncthreads();
-    block_norms(pc, K3, t.norms + (size_t)p * 8, tid, nthr);
+    block_norms8(pc, K3, t.norms + (size_t)p * 8, tid);
 }
 
 __global__ void k_to_float(const double *src, float *dst, size_t n) {

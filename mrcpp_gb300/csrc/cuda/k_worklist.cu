@@ -109,154 +109,222 @@ __device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const Dev
     return pc.fid >= 0;
 }
 
-template <bool FILL>
+// the reference's FP64 norm test for one component (ConvolutionCalculator.cpp:
+// oNorm * fThr > gThreshold, with the products in the same order); kept out of
+// line: it only runs for estimates within the FP32 margin of the threshold
+__device__ __noinline__ bool exact_pass(const double *onorms, int base, int t0, int t1, int t2, int i0, int i1, int i2, int bsz, double fNorm,
+                                        double gthr) {
+    double oNorm = 1.0;
+    oNorm *= onorms[(size_t)(base + t0) * 4 + i0];
+    oNorm *= onorms[(size_t)(base + t1) * 4 + i1];
+    oNorm *= onorms[(size_t)(base + t2) * 4 + i2];
+    const double fThr = (double)bsz * fNorm;
+    return oNorm * fThr > gthr;
+}
+
+// Screening of one (pair, term): the (ft, gt) components of the term that
+// reach g (mask) and the structural set (smask).  The norm test is
+// oNorm * fThr > gThreshold: without screening (gThreshold < 0) every
+// structural component passes; otherwise an FP32 estimate decides when it is
+// clear of the threshold by far more than its rounding error (2^-12 relative
+// against < 2^-20), and the FP64 expression of the reference decides the
+// rest.  For 1e-20 < gThreshold < 1e20 an FP32 underflow of one factor can
+// only happen for products far below the threshold (the other factors are
+// bounded by 1e12).  FP64 arithmetic runs at a small fraction of the FP32
+// rate on this part, so the loop works on FP32 copies of the norms; the
+// component loops are unrolled so that every table index is a constant.
+struct PairNorms {
+    float fnf[8];        // f component norms rounded to FP32
+    unsigned fnz;        // components with norm >= MachineZero
+    float fmx_up;        // FP32 upper bound of the largest f norm
+    const double *fn;    // the FP64 norms
+};
+
+__device__ __forceinline__ void term_mask(const DevOper &op, const TermRow &row, const PairCtx &pc, const PairNorms &pn, bool screen, bool fp32,
+                                          float thr_hi, float thr_lo, double gthr, unsigned long long &mask, unsigned long long &smask,
+                                          unsigned (&inm)[3]) {
+    mask = smask = 0ull;
+    inm[0] = inm[1] = inm[2] = 0u;
+    const int L0 = row.L0, off = row.off;
+    int fac[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) fac[c] = row.wd[c] < 0 ? 1 : 2 * row.wd[c] + 1;
+    if (screen && fp32) {
+        // bound of every component product of this term: the largest operator
+        // norm per direction, band size and f norm; clear of the threshold by
+        // far more than the FP32 rounding -> nothing passes
+        if (off < 0 || abs(pc.tl[0]) > L0 || abs(pc.tl[1]) > L0 || abs(pc.tl[2]) > L0) return;
+        const int fm = max(max(fac[0], fac[1]), max(fac[2], fac[3]));
+        const float bound = op.norm_max[off + pc.tl[0] + L0] * op.norm_max[off + pc.tl[1] + L0] * op.norm_max[off + pc.tl[2] + L0] *
+                            ((float)(fm * fm * fm * 64) * pn.fmx_up);
+        if (bound < thr_lo) return;
+    }
+    // per direction: in-band mask of the 4 operator components and, for the
+    // estimate, FP32 norm x band-size factor (0 outside the band)
+    float an[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const bool in = abs(pc.tl[d]) <= row.wd[c];
+            inm[d] |= (in ? 1u : 0u) << c;
+            an[d][c] = (screen && fp32 && in) ? op.norms32[(size_t)(off + pc.tl[d] + L0) * 4 + c] * (float)fac[c] : 0.0f;
+        }
+#pragma unroll
+    for (int ft = 0; ft < 8; ft++) {
+        if (!((pn.fnz >> ft) & 1u)) continue;
+        const float ff = 64.0f * pn.fnf[ft];
+#pragma unroll
+        for (int gt = 0; gt < 8; gt++) {
+            if (ft == 0 && gt == 0 && pc.depth != 0) continue;
+            const int i0 = 2 * (gt & 1) + (ft & 1), i1 = 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1), i2 = 2 * (gt >> 2) + (ft >> 2);
+            if (!((inm[0] >> i0) & (inm[1] >> i1) & (inm[2] >> i2) & 1u)) continue;
+            const unsigned long long bit = 1ull << (ft * 8 + gt);
+            smask |= bit;
+            if (!screen) {
+                mask |= bit;
+                continue;
+            }
+            if (fp32) {
+                const float est = (an[0][i0] * an[1][i1]) * (an[2][i2] * ff);
+                if (est > thr_hi) {
+                    mask |= bit;
+                    continue;
+                }
+                if (est < thr_lo) continue;
+            }
+            if (exact_pass(op.norms, off + L0, pc.tl[0], pc.tl[1], pc.tl[2], i0, i1, i2, fac[i0] * fac[i1] * fac[i2] * 64, pn.fn[ft], gthr))
+                mask |= bit;
+        }
+    }
+}
+
+// One work-list pass over the band pairs (g, f): COUNT stores the number of
+// items of each pair, FILL writes them at item_off[p] in term order.  A group
+// of G consecutive lanes shares a pair and takes its terms G at a time (lane
+// j term base + j), the items of a round placed by a ballot prefix, so that
+// small levels (few pairs, all terms) spread over G times more threads; the
+// terms are sorted by descending band width, so a pair is finished at its
+// first term whose band misses the cell.
 // n_pairs / n_work are the launch capacity; with np_dev / nw_dev the actual
 // counts come from the device (levels whose work list is made on the device),
 // and COUNT writes zero counts for the pairs in [*np_dev, n_pairs).
+template <bool FILL, int G>
 __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                                                const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts,
                                                const long long *item_off, WorkItem *items, long long items_cap, unsigned long long *ncomp,
                                                unsigned long long *nband, int *err, const long long *np_dev, const int *nw_dev) {
-    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    static_assert(G == 1 || G == 4 || G == 8 || G == 32, "lane group size");
+    const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long p = gid / G;
+    const int j = (int)(gid % G), lane = threadIdx.x & 31;
     int cnt = 0;
     unsigned long long comp = 0, band = 0;
     const long long n_cap = n_pairs;
     if (np_dev) n_pairs = *np_dev;
     if (nw_dev) n_work = *nw_dev;
-    if (!FILL && p >= n_pairs && p < n_cap) counts[p] = 0;
+    if (!FILL && j == 0 && p >= n_pairs && p < n_cap) counts[p] = 0;
+    PairCtx pc;
+    bool ok = false;
     if (p < n_pairs) {
-        PairCtx pc;
-        if (!locate_pair(m, op, fs, gs, work_tree, work, pair_off, n_work, p, pc)) {
-            atomicOr(err, DE_LOOKUP);
-        } else {
-            band = 1;
-            const DevTree &f = fs[pc.tree];
-            const double gthr = gthrs[pc.tree];
-            // Norm test oNorm * fThr > gThreshold: without screening (gThreshold < 0)
-            // every structural component passes; otherwise an FP32 estimate decides
-            // when it is clear of the threshold by far more than its rounding
-            // error (2^-12 relative against < 2^-20), and the FP64 expression of
-            // the reference decides the rest.  For 1e-20 < gThreshold < 1e20 an
-            // FP32 underflow of one factor can only happen for products far below
-            // the threshold (the other factors are bounded by 1e12).
-            const bool screen = !(gthr < 0.0);
-            const bool fp32 = gthr > 1e-20 && gthr < 1e20;
-            const float thr_hi = (float)(gthr * (1.0 + 1.0 / 4096.0)), thr_lo = (float)(gthr * (1.0 - 1.0 / 4096.0));
-            double fn[8];
-            bool any = false;
-            double fmx = 0.0;
-            for (int c = 0; c < 8; c++) {
-                fn[c] = f.norms[(size_t)pc.fid * 8 + c];
-                any |= !(fn[c] < kMachineZero);
-                if (!(fn[c] < kMachineZero)) fmx = fmax(fmx, fn[c]);
-            }
-            const float fmx_up = nextafterf((float)fmx, INFINITY);
-            const int maxdl = max(abs(pc.tl[0]), max(abs(pc.tl[1]), abs(pc.tl[2])));
-            const int T = op.n_terms, depth = pc.depth;
-            long long wpos = FILL ? item_off[p] : 0;
-            for (int ti = 0; any && ti < T; ti++) {
-                const int i = op.term_order[depth * T + ti];
-                const int *bwi = op.bw + ((size_t)i * op.max_rows + depth) * 5;
-                if (maxdl > bwi[4]) break;
-                const int L0 = op.dep_L[i * op.max_rows + depth], off = op.dep_off[i * op.max_rows + depth];
-                int wd[4];
-                for (int c = 0; c < 4; c++) wd[c] = bwi[c];
-                if (screen && fp32) {
-                    // bound of every component product of this term: the largest
-                    // operator norm per direction, band size and f norm; clear of the
-                    // threshold by far more than the FP32 rounding -> nothing passes
-                    if (off < 0 || abs(pc.tl[0]) > L0 || abs(pc.tl[1]) > L0 || abs(pc.tl[2]) > L0) continue;
-                    int fm = 1;
-                    for (int c = 0; c < 4; c++) fm = max(fm, wd[c] < 0 ? 1 : 2 * wd[c] + 1);
-                    const float bound = op.norm_max[off + pc.tl[0] + L0] * op.norm_max[off + pc.tl[1] + L0] * op.norm_max[off + pc.tl[2] + L0] *
-                                        ((float)(fm * fm * fm * 64) * fmx_up);
-                    if (bound < thr_lo) continue;
-                }
-                bool inb[3][4];
-                double nrm[3][4];
-                float nrf[3][4];
-                for (int d = 0; d < 3; d++)
-                    for (int c = 0; c < 4; c++) {
-                        inb[d][c] = abs(pc.tl[d]) <= wd[c];
-                        nrm[d][c] = (screen && inb[d][c]) ? op.norms[(size_t)(off + pc.tl[d] + L0) * 4 + c] : 0.0;
-                        nrf[d][c] = (float)nrm[d][c];
-                    }
-                // band-size factor 64 * prod_d (2 w(2 a_d + b_d) + 1) over directions with w >= 0
-                int fac[4];
-                for (int c = 0; c < 4; c++) fac[c] = wd[c] < 0 ? 1 : 2 * wd[c] + 1;
-                unsigned long long mask = 0, smask = 0;
-                for (int ft = 0; ft < 8; ft++) {
-                    const double fNorm = fn[ft];
-                    if (fNorm < kMachineZero) continue;
-                    for (int gt = 0; gt < 8; gt++) {
-                        if (depth != 0 && ft == 0 && gt == 0) continue;
-                        const int i0 = 2 * (gt & 1) + (ft & 1), i1 = 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1), i2 = 2 * (gt >> 2) + (ft >> 2);
-                        if (!(inb[0][i0] && inb[1][i1] && inb[2][i2])) continue;
-                        const unsigned long long bit = 1ull << (ft * 8 + gt);
-                        smask |= bit;
-                        if (!screen) {
-                            mask |= bit;
-                            continue;
-                        }
-                        const int bsz = fac[i0] * fac[i1] * fac[i2] * 64;
-                        if (fp32) {
-                            const float est = nrf[0][i0] * nrf[1][i1] * nrf[2][i2] * ((float)bsz * (float)fNorm);
-                            if (est > thr_hi) {
-                                mask |= bit;
-                                continue;
-                            }
-                            if (est < thr_lo) continue;
-                        }
-                        double oNorm = 1.0;
-                        oNorm *= nrm[0][i0];
-                        oNorm *= nrm[1][i1];
-                        oNorm *= nrm[2][i2];
-                        const double fThr = (double)bsz * fNorm;
-                        if (oNorm * fThr > gthr) mask |= bit;
-                    }
-                }
-                if (mask == 0ull) continue;
-                if (FILL) {
-                    WorkItem it;
-                    it.mask = mask;
-                    it.fid = pc.fid;
-                    it.term = (short)i;
-                    it.tl[0] = (short)pc.tl[0];
-                    it.tl[1] = (short)pc.tl[1];
-                    it.tl[2] = (short)pc.tl[2];
-                    it.flags = (mask == smask) ? 1 : 0;
-                    it.pad = 0;
-                    it.sched = 0ull;
-                    if (it.flags) {
-                        unsigned nzm = 0;
-                        for (int b = 0; b < 8; b++) nzm |= (((mask >> (8 * b)) & 0xffull) != 0ull) << b;
-                        int ib[3] = {0, 0, 0};
-                        for (int d = 0; d < 3; d++)
-                            for (int c = 0; c < 4; c++) ib[d] |= (inb[d][c] ? 1 : 0) << c;
-                        it.sched = block_schedule(nzm, ib, depth != 0 && (nzm & 1u));
-                    }
-                    if (wpos < items_cap) items[wpos] = it;
-                    else atomicOr(err, DE_POOL_FULL);
-                    wpos++;
-                } else {
-                    comp += __popcll(mask);
-                }
-                cnt++;
+        ok = locate_pair(m, op, fs, gs, work_tree, work, pair_off, n_work, p, pc);
+        if (!ok && j == 0) atomicOr(err, DE_LOOKUP);
+    }
+    PairNorms pn;
+    pn.fnz = 0u;
+    pn.fmx_up = 0.f;
+    pn.fn = nullptr;
+    double gthr = 0.0;
+    int maxdl = 0;
+    if (ok) {
+        band = (j == 0);
+        const DevTree &f = fs[pc.tree];
+        gthr = gthrs[pc.tree];
+        pn.fn = f.norms + (size_t)pc.fid * 8;
+        double fmx = 0.0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const double v = pn.fn[c];
+            pn.fnf[c] = (float)v;
+            if (!(v < kMachineZero)) {
+                pn.fnz |= 1u << c;
+                fmx = fmax(fmx, v);
             }
         }
-        if (!FILL) counts[p] = cnt;
+        pn.fmx_up = nextafterf((float)fmx, INFINITY);
+        maxdl = max(abs(pc.tl[0]), max(abs(pc.tl[1]), abs(pc.tl[2])));
     }
+    const bool screen = !(gthr < 0.0);
+    const bool fp32 = gthr > 1e-20 && gthr < 1e20;
+    const float thr_hi = (float)(gthr * (1.0 + 1.0 / 4096.0)), thr_lo = (float)(gthr * (1.0 - 1.0 / 4096.0));
+    const int T = op.n_terms;
+    long long wpos = (FILL && ok) ? item_off[p] : 0;
+    const bool live = ok && pn.fnz != 0u;
+    for (int base = 0; base < T; base += G) {
+        const int ti = base + j;
+        bool active = live && ti < T;
+        TermRow row;
+        if (active) {
+            row = op.term_rows[(size_t)pc.depth * T + ti];
+            active = maxdl <= row.bw_max;
+        }
+        if (G == 1) {
+            if (!active) break;
+        } else if (!__any_sync(0xffffffffu, active)) {
+            break;
+        }
+        unsigned long long mask = 0ull, smask = 0ull;
+        unsigned inm[3] = {0u, 0u, 0u};
+        if (active) term_mask(op, row, pc, pn, screen, fp32, thr_hi, thr_lo, gthr, mask, smask, inm);
+        const bool pass = mask != 0ull;
+        long long pos = wpos;
+        int n_round = pass ? 1 : 0;
+        if (G > 1) {
+            const unsigned b = __ballot_sync(0xffffffffu, pass);
+            const unsigned grp = G == 32 ? b : (b >> (lane & ~(G - 1))) & (unsigned)((1ull << G) - 1ull);
+            pos = wpos + __popc(grp & ((1u << j) - 1u));
+            n_round = __popc(grp);
+        }
+        if (pass) {
+            if (FILL) {
+                WorkItem it;
+                it.mask = mask;
+                it.fid = pc.fid;
+                it.term = (short)row.term;
+                it.tl[0] = (short)pc.tl[0];
+                it.tl[1] = (short)pc.tl[1];
+                it.tl[2] = (short)pc.tl[2];
+                it.flags = (mask == smask) ? 1 : 0;
+                it.pad = 0;
+                it.sched = 0ull;
+                if (it.flags) {
+                    unsigned nzm = 0;
+                    for (int b = 0; b < 8; b++) nzm |= (((mask >> (8 * b)) & 0xffull) != 0ull) << b;
+                    const int ib[3] = {(int)inm[0], (int)inm[1], (int)inm[2]};
+                    it.sched = block_schedule(nzm, ib, pc.depth != 0 && (nzm & 1u));
+                }
+                if (pos < items_cap) items[pos] = it;
+                else atomicOr(err, DE_POOL_FULL);
+            } else {
+                comp += __popcll(mask);
+            }
+        }
+        wpos += n_round;
+        cnt += n_round;
+    }
+    if (!FILL && j == 0 && p < n_pairs) counts[p] = cnt;
     if (!FILL) {
         for (int o = 16; o > 0; o >>= 1) {
             comp += __shfl_down_sync(0xffffffffu, comp, o);
             band += __shfl_down_sync(0xffffffffu, band, o);
         }
-        if ((threadIdx.x & 31) == 0 && (comp || band)) {
+        if (lane == 0 && (comp || band)) {
             atomicAdd(ncomp, comp);
             atomicAdd(nband, band);
         }
     }
 }
+
 
 // exclusive scan of int counts into long long offsets: per-block scan, scan of
 // the block sums (one block), add.
@@ -361,22 +429,48 @@ __global__ void k_chunk_fill(const long long *g_off, const long long *c_off, int
         if (c < cap) chunks[c] = make_int4(wi, (int)x, (int)min(e, x + per), 0);
 }
 
+// lanes per pair: enough threads for the whole GPU (152 SMs x 2048) on small
+// levels, one lane per pair once the pairs alone fill it
+int pair_group(long long n_pairs) {
+    constexpr long long kThreads = 152LL * 2048;
+    if (n_pairs * 32 <= 2 * kThreads) return 32;
+    if (n_pairs * 8 <= 2 * kThreads) return 8;
+    if (n_pairs * 4 <= 2 * kThreads) return 4;
+    return 1;
+}
+
 }  // namespace
 
 void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                         const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts, unsigned long long *ncomp,
                         unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
     if (n_pairs <= 0) return;
-    k_pairs<false><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts,
-                                                                    nullptr, nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
+    auto go = [&](auto kern, int g) {
+        kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts, nullptr,
+                                                                  nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
+    };
+    switch (pair_group(n_pairs)) {
+        case 32: go(k_pairs<false, 32>, 32); break;
+        case 8: go(k_pairs<false, 8>, 8); break;
+        case 4: go(k_pairs<false, 4>, 4); break;
+        default: go(k_pairs<false, 1>, 1); break;
+    }
 }
 
 void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                        const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const long long *item_off, WorkItem *items,
                        long long items_cap, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
     if (n_pairs <= 0) return;
-    k_pairs<true><<<(unsigned)((n_pairs + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr,
-                                                                   item_off, items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
+    auto go = [&](auto kern, int g) {
+        kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr, item_off,
+                                                                  items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
+    };
+    switch (pair_group(n_pairs)) {
+        case 32: go(k_pairs<true, 32>, 32); break;
+        case 8: go(k_pairs<true, 8>, 8); break;
+        case 4: go(k_pairs<true, 4>, 4); break;
+        default: go(k_pairs<true, 1>, 1); break;
+    }
 }
 
 void launch_chunk_count(const long long *g_off, int n_work, long long per, int *counts, cudaStream_t s, const int *nw_dev) {

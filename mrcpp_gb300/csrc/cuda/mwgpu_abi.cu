@@ -820,12 +820,27 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         for (int c = 0; c < 4; c++) mx = std::max(mx, d->norms[q * 4 + c]);
         nmax[q] = std::nextafter((float)mx, INFINITY);
     }
-    float *p_blk32, *p_nmax;
+    std::vector<TermRow> trows((size_t)rows * T);
+    for (int dd = 0; dd < rows; dd++)
+        for (int ti = 0; ti < T; ti++) {
+            const int i = order[(size_t)dd * T + ti];
+            TermRow &r = trows[(size_t)dd * T + ti];
+            r.term = i;
+            r.L0 = dep_L[(size_t)i * rows + dd];
+            r.off = dep_off[(size_t)i * rows + dd];
+            r.bw_max = bw[((size_t)i * rows + dd) * 5 + 4];
+            for (int c = 0; c < 4; c++) r.wd[c] = bw[((size_t)i * rows + dd) * 5 + c];
+        }
+    TermRow *p_trows;
+    std::vector<float> nrm32(node * 4);
+    for (size_t q = 0; q < nrm32.size(); q++) nrm32[q] = (float)d->norms[q];
+    float *p_blk32, *p_nmax, *p_nrm32;
     mwgpu_status s;
     if ((s = up(&p_td, d->depth, T)) || (s = up(&p_off, dep_off.data(), dep_off.size())) || (s = up(&p_L, dep_L.data(), dep_L.size())) ||
         (s = up(&p_bw, bw.data(), bw.size())) || (s = up(&p_bsz, bsz.data(), bsz.size())) || (s = up(&p_bm, band_max.data(), band_max.size())) ||
         (s = up(&p_ord, order.data(), order.size())) || (s = up(&p_blk, d->blocks, node * 4 * K2)) || (s = up(&p_nrm, d->norms, node * 4)) ||
-        (s = up(&p_blk32, blk32.data(), blk32.size())) || (s = up(&p_nmax, nmax.data(), nmax.size()))) {
+        (s = up(&p_blk32, blk32.data(), blk32.size())) || (s = up(&p_nmax, nmax.data(), nmax.size())) ||
+        (s = up(&p_nrm32, nrm32.data(), nrm32.size())) || (s = up(&p_trows, trows.data(), trows.size()))) {
         for (void *p : o->allocs) cudaFree(p);
         delete o;
         return s;
@@ -845,6 +860,8 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.n_band_max = maxDepth + 1;
     o->op.blocks32 = p_blk32;
     o->op.norm_max = p_nmax;
+    o->op.norms32 = p_nrm32;
+    o->op.term_rows = p_trows;
     *out = o;
     return MWGPU_OK;
 }

@@ -33,6 +33,14 @@ struct DevMRA {
     const double *filt;  // [2 ops][4 filters][K*K] column-major; op 0 = compression, 1 = reconstruction
 };
 
+// one operator term at one depth, in the per-depth term order (descending
+// band width): term index, translation range and node offset of its cache,
+// band widths of the 4 components and their maximum
+struct __align__(16) TermRow {
+    int term, L0, off, bw_max;
+    int wd[4];
+};
+
 struct DevOper {
     int n_terms, K;
     int max_rows;               // rows of per-term tables (= kMaxDepthRows + 1)
@@ -48,6 +56,8 @@ struct DevOper {
     int n_band_max;
     const float *blocks32;      // FP32 copy of blocks (mixed form), each K x K block transposed
     const float *norm_max;      // [nodes] upper bound of the 4 component norms (FP32, rounded up)
+    const float *norms32;       // [nodes * 4] norms rounded to FP32 (screening estimates)
+    const TermRow *term_rows;   // [max_rows * T] term_order with the per-term tables of each depth
 };
 
 struct DevTree {
