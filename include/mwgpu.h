@@ -223,6 +223,9 @@ mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tree, const dou
 
 /* Copies coefficients and/or norms of all real nodes back (either may be NULL). */
 mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tree, double *coefs, double *norms);
+/* Copies coefficients and/or norms of the real nodes ids[0..n) back, node
+ * ids[j] to row j (gathered on the device: one transfer of n rows). */
+mwgpu_status mwgpu_download_nodes(mwgpu_ctx *ctx, const mwgpu_tree *tree, int n, const int *ids, double *coefs, double *norms);
 
 /* Synchronises the context stream; returns device errors. */
 mwgpu_status mwgpu_sync(mwgpu_ctx *ctx);

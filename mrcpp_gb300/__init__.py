@@ -123,6 +123,7 @@ _SIGS = {
     "mwgpu_mlp_grad": (C.c_int, [_P, _P, _PF, _PF, C.c_int, C.c_float, _PF, _PF]),
     "mwgpu_mlp_train": (C.c_int, [_P, _P, _PF, _PF, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint, _PF]),
     "mwgpu_download_tree": (C.c_int, [_P, _P, _PD, _PD]),
+    "mwgpu_download_nodes": (C.c_int, [_P, _P, C.c_int, _PI, _PD, _PD]),
     "mwgpu_sync": (C.c_int, [_P]),
     "mwgpu_tree_clear_generated": (C.c_int, [_P, _P]),
     "mwgpu_timer_mark": (C.c_int, [_P, C.c_int]),

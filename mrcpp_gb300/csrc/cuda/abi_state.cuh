@@ -4,7 +4,9 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../../include/mwgpu.h"
@@ -15,6 +17,19 @@ using mwgpu::DevOper;
 using mwgpu::DevTree;
 using mwgpu::LevelStats;
 using mwgpu::WorkItem;
+
+// Device blocks of trees, cached per context.  Freeing a tree hands its blocks
+// back here instead of to cudaFree (which waits for the whole device and
+// unmaps): they are reused by later trees once the context's stream has
+// passed the last work that may read them, so an apply with host trees in
+// and out does not pay for allocation.  Sizes are rounded to 4 classes per
+// octave (at most 25% over the request).
+struct DevPool {
+    std::multimap<size_t, void *> free_blocks;  // class size -> block
+    std::unordered_map<void *, size_t> bytes_of;  // every block of the pool
+    std::vector<void *> pending;                  // freed, stream work may still read them
+    size_t cached = 0;                            // bytes of free_blocks + pending
+};
 
 struct mwgpu_ctx {
     int device = 0;
@@ -65,6 +80,7 @@ struct mwgpu_ctx {
     size_t arena_bytes = 0;
     void *d_scrub = nullptr;
     size_t scrub_bytes = 0;
+    DevPool pool;
 };
 
 struct mwgpu_oper {
@@ -105,6 +121,78 @@ struct mwgpu_tree {
         }                                     \
     } while (0)
 
+
+constexpr size_t kPoolCacheLimit = 8ull << 30;
+
+inline size_t pool_class(size_t b) {
+    if (b <= 4096) return 4096;
+    const int e = 63 - __builtin_clzll((unsigned long long)b);  // 2^e <= b < 2^(e+1)
+    const size_t q = (size_t)1 << (e - 2);
+    return (b + q - 1) / q * q;
+}
+
+// all cached blocks back to the device (after the stream has drained)
+inline void pool_trim(mwgpu_ctx *ctx) {
+    DevPool &pl = ctx->pool;
+    cudaStreamSynchronize(ctx->stream);
+    for (void *q : pl.pending) pl.free_blocks.emplace(pl.bytes_of[q], q);
+    pl.pending.clear();
+    for (auto &kv : pl.free_blocks) {
+        cudaFree(kv.second);
+        pl.bytes_of.erase(kv.second);
+    }
+    pl.free_blocks.clear();
+    pl.cached = 0;
+}
+
+inline mwgpu_status pool_alloc_bytes(mwgpu_ctx *ctx, void **p, size_t bytes) {
+    DevPool &pl = ctx->pool;
+    *p = nullptr;
+    if (!pl.pending.empty()) {
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        for (void *q : pl.pending) pl.free_blocks.emplace(pl.bytes_of[q], q);
+        pl.pending.clear();
+    }
+    const size_t c = pool_class(bytes);
+    auto it = pl.free_blocks.find(c);
+    if (it != pl.free_blocks.end()) {
+        *p = it->second;
+        pl.free_blocks.erase(it);
+        pl.cached -= c;
+        return MWGPU_OK;
+    }
+    cudaError_t e = cudaMalloc(p, c);
+    if (e == cudaErrorMemoryAllocation && pl.cached > 0) {
+        cudaGetLastError();
+        pool_trim(ctx);
+        e = cudaMalloc(p, c);
+    }
+    MW_CK(e);
+    pl.bytes_of[*p] = c;
+    return MWGPU_OK;
+}
+
+template <class T> inline mwgpu_status pool_alloc(mwgpu_ctx *ctx, T **p, size_t n) {
+    void *v = nullptr;
+    const mwgpu_status s = pool_alloc_bytes(ctx, &v, sizeof(T) * (n == 0 ? 1 : n));
+    *p = (T *)v;
+    return s;
+}
+
+// a block of the pool goes back to it (reusable after the next stream
+// drain); any other pointer is freed
+inline void pool_free(mwgpu_ctx *ctx, void *p) {
+    if (!p) return;
+    DevPool &pl = ctx->pool;
+    auto it = pl.bytes_of.find(p);
+    if (it == pl.bytes_of.end()) {
+        cudaFree(p);
+        return;
+    }
+    pl.pending.push_back(p);
+    pl.cached += it->second;
+    if (pl.cached > kPoolCacheLimit) pool_trim(ctx);
+}
 
 template <class T> inline mwgpu_status dev_alloc(mwgpu_ctx *ctx, T **p, size_t n) {
     *p = nullptr;

@@ -406,9 +406,10 @@ __global__ void k_copy_nodes(DevTree src, DevTree dst, const int *sid, const int
     const int j = blockIdx.x;
     if (j >= n) return;
     const double *a = src.coefs + (size_t)sid[j] * nc;
-    double *b = dst.coefs + (size_t)did[j] * nc;
+    const int d = did ? did[j] : j;  // without did: row j
+    double *b = dst.coefs + (size_t)d * nc;
     for (int e = threadIdx.x; e < nc; e += blockDim.x) b[e] = a[e];
-    if (threadIdx.x < 8) dst.norms[(size_t)did[j] * 8 + threadIdx.x] = src.norms[(size_t)sid[j] * 8 + threadIdx.x];
+    if (threadIdx.x < 8) dst.norms[(size_t)d * 8 + threadIdx.x] = src.norms[(size_t)sid[j] * 8 + threadIdx.x];
 }
 
 }  // namespace

@@ -40,8 +40,8 @@ mwgpu_status make_mra(mwgpu_ctx *ctx, const mwgpu_mra_desc *d, DevMRA &m, double
     }
     m.sf = d->sf;
     size_t bytes = sizeof(double) * 8 * m.K * m.K;
-    MW_CK(cudaMalloc(filt, bytes));
-    MW_CK(cudaMemcpy(*filt, d->filters, bytes, cudaMemcpyHostToDevice));
+    if (auto s = pool_alloc(ctx, filt, (size_t)8 * m.K * m.K)) return s;
+    MW_CK(cudaMemcpyAsync(*filt, d->filters, bytes, cudaMemcpyHostToDevice, ctx->stream));
     m.filt = *filt;
     return MWGPU_OK;
 }
@@ -58,12 +58,12 @@ mwgpu_status rebuild_hash(mwgpu_ctx *ctx, mwgpu_tree *tr, long long entries) {
     DevTree &t = tr->t;
     int hcap = next_pow2(std::max<long long>(1024, 2 * entries + 16));
     if (hcap != t.hcap) {
-        if (t.hkeys) cudaFree(t.hkeys);
-        if (t.hvals) cudaFree(t.hvals);
+        pool_free(ctx, t.hkeys);
+        pool_free(ctx, t.hvals);
         t.hkeys = nullptr;
         t.hvals = nullptr;
-        if (auto s = dev_alloc(ctx, &t.hkeys, hcap)) return s;
-        if (auto s = dev_alloc(ctx, &t.hvals, hcap)) return s;
+        if (auto s = pool_alloc(ctx, &t.hkeys, hcap)) return s;
+        if (auto s = pool_alloc(ctx, &t.hvals, hcap)) return s;
         t.hcap = hcap;
     }
     MW_CK(cudaMemsetAsync(t.hkeys, 0xFF, sizeof(uint64_t) * hcap, ctx->stream));
@@ -91,10 +91,10 @@ mwgpu_status grow_real(mwgpu_ctx *ctx, mwgpu_tree *tr, int need) {
     int4 *idx;
     double *coefs, *norms;
     int *child0;
-    if (auto s = dev_alloc(ctx, &idx, cap)) return s;
-    if (auto s = dev_alloc(ctx, &coefs, (size_t)cap * nc)) return s;
-    if (auto s = dev_alloc(ctx, &norms, (size_t)cap * 8)) return s;
-    if (auto s = dev_alloc(ctx, &child0, cap)) return s;
+    if (auto s = pool_alloc(ctx, &idx, cap)) return s;
+    if (auto s = pool_alloc(ctx, &coefs, (size_t)cap * nc)) return s;
+    if (auto s = pool_alloc(ctx, &norms, (size_t)cap * 8)) return s;
+    if (auto s = pool_alloc(ctx, &child0, cap)) return s;
     MW_CK(cudaMemsetAsync(coefs, 0, sizeof(double) * cap * nc, ctx->stream));
     if (t.n_real > 0) {
         MW_CK(cudaMemcpyAsync(idx, t.idx, sizeof(int4) * t.n_real, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -102,11 +102,11 @@ mwgpu_status grow_real(mwgpu_ctx *ctx, mwgpu_tree *tr, int need) {
         MW_CK(cudaMemcpyAsync(norms, t.norms, sizeof(double) * t.n_real * 8, cudaMemcpyDeviceToDevice, ctx->stream));
         MW_CK(cudaMemcpyAsync(child0, t.child0, sizeof(int) * t.n_real, cudaMemcpyDeviceToDevice, ctx->stream));
     }
-    MW_CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(t.idx);
-    cudaFree(t.coefs);
-    cudaFree(t.norms);
-    cudaFree(t.child0);
+    // (stream order: the old blocks are reused only after these copies)
+    pool_free(ctx, t.idx);
+    pool_free(ctx, t.coefs);
+    pool_free(ctx, t.norms);
+    pool_free(ctx, t.child0);
     t.idx = idx;
     t.coefs = coefs;
     t.norms = norms;
@@ -125,21 +125,20 @@ mwgpu_status grow_gen(mwgpu_ctx *ctx, mwgpu_tree *tr, int need) {
     int4 *idx;
     double *g, *norms;
     float *g32;
-    if (auto s = dev_alloc(ctx, &idx, tot)) return s;
-    if (auto s = dev_alloc(ctx, &norms, (size_t)tot * 8)) return s;
-    if (auto s = dev_alloc(ctx, &g, (size_t)cap * K3)) return s;
-    if (auto s = dev_alloc(ctx, &g32, (size_t)cap * K3)) return s;
+    if (auto s = pool_alloc(ctx, &idx, tot)) return s;
+    if (auto s = pool_alloc(ctx, &norms, (size_t)tot * 8)) return s;
+    if (auto s = pool_alloc(ctx, &g, (size_t)cap * K3)) return s;
+    if (auto s = pool_alloc(ctx, &g32, (size_t)cap * K3)) return s;
     MW_CK(cudaMemcpyAsync(idx, t.idx, sizeof(int4) * (t.cap_real + t.n_gen), cudaMemcpyDeviceToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(norms, t.norms, sizeof(double) * 8 * (t.cap_real + t.n_gen), cudaMemcpyDeviceToDevice, ctx->stream));
     if (t.n_gen > 0) {
         MW_CK(cudaMemcpyAsync(g, t.gcoefs, sizeof(double) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
         MW_CK(cudaMemcpyAsync(g32, t.gcoefs32, sizeof(float) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
     }
-    MW_CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(t.idx);
-    cudaFree(t.norms);
-    if (t.gcoefs) cudaFree(t.gcoefs);
-    if (t.gcoefs32) cudaFree(t.gcoefs32);
+    pool_free(ctx, t.idx);
+    pool_free(ctx, t.norms);
+    pool_free(ctx, t.gcoefs);
+    pool_free(ctx, t.gcoefs32);
     t.idx = idx;
     t.norms = norms;
     t.gcoefs = g;
@@ -208,7 +207,7 @@ mwgpu_status check_err(mwgpu_ctx *ctx, const char *phase) {
     return MWGPU_OK;
 }
 
-void free_tree(mwgpu_tree *tr);
+void free_tree(mwgpu_ctx *ctx, mwgpu_tree *tr);
 
 // grows a device buffer of T to at least n elements (contents not kept)
 template <class T> mwgpu_status grow_buf(mwgpu_ctx *ctx, T **p, long long *cap, long long n) {
@@ -342,7 +341,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     MW_ARG(out && d && d->n_nodes > 0 && d->idx && d->child0, "invalid tree descriptor");
     auto *tr = new mwgpu_tree();
     tr->is_input = input;
-    if (auto s = make_mra(ctx, mra, tr->mra, &tr->d_filt)) { delete tr; return s; }
+    if (auto s = make_mra(ctx, mra, tr->mra, &tr->d_filt)) { free_tree(ctx, tr); return s; }
     tr->h_filt.assign(mra->filters, mra->filters + 8 * tr->mra.K * tr->mra.K);
     DevTree &t = tr->t;
     const int n = d->n_nodes;
@@ -356,9 +355,9 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     tr->h_child0.assign(d->child0, d->child0 + n);
     for (int i = 0; i < n; i++) tr->h_idx[i] = make_int4(d->idx[4 * i], d->idx[4 * i + 1], d->idx[4 * i + 2], d->idx[4 * i + 3]);
     mwgpu_status s;
-    if ((s = dev_alloc(ctx, &t.idx, tot)) || (s = dev_alloc(ctx, &t.coefs, (size_t)tot * nc)) || (s = dev_alloc(ctx, &t.norms, (size_t)tot * 8)) ||
-        (s = dev_alloc(ctx, &t.child0, tot))) {
-        delete tr;
+    if ((s = pool_alloc(ctx, &t.idx, tot)) || (s = pool_alloc(ctx, &t.coefs, (size_t)tot * nc)) || (s = pool_alloc(ctx, &t.norms, (size_t)tot * 8)) ||
+        (s = pool_alloc(ctx, &t.child0, tot))) {
+        free_tree(ctx, tr);
         return s;
     }
     MW_CK(cudaMemcpyAsync(t.idx, tr->h_idx.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -367,7 +366,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     else MW_CK(cudaMemsetAsync(t.coefs, 0, sizeof(double) * tot * nc, ctx->stream));
     if (input) {
         // FP32 copy read by the mixed form
-        if ((s = dev_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(tr); return s; }
+        if ((s = pool_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(ctx, tr); return s; }
         launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
         ctx->launches++;
     }
@@ -376,7 +375,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     } else if (d->coefs) {
         std::vector<int> all(n);
         for (int i = 0; i < n; i++) all[i] = i;
-        if ((s = ensure_work(ctx, n))) { delete tr; return s; }
+        if ((s = ensure_work(ctx, n))) { free_tree(ctx, tr); return s; }
         MW_CK(cudaMemcpyAsync(ctx->d_work, all.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
         launch_node_norms(tr->mra, t, ctx->d_work, n, ctx->stream);
         ctx->launches++;
@@ -385,24 +384,17 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     }
     // only input trees are looked up by node index (band cells, GenNode
     // ancestors); output trees are addressed by position
-    if (input && (s = rebuild_hash(ctx, tr, n))) { delete tr; return s; }
+    if (input && (s = rebuild_hash(ctx, tr, n))) { free_tree(ctx, tr); return s; }
     *out = tr;
     return MWGPU_OK;
 }
 
-void free_tree(mwgpu_tree *tr) {
+void free_tree(mwgpu_ctx *ctx, mwgpu_tree *tr) {
     if (!tr) return;
     DevTree &t = tr->t;
-    cudaFree(t.idx);
-    cudaFree(t.coefs);
-    cudaFree(t.norms);
-    cudaFree(t.child0);
-    if (t.gcoefs) cudaFree(t.gcoefs);
-    if (t.coefs32) cudaFree(t.coefs32);
-    if (t.gcoefs32) cudaFree(t.gcoefs32);
-    if (t.hkeys) cudaFree(t.hkeys);
-    if (t.hvals) cudaFree(t.hvals);
-    if (tr->d_filt) cudaFree(tr->d_filt);
+    for (void *p : {(void *)t.idx, (void *)t.coefs, (void *)t.norms, (void *)t.child0, (void *)t.gcoefs, (void *)t.coefs32, (void *)t.gcoefs32,
+                    (void *)t.hkeys, (void *)t.hvals, (void *)tr->d_filt})
+        pool_free(ctx, p);
     delete tr;
 }
 
@@ -702,6 +694,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
                     (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_nstage, (void *)ctx->d_ltree})
         if (p) cudaFree(p);
+    pool_trim(ctx);
     for (auto &e : ctx->marks)
         if (e) cudaEventDestroy(e);
     if (ctx->d_scrub) cudaFree(ctx->d_scrub);
@@ -842,6 +835,7 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         (s = up(&p_blk32, blk32.data(), blk32.size())) || (s = up(&p_nmax, nmax.data(), nmax.size())) ||
         (s = up(&p_nrm32, nrm32.data(), nrm32.size())) || (s = up(&p_trows, trows.data(), trows.size()))) {
         for (void *p : o->allocs) cudaFree(p);
+        pool_free(ctx, o->d_filt);
         delete o;
         return s;
     }
@@ -869,7 +863,7 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
 mwgpu_status mwgpu_free_operator(mwgpu_ctx *ctx, mwgpu_oper *o) {
     if (!ctx || !o) return MWGPU_ERR_BAD_ARG;
     for (void *p : o->allocs) cudaFree(p);
-    if (o->d_filt) cudaFree(o->d_filt);
+    pool_free(ctx, o->d_filt);
     delete o;
     return MWGPU_OK;
 }
@@ -930,8 +924,7 @@ mwgpu_status mwgpu_free_tree(mwgpu_ctx *ctx, mwgpu_tree *tr) {
     if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
     MW_ARG(tr->plans == 0, "tree is held by a plan (destroy the plan first)");
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    free_tree(tr);
+    free_tree(ctx, tr);
     return MWGPU_OK;
 }
 
@@ -970,6 +963,33 @@ mwgpu_status mwgpu_download_tree(mwgpu_ctx *ctx, const mwgpu_tree *tr, double *c
     if (coefs) MW_CK(cudaMemcpyAsync(coefs, tr->t.coefs, sizeof(double) * n * nc, cudaMemcpyDeviceToHost, ctx->stream));
     if (norms) MW_CK(cudaMemcpyAsync(norms, tr->t.norms, sizeof(double) * n * 8, cudaMemcpyDeviceToHost, ctx->stream));
     MW_CK(cudaStreamSynchronize(ctx->stream));
+    return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_download_nodes(mwgpu_ctx *ctx, const mwgpu_tree *tr, int n, const int *ids, double *coefs, double *norms) {
+    if (!ctx || !tr) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n >= 0 && (n == 0 || ids), "null node list");
+    for (int j = 0; j < n; j++) MW_ARG(ids[j] >= 0 && ids[j] < tr->t.n_real, "node id out of range");
+    if (n == 0 || (!coefs && !norms)) return MWGPU_OK;
+    cudaSetDevice(ctx->device);
+    const size_t nc = 8 * (size_t)tr->mra.kp1_d;
+    if (auto s = ensure_work(ctx, n)) return s;
+    DevTree stage{};
+    if (auto s = pool_alloc(ctx, &stage.coefs, (size_t)n * nc)) return s;
+    if (auto s = pool_alloc(ctx, &stage.norms, (size_t)n * 8)) {
+        pool_free(ctx, stage.coefs);
+        return s;
+    }
+    MW_CK(cudaMemcpyAsync(ctx->d_work, ids, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    launch_copy_nodes(tr->t, stage, ctx->d_work, nullptr, n, (int)nc, ctx->stream);
+    ctx->launches++;
+    cudaError_t e = cudaSuccess;
+    if (coefs) e = cudaMemcpyAsync(coefs, stage.coefs, sizeof(double) * n * nc, cudaMemcpyDeviceToHost, ctx->stream);
+    if (norms && e == cudaSuccess) e = cudaMemcpyAsync(norms, stage.norms, sizeof(double) * n * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    pool_free(ctx, stage.coefs);
+    pool_free(ctx, stage.norms);
+    MW_CK(e);
     return MWGPU_OK;
 }
 

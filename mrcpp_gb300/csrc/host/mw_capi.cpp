@@ -730,7 +730,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         // node order is TreeBuilder's (levels, each in the order of the parents).
         Tree<3> prop(mra);
         std::vector<int> level_begin, flags;
-        std::vector<double> norm_levels, coefs, norms;
+        std::vector<double> norm_levels, norms;
         try {
             dinp = upload_input(ctx, md, inp, acc);
             const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
@@ -864,21 +864,12 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 propose(frontier);
                 ls.proposal_nodes += (int)prop.nodes.size() - level_begin[first];
             }
-            coefs.resize(prop.nodes.size() * (size_t)prop.nCoefs);
-            norms.resize(prop.nodes.size() * 8);
-            ck(mwgpu_download_tree(ctx, dprop, coefs.data(), norms.data()), "download output tree");
-            acc.d2h_bytes += (coefs.size() + norms.size()) * 8;
-            ls.host_round_trips += 1;
         } catch (...) {
             if (dprop) mwgpu_free_tree(ctx, dprop);
             if (dold) mwgpu_free_tree(ctx, dold);
             if (dinp) mwgpu_free_tree(ctx, dinp);
             throw;
         }
-        mwgpu_free_tree(ctx, dprop);
-        mwgpu_free_tree(ctx, dinp);
-        mwgpu_launch_count(ctx, &l1);
-        acc.launches = l1 - l0;
         // the judged tree, created in TreeBuilder's order (the host ids of the plain apply)
         std::vector<int> map(prop.nodes.size(), -1);
         for (size_t i = 0; i < out.nodes.size(); i++) map[i] = (int)i;
@@ -895,14 +886,32 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 for (int c = 0; c < Tree<3>::tDim; c++) map[p0 + c] = c0 + c;
             }
         ls.kept_nodes = kept;
-        for (size_t i = 0; i < prop.nodes.size(); i++) {
-            const int oi = map[i];
-            if (oi < 0 || !(flags[i] & 1)) continue;
-            std::memcpy(out.c(oi), &coefs[i * (size_t)prop.nCoefs], sizeof(double) * prop.nCoefs);
+        // the kept nodes, gathered on the device in the output tree's order,
+        // straight into its coefficient storage
+        std::vector<int> src(out.nodes.size(), -1);
+        for (size_t i = 0; i < prop.nodes.size(); i++)
+            if (map[i] >= 0 && (flags[i] & 1)) src[map[i]] = (int)i;
+        for (size_t oi = 0; oi < src.size(); oi++)
+            if (src[oi] < 0) throw Error(6, "judged tree: output node without a computed source");
+        norms.resize(src.size() * 8);
+        try {
+            ck(mwgpu_download_nodes(ctx, dprop, (int)src.size(), src.data(), out.coefs.data(), norms.data()), "download output tree");
+        } catch (...) {
+            mwgpu_free_tree(ctx, dprop);
+            mwgpu_free_tree(ctx, dinp);
+            throw;
+        }
+        acc.d2h_bytes += (src.size() * (size_t)out.nCoefs + norms.size()) * 8;
+        ls.host_round_trips += 1;
+        mwgpu_free_tree(ctx, dprop);
+        mwgpu_free_tree(ctx, dinp);
+        mwgpu_launch_count(ctx, &l1);
+        acc.launches = l1 - l0;
+        for (size_t oi = 0; oi < src.size(); oi++) {
             double s2 = 0.0;
             for (int c = 0; c < 8; c++) {
-                out.nodes[oi].norms[c] = norms[i * 8 + c];
-                s2 += norms[i * 8 + c] * norms[i * 8 + c];
+                out.nodes[oi].norms[c] = norms[oi * 8 + c];
+                s2 += norms[oi * 8 + c] * norms[oi * 8 + c];
             }
             out.nodes[oi].squareNorm = s2;
             out.nodes[oi].flags |= F_HASCOEFS;
