@@ -4,6 +4,9 @@
 
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <string>
 #include <unordered_map>
@@ -102,6 +105,7 @@ struct mwgpu_tree {
     std::vector<int4> h_idx;
     std::vector<int> h_child0;
     bool is_input = false;
+    int gen_prec = -1;  // precision mode whose GenNode arithmetic made the GenNodes held
 };
 
 #define MW_CK(call)                                                                                 \
@@ -121,6 +125,28 @@ struct mwgpu_tree {
         }                                     \
     } while (0)
 
+
+// Phase timing of one entry point, on when the environment sets MWGPU_TRACE:
+// every mark drains the stream and adds the host time since the previous
+// mark; the line goes to stderr when the call returns.  (Tracing serialises
+// the host and the device; the figures attribute time, they are not a
+// benchmark.)
+struct PhaseTrace {
+    mwgpu_ctx *ctx;
+    const char *fn;
+    bool on;
+    std::chrono::steady_clock::time_point t0, last;
+    std::string line;
+    PhaseTrace(mwgpu_ctx *c, const char *f) : ctx(c), fn(f), on(std::getenv("MWGPU_TRACE") != nullptr) {
+        if (on) t0 = last = std::chrono::steady_clock::now();
+    }
+    void mark(const std::string &phase);
+    ~PhaseTrace() {
+        if (!on) return;
+        const double tot = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(stderr, "[mwgpu] %s%s total=%.3f ms\n", fn, line.c_str(), tot);
+    }
+};
 
 constexpr size_t kPoolCacheLimit = 8ull << 30;
 
@@ -192,6 +218,16 @@ inline void pool_free(mwgpu_ctx *ctx, void *p) {
     pl.pending.push_back(p);
     pl.cached += it->second;
     if (pl.cached > kPoolCacheLimit) pool_trim(ctx);
+}
+
+inline void PhaseTrace::mark(const std::string &phase) {
+    if (!on) return;
+    cudaStreamSynchronize(ctx->stream);
+    const auto now = std::chrono::steady_clock::now();
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), " %s=%.3f", phase.c_str(), std::chrono::duration<double, std::milli>(now - last).count());
+    line += buf;
+    last = now;
 }
 
 template <class T> inline mwgpu_status dev_alloc(mwgpu_ctx *ctx, T **p, size_t n) {

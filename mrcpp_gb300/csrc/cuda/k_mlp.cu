@@ -201,17 +201,22 @@ __device__ inline double norm_estimate(const DevMRA &m, const DevTree &f, int n,
                 s += v * v;
             }
             if (sh == 0) *stored = f.child0[id] >= 0 ? 2 : 1;
-            return sqrt(s) * exp2(-1.5 * sh);
+            // 2^(-1.5 sh) as a power of two times 1 or 2^(-1/2)
+            return ldexp(sqrt(s) * ((sh & 1) ? 0.70710678118654752440 : 1.0), -((3 * sh) / 2));
         }
     }
     return 0.0;
 }
 
-// one warp per node
-__global__ void k_features(DevMRA m, DevTree f, const int4 *nodes, int n, const int *band_w, const int *terms, int rows, double ftot, float *X) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= n) return;
-    const int4 g = nodes[warp];
+// one CTA of kFeatureThreads per node: the band cells spread over all its
+// threads (each walks up to the nearest stored ancestor of its cells), the
+// band sum reduced in a fixed order
+constexpr int kFeatureThreads = 128;
+__global__ void __launch_bounds__(kFeatureThreads) k_features(DevMRA m, DevTree f, const int4 *nodes, int n, const int *band_w, const int *terms,
+                                                              int rows, double ftot, float *X) {
+    const int node = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    if (node >= n) return;
+    const int4 g = nodes[node];
     const int depth = g.x - m.root_scale;
     const int dr = min(max(depth, 0), rows - 1);
     const int w = min(max(band_w[dr], 0), 3);
@@ -225,19 +230,24 @@ __global__ void k_features(DevMRA m, DevTree f, const int4 *nodes, int n, const 
     const int nx = be[0] - bs[0] + 1, ny = be[1] - bs[1] + 1, nz = be[2] - bs[2] + 1;
     const int cells = max(nx, 0) * max(ny, 0) * max(nz, 0);
     double band = 0.0;
-    for (int q = lane; q < cells; q += 32) {
+    for (int q = tid; q < cells; q += kFeatureThreads) {
         int st;
         band += norm_estimate(m, f, g.x, bs[0] + q % nx, bs[1] + (q / nx) % ny, bs[2] + q / (nx * ny), false, &st);
     }
     for (int o = 16; o > 0; o >>= 1) band += __shfl_down_sync(0xffffffffu, band, o);
-    if (lane == 0) {
+    __shared__ double red[kFeatureThreads / 32];
+    if (lane == 0) red[tid >> 5] = band;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = 0.0;
+        for (int i = 0; i < kFeatureThreads / 32; i++) tot += red[i];
         int st;
         const double own = norm_estimate(m, f, g.x, g.y, g.z, g.w, true, &st);
         const double inv = ftot > 0.0 ? 1.0 / ftot : 1.0;
-        float *x = X + (size_t)warp * F;
+        float *x = X + (size_t)node * F;
         x[0] = (float)depth / 16.f;
         x[1] = (float)(log10(fmax(own * inv, 1e-30)) / 8.0);
-        x[2] = (float)(log10(fmax(band * inv, 1e-30)) / 8.0);
+        x[2] = (float)(log10(fmax(tot * inv, 1e-30)) / 8.0);
         x[3] = (float)terms[dr] / 100.f;
         x[4] = (float)(g.y & 1);
         x[5] = (float)(g.z & 1);
@@ -283,7 +293,7 @@ void launch_mlp_to_bf16(const float *src, __nv_bfloat16 *dst, int n, cudaStream_
 void launch_mlp_features(const DevMRA &m, const DevTree &f, const int4 *nodes, int n, const int *band_w, const int *terms, int rows, double ftot,
                          float *X, cudaStream_t s) {
     if (n <= 0) return;
-    mlp::k_features<<<(n * 32 + 255) / 256, 256, 0, s>>>(m, f, nodes, n, band_w, terms, rows, ftot, X);
+    mlp::k_features<<<n, mlp::kFeatureThreads, 0, s>>>(m, f, nodes, n, band_w, terms, rows, ftot, X);
 }
 
 }  // namespace mwgpu

@@ -384,6 +384,112 @@ __global__ void k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *pt
     block_norms8(pc, K3, t.norms + (size_t)p * 8, tid);
 }
 
+// GenNodes of the mixed form: the path reconstruction of k_gen_nodes with FP32
+// products (filters and buffers in shared memory), starting from the FP32 copy
+// of the real ancestor or from an FP32 GenNode.  The result goes to gcoefs32
+// (read by the mixed contraction) and, widened, to gcoefs; the scaling norm is
+// accumulated in FP64.  The intermediate steps stay in FP32, so a chain through
+// stored GenNodes gives the same values as one walk from the real ancestor.
+__global__ void k_gen_nodes32(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, bool real_only) {
+    extern __shared__ float sg32[];
+    const int K = m.K, K2 = K * K, K3 = m.kp1_d;
+    float *b0 = sg32, *b1 = b0 + 4 * K3, *F = b1 + 4 * K3;  // F: the 4 reconstruction filters
+    __shared__ int s_anc, s_ancn;
+    const int p = blockIdx.x;
+    if (p >= n_pend) return;
+    int n, l0, l1, l2;
+    unpack_key(m, plist[p], n, l0, l1, l2);
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    if (tid == 0) {
+        s_anc = -1;
+        s_ancn = 0;
+        for (int a = n - 1; a >= m.root_scale; a--) {
+            const int sh = n - a;
+            uint64_t key;
+            if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
+            const int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
+            if (id >= 0 && (!real_only || id < f.cap_real)) {
+                s_anc = id;
+                s_ancn = a;
+                break;
+            }
+        }
+    }
+    load_filters32(F, m, 1, tid, nthr);
+    __syncthreads();
+    const int anc = s_anc, an = s_ancn;
+    if (anc < 0) {
+        if (tid == 0) atomicOr(err, DE_LOOKUP);
+        return;
+    }
+    const float *src;
+    {
+        const int sh = n - an - 1;
+        const int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
+        if (anc < f.cap_real) {
+            const float *in = f.coefs32 + (size_t)anc * 8 * K3;
+            for (int q = 0; q < 4; q++) fapply<false>(b0 + q * K3, in + (size_t)(2 * q) * K3, F + (2 * c0 + 0) * K2, K, tid, nthr);
+            __syncthreads();
+            for (int q = 0; q < 4; q++) fapply<true>(b0 + q * K3, in + (size_t)(2 * q + 1) * K3, F + (2 * c0 + 1) * K2, K, tid, nthr);
+            __syncthreads();
+            for (int b2 = 0; b2 < 2; b2++) fapply<false>(b1 + b2 * K3, b0 + (0 + 2 * b2) * K3, F + (2 * c1 + 0) * K2, K, tid, nthr);
+            __syncthreads();
+            for (int b2 = 0; b2 < 2; b2++) fapply<true>(b1 + b2 * K3, b0 + (1 + 2 * b2) * K3, F + (2 * c1 + 1) * K2, K, tid, nthr);
+            __syncthreads();
+            fapply<false>(b0, b1, F + (2 * c2 + 0) * K2, K, tid, nthr);
+            __syncthreads();
+            fapply<true>(b0, b1 + K3, F + (2 * c2 + 1) * K2, K, tid, nthr);
+            __syncthreads();
+        } else {
+            const float *in = f.gcoefs32 + (size_t)(anc - f.cap_real) * K3;
+            fapply<false>(b1, in, F + (2 * c0) * K2, K, tid, nthr);
+            __syncthreads();
+            fapply<false>(b1 + K3, b1, F + (2 * c1) * K2, K, tid, nthr);
+            __syncthreads();
+            fapply<false>(b0, b1 + K3, F + (2 * c2) * K2, K, tid, nthr);
+            __syncthreads();
+        }
+        src = b0;
+    }
+    for (int a = an + 1; a < n; a++) {
+        const int sh = n - a - 1;
+        const int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
+        fapply<false>(b1, src, F + (2 * c0) * K2, K, tid, nthr);
+        __syncthreads();
+        fapply<false>(b1 + K3, b1, F + (2 * c1) * K2, K, tid, nthr);
+        __syncthreads();
+        fapply<false>(b0, b1 + K3, F + (2 * c2) * K2, K, tid, nthr);
+        __syncthreads();
+        src = b0;
+    }
+    const int slot = gen_base + p;
+    if (slot >= f.cap_gen) {
+        if (tid == 0) atomicOr(err, DE_POOL_FULL);
+        return;
+    }
+    double *out = f.gcoefs + (size_t)slot * K3;
+    float *out32 = f.gcoefs32 + (size_t)slot * K3;
+    double s = 0.0;
+    for (int e = tid; e < K3; e += nthr) {
+        const float v = src[e];
+        out32[e] = v;
+        out[e] = (double)v;
+        s += (double)v * (double)v;
+    }
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((tid & 31) == 0) red[tid >> 5] = s;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) t += red[w];
+        double *nr = f.norms + (size_t)(f.cap_real + slot) * 8;
+        nr[0] = sqrt(t);
+        for (int c = 1; c < 8; c++) nr[c] = 0.0;
+        f.idx[f.cap_real + slot] = make_int4(n, l0, l1, l2);
+    }
+}
+
 __global__ void k_to_float(const double *src, float *dst, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = (float)src[i];
 }
@@ -436,8 +542,15 @@ void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *er
     k_hash_build<<<(count + 255) / 256, 256, 0, s>>>(m, t, first, count, err);
 }
 
-void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s, bool real_only) {
+void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s, bool real_only,
+                      bool fp32) {
     if (n_pend <= 0) return;
+    if (fp32) {
+        const size_t smem = sizeof(float) * (8 * (size_t)m.kp1_d + 4 * m.K * m.K);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_nodes32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_gen_nodes32<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
+        return;
+    }
     size_t smem = sizeof(double) * 8 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_nodes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);

@@ -407,6 +407,18 @@ namespace {
 mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount, unsigned long long &gen_total) {
     const mwgpu_oper *o = lv.o;
     const int nt = lv.nt;
+    // GenNodes follow the level's precision mode (FP32 products in the mixed
+    // form); ones made in the other mode are dropped first, so that a result
+    // does not depend on which applies ran on the tree before (trees held by
+    // a plan keep theirs: the plan remakes them on every execution)
+    const bool fp32 = ctx->precision == MWGPU_PREC_MIXED;
+    for (int t = 0; t < nt; t++) {
+        mwgpu_tree *inp = lv.inps[t];
+        if (inp->t.n_gen > 0 && inp->gen_prec != ctx->precision && inp->plans == 0) {
+            inp->t.n_gen = 0;
+            if (auto s = rebuild_hash(ctx, inp, inp->t.n_real)) return s;
+        }
+    }
     pcount.assign(nt, 0);
     for (int attempt = 0; attempt < 8; attempt++) {
         if (auto s = ensure_pending(ctx, std::max(ctx->phcap, 1 << 16), std::max(ctx->pcap, 1 << 15), nt)) return s;
@@ -441,11 +453,12 @@ mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount,
         if (2LL * (f.n_real + f.n_gen + pcount[t]) + 16 > f.hcap)
             if (auto s = rebuild_hash(ctx, inp, (long long)f.n_real + f.n_gen + pcount[t])) return s;
         const uint64_t *pl = ctx->d_plist + (size_t)t * ctx->pcap;
-        launch_gen_nodes(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream);
+        launch_gen_nodes(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream, false, fp32);
         launch_gen_insert(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream);
         ctx->launches += 2;
         f.n_gen += pcount[t];
         gen_total += pcount[t];
+        inp->gen_prec = ctx->precision;
     }
     return MWGPU_OK;
 }
@@ -456,6 +469,7 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
                        std::vector<int> *pcount_out = nullptr) {
     const mwgpu_oper *o = lv.o;
     const int n = lv.n, nt = lv.nt;
+    PhaseTrace tr(ctx, "apply_level");
     if (auto s = ensure_work(ctx, n)) return s;
     if (auto s = ensure_trees(ctx, nt)) return s;
     MW_CK(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -465,7 +479,9 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
     MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
     std::vector<int> pcount;
     unsigned long long gen_total = 0;
+    tr.mark("setup");
     if (auto s = gen_pass(ctx, lv, pcount, gen_total)) return s;
+    tr.mark("gen");
     if (pcount_out) *pcount_out = pcount;
     // per-tree screening threshold (ConvolutionCalculator.cpp:297-305)
     lv.gthr.assign(nt, 0.0);
@@ -497,6 +513,7 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
         }
     }
     MW_CK(cudaGetLastError());
+    tr.mark("contract");
     MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
     LevelStats hs{};
     MW_CK(cudaMemcpyAsync(&hs, ctx->d_stats, sizeof(LevelStats), cudaMemcpyDeviceToHost, ctx->stream));
@@ -509,6 +526,7 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
         MW_CK(cudaMemcpyAsync(staged.data(), ctx->d_nstage, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
     }
     if (auto s = check_err(ctx, "apply_level")) return s;
+    tr.mark("result");
     if (norms_out)
         for (int j = 0; j < n; j++) std::memcpy(norms_out + 8 * (size_t)lv.order[j], &staged[8 * (size_t)j], sizeof(double) * 8);
     if (ctx->precision == MWGPU_PREC_MIXED) hs.node_terms = mixed_nt.node_terms;
@@ -1287,7 +1305,8 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
     // GenNode values from the current input coefficients (slots fixed at plan time)
     for (int t = 0; t < pl->nt; t++) {
         if (pl->gcount[t] == 0) continue;
-        launch_gen_nodes(pl->inps[t]->mra, pl->inps[t]->t, pl->d_gkeys[t], pl->gcount[t], 0, pl->d_err, st, true);
+        launch_gen_nodes(pl->inps[t]->mra, pl->inps[t]->t, pl->d_gkeys[t], pl->gcount[t], 0, pl->d_err, st, true,
+                         pl->precision == MWGPU_PREC_MIXED);
         ctx->launches++;
     }
     if (pl->precision == MWGPU_PREC_MIXED) {
@@ -1632,6 +1651,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             MW_ARG(c0 < 0 || (c0 >= level_begin[j + 1] && j + 1 < n_levels && c0 + 8 <= level_begin[j + 2]),
                    "proposed children must lie in the next level");
         }
+    PhaseTrace tr(ctx, "apply_judged");
     std::vector<int> all(N);
     for (int i = 0; i < N; i++) all[i] = i;
     mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
@@ -1651,7 +1671,9 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     // GenNodes for every proposed node (a superset of what the judged tree needs)
     std::vector<int> pcount;
     unsigned long long gen_total = 0;
+    tr.mark("setup");
     if (auto s = gen_pass(ctx, lv, pcount, gen_total)) return s;
+    tr.mark("gen");
     lv.fs.assign(1, inp->t);
     lv.gs.assign(1, out->t);
     MW_CK(cudaMemcpyAsync(ctx->d_fs, lv.fs.data(), sizeof(DevTree), cudaMemcpyHostToDevice, ctx->stream));
@@ -1669,7 +1691,30 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     for (int j = 0; j < n_levels; j++) max_level = std::max(max_level, level_begin[j + 1] - level_begin[j]);
     for (auto v : lvl_pairs) max_pairs = std::max(max_pairs, v);
     std::vector<long long> lvl_per(n_levels, 8);
+    const int T = o->op.n_terms;
+    // Work-list capacity per level: every (pair, term) of the level as an item
+    // while that stays within kJudgedItemBudget (no host round trip); beyond
+    // it, or when a level overflows it, the exact bound from an unscreened
+    // count pass (one synchronisation) and the pass runs again.
+    constexpr long long kJudgedItemBudget = 1LL << 25;
+    const bool estimate_fits = max_pairs * T <= kJudgedItemBudget;
     if (mixed) {
+        cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, ctx->device);
+        grid = std::max(1, dev_sm) * std::max(1, contract_items_resident(o->op.K));
+    }
+    int first_miss = 0x7fffffff;
+    for (int attempt = 0;; attempt++) {
+    const bool exact = attempt > 0 || !estimate_fits;
+    max_items = max_chunks = 0;
+    if (mixed && !exact) {
+        for (int j = 0; j < n_levels; j++) {
+            lvl_items[j] = lvl_pairs[j] * T;
+            lvl_per[j] = 0;
+            max_items = std::max(max_items, lvl_items[j]);
+            max_chunks = std::max(max_chunks, (long long)(level_begin[j + 1] - level_begin[j]) + kChunkTarget + 1);
+        }
+    }
+    if (mixed && exact) {
         // items per proposed node without norm screening (an upper bound of every level's work list)
         if (auto s = grow_buf(ctx, &ctx->d_pair_off, &ctx->pair_off_cap, N + 1)) return s;
         if (auto s = grow_buf(ctx, &ctx->d_pcounts, &ctx->pcounts_cap, poff[N] + 1)) return s;
@@ -1689,8 +1734,6 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
         MW_CK(cudaMemcpyAsync(ub.data(), ctx->d_goff, sizeof(long long) * (N + 1), cudaMemcpyDeviceToHost, ctx->stream));
         MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
         if (auto s = check_err(ctx, "judged apply (work-list bound)")) return s;
-        cudaDeviceGetAttribute(&dev_sm, cudaDevAttrMultiProcessorCount, ctx->device);
-        grid = std::max(1, dev_sm) * std::max(1, contract_items_resident(o->op.K));
         // chunk length from the level's item count on the device (the rule of
         // the host-driven levels, so that both give the same sums): at most
         // n + kChunkTarget + 1 chunks
@@ -1705,6 +1748,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             return MWGPU_ERR_BAD_ARG;
         }
     }
+    tr.mark("bound");
     // scratch, sized then carved
     const int rows = std::max(m.max_scale - m.root_scale + 2, 1);
     auto carve = [&](Carver &c) {
@@ -1774,9 +1818,9 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     MW_CK(cudaMemcpyAsync(b.state, state0, sizeof(state0), cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(b.first_miss, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemsetAsync(b.node_terms, 0, sizeof(unsigned long long), ctx->stream));
+    tr.mark("arena");
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
     cudaStream_t st = ctx->stream;
-    const int T = o->op.n_terms;
     for (int j = first_level; j < n_levels; j++) {
         const int lb = level_begin[j], nl = level_begin[j + 1] - lb;
         launch_keep_counts(b.flags, lb, nl, b.kcnt, st);
@@ -1813,10 +1857,24 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
         }
         launch_judge(m, out->t, b.work, b.nwork, nl, b.state, prec, abs_prec, b.scale_fac, m.max_scale, b.flags, j, b.first_miss, st);
         ctx->launches++;
+        if (tr.on) tr.mark("L" + std::to_string(j));
     }
     MW_CK(cudaGetLastError());
     MW_CK(cudaEventRecord(ctx->ev2, ctx->stream));
-    int first_miss = big;
+    if (mixed && !exact) {
+        int herr = 0;
+        MW_CK(cudaMemcpyAsync(&herr, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        if (herr == DE_POOL_FULL) {
+            // a level's work list outgrew the estimate: exact bound, again
+            // (the pass only overwrites what it computes)
+            MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+            MW_CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(LevelStats), ctx->stream));
+            tr.mark("overflow");
+            continue;
+        }
+    }
+    first_miss = big;
     unsigned long long nt_mixed = 0;
     LevelStats hs{};
     MW_CK(cudaMemcpyAsync(flags_out, b.flags, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
@@ -1826,6 +1884,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     std::vector<double> sqv(3 * (size_t)n_levels);
     MW_CK(cudaMemcpyAsync(sqv.data(), b.sq, sizeof(double) * 3 * n_levels, cudaMemcpyDeviceToHost, st));
     if (auto s = check_err(ctx, "judged apply")) return s;
+    tr.mark("result");
     if (sq_levels) std::memcpy(sq_levels, sqv.data(), sizeof(double) * 3 * n_levels);
     *first_miss_out = first_miss == big ? -1 : first_miss;
     if (stats) {
@@ -1839,7 +1898,10 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
         cudaEventElapsedTime(&ms, ctx->ev1, ctx->ev2);
         stats->contract_ms = ms;
     }
-    if (transforms && first_miss == big) {
+    break;
+    }
+    cudaStream_t st = ctx->stream;
+    if (transforms && first_miss == 0x7fffffff) {
         // TopDown(add) and BottomUp over the judged tree: its parents are the refined nodes
         std::vector<std::vector<int>> levels(n_levels);
         for (int j = 0; j < n_levels; j++)
@@ -1872,6 +1934,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             MW_CK(cudaGetLastError());
             MW_CK(cudaStreamSynchronize(st));
         }
+        tr.mark("transforms");
     }
     return MWGPU_OK;
 }

@@ -148,8 +148,10 @@ void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, c
                          uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s);
 // real_only: reconstruct from the nearest real ancestor even where a GenNode
 // ancestor exists (GenNodes that are rewritten by the same launch)
+// GenNodes of the pending keys plist[0..n_pend) into slots gen_base + p
+// (fp32: FP32 products, the GenNodes of the mixed form)
 void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s,
-                      bool real_only = false);
+                      bool real_only = false, bool fp32 = false);
 void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
                           double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev = nullptr,

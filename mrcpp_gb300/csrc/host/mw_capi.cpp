@@ -8,6 +8,8 @@
 // iteration (ConvolutionCalculator::calcNodeVector) runs on the GPU.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 
@@ -29,6 +31,34 @@ struct mwh_oper {
 };
 
 namespace {
+
+// Phase timing of a host entry point when the environment sets MWGPU_TRACE
+// (every mark drains the device stream; one line to stderr per call).
+struct HostTrace {
+    mwgpu_ctx *ctx = nullptr;
+    const char *fn;
+    bool on;
+    std::chrono::steady_clock::time_point t0, last;
+    std::string line;
+    explicit HostTrace(const char *f) : fn(f), on(std::getenv("MWGPU_TRACE") != nullptr) {
+        if (on) t0 = last = std::chrono::steady_clock::now();
+    }
+    void mark(const std::string &phase) {
+        if (!on) return;
+        if (ctx) mwgpu_sync(ctx);
+        const auto now = std::chrono::steady_clock::now();
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), " %s=%.3f", phase.c_str(), std::chrono::duration<double, std::milli>(now - last).count());
+        line += buf;
+        last = now;
+    }
+    ~HostTrace() {
+        if (on)
+            std::fprintf(stderr, "[mwh] %s%s total=%.3f ms\n", fn, line.c_str(),
+                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
+};
+
 thread_local std::string g_err;
 std::mutex g_gpu_mu;
 mwgpu_ctx *g_ctx = nullptr;
@@ -116,6 +146,29 @@ mwgpu_oper *device_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwh_oper *
     g_oper_cache[{operp, prec}] = dop;
     return dop;
 }
+
+// Topology of a grid proposal: node index and first child only, children
+// appended 8 at a time in the order of Tree::createChildren (no coefficient
+// storage, unlike a Tree, whose nodes each carry 8 (k+1)^3 zeroed doubles).
+struct GridSketch {
+    struct Node {
+        int n;
+        int l[3];
+        int child0;
+    };
+    std::vector<Node> nodes;
+    // the roots of a fresh tree, in its order
+    explicit GridSketch(const Tree<3> &fresh) {
+        nodes.reserve(4 * fresh.nodes.size() + 64);
+        for (const auto &nd : fresh.nodes) nodes.push_back({nd.n, {nd.l[0], nd.l[1], nd.l[2]}, -1});
+    }
+    void createChildren(int i) {
+        const Node p = nodes[i];
+        nodes[i].child0 = (int)nodes.size();
+        for (int c = 0; c < Tree<3>::tDim; c++)
+            nodes.push_back({p.n + 1, {2 * p.l[0] + (c & 1), 2 * p.l[1] + ((c >> 1) & 1), 2 * p.l[2] + ((c >> 2) & 1)}, -1});
+    }
+};
 
 // State of one output tree inside apply: the TreeBuilder loop of
 // TreeBuilder.cpp:38-87 (sNorm from the first iteration, cumulative wNorm,
@@ -224,6 +277,8 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     fill_desc(mra, &md, filters.data());
 
     mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
+    HostTrace ht("apply");
+    ht.ctx = ctx;
     mwh_apply_stats acc{};
     unsigned long long l0 = 0, l1 = 0;
     mwgpu_launch_count(ctx, &l0);
@@ -243,6 +298,13 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
                 continue;
             }
             b.tree = outs[t]->t.get();
+            // room for the refinement without moving the coefficients on every
+            // growth step (untouched capacity costs no memory)
+            {
+                const size_t guess = b.tree->nodes.size() + 2 * inps[t]->t->nodes.size() + 4096;
+                b.tree->nodes.reserve(guess);
+                b.tree->coefs.reserve(guess * (size_t)b.tree->nCoefs);
+            }
             b.dinp = upload_input(ctx, md, *inps[t]->t, acc);
             b.dout = create_output(ctx, md, *b.tree, acc);
             b.synced = b.tree->nodes.size();
@@ -250,6 +312,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
             for (auto &lvl : b.tree->nodesByDepth(false))
                 for (int i : lvl) b.work.push_back(i);
         }
+        ht.mark("upload");
         std::vector<int> wtree, wnode;
         std::vector<double> sq(nt), nbuf;
         std::vector<mwgpu_tree *> dins(nt), douts(nt);
@@ -280,6 +343,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
                 ck(mwgpu_apply_level_batch(ctx, dop, nt, dins.data(), douts.data(), wtree.data(), wnode.data(), n, prec, sq.data(), nbuf.data(),
                                            &ls),
                    "apply level");
+            ht.mark("level" + std::to_string(acc.iterations));
             acc.h2d_bytes += (unsigned long long)n * (nt == 1 ? 4 : 8);
             acc.d2h_bytes += (unsigned long long)n * 8 * 8;
             for (int j = 0; j < n; j++) {
@@ -329,6 +393,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
             }
         }
         for (auto &b : bs) sync_new(ctx, b, acc);
+        ht.mark("split");
         auto t1 = std::chrono::steady_clock::now();
         if (nt == 1) {
             ck(mwgpu_transform(ctx, douts[0], MWGPU_TOPDOWN, 0), "TopDown transform");
@@ -337,6 +402,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
             ck(mwgpu_transform_batch(ctx, nt, douts.data(), MWGPU_TOPDOWN, 0), "TopDown transform");
             ck(mwgpu_transform_batch(ctx, nt, douts.data(), MWGPU_BOTTOMUP, 1), "BottomUp transform");
         }
+        ht.mark("transforms");
         int out_nodes = 0;
         for (auto &b : bs) {
             Tree<3> &out = *b.tree;
@@ -355,6 +421,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
             out.calcSquareNorm();
             out_nodes += (int)out.nodes.size();
         }
+        ht.mark("download");
         auto t2 = std::chrono::steady_clock::now();
         acc.transform_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
         acc.out_nodes = out_nodes;
@@ -721,6 +788,8 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         fill_desc(mra, &md, filters.data());
         mwgpu_oper *dop = device_operator(ctx, md, operp, prec);
         if (!mlp->dev) ck(mwgpu_mlp_create(ctx, mlp->params.data(), &mlp->dev), "network upload");
+        HostTrace ht("apply_learned");
+        ht.ctx = ctx;
         mwh_apply_stats acc{};
         unsigned long long l0 = 0, l1 = 0;
         mwgpu_launch_count(ctx, &l0);
@@ -728,11 +797,12 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         // The proposal, level by level.  `prop` holds the judged tree of the
         // levels before `first` (exact) and the proposed levels after it; its
         // node order is TreeBuilder's (levels, each in the order of the parents).
-        Tree<3> prop(mra);
+        GridSketch prop(out);
         std::vector<int> level_begin, flags;
         std::vector<double> norm_levels, norms;
         try {
             dinp = upload_input(ctx, md, inp, acc);
+            ht.mark("upload");
             const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
             const size_t max_nodes = std::max<size_t>(4096, 4 * inp.nodes.size());
             std::vector<int> idx;
@@ -768,7 +838,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     if (prop.nodes.size() + Tree<3>::tDim * refine.size() > max_nodes) break;
                     std::vector<int> next;
                     for (int i : refine) {
-                        prop.createChildren(i, false);
+                        prop.createChildren(i);
                         const int c0 = prop.nodes[i].child0;
                         for (int c = 0; c < Tree<3>::tDim; c++) next.push_back(c0 + c);
                     }
@@ -779,6 +849,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
             for (size_t i = 0; i < prop.nodes.size(); i++) roots.push_back((int)i);
             level_begin.push_back(0);
             propose(roots);
+            ht.mark("propose");
             ls.proposal_nodes = (int)prop.nodes.size();
             double state[3] = {0.0, 0.0, out.squareNorm};
             int first = 0;
@@ -806,6 +877,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     mwgpu_free_tree(ctx, dold);
                     dold = nullptr;
                 }
+                ht.mark("tree" + std::to_string(pass));
                 const int nlev = (int)level_begin.size() - 1;
                 flags.assign(prop.nodes.size(), 0);
                 norm_levels.assign(3 * (size_t)nlev, 0.0);
@@ -816,6 +888,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                                       norm_levels.data(), &st),
                    "judged apply");
                 ls.judged_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tj).count();
+                ht.mark("judged" + std::to_string(pass));
                 ls.host_round_trips += 1;
                 acc.node_terms += st.node_terms;
                 acc.components += st.components;
@@ -831,7 +904,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 // up to there is kept, all children of the refined nodes of that
                 // level are added, the network proposes below them, next pass
                 ls.fallback = 1;
-                Tree<3> next(mra);
+                GridSketch next(out);
                 std::vector<int> map(prop.nodes.size(), -1), nsrc;
                 for (size_t i = 0; i < next.nodes.size(); i++) {
                     map[i] = (int)i;
@@ -843,7 +916,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                     for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
                         if ((flags[i] & 3) != 3) continue;
                         const int oi = map[i];
-                        next.createChildren(oi, false);
+                        next.createChildren(oi);
                         const int c0 = next.nodes[oi].child0, p0 = prop.nodes[i].child0;
                         for (int c = 0; c < Tree<3>::tDim; c++) {
                             nsrc.push_back(j < miss && p0 >= 0 ? p0 + c : -1);
@@ -862,6 +935,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 state[2] = norm_levels[3 * miss + 2];
                 first = miss + 1;
                 propose(frontier);
+                ht.mark("propose" + std::to_string(pass + 1));
                 ls.proposal_nodes += (int)prop.nodes.size() - level_begin[first];
             }
         } catch (...) {
@@ -874,6 +948,12 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         std::vector<int> map(prop.nodes.size(), -1);
         for (size_t i = 0; i < out.nodes.size(); i++) map[i] = (int)i;
         const int nlev = (int)level_begin.size() - 1;
+        {
+            size_t n_keep = 0;
+            for (size_t i = 0; i < prop.nodes.size(); i++) n_keep += flags[i] & 1;
+            out.nodes.reserve(n_keep);
+            out.coefs.reserve(n_keep * (size_t)out.nCoefs);
+        }
         int kept = 0;
         for (int j = 0; j < nlev; j++)
             for (int i = level_begin[j]; i < level_begin[j + 1]; i++) {
@@ -886,6 +966,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
                 for (int c = 0; c < Tree<3>::tDim; c++) map[p0 + c] = c0 + c;
             }
         ls.kept_nodes = kept;
+        ht.mark("out_tree");
         // the kept nodes, gathered on the device in the output tree's order,
         // straight into its coefficient storage
         std::vector<int> src(out.nodes.size(), -1);
@@ -907,6 +988,7 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         mwgpu_free_tree(ctx, dinp);
         mwgpu_launch_count(ctx, &l1);
         acc.launches = l1 - l0;
+        ht.mark("download");
         for (size_t oi = 0; oi < src.size(); oi++) {
             double s2 = 0.0;
             for (int c = 0; c < 8; c++) {
