@@ -428,6 +428,9 @@ def main_batch(args, rank, world, local, pg):
     barrier(pg)
 
 
+REPEATS = 3
+
+
 def main_learned(args, rank, world, local, pg):
     import mrcpp_gb300 as mw
     from mrcpp_gb300.learned import train_grid as tg
@@ -450,14 +453,20 @@ def main_learned(args, rank, world, local, pg):
     plain_t, learned_t, nt_p, nt_l, it_p, it_l, rt_l, cont, same, diffs, contract, launches = [], [], 0, 0, [], [], [], 0, 0, [], 0.0, 0
     with ClockSampler(local) as cs:
         for f in fs:
-            g0 = mw.FunctionTree(mra)
-            t0 = time.perf_counter()
-            sp = mw.apply(PREC, g0, P, f, precision=mw.MIXED)
-            plain_t.append(time.perf_counter() - t0)
-            g1 = mw.FunctionTree(mra)
-            t0 = time.perf_counter()
-            sl = mw.apply_learned(PREC, g1, P, f, net, threshold=thr, full_levels=full, precision=mw.MIXED)
-            learned_t.append(time.perf_counter() - t0)
+            # each density REPEATS times, the two methods alternating; the
+            # median wall time of each (single host-timed applies are noisy)
+            tp, tl = [], []
+            for _ in range(REPEATS):
+                g0 = mw.FunctionTree(mra)
+                t0 = time.perf_counter()
+                sp = mw.apply(PREC, g0, P, f, precision=mw.MIXED)
+                tp.append(time.perf_counter() - t0)
+                g1 = mw.FunctionTree(mra)
+                t0 = time.perf_counter()
+                sl = mw.apply_learned(PREC, g1, P, f, net, threshold=thr, full_levels=full, precision=mw.MIXED)
+                tl.append(time.perf_counter() - t0)
+            plain_t.append(statistics.median(tp))
+            learned_t.append(statistics.median(tl))
             nt_p += sp["node_terms"]
             nt_l += sl["apply"]["node_terms"]
             it_p.append(sp["iterations"])
@@ -480,7 +489,8 @@ def main_learned(args, rank, world, local, pg):
                 "dtype": "f32 products, f64 accumulation", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "densities": len(fs), "threshold": thr, "full_levels": full,
                            "network": "mrcpp_gb300/data/grid_mlp_k7.npz",
-                           "step": "one adaptive apply of one density (host trees in and out)", "parallelism": "single"},
+                           "step": "one adaptive apply of one density (host trees in and out), median of %d" % REPEATS,
+                           "parallelism": "single"},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                         "note": "the adaptive apply is end to end by construction (host FunctionTrees)"},
                 "plain": {"value": nt_p / t_p, "unit": UNIT, "ms_per_step": 1e3 * t_p / len(fs), "iterations_mean": float(np.mean(it_p))},

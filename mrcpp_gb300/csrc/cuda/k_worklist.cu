@@ -209,21 +209,38 @@ __device__ __forceinline__ void term_mask(const DevOper &op, const TermRow &row,
 // n_pairs / n_work are the launch capacity; with np_dev / nw_dev the actual
 // counts come from the device (levels whose work list is made on the device),
 // and COUNT writes zero counts for the pairs in [*np_dev, n_pairs).
-template <bool FILL, int G>
+// lanes per pair: enough threads for the whole GPU (152 SMs x 2048) on small
+// levels, one lane per pair once the pairs alone fill it
+constexpr long long kPairThreads = 2 * 152LL * 2048;
+__host__ __device__ inline int pair_group(long long n_pairs) {
+    if (n_pairs * 32 <= kPairThreads) return 32;
+    if (n_pairs * 8 <= kPairThreads) return 8;
+    if (n_pairs * 4 <= kPairThreads) return 4;
+    return 1;
+}
+
+// GT > 0: GT lanes per pair; GT == 0: the group size follows the pair count
+// read on the device (levels whose work list is made on the device; the grid
+// then has at least kPairThreads threads, enough for any count's group)
+template <bool FILL, int GT>
 __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                                                const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts,
                                                const long long *item_off, WorkItem *items, long long items_cap, unsigned long long *ncomp,
                                                unsigned long long *nband, int *err, const long long *np_dev, const int *nw_dev) {
-    static_assert(G == 1 || G == 4 || G == 8 || G == 32, "lane group size");
+    static_assert(GT == 0 || GT == 1 || GT == 4 || GT == 8 || GT == 32, "lane group size");
     const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n_cap = n_pairs;
+    if (np_dev) n_pairs = *np_dev;
+    if (nw_dev) n_work = *nw_dev;
+    const int G = GT > 0 ? GT : pair_group(n_pairs);
     const long long p = gid / G;
     const int j = (int)(gid % G), lane = threadIdx.x & 31;
     int cnt = 0;
     unsigned long long comp = 0, band = 0;
-    const long long n_cap = n_pairs;
-    if (np_dev) n_pairs = *np_dev;
-    if (nw_dev) n_work = *nw_dev;
-    if (!FILL && j == 0 && p >= n_pairs && p < n_cap) counts[p] = 0;
+    if (!FILL && np_dev) {
+        // the capacity beyond the device count: zero counts, grid-stride
+        for (long long q = n_pairs + gid; q < n_cap; q += (long long)gridDim.x * blockDim.x) counts[q] = 0;
+    }
     PairCtx pc;
     bool ok = false;
     if (p < n_pairs) {
@@ -281,7 +298,7 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
         int n_round = pass ? 1 : 0;
         if (G > 1) {
             const unsigned b = __ballot_sync(0xffffffffu, pass);
-            const unsigned grp = G == 32 ? b : (b >> (lane & ~(G - 1))) & (unsigned)((1ull << G) - 1ull);
+            const unsigned grp = G == 32 ? b : (b >> (lane & ~(G - 1))) & (unsigned)((1ull << G) - 1ull);  // G: 4, 8 or 32
             pos = wpos + __popc(grp & ((1u << j) - 1u));
             n_round = __popc(grp);
         }
@@ -429,15 +446,6 @@ __global__ void k_chunk_fill(const long long *g_off, const long long *c_off, int
         if (c < cap) chunks[c] = make_int4(wi, (int)x, (int)min(e, x + per), 0);
 }
 
-// lanes per pair: enough threads for the whole GPU (152 SMs x 2048) on small
-// levels, one lane per pair once the pairs alone fill it
-int pair_group(long long n_pairs) {
-    constexpr long long kThreads = 152LL * 2048;
-    if (n_pairs * 32 <= 2 * kThreads) return 32;
-    if (n_pairs * 8 <= 2 * kThreads) return 8;
-    if (n_pairs * 4 <= 2 * kThreads) return 4;
-    return 1;
-}
 
 }  // namespace
 
@@ -449,6 +457,16 @@ void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, c
         kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts, nullptr,
                                                                   nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
     };
+    auto kern_dev_false = [&](long long thr) {
+        k_pairs<false, 0><<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts,
+                                                                       nullptr, nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
+    };
+    if (np_dev) {
+        // group size from the device count: at least kPairThreads threads
+        const long long thr = std::max(n_pairs * pair_group(n_pairs), kPairThreads);
+        kern_dev_false(thr);
+        return;
+    }
     switch (pair_group(n_pairs)) {
         case 32: go(k_pairs<false, 32>, 32); break;
         case 8: go(k_pairs<false, 8>, 8); break;
@@ -465,6 +483,16 @@ void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, co
         kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr, item_off,
                                                                   items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
     };
+    auto kern_dev_true = [&](long long thr) {
+        k_pairs<true, 0><<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr,
+                                                                      item_off, items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
+    };
+    if (np_dev) {
+        // group size from the device count: at least kPairThreads threads
+        const long long thr = std::max(n_pairs * pair_group(n_pairs), kPairThreads);
+        kern_dev_true(thr);
+        return;
+    }
     switch (pair_group(n_pairs)) {
         case 32: go(k_pairs<true, 32>, 32); break;
         case 8: go(k_pairs<true, 8>, 8); break;

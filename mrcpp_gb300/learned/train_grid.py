@@ -177,14 +177,53 @@ def main():
     ap.add_argument("--full-levels", type=int, default=1, help="proposal levels refined without the network")
     ap.add_argument("--evaluate", default=None, help="only evaluate this trained network (npz) on the held-out densities")
     ap.add_argument("--thresholds", default=None, help="with --evaluate: comma-separated thresholds to compare")
+    ap.add_argument("--on", default="held", choices=("held", "validation"),
+                    help="with --evaluate: the held-out densities, or the validation part of the training seeds (for tuning)")
+    ap.add_argument("--tune", default=None,
+                    help="re-tune threshold and full levels of this trained network (npz) by wall time on the validation densities "
+                         "(--thresholds x --full-levels-grid) and write them into it")
+    ap.add_argument("--full-levels-grid", default="1,2,3")
     a = ap.parse_args()
+    if a.tune:
+        import mrcpp_gb300 as mw
+        with np.load(a.tune) as z:
+            saved = {k: z[k] for k in z.files}
+        n_val = max(1, a.train // 10)
+        seeds = list(range(TRAIN_SEED0 + a.train - n_val, TRAIN_SEED0 + a.train))[:a.held]
+        thrs = [float(x) for x in (a.thresholds or "0.1,0.2,0.3,0.5").split(",")]
+        table = []
+        # one untimed pass first: operator and network uploads, device pools
+        evaluate(saved["params"], thrs[0], seeds[:2], mw.MIXED, 1)
+        for fl in [int(x) for x in a.full_levels_grid.split(",")]:
+            for t in thrs:
+                rows = evaluate(saved["params"], t, seeds, mw.MIXED, fl)
+                table.append({"threshold": t, "full_levels": fl, "n": len(rows),
+                              "plain_ms": float(np.median([r["plain_ms"] for r in rows])),
+                              "learned_ms": float(np.median([r["learned_ms"] for r in rows])),
+                              "passes_mean": float(np.mean([r["learned_iterations"] for r in rows])),
+                              "same_topology": int(sum(r["same_topology"] for r in rows))})
+        ok = [r for r in table if r["same_topology"] == r["n"]]
+        best = min(ok, key=lambda r: r["learned_ms"] / r["plain_ms"])
+        summ = json.loads(str(saved["summary"]))
+        summ["usage_tuning"] = {"densities": "validation", "per_density": "median wall ms", "table": table,
+                                "chosen": {"threshold": best["threshold"], "full_levels": best["full_levels"]}}
+        saved["summary"] = np.array(json.dumps(summ))
+        saved["threshold"] = np.float64(best["threshold"])
+        saved["full_levels"] = np.int32(best["full_levels"])
+        np.savez(a.tune, **saved)
+        print(json.dumps(summ["usage_tuning"]))
+        return
     if a.evaluate:
         import mrcpp_gb300 as mw
         with np.load(a.evaluate) as z:
             params = z["params"]
             thr0 = float(z["threshold"])
         thrs = [float(x) for x in a.thresholds.split(",")] if a.thresholds else [thr0]
-        seeds = list(range(HELD_SEED0, HELD_SEED0 + a.held))
+        if a.on == "held":
+            seeds = list(range(HELD_SEED0, HELD_SEED0 + a.held))
+        else:
+            n_val = max(1, a.train // 10)
+            seeds = list(range(TRAIN_SEED0 + a.train - n_val, TRAIN_SEED0 + a.train))[:a.held]
         out = []
         for t in thrs:
             rows = evaluate(params, t, seeds, mw.MIXED, a.full_levels)
@@ -218,7 +257,7 @@ def main():
     # part of the held-out set is kept
     mins = np.array(mins)
     cands = sorted({float(np.quantile(mins, 1.0 - a.success)) * 0.999, float(np.quantile(mins, 0.1)) * 0.999, 0.5, 0.7, 0.85})
-    probe = list(range(HELD_SEED0, HELD_SEED0 + min(a.held, 40)))
+    probe = [r[0] for r in va][:40]  # tuned on validation densities, reported on the held-out ones
     tune = []
     for c in cands:
         r = evaluate(params, c, probe, mw.MIXED, a.full_levels)
