@@ -134,22 +134,52 @@ __device__ __noinline__ bool exact_pass(const double *onorms, int base, int t0, 
 // rate on this part, so the loop works on FP32 copies of the norms; the
 // component loops are unrolled so that every table index is a constant.
 struct PairNorms {
-    float fnf[8];        // f component norms rounded to FP32
-    unsigned fnz;        // components with norm >= MachineZero
-    float fmx_up;        // FP32 upper bound of the largest f norm
-    const double *fn;    // the FP64 norms
+    float fnf[8];               // f component norms rounded to FP32
+    unsigned fnz;               // components with norm >= MachineZero
+    unsigned long long fmask;   // (ft, gt) bits with ft in fnz, less (0, 0) below the roots
+    float fmx_up;               // FP32 upper bound of the largest f norm
+    const double *fn;           // the FP64 norms
 };
+
+// (ft, gt) bits (bit ft * 8 + gt) whose operator component in direction D is
+// I = 2 gt_D + ft_D
+__host__ __device__ constexpr unsigned long long comp_mask(int d, int i) {
+    unsigned long long m = 0ull;
+    for (int ft = 0; ft < 8; ft++)
+        for (int gt = 0; gt < 8; gt++)
+            if (2 * ((gt >> d) & 1) + ((ft >> d) & 1) == i) m |= 1ull << (ft * 8 + gt);
+    return m;
+}
+template <int D> struct DirMasks {
+    static constexpr unsigned long long m0 = comp_mask(D, 0), m1 = comp_mask(D, 1), m2 = comp_mask(D, 2), m3 = comp_mask(D, 3);
+};
+// the (ft, gt) bits whose direction-D component is in the band (4-bit mask)
+template <int D> __device__ __forceinline__ unsigned long long dir_bits(unsigned m) {
+    return ((m & 1u) ? DirMasks<D>::m0 : 0ull) | ((m & 2u) ? DirMasks<D>::m1 : 0ull) | ((m & 4u) ? DirMasks<D>::m2 : 0ull) |
+           ((m & 8u) ? DirMasks<D>::m3 : 0ull);
+}
 
 __device__ __forceinline__ void term_mask(const DevOper &op, const TermRow &row, const PairCtx &pc, const PairNorms &pn, bool screen, bool fp32,
                                           float thr_hi, float thr_lo, double gthr, unsigned long long &mask, unsigned long long &smask,
                                           unsigned (&inm)[3]) {
     mask = smask = 0ull;
     inm[0] = inm[1] = inm[2] = 0u;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) inm[d] |= (abs(pc.tl[d]) <= row.wd[c] ? 1u : 0u) << c;
+    // the structural set: every direction's component in its band, f component present
+    smask = dir_bits<0>(inm[0]) & dir_bits<1>(inm[1]) & dir_bits<2>(inm[2]) & pn.fmask;
+    if (!screen) {
+        mask = smask;
+        return;
+    }
+    if (smask == 0ull) return;
     const int L0 = row.L0, off = row.off;
     int fac[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) fac[c] = row.wd[c] < 0 ? 1 : 2 * row.wd[c] + 1;
-    if (screen && fp32) {
+    if (fp32) {
         // bound of every component product of this term: the largest operator
         // norm per direction, band size and f norm; clear of the threshold by
         // far more than the FP32 rounding -> nothing passes
@@ -159,32 +189,22 @@ __device__ __forceinline__ void term_mask(const DevOper &op, const TermRow &row,
                             ((float)(fm * fm * fm * 64) * pn.fmx_up);
         if (bound < thr_lo) return;
     }
-    // per direction: in-band mask of the 4 operator components and, for the
-    // estimate, FP32 norm x band-size factor (0 outside the band)
+    // per direction, for the estimate: FP32 norm x band-size factor (0 outside the band)
     float an[3][4];
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const bool in = abs(pc.tl[d]) <= row.wd[c];
-            inm[d] |= (in ? 1u : 0u) << c;
-            an[d][c] = (screen && fp32 && in) ? op.norms32[(size_t)(off + pc.tl[d] + L0) * 4 + c] * (float)fac[c] : 0.0f;
-        }
+        for (int c = 0; c < 4; c++)
+            an[d][c] = (fp32 && ((inm[d] >> c) & 1u)) ? op.norms32[(size_t)(off + pc.tl[d] + L0) * 4 + c] * (float)fac[c] : 0.0f;
 #pragma unroll
     for (int ft = 0; ft < 8; ft++) {
-        if (!((pn.fnz >> ft) & 1u)) continue;
+        if (((smask >> (8 * ft)) & 0xffull) == 0ull) continue;
         const float ff = 64.0f * pn.fnf[ft];
 #pragma unroll
         for (int gt = 0; gt < 8; gt++) {
-            if (ft == 0 && gt == 0 && pc.depth != 0) continue;
-            const int i0 = 2 * (gt & 1) + (ft & 1), i1 = 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1), i2 = 2 * (gt >> 2) + (ft >> 2);
-            if (!((inm[0] >> i0) & (inm[1] >> i1) & (inm[2] >> i2) & 1u)) continue;
             const unsigned long long bit = 1ull << (ft * 8 + gt);
-            smask |= bit;
-            if (!screen) {
-                mask |= bit;
-                continue;
-            }
+            if (!(smask & bit)) continue;
+            const int i0 = 2 * (gt & 1) + (ft & 1), i1 = 2 * ((gt >> 1) & 1) + ((ft >> 1) & 1), i2 = 2 * (gt >> 2) + (ft >> 2);
             if (fp32) {
                 const float est = (an[0][i0] * an[1][i1]) * (an[2][i2] * ff);
                 if (est > thr_hi) {
@@ -249,6 +269,7 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
     }
     PairNorms pn;
     pn.fnz = 0u;
+    pn.fmask = 0ull;
     pn.fmx_up = 0.f;
     pn.fn = nullptr;
     double gthr = 0.0;
@@ -269,6 +290,10 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
             }
         }
         pn.fmx_up = nextafterf((float)fmx, INFINITY);
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            if ((pn.fnz >> c) & 1u) pn.fmask |= 0xffull << (8 * c);
+        if (pc.depth != 0) pn.fmask &= ~1ull;  // the (s, s) block only at the roots
         maxdl = max(abs(pc.tl[0]), max(abs(pc.tl[1]), abs(pc.tl[2])));
     }
     const bool screen = !(gthr < 0.0);
@@ -276,7 +301,22 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
     const float thr_hi = (float)(gthr * (1.0 + 1.0 / 4096.0)), thr_lo = (float)(gthr * (1.0 - 1.0 / 4096.0));
     const int T = op.n_terms;
     long long wpos = (FILL && ok) ? item_off[p] : 0;
-    const bool live = ok && pn.fnz != 0u;
+    bool live = ok && pn.fnz != 0u;
+    // FILL with the counts of the COUNT pass: pairs without items are done,
+    // the others stop after their last item
+    const int target = (FILL && counts && live) ? counts[p] : -1;
+    if (FILL && counts && target == 0) live = false;
+    if (live && screen && fp32) {
+        // the largest per-term bound of this cell over all terms: below the
+        // threshold (with room for the FP32 rounding of the per-term bounds,
+        // < 2^-21 relative) no term can pass
+        const int po = op.pair_bound_off[pc.depth], W = op.band_max[pc.depth];
+        if (po >= 0 && maxdl <= W) {
+            const int nw = 2 * W + 1;
+            const float pbv = op.pair_bound[po + ((pc.tl[0] + W) * nw + (pc.tl[1] + W)) * nw + (pc.tl[2] + W)];
+            if (pbv * (64.0f * pn.fmx_up) * (1.0f + 1.0f / 1048576.0f) < thr_lo) live = false;
+        }
+    }
     for (int base = 0; base < T; base += G) {
         const int ti = base + j;
         bool active = live && ti < T;
@@ -328,6 +368,7 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
         }
         wpos += n_round;
         cnt += n_round;
+        if (FILL && target > 0 && cnt >= target) live = false;
     }
     if (!FILL && j == 0 && p < n_pairs) counts[p] = cnt;
     if (!FILL) {
@@ -476,15 +517,16 @@ void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, c
 }
 
 void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
-                       const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const long long *item_off, WorkItem *items,
-                       long long items_cap, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
+                       const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const int *counts_in, const long long *item_off,
+                       WorkItem *items, long long items_cap, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
     if (n_pairs <= 0) return;
+    int *counts = const_cast<int *>(counts_in);  // read only in FILL
     auto go = [&](auto kern, int g) {
-        kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr, item_off,
+        kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts, item_off,
                                                                   items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
     };
     auto kern_dev_true = [&](long long thr) {
-        k_pairs<true, 0><<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, nullptr,
+        k_pairs<true, 0><<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts,
                                                                       item_off, items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
     };
     if (np_dev) {

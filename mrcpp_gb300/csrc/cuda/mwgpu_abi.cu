@@ -294,7 +294,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
         ctx->items_cap = std::max(total, 2 * ctx->items_cap);
         if (auto s = dev_alloc(ctx, &ctx->d_items, (size_t)ctx->items_cap)) return s;
     }
-    launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_item_off,
+    launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_pcounts, ctx->d_item_off,
                       ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream);
     ctx->launches++;
     // chunks of about the same number of items, several waves of CTAs
@@ -843,6 +843,39 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
             for (int c = 0; c < 4; c++) r.wd[c] = bw[((size_t)i * rows + dd) * 5 + c];
         }
     TermRow *p_trows;
+    // pair screening table: per depth and band cell the largest per-term bound
+    std::vector<int> pb_off(rows, -1);
+    std::vector<float> pb;
+    for (int dd = 0; dd <= maxDepth && dd < rows; dd++) {
+        const int W = band_max[dd];
+        if (W < 0) continue;
+        const int nw = 2 * W + 1;
+        const size_t cells = (size_t)nw * nw * nw;
+        if (pb.size() + cells > ((size_t)1 << 26)) break;
+        std::vector<double> tab(cells, 0.0), v(nw);
+        for (int t = 0; t < T; t++) {
+            const int off = dep_off[(size_t)t * rows + dd], L0 = dep_L[(size_t)t * rows + dd];
+            const int *w = &bw[((size_t)t * rows + dd) * 5];
+            if (off < 0 || w[4] < 0) continue;
+            int fm = 1;
+            for (int c = 0; c < 4; c++) fm = std::max(fm, w[c] < 0 ? 1 : 2 * w[c] + 1);
+            const double f3 = (double)fm * fm * fm;
+            for (int l = -W; l <= W; l++) v[l + W] = (std::abs(l) <= L0 && std::abs(l) <= w[4]) ? (double)nmax[off + l + L0] : 0.0;
+            for (int a = 0; a < nw; a++) {
+                if (v[a] == 0.0) continue;
+                for (int b = 0; b < nw; b++) {
+                    const double ab = v[a] * v[b] * f3;
+                    if (ab == 0.0) continue;
+                    double *row = &tab[((size_t)a * nw + b) * nw];
+                    for (int c = 0; c < nw; c++) row[c] = std::max(row[c], ab * v[c]);
+                }
+            }
+        }
+        pb_off[dd] = (int)pb.size();
+        for (double x : tab) pb.push_back(x > 0.0 ? std::nextafter((float)(x * (1.0 + 1e-14)), INFINITY) : 0.0f);
+    }
+    float *p_pb;
+    int *p_pboff;
     std::vector<float> nrm32(node * 4);
     for (size_t q = 0; q < nrm32.size(); q++) nrm32[q] = (float)d->norms[q];
     float *p_blk32, *p_nmax, *p_nrm32;
@@ -851,7 +884,8 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         (s = up(&p_bw, bw.data(), bw.size())) || (s = up(&p_bsz, bsz.data(), bsz.size())) || (s = up(&p_bm, band_max.data(), band_max.size())) ||
         (s = up(&p_ord, order.data(), order.size())) || (s = up(&p_blk, d->blocks, node * 4 * K2)) || (s = up(&p_nrm, d->norms, node * 4)) ||
         (s = up(&p_blk32, blk32.data(), blk32.size())) || (s = up(&p_nmax, nmax.data(), nmax.size())) ||
-        (s = up(&p_nrm32, nrm32.data(), nrm32.size())) || (s = up(&p_trows, trows.data(), trows.size()))) {
+        (s = up(&p_nrm32, nrm32.data(), nrm32.size())) || (s = up(&p_trows, trows.data(), trows.size())) ||
+        (s = up(&p_pb, pb.data(), pb.size())) || (s = up(&p_pboff, pb_off.data(), pb_off.size()))) {
         for (void *p : o->allocs) cudaFree(p);
         pool_free(ctx, o->d_filt);
         delete o;
@@ -874,6 +908,8 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.norm_max = p_nmax;
     o->op.norms32 = p_nrm32;
     o->op.term_rows = p_trows;
+    o->op.pair_bound = p_pb;
+    o->op.pair_bound_off = p_pboff;
     *out = o;
     return MWGPU_OK;
 }
@@ -1315,8 +1351,8 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
                            &dst->components, &dst->band_nodes, pl->d_err, st);
         launch_scan(pl->d_pcounts, pl->d_item_off, pl->np, pl->d_scan, pl->d_scan + (pl->scan_n - 1), st);
         launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st);
-        launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_item_off,
-                          pl->d_items, pl->items_cap, pl->d_err, st);
+        launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
+                          pl->d_item_off, pl->d_items, pl->items_cap, pl->d_err, st);
         ctx->launches += 6;
         plan_contract(ctx, pl, pl->per, true);
     } else {
@@ -1842,7 +1878,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             launch_scan(b.ccnt, b.coff, nl, b.cscan, b.cscan + (scan_blocks(max_level + 1) + 1), st);
             const int ccap = (int)((long long)nl + kChunkTarget + 1);
             launch_chunk_fill(b.goff, b.coff, nl, lvl_per[j], b.chunks, b.chunk_begin, ccap, b.nchunks, ctx->d_err, st, b.nwork);
-            launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.item_off, b.items,
+            launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.pcounts, b.item_off, b.items,
                               lvl_items[j], ctx->d_err, st, np_dev, b.nwork);
             MW_CK(cudaMemsetAsync(b.counter, 0, sizeof(int), st));
             launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,

@@ -58,6 +58,11 @@ struct DevOper {
     const float *norm_max;      // [nodes] upper bound of the 4 component norms (FP32, rounded up)
     const float *norms32;       // [nodes * 4] norms rounded to FP32 (screening estimates)
     const TermRow *term_rows;   // [max_rows * T] term_order with the per-term tables of each depth
+    // per depth d with band_max[d] = W >= 0: for every cell (a, b, c) in
+    // [-W, W]^3 (a slowest) the largest per-term screening bound over the terms
+    // (prod_d norm_max(l_d) * fm^3, FP32 rounded up); pair_bound_off[d] = -1: none
+    const float *pair_bound;
+    const int *pair_bound_off;  // [max_rows]
 };
 
 struct DevTree {
@@ -160,9 +165,11 @@ bool mixed_supported(int K);
 void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                         const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts, unsigned long long *ncomp,
                         unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
+// FILL: counts are the COUNT pass's per-pair item counts (pairs without items
+// are skipped; may be null)
 void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
-                       const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const long long *item_off, WorkItem *items,
-                       long long items_cap, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
+                       const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const int *counts, const long long *item_off,
+                       WorkItem *items, long long items_cap, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
 // chunking of the work list on the device (graph-capturable levels); per <= 0:
 // the chunk length follows from the item count on the device (kChunkTarget)
 void launch_chunk_count(const long long *g_off, int n_work, long long per, int *counts, cudaStream_t s, const int *nw_dev = nullptr);
