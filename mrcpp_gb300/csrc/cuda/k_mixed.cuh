@@ -160,10 +160,13 @@ __device__ __forceinline__ unsigned to_tf32(float x) {
     return r;
 }
 
-// x = hi + lo with hi, lo TF32 (22 significant bits together)
+// x = hi + lo, hi = x rounded to TF32 and lo = x - hi exactly (|lo| <= 2^-11 |x|).
+// lo goes to the tensor core as an FP32 bit pattern: its use as a TF32
+// operand costs at most 2^-11 |lo| <= 2^-22 |x|, the accuracy of a second
+// rounding, without the second conversion.
 __device__ __forceinline__ void split_tf32(float x, unsigned &hi, unsigned &lo) {
     hi = to_tf32(x);
-    lo = to_tf32(x - __uint_as_float(hi));
+    lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
 __device__ __forceinline__ void mma_tf32(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3, unsigned b0, unsigned b1) {
