@@ -18,6 +18,8 @@ namespace mwgpu {
 
 namespace {
 
+constexpr int kTransformThreads = 1024;
+
 // out[c + K2*j] (+)= sum_i in[i + K*c] * F[i + K*j]
 // (consecutive threads take consecutive j of one row c: the row is a broadcast
 // read and the filter columns hit distinct banks)
@@ -306,29 +308,63 @@ __device__ __forceinline__ void load_filters32(float *F, const DevMRA &m, int op
     for (int e = tid; e < n; e += nthr) F[e] = (float)src[e];
 }
 
-__global__ void k_mw_down32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n, bool overwrite) {
+// One 1D filter stage over the 8 blocks of a node, both inputs of an output in
+// one pass: out[gt] = in[gt & ~m] F[2 b] + in[gt | m] F[2 b + 1], m = 1 << d,
+// b = bit d of gt (the sums of fapply<false> then fapply<true>, bit for bit).
+// All threads of the block share the 8 (k+1)^3 outputs.
+__device__ __forceinline__ void fstage8(float *out, const float *in, const float *F, int d, int K, int tid, int nthr) {
+    const int K2 = K * K, K3 = K2 * K, m = 1 << d;
+    for (int e = tid; e < 8 * K3; e += nthr) {
+        const int gt = e / K3, r = e - gt * K3, c = r / K, j = r - c * K;
+        const int b = (gt >> d) & 1;
+        const float *a0 = in + (size_t)(gt & ~m) * K3 + K * c, *a1 = in + (size_t)(gt | m) * K3 + K * c;
+        const float *f0 = F + (2 * b) * K2 + K * j, *f1 = F + (2 * b + 1) * K2 + K * j;
+        float s0 = 0.f, s1 = 0.f;
+        for (int i = 0; i < K; i++) {
+            s0 = fmaf(a0[i], f0[i], s0);
+            s1 = fmaf(a1[i], f1[i], s1);
+        }
+        out[(size_t)gt * K3 + c + K2 * j] = s0 + s1;
+    }
+}
+
+// out[q] = in[2q] F0 + in[2q+1] F1 for q < nout (one filter direction applied
+// to nout pairs of blocks, both inputs of an output in one pass)
+__device__ __forceinline__ void fpairs(float *out, const float *in, int nout, const float *F0, const float *F1, int K, int tid, int nthr) {
+    const int K2 = K * K, K3 = K2 * K;
+    for (int e = tid; e < nout * K3; e += nthr) {
+        const int q = e / K3, r = e - q * K3, c = r / K, j = r - c * K;
+        const float *a0 = in + (size_t)(2 * q) * K3 + K * c, *a1 = a0 + K3;
+        const float *f0 = F0 + K * j, *f1 = F1 + K * j;
+        float s0 = 0.f, s1 = 0.f;
+        for (int i = 0; i < K; i++) {
+            s0 = fmaf(a0[i], f0[i], s0);
+            s1 = fmaf(a1[i], f1[i], s1);
+        }
+        out[(size_t)q * K3 + c + K2 * j] = s0 + s1;
+    }
+}
+
+// (one CTA of kTransformThreads per parent: the levels of a tree are short,
+// so the latency of one parent is the launch's time)
+__global__ void __launch_bounds__(kTransformThreads) k_mw_down32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents,
+                                                                int n, bool overwrite) {
     extern __shared__ float sm32[];
     const DevTree t = ptree ? ts[ptree[blockIdx.x]] : t0;
-    const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
-    float *pin = sm32, *t1 = pin + 8 * K3, *t2 = t1 + 8 * K3, *F = t2 + 8 * K3;
+    const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    float *t1 = sm32, *t2 = t1 + 8 * K3, *F = t2 + 8 * K3;
     const int p = parents[blockIdx.x];
     const int c0 = t.child0[p];
     if (c0 < 0) return;
     const double *in = t.coefs + (size_t)p * 8 * K3;
-    for (int e = tid; e < 8 * K3; e += nthr) pin[e] = (float)in[e];
+    for (int e = tid; e < 8 * K3; e += nthr) t2[e] = (float)in[e];
     load_filters32(F, m, 1, tid, nthr);
     __syncthreads();
-    for (int gt = 0; gt < 8; gt++) fapply<false>(t1 + gt * K3, pin + (gt & ~1) * K3, F + (2 * (gt & 1) + 0) * K2, K, tid, nthr);
+    fstage8(t1, t2, F, 0, K, tid, nthr);
     __syncthreads();
-    for (int gt = 0; gt < 8; gt++) fapply<true>(t1 + gt * K3, pin + (gt | 1) * K3, F + (2 * (gt & 1) + 1) * K2, K, tid, nthr);
+    fstage8(t2, t1, F, 1, K, tid, nthr);
     __syncthreads();
-    for (int gt = 0; gt < 8; gt++) fapply<false>(t2 + gt * K3, t1 + (gt & ~2) * K3, F + (2 * ((gt >> 1) & 1) + 0) * K2, K, tid, nthr);
-    __syncthreads();
-    for (int gt = 0; gt < 8; gt++) fapply<true>(t2 + gt * K3, t1 + (gt | 2) * K3, F + (2 * ((gt >> 1) & 1) + 1) * K2, K, tid, nthr);
-    __syncthreads();
-    for (int gt = 0; gt < 8; gt++) fapply<false>(t1 + gt * K3, t2 + (gt & ~4) * K3, F + (2 * ((gt >> 2) & 1) + 0) * K2, K, tid, nthr);
-    __syncthreads();
-    for (int gt = 0; gt < 8; gt++) fapply<true>(t1 + gt * K3, t2 + (gt | 4) * K3, F + (2 * ((gt >> 2) & 1) + 1) * K2, K, tid, nthr);
+    fstage8(t1, t2, F, 2, K, tid, nthr);
     __syncthreads();
     // child gt receives the scaling block t1[gt] (its wavelet blocks are untouched: only the scaling part is passed down)
     for (int e = tid; e < 8 * K3; e += nthr) {
@@ -344,9 +380,9 @@ __global__ void k_mw_down32(DevMRA m, DevTree t0, const DevTree *ts, const int *
         }
     }
     __syncthreads();
-    // only the scaling component of a child changed: warp w recomputes the
+    // only the scaling component of a child changed: warp w < 8 recomputes the
     // scaling norm of child w (the wavelet norms stay, or are 0 when overwritten)
-    {
+    if (tid < 256) {
         const int w = tid >> 5, lane = tid & 31;
         const double *cc = t.coefs + (size_t)(c0 + w) * 8 * K3;
         double s = 0.0;
@@ -358,10 +394,11 @@ __global__ void k_mw_down32(DevMRA m, DevTree t0, const DevTree *ts, const int *
     }
 }
 
-__global__ void k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents, int n) {
+__global__ void __launch_bounds__(kTransformThreads) k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *ptree, const int *parents,
+                                                              int n) {
     extern __shared__ float sm32[];
     const DevTree t = ptree ? ts[ptree[blockIdx.x]] : t0;
-    const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
     float *t1 = sm32, *t2 = t1 + 8 * K3, *F = t2 + 8 * K3;
     const int p = parents[blockIdx.x];
     const int c0 = t.child0[p];
@@ -369,19 +406,16 @@ __global__ void k_mw_up32(DevMRA m, DevTree t0, const DevTree *ts, const int *pt
     for (int e = tid; e < 8 * K3; e += nthr) t1[e] = (float)t.coefs[(size_t)(c0 + e / K3) * 8 * K3 + e % K3];
     load_filters32(F, m, 0, tid, nthr);
     __syncthreads();
-    float *bufs[2] = {t1, t2};
-    for (int d = 0; d < 3; d++) {
-        float *inb = bufs[d & 1], *outb = bufs[(d + 1) & 1];
-        const int mask = 1 << d;
-        for (int gt = 0; gt < 8; gt++) fapply<false>(outb + gt * K3, inb + (gt & ~mask) * K3, F + (2 * ((gt >> d) & 1) + 0) * K2, K, tid, nthr);
-        __syncthreads();
-        for (int gt = 0; gt < 8; gt++) fapply<true>(outb + gt * K3, inb + (gt | mask) * K3, F + (2 * ((gt >> d) & 1) + 1) * K2, K, tid, nthr);
-        __syncthreads();
-    }
+    fstage8(t2, t1, F, 0, K, tid, nthr);
+    __syncthreads();
+    fstage8(t1, t2, F, 1, K, tid, nthr);
+    __syncthreads();
+    fstage8(t2, t1, F, 2, K, tid, nthr);
+    __syncthreads();
     double *pc = t.coefs + (size_t)p * 8 * K3;
     for (int e = tid; e < 8 * K3; e += nthr) pc[e] = (double)t2[e];
     __syncthreads();
-    block_norms8(pc, K3, t.norms + (size_t)p * 8, tid);
+    if (tid < 256) block_norms8(pc, K3, t.norms + (size_t)p * 8, tid);
 }
 
 // GenNodes of the mixed form: the path reconstruction of k_gen_nodes with FP32
@@ -427,18 +461,14 @@ __global__ void k_gen_nodes32(DevMRA m, DevTree f, const uint64_t *plist, int n_
         const int sh = n - an - 1;
         const int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
         if (anc < f.cap_real) {
+            // from the real ancestor's 8 components: x, y, z with both inputs of
+            // an output in one pass (the sums of fapply<false> then fapply<true>)
             const float *in = f.coefs32 + (size_t)anc * 8 * K3;
-            for (int q = 0; q < 4; q++) fapply<false>(b0 + q * K3, in + (size_t)(2 * q) * K3, F + (2 * c0 + 0) * K2, K, tid, nthr);
+            fpairs(b0, in, 4, F + (2 * c0) * K2, F + (2 * c0 + 1) * K2, K, tid, nthr);
             __syncthreads();
-            for (int q = 0; q < 4; q++) fapply<true>(b0 + q * K3, in + (size_t)(2 * q + 1) * K3, F + (2 * c0 + 1) * K2, K, tid, nthr);
+            fpairs(b1, b0, 2, F + (2 * c1) * K2, F + (2 * c1 + 1) * K2, K, tid, nthr);
             __syncthreads();
-            for (int b2 = 0; b2 < 2; b2++) fapply<false>(b1 + b2 * K3, b0 + (0 + 2 * b2) * K3, F + (2 * c1 + 0) * K2, K, tid, nthr);
-            __syncthreads();
-            for (int b2 = 0; b2 < 2; b2++) fapply<true>(b1 + b2 * K3, b0 + (1 + 2 * b2) * K3, F + (2 * c1 + 1) * K2, K, tid, nthr);
-            __syncthreads();
-            fapply<false>(b0, b1, F + (2 * c2 + 0) * K2, K, tid, nthr);
-            __syncthreads();
-            fapply<true>(b0, b1 + K3, F + (2 * c2 + 1) * K2, K, tid, nthr);
+            fpairs(b0, b1, 1, F + (2 * c2) * K2, F + (2 * c2 + 1) * K2, K, tid, nthr);
             __syncthreads();
         } else {
             const float *in = f.gcoefs32 + (size_t)(anc - f.cap_real) * K3;
@@ -548,7 +578,7 @@ void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_p
     if (fp32) {
         const size_t smem = sizeof(float) * (8 * (size_t)m.kp1_d + 4 * m.K * m.K);
         if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_nodes32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_gen_nodes32<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
+        k_gen_nodes32<<<n_pend, 256, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
         return;
     }
     size_t smem = sizeof(double) * 8 * m.kp1_d;
@@ -570,9 +600,9 @@ void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *pt
                     bool fp32) {
     if (n <= 0) return;
     if (fp32) {
-        const size_t sm = sizeof(float) * (24 * (size_t)m.kp1_d + 4 * m.K * m.K);
+        const size_t sm = sizeof(float) * (16 * (size_t)m.kp1_d + 4 * m.K * m.K);
         if (sm > 48 * 1024) cudaFuncSetAttribute(k_mw_down32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_mw_down32<<<n, 256, sm, s>>>(m, t, ts, ptree, parents, n, overwrite);
+        k_mw_down32<<<n, kTransformThreads, sm, s>>>(m, t, ts, ptree, parents, n, overwrite);
         return;
     }
     size_t smem = sizeof(double) * 16 * m.kp1_d;
@@ -585,7 +615,7 @@ void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptre
     if (fp32) {
         const size_t sm = sizeof(float) * (16 * (size_t)m.kp1_d + 4 * m.K * m.K);
         if (sm > 48 * 1024) cudaFuncSetAttribute(k_mw_up32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k_mw_up32<<<n, 256, sm, s>>>(m, t, ts, ptree, parents, n);
+        k_mw_up32<<<n, kTransformThreads, sm, s>>>(m, t, ts, ptree, parents, n);
         return;
     }
     size_t smem = sizeof(double) * 16 * m.kp1_d;
