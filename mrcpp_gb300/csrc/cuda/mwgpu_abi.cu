@@ -339,6 +339,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
 
 mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *d, bool input, mwgpu_tree **out) {
     MW_ARG(out && d && d->n_nodes > 0 && d->idx && d->child0, "invalid tree descriptor");
+    PhaseTrace trace(ctx, input ? "upload_tree" : "create_tree");
     auto *tr = new mwgpu_tree();
     tr->is_input = input;
     if (auto s = make_mra(ctx, mra, tr->mra, &tr->d_filt)) { free_tree(ctx, tr); return s; }
@@ -360,10 +361,12 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
         free_tree(ctx, tr);
         return s;
     }
+    trace.mark("alloc");
     MW_CK(cudaMemcpyAsync(t.idx, tr->h_idx.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(t.child0, d->child0, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
     if (d->coefs) MW_CK(cudaMemcpyAsync(t.coefs, d->coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
     else MW_CK(cudaMemsetAsync(t.coefs, 0, sizeof(double) * tot * nc, ctx->stream));
+    trace.mark("coefs");
     if (input) {
         // FP32 copy read by the mixed form
         if ((s = pool_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(ctx, tr); return s; }
@@ -382,9 +385,11 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     } else {
         MW_CK(cudaMemsetAsync(t.norms, 0, sizeof(double) * tot * 8, ctx->stream));
     }
+    trace.mark("fp32_norms");
     // only input trees are looked up by node index (band cells, GenNode
     // ancestors); output trees are addressed by position
     if (input && (s = rebuild_hash(ctx, tr, n))) { free_tree(ctx, tr); return s; }
+    trace.mark("hash");
     *out = tr;
     return MWGPU_OK;
 }

@@ -299,14 +299,17 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
             }
             b.tree = outs[t]->t.get();
             // room for the refinement without moving the coefficients on every
-            // growth step (untouched capacity costs no memory)
-            {
+            // growth step (untouched capacity costs no memory; a fixed grid
+            // does not grow)
+            if (max_iter != 0) {
                 const size_t guess = b.tree->nodes.size() + 2 * inps[t]->t->nodes.size() + 4096;
                 b.tree->nodes.reserve(guess);
                 b.tree->coefs.reserve(guess * (size_t)b.tree->nCoefs);
             }
             b.dinp = upload_input(ctx, md, *inps[t]->t, acc);
+            ht.mark("input");
             b.dout = create_output(ctx, md, *b.tree, acc);
+            ht.mark("output");
             b.synced = b.tree->nodes.size();
             // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
             for (auto &lvl : b.tree->nodesByDepth(false))

@@ -256,7 +256,11 @@ template <int D> void Tree<D>::calcSquareNorm() {
 }
 
 template <int D> void Tree<D>::clearGenerated() {
-    // Rebuild without GenNodes (FunctionTree::deleteGenerated).
+    // Rebuild without GenNodes (FunctionTree::deleteGenerated); nothing to do
+    // (and no copy of the coefficients) when the tree holds none.
+    bool any = false;
+    for (size_t i = 0; i < nodes.size() && !any; i++) any = isGen((int)i);
+    if (!any) return;
     std::vector<int> remap(nodes.size(), -1);
     std::vector<Node> nn;
     std::vector<double> nc;
