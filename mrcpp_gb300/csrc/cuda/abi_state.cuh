@@ -65,7 +65,8 @@ struct mwgpu_ctx {
     int list_cap = 0;
     cudaEvent_t marks[16] = {};
     // work list of the mixed form
-    WorkItem *d_items = nullptr;
+    WorkItem *d_items = nullptr;     // work items in term-major order (what the contraction reads)
+    WorkItem *d_items_cm = nullptr;  // the builder's cell-major items (same capacity)
     long long items_cap = 0;
     long long *d_pair_off = nullptr, pair_off_cap = 0;
     int *d_pcounts = nullptr;

@@ -152,6 +152,18 @@ __device__ __forceinline__ void store_block(float *out, int lane, const float (&
             for (int j = 0; j < K; j++) out[(c % K) + S::P * (c / K + K * j)] = s[r][j];
     }
 }
+// adds a task's rows to an output block (same positions as store_block)
+template <int K>
+__device__ __forceinline__ void add_block(float *out, int lane, const float (&s)[Shape<K>::R][K]) {
+    using S = Shape<K>;
+#pragma unroll
+    for (int r = 0; r < S::R; r++) {
+        const int c = row_of<K>(lane, r);
+        if (c < S::K2)
+#pragma unroll
+            for (int j = 0; j < K; j++) out[(c % K) + S::P * (c / K + K * j)] += s[r][j];
+    }
+}
 
 // ---- tensor-core path (K = 8) ----
 __device__ __forceinline__ unsigned to_tf32(float x) {
@@ -250,6 +262,16 @@ __device__ __forceinline__ void store_mma(float *out, int lane, const float (&s)
         out[j * S::S1 + (c & 7) + 12 * (c >> 3)] = s[e >> 3][e & 7];
     }
 }
+template <int K>
+__device__ __forceinline__ void add_mma(float *out, int lane, const float (&s)[Shape<K>::R][K]) {
+    using S = Shape<K>;
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        int c, j;
+        mma_cj(lane, e, c, j);
+        out[j * S::S1 + (c & 7) + 12 * (c >> 3)] += s[e >> 3][e & 7];
+    }
+}
 
 // one warp task / store on either path
 template <int K, int NS, bool FIN>
@@ -262,6 +284,16 @@ template <int K>
 __device__ __forceinline__ void store(float *out, int lane, const float (&s)[Shape<K>::R][K]) {
     if constexpr (Shape<K>::MMA) store_mma<K>(out, lane, s);
     else store_block<K>(out, lane, s);
+}
+// first contribution of a group to an output block: store; later ones: add
+template <int K>
+__device__ __forceinline__ void store_or_add(float *out, int lane, const float (&s)[Shape<K>::R][K], bool add) {
+    if (add) {
+        if constexpr (Shape<K>::MMA) add_mma<K>(out, lane, s);
+        else add_block<K>(out, lane, s);
+    } else {
+        store<K>(out, lane, s);
+    }
 }
 // (c, j) of accumulator element (r, jj) of a lane
 template <int K>
@@ -282,6 +314,36 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// stage-1 (bits 17-34) and stage-2 (bits 35-51) input bits of WorkItem::sched
+constexpr unsigned long long kStage1Bits = ((1ull << 18) - 1ull) << 17;
+constexpr unsigned long long kStage2Bits = ((1ull << 17) - 1ull) << 35;
+
+// block-schedule items whose y and z (resp. z) operator blocks are the same
+__device__ __forceinline__ bool same_s1(const WorkItem &a, const WorkItem &b) {
+    return (a.flags & 1) && (b.flags & 1) && a.term == b.term && a.tl[1] == b.tl[1] && a.tl[2] == b.tl[2];
+}
+__device__ __forceinline__ bool same_s2(const WorkItem &a, const WorkItem &b) {
+    return (a.flags & 1) && (b.flags & 1) && a.term == b.term && a.tl[2] == b.tl[2];
+}
+
+// g accumulators: compensated (Kahan) FP32 sums, or FP32 sums flushed to FP64
+template <int K>
+__device__ __forceinline__ void accumulate(float (&acc)[Shape<K>::R][K], float (&cmp)[Shape<K>::R][K], const float (&sv)[Shape<K>::R][K]) {
+#pragma unroll
+    for (int r = 0; r < Shape<K>::R; r++)
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            if (Shape<K>::KAHAN) {
+                const float y = sv[r][j] - cmp[r][j];
+                const float t = acc[r][j] + y;
+                cmp[r][j] = (t - acc[r][j]) - y;
+                acc[r][j] = t;
+            } else {
+                acc[r][j] += sv[r][j];
+            }
+        }
+}
 
 // copies the f blocks an item needs (mask byte b nonzero) into padded rows
 template <int K>
@@ -382,6 +444,18 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
         cp_async_wait_all();
         __syncthreads();
         int since = 0;
+        // Groups of adjacent block-schedule items (term-major item order):
+        // S1 = same (term, l_y, l_z), whose x-step outputs are summed before one
+        // y step; S2 = same (term, l_z), whose xy-step outputs are summed before
+        // one z step.  O^y and O^z are the same for all items of such a group,
+        // so the sums equal the per-item products.  sc1 / sc2: union of the
+        // group's stage-1 / stage-2 input bits; w1 / w2: S1 / S2 blocks already
+        // written in the group (the first contribution is stored, later ones
+        // are added).
+        float *S1 = BUF, *S2 = BUF + 9 * IB;
+        unsigned long long sc1 = 0ull, sc2 = 0ull;
+        unsigned w1 = 0u, w2 = 0u;
+        WorkItem prev{};
         for (int it = it0; it < it1; it++) {
             const int k = it - it0;
             const WorkItem item = items[it];
@@ -390,68 +464,85 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
             if (has_next) nx = items[it + 1];
             const float *OX = OBS + (k % 3) * 12 * K2, *OY = OX + 4 * K2, *OZ = OX + 8 * K2;
             const bool block = item.flags & 1;
-            int last = 0, nsub = 1;
-            if (!block) {
-                nsub = 8 / CG;
-                for (int g = 0; g < nsub; g++)
-                    if ((item.mask >> (8 * CG * g)) & ((1ull << (8 * CG)) - 1ull)) last = g;
-            }
-            for (int sub = 0; sub < nsub; sub++) {
-                unsigned long long gbits = 0ull;
-                if (!block) {
-                    gbits = (item.mask >> (8 * CG * sub)) & ((1ull << (8 * CG)) - 1ull);
-                    if (gbits == 0ull) continue;
+            float sv[R][K];
+            if (block) {
+                const bool s1_first = !(k > 0 && same_s1(prev, item)), s1_last = !(has_next && same_s1(item, nx));
+                const bool s2_first = !(k > 0 && same_s2(prev, item)), s2_last = !(has_next && same_s2(item, nx));
+                // stage structure from the work-list builder (k_worklist.cu)
+                const unsigned long long sc = item.sched;
+                if (s1_first) {
+                    sc1 = 0ull;
+                    w1 = 0u;
                 }
-                float sv[R][K];
-                if (block) {
-                    // stage structure from the work-list builder (k_worklist.cu)
-                    const unsigned long long sc = item.sched;
-                    float *Y0 = BUF, *U = BUF + 8 * IB, *Y1 = BUF + 9 * IB, *PP = BUF + 17 * IB;
-                    // stage 0: outputs Y0[o] (o < 8) and U (o = 8)
-                    for (int o = warp; o < 9; o += NW) {
-                        unsigned valid = o < 8 ? (unsigned)((sc >> (2 * o)) & 3ull) : (unsigned)((sc >> 16) & 1ull);
-                        if (!valid) continue;
-                        const int a0 = o & 1, b12 = o & 6;  // src = b0 + b12
-                        const float *in[2] = {FB + b12 * BLK, FB + (b12 + 1) * BLK};
-                        const float *O[2] = {OX + 2 * a0 * K2, OX + (2 * a0 + 1) * K2};
-                        if (o == 8) {  // U = O^x_T f[0]
-                            in[0] = FB;
-                            O[0] = OX;
-                        }
-                        task<K, 2, true>(in, O, valid, lane, sv);
-                        store<K>(o < 8 ? Y0 + o * IB : U, lane, sv);
+                if (s2_first) {
+                    sc2 = 0ull;
+                    w2 = 0u;
+                }
+                sc1 |= sc & kStage1Bits;
+                sc2 |= sc & kStage2Bits;
+                // stage 0: outputs Y0[o] (o < 8) and U (o = 8), summed into S1
+                unsigned made = (unsigned)((sc >> 16) & 1ull) << 8;
+#pragma unroll
+                for (int o = 0; o < 8; o++) made |= (((sc >> (2 * o)) & 3ull) ? 1u : 0u) << o;
+                for (int o = warp; o < 9; o += NW) {
+                    unsigned valid = o < 8 ? (unsigned)((sc >> (2 * o)) & 3ull) : (unsigned)((sc >> 16) & 1ull);
+                    if (!valid) continue;
+                    const int a0 = o & 1, b12 = o & 6;  // src = b0 + b12
+                    const float *in[2] = {FB + b12 * BLK, FB + (b12 + 1) * BLK};
+                    const float *O[2] = {OX + 2 * a0 * K2, OX + (2 * a0 + 1) * K2};
+                    if (o == 8) {  // U = O^x_T f[0]
+                        in[0] = FB;
+                        O[0] = OX;
                     }
-                    __syncthreads();
-                    if (has_next) {  // the staged f block is free: the next item's f and operator blocks
-                        stage_f<K>(FB, nx, f_cap_real, f_coefs32, f_gcoefs32);
-                        stage_ob<K>(OBS + ((k + 1) % 3) * 12 * K2, op, nx, depth);
-                    }
-                    // stage 1: outputs Y1[q] (q < 8) and PP (q = 8)
+                    task<K, 2, true>(in, O, valid, lane, sv);
+                    store_or_add<K>(S1 + o * IB, lane, sv, (w1 >> o) & 1u);
+                }
+                w1 |= made;
+                __syncthreads();
+                if (has_next) {  // the staged f block is free: the next item's f and operator blocks
+                    stage_f<K>(FB, nx, f_cap_real, f_coefs32, f_gcoefs32);
+                    stage_ob<K>(OBS + ((k + 1) % 3) * 12 * K2, op, nx, depth);
+                }
+                if (s1_last) {
+                    // stage 1: outputs Y1[q] (q < 8) and PP (q = 8) of the summed S1, summed into S2
+                    unsigned made1 = (unsigned)((sc1 >> 34) & 1ull) << 8;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) made1 |= (((sc1 >> (17 + 2 * q)) & 3ull) || (q == 2 && ((sc1 >> 33) & 1ull)) ? 1u : 0u) << q;
                     for (int q = warp; q < 9; q += NW) {
-                        unsigned valid = q < 8 ? (unsigned)((sc >> (17 + 2 * q)) & 3ull) | (q == 2 ? (unsigned)((sc >> 33) & 1ull) << 2 : 0u)
-                                               : (unsigned)((sc >> 34) & 1ull);
+                        unsigned valid = q < 8 ? (unsigned)((sc1 >> (17 + 2 * q)) & 3ull) | (q == 2 ? (unsigned)((sc1 >> 33) & 1ull) << 2 : 0u)
+                                               : (unsigned)((sc1 >> 34) & 1ull);
                         if (!valid) continue;
                         const int a0 = q & 1, a1 = (q >> 1) & 1, b2 = q >> 2;
-                        const float *in[3] = {Y0 + (a0 + 4 * b2) * IB, Y0 + (a0 + 2 + 4 * b2) * IB, U};  // U -> (0, 1, 0)
+                        const float *in[3] = {S1 + (a0 + 4 * b2) * IB, S1 + (a0 + 2 + 4 * b2) * IB, S1 + 8 * IB};  // U -> (0, 1, 0)
                         const float *O[3] = {OY + 2 * a1 * K2, OY + (2 * a1 + 1) * K2, OY + 2 * K2};
                         if (q == 8) {  // P = O^y_T U
-                            in[0] = U;
+                            in[0] = S1 + 8 * IB;
                             O[0] = OY;
                         }
                         task<K, 3, false>(in, O, valid, lane, sv);
-                        store<K>(q < 8 ? Y1 + q * IB : PP, lane, sv);
+                        store_or_add<K>(S2 + q * IB, lane, sv, (w2 >> q) & 1u);
                     }
-                    __syncthreads();
-                    // stage 2: g component gt = warp; P -> (0, 0, 1), while P -> (0, 0, 0) is
-                    // the dropped s->s product
-                    {
+                    w2 |= made1;
+                    __syncthreads();  // S2 complete; S1 free for the next group
+                    if (s2_last) {
+                        // stage 2: g component gt = warp from the summed S2; P -> (0, 0, 1),
+                        // while P -> (0, 0, 0) is the dropped s->s product
                         const int gt = warp, a2 = gt >> 2;
-                        const float *in[3] = {Y1 + (gt & 3) * IB, Y1 + ((gt & 3) + 4) * IB, PP};
+                        const float *in[3] = {S2 + (gt & 3) * IB, S2 + ((gt & 3) + 4) * IB, S2 + 8 * IB};
                         const float *O[3] = {OZ + 2 * a2 * K2, OZ + (2 * a2 + 1) * K2, OZ + 2 * K2};
-                        const unsigned valid = (unsigned)((sc >> (35 + 2 * gt)) & 3ull) | (gt == 4 ? (unsigned)((sc >> 51) & 1ull) << 2 : 0u);
+                        const unsigned valid = (unsigned)((sc2 >> (35 + 2 * gt)) & 3ull) | (gt == 4 ? (unsigned)((sc2 >> 51) & 1ull) << 2 : 0u);
                         task<K, 3, false>(in, O, valid, lane, sv);
+                        accumulate<K>(acc, cmp, sv);
                     }
-                } else {
+                }
+            } else {
+                int last = 0;
+                constexpr int nsub = 8 / CG;
+                for (int g = 0; g < nsub; g++)
+                    if ((item.mask >> (8 * CG * g)) & ((1ull << (8 * CG)) - 1ull)) last = g;
+                for (int sub = 0; sub < nsub; sub++) {
+                    const unsigned long long gbits = (item.mask >> (8 * CG * sub)) & ((1ull << (8 * CG)) - 1ull);
+                    if (gbits == 0ull) continue;
                     float *X0 = BUF, *X1 = BUF + 2 * CG * IB;
                     const int ft0 = CG * sub;
                     // stage 0: X0[(lft, a0)] = O^x_{a0, ft&1} f[ft]
@@ -495,24 +586,12 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                         }
                         task<K, CG, false>(in, O, valid, lane, sv);
                     }
+                    accumulate<K>(acc, cmp, sv);
                     // no barrier before the next group: its stage 0 writes X0, which stage 2
                     // does not read, and its stage 1 writes X1 only after the next barrier
                 }
-                // accumulate: compensated (Kahan) FP32 sums, or FP32 sums flushed to FP64
-#pragma unroll
-                for (int r = 0; r < R; r++)
-#pragma unroll
-                    for (int j = 0; j < K; j++) {
-                        if (S::KAHAN) {
-                            const float y = sv[r][j] - cmp[r][j];
-                            const float t = acc[r][j] + y;
-                            cmp[r][j] = (t - acc[r][j]) - y;
-                            acc[r][j] = t;
-                        } else {
-                            acc[r][j] += sv[r][j];
-                        }
-                    }
             }
+            prev = item;
             if (!S::KAHAN && ++since >= 16) {
 #pragma unroll
                 for (int r = 0; r < R; r++)

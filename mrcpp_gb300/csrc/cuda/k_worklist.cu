@@ -440,6 +440,77 @@ __global__ void k_gather_goff(const long long *item_off, const long long *pair_o
     if (wi <= n_work) g_off[wi] = item_off[pair_off[wi]];
 }
 
+// Term-major order of the work items of each output node: a stable counting
+// sort by term of the items [g_off[wi], g_off[wi + 1]) of `in` (cell-major
+// from k_pairs: band cells z slowest, x fastest) into the same range of
+// `out`.  The items of one term then follow the band cells in z, y, x order,
+// so that the items with the same (term, l_y, l_z), and the runs of those
+// with the same (term, l_z), are adjacent: the contraction sums their
+// x-step (and xy-step) intermediates before the remaining 1D applications.
+// One CTA per output node; per tile of 256 items a warp ranks the items of
+// each term with __match_any_sync and the warps' counts give the offsets.
+__global__ void __launch_bounds__(kOrderThreads) k_order_terms(const long long *g_off, int n_work, const WorkItem *in, WorkItem *out,
+                                                                int n_terms, int *err, const int *nw_dev) {
+    constexpr int NWARP = kOrderThreads / 32;
+    __shared__ int base[kOrderMaxTerms];
+    __shared__ int wcnt[NWARP][kOrderMaxTerms];
+    if (nw_dev) n_work = *nw_dev;
+    const int wi = blockIdx.x;
+    if (wi >= n_work) return;
+    const long long b = g_off[wi], e = g_off[wi + 1];
+    if (b == e) return;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int t = tid; t < kOrderMaxTerms; t += kOrderThreads) {
+        base[t] = 0;
+        for (int w = 0; w < NWARP; w++) wcnt[w][t] = 0;
+    }
+    __syncthreads();
+    for (long long i = b + tid; i < e; i += kOrderThreads) {
+        const int t = in[i].term;
+        if (t >= 0 && t < n_terms) atomicAdd(&base[t], 1);
+        else atomicOr(err, DE_RANGE);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int s = 0;
+        for (int t = 0; t < n_terms; t++) {
+            const int c = base[t];
+            base[t] = s;
+            s += c;
+        }
+    }
+    __syncthreads();
+    for (long long t0 = b; t0 < e; t0 += kOrderThreads) {
+        const long long i = t0 + tid;
+        WorkItem it;
+        int term = -1;
+        if (i < e) {
+            it = in[i];
+            term = it.term;
+            if (term < 0 || term >= n_terms) term = -1;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, term);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (term >= 0 && rank == 0) wcnt[warp][term] = __popc(peers);
+        __syncthreads();
+        if (term >= 0) {
+            long long pos = base[term] + rank;
+            for (int w = 0; w < warp; w++) pos += wcnt[w][term];
+            if (b + pos < e) out[b + pos] = it;
+        }
+        __syncthreads();
+        for (int t = tid; t < n_terms; t += kOrderThreads) {
+            int s = 0;
+            for (int w = 0; w < NWARP; w++) {
+                s += wcnt[w][t];
+                wcnt[w][t] = 0;
+            }
+            base[t] += s;
+        }
+        __syncthreads();
+    }
+}
+
 // chunks of at most `per` items per work entry (at least one, so that every
 // output node gets its reduction input)
 __device__ inline long long chunk_len(const long long *g_off, int n_work, long long per) {
@@ -563,6 +634,14 @@ void launch_scan(const int *in, long long *out, long long n, long long *block_su
 
 void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev) {
     k_gather_goff<<<(n_work + 1 + 255) / 256, 256, 0, s>>>(item_off, pair_off, n_work, g_off, nw_dev);
+}
+
+bool term_order_supported(int n_terms) { return n_terms > 0 && n_terms <= kOrderMaxTerms; }
+
+void launch_order_terms(const long long *g_off, int n_work, const WorkItem *in, WorkItem *out, int n_terms, int *err, cudaStream_t s,
+                        const int *nw_dev) {
+    if (n_work <= 0) return;
+    k_order_terms<<<n_work, kOrderThreads, 0, s>>>(g_off, n_work, in, out, n_terms, err, nw_dev);
 }
 
 }  // namespace mwgpu

@@ -289,14 +289,20 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
         return MWGPU_ERR_BAD_ARG;
     }
     if (total > ctx->items_cap) {
-        if (ctx->d_items) cudaFree(ctx->d_items);
-        ctx->d_items = nullptr;
+        for (WorkItem **p : {&ctx->d_items, &ctx->d_items_cm}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
         ctx->items_cap = std::max(total, 2 * ctx->items_cap);
         if (auto s = dev_alloc(ctx, &ctx->d_items, (size_t)ctx->items_cap)) return s;
+        if (auto s = dev_alloc(ctx, &ctx->d_items_cm, (size_t)ctx->items_cap)) return s;
     }
+    // cell-major items from the builder, then term-major per output node
+    const bool order = term_order_supported(o->op.n_terms);
     launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_pcounts, ctx->d_item_off,
-                      ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream);
-    ctx->launches++;
+                      order ? ctx->d_items_cm : ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream);
+    if (order) launch_order_terms(ctx->d_goff, n, ctx->d_items_cm, ctx->d_items, o->op.n_terms, ctx->d_err, ctx->stream);
+    ctx->launches += 1 + (order ? 1 : 0);
     // chunks of about the same number of items, several waves of CTAs
     long long per = std::max<long long>(8, (total + kChunkTarget - 1) / kChunkTarget);
     if (const char *e = std::getenv("MWGPU_CHUNK_ITEMS")) per = std::max<long long>(1, std::atoll(e));
@@ -712,7 +718,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
-                    (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_chunks,
+                    (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_items_cm, (void *)ctx->d_chunks,
                     (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
                     (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_nstage, (void *)ctx->d_ltree})
@@ -1278,7 +1284,7 @@ struct mwgpu_plan {
     long long *d_pair_off = nullptr, *d_item_off = nullptr, *d_scan = nullptr, *d_goff = nullptr, *d_coff = nullptr, *d_cscan = nullptr;
     long long scan_n = 0, cscan_n = 0;
     int *d_pcounts = nullptr, *d_ccount = nullptr;
-    WorkItem *d_items = nullptr;
+    WorkItem *d_items = nullptr, *d_items_cm = nullptr;  // term-major / cell-major (null: no reordering)
     long long items_cap = 0;
     int4 *d_chunks = nullptr;
     int *d_chunk_begin = nullptr, *d_nchunks = nullptr, *d_counter = nullptr;
@@ -1357,8 +1363,9 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
         launch_scan(pl->d_pcounts, pl->d_item_off, pl->np, pl->d_scan, pl->d_scan + (pl->scan_n - 1), st);
         launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st);
         launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
-                          pl->d_item_off, pl->d_items, pl->items_cap, pl->d_err, st);
-        ctx->launches += 6;
+                          pl->d_item_off, pl->d_items_cm ? pl->d_items_cm : pl->d_items, pl->items_cap, pl->d_err, st);
+        if (pl->d_items_cm) launch_order_terms(pl->d_goff, pl->n, pl->d_items_cm, pl->d_items, o->op.n_terms, pl->d_err, st);
+        ctx->launches += 6 + (pl->d_items_cm ? 1 : 0);
         plan_contract(ctx, pl, pl->per, true);
     } else {
         launch_stamp(pl->d_stamps + 1, st);
@@ -1551,6 +1558,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
             (s = plan_alloc(ctx, pl, &pl->d_counter, 1)) ||
             (s = plan_alloc(ctx, pl, &pl->d_partial, (size_t)pl->chunks_cap * 8 * o->mra.kp1_d)))
             return fail(s);
+        if (term_order_supported(o->op.n_terms) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
         MW_CK(cudaMemcpyAsync(pl->d_pair_off, poff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
         MW_CK(cudaStreamSynchronize(ctx->stream));
         // chunk length: candidates around the default, each timed on the full
@@ -1733,6 +1741,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
     for (auto v : lvl_pairs) max_pairs = std::max(max_pairs, v);
     std::vector<long long> lvl_per(n_levels, 8);
     const int T = o->op.n_terms;
+    const bool order = term_order_supported(T);  // term-major work items (mixed form)
     // Work-list capacity per level: every (pair, term) of the level as an item
     // while that stays within kJudgedItemBudget (no host round trip); beyond
     // it, or when a level overflows it, the exact bound from an unscreened
@@ -1797,7 +1806,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             int *flags, *kcnt, *work, *nwork, *ccnt, *pcounts, *chunk_begin, *nchunks, *counter, *first_miss, *cells;
             long long *koff, *kscan, *pair_off, *pscan, *item_off, *iscan, *goff, *coff, *cscan;
             int4 *chunks;
-            WorkItem *items;
+            WorkItem *items, *items_cm;
             double *partial, *state, *sq, *scale_fac;
             unsigned long long *node_terms;
         } b{};
@@ -1822,6 +1831,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
         b.nchunks = c.take<int>(1);
         b.counter = c.take<int>(1);
         b.items = c.take<WorkItem>(mixed ? max_items : 1);
+        b.items_cm = c.take<WorkItem>(mixed && order ? max_items : 1);
         b.partial = c.take<double>(mixed ? (size_t)max_chunks * 8 * m.kp1_d : 1);
         b.state = c.take<double>(3);
         b.sq = c.take<double>(3 * (size_t)n_levels);
@@ -1883,14 +1893,15 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             launch_scan(b.ccnt, b.coff, nl, b.cscan, b.cscan + (scan_blocks(max_level + 1) + 1), st);
             const int ccap = (int)((long long)nl + kChunkTarget + 1);
             launch_chunk_fill(b.goff, b.coff, nl, lvl_per[j], b.chunks, b.chunk_begin, ccap, b.nchunks, ctx->d_err, st, b.nwork);
-            launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.pcounts, b.item_off, b.items,
-                              lvl_items[j], ctx->d_err, st, np_dev, b.nwork);
+            launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.pcounts, b.item_off,
+                              order ? b.items_cm : b.items, lvl_items[j], ctx->d_err, st, np_dev, b.nwork);
+            if (order) launch_order_terms(b.goff, nl, b.items_cm, b.items, T, ctx->d_err, st, b.nwork);
             MW_CK(cudaMemsetAsync(b.counter, 0, sizeof(int), st));
             launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,
                          st);
             launch_reduce_chunks(m, ctx->d_gs, ctx->d_wtree, b.work, nl, b.chunk_begin, b.partial, st, b.nwork);
             launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, b.goff, b.node_terms, st);  // sNorm: level 0 only
-            ctx->launches += 17;
+            ctx->launches += 17 + (order ? 1 : 0);
         } else {
             launch_contract_fp64(m, o->op, inp->t, out->t, b.work, nl, 0.0, ctx->d_stats, ctx->d_err, st, b.nwork, ctx->d_gthr);
             launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, nullptr, nullptr, st);

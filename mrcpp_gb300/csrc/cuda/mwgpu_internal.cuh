@@ -22,6 +22,8 @@ constexpr double kMachineZero = 1.0e-14;
 constexpr uint64_t kEmptyKey = ~0ull;
 // chunk length of the mixed contraction: max(8, ceil(items / kChunkTarget))
 constexpr long long kChunkTarget = 8 * 304;
+// term-major ordering of the work items (k_order_terms): threads, most terms
+constexpr int kOrderThreads = 256, kOrderMaxTerms = 256;
 // learned-grid network: features, hidden width, parameter count
 constexpr int kMlpFeatures = 8, kMlpHidden = 64;
 constexpr int kMlpParams = kMlpHidden * kMlpFeatures + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden + kMlpHidden + 1;
@@ -185,6 +187,11 @@ int contract_items_resident(int K);
 long long scan_blocks(long long n);
 void launch_scan(const int *in, long long *out, long long n, long long *block_sums, long long *total, cudaStream_t s);
 void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev = nullptr);
+// term-major order of each output node's items (in -> out, same ranges); only
+// for operators of at most kOrderMaxTerms terms
+bool term_order_supported(int n_terms);
+void launch_order_terms(const long long *g_off, int n_work, const WorkItem *in, WorkItem *out, int n_terms, int *err, cudaStream_t s,
+                        const int *nw_dev = nullptr);
 void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                            int n_work, const int4 *chunks, int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err,
                            cudaStream_t s);
