@@ -42,6 +42,7 @@ struct mwgpu_ctx {
     std::string err;
     int *d_err = nullptr;
     LevelStats *d_stats = nullptr;
+    int *d_tc_counter = nullptr;  // chunk counter of the tensor-core contraction
     int *d_work = nullptr;
     int *d_wtree = nullptr;  // tree of every work entry (batched levels)
     int work_cap = 0;

@@ -1,4 +1,6 @@
 // Instantiations and launcher of the mixed-precision work-list contraction (k_mixed.cuh).
+#include <cstdlib>
+
 #include "k_mixed.cuh"
 
 namespace mwgpu {
@@ -30,9 +32,9 @@ bool mixed_supported(int K) { return K >= 2 && K <= 10; }
 
 void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                            int n_work, const int4 *chunks, int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err,
-                           cudaStream_t s) {
+                           int *tc_counter, cudaStream_t s) {
     if (n_work <= 0) return;
-    launch_items(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, nullptr, nullptr, s);
+    launch_items(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, nullptr, nullptr, tc_counter, s);
     mixed::k_reduce_chunks<<<dim3(n_work, 8), mixed::kReduceThreads, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nullptr);
 }
 
@@ -59,8 +61,12 @@ int contract_items_resident(int K) {
 
 void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                   const int4 *chunks, int n_chunks, const WorkItem *items, double *partial, int *err, const int *n_chunks_dev, int *counter,
-                  cudaStream_t s) {
+                  int *tc_counter, cudaStream_t s) {
     if (n_chunks <= 0) return;
+    // order 7 with MWGPU_TC set: chunks of block-schedule items go to the
+    // tcgen05 kernel (k_tc.cu), the others (screened items) to the kernel below
+    const bool tc = tc_supported(m.K) && op.btc && tc_counter && std::getenv("MWGPU_TC");
+    if (tc) launch_chunk_types(const_cast<int4 *>(chunks), n_chunks, n_chunks_dev, items, s);
     switch (m.K) {
         case 2: launch_k<2>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
         case 3: launch_k<3>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
@@ -73,6 +79,7 @@ void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const D
         case 10: launch_k<10>(m, op, fs, gs, work_tree, work, chunks, n_chunks, items, partial, err, n_chunks_dev, counter, s); break;
         default: break;
     }
+    if (tc) launch_contract_tc(m, op, fs, gs, work_tree, work, chunks, n_chunks, n_chunks_dev, items, partial, err, tc_counter, s);
 }
 
 }  // namespace mwgpu

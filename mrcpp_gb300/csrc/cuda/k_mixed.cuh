@@ -251,6 +251,53 @@ __device__ __forceinline__ void task_mma(const float *const (&in)[NS], const flo
         for (int v = 0; v < 4; v++) s[mt >> 1][4 * (mt & 1) + v] = d[mt][v];
 }
 
+// One m-tile (rows 16 mt .. 16 mt + 15) of a one-input task on the tensor cores:
+// the 9th output block of a stage (the U or P channel) is spread over four
+// warps this way, so that a stage with 9 outputs on 8 warps takes 1 1/8
+// task times instead of 2.
+template <int K, bool FIN>
+__device__ __forceinline__ void task_mma_tile(const float *in, const float *O, int lane, int mt, float (&d)[4]) {
+    using S = Shape<K>;
+    const int g = lane >> 2, t = lane & 3;
+    unsigned bh0, bl0, bh1, bl1;
+    split_tf32(O[g + K * t], bh0, bl0);
+    split_tf32(O[g + K * (t + 4)], bh1, bl1);
+    float x[4];
+    if (FIN) {
+        const float *r0 = in + S::P * (16 * mt + g), *r1 = in + S::P * (16 * mt + g + 8);
+        x[0] = r0[t];
+        x[1] = r1[t];
+        x[2] = r0[t + 4];
+        x[3] = r1[t + 4];
+    } else {
+        const float *r0 = in + (2 * mt) * S::S1 + 12 * g, *r1 = in + (2 * mt + 1) * S::S1 + 12 * g;
+        x[0] = r0[t];
+        x[1] = r1[t];
+        x[2] = r0[t + 4];
+        x[3] = r1[t + 4];
+    }
+    unsigned ah[4], al[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) split_tf32(x[q], ah[q], al[q]);
+#pragma unroll
+    for (int v = 0; v < 4; v++) d[v] = 0.f;
+    mma_tf32(d, al[0], al[1], al[2], al[3], bh0, bh1);
+    mma_tf32(d, ah[0], ah[1], ah[2], ah[3], bl0, bl1);
+    mma_tf32(d, ah[0], ah[1], ah[2], ah[3], bh0, bh1);
+}
+// stores (or adds) the fragment of m-tile mt into an intermediate block
+template <int K>
+__device__ __forceinline__ void store_or_add_tile(float *out, int lane, int mt, const float (&d)[4], bool add) {
+    using S = Shape<K>;
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+        int c, j;
+        mma_cj(lane, 4 * mt + v, c, j);
+        float &dst = out[j * S::S1 + (c & 7) + 12 * (c >> 3)];
+        dst = add ? dst + d[v] : d[v];
+    }
+}
+
 // stores C fragments into an intermediate block: element (c, j) at j S1 + (c % 8) + 12 (c / 8)
 template <int K>
 __device__ __forceinline__ void store_mma(float *out, int lane, const float (&s)[Shape<K>::R][K]) {
@@ -418,6 +465,8 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
     const int n_chunks = n_chunks_dev ? *n_chunks_dev : (int)gridDim.x;
     for (int cix = blockIdx.x; cix < n_chunks;) {
         const int4 ch = chunks[cix];
+        // chunks of type 1 (block-schedule items only, order 7) belong to the tensor-core kernel (k_tc.cu)
+        if (ch.w != 1) {
         const int gi = work[ch.x];
         const int tree = work_tree[ch.x];
         const int depth = gs[tree].idx[gi].x - m.root_scale;
@@ -484,7 +533,7 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                 unsigned made = (unsigned)((sc >> 16) & 1ull) << 8;
 #pragma unroll
                 for (int o = 0; o < 8; o++) made |= (((sc >> (2 * o)) & 3ull) ? 1u : 0u) << o;
-                for (int o = warp; o < 9; o += NW) {
+                for (int o = warp; o < (S::MMA ? 8 : 9); o += NW) {
                     unsigned valid = o < 8 ? (unsigned)((sc >> (2 * o)) & 3ull) : (unsigned)((sc >> 16) & 1ull);
                     if (!valid) continue;
                     const int a0 = o & 1, b12 = o & 6;  // src = b0 + b12
@@ -497,6 +546,14 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                     task<K, 2, true>(in, O, valid, lane, sv);
                     store_or_add<K>(S1 + o * IB, lane, sv, (w1 >> o) & 1u);
                 }
+                if constexpr (S::MMA) {
+                    // U = O^x_T f[0]: one m-tile on each of warps 4-7
+                    if (((sc >> 16) & 1ull) && warp >= 4) {
+                        float d[4];
+                        task_mma_tile<K, true>(FB, OX, lane, warp - 4, d);
+                        store_or_add_tile<K>(S1 + 8 * IB, lane, warp - 4, d, (w1 >> 8) & 1u);
+                    }
+                }
                 w1 |= made;
                 __syncthreads();
                 if (has_next) {  // the staged f block is free: the next item's f and operator blocks
@@ -508,7 +565,7 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                     unsigned made1 = (unsigned)((sc1 >> 34) & 1ull) << 8;
 #pragma unroll
                     for (int q = 0; q < 8; q++) made1 |= (((sc1 >> (17 + 2 * q)) & 3ull) || (q == 2 && ((sc1 >> 33) & 1ull)) ? 1u : 0u) << q;
-                    for (int q = warp; q < 9; q += NW) {
+                    for (int q = warp; q < (S::MMA ? 8 : 9); q += NW) {
                         unsigned valid = q < 8 ? (unsigned)((sc1 >> (17 + 2 * q)) & 3ull) | (q == 2 ? (unsigned)((sc1 >> 33) & 1ull) << 2 : 0u)
                                                : (unsigned)((sc1 >> 34) & 1ull);
                         if (!valid) continue;
@@ -521,6 +578,14 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                         }
                         task<K, 3, false>(in, O, valid, lane, sv);
                         store_or_add<K>(S2 + q * IB, lane, sv, (w2 >> q) & 1u);
+                    }
+                    if constexpr (S::MMA) {
+                        // P = O^y_T U: one m-tile on each of warps 4-7
+                        if (((sc1 >> 34) & 1ull) && warp >= 4) {
+                            float d[4];
+                            task_mma_tile<K, false>(S1 + 8 * IB, OY, lane, warp - 4, d);
+                            store_or_add_tile<K>(S2 + 8 * IB, lane, warp - 4, d, (w2 >> 8) & 1u);
+                        }
                     }
                     w2 |= made1;
                     __syncthreads();  // S2 complete; S1 free for the next group
@@ -619,6 +684,7 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
                     go[e] = S::KAHAN ? (double)acc[r][jj] - (double)cmp[r][jj] : G64[e] + (double)acc[r][jj];
                 }
             }
+        }
         if (!counter) break;
         __syncthreads();
         if (tid == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);

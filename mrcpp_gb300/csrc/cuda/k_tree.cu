@@ -147,9 +147,11 @@ __global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pe
     }
     double *out = f.gcoefs + (size_t)slot * K3;
     float *out32 = f.gcoefs32 + (size_t)slot * K3;
+    float *tc = f.gtc32 ? f.gtc32 + (size_t)slot * kTcGenFloats : nullptr;
     for (int e = tid; e < K3; e += nthr) {
         out[e] = src[e];
         out32[e] = (float)src[e];
+        if (tc) tc_gen_store(tc, e, (float)src[e]);
     }
     // scaling norm (GenNode wavelet norms are zero)
     __shared__ double red[32];
@@ -499,11 +501,13 @@ __global__ void k_gen_nodes32(DevMRA m, DevTree f, const uint64_t *plist, int n_
     }
     double *out = f.gcoefs + (size_t)slot * K3;
     float *out32 = f.gcoefs32 + (size_t)slot * K3;
+    float *tc = f.gtc32 ? f.gtc32 + (size_t)slot * kTcGenFloats : nullptr;
     double s = 0.0;
     for (int e = tid; e < K3; e += nthr) {
         const float v = src[e];
         out32[e] = v;
         out[e] = (double)v;
+        if (tc) tc_gen_store(tc, e, v);
         s += (double)v * (double)v;
     }
     __shared__ double red[32];

@@ -124,25 +124,31 @@ mwgpu_status grow_gen(mwgpu_ctx *ctx, mwgpu_tree *tr, int need) {
     int tot = t.cap_real + cap;
     int4 *idx;
     double *g, *norms;
-    float *g32;
+    float *g32, *gtc = nullptr;
     if (auto s = pool_alloc(ctx, &idx, tot)) return s;
     if (auto s = pool_alloc(ctx, &norms, (size_t)tot * 8)) return s;
     if (auto s = pool_alloc(ctx, &g, (size_t)cap * K3)) return s;
     if (auto s = pool_alloc(ctx, &g32, (size_t)cap * K3)) return s;
+    if (t.tc32)
+        if (auto s = pool_alloc(ctx, &gtc, (size_t)cap * mwgpu::kTcGenFloats)) return s;
     MW_CK(cudaMemcpyAsync(idx, t.idx, sizeof(int4) * (t.cap_real + t.n_gen), cudaMemcpyDeviceToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(norms, t.norms, sizeof(double) * 8 * (t.cap_real + t.n_gen), cudaMemcpyDeviceToDevice, ctx->stream));
     if (t.n_gen > 0) {
         MW_CK(cudaMemcpyAsync(g, t.gcoefs, sizeof(double) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
         MW_CK(cudaMemcpyAsync(g32, t.gcoefs32, sizeof(float) * K3 * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (gtc && t.gtc32)
+            MW_CK(cudaMemcpyAsync(gtc, t.gtc32, sizeof(float) * mwgpu::kTcGenFloats * t.n_gen, cudaMemcpyDeviceToDevice, ctx->stream));
     }
     pool_free(ctx, t.idx);
     pool_free(ctx, t.norms);
     pool_free(ctx, t.gcoefs);
     pool_free(ctx, t.gcoefs32);
+    if (t.gtc32) pool_free(ctx, t.gtc32);
     t.idx = idx;
     t.norms = norms;
     t.gcoefs = g;
     t.gcoefs32 = g32;
+    t.gtc32 = gtc;
     t.cap_gen = cap;
     return MWGPU_OK;
 }
@@ -202,7 +208,7 @@ mwgpu_status check_err(mwgpu_ctx *ctx, const char *phase) {
     MW_CK(cudaStreamSynchronize(ctx->stream));
     if (herr) {
         ctx->err = std::string(phase) + ": device error flags " + std::to_string(herr);
-        return MWGPU_ERR_INTERNAL;
+        return (herr & mwgpu::DE_TIMEOUT) ? MWGPU_ERR_TIMEOUT : MWGPU_ERR_INTERNAL;
     }
     return MWGPU_OK;
 }
@@ -336,7 +342,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     MW_CK(cudaMemcpyAsync(ctx->d_chunk_begin, cbeg.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
     launch_contract_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items,
-                          ctx->d_partial, ctx->d_err, ctx->stream);
+                          ctx->d_partial, ctx->d_err, ctx->d_tc_counter, ctx->stream);
     ctx->launches += 2;
     // (the chunk arrays came from pageable memory: the copies read them before returning)
     hs->node_terms = (unsigned long long)total;
@@ -378,6 +384,12 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
         if ((s = pool_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(ctx, tr); return s; }
         launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
         ctx->launches++;
+        // TF32 hi / lo operands of the tensor-core contraction (order 7)
+        if (mwgpu::tc_supported(tr->mra.K) && n > 0) {
+            if ((s = pool_alloc(ctx, &t.tc32, (size_t)n * mwgpu::kTcNodeFloats))) { free_tree(ctx, tr); return s; }
+            mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
+            ctx->launches++;
+        }
     }
     if (d->norms) {
         MW_CK(cudaMemcpyAsync(t.norms, d->norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
@@ -403,7 +415,7 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
 void free_tree(mwgpu_ctx *ctx, mwgpu_tree *tr) {
     if (!tr) return;
     DevTree &t = tr->t;
-    for (void *p : {(void *)t.idx, (void *)t.coefs, (void *)t.norms, (void *)t.child0, (void *)t.gcoefs, (void *)t.coefs32, (void *)t.gcoefs32,
+    for (void *p : {(void *)t.idx, (void *)t.coefs, (void *)t.norms, (void *)t.child0, (void *)t.gcoefs, (void *)t.coefs32, (void *)t.gcoefs32, (void *)t.tc32, (void *)t.gtc32,
                     (void *)t.hkeys, (void *)t.hvals, (void *)tr->d_filt})
         pool_free(ctx, p);
     delete tr;
@@ -703,7 +715,8 @@ mwgpu_status mwgpu_init(mwgpu_ctx **out, const mwgpu_config *cfg) {
     }
     if (cudaSetDevice(ctx->device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess || cudaEventCreate(&ctx->ev2) != cudaSuccess ||
-        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, sizeof(LevelStats)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&ctx->d_stats, sizeof(LevelStats)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_tc_counter, sizeof(int)) != cudaSuccess) {
         g_init_error = std::string("device initialisation failed: ") + cudaGetErrorString(cudaGetLastError());
         delete ctx;
         return MWGPU_ERR_DEVICE;
@@ -717,7 +730,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
+    for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_tc_counter, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
                     (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_items_cm, (void *)ctx->d_chunks,
                     (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
@@ -921,6 +934,30 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.term_rows = p_trows;
     o->op.pair_bound = p_pb;
     o->op.pair_bound_off = p_pboff;
+    o->op.n_nodes = (int)node;
+    o->op.btc = nullptr;
+    if (mwgpu::tc_supported(K)) {
+        // B operands of the tensor-core contraction per operator node (band zeroed) + a zero record
+        std::vector<int4> ninfo(node);
+        size_t nd = 0;
+        for (int t = 0; t < T; t++)
+            for (int dd = 0; dd < d->depth[t]; dd++) {
+                const int L = dep_L[(size_t)t * rows + dd];
+                for (int l = -L; l <= L; l++) ninfo[nd++] = make_int4(t, dd, l, 0);
+            }
+        int4 *p_ni = nullptr;
+        float *p_btc = nullptr;
+        if ((s = up(&p_ni, ninfo.data(), ninfo.size())) || (s = dev_alloc(ctx, &p_btc, (node + 1) * (size_t)mwgpu::kTcFormFloats))) {
+            for (void *p : o->allocs) cudaFree(p);
+            pool_free(ctx, o->d_filt);
+            delete o;
+            return s;
+        }
+        o->allocs.push_back((void *)p_btc);
+        mwgpu::launch_tc_oper_forms(o->op, p_ni, (int)node, p_btc, ctx->stream);
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        o->op.btc = p_btc;
+    }
     *out = o;
     return MWGPU_OK;
 }
@@ -1073,7 +1110,8 @@ mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tr, const doubl
     const size_t nc = 8 * (size_t)tr->mra.kp1_d;
     MW_CK(cudaMemcpyAsync(t.coefs, coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
     launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
-    ctx->launches++;
+    mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
+    ctx->launches += 1 + (t.tc32 ? 1 : 0);
     if (norms) {
         MW_CK(cudaMemcpyAsync(t.norms, norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
     } else {
@@ -1336,7 +1374,7 @@ void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
     if (reduce) launch_stamp(pl->d_stamps + 1, st);
     else cudaEventRecord(pl->e1, st);
     launch_items(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_chunks, pl->grid, pl->d_items, pl->d_partial, pl->d_err,
-                 pl->d_nchunks, pl->d_counter, st);
+                 pl->d_nchunks, pl->d_counter, pl->d_counter + 1, st);
     if (reduce) launch_reduce_chunks(o->mra, pl->d_gs, pl->d_wtree, pl->d_work, pl->n, pl->d_chunk_begin, pl->d_partial, st);
     ctx->launches += 6 + (reduce ? 2 : 0);
 }
@@ -1555,7 +1593,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
             (s = plan_alloc(ctx, pl, &pl->d_coff, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_cscan, pl->cscan_n)) ||
             (s = plan_alloc(ctx, pl, &pl->d_items, pl->items_cap)) || (s = plan_alloc(ctx, pl, &pl->d_chunks, pl->chunks_cap)) ||
             (s = plan_alloc(ctx, pl, &pl->d_chunk_begin, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_nchunks, 1)) ||
-            (s = plan_alloc(ctx, pl, &pl->d_counter, 1)) ||
+            (s = plan_alloc(ctx, pl, &pl->d_counter, 2)) ||
             (s = plan_alloc(ctx, pl, &pl->d_partial, (size_t)pl->chunks_cap * 8 * o->mra.kp1_d)))
             return fail(s);
         if (term_order_supported(o->op.n_terms) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
@@ -1829,7 +1867,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
         b.chunks = c.take<int4>(mixed ? max_chunks : 1);
         b.chunk_begin = c.take<int>(max_level + 1);
         b.nchunks = c.take<int>(1);
-        b.counter = c.take<int>(1);
+        b.counter = c.take<int>(2);  // CUDA-core and tensor-core chunk counters
         b.items = c.take<WorkItem>(mixed ? max_items : 1);
         b.items_cm = c.take<WorkItem>(mixed && order ? max_items : 1);
         b.partial = c.take<double>(mixed ? (size_t)max_chunks * 8 * m.kp1_d : 1);
@@ -1898,7 +1936,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             if (order) launch_order_terms(b.goff, nl, b.items_cm, b.items, T, ctx->d_err, st, b.nwork);
             MW_CK(cudaMemsetAsync(b.counter, 0, sizeof(int), st));
             launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,
-                         st);
+                         b.counter + 1, st);
             launch_reduce_chunks(m, ctx->d_gs, ctx->d_wtree, b.work, nl, b.chunk_begin, b.partial, st, b.nwork);
             launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, b.goff, b.node_terms, st);  // sNorm: level 0 only
             ctx->launches += 17 + (order ? 1 : 0);

@@ -65,6 +65,11 @@ struct DevOper {
     // (prod_d norm_max(l_d) * fm^3, FP32 rounded up); pair_bound_off[d] = -1: none
     const float *pair_bound;
     const int *pair_bound_off;  // [max_rows]
+    // K = 8: per operator node (and a zero record after the last) the B
+    // operands of the tensor-core contraction (k_tc.cu), TF32 hi and lo parts,
+    // with the blocks outside the band zeroed; null otherwise
+    const float *btc;
+    int n_nodes;
 };
 
 struct DevTree {
@@ -77,6 +82,8 @@ struct DevTree {
     int *child0;                 // [cap_real] first child id or -1
     float *coefs32;              // input trees: FP32 copy of coefs (mixed form)
     float *gcoefs32;             // input trees: FP32 copy of gcoefs
+    float *tc32;                 // K = 8 input trees: TF32 hi / lo of every node in the tensor-core layout (k_tc.cu)
+    float *gtc32;                // K = 8 input trees: the same for the scaling block of every GenNode
     uint64_t *hkeys;             // [hcap]
     int *hvals;                  // [hcap]
     int hcap;                    // power of two
@@ -127,7 +134,7 @@ __device__ inline bool hash_insert(uint64_t *keys, int *vals, int hcap, uint64_t
 }
 
 // error flags written by kernels (host reads them after each phase)
-enum DevError { DE_LOOKUP = 1, DE_HASH_FULL = 2, DE_POOL_FULL = 4, DE_RANGE = 8 };
+enum DevError { DE_LOOKUP = 1, DE_HASH_FULL = 2, DE_POOL_FULL = 4, DE_RANGE = 8, DE_TIMEOUT = 16 };
 
 // One (output node, input node, term) triple with its contracted (ft, gt)
 // components: bit ft*8+gt of mask.  flags bit 0: the mask equals the
@@ -177,9 +184,10 @@ void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, co
 void launch_chunk_count(const long long *g_off, int n_work, long long per, int *counts, cudaStream_t s, const int *nw_dev = nullptr);
 void launch_chunk_fill(const long long *g_off, const long long *c_off, int n_work, long long per, int4 *chunks, int *chunk_begin, int cap,
                        int *n_chunks, int *err, cudaStream_t s, const int *nw_dev = nullptr);
+// tc_counter: a device int for the tensor-core kernel's chunk counter (order 7; null: CUDA cores only)
 void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                   const int4 *chunks, int n_chunks, const WorkItem *items, double *partial, int *err, const int *n_chunks_dev, int *counter,
-                  cudaStream_t s);
+                  int *tc_counter, cudaStream_t s);
 void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tree, const int *work, int n_work, const int *chunk_begin,
                           const double *partial, cudaStream_t s, const int *nw_dev = nullptr);
 // CTAs of the contraction kernel of order K resident on one SM (0 if unknown)
@@ -194,7 +202,7 @@ void launch_order_terms(const long long *g_off, int n_work, const WorkItem *in, 
                         const int *nw_dev = nullptr);
 void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                            int n_work, const int4 *chunks, int n_chunks, const int *chunk_begin, const WorkItem *items, double *partial, int *err,
-                           cudaStream_t s);
+                           int *tc_counter, cudaStream_t s);
 // copies coefficients and norms of nodes sid[j] of src to nodes did[j] of dst
 void launch_copy_nodes(const DevTree &src, const DevTree &dst, const int *sid, const int *did, int n, int nc, cudaStream_t s);
 // writes the device's nanosecond timer (usable inside CUDA graphs)
@@ -219,6 +227,32 @@ void launch_mlp_adam(float *master, float *m1, float *m2, const float *grad, __n
 void launch_mlp_to_bf16(const float *src, __nv_bfloat16 *dst, int n, cudaStream_t s);
 void launch_mlp_features(const DevMRA &m, const DevTree &f, const int4 *nodes, int n, const int *band_w, const int *terms, int rows, double ftot,
                          float *X, cudaStream_t s);
+
+// tensor-core contraction of order K = 8 (k_tc.cu)
+constexpr int kTcNodeFloats = 8192;   // tc32 per real node: hi then lo, 4096 floats each
+constexpr int kTcGenFloats = 1024;    // gtc32 per GenNode: scaling block, hi then lo
+constexpr int kTcFormFloats = 3328;   // btc per operator node
+bool tc_supported(int K);
+// element e = x + 8 (y + 8 z) of a GenNode's scaling block into its gtc32 record (hi, lo)
+__device__ inline void tc_gen_store(float *rec, int e, float v) {
+    const int x = e & 7, yz = e >> 3;
+    const int o = (x >> 2) * 256 + (yz >> 3) * 32 + (yz & 7) * 4 + (x & 3);
+    unsigned h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float hi = __uint_as_float(h);
+    rec[o] = hi;
+    rec[512 + o] = v - hi;
+}
+// layout of real nodes [first, first + n) of an input tree from its FP64 coefficients
+void launch_tc_tree_layout(const DevTree &t, int first, int n, cudaStream_t s);
+// operator forms: node_info[j] = (term, depth, l) of operator node j; writes n_nodes + 1 records
+void launch_tc_oper_forms(const DevOper &op, const int4 *node_info, int n_nodes, float *forms, cudaStream_t s);
+// chunk types: .w = 1 where every item of the chunk is a block-schedule item
+void launch_chunk_types(int4 *chunks, int n_chunks, const int *n_chunks_dev, const WorkItem *items, cudaStream_t s);
+// contraction of the type-1 chunks on the tensor cores (persistent; counter zeroed here)
+void launch_contract_tc(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
+                        const int4 *chunks, int n_chunks, const int *n_chunks_dev, const WorkItem *items, double *partial, int *err,
+                        int *counter, cudaStream_t s);
 
 // judged adaptive apply (k_judged.cu)
 void launch_keep_counts(const int *flags, int begin, int n, int *cnt, cudaStream_t s);
