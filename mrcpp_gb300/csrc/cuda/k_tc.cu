@@ -68,7 +68,7 @@ constexpr int SM_B2 = SM_B1 + 2 * B1_F * 4;
 constexpr int SM_AT = SM_B2 + 2 * B2_F * 4;
 constexpr int SM_BYTES = SM_AT + AT_BYTES;
 // TMEM columns
-constexpr int TM_S1 = 0, TM_S2 = 64, TM_G = 128, TM_COLS = 256;
+constexpr int TM_S1 = 0, TM_S2 = 128, TM_G = 176, TM_COLS = 256;  // S1: two buffers of 64 columns
 
 __host__ __device__ constexpr uint32_t idesc(int M, int N) {
     // kind::tf32: D f32 (bit 4), A and B tf32 (2 at bits 7 and 10), K-major, N >> 3 at 17, M >> 4 at 24
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ __align__(8) uint64_t bar_full[NST], bar_mma[NST], bar_s1, bar_s2, bar_b1, bar_b2, bar_end;
     __shared__ uint32_t s_tmem;
-    __shared__ int s_next, s_bad;
+    __shared__ int s_next;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes 32 quarter .. ; tile = half
     unsigned char *A0 = sm + SM_A0, *AG = sm + SM_AG, *B0 = sm + SM_B0, *B1 = sm + SM_B1, *B2 = sm + SM_B2, *AT = sm + SM_AT;
@@ -210,7 +210,6 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
         bar_init(&bar_b2);
         bar_init(&bar_end);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_bad = 0;
     }
     // zero the GenNode buffers (rows of f[2] stay zero) and the transposed
     // inputs (tile-0 rows 64-127 of k-chunks 4, 5 stay zero: U and P exist
@@ -227,11 +226,12 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
 
     // running counters (uniform over the CTA): staged items, stage-1 / stage-2 commits, B1 / B2 copies
     unsigned q = 0, n1 = 0, n2 = 0, nb1 = 0, nb2 = 0;
-    bool bad = false;
+    // lbad: this thread saw a wait expire; bad: some thread did (CTA-uniform,
+    // refreshed with __syncthreads_or, the only value control flow uses)
+    bool lbad = false, bad = false;
     auto fail = [&]() {
         atomicOr(err, DE_TIMEOUT);
-        s_bad = 1;
-        bad = true;
+        lbad = true;
     };
 
     for (int cix = blockIdx.x; cix < n_chunks && !bad;) {
@@ -244,15 +244,18 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
             const DevTree &f = fs[tree];
             const int cap_real = f.cap_real;
             const int it0 = ch.y, n = ch.z - ch.y;
-            float acc[16], cmp[16];
+            // thread: row r = 32 quarter + lane of tile `half` in every stage
+            const int r = 32 * quarter + lane;
+            float s1[32], s2[32], acc[16], cmp[16];
+#pragma unroll
+            for (int j = 0; j < 32; j++) s1[j] = s2[j] = 0.f;
 #pragma unroll
             for (int j = 0; j < 16; j++) acc[j] = cmp[j] = 0.f;
             // thread 0: stage item j of this chunk (global index q + j) into buffer (q + j) % NST
             auto fetch = [&](int j) {
                 const WorkItem it = items[it0 + j];
                 const int b = (int)((q + (unsigned)j) % NST);
-                uint32_t bytes = 4 * 2 * B0_F;
-                expect_tx(&bar_full[b], (it.fid < cap_real ? (uint32_t)A0_BYTES : 4096u) + bytes);
+                expect_tx(&bar_full[b], (it.fid < cap_real ? (uint32_t)A0_BYTES : 4096u) + 4u * 2 * B0_F);
                 if (it.fid < cap_real) {
                     const float *src = f.tc32 + (size_t)it.fid * kTcNodeFloats;
                     bulk(A0 + b * A0_BYTES, src, A0_HALF, &bar_full[b]);
@@ -270,182 +273,191 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
             };
             if (tid == 0)
                 for (int j = 0; j < NST - 1 && j < n; j++) fetch(j);
-            bool t1_init = false;  // S1 tile 1 written in the current S1 group (GenNode items write tile 0 only)
-            bool s1_open = false, s2_open = false;
-            WorkItem prev{};
-            for (int k = 0; k < n && !bad; k++) {
-                const WorkItem item = items[it0 + k];
-                const bool has_next = k + 1 < n;
-                WorkItem nx = item;
-                if (has_next) nx = items[it0 + k + 1];
-                const bool s1_first = !(k > 0 && same_s1(prev, item)), s1_last = !(has_next && same_s1(item, nx));
-                const bool s2_first = !(k > 0 && same_s2(prev, item)), s2_last = !(has_next && same_s2(item, nx));
-                const bool gen = item.fid >= cap_real;
-                const unsigned b = (q + (unsigned)k) % NST, ph = ((q + (unsigned)k) / NST) & 1u;
-                if (s1_first) {
-                    t1_init = false;
-                    s1_open = false;
-                }
-                if (s2_first) s2_open = false;
-                // stage 0 of item k
-                if (tid == 0) {
+            WorkItem prev{}, cur{};
+            // iteration k issues the x step of item k (TMEM buffer (q + k) & 1) and
+            // drains item k - 1 into the register sums s1 (then the y and z steps
+            // at the ends of its groups), so that the tensor core works on item k
+            // while the threads read item k - 1
+            for (int k = 0; k <= n && !bad; k++) {
+                if (k < n && tid == 0) {
+                    const WorkItem item = items[it0 + k];
+                    const unsigned b = (q + (unsigned)k) % NST, ph = ((q + (unsigned)k) / NST) & 1u;
+                    const uint32_t d = tmem + TM_S1 + 64 * ((q + (unsigned)k) & 1u);
                     if (!bar_wait(&bar_full[b], ph)) fail();
                     fence_after();
-                    const uint32_t idn = idesc(128, 32);
-                    if (!bad) {
-                    const uint32_t b_h = su32(B0 + b * 2 * B0_F * 4), b_l = b_h + B0_F * 4;
-                    if (gen) {
-                        const uint32_t a_h = su32(AG + b * AG_BYTES), a_l = a_h + A0_REG;
-                        mma3(tmem + TM_S1, sdesc(a_h, A0_LBO, A0_SBO), sdesc(a_l, A0_LBO, A0_SBO), sdesc(b_h, B_LBO, B_SBO),
-                             sdesc(b_l, B_LBO, B_SBO), idn, s1_open ? 1u : 0u);
-                    } else {
-                        const uint32_t a_h = su32(A0 + b * A0_BYTES), a_l = a_h + A0_HALF;
+                    if (!lbad) {
+                        const uint32_t idn = idesc(128, 32);
+                        const uint32_t b_h = su32(B0 + b * 2 * B0_F * 4), b_l = b_h + B0_F * 4;
+                        if (item.fid >= cap_real) {
+                            const uint32_t a_h = su32(AG + b * AG_BYTES), a_l = a_h + A0_REG;
+                            mma3(d, sdesc(a_h, A0_LBO, A0_SBO), sdesc(a_l, A0_LBO, A0_SBO), sdesc(b_h, B_LBO, B_SBO), sdesc(b_l, B_LBO, B_SBO), idn, 0u);
+                        } else {
+                            const uint32_t a_h = su32(A0 + b * A0_BYTES), a_l = a_h + A0_HALF;
 #pragma unroll
-                        for (int t = 0; t < 2; t++) {
-                            const bool init = t == 0 ? s1_open : t1_init;
+                            for (int t = 0; t < 2; t++)
 #pragma unroll
-                            for (int s = 0; s < 2; s++) {
-                                const uint32_t ao = (2 * t + s) * A0_REG, bo = s * 4 * 256;
-                                mma3(tmem + TM_S1 + 32 * t, sdesc(a_h + ao, A0_LBO, A0_SBO), sdesc(a_l + ao, A0_LBO, A0_SBO),
-                                     sdesc(b_h + bo, B_LBO, B_SBO), sdesc(b_l + bo, B_LBO, B_SBO), idn, (init || s > 0) ? 1u : 0u);
-                            }
+                                for (int s = 0; s < 2; s++) {
+                                    const uint32_t ao = (2 * t + s) * A0_REG, bo = s * 4 * 256;
+                                    mma3(d + 32 * t, sdesc(a_h + ao, A0_LBO, A0_SBO), sdesc(a_l + ao, A0_LBO, A0_SBO), sdesc(b_h + bo, B_LBO, B_SBO),
+                                         sdesc(b_l + bo, B_LBO, B_SBO), idn, s > 0 ? 1u : 0u);
+                                }
                         }
-                    }
                     }
                     commit(&bar_mma[b]);  // also after a failed wait, so that the waiters below are released
                     // refill: item k + NST - 1 goes to the buffer of item k - 1, free once its products are done
-                    if (k + NST - 1 < n && !bad) {
-                        const unsigned qp = q + (unsigned)k - 1u;  // previous occupant (q + k >= 1 whenever k + NST - 1 >= NST - 1)
+                    if (k + NST - 1 < n && !lbad) {
+                        const unsigned qp = q + (unsigned)k - 1u;
                         if (q + (unsigned)k >= 1u && !bar_wait(&bar_mma[qp % NST], (qp / NST) & 1u)) fail();
-                        if (!bad) fetch(k + NST - 1);
+                        if (!lbad) fetch(k + NST - 1);
                     }
                 }
-                s1_open = true;
-                if (!gen) t1_init = true;
-                prev = item;
-                if (!s1_last) continue;
-                // ---- S1 group complete: stage 1 ----
-                if (!bar_wait(&bar_mma[b], ph)) fail();           // S1 written
-                if (n1 > 0 && !bar_wait(&bar_s1, (n1 - 1) & 1u)) fail();  // A1 / B1 free (previous stage 1 done)
-                fence_after();
-                if (tid == 0) {
-                    const float *form = op.btc + (size_t)oper_node(op, item.term, depth, item.tl[1]) * kTcFormFloats;
-                    expect_tx(&bar_b1, 2 * B1_F * 4);
-                    bulk(B1, form + F_B1H, 2 * B1_F * 4, &bar_b1);
-                }
+                if (k == 0) continue;
+                // ---- drain item j = k - 1 ----
+                const int j = k - 1;
+                prev = cur;
+                cur = items[it0 + j];
+                const bool has_next = j + 1 < n;
+                WorkItem nx = cur;
+                if (has_next) nx = items[it0 + j + 1];
+                const bool s1_first = !(j > 0 && same_s1(prev, cur)), s1_last = !(has_next && same_s1(cur, nx));
+                const bool s2_first = !(j > 0 && same_s2(prev, cur)), s2_last = !(has_next && same_s2(cur, nx));
+                if (s1_first)
+#pragma unroll
+                    for (int i = 0; i < 32; i++) s1[i] = 0.f;
+                if (s2_first)
+#pragma unroll
+                    for (int i = 0; i < 32; i++) s2[i] = 0.f;
                 {
-                    // thread: S1 tile t = half (b2 = t), row r = (b1, y, z)
-                    const int t = half, r = 32 * quarter + lane, b1 = r >> 6, y = r & 7, z = (r >> 3) & 7;
-                    float v[32];
-                    if (t == 0 || t1_init) tmem_ld<32>(tmem + lane_base + TM_S1 + 32 * t, v);
-                    else
+                    const unsigned qj = q + (unsigned)j;
+                    if (!bar_wait(&bar_mma[qj % NST], (qj / NST) & 1u)) fail();
+                    fence_after();
+                    if (half == 0 || cur.fid < cap_real) {  // GenNode items write tile 0 only
+                        float v[32];
+                        tmem_ld<32>(tmem + lane_base + TM_S1 + 64 * (qj & 1u) + 32 * half, v);
 #pragma unroll
-                        for (int i = 0; i < 32; i++) v[i] = 0.f;
-                    const bool u = pure && t == 0 && b1 == 0;
-#pragma unroll
-                    for (int xo = 0; xo < 8; xo++) {
-                        const float y0 = u ? v[xo] : v[xo] + v[16 + xo];
-                        at_store(AT, t, 8 * z + xo, 8 * b1 + y, y0);
-                        at_store(AT, t, 64 + 8 * z + xo, 8 * b1 + y, v[8 + xo]);
-                        if (u) at_store(AT, 0, 8 * z + xo, 16 + y, v[16 + xo]);
+                        for (int i = 0; i < 32; i++) s1[i] += v[i];
                     }
                 }
-                fence_async_smem();
-                fence_before();
-                __syncthreads();
-                if (s_bad) bad = true;
-                if (tid == 0 && !bad) {
-                    fence_after();
-                    if (!bar_wait(&bar_b1, nb1 & 1u)) fail();
-                    const uint32_t a_h = su32(AT), a_l = a_h + AT_HALF, b_h = su32(B1), b_l = b_h + B1_F * 4;
+                if (s1_last) {
+                    // ---- S1 group complete: stage 1 ----
+                    if (n1 > 0 && !bar_wait(&bar_s1, (n1 - 1) & 1u)) fail();  // A1 / B1 free (previous stage 1 done)
+                    if (n2 > 0 && !bar_wait(&bar_s2, (n2 - 1) & 1u)) fail();  // (A2 aliases A1)
+                    if (tid == 0) {
+                        const float *form = op.btc + (size_t)oper_node(op, cur.term, depth, cur.tl[1]) * kTcFormFloats;
+                        expect_tx(&bar_b1, 2 * B1_F * 4);
+                        bulk(B1, form + F_B1H, 2 * B1_F * 4, &bar_b1);
+                    }
+                    {
+                        // S1 tile t = half (b2 = t), row r = (b1, y, z)
+                        const int t = half, b1 = r >> 6, y = r & 7, z = (r >> 3) & 7;
+                        const bool u = pure && t == 0 && b1 == 0;
 #pragma unroll
-                    for (int t = 0; t < 2; t++) {
-                        const int nks = (t == 0 && pure) ? 3 : 2;
-                        const uint32_t idn = idesc(128, t == 0 ? 32 : 16);
-                        for (int s = 0; s < nks; s++) {
-                            const uint32_t ao = (t ? AT_T0 : 0) + s * 2 * AT_LBO, bo = s * 4 * 256;
-                            mma3(tmem + TM_S2 + 32 * t, sdesc(a_h + ao, AT_LBO, AT_SBO), sdesc(a_l + ao, AT_LBO, AT_SBO), sdesc(b_h + bo, B_LBO, B_SBO),
-                                 sdesc(b_l + bo, B_LBO, B_SBO), idn, (s2_open || s > 0) ? 1u : 0u);
+                        for (int xo = 0; xo < 8; xo++) {
+                            at_store(AT, t, 8 * z + xo, 8 * b1 + y, u ? s1[xo] : s1[xo] + s1[16 + xo]);
+                            at_store(AT, t, 64 + 8 * z + xo, 8 * b1 + y, s1[8 + xo]);
+                            if (u) at_store(AT, 0, 8 * z + xo, 16 + y, s1[16 + xo]);
                         }
                     }
-                    commit(&bar_s1);
-                }
-                nb1++;
-                n1++;
-                s2_open = true;
-                if (!s2_last || bad) continue;
-                // ---- S2 group complete: stage 2 ----
-                if (!bar_wait(&bar_s1, (n1 - 1) & 1u)) fail();  // S2 written, A1 free
-                fence_after();
-                if (tid == 0) {
-                    const float *form = op.btc + (size_t)oper_node(op, item.term, depth, item.tl[2]) * kTcFormFloats;
-                    expect_tx(&bar_b2, 2 * B2_F * 4);
-                    bulk(B2, form + F_B2H, 2 * B2_F * 4, &bar_b2);
-                }
-                {
-                    // thread: S2 tile t = half (b2 = t), row r = (a0, z, x')
-                    const int t = half, r = 32 * quarter + lane, a0 = r >> 6, xo = r & 7, z = (r >> 3) & 7;
-                    float v[32];
-                    if (t == 0) tmem_ld<32>(tmem + lane_base + TM_S2, v);
-                    else {
-                        float w16[16];
-                        tmem_ld<16>(tmem + lane_base + TM_S2 + 32, w16);
+                    fence_async_smem();
+                    fence_before();
+                    bad = __syncthreads_or(lbad) != 0 || bad;
+                    if (tid == 0 && !bad) {
+                        fence_after();
+                        if (!bar_wait(&bar_b1, nb1 & 1u)) fail();
+                        const uint32_t a_h = su32(AT), a_l = a_h + AT_HALF, b_h = su32(B1), b_l = b_h + B1_F * 4;
 #pragma unroll
-                        for (int i = 0; i < 16; i++) v[i] = w16[i];
-#pragma unroll
-                        for (int i = 16; i < 32; i++) v[i] = 0.f;
-                    }
-                    const bool p = pure && t == 0 && a0 == 0;
-#pragma unroll
-                    for (int yo = 0; yo < 8; yo++) {
-                        at_store(AT, a0, 8 * yo + xo, 8 * t + z, v[yo]);
-                        at_store(AT, a0, 64 + 8 * yo + xo, 8 * t + z, v[8 + yo]);
-                        if (p) at_store(AT, 0, 8 * yo + xo, 16 + z, v[16 + yo]);
-                    }
-                }
-                fence_async_smem();
-                fence_before();
-                __syncthreads();
-                if (s_bad) bad = true;
-                if (tid == 0 && !bad) {
-                    fence_after();
-                    if (!bar_wait(&bar_b2, nb2 & 1u)) fail();
-                    const uint32_t a_h = su32(AT), a_l = a_h + AT_HALF, b_h = su32(B2), b_l = b_h + B2_F * 4;
-                    const uint32_t idn = idesc(128, 16);
-#pragma unroll
-                    for (int t = 0; t < 2; t++) {
-                        const int nks = (t == 0 && pure) ? 3 : 2;
-                        for (int s = 0; s < nks; s++) {
-                            const uint32_t ao = (t ? AT_T0 : 0) + s * 2 * AT_LBO, bo = s * 2 * 256;
-                            mma3(tmem + TM_G + 16 * t, sdesc(a_h + ao, AT_LBO, AT_SBO), sdesc(a_l + ao, AT_LBO, AT_SBO), sdesc(b_h + bo, B_LBO, B_SBO),
-                                 sdesc(b_l + bo, B_LBO, B_SBO), idn, s > 0 ? 1u : 0u);
+                        for (int t = 0; t < 2; t++) {
+                            const int nks = (t == 0 && pure) ? 3 : 2;
+                            const uint32_t idn = idesc(128, t == 0 ? 32 : 16);
+                            for (int s = 0; s < nks; s++) {
+                                const uint32_t ao = (t ? AT_T0 : 0) + s * 2 * AT_LBO, bo = s * 4 * 256;
+                                mma3(tmem + TM_S2 + 32 * t, sdesc(a_h + ao, AT_LBO, AT_SBO), sdesc(a_l + ao, AT_LBO, AT_SBO), sdesc(b_h + bo, B_LBO, B_SBO),
+                                     sdesc(b_l + bo, B_LBO, B_SBO), idn, s > 0 ? 1u : 0u);
+                            }
                         }
                     }
-                    commit(&bar_s2);
-                }
-                nb2++;
-                n2++;
-                if (bad) continue;
-                if (!bar_wait(&bar_s2, (n2 - 1) & 1u)) fail();
-                fence_after();
-                {
-                    // thread: g tile t = half (a0 = t), row r = (a1, y', x'); columns (a2, z')
-                    float v[16];
-                    tmem_ld<16>(tmem + lane_base + TM_G + 16 * half, v);
+                    if (tid == 0) commit(&bar_s1);
+                    nb1++;
+                    n1++;
+                    // drain the stage-1 products into the register sums s2
+                    if (!bar_wait(&bar_s1, (n1 - 1) & 1u)) fail();
+                    fence_after();
+                    {
+                        if (half == 0) {
+                            float v[32];
+                            tmem_ld<32>(tmem + lane_base + TM_S2, v);
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const float yv = v[j] - cmp[j];
-                        const float tv = acc[j] + yv;
-                        cmp[j] = (tv - acc[j]) - yv;
-                        acc[j] = tv;
+                            for (int i = 0; i < 32; i++) s2[i] += v[i];
+                        } else {
+                            float v[16];
+                            tmem_ld<16>(tmem + lane_base + TM_S2 + 32, v);
+#pragma unroll
+                            for (int i = 0; i < 16; i++) s2[i] += v[i];
+                        }
+                    }
+                    if (s2_last && !bad) {
+                        // ---- S2 group complete: stage 2 ----
+                        if (tid == 0) {
+                            const float *form = op.btc + (size_t)oper_node(op, cur.term, depth, cur.tl[2]) * kTcFormFloats;
+                            expect_tx(&bar_b2, 2 * B2_F * 4);
+                            bulk(B2, form + F_B2H, 2 * B2_F * 4, &bar_b2);
+                        }
+                        {
+                            // S2 tile t = half (b2 = t), row r = (a0, z, x')
+                            const int t = half, a0 = r >> 6, xo = r & 7, z = (r >> 3) & 7;
+                            const bool p = pure && t == 0 && a0 == 0;
+#pragma unroll
+                            for (int yo = 0; yo < 8; yo++) {
+                                at_store(AT, a0, 8 * yo + xo, 8 * t + z, s2[yo]);
+                                at_store(AT, a0, 64 + 8 * yo + xo, 8 * t + z, s2[8 + yo]);
+                                if (p) at_store(AT, 0, 8 * yo + xo, 16 + z, s2[16 + yo]);
+                            }
+                        }
+                        fence_async_smem();
+                        fence_before();
+                        bad = __syncthreads_or(lbad) != 0 || bad;
+                        if (tid == 0 && !bad) {
+                            fence_after();
+                            if (!bar_wait(&bar_b2, nb2 & 1u)) fail();
+                            const uint32_t a_h = su32(AT), a_l = a_h + AT_HALF, b_h = su32(B2), b_l = b_h + B2_F * 4;
+                            const uint32_t idn = idesc(128, 16);
+#pragma unroll
+                            for (int t = 0; t < 2; t++) {
+                                const int nks = (t == 0 && pure) ? 3 : 2;
+                                for (int s = 0; s < nks; s++) {
+                                    const uint32_t ao = (t ? AT_T0 : 0) + s * 2 * AT_LBO, bo = s * 2 * 256;
+                                    mma3(tmem + TM_G + 16 * t, sdesc(a_h + ao, AT_LBO, AT_SBO), sdesc(a_l + ao, AT_LBO, AT_SBO),
+                                         sdesc(b_h + bo, B_LBO, B_SBO), sdesc(b_l + bo, B_LBO, B_SBO), idn, s > 0 ? 1u : 0u);
+                                }
+                            }
+                        }
+                        if (tid == 0) commit(&bar_s2);
+                        nb2++;
+                        n2++;
+                        if (!bar_wait(&bar_s2, (n2 - 1) & 1u)) fail();
+                        fence_after();
+                        {
+                            // g tile t = half (a0 = t), row r = (a1, y', x'); columns (a2, z')
+                            float v[16];
+                            tmem_ld<16>(tmem + lane_base + TM_G + 16 * half, v);
+#pragma unroll
+                            for (int i = 0; i < 16; i++) {
+                                const float yv = v[i] - cmp[i];
+                                const float tv = acc[i] + yv;
+                                cmp[i] = (tv - acc[i]) - yv;
+                                acc[i] = tv;
+                            }
+                        }
                     }
                 }
+                // every thread has read TMEM buffer (q + j) & 1 before item j + 2 is issued into it
                 fence_before();
+                bad = __syncthreads_or(lbad) != 0 || bad;
             }
             q += (unsigned)n;
             // partial of this chunk: component gt = a0 + 2 a1 + 4 a2, element x' + 8 y' + 64 z'
             {
-                const int r = 32 * quarter + lane, a0 = half, a1 = r >> 6, yo = (r >> 3) & 7, xo = r & 7;
+                const int a0 = half, a1 = r >> 6, yo = (r >> 3) & 7, xo = r & 7;
                 double *go = partial + (size_t)cix * 8 * 512;
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
@@ -454,9 +466,8 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
                 }
             }
         }
-        __syncthreads();
-        if (s_bad) bad = true;
-        if (!counter) break;
+        bad = __syncthreads_or(lbad) != 0 || bad;
+        if (!counter || bad) break;
         if (tid == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);
         __syncthreads();
         cix = s_next;

@@ -154,3 +154,34 @@ def test_helmholtz_k9_mixed_vs_fp64_and_oracle(gpu):
     # per node, relative to the largest node norm
     per_node = np.linalg.norm(a["coefs"] - b["coefs"], axis=1) / np.linalg.norm(b["coefs"], axis=1).max()
     assert per_node.max() <= MIXED_TOL
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_tcgen05_contraction_k7(gpu, monkeypatch, adaptive):
+    # the opt-in tcgen05 contraction (order 7, MWGPU_TC) against the FP64 form:
+    # same node-term count, relative L2 error <= 1e-5 per apply; on the fixed
+    # grid every item is a block-schedule item (tensor-core chunks only), the
+    # adaptive apply mixes in screened items (CUDA-core chunks)
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, 1e-4)
+    f = project(mra, 1e-4, gaussian_sum(11, 4, (1.0, 50.0), (-3.0, 3.0)))
+    grid = mw.FunctionTree(mra)
+    s0 = mw.apply(1e-4, grid, P, f, precision=mw.FP64)
+    monkeypatch.setenv("MWGPU_TC", "1")
+    g1, g2 = mw.FunctionTree(mra), mw.FunctionTree(mra)
+    if adaptive:
+        s1 = mw.apply(1e-4, g1, P, f, precision=mw.MIXED)
+        same, perm = match(g1.export(), grid.export())
+        assert same, "topology differs from the FP64 form"
+        a, b = g1.export()["coefs"], grid.export()["coefs"][perm]
+        assert s1["node_terms"] == s0["node_terms"]
+    else:
+        mw.copy_grid(g1, grid)
+        mw.copy_grid(g2, grid)
+        s1 = mw.apply(1e-4, g1, P, f, max_iter=0, precision=mw.MIXED)
+        monkeypatch.delenv("MWGPU_TC")
+        s2 = mw.apply(1e-4, g2, P, f, max_iter=0, precision=mw.FP64)
+        a, b = g1.export()["coefs"], g2.export()["coefs"]
+        assert s1["node_terms"] == s2["node_terms"]
+    assert np.isfinite(a).all()
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= MIXED_TOL
