@@ -69,6 +69,15 @@ int mwh_tree_info(const mwh_tree *tree, int *n_nodes, double *square_norm);
 int mwh_tree_export(const mwh_tree *tree, int *idx, int *child0, double *coefs, double *norms);
 /* replaces the tree with the given flat tree (same layout as export; roots first) */
 int mwh_tree_import(mwh_tree *tree, int n, const int *idx, const int *child0, const double *coefs, double square_norm);
+/* Tree files ("<file>.mwtree"): replaces FunctionTree::saveTree / loadTree
+ * (src/trees/FunctionTree.cpp:378-435), which dump the node allocator's
+ * chunks (layout-bound).  This format is flat and versioned: header (MRA:
+ * basis, order, world box, max depth; square norm; node count), then node
+ * indices, first-child indices and the compressed coefficients, parents
+ * before children, little-endian.  load requires the tree's MRA to equal the
+ * file's (as loadTree does) and replaces the tree's nodes. */
+int mwh_tree_save(const mwh_tree *tree, const char *file);
+int mwh_tree_load(mwh_tree *tree, const char *file);
 double mwh_dot(const mwh_tree *a, const mwh_tree *b);
 double mwh_evalf(const mwh_tree *tree, double x, double y, double z);
 double mwh_integrate(const mwh_tree *tree);

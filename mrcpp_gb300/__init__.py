@@ -145,6 +145,8 @@ _SIGS = {
     "mwh_tree_info": (C.c_int, [_P, _PI, _PD]),
     "mwh_tree_export": (C.c_int, [_P, _PI, _PI, _PD, _PD]),
     "mwh_tree_import": (C.c_int, [_P, C.c_int, _PI, _PI, _PD, C.c_double]),
+    "mwh_tree_save": (C.c_int, [_P, C.c_char_p]),
+    "mwh_tree_load": (C.c_int, [_P, C.c_char_p]),
     "mwh_dot": (C.c_double, [_P, _P]),
     "mwh_evalf": (C.c_double, [_P, C.c_double, C.c_double, C.c_double]),
     "mwh_integrate": (C.c_double, [_P]),
@@ -277,6 +279,14 @@ class FunctionTree:
         c0 = np.ascontiguousarray(child0, dtype=np.int32)
         coefs = np.ascontiguousarray(coefs, dtype=np.float64)
         _ck(lib().mwh_tree_import(self._h, len(c0), _pi(idx), _pi(c0), _pd(coefs), float(square_norm)))
+
+    def saveTree(self, file):
+        """FunctionTree::saveTree: writes `file` + ".mwtree" (flat, versioned layout)."""
+        _ck(lib().mwh_tree_save(self._h, os.fsencode(file)))
+
+    def loadTree(self, file):
+        """FunctionTree::loadTree: reads `file` + ".mwtree"; the tree's MRA must be the file's."""
+        _ck(lib().mwh_tree_load(self._h, os.fsencode(file)))
 
     def evalf(self, r):
         return lib().mwh_evalf(self._h, float(r[0]), float(r[1]), float(r[2]))

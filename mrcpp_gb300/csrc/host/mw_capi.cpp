@@ -10,8 +10,10 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
+#include <string>
 
 #include "../../../include/mwhost.h"
 #include "mw_host.h"
@@ -574,6 +576,90 @@ int mwh_tree_import(mwh_tree *t, int n, const int *idx, const int *child0, const
         nt->squareNorm = square_norm;
         t->t = std::move(nt);
         return 0;
+    });
+}
+
+// ---- tree files: a flat, versioned layout (FunctionTree::saveTree / loadTree,
+// FunctionTree.cpp:378-435, write the node allocator's raw chunks instead) ----
+namespace {
+const char kTreeMagic[8] = {'M', 'W', 'T', 'R', 'E', 'E', 0, 1};
+// header: magic, then int32 dimension, basis type, order, root scale, corner[3],
+// nbox[3], max depth, then double sf[3], square norm, then int64 node count;
+// body: int32 idx[n][4] (scale, l0, l1, l2), int32 child0[n], double coefs[n][8 (k+1)^3]
+// (compressed s+d form), nodes parents before children, roots first; little-endian
+struct TreeHeader {
+    int32_t dim, type, order, root_scale, corner[3], nbox[3], max_depth;
+    double sf[3], square_norm;
+    int64_t n;
+};
+std::string tree_path(const char *file) { return std::string(file) + ".mwtree"; }
+}  // namespace
+
+int mwh_tree_save(const mwh_tree *t, const char *file) {
+    return guard([&] {
+        if (!t || !file) return fail(1, "null argument");
+        const Tree<3> &tr = *t->t;
+        std::vector<int> order, ix, c0;
+        export_tree(tr, order, ix, c0);
+        const MRA<3> &m = *tr.mra;
+        TreeHeader h{};
+        h.dim = 3;
+        h.type = m.basis->type;
+        h.order = m.order();
+        h.root_scale = m.rootScale();
+        for (int d = 0; d < 3; d++) {
+            h.corner[d] = m.world.corner[d];
+            h.nbox[d] = m.world.nbox[d];
+            h.sf[d] = m.world.sf[d];
+        }
+        h.max_depth = m.maxDepth;
+        h.square_norm = tr.squareNorm;
+        h.n = (int64_t)order.size();
+        const std::string path = tree_path(file);
+        FILE *fh = std::fopen(path.c_str(), "wb");
+        if (!fh) return fail(1, "unable to open " + path + " for writing");
+        bool ok = std::fwrite(kTreeMagic, 1, 8, fh) == 8 && std::fwrite(&h, sizeof(h), 1, fh) == 1 &&
+                  std::fwrite(ix.data(), sizeof(int), ix.size(), fh) == ix.size() && std::fwrite(c0.data(), sizeof(int), c0.size(), fh) == c0.size();
+        for (size_t j = 0; ok && j < order.size(); j++) ok = std::fwrite(tr.c(order[j]), sizeof(double), tr.nCoefs, fh) == tr.nCoefs;
+        ok = (std::fclose(fh) == 0) && ok;
+        if (!ok) return fail(1, "write error on " + path);
+        return 0;
+    });
+}
+
+int mwh_tree_load(mwh_tree *t, const char *file) {
+    return guard([&] {
+        if (!t || !file) return fail(1, "null argument");
+        const std::string path = tree_path(file);
+        FILE *fh = std::fopen(path.c_str(), "rb");
+        if (!fh) return fail(1, "unable to open " + path);
+        char magic[8];
+        TreeHeader h{};
+        bool ok = std::fread(magic, 1, 8, fh) == 8 && std::memcmp(magic, kTreeMagic, 8) == 0 && std::fread(&h, sizeof(h), 1, fh) == 1;
+        if (!ok) {
+            std::fclose(fh);
+            return fail(1, path + " is not a tree file of this format");
+        }
+        // the tree must have the MRA the file was written with (loadTree's requirement)
+        const MRA<3> &m = *t->t->mra;
+        bool same = h.dim == 3 && h.type == m.basis->type && h.order == m.order() && h.root_scale == m.rootScale() && h.max_depth == m.maxDepth;
+        for (int d = 0; d < 3; d++) same = same && h.corner[d] == m.world.corner[d] && h.nbox[d] == m.world.nbox[d] && h.sf[d] == m.world.sf[d];
+        if (!same) {
+            std::fclose(fh);
+            return fail(1, "the MRA of " + path + " differs from the tree's");
+        }
+        if (h.n <= 0 || h.n > (int64_t)1 << 31) {
+            std::fclose(fh);
+            return fail(1, "invalid node count in " + path);
+        }
+        const size_t n = (size_t)h.n, nc = t->t->nCoefs;
+        std::vector<int> ix(4 * n), c0(n);
+        std::vector<double> coefs(n * nc);
+        ok = std::fread(ix.data(), sizeof(int), ix.size(), fh) == ix.size() && std::fread(c0.data(), sizeof(int), n, fh) == n &&
+             std::fread(coefs.data(), sizeof(double), coefs.size(), fh) == coefs.size();
+        std::fclose(fh);
+        if (!ok) return fail(1, path + " is truncated");
+        return mwh_tree_import(t, (int)n, ix.data(), c0.data(), coefs.data(), h.square_norm);
     });
 }
 

@@ -72,3 +72,49 @@ def test_compressed_form_is_consistent():
         if x["child0"][i] < 0:
             tot += (x["norms"][i] ** 2).sum()
     assert tot == pytest.approx(f.square_norm, rel=1e-12)
+
+
+def test_tree_file_roundtrip(tmp_path):
+    # saveTree / loadTree (FunctionTree.cpp:378-435) in the flat tree-file layout:
+    # same topology, bit-identical coefficients, square norm and values
+    mra = mw.MRA(box=(-20, 20), order=5, basis=mw.INTERPOLATING)
+    f = project(mra, 1e-4, gaussian_sum(7, 4, (1.0, 40.0), (-2.0, 2.0)))
+    path = str(tmp_path / "density")
+    f.saveTree(path)
+    assert (tmp_path / "density.mwtree").exists()
+    g = mw.FunctionTree(mra)
+    g.loadTree(path)
+    a, b = f.export(), g.export()
+    assert np.array_equal(a["idx"], b["idx"]) and np.array_equal(a["child0"], b["child0"])
+    assert np.array_equal(a["coefs"], b["coefs"])
+    assert g.square_norm == f.square_norm
+    for r in [(0.1, -0.4, 0.3), (1.5, 0.2, -1.0)]:
+        assert g.evalf(r) == f.evalf(r)
+
+
+def test_tree_file_errors(tmp_path):
+    mra = mw.MRA(box=(-20, 20), order=5, basis=mw.INTERPOLATING)
+    f = project(mra, 1e-3, unit_gaussian(5.0, (0.0, 0.0, 0.0)))
+    path = str(tmp_path / "f")
+    f.saveTree(path)
+    # another MRA (order, basis or world) is refused, like loadTree's requirement
+    for other in (mw.MRA(box=(-20, 20), order=6, basis=mw.INTERPOLATING), mw.MRA(box=(-20, 20), order=5, basis=mw.LEGENDRE),
+                  mw.MRA(box=(-32, 32), order=5, basis=mw.INTERPOLATING)):
+        with pytest.raises(mw.MWGPUError):
+            mw.FunctionTree(other).loadTree(path)
+    # missing, foreign and truncated files
+    with pytest.raises(mw.MWGPUError):
+        mw.FunctionTree(mra).loadTree(str(tmp_path / "missing"))
+    (tmp_path / "junk.mwtree").write_bytes(b"not a tree file at all")
+    with pytest.raises(mw.MWGPUError):
+        mw.FunctionTree(mra).loadTree(str(tmp_path / "junk"))
+    data = (tmp_path / "f.mwtree").read_bytes()
+    (tmp_path / "cut.mwtree").write_bytes(data[: len(data) // 2])
+    with pytest.raises(mw.MWGPUError):
+        mw.FunctionTree(mra).loadTree(str(tmp_path / "cut"))
+    # a tree that failed to load keeps its nodes
+    h = project(mra, 1e-3, unit_gaussian(5.0, (0.0, 0.0, 0.0)))
+    n0 = h.n_nodes
+    with pytest.raises(mw.MWGPUError):
+        h.loadTree(str(tmp_path / "cut"))
+    assert h.n_nodes == n0
