@@ -161,6 +161,17 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tre
  * MWTree.cpp:166-181). */
 mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tree, int direction, int overwrite);
 
+/* Derivative level: replaces DerivativeCalculator::calcNodeVector
+ * (src/treebuilders/DerivativeCalculator.cpp:113-151) for the output end nodes
+ * node_ix[0..n) of `out` (a grid made by CopyAdaptor, CopyAdaptor.cpp:55-71):
+ * per node the input nodes within the operator band along `dir` (GenNodes made
+ * as needed), the 1D application of the one-term derivative operator along dir
+ * with the identity in the other directions, division by sf^order, node norms.
+ * FP64 in every precision mode.  The caller then runs the BottomUp transform
+ * (apply.cpp:379-412). */
+mwgpu_status mwgpu_apply_derivative(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n, int dir,
+                                    int order, mwgpu_level_stats *stats);
+
 /* Batched level: one TreeBuilder iteration of n_trees independent applies of
  * the same operator (the loop over functions that calls mrcpp::apply once per
  * function, apply.cpp:68-93), computed by one work list and one contraction

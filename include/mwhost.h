@@ -84,6 +84,10 @@ double mwh_integrate(const mwh_tree *tree);
 
 int mwh_poisson(const mwh_mra *mra, double prec, mwh_oper **out);
 int mwh_helmholtz(const mwh_mra *mra, double mu, double prec, mwh_oper **out);
+/* ABGVOperator(mra, a, b) (src/operators/ABGVOperator.cpp:45-71): first
+ * derivative; a = b = 0 center difference (band 0), a = b = 0.5 central
+ * difference (band 1). */
+int mwh_abgv(const mwh_mra *mra, double a, double b, mwh_oper **out);
 void mwh_oper_free(mwh_oper *oper);
 /* number of terms, total operator nodes, total (term, depth) rows */
 int mwh_oper_info(const mwh_oper *oper, int *n_terms, int *n_nodes, int *n_rows);
@@ -99,6 +103,11 @@ int mwh_helmholtz_kernel(double mu, double eps, double r_min, double r_max, int 
 
 /* mrcpp::apply on the GPU: precision = MWGPU_PREC_FP64 or MWGPU_PREC_MIXED. */
 int mwh_apply(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int max_iter, int abs_prec, int precision, mwh_apply_stats *stats);
+/* apply(out, DerivativeOperator, inp, dir) (src/treebuilders/apply.cpp:379-412):
+ * out must hold only its root nodes; its grid becomes the input grid widened
+ * by the operator band along dir (CopyAdaptor), the end nodes are computed on
+ * the device (mwgpu_apply_derivative, FP64), then BottomUp. */
+int mwh_apply_derivative(mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int dir, mwh_apply_stats *stats);
 /* n independent applies of one operator, outs[t] = oper(inps[t]) (the loop over
  * functions around mrcpp::apply, apply.h:41), advanced in lockstep: each
  * TreeBuilder iteration of all trees is one mwgpu_apply_level_batch call and

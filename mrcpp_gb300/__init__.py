@@ -100,6 +100,7 @@ _SIGS = {
     "mwgpu_tree_size": (C.c_int, [_P, _PI]),
     "mwgpu_free_tree": (C.c_int, [_P, _P]),
     "mwgpu_apply_level": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_double, C.c_double, _PD, C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_apply_derivative": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_int, C.c_int, C.POINTER(MwgpuLevelStats)]),
     "mwgpu_transform": (C.c_int, [_P, _P, C.c_int, C.c_int]),
     "mwgpu_apply_level_batch": (C.c_int, [_P, _P, C.c_int, C.POINTER(_P), C.POINTER(_P), _PI, _PI, C.c_int, C.c_double, _PD, _PD,
                                           C.POINTER(MwgpuLevelStats)]),
@@ -152,6 +153,8 @@ _SIGS = {
     "mwh_integrate": (C.c_double, [_P]),
     "mwh_poisson": (C.c_int, [_P, C.c_double, C.POINTER(_P)]),
     "mwh_helmholtz": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(_P)]),
+    "mwh_abgv": (C.c_int, [_P, C.c_double, C.c_double, C.POINTER(_P)]),
+    "mwh_apply_derivative": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwh_oper_free": (None, [_P]),
     "mwh_oper_info": (C.c_int, [_P, _PI, _PI, _PI]),
     "mwh_oper_export": (C.c_int, [_P, _PI, _PI, _PD, _PD, _PD, _PD]),
@@ -381,6 +384,18 @@ class HelmholtzOperator(ConvolutionOperator):
         self.mu = mu
 
 
+class ABGVOperator(ConvolutionOperator):
+    """ABGVOperator(MRA, a, b): first derivative with boundary parameters a, b
+    (src/operators/ABGVOperator.cpp:45-71); a = b = 0.5 central difference,
+    a = b = 0 center difference."""
+
+    def __init__(self, mra, a, b):
+        h = _P()
+        _ck(lib().mwh_abgv(mra._h, float(a), float(b), C.byref(h)))
+        super().__init__(mra, h)
+        self.a, self.b = a, b
+
+
 def _kernel(fn, *args):
     n = fn(*args, 0, None, None)
     if n < 0:
@@ -401,10 +416,26 @@ def helmholtz_kernel(mu, eps, r_min, r_max):
     return _kernel(lib().mwh_helmholtz_kernel, float(mu), float(eps), float(r_min), float(r_max))
 
 
-def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64):
-    """mrcpp::apply(prec, out, oper, inp, maxIter, absPrec) on the GPU; returns the apply statistics."""
+def apply(*args, **kw):
+    """mrcpp::apply on the GPU, returning the apply statistics:
+    apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64) for a
+    convolution operator, apply(out, oper, inp, dir) for a derivative operator
+    (ABGVOperator; output grid = input grid widened along dir, FP64)."""
+    if args and isinstance(args[0], FunctionTree):
+        return apply_derivative(*args, **kw)
+    return _apply_convolution(*args, **kw)
+
+
+def _apply_convolution(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64):
     st = MwhApplyStats()
     _ck(lib().mwh_apply(float(prec), out._h, oper._h, inp._h, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
+    return st.as_dict()
+
+
+def apply_derivative(out, oper, inp, dir):
+    """apply(out, DerivativeOperator, inp, dir) (src/treebuilders/apply.cpp:379-412)."""
+    st = MwhApplyStats()
+    _ck(lib().mwh_apply_derivative(out._h, oper._h, inp._h, int(dir), C.byref(st)))
     return st.as_dict()
 
 

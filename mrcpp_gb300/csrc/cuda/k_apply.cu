@@ -42,14 +42,16 @@ struct Box {
 __device__ inline bool band_box(const DevMRA &m, const DevOper &op, int4 g, int &depth, Box &b) {
     depth = g.x - m.root_scale;
     int w = (depth >= 0 && depth < op.n_band_max) ? op.band_max[depth] : -1;
+    if (op.band_dir >= 0) w = op.band_dir_w;  // derivative: one direction
     if (w < 0) return false;
     int gl[3] = {g.y, g.z, g.w};
     b.total = 1;
     for (int d = 0; d < 3; d++) {
         int nboxes = m.nbox[d] * (1 << depth);
         int c = m.corner[d] * (1 << depth);
-        b.s[d] = max(gl[d] - w, c);
-        b.e[d] = min(gl[d] + w, c + nboxes - 1);
+        const int wd = (op.band_dir < 0 || op.band_dir == d) ? w : 0;
+        b.s[d] = max(gl[d] - wd, c);
+        b.e[d] = min(gl[d] + wd, c + nboxes - 1);
         b.total *= (b.e[d] - b.s[d] + 1);
     }
     return b.total > 0;
@@ -217,7 +219,122 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
     }
 }
 
+
+// DerivativeCalculator::calcNode(gNode) (DerivativeCalculator.cpp:113-151) for
+// one output node per CTA: the band along dir (makeOperBand :153-176), per
+// (f, ft, gt) the checks of applyOperator (:199-241: the component's band width
+// in every direction, the identity -- T or A block at l = 0 -- off the apply
+// direction), the 1D application along dir (tensorApplyOperComp :245-268 with
+// identity factors), division by sf^order and the node norms.  FP64.
+__global__ void __launch_bounds__(256) k_deriv(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work, int order,
+                                               LevelStats *stats, int *err) {
+    extern __shared__ double sm[];
+    const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    const int dir = op.band_dir, width = op.band_dir_w;
+    double *acc = sm;
+    __shared__ double red[8][8];
+    const int gi = work[blockIdx.x];
+    const int4 gx = g.idx[gi];
+    const int depth = gx.x - m.root_scale;
+    for (int e = tid; e < 8 * K3; e += nthr) acc[e] = 0.0;
+    __syncthreads();
+    unsigned long long nt = 0, nc = 0, nb = 0;
+    if (depth >= 0 && depth < op.max_rows && dir >= 0 && dir < 3) {
+        const int gl[3] = {gx.y, gx.z, gx.w};
+        const int *bw = op.bw + (size_t)depth * 5;  // term 0
+        const int off = op.dep_off[depth], L0 = op.dep_L[depth];
+        for (int w = -width; w <= width; w++) {
+            int fl[3] = {gl[0], gl[1], gl[2]};
+            fl[dir] += w;
+            const int c0 = m.corner[dir] * (1 << depth), nbx = m.nbox[dir] * (1 << depth);
+            if (fl[dir] < c0 || fl[dir] >= c0 + nbx) continue;  // outside the world (getRootIndex < 0)
+            uint64_t key;
+            if (!pack_key(m, gx.x, fl[0], fl[1], fl[2], key)) {
+                if (tid == 0) atomicOr(err, DE_RANGE);
+                continue;
+            }
+            const int fid = hash_find(f.hkeys, f.hvals, f.hcap, key);
+            if (fid < 0) {
+                if (tid == 0) atomicOr(err, DE_LOOKUP);
+                continue;
+            }
+            nb++;
+            const bool gen = fid >= f.cap_real;
+            const double *fc = gen ? f.gcoefs + (size_t)(fid - f.cap_real) * K3 : f.coefs + (size_t)fid * 8 * K3;
+            const double *fn = f.norms + (size_t)fid * 8;
+            bool any = false;
+            for (int ft = 0; ft < 8; ft++) {
+                if (fn[ft] < kMachineZero || (gen && ft > 0)) continue;
+                for (int gt = 0; gt < 8; gt++) {
+                    bool ok = true;
+                    int oi_dir = 0;
+                    for (int d = 0; d < 3; d++) {
+                        const int oi = 2 * ((gt >> d) & 1) + ((ft >> d) & 1);
+                        const int l = d == dir ? w : 0;
+                        if (abs(l) > bw[oi]) { ok = false; break; }
+                        if (d == dir) oi_dir = oi;
+                        else if (!(oi == 0 || oi == 3)) { ok = false; break; }
+                    }
+                    if (!ok || off < 0 || abs(w) > L0) continue;
+                    any = true;
+                    nc++;
+                    const double *O = op.blocks + ((size_t)(off + w + L0) * 4 + oi_dir) * K2;
+                    const double *src = fc + (size_t)ft * K3;
+                    double *dst = acc + (size_t)gt * K3;
+                    // g(.., j, ..) += sum_i O(i, j) f(.., i, ..) along dir (column-major O, g = f^T O)
+                    for (int e = tid; e < K3; e += nthr) {
+                        int cd[3] = {e % K, (e / K) % K, e / K2};
+                        const int j = cd[dir];
+                        double s = 0.0;
+                        for (int i = 0; i < K; i++) {
+                            cd[dir] = i;
+                            s += O[i + K * j] * src[cd[0] + K * cd[1] + K2 * cd[2]];
+                        }
+                        dst[e] += s;
+                    }
+                }
+            }
+            if (any) nt++;
+        }
+    }
+    __syncthreads();  // the accumulator's elements were owned per (gt, e); below per flat index
+    // division by the scaling factor to the operator order, coefficients and norms
+    double sfo = 1.0;
+    for (int i = 0; i < order; i++) sfo *= m.sf;
+    double *go = g.coefs + (size_t)gi * 8 * K3;
+    double part[8];
+    for (int c = 0; c < 8; c++) part[c] = 0.0;
+    for (int e = tid; e < 8 * K3; e += nthr) {
+        const double v = acc[e] / sfo;
+        go[e] = v;
+        part[e / K3] += v * v;
+    }
+    for (int c = 0; c < 8; c++)
+        for (int o = 16; o > 0; o >>= 1) part[c] += __shfl_down_sync(0xffffffffu, part[c], o);
+    if ((tid & 31) == 0)
+        for (int c = 0; c < 8; c++) red[tid >> 5][c] = part[c];
+    __syncthreads();
+    if (tid < 8) {
+        double t = 0.0;
+        for (int w = 0; w < (nthr + 31) / 32; w++) t += red[w][tid];
+        g.norms[(size_t)gi * 8 + tid] = sqrt(t);
+    }
+    if (tid == 0) {
+        atomicAdd(&stats->node_terms, nt);
+        atomicAdd(&stats->components, nc);
+        atomicAdd(&stats->band_nodes, nb);
+    }
+}
+
 }  // namespace
+
+void launch_deriv(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work, int order, LevelStats *stats,
+                  int *err, cudaStream_t s) {
+    if (n_work <= 0) return;
+    const size_t smem = sizeof(double) * 8 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_deriv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_deriv<<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, order, stats, err);
+}
 
 void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
                          uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s) {

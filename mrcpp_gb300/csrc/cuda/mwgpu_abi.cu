@@ -237,6 +237,14 @@ struct Level {
     std::vector<int> seg;
     std::vector<double> gthr;
     std::vector<DevTree> fs, gs;
+    // derivative levels: band direction (-1: convolution), band width, operator order
+    int band_dir = -1, band_w = 0, deriv_order = 0;
+    DevOper op() const {
+        DevOper d = o->op;
+        d.band_dir = band_dir;
+        d.band_dir_w = band_w;
+        return d;
+    }
 };
 
 // (g, band cell) pairs of every work entry: the band boxes of makeOperBand
@@ -450,7 +458,7 @@ mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount,
         for (int t = 0; t < nt; t++) {
             const int b = lv.seg[t], e = lv.seg[t + 1];
             if (b == e) continue;
-            launch_band_missing(o->mra, o->op, lv.inps[t]->t, lv.outs[t]->t, ctx->d_work + b, e - b, ctx->d_pkeys + (size_t)t * ctx->phcap,
+            launch_band_missing(o->mra, lv.op(), lv.inps[t]->t, lv.outs[t]->t, ctx->d_work + b, e - b, ctx->d_pkeys + (size_t)t * ctx->phcap,
                                 ctx->d_pvals + (size_t)t * ctx->phcap, ctx->phcap, ctx->d_plist + (size_t)t * ctx->pcap, ctx->d_pcount + t,
                                 ctx->pcap, ctx->d_err, ctx->stream);
             ctx->launches++;
@@ -523,7 +531,11 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
     MW_CK(cudaMemcpyAsync(ctx->d_gs, lv.gs.data(), sizeof(DevTree) * nt, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(ctx->d_gthr, lv.gthr.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->stream));
     LevelStats mixed_nt{};
-    if (ctx->precision == MWGPU_PREC_MIXED) {
+    if (lv.band_dir >= 0) {
+        MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        launch_deriv(o->mra, lv.op(), lv.inps[0]->t, lv.outs[0]->t, ctx->d_work, n, lv.deriv_order, ctx->d_stats, ctx->d_err, ctx->stream);
+        ctx->launches++;
+    } else if (ctx->precision == MWGPU_PREC_MIXED) {
         if (auto s = run_mixed(ctx, lv, &mixed_nt)) return s;
     } else {
         MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -552,7 +564,7 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
     tr.mark("result");
     if (norms_out)
         for (int j = 0; j < n; j++) std::memcpy(norms_out + 8 * (size_t)lv.order[j], &staged[8 * (size_t)j], sizeof(double) * 8);
-    if (ctx->precision == MWGPU_PREC_MIXED) hs.node_terms = mixed_nt.node_terms;
+    if (ctx->precision == MWGPU_PREC_MIXED && lv.band_dir < 0) hs.node_terms = mixed_nt.node_terms;
     if (stats) {
         stats->node_terms = hs.node_terms;
         stats->components = hs.components;
@@ -936,6 +948,8 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.pair_bound_off = p_pboff;
     o->op.n_nodes = (int)node;
     o->op.btc = nullptr;
+    o->op.band_dir = -1;
+    o->op.band_dir_w = 0;
     if (mwgpu::tc_supported(K)) {
         // B operands of the tensor-core contraction per operator node (band zeroed) + a zero record
         std::vector<int4> ninfo(node);
@@ -1035,6 +1049,34 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
     return level_entry(ctx, o, 1, inps, outs, nullptr, node_ix, n, prec, &out_sqnorm, norms_out, stats);
+}
+
+mwgpu_status mwgpu_apply_derivative(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n, int dir,
+                                    int order, mwgpu_level_stats *stats) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(dir >= 0 && dir < 3, "derivative direction must be 0, 1 or 2");
+    MW_ARG(order >= 1, "derivative order must be >= 1");
+    MW_ARG(o && o->op.n_terms == 1, "a derivative operator has one term");
+    Level lv;
+    mwgpu_tree *ins[1] = {inp}, *outs[1] = {out};
+    // the FP64 form: GenNodes in FP64 as well, whatever the context's mode
+    const int prev = ctx->precision;
+    ctx->precision = MWGPU_PREC_FP64;
+    mwgpu_status s = make_level(ctx, o, 1, ins, outs, nullptr, node_ix, n, lv);
+    if (s == MWGPU_OK) {
+        // DerivativeCalculator::makeOperBand: width = the operator's largest band width
+        int w = -1;
+        for (int b : o->band_max) w = std::max(w, b);
+        lv.band_dir = dir;
+        lv.band_w = std::max(w, 0);
+        lv.deriv_order = order;
+        cudaSetDevice(ctx->device);
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        const double zero = 0.0;
+        if (n > 0) s = level_run(ctx, lv, &zero, 0.0, nullptr, stats);
+    }
+    ctx->precision = prev;
+    return s;
 }
 
 mwgpu_status mwgpu_apply_level_batch(mwgpu_ctx *ctx, const mwgpu_oper *o, int n_trees, mwgpu_tree *const *inps, mwgpu_tree *const *outs,

@@ -70,6 +70,9 @@ struct DevOper {
     // with the blocks outside the band zeroed; null otherwise
     const float *btc;
     int n_nodes;
+    // derivative operators (DerivativeCalculator::makeOperBand): the band runs
+    // along band_dir only, band_dir_w wide; -1: the convolution band box
+    int band_dir, band_dir_w;
 };
 
 struct DevTree {
@@ -167,6 +170,11 @@ void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, c
 void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s,
                       bool real_only = false, bool fp32 = false);
 void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
+// DerivativeCalculator::calcNode for the work entries (output leaves): band along
+// op.band_dir, 1D application of term 0 with the identity elsewhere, divided by
+// sf^order; FP64
+void launch_deriv(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work, int order, LevelStats *stats,
+                  int *err, cudaStream_t s);
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
                           double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev = nullptr,
                           const double *gthr_dev = nullptr);

@@ -84,6 +84,8 @@ Mat inverse(const Mat &A) {
     return inv;
 }
 
+}  // namespace
+
 double legendre_scaled(int j, double x) {  // sqrt(2j+1) P_j(2x-1)
     double t = 2.0 * x - 1.0, p0 = 1.0, p1 = t;
     if (j == 0) return 1.0;
@@ -94,7 +96,6 @@ double legendre_scaled(int j, double x) {  // sqrt(2j+1) P_j(2x-1)
     }
     return std::sqrt(2.0 * j + 1.0) * p1;
 }
-}  // namespace
 
 void set_table_path(const std::string &path) {
     std::lock_guard<std::mutex> lk(g_mu);

@@ -441,6 +441,108 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     if (stats) *stats = acc;
     return 0;
 }
+// CopyAdaptor (CopyAdaptor.cpp:55-71) with TreeBuilder: refine `out` wherever a
+// child of a node, shifted by up to bw[d] boxes in direction d, is a node of `inp`
+void copy_adapt(Tree<3> &out, const Tree<3> &inp, const int bw[3]) {
+    const int maxScale = out.mra->maxScale();
+    std::vector<int> work = out.endNodes(), next;
+    while (!work.empty()) {
+        next.clear();
+        for (int i : work) {
+            if (out.isBranch(i) || out.nodes[i].n + 2 > maxScale) continue;
+            const auto nd = out.nodes[i];
+            bool split = false;
+            for (int c = 0; c < 8 && !split; c++) {
+                const int cl[3] = {2 * nd.l[0] + (c & 1), 2 * nd.l[1] + ((c >> 1) & 1), 2 * nd.l[2] + ((c >> 2) & 1)};
+                for (int d = 0; d < 3 && !split; d++)
+                    for (int w = -bw[d]; w <= bw[d] && !split; w++) {
+                        int l[3] = {cl[0], cl[1], cl[2]};
+                        l[d] += w;
+                        const int id = inp.find(nd.n + 1, l);
+                        split = id >= 0 && !inp.isGen(id);
+                    }
+            }
+            if (!split) continue;
+            out.createChildren(i, false);
+            const int c0 = out.nodes[i].child0;
+            for (int c = 0; c < 8; c++) next.push_back(c0 + c);
+        }
+        work.swap(next);
+    }
+}
+
+// apply(out, DerivativeOperator, inp, dir) (apply.cpp:379-412): the output grid is
+// the input grid widened by the band along dir, the end nodes are computed on
+// the device, then BottomUp and the square norm
+int apply_derivative_impl(mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int dir, mwh_apply_stats *stats) {
+    ConvolutionOperator &op = *operp->op;
+    if (op.derivOrder <= 0) return fail(1, "not a derivative operator");
+    if (dir < 0 || dir > 2) return fail(1, "invalid apply direction");
+    if (!(*outp->t->mra == *inpp->t->mra)) return fail(1, "Incompatible MRA");
+    if (!(*outp->t->mra == op.mra)) return fail(1, "Operator MRA differs from the function MRA");
+    Tree<3> &out = *outp->t;
+    for (size_t i = 0; i < out.nodes.size(); i++)
+        if (out.isBranch((int)i)) return fail(1, "the output function must contain only empty root nodes");
+    auto t0 = std::chrono::steady_clock::now();
+    // oper.calcBandWidths(1.0): band widths 0 or 1
+    op.calcBandWidths(1.0);
+    int bw[3] = {0, 0, 0};
+    bw[dir] = std::max(op.getMaxBandWidth(-1), 0);
+    copy_adapt(out, *inpp->t, bw);
+    std::lock_guard<std::mutex> lk(g_gpu_mu);
+    mwgpu_ctx *ctx = gpu_ctx(MWGPU_PREC_FP64);
+    const MRA<3> &mra = *out.mra;
+    std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
+    mwgpu_mra_desc md{};
+    fill_desc(mra, &md, filters.data());
+    mwgpu_oper *dop = device_operator(ctx, md, operp, 1.0);
+    mwh_apply_stats acc{};
+    unsigned long long l0 = 0, l1 = 0;
+    mwgpu_launch_count(ctx, &l0);
+    mwgpu_tree *dinp = nullptr, *dout = nullptr;
+    try {
+        dinp = upload_input(ctx, md, *inpp->t, acc);
+        dout = create_output(ctx, md, out, acc);
+        // DerivativeCalculator::getInitialWorkVector: the end nodes
+        std::vector<int> work = out.endNodes();
+        mwgpu_level_stats ls{};
+        ck(mwgpu_apply_derivative(ctx, dop, dinp, dout, work.data(), (int)work.size(), dir, op.derivOrder, &ls), "apply derivative");
+        ck(mwgpu_transform(ctx, dout, MWGPU_BOTTOMUP, 1), "BottomUp transform");
+        std::vector<double> nn(out.nodes.size() * 8);
+        ck(mwgpu_download_tree(ctx, dout, out.coefs.data(), nn.data()), "download output tree");
+        acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
+        for (size_t i = 0; i < out.nodes.size(); i++) {
+            double s2 = 0.0;
+            for (int c = 0; c < 8; c++) {
+                out.nodes[i].norms[c] = nn[i * 8 + c];
+                s2 += nn[i * 8 + c] * nn[i * 8 + c];
+            }
+            out.nodes[i].squareNorm = s2;
+            out.nodes[i].flags |= F_HASCOEFS;
+        }
+        out.calcSquareNorm();
+        acc.node_terms = ls.node_terms;
+        acc.components = ls.components;
+        acc.band_nodes = ls.band_nodes;
+        acc.gen_nodes = ls.gen_nodes;
+        acc.device_ms = ls.device_ms;
+        acc.contract_ms = ls.contract_ms;
+        acc.iterations = 1;
+        acc.out_nodes = (int)out.nodes.size();
+    } catch (...) {
+        if (dout) mwgpu_free_tree(ctx, dout);
+        if (dinp) mwgpu_free_tree(ctx, dinp);
+        throw;
+    }
+    mwgpu_free_tree(ctx, dout);
+    mwgpu_free_tree(ctx, dinp);
+    mwgpu_launch_count(ctx, &l1);
+    acc.launches = l1 - l0;
+    acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = acc;
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -701,6 +803,23 @@ int mwh_helmholtz(const mwh_mra *m, double mu, double prec, mwh_oper **out) {
         finish_oper(o);
         *out = o;
         return 0;
+    });
+}
+
+int mwh_abgv(const mwh_mra *m, double a, double b, mwh_oper **out) {
+    return guard([&] {
+        if (!m || !out) return fail(1, "invalid ABGV operator arguments");
+        auto *o = new mwh_oper{make_abgv(m->m, a, b), {}, {}, {}, {}};
+        finish_oper(o);
+        *out = o;
+        return 0;
+    });
+}
+
+int mwh_apply_derivative(mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int dir, mwh_apply_stats *stats) {
+    return guard([&] {
+        if (!out || !oper || !inp) return fail(1, "null argument");
+        return apply_derivative_impl(out, oper, inp, dir, stats);
     });
 }
 

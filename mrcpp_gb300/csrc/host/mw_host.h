@@ -80,6 +80,8 @@ struct ScalingBasis {
     double eval(int j, double x) const;  // phi_j(x), x in [0,1]
 };
 const ScalingBasis &get_basis(int type, int order);
+// sqrt(2j+1) P_j(2x - 1): the Legendre scaling function j on [0, 1]
+double legendre_scaled(int j, double x);
 
 // Gauss-Legendre nodes/weights on [0,1] computed in double (ascending).
 void gauss_legendre01(int n, std::vector<double> &x, std::vector<double> &w);
@@ -270,6 +272,7 @@ struct ConvolutionOperator {
     std::vector<OperatorTerm> terms;     // one per kernel term (isotropic: same in x,y,z)
     std::vector<int> bandMax;            // MWOperator::band_max
     double bandPrec = -2.0;              // precision of the current band widths
+    int derivOrder = 0;                  // DerivativeOperator::getOrder (0: a convolution)
     int K() const { return mra.kp1(); }
     int size() const { return (int)terms.size(); }
     void calcBandWidths(double prec);    // MWOperator.cpp:78-108
@@ -282,6 +285,8 @@ std::vector<GaussFunc<1>> helmholtz_kernel(double mu, double epsilon, double r_m
 // PoissonOperator.cpp:40-55, HelmholtzOperator.cpp:41-56
 std::unique_ptr<ConvolutionOperator> make_poisson(const MRA<3> &mra, double prec);
 std::unique_ptr<ConvolutionOperator> make_helmholtz(const MRA<3> &mra, double mu, double prec);
+// ABGVOperator(mra, a, b) (ABGVOperator.cpp:45-71): first derivative, band 0 (a = b = 0) or 1
+std::unique_ptr<ConvolutionOperator> make_abgv(const MRA<3> &mra, double a, double b);
 // ConvolutionOperator(mra, kernel, prec) (ConvolutionOperator.cpp:51-62)
 std::unique_ptr<ConvolutionOperator> make_convolution(const MRA<3> &mra, const std::vector<GaussFunc<1>> &kernel, double prec);
 // ConvolutionOperator::initialize (ConvolutionOperator.cpp:78-108), k_prec/o_prec given

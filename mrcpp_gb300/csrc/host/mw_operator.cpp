@@ -98,6 +98,49 @@ static double oper_component_norm(const Tree<2> &t, int node, int comp, double n
     return norm;
 }
 
+// OperatorTree::setupOperNodeCache (OperatorTree.cpp:200-238): per depth the
+// nodes (0, i) for l = -i and (i, 0) for l = i, l in [-L, L]
+static OperatorTerm term_from_tree(Tree<2> &otree, int operRoot, int K) {
+    OperatorTerm term;
+    auto levels = otree.nodesByDepth(false);
+    int nScales = (int)levels.size();
+    term.depth = nScales;
+    term.maxTransl.assign(nScales, 0);
+    for (int n = 0; n < nScales; n++)
+        for (int i : levels[n]) {
+            term.maxTransl[n] = std::max(term.maxTransl[n], std::abs(otree.nodes[i].l[0]));
+            term.maxTransl[n] = std::max(term.maxTransl[n], std::abs(otree.nodes[i].l[1]));
+        }
+    std::vector<std::vector<int>> cache(nScales);
+    for (int n = 0; n < nScales; n++) {
+        int scale = operRoot + n;
+        int L = term.maxTransl[n];
+        cache[n].assign(2 * L + 1, -1);
+        for (int i = L; i >= 0; i--) {
+            int l[2] = {0, i};
+            cache[n][L - i] = otree.getNode(scale, l, false);
+        }
+        for (int i = 1; i <= L; i++) {
+            int l[2] = {i, 0};
+            cache[n][L + i] = otree.getNode(scale, l, false);
+        }
+    }
+    size_t total = 0;
+    term.offset.resize(nScales);
+    for (int n = 0; n < nScales; n++) { term.offset[n] = total; total += cache[n].size(); }
+    term.blocks.assign(total * 4 * K * K, 0.0);
+    term.norms.assign(total * 4, 0.0);
+    for (int n = 0; n < nScales; n++)
+        for (size_t j = 0; j < cache[n].size(); j++) {
+            int node = cache[n][j];
+            if (node < 0) continue;  // not in the tree: a zero node
+            size_t idx = term.offset[n] + j;
+            std::memcpy(&term.blocks[idx * 4 * K * K], otree.c(node), sizeof(double) * 4 * K * K);
+            for (int c = 0; c < 4; c++) term.norms[idx * 4 + c] = otree.nodes[node].norms[c];
+        }
+    return term;
+}
+
 void build_operator_terms(ConvolutionOperator &op, double k_prec, double o_prec) {
     const MRA<3> &mra = op.mra;
     const auto &box = mra.world;
@@ -164,44 +207,7 @@ void build_operator_terms(ConvolutionOperator &op, double k_prec, double o_prec)
         tree_build<2>(otree, otree.endNodes(), calc, split, -1, omra.maxScale());
         otree.mwTransformUp();
 
-        // setupOperNodeCache
-        OperatorTerm term;
-        auto levels = otree.nodesByDepth(false);
-        int nScales = (int)levels.size();
-        term.depth = nScales;
-        term.maxTransl.assign(nScales, 0);
-        for (int n = 0; n < nScales; n++)
-            for (int i : levels[n]) {
-                term.maxTransl[n] = std::max(term.maxTransl[n], std::abs(otree.nodes[i].l[0]));
-                term.maxTransl[n] = std::max(term.maxTransl[n], std::abs(otree.nodes[i].l[1]));
-            }
-        std::vector<std::vector<int>> cache(nScales);
-        for (int n = 0; n < nScales; n++) {
-            int scale = op.operRoot + n;
-            int L = term.maxTransl[n];
-            cache[n].assign(2 * L + 1, -1);
-            for (int i = L; i >= 0; i--) {
-                int l[2] = {0, i};
-                cache[n][L - i] = otree.getNode(scale, l, false);
-            }
-            for (int i = 1; i <= L; i++) {
-                int l[2] = {i, 0};
-                cache[n][L + i] = otree.getNode(scale, l, false);
-            }
-        }
-        size_t total = 0;
-        term.offset.resize(nScales);
-        for (int n = 0; n < nScales; n++) { term.offset[n] = total; total += cache[n].size(); }
-        term.blocks.assign(total * 4 * K * K, 0.0);
-        term.norms.assign(total * 4, 0.0);
-        for (int n = 0; n < nScales; n++)
-            for (size_t j = 0; j < cache[n].size(); j++) {
-                int node = cache[n][j];
-                size_t idx = term.offset[n] + j;
-                std::memcpy(&term.blocks[idx * 4 * K * K], otree.c(node), sizeof(double) * 4 * K * K);
-                for (int c = 0; c < 4; c++) term.norms[idx * 4 + c] = otree.nodes[node].norms[c];
-            }
-        op.terms.push_back(std::move(term));
+        op.terms.push_back(term_from_tree(otree, op.operRoot, K));
     }
     op.bandPrec = -2.0;
 }
@@ -253,6 +259,116 @@ std::unique_ptr<ConvolutionOperator> make_convolution(const MRA<3> &mra, const s
     op->buildPrec = prec;
     op->kernel = kernel;
     build_operator_terms(*op, prec / 10.0, prec);
+    return op;
+}
+
+// P'_m(t) = sum over k = m-1, m-3, ... >= 0 of (2k+1) P_k(t)
+static double legendre_deriv(int m, double t) {
+    double p0 = 1.0, p1 = t, s = 0.0;
+    for (int k = 0; k < m; k++) {
+        const double pk = k == 0 ? p0 : p1;
+        if ((m - 1 - k) % 2 == 0) s += (2.0 * k + 1.0) * pk;
+        if (k >= 1) {
+            const double p2 = ((2.0 * k + 1.0) * t * p1 - k * p0) / (k + 1.0);
+            p0 = p1;
+            p1 = p2;
+        }
+    }
+    return s;
+}
+
+// ABGVOperator (ABGVOperator.cpp:45-71): the operator tree of the first
+// derivative with boundary parameters a, b, node by node from
+// ABGVCalculator::calcNode (ABGVCalculator.cpp:118-170), refined along the
+// diagonal only (BandWidthAdaptor.h:35-52: split where l0 = 0 and 2 |dl| <= bw).
+std::unique_ptr<ConvolutionOperator> make_abgv(const MRA<3> &mra, double a, double b) {
+    auto op = std::make_unique<ConvolutionOperator>();
+    op->mra = mra;
+    op->operRoot = mra.rootScale();
+    op->operReach = 1;
+    op->buildPrec = MachineZero;
+    op->derivOrder = 1;
+    const int bw = (std::fabs(a) > MachineZero || std::fabs(b) > MachineZero) ? 1 : 0;
+    const ScalingBasis &basis = *mra.basis;
+    const int K = mra.kp1(), type = basis.type;
+    const double sf = mra.world.sf[0];
+    // value vectors and K matrix (ABGVCalculator.cpp:48-116)
+    std::vector<double> v0(K), v1(K);
+    Mat Km(K, K);
+    if (type == Legendre) {
+        for (int i = 0; i < K; i++) {
+            const double c = std::sqrt(2.0 * i + 1.0);
+            v1[i] = c;
+            v0[i] = (i % 2) ? -c : c;
+        }
+        for (int i = 0; i < K; i++)
+            for (int j = i; j < K; j++)
+                if ((i - j) % 2 != 0) Km(j, i) = 2.0 * std::sqrt(2.0 * i + 1.0) * std::sqrt(2.0 * j + 1.0);
+    } else {
+        for (int i = 0; i < K; i++) {
+            v0[i] = basis.eval(i, 0.0);
+            v1[i] = basis.eval(i, 1.0);
+        }
+        // K(i, j) = 2 sqrt(w_j) p_i'(r_j), where p_i' is the derivative of
+        // phi_i(x) = sqrt(w_i) sum_m L_m(r_i) L_m(x), L_m(x) = sqrt(2m+1) P_m(2x - 1),
+        // taken with respect to the polynomial's own argument 2x - 1
+        // (Polynomial::calcDerivative, Polynomial.cpp:222-236): half of d/dx, so
+        // K(i, j) is the integral of phi_i' phi_j over [0, 1], as in the Legendre case
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) {
+                double d = 0.0;
+                for (int mm = 0; mm < K; mm++)
+                    d += legendre_scaled(mm, basis.roots[i]) * std::sqrt(2.0 * mm + 1.0) * legendre_deriv(mm, 2.0 * basis.roots[j] - 1.0);
+                Km(i, j) = 2.0 * std::sqrt(basis.weights[j]) * std::sqrt(basis.weights[i]) * d;
+            }
+    }
+    MRA<2> omra(BoundingBox<2>(op->operRoot, {0, 0}, {op->operReach + 1, op->operReach + 1}, {sf, sf}), type, mra.order());
+    Tree<2> otree(omra);
+    otree.componentNorm = [](const Tree<2> &t, int i, int c) { return oper_component_norm(t, i, c, MachineZero); };
+    const int K2 = K * K;
+    auto calc = [&](Tree<2> &t, const std::vector<int> &work) {
+        for (int node : work) {
+            double *coefs = t.c(node);
+            std::fill(coefs, coefs + t.nCoefs, 0.0);
+            const auto &nd = t.nodes[node];
+            const double two_np1 = std::pow(2.0, nd.n + 1);
+            switch (nd.l[1] - nd.l[0]) {
+                case 1:
+                    if (b > MachineZero)
+                        for (int i = 0; i < K; i++)
+                            for (int j = 0; j < K; j++) coefs[1 * K2 + i * K + j] = -b * v0[i] * v1[j];
+                    break;
+                case 0:
+                    for (int i = 0; i < K; i++)
+                        for (int j = 0; j < K; j++) {
+                            const double diag = (1.0 - a) * v1[i] * v1[j] - (1.0 - b) * v0[i] * v0[j] - Km(i, j);
+                            coefs[0 * K2 + i * K + j] = diag;
+                            coefs[1 * K2 + i * K + j] = a * v1[i] * v0[j];
+                            coefs[2 * K2 + i * K + j] = -b * v0[i] * v1[j];
+                            coefs[3 * K2 + i * K + j] = diag;
+                        }
+                    break;
+                case -1:
+                    if (a > MachineZero)
+                        for (int i = 0; i < K; i++)
+                            for (int j = 0; j < K; j++) coefs[2 * K2 + i * K + j] = a * v1[i] * v0[j];
+                    break;
+                default:
+                    break;
+            }
+            for (int j = 0; j < t.nCoefs; j++) coefs[j] *= two_np1;
+            t.mwTransformNode(node, Compression);
+            t.nodes[node].flags |= F_HASCOEFS;
+            t.calcNorms(node);
+        }
+    };
+    auto split = [bw](const Tree<2> &t, int i) {
+        const auto &n = t.nodes[i];
+        return n.l[0] == 0 && 2 * std::abs(n.l[0] - n.l[1]) <= bw;
+    };
+    tree_build<2>(otree, otree.endNodes(), calc, split, -1, omra.maxScale());
+    op->terms.push_back(term_from_tree(otree, op->operRoot, K));
+    op->bandPrec = -2.0;
     return op;
 }
 

@@ -59,6 +59,9 @@ def lib(fast=False):
         L.oracle_result_info.argtypes = [C.c_void_p, _PI, _PD, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), _PI]
         L.oracle_result_export.restype = C.c_int
         L.oracle_result_export.argtypes = [C.c_void_p, _PI, _PI, _PD, _PD]
+        L.oracle_apply_derivative.restype = C.c_int
+        L.oracle_apply_derivative.argtypes = [C.POINTER(OracleMra), C.POINTER(OracleOper), C.POINTER(OracleTree), C.POINTER(OracleTree), C.c_int,
+                                              C.c_int, C.c_int, C.POINTER(C.c_void_p)]
         L.oracle_result_free.restype = None
         L.oracle_result_free.argtypes = [C.c_void_p]
         _libs[path] = L
@@ -93,7 +96,7 @@ class Prepared:
         m.filters = _pd(filt)
         ex = oper.export()
         o = OracleOper()
-        o.n_terms, o.order, o.build_prec = oper.n_terms, mra.order, float(oper.prec)
+        o.n_terms, o.order, o.build_prec = oper.n_terms, mra.order, float(getattr(oper, "prec", 1.0))
         self.keep.append(ex)
         o.depth, o.max_transl = _pi(ex["depth"]), _pi(ex["max_transl"])
         o.blocks, o.norms = _pd(ex["blocks"]), _pd(ex["norms"])
@@ -106,11 +109,15 @@ class Prepared:
         self.m, self.o, self.ft, self.gt = m, o, ft, gt
         self.out_sqnorm = float(out.square_norm)
 
-    def run(self, nthreads=0, count_terms=True, sample=1, export=True, fast=False):
+    def run(self, nthreads=0, count_terms=True, sample=1, export=True, fast=False, deriv_dir=None):
         L = lib(fast)
         res = C.c_void_p()
-        rc = L.oracle_apply_sampled(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), self.out_sqnorm, self.prec,
+        if deriv_dir is None:
+            rc = L.oracle_apply_sampled(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), self.out_sqnorm, self.prec,
                                         self.max_iter, self.abs_prec, int(nthreads), int(bool(count_terms)), int(sample), C.byref(res))
+        else:
+            rc = L.oracle_apply_derivative(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), int(deriv_dir), 1,
+                                           int(nthreads), C.byref(res))
         if rc != 0:
             raise RuntimeError("oracle_apply failed with code %d" % rc)
         n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()
@@ -132,6 +139,12 @@ def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, nthreads=0, count_t
     norm; `oper` a mrcpp_gb300 ConvolutionOperator; `inp` the input FunctionTree.
     Returns a dict with the flat output tree and the counters."""
     return Prepared(prec, out, oper, inp, max_iter, abs_prec).run(nthreads, count_terms, sample)
+
+
+def apply_derivative(out, oper, inp, dir, nthreads=0):
+    """Oracle apply(out, DerivativeOperator, inp, dir) (first derivative):
+    `out` holds only its roots; returns the flat copy-adapted output tree."""
+    return Prepared(1.0, out, oper, inp).run(nthreads, deriv_dir=dir)
 
 
 def to_tree(result, mra):

@@ -822,6 +822,167 @@ int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracl
     return 0;
 }
 
+/* ---------------------------------------------------------------- derivative */
+
+/* CopyAdaptor::splitNode (CopyAdaptor.cpp:55-71): a child of node i, shifted by
+   up to bw[d] boxes along d, is a node of f */
+static int copy_split(const otree *f, const otree *g, int i, const int bw[3]) {
+    for (int c = 0; c < 8; c++) {
+        okey ck;
+        ck.n = g->idx[i].n + 1;
+        for (int d = 0; d < 3; d++) ck.l[d] = 2 * g->idx[i].l[d] + ((c >> d) & 1);
+        for (int d = 0; d < 3; d++)
+            for (int w = -bw[d]; w <= bw[d]; w++) {
+                okey k = ck;
+                k.l[d] += w;
+                if (omap_find(&f->map, k) >= 0) return 1;
+            }
+    }
+    return 0;
+}
+
+/* apply(out, DerivativeOperator, inp, dir) (apply.cpp:379-412) with
+   DerivativeCalculator::calcNode (DerivativeCalculator.cpp:113-151),
+   makeOperBand (:153-176), applyOperator (:199-241) and tensorApplyOperComp
+   (:245-268; the identity off the apply direction).  out0 holds the roots of
+   the output; the result is the copy-adapted grid with all coefficients. */
+int oracle_apply_derivative(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, int dir, int order,
+                            int nthreads, oracle_result **res) {
+    if (!m || !od || !inp || !out0 || !res || dir < 0 || dir > 2 || od->n_terms != 1 || od->order != m->order) return 1;
+    ooper o;
+    oper_setup(&o, od, 1.0); /* oper.calcBandWidths(1.0) */
+    int width = 0;
+    for (int n = 0; n < o.n_band_max; n++)
+        if (o.band_max[n] > width) width = o.band_max[n];
+    otree f;
+    if (tree_load(&f, m, inp->n_nodes, inp->idx, inp->child0, inp->coefs, inp->norms)) return 2;
+    oracle_result *R = (oracle_result *)calloc(1, sizeof(oracle_result));
+    if (tree_load(&R->g, m, out0->n_nodes, out0->idx, out0->child0, NULL, NULL)) return 2;
+    otree *g = &R->g;
+    const int K = g->K, K2 = K * K, K3 = g->K3;
+    /* the output grid: TreeBuilder with CopyAdaptor(inp, maxScale, bw) */
+    int bw[3] = {0, 0, 0};
+    bw[dir] = width;
+    size_t nwork;
+    int *lvl, nl;
+    int *work = bfs(g, &nwork, &lvl, &nl);
+    free(lvl);
+    while (nwork > 0) {
+        int *next = (int *)malloc(sizeof(int) * (8 * nwork + 1));
+        size_t nn = 0;
+        for (size_t w = 0; w < nwork; w++) {
+            int i = work[w];
+            if (g->child0[i] >= 0 || g->idx[i].n + 2 > m->max_scale) continue;
+            if (copy_split(&f, g, i, bw)) {
+                int c0 = create_children(g, i, 0);
+                for (int c = 0; c < 8; c++) next[nn++] = c0 + c;
+            }
+        }
+        free(work);
+        work = next;
+        nwork = nn;
+    }
+    free(work);
+    size_t cnt;
+    int *order_ = bfs(g, &cnt, &lvl, &nl);
+    double *tmp1 = (double *)malloc(sizeof(double) * 8 * K3), *tmp2 = (double *)malloc(sizeof(double) * 8 * K3);
+    /* GenNodes of the bands of the end nodes (serially) */
+    for (size_t q = 0; q < cnt; q++) {
+        int gi = order_[q];
+        if (g->child0[gi] >= 0) continue;
+        okey gk = g->idx[gi];
+        int depth = gk.n - m->root_scale;
+        for (int w = -width; w <= width; w++) {
+            okey fk = gk;
+            fk.l[dir] += w;
+            int c_i = m->corner[dir] * (1 << depth), nb = m->nbox[dir] * (1 << depth);
+            if (fk.l[dir] < c_i || fk.l[dir] >= c_i + nb) continue;
+            get_node(&f, m, fk, tmp1, tmp2);
+        }
+    }
+    double sfo = 1.0;
+    for (int i = 0; i < order; i++) sfo *= m->sf;
+    unsigned long long nts = 0, comps = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : nts, comps)
+    for (long q = 0; q < (long)cnt; q++) {
+        int gi = order_[q];
+        if (g->child0[gi] >= 0) continue;
+        double *gc = g->coefs + (size_t)gi * g->nc;
+        memset(gc, 0, sizeof(double) * g->nc);
+        okey gk = g->idx[gi];
+        int depth = gk.n - m->root_scale;
+        for (int w = -width; w <= width; w++) {
+            okey fk = gk;
+            fk.l[dir] += w;
+            int c_i = m->corner[dir] * (1 << depth), nb = m->nbox[dir] * (1 << depth);
+            if (fk.l[dir] < c_i || fk.l[dir] >= c_i + nb) continue;
+            int fi = omap_find(&f.map, fk);
+            if (fi < 0) continue;
+            const double *fc = f.coefs + (size_t)fi * f.nc;
+            int any = 0;
+            for (int ft = 0; ft < 8; ft++) {
+                if (f.norms[(size_t)fi * 8 + ft] < MACHINE_ZERO) continue;
+                for (int gt = 0; gt < 8; gt++) {
+                    int ok = 1, oi_dir = 0;
+                    for (int d = 0; d < 3; d++) {
+                        int oi = 2 * ((gt >> d) & 1) + ((ft >> d) & 1);
+                        int l = d == dir ? w : 0;
+                        if (abs(l) > bw_get(&o, 0, depth, oi)) { ok = 0; break; }
+                        if (d == dir) oi_dir = oi;
+                        else if (!(oi == 0 || oi == 3)) { ok = 0; break; }
+                    }
+                    if (!ok) continue;
+                    any = 1;
+                    comps++;
+                    const double *O = o.blocks + (oper_node(&o, 0, depth, w) * 4 + (size_t)oi_dir) * K2;
+                    const double *src = fc + (size_t)ft * K3;
+                    double *dst = gc + (size_t)gt * K3;
+                    for (int e = 0; e < K3; e++) {
+                        int cd[3] = {e % K, (e / K) % K, e / K2};
+                        int j = cd[dir];
+                        double sum = 0.0;
+                        for (int i = 0; i < K; i++) {
+                            cd[dir] = i;
+                            sum += O[i + K * j] * src[cd[0] + K * cd[1] + K2 * cd[2]];
+                        }
+                        dst[e] += sum;
+                    }
+                }
+            }
+            if (any) nts++;
+        }
+        for (int e = 0; e < 8 * K3; e++) gc[e] /= sfo;
+        calc_norms(g, gi);
+    }
+    R->st.node_terms = nts;
+    R->st.components = comps;
+    R->iterations = 1;
+    /* mwTransform(BottomUp) */
+    for (int L = nl - 2; L >= 0; L--)
+        for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+            int i = order_[q];
+            int c0 = g->child0[i];
+            if (c0 < 0) continue;
+            mw_transform_back(m, g->coefs + (size_t)c0 * g->nc, g->coefs + (size_t)i * g->nc, g->nc, tmp1);
+            calc_norms(g, i);
+        }
+    double sq = 0.0;
+    for (size_t q = 0; q < cnt; q++)
+        if (g->child0[order_[q]] < 0) sq += g->sqn[order_[q]];
+    g->square_norm = sq;
+    free(order_);
+    free(lvl);
+    free(tmp1);
+    free(tmp2);
+    tree_free(&f);
+    oper_free(&o);
+    *res = R;
+    return 0;
+}
+
 int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
                        unsigned long long *components, int *iterations) {
     if (!r) return 1;

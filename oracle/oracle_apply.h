@@ -45,6 +45,10 @@ int oracle_apply(const oracle_mra *mra, const oracle_oper *oper, const oracle_tr
                  double prec, int max_iter, int abs_prec, int nthreads, int count_terms, oracle_result **res);
 int oracle_apply_sampled(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
                          double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, oracle_result **res);
+/* apply(out, DerivativeOperator, inp, dir): out0 holds the output roots; the
+ * grid is copy-adapted from inp along dir, end nodes computed, then BottomUp. */
+int oracle_apply_derivative(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, int dir, int order,
+                            int nthreads, oracle_result **res);
 int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
                        unsigned long long *components, int *iterations);
 int oracle_result_export(const oracle_result *r, int *idx, int *child0, double *coefs, double *norms);
