@@ -161,6 +161,18 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tre
  * MWTree.cpp:166-181). */
 mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tree, int direction, int overwrite);
 
+/* Projection level: replaces ProjectionCalculator::calcNode
+ * (src/treebuilders/ProjectionCalculator.cpp:34-51) for the nodes
+ * node_ix[0..n) of `tree` (an output tree), for a sum of Gaussians
+ * gauss[j] = {coefficient, exponent, x, y, z}: values at the children's
+ * quadrature points, cvTransform(Backward) with the basis's value-to-coefficient
+ * map vc_map (K x K, column-major) and quadrature roots (K, on [0, 1]),
+ * compression, node norms (norms_out: 8 per node, optional).  FP64.  The
+ * caller's TreeBuilder loop does the split test and the final BottomUp
+ * (project.cpp:47-66). */
+mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *vc_map, const double *roots,
+                                 const int *node_ix, int n, double *norms_out);
+
 /* Derivative level: replaces DerivativeCalculator::calcNodeVector
  * (src/treebuilders/DerivativeCalculator.cpp:113-151) for the output end nodes
  * node_ix[0..n) of `out` (a grid made by CopyAdaptor, CopyAdaptor.cpp:55-71):

@@ -62,6 +62,13 @@ void mwh_tree_free(mwh_tree *tree);
 int mwh_build_grid_gauss(mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos);
 int mwh_project_gauss(double prec, mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos, int max_iter,
                       int abs_prec);
+/* project(prec, tree, GaussExp, maxIter, absPrec) (src/treebuilders/project.cpp:47-66)
+ * with the node computations (ProjectionCalculator::calcNode) and the final
+ * BottomUp on the device (mwgpu_project_level); the split test and tree
+ * growth stay on the host.  stats: iterations, output nodes, wall time
+ * (optional). */
+int mwh_project_gauss_device(double prec, mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos, int max_iter,
+                             int abs_prec, mwh_apply_stats *stats);
 int mwh_copy_grid(mwh_tree *out, const mwh_tree *inp);
 /* node count (non-generated nodes) and tree square norm */
 int mwh_tree_info(const mwh_tree *tree, int *n_nodes, double *square_norm);

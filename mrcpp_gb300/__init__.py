@@ -143,6 +143,8 @@ _SIGS = {
     "mwh_build_grid_gauss": (C.c_int, [_P, C.c_int, _PD, _PD, _PD]),
     "mwh_project_gauss": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int]),
     "mwh_copy_grid": (C.c_int, [_P, _P]),
+    "mwh_project_gauss_device": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwgpu_project_level": (C.c_int, [_P, _P, C.c_int, _PD, _PD, _PD, _PI, C.c_int, _PD]),
     "mwh_tree_info": (C.c_int, [_P, _PI, _PD]),
     "mwh_tree_export": (C.c_int, [_P, _PI, _PI, _PD, _PD]),
     "mwh_tree_import": (C.c_int, [_P, C.c_int, _PI, _PI, _PD, C.c_double]),
@@ -311,11 +313,18 @@ def build_grid(tree, gaussians):
     _ck(lib().mwh_build_grid_gauss(tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos)))
 
 
-def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True):
-    """build_grid (optional) + project(prec, tree, GaussExp) (src/treebuilders/project.cpp:41-66)."""
+def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True, device=False):
+    """build_grid (optional) + project(prec, tree, GaussExp) (src/treebuilders/project.cpp:41-66).
+    device=True computes the nodes on the GPU (mwgpu_project_level) and returns
+    the statistics; the default projects on the host like the reference."""
     if grid:
         build_grid(tree, gaussians)
     coef, ex, pos = _gauss_arrays(gaussians)
+    if device:
+        st = MwhApplyStats()
+        _ck(lib().mwh_project_gauss_device(float(prec), tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos), int(max_iter), int(bool(abs_prec)),
+                                           C.byref(st)))
+        return st.as_dict()
     _ck(lib().mwh_project_gauss(float(prec), tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos), int(max_iter), int(bool(abs_prec))))
 
 

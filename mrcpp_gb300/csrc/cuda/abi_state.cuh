@@ -43,6 +43,8 @@ struct mwgpu_ctx {
     int *d_err = nullptr;
     LevelStats *d_stats = nullptr;
     int *d_tc_counter = nullptr;  // chunk counter of the tensor-core contraction
+    double *d_proj = nullptr;     // projection: Gaussians, value-to-coefficient map, roots
+    long long proj_cap = 0;
     int *d_work = nullptr;
     int *d_wtree = nullptr;  // tree of every work entry (batched levels)
     int work_cap = 0;

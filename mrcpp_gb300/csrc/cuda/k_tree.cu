@@ -287,6 +287,68 @@ __global__ void k_mw_up(DevMRA m, DevTree t0, const DevTree *ts, const int *ptre
     block_norms(pc, K3, t.norms + (size_t)p * 8, tid, nthr);
 }
 
+// ProjectionCalculator::calcNode (ProjectionCalculator.cpp:34-51) for one node
+// per CTA, of a sum of Gaussians c_g exp(-a_g |r - R_g|^2): the function at the
+// quadrature points of the 8 children (MWNode::getExpandedChildPts,
+// MWNode.cpp:854-935; x fastest), cvTransform(Backward) (MWNode.cpp:448-490:
+// the value-to-coefficient map along each direction, times
+// sqrt(sf^3 2^(-3 (n+1)))), the compression of the 8 child blocks
+// (mwTransform(Compression)) and the node norms.  FP64.  gauss: [n][5] =
+// coefficient, exponent, position.
+__global__ void k_project(DevMRA m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map, const double *roots) {
+    extern __shared__ double sm[];
+    const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    double *t1 = sm, *t2 = sm + 8 * K3;
+    const int i = nodes[blockIdx.x];
+    const int4 nd = t.idx[i];
+    const double sfac = exp2(-(double)(nd.x + 1));
+    const int lq[3] = {nd.y, nd.z, nd.w};
+    for (int e = tid; e < 8 * K3; e += nthr) {
+        const int ct = e / K3, p = e % K3;
+        double r[3];
+        int rem = p;
+        for (int d = 0; d < 3; d++) {
+            const int q = rem % K;
+            rem /= K;
+            r[d] = m.sf * (sfac * (roots[q] + 2.0 * lq[d] + ((ct >> d) & 1)));
+        }
+        double v = 0.0;
+        for (int g = 0; g < ng; g++) {
+            const double *G = gauss + 5 * g;
+            const double dx = r[0] - G[2], dy = r[1] - G[3], dz = r[2] - G[4];
+            v += G[0] * exp(-G[1] * (dx * dx + dy * dy + dz * dz));
+        }
+        t1[e] = v;
+    }
+    __syncthreads();
+    // cvTransform(Backward): the K x K value-to-coefficient map along x, y, z of every child block
+    double *bufs[2] = {t1, t2};
+    for (int d = 0; d < 3; d++) {
+        double *in = bufs[d & 1], *out = bufs[(d + 1) & 1];
+        for (int ct = 0; ct < 8; ct++) dapply<false>(out + ct * K3, in + ct * K3, vc_map, K, tid, nthr);
+        __syncthreads();
+    }
+    // result in t2; scale: sqrt(sf^3 / 2^(3 (n+1)))
+    const double two_fac = sqrt(m.sf * m.sf * m.sf / exp2(3.0 * (nd.x + 1)));
+    for (int e = tid; e < 8 * K3; e += nthr) t1[e] = two_fac * t2[e];
+    __syncthreads();
+    // mwTransform(Compression): 8 child scaling blocks -> s + d of the node
+    for (int d = 0; d < 3; d++) {
+        double *in = bufs[d & 1], *out = bufs[(d + 1) & 1];
+        const int mask = 1 << d;
+        for (int gt = 0; gt < 8; gt++)
+            dapply<false>(out + gt * K3, in + (gt & ~mask) * K3, filt(m, 0, 2 * ((gt >> d) & 1) + 0), K, tid, nthr);
+        __syncthreads();
+        for (int gt = 0; gt < 8; gt++)
+            dapply<true>(out + gt * K3, in + (gt | mask) * K3, filt(m, 0, 2 * ((gt >> d) & 1) + 1), K, tid, nthr);
+        __syncthreads();
+    }
+    double *pc = t.coefs + (size_t)i * 8 * K3;
+    for (int e = tid; e < 8 * K3; e += nthr) pc[e] = t2[e];
+    __syncthreads();
+    block_norms(pc, K3, t.norms + (size_t)i * 8, tid, nthr);
+}
+
 // The transforms of the mixed form: the same three filter stages with FP32
 // products in shared memory, the children / parent coefficients kept in FP64.
 template <bool ADD>
@@ -612,6 +674,14 @@ void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *pt
     size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_mw_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_mw_down<<<n, 256, smem, s>>>(m, t, ts, ptree, parents, n, overwrite);
+}
+
+void launch_project(const DevMRA &m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map,
+                    const double *roots, cudaStream_t s) {
+    if (n <= 0) return;
+    const size_t smem = sizeof(double) * 16 * m.kp1_d;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_project<<<n, 256, smem, s>>>(m, t, nodes, n, gauss, ng, vc_map, roots);
 }
 
 void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s, bool fp32) {

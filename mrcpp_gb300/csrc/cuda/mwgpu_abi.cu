@@ -742,7 +742,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_tc_counter, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
+    for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_tc_counter, (void *)ctx->d_proj, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
                     (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_items_cm, (void *)ctx->d_chunks,
                     (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
@@ -1049,6 +1049,41 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
     return level_entry(ctx, o, 1, inps, outs, nullptr, node_ix, n, prec, &out_sqnorm, norms_out, stats);
+}
+
+mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *vc_map, const double *roots,
+                                 const int *node_ix, int n, double *norms_out) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(tree && !tree->is_input, "projection writes an output tree");
+    MW_ARG(n_gauss >= 0 && (n_gauss == 0 || gauss) && vc_map && roots, "invalid Gaussian list or basis tables");
+    MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
+    for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < tree->t.n_real, "node index out of range");
+    cudaSetDevice(ctx->device);
+    if (n == 0) return MWGPU_OK;
+    const int K = tree->mra.K;
+    const long long need = 5LL * std::max(n_gauss, 1) + (long long)K * K + K;
+    if (auto s = grow_buf(ctx, &ctx->d_proj, &ctx->proj_cap, need)) return s;
+    if (auto s = ensure_work(ctx, n)) return s;
+    double *d_g = ctx->d_proj, *d_vc = d_g + 5 * std::max(n_gauss, 1), *d_roots = d_vc + K * K;
+    if (n_gauss > 0) MW_CK(cudaMemcpyAsync(d_g, gauss, sizeof(double) * 5 * n_gauss, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(d_vc, vc_map, sizeof(double) * K * K, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(d_roots, roots, sizeof(double) * K, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_work, node_ix, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    launch_project(tree->mra, tree->t, ctx->d_work, n, d_g, n_gauss, d_vc, d_roots, ctx->stream);
+    ctx->launches++;
+    if (norms_out) {
+        if (auto s = grow_buf(ctx, &ctx->d_nstage, &ctx->nstage_cap, 8LL * n)) return s;
+        if (auto s = ensure_trees(ctx, 1)) return s;
+        std::vector<int> zeros(n, 0);
+        MW_CK(cudaMemcpyAsync(ctx->d_wtree, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_gs, &tree->t, sizeof(DevTree), cudaMemcpyHostToDevice, ctx->stream));
+        launch_gather_norms(ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_nstage, ctx->stream);
+        ctx->launches++;
+        MW_CK(cudaMemcpyAsync(norms_out, ctx->d_nstage, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    MW_CK(cudaGetLastError());
+    MW_CK(cudaStreamSynchronize(ctx->stream));
+    return MWGPU_OK;
 }
 
 mwgpu_status mwgpu_apply_derivative(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n, int dir,

@@ -543,6 +543,78 @@ int apply_derivative_impl(mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int d
     return 0;
 }
 
+// project(prec, out, GaussExp, maxIter, absPrec) (project.cpp:47-66) with the
+// node computations on the device: TreeBuilder + WaveletAdaptor on the host,
+// ProjectionCalculator::calcNode per iteration through mwgpu_project_level,
+// BottomUp on the device, then the coefficients come back
+int project_device_impl(double prec, Tree<3> &tree, int n, const double *coef, const double *ex, const double *pos, int max_iter, bool abs_prec,
+                        mwh_apply_stats *stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> gauss(5 * (size_t)n);
+    for (int j = 0; j < n; j++) {
+        gauss[5 * j] = coef[j];
+        gauss[5 * j + 1] = ex[j];
+        for (int d = 0; d < 3; d++) gauss[5 * j + 2 + d] = pos[3 * j + d];
+    }
+    const MRA<3> &mra = *tree.mra;
+    const ScalingBasis &basis = *mra.basis;
+    std::lock_guard<std::mutex> lk(g_gpu_mu);
+    mwgpu_ctx *ctx = gpu_ctx(MWGPU_PREC_FP64);
+    std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
+    mwgpu_mra_desc md{};
+    fill_desc(mra, &md, filters.data());
+    mwh_apply_stats acc{};
+    BuildState b;
+    b.tree = &tree;
+    tree.clearGenerated();
+    b.dout = create_output(ctx, md, tree, acc);
+    b.synced = tree.nodes.size();
+    try {
+        std::vector<double> nbuf;
+        auto calc = [&](Tree<3> &t, const std::vector<int> &work) {
+            sync_new(ctx, b, acc);
+            nbuf.resize(8 * work.size());
+            ck(mwgpu_project_level(ctx, b.dout, n, gauss.data(), basis.vcMap.data(), basis.roots.data(), work.data(), (int)work.size(), nbuf.data()),
+               "projection level");
+            for (size_t j = 0; j < work.size(); j++) {
+                auto &nd = t.nodes[work[j]];
+                double s2 = 0.0;
+                for (int c = 0; c < 8; c++) {
+                    nd.norms[c] = nbuf[8 * j + c];
+                    s2 += nd.norms[c] * nd.norms[c];
+                }
+                nd.squareNorm = s2;
+                nd.flags |= F_HASCOEFS;
+            }
+            acc.iterations++;
+        };
+        auto split = [prec, abs_prec](const Tree<3> &t, int i) { return split_check(t, i, prec, 1.0, abs_prec); };
+        tree_build<3>(tree, tree.endNodes(), calc, split, max_iter, mra.maxScale());
+        sync_new(ctx, b, acc);
+        ck(mwgpu_transform(ctx, b.dout, MWGPU_BOTTOMUP, 1), "BottomUp transform");
+        std::vector<double> nn(tree.nodes.size() * 8);
+        ck(mwgpu_download_tree(ctx, b.dout, tree.coefs.data(), nn.data()), "download projected tree");
+        for (size_t i = 0; i < tree.nodes.size(); i++) {
+            double s2 = 0.0;
+            for (int c = 0; c < 8; c++) {
+                tree.nodes[i].norms[c] = nn[i * 8 + c];
+                s2 += nn[i * 8 + c] * nn[i * 8 + c];
+            }
+            tree.nodes[i].squareNorm = s2;
+            tree.nodes[i].flags |= F_HASCOEFS;
+        }
+        tree.calcSquareNorm();
+    } catch (...) {
+        mwgpu_free_tree(ctx, b.dout);
+        throw;
+    }
+    mwgpu_free_tree(ctx, b.dout);
+    acc.out_nodes = (int)tree.nodes.size();
+    acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = acc;
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -610,6 +682,14 @@ int mwh_project_gauss(double prec, mwh_tree *t, int n, const double *coef, const
         auto g = make_gexp(n, coef, ex, pos);
         project<3>(prec, *t->t, [&g](const double *r) { return g.evalf(r); }, max_iter, abs_prec != 0);
         return 0;
+    });
+}
+
+int mwh_project_gauss_device(double prec, mwh_tree *t, int n, const double *coef, const double *ex, const double *pos, int max_iter, int abs_prec,
+                             mwh_apply_stats *stats) {
+    return guard([&] {
+        if (!t || n < 0 || (n > 0 && (!coef || !ex || !pos))) return fail(1, "invalid Gaussian list");
+        return project_device_impl(prec, *t->t, n, coef, ex, pos, max_iter, abs_prec != 0, stats);
     });
 }
 
