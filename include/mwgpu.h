@@ -161,6 +161,20 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tre
  * MWTree.cpp:166-181). */
 mwgpu_status mwgpu_transform(mwgpu_ctx *ctx, mwgpu_tree *tree, int direction, int overwrite);
 
+/* Sum / product level: replaces AdditionCalculator::calcNode
+ * (src/treebuilders/AdditionCalculator.h:42-66) or MultiplicationCalculator::calcNode
+ * (MultiplicationCalculator.h:42-72) for the nodes node_ix[0..n) of `out`:
+ * out = sum_j c[j] inps[j] (compressed coefficients) or the pointwise product
+ * prod_j c[j] inps[j] at the children's quadrature points (reconstruction,
+ * cvTransform with the basis's cv_map / vc_map (K x K, column-major),
+ * compression).  Missing input nodes become GenNodes (getNode).  FP64; node
+ * norms to norms_out (8 per node, optional).  The caller's TreeBuilder loop
+ * does the split test and the final BottomUp (add.cpp, multiply.cpp). */
+#define MWGPU_COMBINE_ADD 0
+#define MWGPU_COMBINE_MULTIPLY 1
+mwgpu_status mwgpu_combine_level(mwgpu_ctx *ctx, int op, int n_in, mwgpu_tree *const *inps, const double *c, const double *cv_map, const double *vc_map,
+                                 mwgpu_tree *out, const int *node_ix, int n, double *norms_out);
+
 /* Projection level: replaces ProjectionCalculator::calcNode
  * (src/treebuilders/ProjectionCalculator.cpp:34-51) for the nodes
  * node_ix[0..n) of `tree` (an output tree), for a sum of Gaussians

@@ -56,6 +56,10 @@ void mwh_mra_free(mwh_mra *mra);
 /* MRA descriptor for the C-ABI; filters must hold 8*(k+1)^2 doubles. */
 int mwh_mra_desc(const mwh_mra *mra, mwgpu_mra_desc *desc, double *filters);
 
+/* The scaling basis's coefficient-to-value and value-to-coefficient maps
+ * (K x K, column-major) and its quadrature roots and weights on [0, 1]
+ * (ScalingBasis::getCVMap, src/core/ScalingBasis.h). */
+int mwh_mra_maps(const mwh_mra *mra, double *cv_map, double *vc_map, double *roots, double *weights);
 int mwh_tree_create(const mwh_mra *mra, mwh_tree **out);
 void mwh_tree_free(mwh_tree *tree);
 /* n Gaussians coef * exp(-exp * |r - pos|^2) (pos: 3n doubles). */
@@ -69,6 +73,13 @@ int mwh_project_gauss(double prec, mwh_tree *tree, int n, const double *coef, co
  * (optional). */
 int mwh_project_gauss_device(double prec, mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos, int max_iter,
                              int abs_prec, mwh_apply_stats *stats);
+/* add(prec, out, FunctionTreeVector, maxIter, absPrec) (src/treebuilders/add.cpp:58-83)
+ * and multiply(prec, out, FunctionTreeVector, maxIter, absPrec) with the
+ * wavelet adaptor (multiply.cpp:70-101): out = sum_j c[j] inps[j] or
+ * prod_j c[j] inps[j], built adaptively from out's current grid; node
+ * computations and BottomUp on the device (mwgpu_combine_level). */
+int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats);
+int mwh_multiply(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats);
 int mwh_copy_grid(mwh_tree *out, const mwh_tree *inp);
 /* node count (non-generated nodes) and tree square norm */
 int mwh_tree_info(const mwh_tree *tree, int *n_nodes, double *square_norm);

@@ -138,11 +138,15 @@ _SIGS = {
     "mwh_mra_from_bounds": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_P)]),
     "mwh_mra_free": (None, [_P]),
     "mwh_mra_desc": (C.c_int, [_P, C.POINTER(MwgpuMraDesc), _PD]),
+    "mwh_mra_maps": (C.c_int, [_P, _PD, _PD, _PD, _PD]),
     "mwh_tree_create": (C.c_int, [_P, C.POINTER(_P)]),
     "mwh_tree_free": (None, [_P]),
     "mwh_build_grid_gauss": (C.c_int, [_P, C.c_int, _PD, _PD, _PD]),
     "mwh_project_gauss": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int]),
     "mwh_copy_grid": (C.c_int, [_P, _P]),
+    "mwh_add": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwh_multiply": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwgpu_combine_level": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P), _PD, _PD, _PD, _P, _PI, C.c_int, _PD]),
     "mwh_project_gauss_device": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwgpu_project_level": (C.c_int, [_P, _P, C.c_int, _PD, _PD, _PD, _PI, C.c_int, _PD]),
     "mwh_tree_info": (C.c_int, [_P, _PI, _PD]),
@@ -226,6 +230,13 @@ class MRA:
         self.nbox = tuple(self._desc.nbox)
         self.sf = self._desc.sf
         self.max_scale = self._desc.max_scale
+
+    def maps(self):
+        """(cv_map, vc_map, roots, weights) of the scaling basis; the maps K x K column-major."""
+        K = self.kp1
+        cv, vc, r, w = np.zeros(K * K), np.zeros(K * K), np.zeros(K), np.zeros(K)
+        _ck(lib().mwh_mra_maps(self._h, _pd(cv), _pd(vc), _pd(r), _pd(w)))
+        return cv, vc, r, w
 
     @property
     def filters(self):
@@ -326,6 +337,28 @@ def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True, devic
                                            C.byref(st)))
         return st.as_dict()
     _ck(lib().mwh_project_gauss(float(prec), tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos), int(max_iter), int(bool(abs_prec))))
+
+
+def _combine(fn, prec, out, terms, max_iter, abs_prec):
+    c = np.ascontiguousarray([float(t[0]) for t in terms], dtype=np.float64)
+    hs = (_P * len(terms))(*[t[1]._h for t in terms])
+    st = MwhApplyStats()
+    _ck(fn(float(prec), out._h, len(terms), _pd(c), hs, int(max_iter), int(bool(abs_prec)), C.byref(st)))
+    return st.as_dict()
+
+
+def add(prec, out, *args, max_iter=-1, abs_prec=False):
+    """add(prec, out, a, A, b, B) or add(prec, out, [(c, tree), ...]) (src/treebuilders/add.cpp):
+    out = sum of c_j f_j, built adaptively on the GPU; returns the statistics."""
+    terms = args[0] if len(args) == 1 else [(args[0], args[1]), (args[2], args[3])]
+    return _combine(lib().mwh_add, prec, out, terms, max_iter, abs_prec)
+
+
+def multiply(prec, out, *args, max_iter=-1, abs_prec=False):
+    """multiply(prec, out, c, A, B) or multiply(prec, out, [(c, tree), ...]) (src/treebuilders/multiply.cpp):
+    out = product of c_j f_j, built adaptively on the GPU; returns the statistics."""
+    terms = args[0] if len(args) == 1 else [(args[0], args[1]), (1.0, args[2])]
+    return _combine(lib().mwh_multiply, prec, out, terms, max_iter, abs_prec)
 
 
 def copy_grid(out, inp):

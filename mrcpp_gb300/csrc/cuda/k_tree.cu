@@ -349,6 +349,97 @@ __global__ void k_project(DevMRA m, DevTree t, const int *nodes, int n, const do
     block_norms(pc, K3, t.norms + (size_t)i * 8, tid, nthr);
 }
 
+// The three directional filter stages of a node transform in shared memory:
+// op 0 compresses 8 child scaling blocks into s + d, op 1 reconstructs
+// (tree_utils::mw_transform / mw_transform_back, tree_utils.cpp:113-301).
+// in: t1, result in t2 (t1 is overwritten).
+__device__ void node_mw3(const DevMRA &m, int op, double *t1, double *t2, int tid, int nthr) {
+    const int K = m.K, K3 = m.kp1_d;
+    double *bufs[2] = {t1, t2};
+    for (int d = 0; d < 3; d++) {
+        double *in = bufs[d & 1], *out = bufs[(d + 1) & 1];
+        const int mask = 1 << d;
+        for (int gt = 0; gt < 8; gt++) dapply<false>(out + gt * K3, in + (gt & ~mask) * K3, filt(m, op, 2 * ((gt >> d) & 1) + 0), K, tid, nthr);
+        __syncthreads();
+        for (int gt = 0; gt < 8; gt++) dapply<true>(out + gt * K3, in + (gt | mask) * K3, filt(m, op, 2 * ((gt >> d) & 1) + 1), K, tid, nthr);
+        __syncthreads();
+    }
+}
+
+// cvTransform (MWNode.cpp:448-490) of 8 child blocks with the K x K map S along
+// x, y, z, times fac: in t1, result in t2
+__device__ void node_cv(const DevMRA &m, const double *S, double fac, double *t1, double *t2, int tid, int nthr) {
+    const int K = m.K, K3 = m.kp1_d;
+    double *bufs[2] = {t1, t2};
+    for (int d = 0; d < 3; d++) {
+        double *in = bufs[d & 1], *out = bufs[(d + 1) & 1];
+        for (int ct = 0; ct < 8; ct++) dapply<false>(out + ct * K3, in + ct * K3, S, K, tid, nthr);
+        __syncthreads();
+    }
+    for (int e = tid; e < 8 * K3; e += nthr) t2[e] *= fac;
+    __syncthreads();
+}
+
+// AdditionCalculator / MultiplicationCalculator::calcNode (AdditionCalculator.h:42-66,
+// MultiplicationCalculator.h:42-72) for one output node per CTA and inputs
+// ins[0..n_in) with factors c[j]: the input node of the same index (a GenNode
+// made beforehand where the input tree has none: scaling block only).  Sum:
+// out = sum_j c_j in_j in the compressed form.  Product: every input node is
+// reconstructed to its children's scaling blocks and transformed to values at
+// the children's quadrature points (cvTransform Forward), the values are
+// multiplied, transformed back (Backward) and compressed.  FP64; node norms.
+template <bool MUL>
+__global__ void k_combine(DevMRA m, const DevTree *ins, const double *c, int n_in, DevTree out, const int *nodes, int n, const double *cv_map,
+                          const double *vc_map, int *err) {
+    extern __shared__ double sm[];
+    const int K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
+    double *acc = sm, *t1 = sm + 8 * K3, *t2 = sm + 16 * K3;
+    const int i = nodes[blockIdx.x];
+    const int4 nd = out.idx[i];
+    const double fw = sqrt(exp2(3.0 * (nd.x + 1)) / (m.sf * m.sf * m.sf));
+    for (int e = tid; e < 8 * K3; e += nthr) acc[e] = MUL ? 1.0 : 0.0;
+    __syncthreads();
+    uint64_t key;
+    const bool kok = pack_key(m, nd.x, nd.y, nd.z, nd.w, key);
+    for (int j = 0; j < n_in; j++) {
+        const DevTree &f = ins[j];
+        const int fid = kok ? hash_find(f.hkeys, f.hvals, f.hcap, key) : -1;
+        if (fid < 0) {
+            if (tid == 0) atomicOr(err, DE_LOOKUP);
+            continue;
+        }
+        const bool gen = fid >= f.cap_real;
+        const double *fc = gen ? f.gcoefs + (size_t)(fid - f.cap_real) * K3 : f.coefs + (size_t)fid * 8 * K3;
+        if (!MUL) {
+            for (int e = tid; e < 8 * K3; e += nthr) acc[e] += c[j] * ((gen && e >= K3) ? 0.0 : fc[e]);
+            continue;
+        }
+        for (int e = tid; e < 8 * K3; e += nthr) t1[e] = (gen && e >= K3) ? 0.0 : fc[e];
+        __syncthreads();
+        node_mw3(m, 1, t1, t2, tid, nthr);        // children's scaling blocks in t2
+        for (int e = tid; e < 8 * K3; e += nthr) t1[e] = t2[e];
+        __syncthreads();
+        node_cv(m, cv_map, fw, t1, t2, tid, nthr);  // values in t2
+        for (int e = tid; e < 8 * K3; e += nthr) acc[e] *= c[j] * t2[e];
+        __syncthreads();
+    }
+    __syncthreads();
+    double *oc = out.coefs + (size_t)i * 8 * K3;
+    if (MUL) {
+        for (int e = tid; e < 8 * K3; e += nthr) t1[e] = acc[e];
+        __syncthreads();
+        node_cv(m, vc_map, 1.0 / fw, t1, t2, tid, nthr);  // coefficients of the children in t2
+        for (int e = tid; e < 8 * K3; e += nthr) t1[e] = t2[e];
+        __syncthreads();
+        node_mw3(m, 0, t1, t2, tid, nthr);                // compressed in t2
+        for (int e = tid; e < 8 * K3; e += nthr) oc[e] = t2[e];
+    } else {
+        for (int e = tid; e < 8 * K3; e += nthr) oc[e] = acc[e];
+    }
+    __syncthreads();
+    block_norms(oc, K3, out.norms + (size_t)i * 8, tid, nthr);
+}
+
 // The transforms of the mixed form: the same three filter stages with FP32
 // products in shared memory, the children / parent coefficients kept in FP64.
 template <bool ADD>
@@ -682,6 +773,15 @@ void launch_project(const DevMRA &m, DevTree t, const int *nodes, int n, const d
     const size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_project<<<n, 256, smem, s>>>(m, t, nodes, n, gauss, ng, vc_map, roots);
+}
+
+void launch_combine(const DevMRA &m, bool mul, const DevTree *ins, const double *c, int n_in, DevTree out, const int *nodes, int n,
+                    const double *cv_map, const double *vc_map, int *err, cudaStream_t s) {
+    if (n <= 0) return;
+    const size_t smem = sizeof(double) * 24 * m.kp1_d;
+    auto kern = mul ? k_combine<true> : k_combine<false>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<n, 256, smem, s>>>(m, ins, c, n_in, out, nodes, n, cv_map, vc_map, err);
 }
 
 void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s, bool fp32) {

@@ -1051,6 +1051,77 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
     return level_entry(ctx, o, 1, inps, outs, nullptr, node_ix, n, prec, &out_sqnorm, norms_out, stats);
 }
 
+mwgpu_status mwgpu_combine_level(mwgpu_ctx *ctx, int op, int n_in, mwgpu_tree *const *inps, const double *c, const double *cv_map, const double *vc_map,
+                                 mwgpu_tree *out, const int *node_ix, int n, double *norms_out) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(op == MWGPU_COMBINE_ADD || op == MWGPU_COMBINE_MULTIPLY, "invalid combine operation");
+    MW_ARG(n_in >= 1 && inps && c && cv_map && vc_map, "invalid inputs or basis tables");
+    MW_ARG(out && !out->is_input, "the result is an output tree");
+    for (int j = 0; j < n_in; j++) MW_ARG(inps[j] && inps[j]->is_input && inps[j]->mra.K == out->mra.K && inps[j]->plans == 0, "invalid input tree");
+    MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
+    for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < out->t.n_real, "node index out of range");
+    cudaSetDevice(ctx->device);
+    if (n == 0) return MWGPU_OK;
+    // GenNodes of the inputs where the output has a node they lack (getNode):
+    // the band machinery with a one-cell band, one segment per input
+    mwgpu_oper cell{};
+    cell.mra = out->mra;
+    cell.op.band_dir = 0;
+    cell.op.band_dir_w = 0;
+    Level lv;
+    lv.o = &cell;
+    lv.nt = n_in;
+    lv.inps = inps;
+    std::vector<mwgpu_tree *> outs(n_in, out);
+    lv.outs = outs.data();
+    lv.n = n * n_in;
+    lv.band_dir = 0;
+    lv.band_w = 0;
+    lv.seg.resize(n_in + 1);
+    for (int j = 0; j <= n_in; j++) lv.seg[j] = j * n;
+    for (int j = 0; j < n_in; j++)
+        for (int i = 0; i < n; i++) {
+            lv.node.push_back(node_ix[i]);
+            lv.tree.push_back(j);
+        }
+    const int prev = ctx->precision;
+    ctx->precision = MWGPU_PREC_FP64;
+    auto restore = [&](mwgpu_status s) {
+        ctx->precision = prev;
+        return s;
+    };
+    if (auto s = ensure_work(ctx, lv.n)) return restore(s);
+    if (auto s = ensure_trees(ctx, n_in)) return restore(s);
+    MW_CK(cudaMemcpyAsync(ctx->d_work, lv.node.data(), sizeof(int) * lv.n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(ctx->d_wtree, lv.tree.data(), sizeof(int) * lv.n, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    std::vector<int> pcount;
+    unsigned long long gen_total = 0;
+    if (auto s = gen_pass(ctx, lv, pcount, gen_total)) return restore(s);
+    ctx->precision = prev;
+    std::vector<DevTree> fs(n_in);
+    for (int j = 0; j < n_in; j++) fs[j] = inps[j]->t;
+    const int K = out->mra.K;
+    if (auto s = grow_buf(ctx, &ctx->d_proj, &ctx->proj_cap, (long long)n_in + 2LL * K * K)) return s;
+    double *d_c = ctx->d_proj, *d_cv = d_c + n_in, *d_vc = d_cv + K * K;
+    MW_CK(cudaMemcpyAsync(ctx->d_fs, fs.data(), sizeof(DevTree) * n_in, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(d_c, c, sizeof(double) * n_in, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(d_cv, cv_map, sizeof(double) * K * K, cudaMemcpyHostToDevice, ctx->stream));
+    MW_CK(cudaMemcpyAsync(d_vc, vc_map, sizeof(double) * K * K, cudaMemcpyHostToDevice, ctx->stream));
+    launch_combine(out->mra, op == MWGPU_COMBINE_MULTIPLY, ctx->d_fs, d_c, n_in, out->t, ctx->d_work, n, d_cv, d_vc, ctx->d_err, ctx->stream);
+    ctx->launches++;
+    if (norms_out) {
+        if (auto s = grow_buf(ctx, &ctx->d_nstage, &ctx->nstage_cap, 8LL * n)) return s;
+        std::vector<int> zeros(n, 0);
+        MW_CK(cudaMemcpyAsync(ctx->d_wtree, zeros.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_gs, &out->t, sizeof(DevTree), cudaMemcpyHostToDevice, ctx->stream));
+        launch_gather_norms(ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_nstage, ctx->stream);
+        ctx->launches++;
+        MW_CK(cudaMemcpyAsync(norms_out, ctx->d_nstage, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    return check_err(ctx, "combine level");
+}
+
 mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *vc_map, const double *roots,
                                  const int *node_ix, int n, double *norms_out) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;

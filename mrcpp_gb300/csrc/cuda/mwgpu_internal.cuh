@@ -222,6 +222,10 @@ void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *pt
                     bool fp32 = false);
 void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s, bool fp32 = false);
 void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s);
+// AdditionCalculator / MultiplicationCalculator::calcNode for the given output
+// nodes over the input trees ins[0..n_in) (device array) with factors c (device)
+void launch_combine(const DevMRA &m, bool mul, const DevTree *ins, const double *c, int n_in, DevTree out, const int *nodes, int n,
+                    const double *cv_map, const double *vc_map, int *err, cudaStream_t s);
 // ProjectionCalculator::calcNode of a Gaussian sum (gauss [ng][5]: coefficient,
 // exponent, position) for the given nodes; vc_map (K x K) and roots (K) of the basis
 void launch_project(const DevMRA &m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map,

@@ -615,6 +615,82 @@ int project_device_impl(double prec, Tree<3> &tree, int n, const double *coef, c
     return 0;
 }
 
+// add (add.cpp:58-83) / multiply (multiply.cpp:70-101, WaveletAdaptor) with
+// the node computations on the device: TreeBuilder + WaveletAdaptor on the
+// host, AdditionCalculator / MultiplicationCalculator::calcNode per iteration
+// through mwgpu_combine_level, BottomUp on the device
+int combine_device_impl(int op, double prec, Tree<3> &out, int n, const double *c, mwh_tree *const *inps, int max_iter, bool abs_prec,
+                        mwh_apply_stats *stats) {
+    for (int j = 0; j < n; j++)
+        if (!(*inps[j]->t->mra == *out.mra)) return fail(1, "Incompatible MRA");
+    auto t0 = std::chrono::steady_clock::now();
+    const MRA<3> &mra = *out.mra;
+    const ScalingBasis &basis = *mra.basis;
+    std::lock_guard<std::mutex> lk(g_gpu_mu);
+    mwgpu_ctx *ctx = gpu_ctx(MWGPU_PREC_FP64);
+    std::vector<double> filters(8 * (size_t)mra.kp1() * mra.kp1());
+    mwgpu_mra_desc md{};
+    fill_desc(mra, &md, filters.data());
+    mwh_apply_stats acc{};
+    std::vector<mwgpu_tree *> dins(n, nullptr);
+    BuildState b;
+    b.tree = &out;
+    auto release = [&] {
+        if (b.dout) mwgpu_free_tree(ctx, b.dout);
+        for (auto *d : dins)
+            if (d) mwgpu_free_tree(ctx, d);
+    };
+    try {
+        for (int j = 0; j < n; j++) dins[j] = upload_input(ctx, md, *inps[j]->t, acc);
+        out.clearGenerated();
+        b.dout = create_output(ctx, md, out, acc);
+        b.synced = out.nodes.size();
+        std::vector<double> nbuf;
+        auto calc = [&](Tree<3> &t, const std::vector<int> &work) {
+            sync_new(ctx, b, acc);
+            nbuf.resize(8 * work.size());
+            ck(mwgpu_combine_level(ctx, op, n, dins.data(), c, basis.cvMap.data(), basis.vcMap.data(), b.dout, work.data(), (int)work.size(),
+                                   nbuf.data()),
+               op == MWGPU_COMBINE_ADD ? "addition level" : "multiplication level");
+            for (size_t j = 0; j < work.size(); j++) {
+                auto &nd = t.nodes[work[j]];
+                double s2 = 0.0;
+                for (int q = 0; q < 8; q++) {
+                    nd.norms[q] = nbuf[8 * j + q];
+                    s2 += nd.norms[q] * nd.norms[q];
+                }
+                nd.squareNorm = s2;
+                nd.flags |= F_HASCOEFS;
+            }
+            acc.iterations++;
+        };
+        auto split = [prec, abs_prec](const Tree<3> &t, int i) { return split_check(t, i, prec, 1.0, abs_prec); };
+        tree_build<3>(out, out.endNodes(), calc, split, max_iter, mra.maxScale());
+        sync_new(ctx, b, acc);
+        ck(mwgpu_transform(ctx, b.dout, MWGPU_BOTTOMUP, 1), "BottomUp transform");
+        std::vector<double> nn(out.nodes.size() * 8);
+        ck(mwgpu_download_tree(ctx, b.dout, out.coefs.data(), nn.data()), "download result tree");
+        for (size_t i = 0; i < out.nodes.size(); i++) {
+            double s2 = 0.0;
+            for (int q = 0; q < 8; q++) {
+                out.nodes[i].norms[q] = nn[i * 8 + q];
+                s2 += nn[i * 8 + q] * nn[i * 8 + q];
+            }
+            out.nodes[i].squareNorm = s2;
+            out.nodes[i].flags |= F_HASCOEFS;
+        }
+        out.calcSquareNorm();
+    } catch (...) {
+        release();
+        throw;
+    }
+    release();
+    acc.out_nodes = (int)out.nodes.size();
+    acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = acc;
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -649,6 +725,17 @@ void mwh_mra_free(mwh_mra *m) { delete m; }
 int mwh_mra_desc(const mwh_mra *m, mwgpu_mra_desc *d, double *filters) {
     if (!m || !d || !filters) return fail(1, "null argument");
     fill_desc(m->m, d, filters);
+    return 0;
+}
+
+int mwh_mra_maps(const mwh_mra *m, double *cv_map, double *vc_map, double *roots, double *weights) {
+    if (!m) return fail(1, "null MRA");
+    const ScalingBasis &b = *m->m.basis;
+    const size_t K = b.K;
+    if (cv_map) std::memcpy(cv_map, b.cvMap.data(), sizeof(double) * K * K);
+    if (vc_map) std::memcpy(vc_map, b.vcMap.data(), sizeof(double) * K * K);
+    if (roots) std::memcpy(roots, b.roots.data(), sizeof(double) * K);
+    if (weights) std::memcpy(weights, b.weights.data(), sizeof(double) * K);
     return 0;
 }
 
@@ -690,6 +777,24 @@ int mwh_project_gauss_device(double prec, mwh_tree *t, int n, const double *coef
     return guard([&] {
         if (!t || n < 0 || (n > 0 && (!coef || !ex || !pos))) return fail(1, "invalid Gaussian list");
         return project_device_impl(prec, *t->t, n, coef, ex, pos, max_iter, abs_prec != 0, stats);
+    });
+}
+
+int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats) {
+    return guard([&] {
+        if (!out || n < 1 || !c || !inps) return fail(1, "invalid sum");
+        for (int j = 0; j < n; j++)
+            if (!inps[j]) return fail(1, "null input tree");
+        return combine_device_impl(MWGPU_COMBINE_ADD, prec, *out->t, n, c, inps, max_iter, abs_prec != 0, stats);
+    });
+}
+
+int mwh_multiply(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats) {
+    return guard([&] {
+        if (!out || n < 1 || !c || !inps) return fail(1, "invalid product");
+        for (int j = 0; j < n; j++)
+            if (!inps[j]) return fail(1, "null input tree");
+        return combine_device_impl(MWGPU_COMBINE_MULTIPLY, prec, *out->t, n, c, inps, max_iter, abs_prec != 0, stats);
     });
 }
 

@@ -62,6 +62,9 @@ def lib(fast=False):
         L.oracle_apply_derivative.restype = C.c_int
         L.oracle_apply_derivative.argtypes = [C.POINTER(OracleMra), C.POINTER(OracleOper), C.POINTER(OracleTree), C.POINTER(OracleTree), C.c_int,
                                               C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        L.oracle_combine.restype = C.c_int
+        L.oracle_combine.argtypes = [C.POINTER(OracleMra), C.c_int, C.c_int, C.POINTER(OracleTree), _PD, _PD, _PD, C.POINTER(OracleTree),
+                                     C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
         L.oracle_result_free.restype = None
         L.oracle_result_free.argtypes = [C.c_void_p]
         _libs[path] = L
@@ -145,6 +148,44 @@ def apply_derivative(out, oper, inp, dir, nthreads=0):
     """Oracle apply(out, DerivativeOperator, inp, dir) (first derivative):
     `out` holds only its roots; returns the flat copy-adapted output tree."""
     return Prepared(1.0, out, oper, inp).run(nthreads, deriv_dir=dir)
+
+
+def combine(op, prec, out, terms, max_iter=-1, abs_prec=False):
+    """Oracle add (op 0) / multiply (op 1) of terms [(c, FunctionTree), ...] from
+    the grid of `out`; returns the flat result tree."""
+    mra = out.mra
+    d = mra.desc()
+    m = OracleMra()
+    m.order, m.root_scale, m.max_scale, m.sf = d.order, d.root_scale, d.max_scale, d.sf
+    for i in range(3):
+        m.corner[i] = d.corner[i]
+        m.nbox[i] = d.nbox[i]
+    filt = np.ascontiguousarray(mra._filters)
+    m.filters = _pd(filt)
+    keep = [filt]
+    trees = (OracleTree * len(terms))()
+    for j, (_, t) in enumerate(terms):
+        x = t.export()
+        keep.append(x)
+        trees[j] = OracleTree(len(x["child0"]), _pi(x["idx"]), _pi(x["child0"]), _pd(x["coefs"]), _pd(x["norms"]))
+    c = np.ascontiguousarray([float(t[0]) for t in terms])
+    cv, vc, _, _ = mra.maps()
+    go = out.export()
+    gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
+    res = C.c_void_p()
+    L = lib()
+    rc = L.oracle_combine(C.byref(m), int(op), len(terms), trees, _pd(c), _pd(cv), _pd(vc), C.byref(gt), float(prec), int(max_iter),
+                          int(bool(abs_prec)), C.byref(res))
+    if rc != 0:
+        raise RuntimeError("oracle_combine failed with code %d" % rc)
+    n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()
+    L.oracle_result_info(res, C.byref(n), C.byref(sq), C.byref(nt), C.byref(nc), C.byref(it))
+    K3 = mra.kp1 ** 3
+    out_ = {"square_norm": sq.value, "iterations": it.value, "n_nodes": n.value, "idx": np.zeros((n.value, 4), dtype=np.int32),
+            "child0": np.zeros(n.value, dtype=np.int32), "coefs": np.zeros((n.value, 8 * K3)), "norms": np.zeros((n.value, 8))}
+    L.oracle_result_export(res, _pi(out_["idx"]), _pi(out_["child0"]), _pd(out_["coefs"]), _pd(out_["norms"]))
+    L.oracle_result_free(res)
+    return out_
 
 
 def to_tree(result, mra):

@@ -983,6 +983,126 @@ int oracle_apply_derivative(const oracle_mra *m, const oracle_oper *od, const or
     return 0;
 }
 
+/* ---------------------------------------------------------------- add / multiply */
+
+/* cvTransform (MWNode.cpp:448-490) of 8 child blocks: S along x, y, z, times fac; in -> out (tmp scratch) */
+static void cv_transform(const oracle_mra *m, const double *S, double fac, double *in, double *out, double *tmp) {
+    const int K = m->order + 1, K3 = K * K * K;
+    for (int ct = 0; ct < 8; ct++) {
+        apply_filter(tmp + (size_t)ct * K3, in + (size_t)ct * K3, S, K, 0);
+        apply_filter(out + (size_t)ct * K3, tmp + (size_t)ct * K3, S, K, 0);
+        apply_filter(tmp + (size_t)ct * K3, out + (size_t)ct * K3, S, K, 0);
+    }
+    for (int e = 0; e < 8 * K3; e++) out[e] = fac * tmp[e];
+}
+
+/* AdditionCalculator / MultiplicationCalculator::calcNode (AdditionCalculator.h:42-66,
+   MultiplicationCalculator.h:42-72) for output node gi */
+static void combine_node(const oracle_mra *m, int op, int n_in, otree *f, const double *c, const double *cv, const double *vc, otree *g, int gi,
+                         double *acc, double *t1, double *t2, double *t3) {
+    const int K3 = g->K3, nc = g->nc;
+    okey gk = g->idx[gi];
+    double fw = sqrt(pow(2.0, 3.0 * (gk.n + 1)) / (m->sf * m->sf * m->sf));
+    for (int e = 0; e < nc; e++) acc[e] = op ? 1.0 : 0.0;
+    for (int j = 0; j < n_in; j++) {
+        int fi = omap_find(&f[j].map, gk);
+        if (fi < 0) continue;
+        const double *fc = f[j].coefs + (size_t)fi * f[j].nc;
+        if (!op) {
+            for (int e = 0; e < nc; e++) acc[e] += c[j] * fc[e];
+            continue;
+        }
+        mw_transform(m, fc, t1, f[j].gen[fi], K3, 1, t2, t3); /* mwTransform(Reconstruction) */
+        cv_transform(m, cv, fw, t1, t2, t3);                  /* cvTransform(Forward) */
+        for (int e = 0; e < nc; e++) acc[e] *= c[j] * t2[e];
+    }
+    double *gc = g->coefs + (size_t)gi * nc;
+    if (op) {
+        cv_transform(m, vc, 1.0 / fw, acc, t1, t3); /* cvTransform(Backward) */
+        mw_transform_back(m, t1, gc, K3, t3);      /* mwTransform(Compression) */
+    } else {
+        memcpy(gc, acc, sizeof(double) * nc);
+    }
+    calc_norms(g, gi);
+}
+
+/* add (add.cpp:58-83) / multiply with the wavelet adaptor (multiply.cpp:70-101):
+   TreeBuilder from the end nodes of out0, then BottomUp and the square norm */
+int oracle_combine(const oracle_mra *m, int op, int n_in, const oracle_tree *inps, const double *c, const double *cv_map, const double *vc_map,
+                   const oracle_tree *out0, double prec, int max_iter, int abs_prec, oracle_result **res) {
+    if (!m || !inps || !c || !cv_map || !vc_map || !out0 || !res || n_in < 1) return 1;
+    otree *f = (otree *)calloc((size_t)n_in, sizeof(otree));
+    for (int j = 0; j < n_in; j++)
+        if (tree_load(&f[j], m, inps[j].n_nodes, inps[j].idx, inps[j].child0, inps[j].coefs, inps[j].norms)) return 2;
+    oracle_result *R = (oracle_result *)calloc(1, sizeof(oracle_result));
+    if (tree_load(&R->g, m, out0->n_nodes, out0->idx, out0->child0, NULL, NULL)) return 2;
+    otree *g = &R->g;
+    const int K3 = g->K3;
+    double *bufs = (double *)malloc(sizeof(double) * 4 * 8 * K3);
+    double *acc = bufs, *t1 = bufs + 8 * K3, *t2 = bufs + 16 * K3, *t3 = bufs + 24 * K3;
+    size_t cnt, nwork = 0;
+    int *lvl, nl;
+    int *all = bfs(g, &cnt, &lvl, &nl);
+    free(lvl);
+    int *work = (int *)malloc(sizeof(int) * (cnt + 1));
+    for (size_t q = 0; q < cnt; q++)
+        if (g->child0[all[q]] < 0) work[nwork++] = all[q];
+    free(all);
+    double sNorm = 0.0, wNorm = 0.0;
+    int iter = 0;
+    while (nwork > 0) {
+        for (size_t w = 0; w < nwork; w++) {
+            for (int j = 0; j < n_in; j++) get_node(&f[j], m, g->idx[work[w]], t1, t2); /* getNode: GenNodes */
+            combine_node(m, op, n_in, f, c, cv_map, vc_map, g, work[w], acc, t1, t2, t3);
+        }
+        if (iter == 0) {
+            sNorm = 0.0;
+            for (size_t w = 0; w < nwork; w++)
+                if (g->idx[work[w]].n - m->root_scale >= 0) sNorm += scaling_norm(g, work[w]);
+        }
+        for (size_t w = 0; w < nwork; w++)
+            if (g->idx[work[w]].n - m->root_scale >= 0) wNorm += wavelet_norm(g, work[w]);
+        g->square_norm = (sNorm < 0.0 || wNorm < 0.0) ? -1.0 : sNorm + wNorm;
+        if (iter >= max_iter && max_iter >= 0) nwork = 0;
+        int *next = (int *)malloc(sizeof(int) * (8 * nwork + 1));
+        size_t nn = 0;
+        for (size_t w = 0; w < nwork; w++) {
+            int i = work[w];
+            if (g->child0[i] >= 0 || g->idx[i].n + 2 > m->max_scale) continue;
+            if (split_check(g, i, prec, 1.0, abs_prec)) {
+                int c0 = create_children(g, i, 0);
+                for (int q = 0; q < 8; q++) next[nn++] = c0 + q;
+            }
+        }
+        free(work);
+        work = next;
+        nwork = nn;
+        iter++;
+    }
+    free(work);
+    R->iterations = iter;
+    int *order_ = bfs(g, &cnt, &lvl, &nl);
+    for (int L = nl - 2; L >= 0; L--)
+        for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+            int i = order_[q];
+            int c0 = g->child0[i];
+            if (c0 < 0) continue;
+            mw_transform_back(m, g->coefs + (size_t)c0 * g->nc, g->coefs + (size_t)i * g->nc, g->nc, t1);
+            calc_norms(g, i);
+        }
+    double sq = 0.0;
+    for (size_t q = 0; q < cnt; q++)
+        if (g->child0[order_[q]] < 0) sq += g->sqn[order_[q]];
+    g->square_norm = sq;
+    free(order_);
+    free(lvl);
+    free(bufs);
+    for (int j = 0; j < n_in; j++) tree_free(&f[j]);
+    free(f);
+    *res = R;
+    return 0;
+}
+
 int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
                        unsigned long long *components, int *iterations) {
     if (!r) return 1;

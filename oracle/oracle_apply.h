@@ -49,6 +49,10 @@ int oracle_apply_sampled(const oracle_mra *mra, const oracle_oper *oper, const o
  * grid is copy-adapted from inp along dir, end nodes computed, then BottomUp. */
 int oracle_apply_derivative(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, int dir, int order,
                             int nthreads, oracle_result **res);
+/* add (op 0) / multiply (op 1): out = sum / product of c[j] inps[j], adaptive
+ * from out0's end nodes at prec; cv_map / vc_map the basis's value maps. */
+int oracle_combine(const oracle_mra *mra, int op, int n_in, const oracle_tree *inps, const double *c, const double *cv_map, const double *vc_map,
+                   const oracle_tree *out0, double prec, int max_iter, int abs_prec, oracle_result **res);
 int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
                        unsigned long long *components, int *iterations);
 int oracle_result_export(const oracle_result *r, int *idx, int *child0, double *coefs, double *norms);
