@@ -65,6 +65,8 @@ void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const D
     if (n_chunks <= 0) return;
     // order 7 with MWGPU_TC set: chunks of block-schedule items go to the
     // tcgen05 kernel (k_tc.cu), the others (screened items) to the kernel below
+    // (the input trees of the level carry their TF32 operands only when they
+    // were uploaded with MWGPU_TC set; the kernel reads them from fs[tree].tc32)
     const bool tc = tc_supported(m.K) && op.btc && tc_counter && std::getenv("MWGPU_TC");
     if (tc) launch_chunk_types(const_cast<int4 *>(chunks), n_chunks, n_chunks_dev, items, s);
     switch (m.K) {

@@ -349,8 +349,11 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     MW_CK(cudaMemcpyAsync(ctx->d_chunks, chunks.data(), sizeof(int4) * nch, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(ctx->d_chunk_begin, cbeg.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    // the tensor-core kernel only where every input tree carries its TF32 operands
+    bool tc_ok = true;
+    for (int t = 0; t < lv.nt; t++) tc_ok = tc_ok && lv.inps[t]->t.tc32 != nullptr;
     launch_contract_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items,
-                          ctx->d_partial, ctx->d_err, ctx->d_tc_counter, ctx->stream);
+                          ctx->d_partial, ctx->d_err, tc_ok ? ctx->d_tc_counter : nullptr, ctx->stream);
     ctx->launches += 2;
     // (the chunk arrays came from pageable memory: the copies read them before returning)
     hs->node_terms = (unsigned long long)total;
@@ -392,8 +395,8 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
         if ((s = pool_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(ctx, tr); return s; }
         launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
         ctx->launches++;
-        // TF32 hi / lo operands of the tensor-core contraction (order 7)
-        if (mwgpu::tc_supported(tr->mra.K) && n > 0) {
+        // TF32 hi / lo operands of the opt-in tensor-core contraction (order 7, MWGPU_TC)
+        if (mwgpu::tc_supported(tr->mra.K) && n > 0 && std::getenv("MWGPU_TC")) {
             if ((s = pool_alloc(ctx, &t.tc32, (size_t)n * mwgpu::kTcNodeFloats))) { free_tree(ctx, tr); return s; }
             mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
             ctx->launches++;
@@ -1521,8 +1524,10 @@ void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
     cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st);
     if (reduce) launch_stamp(pl->d_stamps + 1, st);
     else cudaEventRecord(pl->e1, st);
+    bool tc_ok = true;
+    for (int t = 0; t < pl->nt; t++) tc_ok = tc_ok && pl->inps[t]->t.tc32 != nullptr;
     launch_items(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_chunks, pl->grid, pl->d_items, pl->d_partial, pl->d_err,
-                 pl->d_nchunks, pl->d_counter, pl->d_counter + 1, st);
+                 pl->d_nchunks, pl->d_counter, tc_ok ? pl->d_counter + 1 : nullptr, st);
     if (reduce) launch_reduce_chunks(o->mra, pl->d_gs, pl->d_wtree, pl->d_work, pl->n, pl->d_chunk_begin, pl->d_partial, st);
     ctx->launches += 6 + (reduce ? 2 : 0);
 }
@@ -2084,7 +2089,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             if (order) launch_order_terms(b.goff, nl, b.items_cm, b.items, T, ctx->d_err, st, b.nwork);
             MW_CK(cudaMemsetAsync(b.counter, 0, sizeof(int), st));
             launch_items(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.chunks, grid, b.items, b.partial, ctx->d_err, b.nchunks, b.counter,
-                         b.counter + 1, st);
+                         inp->t.tc32 ? b.counter + 1 : nullptr, st);
             launch_reduce_chunks(m, ctx->d_gs, ctx->d_wtree, b.work, nl, b.chunk_begin, b.partial, st, b.nwork);
             launch_level_norm(out->t, b.work, b.nwork, j == 0, b.state, b.sq + 3 * j, b.goff, b.node_terms, st);  // sNorm: level 0 only
             ctx->launches += 17 + (order ? 1 : 0);
