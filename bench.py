@@ -14,9 +14,11 @@ operator band with at least one contracted component (the reference's own
 screening rules); the count is an integer that equals the oracle's.
 
   value      node-terms/s of the mixed form with the input tree and the
-             operator resident in HBM: per step GenNodes are dropped and
-             rebuilt, every output node is computed, then the TopDown and
-             BottomUp transforms run (CUDA events on the library stream)
+             operator resident in HBM: one planned level per step (GenNode
+             values from the current input, work list, persistent
+             contraction, reduction, TopDown and BottomUp, replayed as one
+             CUDA graph; CUDA events on the library stream); level_path
+             gives the same level through the host-driven mwgpu_apply_level
   e2e        the same metric through mrcpp_gb300.apply (the host mirror of
              mrcpp::apply) with host buffers: input-tree upload, level
              norms and the output-tree download inside the timed region
@@ -598,12 +600,64 @@ def main():
     rel_l2 = float(np.linalg.norm(out_mixed - out_fp64) / np.linalg.norm(out_fp64))
     node_err = float((np.linalg.norm(out_mixed - out_fp64, axis=1) / np.linalg.norm(out_fp64, axis=1).max()).max())
 
-    node_terms = st_mixed.node_terms
-    t_mixed = reduce_max(pg, statistics.mean(ms_mixed))
-    t_fp64 = reduce_max(pg, statistics.mean(ms_fp64))
+    # the same level as a plan (mwgpu_plan_create): GenNode values, work list,
+    # persistent contraction with autotuned chunks, reduction and both
+    # transforms captured once as a CUDA graph and replayed per step (the
+    # path of a fixed-grid apply repeated with new input values)
+    PA1 = C.c_void_p * 1
+    wt0 = np.zeros(n_out, dtype=np.int32)
+
+    def plan_timed(precision):
+        ck(L.mwgpu_set_precision(ctx, precision))
+        ck(L.mwgpu_tree_clear_generated(ctx, dinp))
+        plan = C.c_void_p()
+        sq1 = np.full(1, -1.0)
+        ck(L.mwgpu_plan_create(ctx, dop, 1, PA1(dinp), PA1(dout), mw._pi(wt0), mw._pi(work), n_out, PREC, mw._pd(sq1), 3, C.byref(plan)))
+
+        def pstep():
+            ck(L.mwgpu_scrub_l2(ctx, scrub))
+            ck(L.mwgpu_timer_mark(ctx, 0))
+            ck(L.mwgpu_plan_execute(ctx, plan, None))
+            ck(L.mwgpu_timer_mark(ctx, 1))
+            ms = C.c_double()
+            ck(L.mwgpu_timer_elapsed(ctx, 0, 1, C.byref(ms)))
+            return ms.value
+
+        for _ in range(args.warm):
+            pstep()
+        barrier(pg)
+        ck(L.mwgpu_sync(ctx))
+        l0 = C.c_ulonglong()
+        ck(L.mwgpu_launch_count(ctx, C.byref(l0)))
+        with ClockSampler(local) as cs:
+            ms = [pstep() for _ in range(args.steps)]
+        ck(L.mwgpu_sync(ctx))
+        l1 = C.c_ulonglong()
+        ck(L.mwgpu_launch_count(ctx, C.byref(l1)))
+        pst = mw.MwgpuLevelStats()
+        ck(L.mwgpu_plan_check(ctx, plan, C.byref(pst)))
+        out = np.zeros((n_out, 8 * K ** 3))
+        ck(L.mwgpu_download_tree(ctx, dout, mw._pd(out), None))
+        ck(L.mwgpu_plan_destroy(ctx, plan))
+        barrier(pg)
+        return ms, pst, cs.summary(), (l1.value - l0.value), out
+
+    ms_plan, st_plan, clk_plan, launches_plan, out_plan = plan_timed(mw.MIXED)
+    ms_plan64, st_plan64, _, _, out_plan64 = plan_timed(mw.FP64)
+    plan_l2 = float(np.linalg.norm(out_plan - out_plan64) / np.linalg.norm(out_plan64))
+    plan_node_err = float((np.linalg.norm(out_plan - out_plan64, axis=1) / np.linalg.norm(out_plan64, axis=1).max()).max())
+
+    node_terms = st_plan.node_terms
+    t_level = reduce_max(pg, statistics.mean(ms_mixed))
+    t_mixed = reduce_max(pg, statistics.mean(ms_plan))
+    t_fp64 = reduce_max(pg, statistics.mean(ms_plan64))
     total_nt = reduce_sum(pg, node_terms)
     value = total_nt / (t_mixed / 1e3)
-    value_fp64 = reduce_sum(pg, st_fp64.node_terms) / (t_fp64 / 1e3)
+    value_fp64 = reduce_sum(pg, st_plan64.node_terms) / (t_fp64 / 1e3)
+    value_level = reduce_sum(pg, st_mixed.node_terms) / (t_level / 1e3)
+    t_level64 = reduce_max(pg, statistics.mean(ms_fp64))
+    value_level64 = reduce_sum(pg, st_fp64.node_terms) / (t_level64 / 1e3)
+    clk, launches = clk_plan, launches_plan
 
     # end to end through the public apply (host buffers in, host buffers out)
     e2e_times, h2d, d2h = [], 0, 0
@@ -622,12 +676,13 @@ def main():
 
     # roofline of the contraction kernel (mixed form, last timed launch)
     bf16_peak, hbm_peak, peak_kind = load_peaks()
-    achieved = node_terms * flop_per_nt / (st_mixed.contract_ms / 1e3) / 1e12
+    achieved = node_terms * flop_per_nt / (st_plan.contract_ms / 1e3) / 1e12
     tr = load_traffic() if (args.workload == "poisson" and not args.small) else None
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
             "traffic": (tr or {}).get("dram_bytes_per_launch"), "peak_kind": peak_kind + " bf16 dense burst",
-            "kernel": "k_contract_items<%d> (mixed form, %s)" % (ORDER + 1, "TF32-split mma.sync" if ORDER == 7 else "FP32 FMA"),
-            "kernel_ms": st_mixed.contract_ms,
+            "kernel": ("k_contract_tc (mixed form, tcgen05, MWGPU_TC)" if (ORDER == 7 and os.environ.get("MWGPU_TC")) else
+                       "k_contract_items<%d> (mixed form, %s)" % (ORDER + 1, "TF32-split mma.sync" if ORDER == 7 else "FP32 FMA")),
+            "kernel_ms": st_plan.contract_ms, "kernel_ms_level_path": st_mixed.contract_ms,
             "flop_per_node_term": flop_per_nt}
 
     cpu = None
@@ -651,8 +706,13 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "ms_per_step": t_e2e * 1e3},
-                "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": t_fp64, "contract_ms": st_fp64.contract_ms},
-                "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error": rel_l2, "max_node_error": node_err},
+                "step": "one planned level (mwgpu_plan_execute: GenNode values, work list, persistent contraction, reduction, "
+                        "TopDown and BottomUp replayed as one CUDA graph)",
+                "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": t_fp64, "contract_ms": st_plan64.contract_ms},
+                "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error": plan_l2, "max_node_error": plan_node_err},
+                "level_path": {"value": value_level, "fp64_value": value_level64, "unit": UNIT, "ms_per_step": t_level,
+                               "rel_l2_error": rel_l2, "max_node_error": node_err,
+                               "note": "the host-driven mwgpu_apply_level + transforms (GenNodes dropped and rebuilt each step)"},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     barrier(pg)
