@@ -60,6 +60,9 @@ int mwh_mra_desc(const mwh_mra *mra, mwgpu_mra_desc *desc, double *filters);
  * (K x K, column-major) and its quadrature roots and weights on [0, 1]
  * (ScalingBasis::getCVMap, src/core/ScalingBasis.h). */
 int mwh_mra_maps(const mwh_mra *mra, double *cv_map, double *vc_map, double *roots, double *weights);
+/* MultiResolutionAnalysis::calcMinDistance(eps) and calcMaxDistance()
+ * (src/trees/MultiResolutionAnalysis.h:65-66): the kernel range of an operator. */
+int mwh_mra_distances(const mwh_mra *mra, double eps, double *r_min, double *r_max);
 int mwh_tree_create(const mwh_mra *mra, mwh_tree **out);
 void mwh_tree_free(mwh_tree *tree);
 /* n Gaussians coef * exp(-exp * |r - pos|^2) (pos: 3n doubles). */
@@ -73,6 +76,14 @@ int mwh_project_gauss(double prec, mwh_tree *tree, int n, const double *coef, co
  * (optional). */
 int mwh_project_gauss_device(double prec, mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos, int max_iter,
                              int abs_prec, mwh_apply_stats *stats);
+/* project(prec, tree, std::function<double(const Coord<3> &)>, maxIter, absPrec)
+ * (src/treebuilders/project.cpp:59-63, 85-102) for a host function that is evaluated
+ * on many points per call: f(n, r, values, user) writes the values at the n
+ * points r (3 doubles each).  The points of a TreeBuilder iteration are
+ * passed in calls of at most 2^20 points; the node computations
+ * (ProjectionCalculator::calcNode) and the final BottomUp run on the host. */
+typedef void (*mwh_func)(long long n, const double *r, double *values, void *user);
+int mwh_project_func(double prec, mwh_tree *tree, mwh_func f, void *user, int max_iter, int abs_prec);
 /* add(prec, out, FunctionTreeVector, maxIter, absPrec) (src/treebuilders/add.cpp:58-83)
  * and multiply(prec, out, FunctionTreeVector, maxIter, absPrec) with the
  * wavelet adaptor (multiply.cpp:70-101): out = sum_j c[j] inps[j] or
@@ -81,6 +92,9 @@ int mwh_project_gauss_device(double prec, mwh_tree *tree, int n, const double *c
 int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats);
 int mwh_multiply(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats);
 int mwh_copy_grid(mwh_tree *out, const mwh_tree *inp);
+/* FunctionTree::rescale(c) (src/trees/FunctionTree.cpp:651-668): every stored
+ * coefficient times c, norms and square norm recomputed. */
+int mwh_tree_rescale(mwh_tree *tree, double c);
 /* node count (non-generated nodes) and tree square norm */
 int mwh_tree_info(const mwh_tree *tree, int *n_nodes, double *square_norm);
 /* flat copy: idx[4n], child0[n] (local numbering), coefs[n*8K^3], norms[n*8]; any may be NULL */
@@ -102,6 +116,11 @@ double mwh_integrate(const mwh_tree *tree);
 
 int mwh_poisson(const mwh_mra *mra, double prec, mwh_oper **out);
 int mwh_helmholtz(const mwh_mra *mra, double mu, double prec, mwh_oper **out);
+/* ConvolutionOperator<3>(mra, kernel, prec) (src/operators/ConvolutionOperator.cpp:51-62):
+ * the operator of the 1D Gaussian kernel sum_i coefs[i] exp(-exps[i] x^2)
+ * (e.g. from mwh_poisson_kernel / mwh_helmholtz_kernel), kernel projected at
+ * prec / 10, operator built at prec. */
+int mwh_convolution(const mwh_mra *mra, int n, const double *exps, const double *coefs, double prec, mwh_oper **out);
 /* ABGVOperator(mra, a, b) (src/operators/ABGVOperator.cpp:45-71): first
  * derivative; a = b = 0 center difference (band 0), a = b = 0.5 central
  * difference (band 1). */

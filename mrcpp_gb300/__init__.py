@@ -143,6 +143,10 @@ _SIGS = {
     "mwh_tree_free": (None, [_P]),
     "mwh_build_grid_gauss": (C.c_int, [_P, C.c_int, _PD, _PD, _PD]),
     "mwh_project_gauss": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int]),
+    "mwh_project_func": (C.c_int, [C.c_double, _P, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "mwh_tree_rescale": (C.c_int, [_P, C.c_double]),
+    "mwh_convolution": (C.c_int, [_P, C.c_int, _PD, _PD, C.c_double, C.POINTER(_P)]),
+    "mwh_mra_distances": (C.c_int, [_P, C.c_double, _PD, _PD]),
     "mwh_copy_grid": (C.c_int, [_P, _P]),
     "mwh_add": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwh_multiply": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
@@ -231,6 +235,18 @@ class MRA:
         self.sf = self._desc.sf
         self.max_scale = self._desc.max_scale
 
+    def calcMinDistance(self, eps):
+        """sqrt(eps 2^-maxScale) (MultiResolutionAnalysis.h:65)."""
+        r = C.c_double()
+        _ck(lib().mwh_mra_distances(self._h, float(eps), C.byref(r), None))
+        return r.value
+
+    def calcMaxDistance(self):
+        """Diagonal of the world box (MultiResolutionAnalysis::calcMaxDistance)."""
+        r = C.c_double()
+        _ck(lib().mwh_mra_distances(self._h, 1.0, None, C.byref(r)))
+        return r.value
+
     def maps(self):
         """(cv_map, vc_map, roots, weights) of the scaling basis; the maps K x K column-major."""
         K = self.kp1
@@ -310,6 +326,10 @@ class FunctionTree:
     def integrate(self):
         return lib().mwh_integrate(self._h)
 
+    def rescale(self, c):
+        """FunctionTree::rescale(c) (src/trees/FunctionTree.cpp:651-668)."""
+        _ck(lib().mwh_tree_rescale(self._h, float(c)))
+
 
 def _gauss_arrays(gaussians):
     coef = np.ascontiguousarray([g[0] for g in gaussians], dtype=np.float64)
@@ -324,10 +344,40 @@ def build_grid(tree, gaussians):
     _ck(lib().mwh_build_grid_gauss(tree._h, len(coef), _pd(coef), _pd(ex), _pd(pos)))
 
 
+_FUNC = C.CFUNCTYPE(None, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
+
+
+def _project_func(prec, tree, func, max_iter, abs_prec):
+    errors = []
+
+    def cb(n, r, v, _user):
+        try:
+            pts = np.ctypeslib.as_array(r, shape=(n, 3))
+            out = np.ctypeslib.as_array(v, shape=(n,))
+            out[:] = np.asarray(func(pts), dtype=np.float64).reshape(n)
+        except BaseException as e:  # reported after the C call returns
+            errors.append(e)
+
+    f = _FUNC(cb)
+    code = lib().mwh_project_func(float(prec), tree._h, C.cast(f, C.c_void_p), None, int(max_iter), int(bool(abs_prec)))
+    if errors:
+        raise errors[0]
+    _ck(code)
+
+
 def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True, device=False):
     """build_grid (optional) + project(prec, tree, GaussExp) (src/treebuilders/project.cpp:41-66).
     device=True computes the nodes on the GPU (mwgpu_project_level) and returns
-    the statistics; the default projects on the host like the reference."""
+    the statistics; the default projects on the host like the reference.
+
+    gaussians may also be a function: project(prec, tree, func) with func
+    taking an (n, 3) array of points and returning n values is
+    project(prec, tree, std::function) (project.cpp:59-63), projected on the
+    host from the tree's current grid (no grid is built for it)."""
+    if callable(gaussians):
+        if device:
+            raise ValueError("functions are projected on the host; device=True takes Gaussians")
+        return _project_func(prec, tree, gaussians, max_iter, abs_prec)
     if grid:
         build_grid(tree, gaussians)
     coef, ex, pos = _gauss_arrays(gaussians)
@@ -370,9 +420,22 @@ def dot(a, b):
 
 
 class ConvolutionOperator:
-    """Separated Gaussian convolution operator (src/operators/ConvolutionOperator.h)."""
+    """Separated Gaussian convolution operator (src/operators/ConvolutionOperator.h).
 
-    def __init__(self, mra, handle):
+    ConvolutionOperator(mra, kernel, prec) is ConvolutionOperator<3>(MRA, kernel,
+    prec) (ConvolutionOperator.cpp:51-62): kernel = (exponents, coefficients) of
+    the 1D Gaussians, e.g. from helmholtz_kernel / poisson_kernel."""
+
+    def __init__(self, mra, handle, prec=None):
+        if prec is not None:
+            ex = np.ascontiguousarray(handle[0], dtype=np.float64)
+            co = np.ascontiguousarray(handle[1], dtype=np.float64)
+            if ex.shape != co.shape or ex.ndim != 1:
+                raise ValueError("kernel: exponents and coefficients of equal length")
+            h = _P()
+            _ck(lib().mwh_convolution(mra._h, len(ex), _pd(ex), _pd(co), float(prec), C.byref(h)))
+            handle = h
+            self.prec = prec
         self.mra = mra
         self._h = handle
         nt, nn, nr = C.c_int(), C.c_int(), C.c_int()

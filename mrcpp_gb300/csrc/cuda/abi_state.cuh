@@ -19,6 +19,7 @@ using mwgpu::DevMRA;
 using mwgpu::DevOper;
 using mwgpu::DevTree;
 using mwgpu::LevelStats;
+using mwgpu::NodeKey;
 using mwgpu::WorkItem;
 
 // Device blocks of trees, cached per context.  Freeing a tree hands its blocks
@@ -55,10 +56,10 @@ struct mwgpu_ctx {
     double *d_nstage = nullptr;  // norms of the computed nodes, staged for the host
     long long nstage_cap = 0;
     // pending GenNode set
-    uint64_t *d_pkeys = nullptr;
+    NodeKey *d_pkeys = nullptr;
     int *d_pvals = nullptr;
     int phcap = 0;
-    uint64_t *d_plist = nullptr;
+    NodeKey *d_plist = nullptr;
     int pcap = 0;
     long long ph_total = 0, pl_total = 0;
     int *d_pcount = nullptr;  // one pending count per tree

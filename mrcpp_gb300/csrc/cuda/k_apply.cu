@@ -47,11 +47,11 @@ __device__ inline bool band_box(const DevMRA &m, const DevOper &op, int4 g, int 
     int gl[3] = {g.y, g.z, g.w};
     b.total = 1;
     for (int d = 0; d < 3; d++) {
-        int nboxes = m.nbox[d] * (1 << depth);
-        int c = m.corner[d] * (1 << depth);
+        // world bounds at this depth (64-bit: nbox 2^30 exceeds int)
+        const long long c = (long long)m.corner[d] * (1ll << depth), nboxes = (long long)m.nbox[d] * (1ll << depth);
         const int wd = (op.band_dir < 0 || op.band_dir == d) ? w : 0;
-        b.s[d] = max(gl[d] - wd, c);
-        b.e[d] = min(gl[d] + wd, c + nboxes - 1);
+        b.s[d] = (int)max((long long)gl[d] - wd, c);
+        b.e[d] = (int)min((long long)gl[d] + wd, c + nboxes - 1);
         b.total *= (b.e[d] - b.s[d] + 1);
     }
     return b.total > 0;
@@ -64,8 +64,8 @@ __device__ inline void box_cell(const Box &b, int q, int &x, int &y, int &z) {
     z = b.s[2] + q / (nx * ny);
 }
 
-__global__ void k_band_missing(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work, uint64_t *pkeys,
-                               int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err) {
+__global__ void k_band_missing(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work, NodeKey *pkeys,
+                               int *pvals, int phcap, NodeKey *plist, int *pcount, int pcap, int *err) {
     int gi = work[blockIdx.x];
     int4 gx = g.idx[gi];
     int depth;
@@ -74,7 +74,7 @@ __global__ void k_band_missing(DevMRA m, DevOper op, DevTree f, DevTree g, const
     for (int q = threadIdx.x; q < b.total; q += blockDim.x) {
         int x, y, z;
         box_cell(b, q, x, y, z);
-        uint64_t key;
+        NodeKey key;
         if (!pack_key(m, gx.x, x, y, z, key)) { atomicOr(err, DE_RANGE); continue; }
         if (hash_find(f.hkeys, f.hvals, f.hcap, key) >= 0) continue;
         bool full = false;
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
             int fx, fy, fz;
             box_cell(b, q, fx, fy, fz);
             if (tid == 0) {
-                uint64_t key;
+                NodeKey key;
                 int id = -1;
                 if (pack_key(m, gx.x, fx, fy, fz, key)) id = hash_find(f.hkeys, f.hvals, f.hcap, key);
                 if (id < 0) atomicOr(err, DE_LOOKUP);
@@ -246,9 +246,9 @@ __global__ void __launch_bounds__(256) k_deriv(DevMRA m, DevOper op, DevTree f, 
         for (int w = -width; w <= width; w++) {
             int fl[3] = {gl[0], gl[1], gl[2]};
             fl[dir] += w;
-            const int c0 = m.corner[dir] * (1 << depth), nbx = m.nbox[dir] * (1 << depth);
-            if (fl[dir] < c0 || fl[dir] >= c0 + nbx) continue;  // outside the world (getRootIndex < 0)
-            uint64_t key;
+            const long long c0 = (long long)m.corner[dir] * (1ll << depth), nbx = (long long)m.nbox[dir] * (1ll << depth);
+            if ((long long)gl[dir] + w < c0 || (long long)gl[dir] + w >= c0 + nbx) continue;  // outside the world (getRootIndex < 0)
+            NodeKey key;
             if (!pack_key(m, gx.x, fl[0], fl[1], fl[2], key)) {
                 if (tid == 0) atomicOr(err, DE_RANGE);
                 continue;
@@ -337,7 +337,7 @@ void launch_deriv(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree 
 }
 
 void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
-                         uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s) {
+                         NodeKey *pkeys, int *pvals, int phcap, NodeKey *plist, int *pcount, int pcap, int *err, cudaStream_t s) {
     if (n_work <= 0) return;
     k_band_missing<<<n_work, 256, 0, s>>>(m, op, f, g, work, n_work, pkeys, pvals, phcap, plist, pcount, pcap, err);
 }

@@ -191,7 +191,7 @@ __device__ inline double norm_estimate(const DevMRA &m, const DevTree &f, int n,
     *stored = 0;
     for (int a = n; a >= m.root_scale; a--) {
         const int sh = n - a;
-        uint64_t key;
+        NodeKey key;
         if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) return 0.0;
         const int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
         if (id >= 0 && id < f.cap_real) {

@@ -37,16 +37,6 @@ __device__ __forceinline__ void dapply(double *out, const double *in, const doub
     }
 }
 
-__device__ inline void unpack_key(const DevMRA &m, uint64_t key, int &n, int &l0, int &l1, int &l2) {
-    int d = (int)(key & 31);
-    n = m.root_scale + d;
-    int l[3];
-    for (int i = 0; i < 3; i++) l[i] = (int)((key >> (5 + 19 * i)) & ((1u << 19) - 1)) + m.corner[i] * (1 << d);
-    l0 = l[0];
-    l1 = l[1];
-    l2 = l[2];
-}
-
 __device__ inline const double *filt(const DevMRA &m, int op, int fidx) { return m.filt + ((size_t)op * 4 + fidx) * m.K * m.K; }
 
 __global__ void k_hash_build(DevMRA m, DevTree t, int first, int count, int *err) {
@@ -54,7 +44,7 @@ __global__ void k_hash_build(DevMRA m, DevTree t, int first, int count, int *err
     if (i >= count) return;
     int id = first + i;
     int4 x = t.idx[id];
-    uint64_t key;
+    NodeKey key;
     if (!pack_key(m, x.x, x.y, x.z, x.w, key)) { atomicOr(err, DE_RANGE); return; }
     bool full = false;
     hash_insert(t.hkeys, t.hvals, t.hcap, key, id, &full);
@@ -63,7 +53,7 @@ __global__ void k_hash_build(DevMRA m, DevTree t, int first, int count, int *err
 
 // One CTA per pending GenNode: walk up to the nearest node present in the
 // lookup table, then reconstruct down along the path to the requested child.
-__global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, bool real_only) {
+__global__ void k_gen_nodes(DevMRA m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, bool real_only) {
     extern __shared__ double sm[];
     const int K = m.K, K3 = m.kp1_d;
     double *b0 = sm;           // 4 K^3
@@ -78,7 +68,7 @@ __global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pe
         s_ancn = 0;
         for (int a = n - 1; a >= m.root_scale; a--) {
             int sh = n - a;
-            uint64_t key;
+            NodeKey key;
             if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
             int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
             if (id >= 0 && (!real_only || id < f.cap_real)) { s_anc = id; s_ancn = a; break; }
@@ -170,7 +160,7 @@ __global__ void k_gen_nodes(DevMRA m, DevTree f, const uint64_t *plist, int n_pe
     }
 }
 
-__global__ void k_gen_insert(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err) {
+__global__ void k_gen_insert(DevMRA m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n_pend) return;
     bool full = false;
@@ -399,7 +389,7 @@ __global__ void k_combine(DevMRA m, const DevTree *ins, const double *c, int n_i
     const double fw = sqrt(exp2(3.0 * (nd.x + 1)) / (m.sf * m.sf * m.sf));
     for (int e = tid; e < 8 * K3; e += nthr) acc[e] = MUL ? 1.0 : 0.0;
     __syncthreads();
-    uint64_t key;
+    NodeKey key;
     const bool kok = pack_key(m, nd.x, nd.y, nd.z, nd.w, key);
     for (int j = 0; j < n_in; j++) {
         const DevTree &f = ins[j];
@@ -579,7 +569,7 @@ __global__ void __launch_bounds__(kTransformThreads) k_mw_up32(DevMRA m, DevTree
 // (read by the mixed contraction) and, widened, to gcoefs; the scaling norm is
 // accumulated in FP64.  The intermediate steps stay in FP32, so a chain through
 // stored GenNodes gives the same values as one walk from the real ancestor.
-__global__ void k_gen_nodes32(DevMRA m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, bool real_only) {
+__global__ void k_gen_nodes32(DevMRA m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, bool real_only) {
     extern __shared__ float sg32[];
     const int K = m.K, K2 = K * K, K3 = m.kp1_d;
     float *b0 = sg32, *b1 = b0 + 4 * K3, *F = b1 + 4 * K3;  // F: the 4 reconstruction filters
@@ -594,7 +584,7 @@ __global__ void k_gen_nodes32(DevMRA m, DevTree f, const uint64_t *plist, int n_
         s_ancn = 0;
         for (int a = n - 1; a >= m.root_scale; a--) {
             const int sh = n - a;
-            uint64_t key;
+            NodeKey key;
             if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
             const int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
             if (id >= 0 && (!real_only || id < f.cap_real)) {
@@ -729,7 +719,7 @@ void launch_hash_build(const DevMRA &m, DevTree t, int first, int count, int *er
     k_hash_build<<<(count + 255) / 256, 256, 0, s>>>(m, t, first, count, err);
 }
 
-void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s, bool real_only,
+void launch_gen_nodes(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s, bool real_only,
                       bool fp32) {
     if (n_pend <= 0) return;
     if (fp32) {
@@ -743,7 +733,7 @@ void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_p
     k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
 }
 
-void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {
+void launch_gen_insert(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {
     if (n_pend <= 0) return;
     k_gen_insert<<<(n_pend + 255) / 256, 256, 0, s>>>(m, f, plist, n_pend, gen_base, err);
 }

@@ -90,9 +90,9 @@ __device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const Dev
     const int gl[3] = {gx.y, gx.z, gx.w};
     int bs[3], be[3];
     for (int d = 0; d < 3; d++) {
-        int nboxes = m.nbox[d] * (1 << depth), c = m.corner[d] * (1 << depth);
-        bs[d] = max(gl[d] - w, c);
-        be[d] = min(gl[d] + w, c + nboxes - 1);
+        const long long c = (long long)m.corner[d] * (1ll << depth), nboxes = (long long)m.nbox[d] * (1ll << depth);
+        bs[d] = (int)max((long long)gl[d] - w, c);
+        be[d] = (int)min((long long)gl[d] + w, c + nboxes - 1);
     }
     const long long q = p - pair_off[wi];
     const int nx = be[0] - bs[0] + 1, ny = be[1] - bs[1] + 1;
@@ -103,7 +103,7 @@ __device__ inline bool locate_pair(const DevMRA &m, const DevOper &op, const Dev
     pc.tl[0] = fx - gl[0];
     pc.tl[1] = fy - gl[1];
     pc.tl[2] = fz - gl[2];
-    uint64_t key;
+    NodeKey key;
     pc.fid = -1;
     if (pack_key(m, gx.x, fx, fy, fz, key)) pc.fid = hash_find(f.hkeys, f.hvals, f.hcap, key);
     return pc.fid >= 0;

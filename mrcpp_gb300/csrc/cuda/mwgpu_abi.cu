@@ -66,7 +66,7 @@ mwgpu_status rebuild_hash(mwgpu_ctx *ctx, mwgpu_tree *tr, long long entries) {
         if (auto s = pool_alloc(ctx, &t.hvals, hcap)) return s;
         t.hcap = hcap;
     }
-    MW_CK(cudaMemsetAsync(t.hkeys, 0xFF, sizeof(uint64_t) * hcap, ctx->stream));
+    MW_CK(cudaMemsetAsync(t.hkeys, 0xFF, sizeof(NodeKey) * hcap, ctx->stream));
     MW_CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     launch_hash_build(tr->mra, t, 0, t.n_real, ctx->d_err, ctx->stream);
     ctx->launches += t.n_real > 0;
@@ -456,7 +456,7 @@ mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount,
     pcount.assign(nt, 0);
     for (int attempt = 0; attempt < 8; attempt++) {
         if (auto s = ensure_pending(ctx, std::max(ctx->phcap, 1 << 16), std::max(ctx->pcap, 1 << 15), nt)) return s;
-        MW_CK(cudaMemsetAsync(ctx->d_pkeys, 0xFF, sizeof(uint64_t) * ctx->phcap * nt, ctx->stream));
+        MW_CK(cudaMemsetAsync(ctx->d_pkeys, 0xFF, sizeof(NodeKey) * ctx->phcap * nt, ctx->stream));
         MW_CK(cudaMemsetAsync(ctx->d_pcount, 0, sizeof(int) * nt, ctx->stream));
         for (int t = 0; t < nt; t++) {
             const int b = lv.seg[t], e = lv.seg[t + 1];
@@ -486,7 +486,7 @@ mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount,
         if (auto s = grow_gen(ctx, inp, f.n_gen + pcount[t])) return s;
         if (2LL * (f.n_real + f.n_gen + pcount[t]) + 16 > f.hcap)
             if (auto s = rebuild_hash(ctx, inp, (long long)f.n_real + f.n_gen + pcount[t])) return s;
-        const uint64_t *pl = ctx->d_plist + (size_t)t * ctx->pcap;
+        const NodeKey *pl = ctx->d_plist + (size_t)t * ctx->pcap;
         launch_gen_nodes(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream, false, fp32);
         launch_gen_insert(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream);
         ctx->launches += 2;
@@ -1482,7 +1482,7 @@ struct mwgpu_plan {
     LevelStats *d_stats = nullptr;
     int *d_err = nullptr;
     unsigned long long *d_stamps = nullptr;  // level start, contraction start / end, level end (ns)
-    std::vector<uint64_t *> d_gkeys;
+    std::vector<NodeKey *> d_gkeys;
     std::vector<int> gcount;
     int *d_list = nullptr, *d_ltree = nullptr;
     std::vector<std::pair<int, int>> ranges;
@@ -1691,7 +1691,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
     for (int t = 0; t < n_trees; t++) {
         if (pcount[t] == 0) continue;
         if ((s = plan_alloc(ctx, pl, &pl->d_gkeys[t], pcount[t]))) return fail(s);
-        MW_CK(cudaMemcpyAsync(pl->d_gkeys[t], ctx->d_plist + (size_t)t * ctx->pcap, sizeof(uint64_t) * pcount[t], cudaMemcpyDeviceToDevice,
+        MW_CK(cudaMemcpyAsync(pl->d_gkeys[t], ctx->d_plist + (size_t)t * ctx->pcap, sizeof(NodeKey) * pcount[t], cudaMemcpyDeviceToDevice,
                               ctx->stream));
     }
     // transforms: parents per depth over all output trees

@@ -19,7 +19,16 @@ namespace mwgpu {
 
 constexpr int kMaxDepthRows = 30;   // ConvolutionCalculator band-size rows (MaxDepth)
 constexpr double kMachineZero = 1.0e-14;
-constexpr uint64_t kEmptyKey = ~0ull;
+// Node key of the lookup tables: depth d and the three translation offsets
+// from the world corner, t_i = l_i - corner_i 2^d (0 <= t_i < nbox_i 2^d):
+// lo = t0 | t1 << 32, hi = t2 | d << 32.  Every node index the reference can
+// form (depth <= 30 below the root scale, 32-bit translations) has a key; a
+// slot with every bit set is empty.
+struct __align__(16) NodeKey {
+    unsigned long long lo, hi;
+};
+__host__ __device__ inline bool operator==(const NodeKey &a, const NodeKey &b) { return a.lo == b.lo && a.hi == b.hi; }
+__host__ __device__ inline bool key_empty(const NodeKey &k) { return k.lo == ~0ull && k.hi == ~0ull; }
 // chunk length of the mixed contraction: max(8, ceil(items / kChunkTarget))
 constexpr long long kChunkTarget = 8 * 304;
 // term-major ordering of the work items (k_order_terms): threads, most terms
@@ -87,48 +96,77 @@ struct DevTree {
     float *gcoefs32;             // input trees: FP32 copy of gcoefs
     float *tc32;                 // K = 8 input trees: TF32 hi / lo of every node in the tensor-core layout (k_tc.cu)
     float *gtc32;                // K = 8 input trees: the same for the scaling block of every GenNode
-    uint64_t *hkeys;             // [hcap]
+    NodeKey *hkeys;              // [hcap]
     int *hvals;                  // [hcap]
     int hcap;                    // power of two
 };
 
-__host__ __device__ inline bool pack_key(const DevMRA &m, int n, int l0, int l1, int l2, uint64_t &key) {
-    int d = n - m.root_scale;
+__host__ __device__ inline bool pack_key(const DevMRA &m, int n, int l0, int l1, int l2, NodeKey &key) {
+    const int d = n - m.root_scale;
     if (d < 0 || d > 30) return false;
-    int l[3] = {l0, l1, l2};
-    uint64_t k = (uint64_t)d;
+    const int l[3] = {l0, l1, l2};
+    unsigned long long t[3];
     for (int i = 0; i < 3; i++) {
-        long long t = (long long)l[i] - (long long)m.corner[i] * (1ll << d);
-        if (t < 0 || t >= (long long)m.nbox[i] * (1ll << d) || t >= (1ll << 19)) return false;
-        k |= (uint64_t)t << (5 + 19 * i);
+        const long long v = (long long)l[i] - (long long)m.corner[i] * (1ll << d);
+        if (v < 0 || v >= (long long)m.nbox[i] * (1ll << d) || v > 0xffffffffll) return false;
+        t[i] = (unsigned long long)v;
     }
-    key = k;
+    key.lo = t[0] | t[1] << 32;
+    key.hi = t[2] | (unsigned long long)d << 32;
     return true;
 }
 
-__host__ __device__ inline uint32_t hash_slot(uint64_t key, int hcap) {
-    uint64_t h = key * 0x9E3779B97F4A7C15ull;
-    h ^= h >> 29;
+__host__ __device__ inline void unpack_key(const DevMRA &m, const NodeKey &key, int &n, int &l0, int &l1, int &l2) {
+    const int d = (int)(key.hi >> 32);
+    n = m.root_scale + d;
+    l0 = (int)((long long)(key.lo & 0xffffffffull) + (long long)m.corner[0] * (1ll << d));
+    l1 = (int)((long long)(key.lo >> 32) + (long long)m.corner[1] * (1ll << d));
+    l2 = (int)((long long)(key.hi & 0xffffffffull) + (long long)m.corner[2] * (1ll << d));
+}
+
+__host__ __device__ inline uint32_t hash_slot(const NodeKey &key, int hcap) {
+    // both words folded, then the 64-bit finaliser of MurmurHash3 (every key
+    // bit reaches every slot bit)
+    uint64_t h = key.lo ^ (key.hi * 0x9E3779B97F4A7C15ull);
+    h ^= h >> 33;
+    h *= 0xFF51AFD7ED558CCDull;
+    h ^= h >> 33;
+    h *= 0xC4CEB9FE1A85EC53ull;
+    h ^= h >> 33;
     return (uint32_t)(h & (uint64_t)(hcap - 1));
 }
 
-__device__ inline int hash_find(const uint64_t *keys, const int *vals, int hcap, uint64_t key) {
+__device__ inline int hash_find(const NodeKey *keys, const int *vals, int hcap, const NodeKey &key) {
     uint32_t s = hash_slot(key, hcap);
     for (int probe = 0; probe < hcap; probe++) {
-        uint64_t k = keys[s];
+        const NodeKey k = keys[s];
         if (k == key) return vals[s];
-        if (k == kEmptyKey) return -1;
+        if (key_empty(k)) return -1;
         s = (s + 1) & (hcap - 1);
     }
     return -1;
 }
 
+// 128-bit compare-and-swap of a global table slot (PTX atom.cas.b128, sm_90
+// and later); returns the slot's previous content.
+__device__ inline NodeKey key_cas(NodeKey *slot, const NodeKey &cmp, const NodeKey &val) {
+    NodeKey old;
+    asm volatile(
+        "{\n\t.reg .b128 d, b, c;\n\tmov.b128 b, {%2, %3};\n\tmov.b128 c, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], b, c;\n\tmov.b128 {%0, %1}, d;\n}\n"
+        : "=l"(old.lo), "=l"(old.hi)
+        : "l"(cmp.lo), "l"(cmp.hi), "l"(val.lo), "l"(val.hi), "l"(slot)
+        : "memory");
+    return old;
+}
+
 // Inserts key; returns true if this call inserted it. Bounded probing.
-__device__ inline bool hash_insert(uint64_t *keys, int *vals, int hcap, uint64_t key, int val, bool *full) {
+__device__ inline bool hash_insert(NodeKey *keys, int *vals, int hcap, const NodeKey &key, int val, bool *full) {
+    const NodeKey empty{~0ull, ~0ull};
     uint32_t s = hash_slot(key, hcap);
     for (int probe = 0; probe < hcap; probe++) {
-        unsigned long long prev = atomicCAS((unsigned long long *)&keys[s], (unsigned long long)kEmptyKey, (unsigned long long)key);
-        if (prev == kEmptyKey) { vals[s] = val; return true; }
+        const NodeKey prev = key_cas(&keys[s], empty, key);
+        if (key_empty(prev)) { vals[s] = val; return true; }
         if (prev == key) return false;
         s = (s + 1) & (hcap - 1);
     }
@@ -162,14 +200,14 @@ struct LevelStats {
 
 // kernel launchers (k_apply.cu / k_tree.cu)
 void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
-                         uint64_t *pkeys, int *pvals, int phcap, uint64_t *plist, int *pcount, int pcap, int *err, cudaStream_t s);
+                         NodeKey *pkeys, int *pvals, int phcap, NodeKey *plist, int *pcount, int pcap, int *err, cudaStream_t s);
 // real_only: reconstruct from the nearest real ancestor even where a GenNode
 // ancestor exists (GenNodes that are rewritten by the same launch)
 // GenNodes of the pending keys plist[0..n_pend) into slots gen_base + p
 // (fp32: FP32 products, the GenNodes of the mixed form)
-void launch_gen_nodes(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s,
+void launch_gen_nodes(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s,
                       bool real_only = false, bool fp32 = false);
-void launch_gen_insert(const DevMRA &m, DevTree f, const uint64_t *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
+void launch_gen_insert(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
 // DerivativeCalculator::calcNode for the work entries (output leaves): band along
 // op.band_dir, 1D application of term 0 with the identity elsewhere, divided by
 // sf^order; FP64

@@ -739,6 +739,13 @@ int mwh_mra_maps(const mwh_mra *m, double *cv_map, double *vc_map, double *roots
     return 0;
 }
 
+int mwh_mra_distances(const mwh_mra *m, double eps, double *r_min, double *r_max) {
+    if (!m || !(eps > 0.0)) return fail(1, "invalid MRA distance arguments");
+    if (r_min) *r_min = m->m.calcMinDistance(eps);
+    if (r_max) *r_max = m->m.calcMaxDistance();
+    return 0;
+}
+
 int mwh_tree_create(const mwh_mra *m, mwh_tree **out) {
     return guard([&] {
         if (!m || !out) return fail(1, "null argument");
@@ -768,6 +775,14 @@ int mwh_project_gauss(double prec, mwh_tree *t, int n, const double *coef, const
         if (!t || n < 0 || (n > 0 && (!coef || !ex || !pos))) return fail(1, "invalid Gaussian list");
         auto g = make_gexp(n, coef, ex, pos);
         project<3>(prec, *t->t, [&g](const double *r) { return g.evalf(r); }, max_iter, abs_prec != 0);
+        return 0;
+    });
+}
+
+int mwh_project_func(double prec, mwh_tree *t, mwh_func f, void *user, int max_iter, int abs_prec) {
+    return guard([&] {
+        if (!t || !f) return fail(1, "invalid projection arguments");
+        project_batched<3>(prec, *t->t, [f, user](long long n, const double *r, double *v) { f(n, r, v, user); }, max_iter, abs_prec != 0);
         return 0;
     });
 }
@@ -814,6 +829,22 @@ int mwh_tree_info(const mwh_tree *t, int *n, double *sq) {
     if (n) *n = c;
     if (sq) *sq = t->t->squareNorm;
     return 0;
+}
+
+int mwh_tree_rescale(mwh_tree *t, double c) {
+    return guard([&] {
+        if (!t) return fail(1, "null tree");
+        auto &tr = *t->t;
+        const size_t nc = (size_t)tr.nCoefs;
+        for (size_t i = 0; i < tr.nodes.size(); i++) {
+            if (tr.isGen((int)i) || !(tr.nodes[i].flags & F_HASCOEFS)) continue;
+            double *x = tr.c((int)i);
+            for (size_t j = 0; j < nc; j++) x[j] *= c;
+            tr.calcNorms((int)i);
+        }
+        tr.calcSquareNorm();
+        return 0;
+    });
 }
 
 int mwh_tree_export(const mwh_tree *t, int *idx, int *child0, double *coefs, double *norms) {
@@ -985,6 +1016,21 @@ int mwh_helmholtz(const mwh_mra *m, double mu, double prec, mwh_oper **out) {
     return guard([&] {
         if (!m || !out || !(prec > 0.0) || !(mu > 0.0)) return fail(1, "invalid Helmholtz operator arguments");
         auto *o = new mwh_oper{make_helmholtz(m->m, mu, prec), {}, {}, {}, {}};
+        finish_oper(o);
+        *out = o;
+        return 0;
+    });
+}
+
+int mwh_convolution(const mwh_mra *m, int n, const double *exps, const double *coefs, double prec, mwh_oper **out) {
+    return guard([&] {
+        if (!m || !out || n < 1 || !exps || !coefs || !(prec > 0.0)) return fail(1, "invalid convolution operator arguments");
+        std::vector<GaussFunc<1>> kernel;
+        for (int i = 0; i < n; i++) {
+            if (!(exps[i] > 0.0)) return fail(1, "kernel exponents must be positive");
+            kernel.emplace_back(exps[i], coefs[i]);
+        }
+        auto *o = new mwh_oper{make_convolution(m->m, kernel, prec), {}, {}, {}, {}};
         finish_oper(o);
         *out = o;
         return 0;

@@ -231,6 +231,10 @@ template <int D> struct GaussExp {
 template <int D> void build_grid(Tree<D> &tree, const GaussFunc<D> &f);
 template <int D> void build_grid(Tree<D> &tree, const GaussExp<D> &f);
 template <int D> void project(double prec, Tree<D> &tree, const std::function<double(const double *)> &f, int maxIter = -1, bool absPrec = false);
+// a function of n points (3 doubles each) writing n values
+using BatchFunc = std::function<void(long long n, const double *r, double *values)>;
+constexpr size_t kProjectBatch = size_t(1) << 20;  // points per callback call
+template <int D> void project_batched(double prec, Tree<D> &tree, const BatchFunc &f, int maxIter = -1, bool absPrec = false);
 // copy_grid (grid.cpp:220): out gets the topology of inp, no coefficients
 template <int D> void copy_grid(Tree<D> &out, const Tree<D> &inp);
 // dot product of two compressed trees (multiply.cpp:286)

@@ -8,6 +8,8 @@
 // :854-935 (child quadrature points), src/treebuilders/grid.cpp:220 (copy_grid).
 #include "mw_host.h"
 
+#include <algorithm>
+
 namespace mwh {
 
 template <int D> double GaussFunc<D>::evalf(const double *r) const {
@@ -87,34 +89,44 @@ template <int D> void build_grid(Tree<D> &tree, const GaussExp<D> &f) {
 }
 
 // ProjectionCalculator::calcNode for node i.
-template <int D> static void project_node(Tree<D> &t, int i, const std::function<double(const double *)> &f) {
+// The tDim * kp1_d points of node i at which ProjectionCalculator::calcNode
+// evaluates the function (ProjectionCalculator.cpp:34-51): the quadrature
+// points of the children, child by child, x fastest
+// (math_utils::tensor_expand_coords_3D); r holds 3 doubles per point.
+template <int D> static void node_points(const Tree<D> &t, int i, double *r) {
     const auto &b = *t.mra->basis;
     const auto &w = t.mra->world;
     const int K = t.K, kp1_d = t.kp1_d, tDim = Tree<D>::tDim;
     const auto &nd = t.nodes[i];
-    double sFac = std::pow(2.0, -(nd.n + 1));
-    double *coefs = t.c(i);
-    // expanded child quadrature points, x fastest (math_utils::tensor_expand_coords_3D)
+    const double sFac = std::pow(2.0, -(nd.n + 1));
     std::vector<double> prim((size_t)D * 2 * K);
     for (int d = 0; d < D; d++)
         for (int q = 0; q < K; q++) {
             prim[(size_t)d * 2 * K + q] = sFac * (b.roots[q] + 2.0 * nd.l[d]);
             prim[(size_t)d * 2 * K + K + q] = sFac * (b.roots[q] + 2.0 * nd.l[d] + 1.0);
         }
-    for (int ct = 0; ct < tDim; ct++) {
+    for (int ct = 0; ct < tDim; ct++)
         for (int p = 0; p < kp1_d; p++) {
-            double r[3];
             int rem = p;
+            double *x = r + 3 * ((size_t)ct * kp1_d + p);
+            x[0] = x[1] = x[2] = 0.0;
             for (int d = 0; d < D; d++) {
-                int q = rem % K;
+                const int q = rem % K, bit = (ct >> d) & 1;
                 rem /= K;
-                int bit = (ct >> d) & 1;
-                r[d] = w.sf[d] * prim[(size_t)d * 2 * K + bit * K + q];
+                x[d] = w.sf[d] * prim[(size_t)d * 2 * K + bit * K + q];
             }
-            coefs[(size_t)ct * kp1_d + p] = f(r);
         }
-    }
-    // cvTransform(Backward)
+}
+
+// Node i from its function values at node_points (in its coefficient storage):
+// cvTransform(Backward), the 2^{-D(n+1)/2} scaling, compression and norms
+// (ProjectionCalculator.cpp:40-50).
+template <int D> static void node_from_values(Tree<D> &t, int i) {
+    const auto &b = *t.mra->basis;
+    const auto &w = t.mra->world;
+    const int K = t.K, kp1_d = t.kp1_d, tDim = Tree<D>::tDim;
+    const auto &nd = t.nodes[i];
+    double *coefs = t.c(i);
     std::vector<double> tmp(t.nCoefs);
     double *in = coefs, *out = tmp.data();
     int kp1_dm1 = kp1_d / K;
@@ -137,6 +149,15 @@ template <int D> static void project_node(Tree<D> &t, int i, const std::function
     t.calcNorms(i);
 }
 
+template <int D> static void project_node(Tree<D> &t, int i, const std::function<double(const double *)> &f) {
+    const int n = Tree<D>::tDim * t.kp1_d;
+    std::vector<double> r(3 * (size_t)n);
+    node_points(t, i, r.data());
+    double *coefs = t.c(i);
+    for (int p = 0; p < n; p++) coefs[p] = f(r.data() + 3 * (size_t)p);
+    node_from_values(t, i);
+}
+
 template <int D> void project(double prec, Tree<D> &tree, const std::function<double(const double *)> &f, int maxIter, bool absPrec) {
     int maxScale = tree.mra->maxScale();
     std::vector<int> work = tree.endNodes();
@@ -145,6 +166,36 @@ template <int D> void project(double prec, Tree<D> &tree, const std::function<do
         // computed in parallel here
 #pragma omp parallel for schedule(dynamic)
         for (size_t j = 0; j < w.size(); j++) project_node(t, w[j], f);
+    };
+    auto split = [prec, absPrec](const Tree<D> &t, int i) { return split_check(t, i, prec, 1.0, absPrec); };
+    tree_build<D>(tree, work, calc, split, maxIter, maxScale);
+    tree.mwTransformUp();
+    tree.calcSquareNorm();
+}
+
+// project() for a function evaluated on many points per call: the points of
+// a level's nodes are gathered (at most kProjectBatch per call), the callback
+// fills the values, the node computations run in parallel.
+template <int D> void project_batched(double prec, Tree<D> &tree, const BatchFunc &f, int maxIter, bool absPrec) {
+    int maxScale = tree.mra->maxScale();
+    std::vector<int> work = tree.endNodes();
+    auto calc = [&f](Tree<D> &t, const std::vector<int> &w) {
+        const size_t per = (size_t)Tree<D>::tDim * t.kp1_d;
+        const size_t nodes_per_call = std::max<size_t>(1, kProjectBatch / per);
+        std::vector<double> r, v;
+        for (size_t j0 = 0; j0 < w.size(); j0 += nodes_per_call) {
+            const size_t nj = std::min(nodes_per_call, w.size() - j0);
+            r.resize(3 * per * nj);
+            v.assign(per * nj, 0.0);
+#pragma omp parallel for schedule(static)
+            for (size_t j = 0; j < nj; j++) node_points(t, w[j0 + j], r.data() + 3 * per * j);
+            f((long long)(per * nj), r.data(), v.data());
+#pragma omp parallel for schedule(dynamic)
+            for (size_t j = 0; j < nj; j++) {
+                std::copy(v.begin() + per * j, v.begin() + per * (j + 1), t.c(w[j0 + j]));
+                node_from_values(t, w[j0 + j]);
+            }
+        }
     };
     auto split = [prec, absPrec](const Tree<D> &t, int i) { return split_check(t, i, prec, 1.0, absPrec); };
     tree_build<D>(tree, work, calc, split, maxIter, maxScale);
@@ -259,6 +310,7 @@ template <int D> double integrate(const Tree<D> &t) {
     template void build_grid<D>(Tree<D> &, const GaussFunc<D> &);                                         \
     template void build_grid<D>(Tree<D> &, const GaussExp<D> &);                                          \
     template void project<D>(double, Tree<D> &, const std::function<double(const double *)> &, int, bool); \
+    template void project_batched<D>(double, Tree<D> &, const BatchFunc &, int, bool); \
     template void copy_grid<D>(Tree<D> &, const Tree<D> &);                                               \
     template double dot<D>(const Tree<D> &, const Tree<D> &);                                             \
     template double evalf<D>(const Tree<D> &, const double *);                                            \
