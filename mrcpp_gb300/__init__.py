@@ -489,6 +489,16 @@ class HelmholtzOperator(ConvolutionOperator):
         self.mu = mu
 
 
+class IdentityConvolution(ConvolutionOperator):
+    """IdentityConvolution<3>(MRA, prec) (src/operators/IdentityConvolution.cpp:41-55):
+    the kernel is one normalised Gaussian of exponent sqrt(1 / k_prec),
+    k_prec = prec / 10 (IdentityKernel.h:34-41), an approximate delta function."""
+
+    def __init__(self, mra, prec):
+        expo = float(np.sqrt(10.0 / prec))
+        super().__init__(mra, ([expo], [(expo / np.pi) ** 1.5]), prec)
+
+
 class ABGVOperator(ConvolutionOperator):
     """ABGVOperator(MRA, a, b): first derivative with boundary parameters a, b
     (src/operators/ABGVOperator.cpp:45-71); a = b = 0.5 central difference,
