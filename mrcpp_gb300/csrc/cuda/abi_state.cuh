@@ -33,6 +33,7 @@ struct DevPool {
     std::unordered_map<void *, size_t> bytes_of;  // every block of the pool
     std::vector<void *> pending;                  // freed, stream work may still read them
     size_t cached = 0;                            // bytes of free_blocks + pending
+    size_t limit = size_t(8) << 30;               // cached bytes kept (a quarter of the device, set at init)
 };
 
 struct mwgpu_ctx {
@@ -153,8 +154,6 @@ struct PhaseTrace {
     }
 };
 
-constexpr size_t kPoolCacheLimit = 8ull << 30;
-
 inline size_t pool_class(size_t b) {
     if (b <= 4096) return 4096;
     const int e = 63 - __builtin_clzll((unsigned long long)b);  // 2^e <= b < 2^(e+1)
@@ -222,7 +221,7 @@ inline void pool_free(mwgpu_ctx *ctx, void *p) {
     }
     pl.pending.push_back(p);
     pl.cached += it->second;
-    if (pl.cached > kPoolCacheLimit) pool_trim(ctx);
+    if (pl.cached > pl.limit) pool_trim(ctx);
 }
 
 inline void PhaseTrace::mark(const std::string &phase) {

@@ -667,6 +667,147 @@ __global__ void k_gen_nodes32(DevMRA m, DevTree f, const NodeKey *plist, int n_p
     }
 }
 
+// GenNodes of the mixed form, one parent (family) per CTA: the children
+// fam_slots[8 q + c] >= 0 of parent fam_keys[q] (c = x bit | y bit << 1 |
+// z bit << 2) from the parent's nearest real ancestor.  The x- and y-step
+// blocks are computed once for the children that share them; each child's
+// value is the same sequence of filter products as in k_gen_nodes32 (real
+// parent: the two-input steps from its 8 components; otherwise the parent's
+// scaling block along the path, then one-input steps), so the values are
+// bit-identical to it.  Shared memory: three regions of 8 blocks + filters.
+__global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, int *err) {
+    extern __shared__ float sh_fam[];
+    const int K = m.K, K2 = K * K, K3 = m.kp1_d;
+    float *R0 = sh_fam, *R1 = R0 + 8 * K3, *R2 = R1 + 8 * K3, *F = R2 + 8 * K3;
+    __shared__ int s_anc, s_ancn, s_slot[8];
+    __shared__ double red[32];
+    const int q = blockIdx.x;
+    if (q >= n_fam) return;
+    int n, l0, l1, l2;  // the parent
+    unpack_key(m, fam_keys[q], n, l0, l1, l2);
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    if (tid < 8) s_slot[tid] = fam_slots[8 * q + tid];
+    if (tid == 0) {
+        s_anc = -1;
+        s_ancn = 0;
+        for (int a = n; a >= m.root_scale; a--) {
+            const int sh = n - a;
+            NodeKey key;
+            if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
+            const int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
+            if (id >= 0 && id < f.cap_real) {
+                s_anc = id;
+                s_ancn = a;
+                break;
+            }
+        }
+    }
+    load_filters32(F, m, 1, tid, nthr);
+    __syncthreads();
+    const int anc = s_anc, an = s_ancn;
+    if (anc < 0) {
+        if (tid == 0) atomicOr(err, DE_LOOKUP);
+        return;
+    }
+    unsigned need = 0, need_x = 0, need_xy = 0;
+    for (int c = 0; c < 8; c++)
+        if (s_slot[c] >= 0) {
+            need |= 1u << c;
+            need_x |= 1u << (c & 1);
+            need_xy |= 1u << (c & 3);
+        }
+    const float *child[8];
+    if (an == n) {
+        // real parent: x, y, z steps with both inputs of an output in one pass
+        const float *in = f.coefs32 + (size_t)anc * 8 * K3;
+        for (int c0 = 0; c0 < 2; c0++)
+            if (need_x >> c0 & 1) fpairs(R0 + 4 * c0 * K3, in, 4, F + (2 * c0) * K2, F + (2 * c0 + 1) * K2, K, tid, nthr);
+        __syncthreads();
+        for (int c01 = 0; c01 < 4; c01++)
+            if (need_xy >> c01 & 1) {
+                const int c0 = c01 & 1, c1 = c01 >> 1;
+                fpairs(R1 + 2 * c01 * K3, R0 + 4 * c0 * K3, 2, F + (2 * c1) * K2, F + (2 * c1 + 1) * K2, K, tid, nthr);
+            }
+        __syncthreads();
+        for (int c = 0; c < 8; c++) {
+            child[c] = R2 + c * K3;
+            if (need >> c & 1) fpairs(R2 + c * K3, R1 + 2 * (c & 3) * K3, 1, F + (2 * (c >> 2)) * K2, F + (2 * (c >> 2) + 1) * K2, K, tid, nthr);
+        }
+        __syncthreads();
+    } else {
+        // the parent's scaling block along the path from the real ancestor
+        {
+            const int sh = n - an;  // levels from the ancestor's child to the parent: the path bit at level an + 1
+            const int c0 = (l0 >> (sh - 1)) & 1, c1 = (l1 >> (sh - 1)) & 1, c2 = (l2 >> (sh - 1)) & 1;
+            const float *in = f.coefs32 + (size_t)anc * 8 * K3;
+            fpairs(R0, in, 4, F + (2 * c0) * K2, F + (2 * c0 + 1) * K2, K, tid, nthr);
+            __syncthreads();
+            fpairs(R1, R0, 2, F + (2 * c1) * K2, F + (2 * c1 + 1) * K2, K, tid, nthr);
+            __syncthreads();
+            fpairs(R2, R1, 1, F + (2 * c2) * K2, F + (2 * c2 + 1) * K2, K, tid, nthr);
+            __syncthreads();
+        }
+        float *src = R2, *dst = R1;
+        for (int a = an + 1; a < n; a++) {
+            const int sh = n - a - 1;
+            const int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
+            fapply<false>(R0, src, F + (2 * c0) * K2, K, tid, nthr);
+            __syncthreads();
+            fapply<false>(R0 + K3, R0, F + (2 * c1) * K2, K, tid, nthr);
+            __syncthreads();
+            fapply<false>(dst, R0 + K3, F + (2 * c2) * K2, K, tid, nthr);
+            __syncthreads();
+            float *t = src;
+            src = dst;
+            dst = t;
+        }
+        // children of the parent block src: one-input steps; results in the other region
+        for (int c0 = 0; c0 < 2; c0++)
+            if (need_x >> c0 & 1) fapply<false>(R0 + c0 * K3, src, F + (2 * c0) * K2, K, tid, nthr);
+        __syncthreads();
+        for (int c01 = 0; c01 < 4; c01++)
+            if (need_xy >> c01 & 1) fapply<false>(R0 + (2 + c01) * K3, R0 + (c01 & 1) * K3, F + (2 * (c01 >> 1)) * K2, K, tid, nthr);
+        __syncthreads();
+        for (int c = 0; c < 8; c++) {
+            child[c] = dst + c * K3;
+            if (need >> c & 1) fapply<false>(dst + c * K3, R0 + (2 + (c & 3)) * K3, F + (2 * (c >> 2)) * K2, K, tid, nthr);
+        }
+        __syncthreads();
+    }
+    for (int c = 0; c < 8; c++) {
+        const int slot = s_slot[c];
+        if (slot < 0) continue;
+        if (slot >= f.cap_gen) {
+            if (tid == 0) atomicOr(err, DE_POOL_FULL);
+            continue;
+        }
+        const float *v = child[c];
+        double *out = f.gcoefs + (size_t)slot * K3;
+        float *out32 = f.gcoefs32 + (size_t)slot * K3;
+        float *tc = f.gtc32 ? f.gtc32 + (size_t)slot * kTcGenFloats : nullptr;
+        double s2 = 0.0;
+        for (int e = tid; e < K3; e += nthr) {
+            const float x = v[e];
+            out32[e] = x;
+            out[e] = (double)x;
+            if (tc) tc_gen_store(tc, e, x);
+            s2 += (double)x * (double)x;
+        }
+        for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xffffffffu, s2, o);
+        if ((tid & 31) == 0) red[tid >> 5] = s2;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < (nthr + 31) / 32; w++) t += red[w];
+            double *nr = f.norms + (size_t)(f.cap_real + slot) * 8;
+            nr[0] = sqrt(t);
+            for (int cc = 1; cc < 8; cc++) nr[cc] = 0.0;
+            f.idx[f.cap_real + slot] = make_int4(n + 1, 2 * l0 + (c & 1), 2 * l1 + ((c >> 1) & 1), 2 * l2 + (c >> 2));
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void k_to_float(const double *src, float *dst, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = (float)src[i];
 }
@@ -731,6 +872,13 @@ void launch_gen_nodes(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pe
     size_t smem = sizeof(double) * 8 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_nodes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
+}
+
+void launch_gen_family32(const DevMRA &m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, int *err, cudaStream_t s) {
+    if (n_fam <= 0) return;
+    const size_t smem = sizeof(float) * (24 * (size_t)m.kp1_d + 4 * m.K * m.K);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_family32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_gen_family32<<<n_fam, 256, smem, s>>>(m, f, fam_keys, fam_slots, n_fam, err);
 }
 
 void launch_gen_insert(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {

@@ -737,6 +737,11 @@ mwgpu_status mwgpu_init(mwgpu_ctx **out, const mwgpu_config *cfg) {
         return MWGPU_ERR_DEVICE;
     }
     cudaMemset(ctx->d_err, 0, sizeof(int));
+    // freed tree storage stays cached for reuse up to a quarter of the device
+    // (a batch of input trees is re-uploaded every step); an allocation that
+    // fails returns the whole cache to the device first
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && total_b > 0) ctx->pool.limit = std::max<size_t>(size_t(1) << 30, total_b / 4);
     *out = ctx;
     return MWGPU_OK;
 }
@@ -1484,6 +1489,10 @@ struct mwgpu_plan {
     unsigned long long *d_stamps = nullptr;  // level start, contraction start / end, level end (ns)
     std::vector<NodeKey *> d_gkeys;
     std::vector<int> gcount;
+    // mixed form: the GenNodes grouped by parent (keys, 8 slots per parent)
+    std::vector<NodeKey *> d_fam_keys;
+    std::vector<int *> d_fam_slots;
+    std::vector<int> fcount;
     int *d_list = nullptr, *d_ltree = nullptr;
     std::vector<std::pair<int, int>> ranges;
     long long per = 0;
@@ -1543,8 +1552,11 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
     // GenNode values from the current input coefficients (slots fixed at plan time)
     for (int t = 0; t < pl->nt; t++) {
         if (pl->gcount[t] == 0) continue;
-        launch_gen_nodes(pl->inps[t]->mra, pl->inps[t]->t, pl->d_gkeys[t], pl->gcount[t], 0, pl->d_err, st, true,
-                         pl->precision == MWGPU_PREC_MIXED);
+        if (!pl->fcount.empty() && pl->fcount[t] > 0)
+            launch_gen_family32(pl->inps[t]->mra, pl->inps[t]->t, pl->d_fam_keys[t], pl->d_fam_slots[t], pl->fcount[t], pl->d_err, st);
+        else
+            launch_gen_nodes(pl->inps[t]->mra, pl->inps[t]->t, pl->d_gkeys[t], pl->gcount[t], 0, pl->d_err, st, true,
+                             pl->precision == MWGPU_PREC_MIXED);
         ctx->launches++;
     }
     if (pl->precision == MWGPU_PREC_MIXED) {
@@ -1693,6 +1705,50 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         if ((s = plan_alloc(ctx, pl, &pl->d_gkeys[t], pcount[t]))) return fail(s);
         MW_CK(cudaMemcpyAsync(pl->d_gkeys[t], ctx->d_plist + (size_t)t * ctx->pcap, sizeof(NodeKey) * pcount[t], cudaMemcpyDeviceToDevice,
                               ctx->stream));
+    }
+    // mixed form: GenNodes grouped by parent, so that the children of a parent
+    // share its x and y steps (k_gen_family32); the slots stay those above
+    if (pl->precision == MWGPU_PREC_MIXED && !std::getenv("MWGPU_GEN_PER_NODE")) {
+        pl->fcount.assign(n_trees, 0);
+        pl->d_fam_keys.assign(n_trees, nullptr);
+        pl->d_fam_slots.assign(n_trees, nullptr);
+        for (int t = 0; t < n_trees; t++) {
+            if (pcount[t] == 0) continue;
+            const DevMRA &m = pl->inps[t]->mra;
+            std::vector<NodeKey> keys(pcount[t]);
+            MW_CK(cudaMemcpyAsync(keys.data(), pl->d_gkeys[t], sizeof(NodeKey) * pcount[t], cudaMemcpyDeviceToHost, ctx->stream));
+            MW_CK(cudaStreamSynchronize(ctx->stream));
+            std::vector<NodeKey> fkeys;
+            std::vector<int> fslots;
+            std::unordered_map<unsigned long long, std::vector<int>> by_parent;  // parent key hash -> families
+            for (int p = 0; p < pcount[t]; p++) {
+                int n, l0, l1, l2;
+                unpack_key(m, keys[p], n, l0, l1, l2);
+                NodeKey pk;
+                if (!pack_key(m, n - 1, l0 >> 1, l1 >> 1, l2 >> 1, pk)) {
+                    ctx->err = "plan: a GenNode without a parent in the world";
+                    return fail(MWGPU_ERR_BAD_ARG);
+                }
+                const int c = (l0 & 1) | ((l1 & 1) << 1) | ((l2 & 1) << 2);
+                auto &cand = by_parent[pk.lo * 0x9E3779B97F4A7C15ull ^ pk.hi];
+                int fam = -1;
+                for (int q : cand)
+                    if (fkeys[q] == pk) fam = q;
+                if (fam < 0) {
+                    fam = (int)fkeys.size();
+                    fkeys.push_back(pk);
+                    fslots.insert(fslots.end(), 8, -1);
+                    cand.push_back(fam);
+                }
+                fslots[8 * (size_t)fam + c] = p;
+            }
+            pl->fcount[t] = (int)fkeys.size();
+            if ((s = plan_alloc(ctx, pl, &pl->d_fam_keys[t], fkeys.size())) || (s = plan_alloc(ctx, pl, &pl->d_fam_slots[t], fslots.size())))
+                return fail(s);
+            MW_CK(cudaMemcpyAsync(pl->d_fam_keys[t], fkeys.data(), sizeof(NodeKey) * fkeys.size(), cudaMemcpyHostToDevice, ctx->stream));
+            MW_CK(cudaMemcpyAsync(pl->d_fam_slots[t], fslots.data(), sizeof(int) * fslots.size(), cudaMemcpyHostToDevice, ctx->stream));
+            MW_CK(cudaStreamSynchronize(ctx->stream));
+        }
     }
     // transforms: parents per depth over all output trees
     if (flags & MWGPU_PLAN_TRANSFORMS) {

@@ -207,6 +207,9 @@ void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, c
 // (fp32: FP32 products, the GenNodes of the mixed form)
 void launch_gen_nodes(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s,
                       bool real_only = false, bool fp32 = false);
+// Mixed-form GenNodes grouped by parent (one CTA per parent, the requested
+// children fam_slots[8 q + c] >= 0; values bit-identical to launch_gen_nodes)
+void launch_gen_family32(const DevMRA &m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, int *err, cudaStream_t s);
 void launch_gen_insert(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
 // DerivativeCalculator::calcNode for the work entries (output leaves): band along
 // op.band_dir, 1D application of term 0 with the identity elsewhere, divided by

@@ -270,3 +270,56 @@ def test_plan_graph_replays_the_level(gpu, precision):
         if plan:
             L.mwgpu_plan_destroy(ctx, plan)
         L.mwgpu_destroy(ctx)
+
+
+def test_plan_gen_node_families_are_bit_identical(gpu, monkeypatch):
+    """Mixed-form plans compute their GenNodes per parent (k_gen_family32: the
+    children of a parent share its x and y steps); the level they leave equals,
+    bit for bit, the one of a plan with one GenNode per CTA
+    (MWGPU_GEN_PER_NODE at plan creation).  Same chunking (no autotuning)."""
+    L = mw.lib()
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, 1e-4)
+    inps = _inputs(mra, 1e-4, (4, 2), 1200)
+    grids = []
+    for f in inps:
+        g = mw.FunctionTree(mra)
+        mw.apply(1e-4, g, P, f, precision=mw.FP64)
+        grids.append(g)
+    ctx = C.c_void_p()
+    assert L.mwgpu_init(C.byref(ctx), C.byref(mw.MwgpuConfig())) == 0
+    try:
+        dop = C.c_void_p()
+        assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
+        assert L.mwgpu_set_precision(ctx, mw.MIXED) == 0
+        K8 = 8 * mra.kp1 ** 3
+        res, gen = {}, {}
+        for per_node in (True, False):
+            if per_node:
+                monkeypatch.setenv("MWGPU_GEN_PER_NODE", "1")
+            else:
+                monkeypatch.delenv("MWGPU_GEN_PER_NODE", raising=False)
+            fin = [_upload_input(L, ctx, mra, f)[0] for f in inps]
+            outs, sizes = [], []
+            for g in grids:
+                t, gx = _create_output(L, ctx, mra, g)
+                outs.append(t)
+                sizes.append(len(gx["child0"]))
+            wt = np.concatenate([np.full(s, t, dtype=np.int32) for t, s in enumerate(sizes)])
+            wn = np.concatenate([np.arange(s, dtype=np.int32) for s in sizes])
+            PA = C.c_void_p * len(inps)
+            sq = np.full(len(inps), -1.0)
+            plan = C.c_void_p()
+            rc = L.mwgpu_plan_create(ctx, dop, len(inps), PA(*fin), PA(*outs), mw._pi(wt), mw._pi(wn), len(wt), 1e-4, mw._pd(sq),
+                                     1, C.byref(plan))  # MWGPU_PLAN_TRANSFORMS, no autotuning
+            assert rc == 0, L.mwgpu_last_error(ctx).decode()
+            st = mw.MwgpuLevelStats()
+            assert L.mwgpu_plan_execute(ctx, plan, C.byref(st)) == 0, L.mwgpu_last_error(ctx).decode()
+            gen[per_node] = st.gen_nodes
+            res[per_node] = [_download(L, ctx, outs[t], sizes[t], K8) for t in range(len(inps))]
+            assert L.mwgpu_plan_destroy(ctx, plan) == 0
+        assert gen[True] == gen[False] > 0
+        for a, b in zip(res[True], res[False]):
+            assert np.array_equal(a, b)
+    finally:
+        L.mwgpu_destroy(ctx)
