@@ -74,6 +74,10 @@ struct mwgpu_ctx {
     WorkItem *d_items_cm = nullptr;  // the builder's cell-major items (same capacity)
     long long items_cap = 0;
     long long *d_pair_off = nullptr, pair_off_cap = 0;
+    // mixed-form GenNode families of a level (gen_pass)
+    NodeKey *d_fkeys = nullptr, *d_fam_keys = nullptr;
+    int *d_fvals = nullptr, *d_famid = nullptr, *d_fam_slots = nullptr, *d_fam_count = nullptr;
+    long long fkeys_cap = 0, fvals_cap = 0, famid_cap = 0, fam_keys_cap = 0, fam_slots_cap = 0, fam_count_cap = 0;
     int *d_pcounts = nullptr;
     long long pcounts_cap = 0;
     long long *d_item_off = nullptr, item_off_cap = 0;

@@ -675,14 +675,15 @@ __global__ void k_gen_nodes32(DevMRA m, DevTree f, const NodeKey *plist, int n_p
 // parent: the two-input steps from its 8 components; otherwise the parent's
 // scaling block along the path, then one-input steps), so the values are
 // bit-identical to it.  Shared memory: three regions of 8 blocks + filters.
-__global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, int *err) {
+__global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, const int *n_fam_dev, int gen_base,
+                               bool real_only, int *err) {
     extern __shared__ float sh_fam[];
     const int K = m.K, K2 = K * K, K3 = m.kp1_d;
     float *R0 = sh_fam, *R1 = R0 + 8 * K3, *R2 = R1 + 8 * K3, *F = R2 + 8 * K3;
     __shared__ int s_anc, s_ancn, s_slot[8];
     __shared__ double red[32];
     const int q = blockIdx.x;
-    if (q >= n_fam) return;
+    if (q >= (n_fam_dev ? min(n_fam, *n_fam_dev) : n_fam)) return;
     int n, l0, l1, l2;  // the parent
     unpack_key(m, fam_keys[q], n, l0, l1, l2);
     const int tid = threadIdx.x, nthr = blockDim.x;
@@ -695,7 +696,7 @@ __global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, con
             NodeKey key;
             if (!pack_key(m, a, l0 >> sh, l1 >> sh, l2 >> sh, key)) break;
             const int id = hash_find(f.hkeys, f.hvals, f.hcap, key);
-            if (id >= 0 && id < f.cap_real) {
+            if (id >= 0 && (!real_only || id < f.cap_real)) {
                 s_anc = id;
                 s_ancn = a;
                 break;
@@ -709,6 +710,7 @@ __global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, con
         if (tid == 0) atomicOr(err, DE_LOOKUP);
         return;
     }
+    const bool anc_real = anc < f.cap_real;
     unsigned need = 0, need_x = 0, need_xy = 0;
     for (int c = 0; c < 8; c++)
         if (s_slot[c] >= 0) {
@@ -717,7 +719,7 @@ __global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, con
             need_xy |= 1u << (c & 3);
         }
     const float *child[8];
-    if (an == n) {
+    if (an == n && anc_real) {
         // real parent: x, y, z steps with both inputs of an output in one pass
         const float *in = f.coefs32 + (size_t)anc * 8 * K3;
         for (int c0 = 0; c0 < 2; c0++)
@@ -735,19 +737,34 @@ __global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, con
         }
         __syncthreads();
     } else {
-        // the parent's scaling block along the path from the real ancestor
-        {
-            const int sh = n - an;  // levels from the ancestor's child to the parent: the path bit at level an + 1
+        // the parent's scaling block: a GenNode's own block, or along the path
+        // from the ancestor (its 8 components if real, its scaling block if a GenNode)
+        const float *src;
+        float *dst = R1;
+        if (an == n) {
+            src = f.gcoefs32 + (size_t)(anc - f.cap_real) * K3;
+        } else {
+            const int sh = n - an;  // the path bit at level an + 1
             const int c0 = (l0 >> (sh - 1)) & 1, c1 = (l1 >> (sh - 1)) & 1, c2 = (l2 >> (sh - 1)) & 1;
-            const float *in = f.coefs32 + (size_t)anc * 8 * K3;
-            fpairs(R0, in, 4, F + (2 * c0) * K2, F + (2 * c0 + 1) * K2, K, tid, nthr);
-            __syncthreads();
-            fpairs(R1, R0, 2, F + (2 * c1) * K2, F + (2 * c1 + 1) * K2, K, tid, nthr);
-            __syncthreads();
-            fpairs(R2, R1, 1, F + (2 * c2) * K2, F + (2 * c2 + 1) * K2, K, tid, nthr);
-            __syncthreads();
+            if (anc_real) {
+                const float *in = f.coefs32 + (size_t)anc * 8 * K3;
+                fpairs(R0, in, 4, F + (2 * c0) * K2, F + (2 * c0 + 1) * K2, K, tid, nthr);
+                __syncthreads();
+                fpairs(R1, R0, 2, F + (2 * c1) * K2, F + (2 * c1 + 1) * K2, K, tid, nthr);
+                __syncthreads();
+                fpairs(R2, R1, 1, F + (2 * c2) * K2, F + (2 * c2 + 1) * K2, K, tid, nthr);
+                __syncthreads();
+            } else {
+                const float *in = f.gcoefs32 + (size_t)(anc - f.cap_real) * K3;
+                fapply<false>(R1, in, F + (2 * c0) * K2, K, tid, nthr);
+                __syncthreads();
+                fapply<false>(R1 + K3, R1, F + (2 * c1) * K2, K, tid, nthr);
+                __syncthreads();
+                fapply<false>(R2, R1 + K3, F + (2 * c2) * K2, K, tid, nthr);
+                __syncthreads();
+            }
+            src = R2;
         }
-        float *src = R2, *dst = R1;
         for (int a = an + 1; a < n; a++) {
             const int sh = n - a - 1;
             const int c0 = (l0 >> sh) & 1, c1 = (l1 >> sh) & 1, c2 = (l2 >> sh) & 1;
@@ -757,9 +774,8 @@ __global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, con
             __syncthreads();
             fapply<false>(dst, R0 + K3, F + (2 * c2) * K2, K, tid, nthr);
             __syncthreads();
-            float *t = src;
             src = dst;
-            dst = t;
+            dst = dst == R1 ? R2 : R1;
         }
         // children of the parent block src: one-input steps; results in the other region
         for (int c0 = 0; c0 < 2; c0++)
@@ -775,8 +791,8 @@ __global__ void k_gen_family32(DevMRA m, DevTree f, const NodeKey *fam_keys, con
         __syncthreads();
     }
     for (int c = 0; c < 8; c++) {
-        const int slot = s_slot[c];
-        if (slot < 0) continue;
+        if (s_slot[c] < 0) continue;
+        const int slot = gen_base + s_slot[c];
         if (slot >= f.cap_gen) {
             if (tid == 0) atomicOr(err, DE_POOL_FULL);
             continue;
@@ -874,11 +890,73 @@ void launch_gen_nodes(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pe
     k_gen_nodes<<<n_pend, 128, smem, s>>>(m, f, plist, n_pend, gen_base, err, real_only);
 }
 
-void launch_gen_family32(const DevMRA &m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, int *err, cudaStream_t s) {
+void launch_gen_family32(const DevMRA &m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, const int *n_fam_dev, int gen_base,
+                         bool real_only, int *err, cudaStream_t s) {
     if (n_fam <= 0) return;
     const size_t smem = sizeof(float) * (24 * (size_t)m.kp1_d + 4 * m.K * m.K);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_gen_family32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_gen_family32<<<n_fam, 256, smem, s>>>(m, f, fam_keys, fam_slots, n_fam, err);
+    k_gen_family32<<<n_fam, 256, smem, s>>>(m, f, fam_keys, fam_slots, n_fam, n_fam_dev, gen_base, real_only, err);
+}
+
+// Families of the pending GenNode keys plist[0..n) on the device: the parent
+// keys go into a table whose value is the pending index of the inserting key
+// (the family's leader); leaders are numbered; every key takes its child slot.
+__device__ inline bool parent_of(const DevMRA &m, const NodeKey &k, NodeKey &pk, int &c) {
+    int n, l0, l1, l2;
+    unpack_key(m, k, n, l0, l1, l2);
+    c = (l0 & 1) | ((l1 & 1) << 1) | ((l2 & 1) << 2);
+    return pack_key(m, n - 1, l0 >> 1, l1 >> 1, l2 >> 1, pk);
+}
+
+__global__ void k_fam_insert(DevMRA m, const NodeKey *plist, int n, NodeKey *fkeys, int *fvals, int fcap, int *err) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    NodeKey pk;
+    int c;
+    if (!parent_of(m, plist[p], pk, c)) {
+        atomicOr(err, DE_RANGE);
+        return;
+    }
+    bool full = false;
+    hash_insert(fkeys, fvals, fcap, pk, p, &full);
+    if (full) atomicOr(err, DE_HASH_FULL);
+}
+
+__global__ void k_fam_number(DevMRA m, const NodeKey *plist, int n, const NodeKey *fkeys, const int *fvals, int fcap, int *famid, NodeKey *fam_keys,
+                             int *fam_count) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    NodeKey pk;
+    int c;
+    if (!parent_of(m, plist[p], pk, c)) return;
+    if (hash_find(fkeys, fvals, fcap, pk) != p) return;
+    const int fam = atomicAdd(fam_count, 1);
+    famid[p] = fam;
+    fam_keys[fam] = pk;
+}
+
+__global__ void k_fam_place(DevMRA m, const NodeKey *plist, int n, const NodeKey *fkeys, const int *fvals, int fcap, const int *famid, int *fam_slots,
+                            int *err) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    NodeKey pk;
+    int c;
+    if (!parent_of(m, plist[p], pk, c)) return;
+    const int leader = hash_find(fkeys, fvals, fcap, pk);
+    if (leader < 0 || leader >= n) {
+        atomicOr(err, DE_LOOKUP);
+        return;
+    }
+    fam_slots[8 * (size_t)famid[leader] + c] = p;
+}
+
+void launch_gen_families(const DevMRA &m, const NodeKey *plist, int n, NodeKey *fkeys, int *fvals, int fcap, int *famid, NodeKey *fam_keys,
+                         int *fam_slots, int *fam_count, int *err, cudaStream_t s) {
+    if (n <= 0) return;
+    const int b = (n + 255) / 256;
+    k_fam_insert<<<b, 256, 0, s>>>(m, plist, n, fkeys, fvals, fcap, err);
+    k_fam_number<<<b, 256, 0, s>>>(m, plist, n, fkeys, fvals, fcap, famid, fam_keys, fam_count);
+    k_fam_place<<<b, 256, 0, s>>>(m, plist, n, fkeys, fvals, fcap, famid, fam_slots, err);
 }
 
 void launch_gen_insert(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s) {

@@ -487,9 +487,30 @@ mwgpu_status gen_pass(mwgpu_ctx *ctx, const Level &lv, std::vector<int> &pcount,
         if (2LL * (f.n_real + f.n_gen + pcount[t]) + 16 > f.hcap)
             if (auto s = rebuild_hash(ctx, inp, (long long)f.n_real + f.n_gen + pcount[t])) return s;
         const NodeKey *pl = ctx->d_plist + (size_t)t * ctx->pcap;
-        launch_gen_nodes(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream, false, fp32);
+        if (fp32 && !std::getenv("MWGPU_GEN_PER_NODE")) {
+            // GenNodes by parent (k_gen_family32): families formed on the device
+            const int n = pcount[t];
+            long long fcap = 64;
+            while (fcap < 2LL * n + 16) fcap *= 2;
+            if (auto s = grow_buf(ctx, &ctx->d_fkeys, &ctx->fkeys_cap, fcap)) return s;
+            if (auto s = grow_buf(ctx, &ctx->d_fvals, &ctx->fvals_cap, fcap)) return s;
+            if (auto s = grow_buf(ctx, &ctx->d_famid, &ctx->famid_cap, n)) return s;
+            if (auto s = grow_buf(ctx, &ctx->d_fam_keys, &ctx->fam_keys_cap, n)) return s;
+            if (auto s = grow_buf(ctx, &ctx->d_fam_slots, &ctx->fam_slots_cap, 8LL * n)) return s;
+            if (auto s = grow_buf(ctx, &ctx->d_fam_count, &ctx->fam_count_cap, 1)) return s;
+            MW_CK(cudaMemsetAsync(ctx->d_fkeys, 0xFF, sizeof(NodeKey) * fcap, ctx->stream));
+            MW_CK(cudaMemsetAsync(ctx->d_fam_slots, 0xFF, sizeof(int) * 8 * (size_t)n, ctx->stream));
+            MW_CK(cudaMemsetAsync(ctx->d_fam_count, 0, sizeof(int), ctx->stream));
+            launch_gen_families(inp->mra, pl, n, ctx->d_fkeys, ctx->d_fvals, (int)fcap, ctx->d_famid, ctx->d_fam_keys, ctx->d_fam_slots,
+                                ctx->d_fam_count, ctx->d_err, ctx->stream);
+            launch_gen_family32(inp->mra, f, ctx->d_fam_keys, ctx->d_fam_slots, n, ctx->d_fam_count, f.n_gen, false, ctx->d_err, ctx->stream);
+            ctx->launches += 4;
+        } else {
+            launch_gen_nodes(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream, false, fp32);
+            ctx->launches++;
+        }
         launch_gen_insert(inp->mra, f, pl, pcount[t], f.n_gen, ctx->d_err, ctx->stream);
-        ctx->launches += 2;
+        ctx->launches++;
         f.n_gen += pcount[t];
         gen_total += pcount[t];
         inp->gen_prec = ctx->precision;
@@ -750,7 +771,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_tc_counter, (void *)ctx->d_proj, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_pvals,
+    for (void *p : {(void *)ctx->d_err, (void *)ctx->d_stats, (void *)ctx->d_tc_counter, (void *)ctx->d_proj, (void *)ctx->d_work, (void *)ctx->d_pkeys, (void *)ctx->d_fkeys, (void *)ctx->d_fam_keys, (void *)ctx->d_fvals, (void *)ctx->d_famid, (void *)ctx->d_fam_slots, (void *)ctx->d_fam_count, (void *)ctx->d_pvals,
                     (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_items_cm, (void *)ctx->d_chunks,
                     (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
@@ -1553,7 +1574,8 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
     for (int t = 0; t < pl->nt; t++) {
         if (pl->gcount[t] == 0) continue;
         if (!pl->fcount.empty() && pl->fcount[t] > 0)
-            launch_gen_family32(pl->inps[t]->mra, pl->inps[t]->t, pl->d_fam_keys[t], pl->d_fam_slots[t], pl->fcount[t], pl->d_err, st);
+            launch_gen_family32(pl->inps[t]->mra, pl->inps[t]->t, pl->d_fam_keys[t], pl->d_fam_slots[t], pl->fcount[t], nullptr, 0, true, pl->d_err,
+                                st);
         else
             launch_gen_nodes(pl->inps[t]->mra, pl->inps[t]->t, pl->d_gkeys[t], pl->gcount[t], 0, pl->d_err, st, true,
                              pl->precision == MWGPU_PREC_MIXED);

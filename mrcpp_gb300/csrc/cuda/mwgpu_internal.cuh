@@ -209,7 +209,14 @@ void launch_gen_nodes(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pe
                       bool real_only = false, bool fp32 = false);
 // Mixed-form GenNodes grouped by parent (one CTA per parent, the requested
 // children fam_slots[8 q + c] >= 0; values bit-identical to launch_gen_nodes)
-void launch_gen_family32(const DevMRA &m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, int *err, cudaStream_t s);
+// (n_fam_dev: the family count on the device, n_fam an upper bound; slots
+// gen_base + fam_slots[...]; real_only as for launch_gen_nodes)
+void launch_gen_family32(const DevMRA &m, DevTree f, const NodeKey *fam_keys, const int *fam_slots, int n_fam, const int *n_fam_dev, int gen_base,
+                         bool real_only, int *err, cudaStream_t s);
+// families of the pending keys plist[0..n) on the device (fkeys: a table of
+// fcap >= 2 n slots, all bits set; fam_slots: 8 n entries of -1; fam_count 0)
+void launch_gen_families(const DevMRA &m, const NodeKey *plist, int n, NodeKey *fkeys, int *fvals, int fcap, int *famid, NodeKey *fam_keys,
+                         int *fam_slots, int *fam_count, int *err, cudaStream_t s);
 void launch_gen_insert(const DevMRA &m, DevTree f, const NodeKey *plist, int n_pend, int gen_base, int *err, cudaStream_t s);
 // DerivativeCalculator::calcNode for the work entries (output leaves): band along
 // op.band_dir, 1D application of term 0 with the identity elsewhere, divided by

@@ -323,3 +323,25 @@ def test_plan_gen_node_families_are_bit_identical(gpu, monkeypatch):
             assert np.array_equal(a, b)
     finally:
         L.mwgpu_destroy(ctx)
+
+
+def test_level_gen_node_families_are_bit_identical(gpu, monkeypatch):
+    """Mixed-form levels form GenNode families on the device (k_fam_* kernels,
+    then k_gen_family32, ancestors may be GenNodes of earlier levels); the
+    adaptive apply equals, bit for bit, the one with one GenNode per CTA."""
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, 1e-4)
+    f = _inputs(mra, 1e-4, (5,), 1300)[0]
+    res = {}
+    for per_node in (True, False):
+        if per_node:
+            monkeypatch.setenv("MWGPU_GEN_PER_NODE", "1")
+        else:
+            monkeypatch.delenv("MWGPU_GEN_PER_NODE", raising=False)
+        g = mw.FunctionTree(mra)
+        st = mw.apply(1e-4, g, P, f, precision=mw.MIXED)
+        res[per_node] = (g.export(), st["gen_nodes"])
+    (a, ga), (b, gb) = res[True], res[False]
+    assert ga == gb > 0
+    assert np.array_equal(a["idx"], b["idx"])
+    assert np.array_equal(a["coefs"], b["coefs"])
