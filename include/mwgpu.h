@@ -360,8 +360,12 @@ mwgpu_status mwgpu_tree_copy_nodes(mwgpu_ctx *ctx, const mwgpu_tree *src, mwgpu_
  *   - FP64 form only (the context precision must be MWGPU_PREC_FP64);
  *   - n <= 65536 nodes, else MWGPU_ERR_BAD_ARG;
  *   - it creates no GenNodes: every node of the operator bands must already be
- *     in the input tree (run mwgpu_apply_level once on the same nodes first),
- *     else MWGPU_ERR_BAD_ARG;
+ *     in the input tree (run mwgpu_apply_level once on the same nodes first,
+ *     in the FP64 form: GenNodes made by the mixed form are rejected), else
+ *     MWGPU_ERR_BAD_ARG; when a band node turns out to be missing during the
+ *     contraction the call returns MWGPU_ERR_BAD_ARG after the kernel has
+ *     run, and the listed output nodes are then undefined;
+ *   - trees held by a plan are rejected (MWGPU_ERR_BAD_ARG);
  *   - the first call on a device looks up the array's device address; make
  *     that first call before any stream capture;
  *   - all calls share the one array: calls that overlap on the GPU (other host

@@ -1410,6 +1410,11 @@ extern "C" mwgpu_status mwgpu_apply_level_static(mwgpu_ctx *ctx, const mwgpu_ope
     MW_ARG(inp->mra.K == o->op.K && out->mra.K == o->op.K, "order mismatch");
     MW_ARG(ctx->device >= 0 && ctx->device < kStaticMaxDevices, "device ordinal beyond the static scratch table");
     MW_ARG(ctx->precision == MWGPU_PREC_FP64, "mwgpu_apply_level_static computes the FP64 form only");
+    MW_ARG(inp->plans == 0 && out->plans == 0, "tree is held by a plan (destroy the plan first)");
+    // GenNodes made by a mixed-form level hold FP32-product values; the FP64
+    // contraction must not read them
+    MW_ARG(inp->t.n_gen == 0 || inp->gen_prec == MWGPU_PREC_FP64,
+           "the input tree's GenNodes were made by the mixed form: run mwgpu_apply_level in FP64 on these nodes first");
     for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < out->t.n_real, "node index out of range");
     MW_CK(cudaSetDevice(ctx->device));
     if (stats) std::memset(stats, 0, sizeof(*stats));

@@ -110,5 +110,15 @@ def test_static_level_rejects_what_it_cannot_do(gpu):
             assert rc == 0
         # once they exist the same call succeeds
         assert L.mwgpu_apply_level_static(ctx, dop, dinp, out_b, mw._pi(work), n, 1e-3, -1.0, None, None) == 0
+        if st.gen_nodes > 0:
+            # GenNodes remade by a mixed-form level hold FP32-product values:
+            # rejected until an FP64 level has remade them
+            assert L.mwgpu_set_precision(ctx, mw.MIXED) == 0
+            assert L.mwgpu_apply_level(ctx, dop, dinp, out_b, mw._pi(work), n, 1e-3, -1.0, None, None) == 0
+            assert L.mwgpu_set_precision(ctx, mw.FP64) == 0
+            rc = L.mwgpu_apply_level_static(ctx, dop, dinp, out_b, mw._pi(work), n, 1e-3, -1.0, None, None)
+            assert rc == 1 and b"mixed" in L.mwgpu_last_error(ctx)
+            assert L.mwgpu_apply_level(ctx, dop, dinp, out_b, mw._pi(work), n, 1e-3, -1.0, None, None) == 0
+            assert L.mwgpu_apply_level_static(ctx, dop, dinp, out_b, mw._pi(work), n, 1e-3, -1.0, None, None) == 0
     finally:
         L.mwgpu_destroy(ctx)
