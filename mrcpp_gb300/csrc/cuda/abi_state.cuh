@@ -88,6 +88,20 @@ struct mwgpu_ctx {
     int chunks_cap = 0;
     double *d_partial = nullptr;
     size_t partial_cap = 0;  // doubles
+    // pencil contraction (k_pencil.cu): units, task order, task sums, per-entry task ranges
+    mwgpu::PencilUnit *d_units = nullptr;
+    long long units_cap = 0;
+    int *d_task_unit = nullptr;
+    long long task_unit_cap = 0;
+    double *d_pen_partial = nullptr;
+    size_t pen_partial_cap = 0;  // doubles
+    int *d_pen_begin = nullptr;
+    long long pen_begin_cap = 0;
+    int *d_keep = nullptr;
+    long long keep_cap = 0;
+    long long *d_keep_off = nullptr;
+    long long keep_off_cap = 0;
+    int *d_pen_counter = nullptr;
     unsigned long long launches = 0;
     void *d_arena = nullptr;  // scratch of the judged apply, carved per call
     size_t arena_bytes = 0;
@@ -104,6 +118,16 @@ struct mwgpu_oper {
     int n_rows = 0;
     std::vector<int> widths;    // [T * n_rows * 5]
     std::vector<int> band_max;  // [n_rows]
+    // pencil contraction (order 7): per depth and k = 0..kPencilMaxL the number
+    // of terms with band width >= k among those of width <= kPencilMaxW, the
+    // term row of the first such term (the wider ones come first), and per
+    // (depth, group, x slot) the float offset of the stacked form in
+    // op.btc_stack (-1: none) and its number of terms
+    std::vector<int> pen_tk;    // [rows][kPencilMaxL + 1]
+    std::vector<int> pen_r0;    // [rows]
+    int pen_groups = 0;
+    std::vector<long long> pen_form;
+    std::vector<short> pen_nform;
 };
 
 struct mwgpu_tree {

@@ -39,9 +39,10 @@ void launch_contract_items(const DevMRA &m, const DevOper &op, const DevTree *fs
 }
 
 void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tree, const int *work, int n_work, const int *chunk_begin,
-                          const double *partial, cudaStream_t s, const int *nw_dev) {
+                          const double *partial, cudaStream_t s, const int *nw_dev, const int *pen_begin, const double *pen_partial) {
     if (n_work <= 0) return;
-    mixed::k_reduce_chunks<<<dim3(n_work, 8), mixed::kReduceThreads, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nw_dev);
+    mixed::k_reduce_chunks<<<dim3(n_work, 8), mixed::kReduceThreads, 0, s>>>(gs, work_tree, work, chunk_begin, partial, 8 * m.kp1_d, nw_dev,
+                                                                             pen_begin, pen_partial);
 }
 
 int contract_items_resident(int K) {

@@ -699,8 +699,11 @@ __global__ void __launch_bounds__(Shape<K>::NT, Shape<K>::MIN_BLOCKS) k_contract
 // additions per coefficient stay in chunk order), so coarse levels with few
 // g nodes and many chunks each still spread over 8 CTAs per node.
 constexpr int kReduceThreads = 128;
+// pen_begin / pen_partial (optional): the pencil contraction's task sums of
+// each g (k_pencil.cu), added after its chunks, in task order.
 __global__ void __launch_bounds__(kReduceThreads) k_reduce_chunks(const DevTree *gs, const int *work_tree, const int *work, const int *chunk_begin,
-                                                                  const double *partial, int nc, const int *nw_dev) {
+                                                                  const double *partial, int nc, const int *nw_dev, const int *pen_begin = nullptr,
+                                                                  const double *pen_partial = nullptr) {
     constexpr int NT = kReduceThreads, E = 4, U = 4;
     const int tid = threadIdx.x, wi = blockIdx.x, comp = blockIdx.y;
     if (nw_dev && wi >= *nw_dev) return;
@@ -734,6 +737,12 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_chunks(const DevTree 
         for (; c < c1; c++)
 #pragma unroll
             for (int j = 0; j < E; j++) v[j] += ok[j] ? src[(size_t)c * nc + e0 + j * NT] : 0.0;
+        if (pen_begin) {
+            const double *psrc = pen_partial + (size_t)comp * K3;
+            for (int t = pen_begin[wi]; t < pen_begin[wi + 1]; t++)
+#pragma unroll
+                for (int j = 0; j < E; j++) v[j] += ok[j] ? psrc[(size_t)t * nc + e0 + j * NT] : 0.0;
+        }
 #pragma unroll
         for (int j = 0; j < E; j++)
             if (ok[j]) {

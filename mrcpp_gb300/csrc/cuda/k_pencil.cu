@@ -1,0 +1,764 @@
+// Pencil contraction of the mixed form for order K = 8 (k = 7): the x step
+// on the 5th-generation tensor cores with the operator terms stacked along N,
+// the y and z steps in FP32 on the CUDA cores, concurrently.
+//
+// What it computes.  For one output node g, one band cell l = (l_x, l_y, l_z)
+// and one operator term i, the reference adds (ConvolutionCalculator.cpp:
+// 277-382) the three 1D applications
+//     g[gt] += O^z_i(l_z) O^y_i(l_y) O^x_i(l_x) f(g + l)[ft]
+// over every (ft, gt) component its band and zero-norm rules keep, leaving
+// out ft = gt = 0 below the roots (:261).  Without norm screening (levels
+// whose gThreshold is negative, ConvolutionCalculator.cpp:241-248 -- the
+// fixed-grid applies and the first TreeBuilder iteration) the kept set is
+// structural: an operator block (a, b) of a direction takes part iff
+// |l_d| <= bw_i[2a+b], and an f component takes part iff its norm is at least
+// MachineZero.  Both are folded into the operands (zeroed operator blocks,
+// zeroed f components), so the dense block products below equal the sum of
+// the reference's component products.  This kernel takes the terms whose band
+// width at the depth is at most kPencilMaxW (the item kernel the wider ones).
+//
+// Schedule.  The cells of one g with the same (l_y, l_z) form a pencil along
+// x.  A pencil's f nodes f(g + (l_x, l_y, l_z)) are the A operand of every
+// term, so the terms are stacked along N:
+//     S1[(y,z)][(j, c)] = sum_{l_x} sum_{x_in} f(l_x)[(y,z)][x_in] B_j(l_x)[c][x_in]
+// (tcgen05.mma kind::tf32, M = 128 rows per z half, N = 24 per term, up to 5
+// terms per product, K = 8 per instruction, 3 products of TF32 hi / lo parts
+// for FP32 accuracy; measured on this GPU a tcgen05.mma costs about 131 cycles
+// for any N up to 128 and 170 cycles at N = 256, so only wide N pays, and
+// legacy mma.sync shares the same tensor pipe).  The 24 columns of a term are
+// its x-step outputs a0 = 0 from b0 = 1 (C block), a0 = 1 (B, A blocks) and
+// a0 = 0 from b0 = 0 (T block), so that the s->s path can be split off (U
+// channel below).  Per term the consumers then apply the y and z steps in FP32
+// (CUDA-core FMA pipe, which runs beside the tensor pipe):
+//     Y[x][y_out][z]  = sum_{y_in} O^y[y_out][y_in] S1[x][y_in][z]
+//     G[x][y][z_out] += sum_{z_in} O^z[z_out][z_in] Y[x][y][z_in]
+// Below the roots the T-block part of S1 on the (b1, b2) = (0, 0) rows is the
+// U channel: it goes through y with the B block (a1 = 1) into Y and with the T
+// block into P, and P goes through z with the B block only (a2 = 1), which
+// leaves out exactly the T.T.T path from f[0] to g[0].
+//
+// Roles (320 threads): warp 0 lane 0 stages operands with cp.async.bulk into
+// mbarrier-tracked slots (a pencil's f nodes once for all its term groups,
+// stacked operator forms, per-term operator blocks); warp 1 lane 0 issues the
+// tensor-core products and commits into one of two TMEM buffers, so that the
+// products of the next unit overlap the consumers; warps 2-9 (consumers) read
+// TMEM, transpose through shared memory, run the y / z steps and keep the g
+// accumulators (FP32 sums per unit, compensated sums over the units) of the
+// task.  A task is (g, l_z): its pencils x their term groups ("units", made by
+// the host and k_pencil_units); its 8 (k+1)^3 sums go to pen_partial[slot] in
+// FP64, and the chunk reduction adds the tasks of g after its chunk partials.
+//
+// Every wait is bounded (about a second of cycles); on expiry a thread sets
+// DE_TIMEOUT, its role stops, the others then time out too, and the CTA
+// waits (bounded) for its tensor-core work and frees TMEM.
+#include "mwgpu_internal.cuh"
+
+namespace mwgpu {
+namespace pencil {
+
+constexpr int NT = 320;                    // threads: producer warp, MMA warp, 8 consumer warps
+constexpr int NCW = 8;                     // consumer warps
+constexpr int GT = kPencilGroup;           // terms per group (per product)
+constexpr int CPT = 24;                    // D columns per term
+constexpr int NMAX = (GT * CPT + 15) / 16 * 16;   // 128: two D buffers of two tiles fit the 512 TMEM columns
+constexpr int NFS = kPencilSlots;          // f slots: one per x slot of a pencil
+constexpr int FREC = kTcNodeFloats * 4;    // bytes of a staged real node (hi 16 KB, lo 16 KB)
+constexpr int GREC = 8192;                 // bytes of a staged GenNode (hi 4 KB, lo 4 KB; rows 64-127 zero)
+constexpr int BREC = 128 * NMAX;           // bytes of a stacked form (hi s0, hi s1, lo s0, lo s1)
+constexpr int OREC = GT * 2 * 256 * 4;     // bytes of the per-term operator blocks of a unit (O^y, O^z)
+// S1 staging: S1[x][y][z] at x XS + y YS + z; U[x][y][z] at x US + y UYS + z
+// (strides chosen so that the drain stores and the float4 loads avoid bank conflicts)
+constexpr int YS = 20, XS = 336, UYS = 12, US = 112;
+constexpr int S1_FLOATS = 16 * XS + 8 * US;
+// Y / P exchange (per consumer warp): Y[xl][y][z] at xl 336 + y 20 + z, P[xl][y][z] at xl 112 + y 12 + z
+constexpr int YW = 2 * 336, PW = 2 * 112;
+// shared memory map (bytes)
+constexpr int SM_F = 0;                              // NFS real-node slots
+constexpr int SM_G = SM_F + NFS * FREC;              // NFS GenNode slots (a slot's node is real or generated)
+constexpr int SM_B = SM_G + NFS * GREC;              // 2 form slots
+constexpr int SM_O = SM_B + 2 * BREC;                // 2 operator-block slots
+constexpr int SM_S1 = SM_O + 2 * OREC;               // S1 staging
+constexpr int SM_Y = SM_S1 + 4 * S1_FLOATS;          // Y / P exchange
+constexpr int SM_BYTES = SM_Y + 4 * NCW * (YW + PW);
+static_assert(SM_BYTES + 1024 <= 227 * 1024, "pencil kernel shared memory");
+static_assert(SM_F % 1024 == 0 && SM_G % 1024 == 0 && SM_B % 1024 == 0 && SM_O % 16 == 0 && SM_S1 % 16 == 0, "alignment");
+constexpr int TM_COLS = 512;                         // D buffer db at column 256 db, tile t at + 128 t
+constexpr long long kSpin = 1ll << 31;               // about a second at 2 GHz
+
+__host__ __device__ constexpr uint32_t idesc(int M, int N) {
+    // kind::tf32: D f32, A and B tf32, both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: no swizzle, K-major; lbo = byte stride between
+// the two 16-byte k chunks, sbo = byte stride between 8-row groups
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
+           ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
+}
+__device__ __forceinline__ void bar_init(uint64_t *bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count));
+}
+__device__ __forceinline__ void bar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+__device__ __forceinline__ void expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(su32(dst)), "l"(src),
+                 "r"(bytes), "r"(su32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(su32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > kSpin) return false;
+    }
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+// true on every consumer thread iff v is true on all of them (named barrier 1,
+// so that control flow around the consumers' barriers stays uniform)
+__device__ __forceinline__ bool consumers_all(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 1, 256, q;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];" : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 4; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// x = hi + lo: hi the TF32 rounding of x, lo the exact remainder
+__device__ __forceinline__ void split(float x, float &hi, float &lo) {
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    hi = __uint_as_float(h);
+    lo = x - hi;
+}
+
+// padded N of a tensor-core product with n terms (M = 128 needs N % 16 == 0)
+__host__ __device__ constexpr int n_pad(int n) { return (CPT * n + 15) / 16 * 16; }
+
+// ---------------------------------------------------------------------------
+// Stacked operator forms: per (depth, group, slot b: l_x = 0, -k, +k) the B
+// operand of the x step for the group's terms (rows q .. of the depth's term
+// rows, band width <= kPencilMaxW, GT per group) that reach |l_x|.  Row
+// n = 24 j + c (term j of the group, column c), k = 8 s + q0 (s = b0, the
+// input x bit; q0 the input index):
+//   c in  0..7:  a0 = 0, p0 = c      from b0 = 1 (C block, idx 1)
+//   c in  8..15: a0 = 1, p0 = c - 8  (B block idx 2 from b0 = 0, A block idx 3 from b0 = 1)
+//   c in 16..23: a0 = 0, p0 = c - 16 from b0 = 0 (T block, idx 0)
+// value = block[q0 + K p0] (MRCPP's K x K column-major block of g = f^T op),
+// zero where |l_x| > bw[idx].  Layout per k step s: (n >> 3) 256 + (k >> 2) 128
+// + (n & 7) 16 + (k & 3) 4 bytes (LBO 128, SBO 256); hi s0, hi s1, lo s0, lo s1,
+// each 32 N_pad bytes.
+__global__ void k_stack_forms(DevOper op, const PencilFormJob *jobs, int n_jobs, float *forms) {
+    const int jb = blockIdx.x;
+    if (jb >= n_jobs) return;
+    const PencilFormJob J = jobs[jb];
+    const int N = n_pad(J.nt);
+    const int T = op.n_terms;
+    float *out = forms + J.off;
+    const int per = 16 * N;  // elements per hi (or lo) copy: N rows x 16 k
+    for (int e = threadIdx.x; e < per; e += blockDim.x) {
+        const int n = e >> 4, k = e & 15, s = k >> 3, kl = k & 7;
+        float hi = 0.f, lo = 0.f;
+        if (n < CPT * J.nt) {
+            const int j = n / CPT, c = n % CPT;
+            const TermRow row = op.term_rows[(size_t)J.depth * T + J.q + j];
+            int idx = -1, p0 = 0;
+            if (c < 8) { if (s == 1) idx = 1; p0 = c; }
+            else if (c < 16) { idx = s == 0 ? 2 : 3; p0 = c - 8; }
+            else { if (s == 0) idx = 0; p0 = c - 16; }
+            if (idx >= 0 && row.off >= 0 && abs(J.lx) <= row.L0 && abs(J.lx) <= row.wd[idx]) {
+                const double v = op.blocks[((size_t)(row.off + J.lx + row.L0) * 4 + idx) * 64 + kl + 8 * p0];
+                split((float)v, hi, lo);
+            }
+        }
+        const int o = s * 8 * N + (n >> 3) * 64 + (kl >> 2) * 32 + (n & 7) * 4 + (kl & 3);
+        out[o] = hi;
+        out[16 * N + o] = lo;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Units (PencilUnit, mwgpu_internal.cuh): made on the host from the topology;
+// k_pencil_units fills the f nodes of the pencil and what the contraction
+// needs to know about them.
+using Unit = PencilUnit;
+
+__device__ inline bool node_nonzero(const DevTree &f, int fid) {
+    const double *nrm = f.norms + (size_t)fid * 8;
+    if (fid >= f.cap_real) return !(nrm[0] < kMachineZero);
+    for (int c = 0; c < 8; c++)
+        if (!(nrm[c] < kMachineZero)) return true;
+    return false;
+}
+
+__device__ __forceinline__ int slot_lx(int b) { return b == 0 ? 0 : ((b & 1) ? -((b + 1) >> 1) : (b >> 1)); }
+
+__global__ void k_pencil_units(DevMRA m, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, Unit *units, int n_units,
+                               int *err) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= n_units) return;
+    Unit U = units[u];
+    const int tr = work_tree[U.wi];
+    const DevTree &f = fs[tr];
+    const int4 gx = gs[tr].idx[work[U.wi]];
+    int flags = 0, w0 = 0, w1 = 0;
+    for (int b = 0; b < kPencilSlots; b++) {
+        U.fid[b] = -1;
+        const int lx = slot_lx(b);
+        if (abs(lx) > U.xw || U.ntk[abs(lx)] == 0) continue;
+        NodeKey key;
+        if (!pack_key(m, gx.x, gx.y + lx, gx.z + U.ly, gx.w + U.lz, key)) continue;  // outside the world
+        const int fid = hash_find(f.hkeys, f.hvals, f.hcap, key);
+        if (fid < 0) {
+            atomicOr(err, DE_LOOKUP);
+            continue;
+        }
+        if (!node_nonzero(f, fid)) continue;
+        U.fid[b] = fid;
+        const bool gen = fid >= f.cap_real;
+        if (gen) flags |= 1 << b;
+        // the first product of a tile (slot order) sets how many terms its D holds
+        const int n = U.ntk[abs(lx)];
+        if (w0 == 0) w0 = n;
+        if (w1 == 0 && !gen) w1 = n;
+    }
+    U.flags = flags;
+    U.wt0 = (short)w0;
+    U.wt1 = (short)w1;
+    units[u] = U;
+}
+
+// ---------------------------------------------------------------------------
+// The contraction.
+__global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs, const int *work_tree, const Unit *units, const int *task_unit,
+                                                  int n_tasks, double *pen_partial, int *err, int *counter) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t f_full[NFS], f_empty[NFS], b_full[2], b_empty[2], o_full[2], o_empty[2], d_full[2], d_empty[2], bar_end;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_task;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int T = op.n_terms;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&s_tmem)), "r"(TM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < NFS; i++) {
+            bar_init(&f_full[i], 1);
+            bar_init(&f_empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            bar_init(&b_full[i], 1);
+            bar_init(&b_empty[i], 1);
+            bar_init(&o_full[i], 1);
+            bar_init(&o_empty[i], NCW);
+            bar_init(&d_full[i], 1);
+            bar_init(&d_empty[i], NCW);
+        }
+        bar_init(&bar_end, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // GenNode slots: rows 64-127 of both k chunks stay zero (only the b1 = 0 rows are copied)
+    for (int i = tid; i < NFS * GREC / 16; i += NT) reinterpret_cast<float4 *>(sm + SM_G)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = s_tmem;
+
+    // running counters (the producer and the MMA lane walk the same units and nodes)
+    unsigned nu = 0;            // units done
+    unsigned nb = 0;            // forms
+    unsigned nfs[NFS];          // pencils staged in (producer) / released from (MMA) each f slot
+    for (int i = 0; i < NFS; i++) nfs[i] = 0;
+    unsigned pmask = 0;         // f slots of the current pencil
+    bool lbad = false;
+    auto fail = [&]() {
+        if (!lbad) atomicOr(err, DE_TIMEOUT);
+        lbad = true;
+    };
+    const int cw = warp - 2;                       // consumer index 0..7 (x pair 2 cw, 2 cw + 1)
+    float *S1s = reinterpret_cast<float *>(sm + SM_S1);
+    float *Us = S1s + 16 * XS;
+    float *Yw = reinterpret_cast<float *>(sm + SM_Y) + (cw >= 0 ? cw : 0) * (YW + PW);
+    float *Pw = Yw + YW;
+    const int xl = lane >> 4;                      // which of the two x of this warp
+    const int xo = 2 * (cw >= 0 ? cw : 0) + xl;    // x of this lane
+    const int yq = (lane >> 2) & 3, zq = lane & 3; // lane tile: y 4 yq .. +3, z 4 zq .. +3
+    float G[16], Gc[16];
+
+    for (;;) {
+        if (tid == 0) s_task = atomicAdd(counter, 1);
+        __syncthreads();
+        const int task = s_task;
+        if (task >= n_tasks) break;
+        const int u0 = task_unit[task], u1 = task_unit[task + 1];
+#pragma unroll
+        for (int i = 0; i < 16; i++) G[i] = Gc[i] = 0.f;
+
+        if (warp == 0) {
+            // ---------------- producer ----------------
+            if (lane == 0 && !lbad) {
+                for (int u = u0; u < u1 && !lbad; u++) {
+                    const Unit &U = units[u];
+                    const DevTree &f = fs[work_tree[U.wi]];
+                    if (U.pflags & 1) {
+                        // the pencil's f nodes, once for all its term groups (the first group has the widest window)
+                        for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                            const int fid = U.fid[b];
+                            if (fid < 0) continue;
+                            if (nfs[b] >= 1 && !bar_wait(&f_empty[b], (nfs[b] - 1) & 1)) { fail(); break; }
+                            if (fid < f.cap_real) {
+                                expect_tx(&f_full[b], FREC);
+                                bulk(sm + SM_F + b * FREC, f.tc32 + (size_t)fid * kTcNodeFloats, FREC, &f_full[b]);
+                            } else {
+                                const float *src = f.gtc32 + (size_t)(fid - f.cap_real) * kTcGenFloats;
+                                unsigned char *dst = sm + SM_G + b * GREC;
+                                expect_tx(&f_full[b], 4096);
+                                bulk(dst, src, 1024, &f_full[b]);               // hi, k chunk 0, rows 0-63
+                                bulk(dst + 2048, src + 256, 1024, &f_full[b]);  // hi, k chunk 1
+                                bulk(dst + 4096, src + 512, 1024, &f_full[b]);  // lo, k chunk 0
+                                bulk(dst + 6144, src + 768, 1024, &f_full[b]);  // lo, k chunk 1
+                            }
+                            nfs[b]++;
+                        }
+                    }
+                    for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                        if (U.fid[b] < 0) continue;
+                        const int s = nb & 1;
+                        if (nb >= 2 && !bar_wait(&b_empty[s], ((nb >> 1) - 1) & 1)) { fail(); break; }
+                        const uint32_t bytes = 128u * (uint32_t)n_pad(U.nform[b]);
+                        expect_tx(&b_full[s], bytes);
+                        bulk(sm + SM_B + s * BREC, op.btc_stack + U.form[b], bytes, &b_full[s]);
+                        nb++;
+                    }
+                    if (lbad) break;
+                    // per-term O^y(l_y), O^z(l_z) blocks for the consumers
+                    const int so = nu & 1;
+                    if (nu >= 2 && !bar_wait(&o_empty[so], ((nu >> 1) - 1) & 1)) { fail(); break; }
+                    expect_tx(&o_full[so], (uint32_t)U.nt * 2048u);
+                    for (int j = 0; j < U.nt; j++) {
+                        const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
+                        unsigned char *dst = sm + SM_O + so * OREC + j * 2048;
+                        bulk(dst, op.blocks32 + (size_t)(row.off + U.ly + row.L0) * 256, 1024, &o_full[so]);
+                        bulk(dst + 1024, op.blocks32 + (size_t)(row.off + U.lz + row.L0) * 256, 1024, &o_full[so]);
+                    }
+                    nu++;
+                }
+            }
+        } else if (warp == 1) {
+            // ---------------- MMA issue ----------------
+            if (lane == 0 && !lbad) {
+                for (int u = u0; u < u1 && !lbad; u++) {
+                    const Unit &U = units[u];
+                    const DevTree &f = fs[work_tree[U.wi]];
+                    const int db = nu & 1;
+                    if (U.pflags & 1) {
+                        // the pencil's f nodes are staged
+                        pmask = 0;
+                        for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                            if (U.fid[b] < 0) continue;
+                            if (!bar_wait(&f_full[b], nfs[b] & 1)) { fail(); break; }
+                            pmask |= 1u << b;
+                        }
+                        if (lbad) break;
+                    }
+                    // the consumers have read this D buffer (unit nu - 2)
+                    if (nu >= 2 && !bar_wait(&d_empty[db], ((nu >> 1) - 1) & 1)) { fail(); break; }
+                    fence_after();
+                    const uint32_t dbase = tmem + 256u * db;
+                    bool first[2] = {true, true};
+                    for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                        const int fid = U.fid[b];
+                        if (fid < 0) continue;
+                        const bool gen = fid >= f.cap_real;
+                        const uint32_t a_hi = gen ? su32(sm + SM_G + b * GREC) : su32(sm + SM_F + b * FREC);
+                        const int nt_tiles = gen ? 1 : 2, nks = gen ? 1 : 2;
+                        const int sbix = nb & 1;
+                        if (!bar_wait(&b_full[sbix], (nb >> 1) & 1)) { fail(); break; }
+                        nb++;
+                        fence_after();
+                        const int nt = U.ntk[(b + 1) >> 1];
+                        const int N = n_pad(nt), NF = n_pad(U.nform[b]);   // product N; the form's own N sets its layout
+                        const uint32_t id = idesc(128, N);
+                        const uint32_t b_hi = su32(sm + SM_B + sbix * BREC), b_lo = b_hi + 64u * NF;
+                        // real nodes: region (tile t, k step s) at (2 t + s) 4 KB, lo at +16 KB;
+                        // GenNodes: one region, lo at +4 KB
+                        const uint32_t lo_off = gen ? 4096u : 16384u;
+                        for (int t = 0; t < nt_tiles; t++)
+                            for (int s = 0; s < nks; s++) {
+                                const uint32_t ao = gen ? 0u : (uint32_t)(2 * t + s) * 4096u, bo = (uint32_t)s * 32u * NF;
+                                const uint64_t ah = sdesc(a_hi + ao, 2048, 128), al = sdesc(a_hi + lo_off + ao, 2048, 128);
+                                const uint64_t bh = sdesc(b_hi + bo, 128, 256), bl = sdesc(b_lo + bo, 128, 256);
+                                const uint32_t d = dbase + 128u * t;
+                                const uint32_t acc0 = (first[t] && s == 0) ? 0u : 1u;
+                                mma(d, al, bh, id, acc0);
+                                mma(d, ah, bl, id, 1u);
+                                mma(d, ah, bh, id, 1u);
+                            }
+                        for (int t = 0; t < nt_tiles; t++) first[t] = false;
+                        commit(&b_empty[sbix]);    // the form slot is free once these products finish
+                    }
+                    commit(&d_full[db]);           // also after a failure, so that the consumers are released
+                    if (U.pflags & 2) {
+                        // last group of the pencil: its f slots are free once the products finish
+                        for (int b = 0; b < NFS; b++)
+                            if ((pmask >> b) & 1u) {
+                                commit(&f_empty[b]);
+                                nfs[b]++;
+                            }
+                    }
+                    nu++;
+                }
+            }
+        } else {
+            // ---------------- consumers ----------------
+            const int quarter = warp & 3, half = cw >> 2;   // TMEM lanes 32 quarter ..; columns of half
+            const int r = 32 * quarter + lane;              // D row of this thread: b1 64 + q1 + 8 q2
+            const int b1 = r >> 6, q1 = r & 7, q2 = (r >> 3) & 7;
+            const int yrow = 8 * b1 + q1;
+            const int a1 = yq >> 1, ph1 = yq & 1;           // y_out = 8 a1 + 4 ph1 + (0..3)
+            const int a2 = zq >> 1, ph2 = zq & 1;           // z_out = 8 a2 + 4 ph2 + (0..3)
+            const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int u = u0; u < u1; u++) {
+                const Unit &U = units[u];
+                const bool pure = U.depth > 0;   // the s->s path is left out below the roots
+                const int so = nu & 1, db = nu & 1;
+                bool ok = !lbad;
+                if (ok && !bar_wait(&o_full[so], (nu >> 1) & 1)) { fail(); ok = false; }
+                if (ok && !bar_wait(&d_full[db], (nu >> 1) & 1)) { fail(); ok = false; }
+                ok = consumers_all(ok);
+                fence_after();
+                const float *OB = reinterpret_cast<const float *>(sm + SM_O + so * OREC);
+                const int nw = U.wt0;
+                const int ly = U.ly, lz = U.lz;
+                float Gu[16];
+#pragma unroll
+                for (int i = 0; i < 16; i++) Gu[i] = 0.f;
+                for (int j = 0; j < nw && ok; j++) {
+                    // ---- drain S1 of term j (both z halves) into shared memory ----
+                    const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
+                    for (int t = 0; t < 2; t++) {
+                        const bool have = j < (t == 0 ? U.wt0 : U.wt1);
+                        float cC[4], cA[4], cT[4];
+                        if (have) {
+                            const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16) + 256u * db + 128u * t + CPT * j;
+                            tmem_ld4(base + 4 * half, cC);
+                            tmem_ld4(base + 8 + 4 * half, cA);
+                            tmem_ld4(base + 16 + 4 * half, cT);
+                            tmem_wait_ld();
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < 4; i++) cC[i] = cA[i] = cT[i] = 0.f;
+                        }
+                        const int z = 8 * t + q2;
+                        const bool u_row = pure && t == 0 && b1 == 0;
+#pragma unroll
+                        for (int i = 0; i < 4; i++) {
+                            const int x0 = 4 * half + i;     // a0 = 0
+                            S1s[x0 * XS + yrow * YS + z] = u_row ? cC[i] : cC[i] + cT[i];
+                            S1s[(8 + x0) * XS + yrow * YS + z] = cA[i];
+                            if (u_row) Us[x0 * US + q1 * UYS + q2] = cT[i];
+                        }
+                    }
+                    consumers_sync();
+                    // blocks (a, b) of a direction take part iff |l| <= bw[2a + b]
+                    unsigned vy = 0, vz = 0;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        vy |= (abs(ly) <= row.wd[c] ? 1u : 0u) << c;
+                        vz |= (abs(lz) <= row.wd[c] ? 1u : 0u) << c;
+                    }
+                    const float4 *Oy4 = reinterpret_cast<const float4 *>(OB + j * 512);
+                    const float4 *Oz4 = Oy4 + 64;
+                    // ---- y step: Y[x][y_out][z] (lane tile y 4 yq.., z 4 zq..), P (U channel) ----
+                    float Y[4][4], P[4][4];
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++) Y[a][c] = P[a][c] = 0.f;
+                    const float4 *S14 = reinterpret_cast<const float4 *>(S1s + xo * XS) + zq;
+#pragma unroll
+                    for (int bb = 0; bb < 2; bb++) {
+                        const int idx = 2 * a1 + bb;
+                        const bool v = (vy >> idx) & 1u;
+#pragma unroll 4
+                        for (int qq = 0; qq < 8; qq++) {
+                            // O^y[y_out][y_in] = block_idx(in q1 -> out p1) = blocks32[idx 64 + 8 q1 + p1]
+                            const float4 w = v ? Oy4[idx * 16 + 2 * qq + ph1] : zero4;
+                            const float4 sv = S14[(8 * bb + qq) * (YS / 4)];
+                            const float wv[4] = {w.x, w.y, w.z, w.w}, s4[4] = {sv.x, sv.y, sv.z, sv.w};
+#pragma unroll
+                            for (int a = 0; a < 4; a++)
+#pragma unroll
+                                for (int c = 0; c < 4; c++) Y[a][c] = fmaf(wv[a], s4[c], Y[a][c]);
+                        }
+                    }
+                    // U channel: rows x < 8 (a0 = 0), z < 8 (b2 = 0), y_in < 8 (b1 = 0):
+                    // T (a1 = 0) into P, B (a1 = 1) into Y
+                    const bool uch = pure && xo < 8 && zq < 2;
+                    if (uch) {
+                        const int idx = 2 * a1;
+                        const bool v = (vy >> idx) & 1u;
+                        const float4 *U4 = reinterpret_cast<const float4 *>(Us + xo * US) + zq;
+#pragma unroll 4
+                        for (int k = 0; k < 8; k++) {
+                            const float4 w = v ? Oy4[idx * 16 + 2 * k + ph1] : zero4;
+                            const float4 sv = U4[k * (UYS / 4)];
+                            const float wv[4] = {w.x, w.y, w.z, w.w}, s4[4] = {sv.x, sv.y, sv.z, sv.w};
+                            if (a1 == 1) {
+#pragma unroll
+                                for (int a = 0; a < 4; a++)
+#pragma unroll
+                                    for (int c = 0; c < 4; c++) Y[a][c] = fmaf(wv[a], s4[c], Y[a][c]);
+                            } else {
+#pragma unroll
+                                for (int a = 0; a < 4; a++)
+#pragma unroll
+                                    for (int c = 0; c < 4; c++) P[a][c] = fmaf(wv[a], s4[c], P[a][c]);
+                            }
+                        }
+                    }
+                    // the S1 staging may be overwritten once every consumer has read it
+                    consumers_sync();
+                    // ---- exchange: Y rows (and P) to the lanes of the z step ----
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+                        *reinterpret_cast<float4 *>(Yw + xl * 336 + (4 * yq + a) * 20 + 4 * zq) = make_float4(Y[a][0], Y[a][1], Y[a][2], Y[a][3]);
+                    if (uch && a1 == 0)
+#pragma unroll
+                        for (int a = 0; a < 4; a++)
+                            *reinterpret_cast<float4 *>(Pw + xl * 112 + (4 * yq + a) * 12 + 4 * zq) = make_float4(P[a][0], P[a][1], P[a][2], P[a][3]);
+                    __syncwarp();
+                    // ---- z step into the unit sums: lane tile y 4 yq .., z_out 4 zq .. ----
+#pragma unroll
+                    for (int bb = 0; bb < 2; bb++) {
+                        const int idx = 2 * a2 + bb;
+                        const bool v = (vz >> idx) & 1u;
+#pragma unroll
+                        for (int q4 = 0; q4 < 8; q4 += 4) {
+                            float yv[4][4];
+#pragma unroll
+                            for (int a = 0; a < 4; a++) {
+                                const float4 t4 = *reinterpret_cast<const float4 *>(Yw + xl * 336 + (4 * yq + a) * 20 + 8 * bb + q4);
+                                yv[a][0] = t4.x;
+                                yv[a][1] = t4.y;
+                                yv[a][2] = t4.z;
+                                yv[a][3] = t4.w;
+                            }
+#pragma unroll
+                            for (int kk = 0; kk < 4; kk++) {
+                                const float4 w = v ? Oz4[idx * 16 + 2 * (q4 + kk) + ph2] : zero4;
+                                const float wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                                for (int a = 0; a < 4; a++)
+#pragma unroll
+                                    for (int c = 0; c < 4; c++) Gu[4 * a + c] = fmaf(yv[a][kk], wv[c], Gu[4 * a + c]);
+                            }
+                        }
+                    }
+                    // P through z with the B block only (a2 = 1 from b2 = 0): the T.T.T path is left out
+                    if (pure && xo < 8 && yq < 2 && a2 == 1 && ((vz >> 2) & 1u)) {
+#pragma unroll
+                        for (int q4 = 0; q4 < 8; q4 += 4) {
+                            float pv[4][4];
+#pragma unroll
+                            for (int a = 0; a < 4; a++) {
+                                const float4 t4 = *reinterpret_cast<const float4 *>(Pw + xl * 112 + (4 * yq + a) * 12 + q4);
+                                pv[a][0] = t4.x;
+                                pv[a][1] = t4.y;
+                                pv[a][2] = t4.z;
+                                pv[a][3] = t4.w;
+                            }
+#pragma unroll
+                            for (int kk = 0; kk < 4; kk++) {
+                                const float4 w = Oz4[2 * 16 + 2 * (q4 + kk) + ph2];
+                                const float wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                                for (int a = 0; a < 4; a++)
+#pragma unroll
+                                    for (int c = 0; c < 4; c++) Gu[4 * a + c] = fmaf(pv[a][kk], wv[c], Gu[4 * a + c]);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+                // compensated sums over the units
+#pragma unroll
+                for (int e = 0; e < 16; e++) {
+                    const float yv = Gu[e] - Gc[e];
+                    const float tv = G[e] + yv;
+                    Gc[e] = (tv - G[e]) - yv;
+                    G[e] = tv;
+                }
+                // D and the operator blocks of this unit are free
+                fence_before();
+                __syncwarp();
+                if (lane == 0) {
+                    bar_arrive(&d_empty[db]);
+                    bar_arrive(&o_empty[so]);
+                }
+                nu++;
+            }
+            // the task's sums (slot of its units; every task has one): g component
+            // gt = a0 + 2 a1 + 4 a2, element p0 + 8 p1 + 64 p2
+            double *go = pen_partial + (size_t)units[u0].task * 4096;
+            const int a0 = xo >> 3, p0 = xo & 7;
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const int yo = 4 * yq + a, zo = 4 * zq + c;
+                    const int gt = a0 + 2 * (yo >> 3) + 4 * (zo >> 3);
+                    go[gt * 512 + p0 + 8 * (yo & 7) + 64 * (zo & 7)] = (double)G[4 * a + c] - (double)Gc[4 * a + c];
+                }
+        }
+        // the producer / MMA lanes other than 0 did not walk the units: bring their counters along
+        if (warp <= 1) {
+            nu = __shfl_sync(0xffffffffu, nu, 0);
+            nb = __shfl_sync(0xffffffffu, nb, 0);
+            for (int i = 0; i < NFS; i++) nfs[i] = __shfl_sync(0xffffffffu, nfs[i], 0);
+        }
+        const bool any_bad = __syncthreads_or(lbad) != 0;
+        if (any_bad) {
+            lbad = true;
+            break;
+        }
+    }
+    // wait (bounded) for the tensor-core work in flight, then free TMEM
+    __syncthreads();
+    if (tid == 32) {
+        fence_after();
+        commit(&bar_end);
+        bar_wait(&bar_end, 0);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TM_COLS));
+}
+
+// ---------------------------------------------------------------------------
+// Work items that the pencil kernel covers (terms of band width <= kPencilMaxW
+// at the depth of g) leave the list of the item kernel: per work entry a
+// stable compaction.
+__device__ __forceinline__ bool kept(const DevOper &op, int depth, const WorkItem &it) {
+    return op.bw[((size_t)it.term * op.max_rows + depth) * 5 + 4] > kPencilMaxW;
+}
+
+__global__ void k_keep_count(DevMRA m, DevOper op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off, int n_work,
+                             const WorkItem *items, int *keep, const int *nw_dev) {
+    const int wi = blockIdx.x;
+    if (nw_dev && wi >= *nw_dev) {
+        if (threadIdx.x == 0) keep[wi] = 0;
+        return;
+    }
+    if (wi >= n_work) return;
+    const int depth = gs[work_tree[wi]].idx[work[wi]].x - m.root_scale;
+    int c = 0;
+    for (long long i = g_off[wi] + threadIdx.x; i < g_off[wi + 1]; i += blockDim.x) c += kept(op, depth, items[i]) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    __shared__ int red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        keep[wi] = t;
+    }
+}
+
+__global__ void k_keep_fill(DevMRA m, DevOper op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
+                            const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, const int *nw_dev) {
+    const int wi = blockIdx.x;
+    if (wi >= n_work || (nw_dev && wi >= *nw_dev)) return;
+    const int depth = gs[work_tree[wi]].idx[work[wi]].x - m.root_scale;
+    const long long b = g_off[wi], e = g_off[wi + 1];
+    long long dst = k_off[wi];
+    const int lane = threadIdx.x & 31;
+    // one warp keeps the order: ballot prefix per 32 items
+    for (long long i0 = b; i0 < e; i0 += 32) {
+        const long long i = i0 + lane;
+        const bool k = i < e && kept(op, depth, in[i]);
+        const unsigned mk = __ballot_sync(0xffffffffu, k);
+        if (k) out[dst + __popc(mk & ((1u << lane) - 1u))] = in[i];
+        dst += __popc(mk);
+    }
+}
+
+}  // namespace pencil
+
+bool pencil_supported(int K) { return K == 8; }
+
+void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *forms, cudaStream_t s) {
+    if (n_jobs <= 0) return;
+    pencil::k_stack_forms<<<n_jobs, 256, 0, s>>>(op, (const PencilFormJob *)jobs, n_jobs, forms);
+}
+
+void launch_pencil_units(const DevMRA &m, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, void *units, int n_units,
+                         int *err, cudaStream_t s) {
+    if (n_units <= 0) return;
+    pencil::k_pencil_units<<<(n_units + 127) / 128, 128, 0, s>>>(m, fs, gs, work_tree, work, (pencil::Unit *)units, n_units, err);
+}
+
+void launch_keep_items(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
+                       int n_work, const WorkItem *in, int *keep, cudaStream_t s, const int *nw_dev) {
+    if (n_work <= 0) return;
+    pencil::k_keep_count<<<n_work, 256, 0, s>>>(m, op, gs, work_tree, work, g_off, n_work, in, keep, nw_dev);
+}
+
+void launch_keep_fill(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
+                      const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, const int *nw_dev) {
+    if (n_work <= 0) return;
+    pencil::k_keep_fill<<<n_work, 32, 0, s>>>(m, op, gs, work_tree, work, g_off, k_off, n_work, in, out, nw_dev);
+}
+
+void launch_pencil(const DevOper &op, const DevTree *fs, const int *work_tree, const void *units, const int *task_unit, int n_tasks,
+                   double *pen_partial, int *err, int *counter, cudaStream_t s) {
+    if (n_tasks <= 0) return;
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncSetAttribute(pencil::k_pencil, cudaFuncAttributeMaxDynamicSharedMemorySize, pencil::SM_BYTES);
+        if (sms <= 0) sms = 1;
+    }
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    pencil::k_pencil<<<std::min(sms, n_tasks), pencil::NT, pencil::SM_BYTES, s>>>(op, fs, work_tree, (const pencil::Unit *)units, task_unit,
+                                                                                   n_tasks, pen_partial, err, counter);
+}
+
+}  // namespace mwgpu

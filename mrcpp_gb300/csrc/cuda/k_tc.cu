@@ -487,8 +487,10 @@ __global__ void __launch_bounds__(NT, 1) k_contract_tc(DevMRA m, DevOper op, con
 
 // ---- layouts made at upload / GenNode creation ----
 
-// real nodes: element (b, x, yz) of node i -> tile b >> 2, k-step b & 1, row (b >> 1 & 1) 64 + yz, k = x
-__global__ void k_tree_layout(const double *coefs, int first, int n, float *tc) {
+// real nodes: element (b, x, yz) of node i -> tile b >> 2, k-step b & 1, row (b >> 1 & 1) 64 + yz, k = x.
+// A component whose norm is below MachineZero is stored as zero: the reference
+// skips such a component for every output node (ConvolutionCalculator.cpp:258)
+__global__ void k_tree_layout(const double *coefs, const double *norms, int first, int n, float *tc) {
     const int i = first + blockIdx.x;
     if (blockIdx.x >= n) return;
     const double *src = coefs + (size_t)i * 4096;
@@ -498,7 +500,7 @@ __global__ void k_tree_layout(const double *coefs, int first, int n, float *tc) 
         const int reg = 2 * (bb >> 2) + (bb & 1), mm = ((bb >> 1) & 1) * 64 + yz;
         const int o = reg * 1024 + (x >> 2) * 512 + (mm >> 3) * 32 + (mm & 7) * 4 + (x & 3);
         float hi, lo;
-        split((float)src[e], hi, lo);
+        split(norms[(size_t)i * 8 + bb] < kMachineZero ? 0.f : (float)src[e], hi, lo);
         dst[o] = hi;
         dst[4096 + o] = lo;
     }
@@ -573,7 +575,7 @@ bool tc_supported(int K) { return K == 8; }
 
 void launch_tc_tree_layout(const DevTree &t, int first, int n, cudaStream_t s) {
     if (n <= 0 || !t.tc32) return;
-    tc::k_tree_layout<<<n, 256, 0, s>>>(t.coefs, first, n, t.tc32);
+    tc::k_tree_layout<<<n, 256, 0, s>>>(t.coefs, t.norms, first, n, t.tc32);
 }
 
 void launch_tc_oper_forms(const DevOper &op, const int4 *node_info, int n_nodes, float *forms, cudaStream_t s) {

@@ -272,6 +272,107 @@ void pair_offsets(const Level &lv, std::vector<long long> &poff) {
     }
 }
 
+// The pencil contraction (k_pencil.cu) takes the terms of band width <=
+// kPencilMaxW on levels without norm screening (every gThreshold negative:
+// fixed grids, first TreeBuilder iterations), order 7, input trees with their
+// TF32 operands; the item kernel keeps the wider terms.  MWGPU_NO_PENCIL
+// selects the item kernel for everything (the same sums).
+bool use_pencil(const Level &lv) {
+    const mwgpu_oper *o = lv.o;
+    if (!pencil_supported(o->op.K) || !o->op.btc_stack || lv.band_dir >= 0 || std::getenv("MWGPU_NO_PENCIL")) return false;
+    for (double g : lv.gthr)
+        if (!(g < 0.0)) return false;
+    for (int t = 0; t < lv.nt; t++)
+        if (!lv.inps[t]->t.tc32) return false;
+    return true;
+}
+
+// Units of the pencil contraction from the topology: per work entry the tasks
+// (l_z in the world) with their pencils (l_y in the world) and term groups;
+// tasks in descending size (the persistent kernel takes them in this order),
+// each with its partial slot (slots of a work entry consecutive, pen_begin).
+struct PencilPlan {
+    std::vector<PencilUnit> units;  // in processing order of their tasks
+    std::vector<int> task_unit;     // first unit of every processed task, + total
+    std::vector<int> pen_begin;     // per work entry its first slot, + total
+    int n_tasks = 0;
+};
+
+void pencil_build(const Level &lv, PencilPlan &pp) {
+    const mwgpu_oper *o = lv.o;
+    const DevMRA &m = o->mra;
+    const int G = o->pen_groups, n = lv.n;
+    constexpr int G5 = mwgpu::kPencilGroup, NK = mwgpu::kPencilMaxL + 1, NS = mwgpu::kPencilSlots;
+    std::vector<std::vector<PencilUnit>> tasks;
+    std::vector<long long> cost;
+    pp.pen_begin.assign(n + 1, 0);
+    for (int wi = 0; wi < n; wi++) {
+        pp.pen_begin[wi] = (int)tasks.size();
+        const int4 gx = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]];
+        const int depth = gx.x - m.root_scale;
+        if (depth < 0 || depth >= o->n_rows || o->band_max[depth] < 0) continue;
+        const int *tk = &o->pen_tk[(size_t)depth * NK];
+        if (tk[0] == 0) continue;
+        const int W = std::min(o->band_max[depth], mwgpu::kPencilMaxL);
+        auto inworld = [&](int d, long long l) {
+            const long long c = (long long)m.corner[d] << depth, nb = (long long)m.nbox[d] << depth;
+            return l >= c && l < c + nb;
+        };
+        const int gl[3] = {gx.y, gx.z, gx.w};
+        for (int lz = -W; lz <= W; lz++) {
+            if (!inworld(2, (long long)gl[2] + lz)) continue;
+            std::vector<PencilUnit> us;
+            long long c = 0;
+            for (int ly = -W; ly <= W; ly++) {
+                if (!inworld(1, (long long)gl[1] + ly)) continue;
+                const int mm = std::max(std::abs(ly), std::abs(lz));
+                const int tm = tk[mm];
+                for (int q = 0; q * G5 < tm; q++) {
+                    PencilUnit U{};
+                    U.pflags = (short)((q == 0 ? 1 : 0) | ((q + 1) * G5 >= tm ? 2 : 0));
+                    U.task = (int)tasks.size();
+                    U.wi = wi;
+                    U.depth = (short)depth;
+                    U.ly = (signed char)ly;
+                    U.lz = (signed char)lz;
+                    U.q = (short)(o->pen_r0[depth] + G5 * q);
+                    U.nt = (short)std::min(G5, tm - G5 * q);
+                    int xw = 0;
+                    for (int k = 0; k < NK; k++) {
+                        U.ntk[k] = (short)std::min((int)U.nt, std::max(0, tk[k] - G5 * q));
+                        if (U.ntk[k] > 0) xw = k;
+                    }
+                    U.xw = (short)xw;
+                    for (int b = 0; b < NS; b++) {
+                        const size_t ix = ((size_t)depth * G + q) * NS + b;
+                        U.form[b] = o->pen_form[ix];
+                        U.nform[b] = o->pen_nform[ix];
+                        U.fid[b] = -1;
+                        if ((b + 1) / 2 <= xw) c += 2;   // tensor-core products
+                    }
+                    us.push_back(U);
+                    c += 3 * U.nt;                       // y / z steps
+                }
+            }
+            if (us.empty()) continue;
+            tasks.push_back(std::move(us));
+            cost.push_back(c);
+        }
+    }
+    pp.pen_begin[n] = (int)tasks.size();
+    pp.n_tasks = (int)tasks.size();
+    std::vector<int> ord(pp.n_tasks);
+    for (int i = 0; i < pp.n_tasks; i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    pp.units.clear();
+    pp.task_unit.assign(pp.n_tasks + 1, 0);
+    for (int k = 0; k < pp.n_tasks; k++) {
+        pp.task_unit[k] = (int)pp.units.size();
+        for (auto &U : tasks[ord[k]]) pp.units.push_back(U);
+    }
+    pp.task_unit[pp.n_tasks] = (int)pp.units.size();
+}
+
 // Mixed form: work list (pair counts, scan, fill) then the contraction over
 // chunks of items and the per-node reduction.  node_terms is returned in *hs.
 mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
@@ -317,8 +418,43 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
                       order ? ctx->d_items_cm : ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream);
     if (order) launch_order_terms(ctx->d_goff, n, ctx->d_items_cm, ctx->d_items, o->op.n_terms, ctx->d_err, ctx->stream);
     ctx->launches += 1 + (order ? 1 : 0);
+    // pencil path: the items of the wider terms stay with the item kernel (stable compaction into d_items_cm)
+    const bool pencil = use_pencil(lv);
+    const WorkItem *kitems = ctx->d_items;
+    PencilPlan pp;
+    if (pencil) {
+        if (auto s = grow_buf(ctx, &ctx->d_keep, &ctx->keep_cap, n + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_keep_off, &ctx->keep_off_cap, n + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_scan, &ctx->scan_cap, std::max(scan_blocks(np + 1), scan_blocks(n + 1)) + 2)) return s;
+        launch_keep_items(m, o->op, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_goff, n, ctx->d_items, ctx->d_keep, ctx->stream);
+        launch_scan(ctx->d_keep, ctx->d_keep_off, n, ctx->d_scan, ctx->d_scan + (ctx->scan_cap - 1), ctx->stream);
+        launch_keep_fill(m, o->op, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_goff, ctx->d_keep_off, n, ctx->d_items, ctx->d_items_cm,
+                         ctx->stream);
+        ctx->launches += 5;
+        MW_CK(cudaMemcpyAsync(offs.data(), ctx->d_keep_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
+        kitems = ctx->d_items_cm;
+        pencil_build(lv, pp);
+        const long long nu = (long long)pp.units.size();
+        if (auto s = grow_buf(ctx, &ctx->d_units, &ctx->units_cap, std::max(nu, 1LL))) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_task_unit, &ctx->task_unit_cap, pp.n_tasks + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_pen_begin, &ctx->pen_begin_cap, n + 1)) return s;
+        const size_t pneed = (size_t)std::max(pp.n_tasks, 1) * 8 * (size_t)o->mra.kp1_d;
+        if (pneed > ctx->pen_partial_cap) {
+            if (ctx->d_pen_partial) cudaFree(ctx->d_pen_partial);
+            ctx->d_pen_partial = nullptr;
+            ctx->pen_partial_cap = std::max(pneed, 2 * ctx->pen_partial_cap);
+            if (auto s = dev_alloc(ctx, &ctx->d_pen_partial, ctx->pen_partial_cap)) return s;
+        }
+        if (!ctx->d_pen_counter)
+            if (auto s = dev_alloc(ctx, &ctx->d_pen_counter, 1)) return s;
+        if (nu > 0) MW_CK(cudaMemcpyAsync(ctx->d_units, pp.units.data(), sizeof(PencilUnit) * nu, cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_task_unit, pp.task_unit.data(), sizeof(int) * (pp.n_tasks + 1), cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_pen_begin, pp.pen_begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+    }
     // chunks of about the same number of items, several waves of CTAs
-    long long per = std::max<long long>(8, (total + kChunkTarget - 1) / kChunkTarget);
+    const long long kept = offs[n];
+    long long per = std::max<long long>(8, (kept + kChunkTarget - 1) / kChunkTarget);
     if (const char *e = std::getenv("MWGPU_CHUNK_ITEMS")) per = std::max<long long>(1, std::atoll(e));
     std::vector<int4> chunks;
     std::vector<int> cbeg(n + 1, 0);
@@ -352,9 +488,21 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     // the tensor-core kernel only where every input tree carries its TF32 operands
     bool tc_ok = true;
     for (int t = 0; t < lv.nt; t++) tc_ok = tc_ok && lv.inps[t]->t.tc32 != nullptr;
-    launch_contract_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin, ctx->d_items,
-                          ctx->d_partial, ctx->d_err, tc_ok ? ctx->d_tc_counter : nullptr, ctx->stream);
-    ctx->launches += 2;
+    if (pencil) {
+        // the wider terms' items (chunks; a chunk of an entry without kept items is empty), the pencils, then both sums
+        launch_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_chunks, nch, kitems, ctx->d_partial, ctx->d_err,
+                     nullptr, nullptr, tc_ok ? ctx->d_tc_counter : nullptr, ctx->stream);
+        launch_pencil_units(o->mra, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_units, (int)pp.units.size(), ctx->d_err, ctx->stream);
+        launch_pencil(o->op, ctx->d_fs, ctx->d_wtree, ctx->d_units, ctx->d_task_unit, pp.n_tasks, ctx->d_pen_partial, ctx->d_err,
+                      ctx->d_pen_counter, ctx->stream);
+        launch_reduce_chunks(o->mra, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunk_begin, ctx->d_partial, ctx->stream, nullptr,
+                             ctx->d_pen_begin, ctx->d_pen_partial);
+        ctx->launches += 4;
+    } else {
+        launch_contract_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunks, nch, ctx->d_chunk_begin,
+                              ctx->d_items, ctx->d_partial, ctx->d_err, tc_ok ? ctx->d_tc_counter : nullptr, ctx->stream);
+        ctx->launches += 2;
+    }
     // (the chunk arrays came from pageable memory: the copies read them before returning)
     hs->node_terms = (unsigned long long)total;
     return MWGPU_OK;
@@ -395,12 +543,9 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
         if ((s = pool_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(ctx, tr); return s; }
         launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
         ctx->launches++;
-        // TF32 hi / lo operands of the opt-in tensor-core contraction (order 7, MWGPU_TC)
-        if (mwgpu::tc_supported(tr->mra.K) && n > 0 && std::getenv("MWGPU_TC")) {
+        // TF32 hi / lo operands of the tensor-core x step (order 7; made below, once the norms are there)
+        if (mwgpu::tc_supported(tr->mra.K) && n > 0)
             if ((s = pool_alloc(ctx, &t.tc32, (size_t)n * mwgpu::kTcNodeFloats))) { free_tree(ctx, tr); return s; }
-            mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
-            ctx->launches++;
-        }
     }
     if (d->norms) {
         MW_CK(cudaMemcpyAsync(t.norms, d->norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
@@ -413,6 +558,10 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
         ctx->launches++;
     } else {
         MW_CK(cudaMemsetAsync(t.norms, 0, sizeof(double) * tot * 8, ctx->stream));
+    }
+    if (input && t.tc32) {
+        mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
+        ctx->launches++;
     }
     trace.mark("fp32_norms");
     // only input trees are looked up by node index (band cells, GenNode
@@ -775,7 +924,9 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
                     (void *)ctx->d_plist, (void *)ctx->d_pcount, (void *)ctx->d_list, (void *)ctx->d_items, (void *)ctx->d_items_cm, (void *)ctx->d_chunks,
                     (void *)ctx->d_chunk_begin, (void *)ctx->d_partial, (void *)ctx->d_pair_off, (void *)ctx->d_pcounts,
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
-                    (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_nstage, (void *)ctx->d_ltree})
+                    (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_nstage, (void *)ctx->d_ltree, (void *)ctx->d_units,
+                    (void *)ctx->d_task_unit, (void *)ctx->d_pen_partial, (void *)ctx->d_pen_begin, (void *)ctx->d_keep, (void *)ctx->d_keep_off,
+                    (void *)ctx->d_pen_counter})
         if (p) cudaFree(p);
     pool_trim(ctx);
     for (auto &e : ctx->marks)
@@ -977,6 +1128,7 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.pair_bound_off = p_pboff;
     o->op.n_nodes = (int)node;
     o->op.btc = nullptr;
+    o->op.btc_stack = nullptr;
     o->op.band_dir = -1;
     o->op.band_dir_w = 0;
     if (mwgpu::tc_supported(K)) {
@@ -1000,6 +1152,60 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         mwgpu::launch_tc_oper_forms(o->op, p_ni, (int)node, p_btc, ctx->stream);
         MW_CK(cudaStreamSynchronize(ctx->stream));
         o->op.btc = p_btc;
+    }
+    if (mwgpu::pencil_supported(K)) {
+        // stacked x-step forms of the pencil contraction: per depth the terms of
+        // band width <= kPencilMaxW (after the wider ones in term-row order), in
+        // groups of kPencilGroup, for every x slot (l_x = 0, -k, +k) the group's
+        // terms with band width >= k
+        constexpr int G5 = mwgpu::kPencilGroup, NK = mwgpu::kPencilMaxL + 1, NS = mwgpu::kPencilSlots;
+        const int G = (T + G5 - 1) / G5;
+        o->pen_groups = G;
+        o->pen_tk.assign((size_t)rows * NK, 0);
+        o->pen_r0.assign(rows, 0);
+        o->pen_form.assign((size_t)rows * G * NS, -1);
+        o->pen_nform.assign((size_t)rows * G * NS, 0);
+        std::vector<mwgpu::PencilFormJob> jobs;
+        long long fl = 0;
+        for (int dd = 0; dd < rows; dd++) {
+            int r0 = 0;
+            for (int ti = 0; ti < T; ti++) {
+                const TermRow &tr = trows[(size_t)dd * T + ti];
+                if (tr.off < 0) continue;
+                if (tr.bw_max > mwgpu::kPencilMaxW) {
+                    r0++;
+                    continue;
+                }
+                for (int k = 0; k < NK; k++)
+                    if (tr.bw_max >= k) o->pen_tk[(size_t)dd * NK + k]++;
+            }
+            o->pen_r0[dd] = r0;
+            const int t0 = o->pen_tk[(size_t)dd * NK];
+            for (int q = 0; q * G5 < t0; q++)
+                for (int b = 0; b < NS; b++) {
+                    const int k = (b + 1) / 2, lx = b == 0 ? 0 : ((b & 1) ? -k : k);
+                    const int nt = std::max(0, std::min(G5, o->pen_tk[(size_t)dd * NK + k] - G5 * q));
+                    if (nt <= 0) continue;
+                    const size_t ix = ((size_t)dd * G + q) * NS + b;
+                    o->pen_form[ix] = fl;
+                    o->pen_nform[ix] = (short)nt;
+                    jobs.push_back({dd, r0 + G5 * q, lx, nt, fl});
+                    fl += 32LL * ((24 * nt + 15) / 16 * 16);
+                }
+        }
+        mwgpu::PencilFormJob *p_jobs = nullptr;
+        float *p_stack = nullptr;
+        if ((s = up(&p_jobs, jobs.data(), jobs.size())) || (s = dev_alloc(ctx, &p_stack, (size_t)std::max(fl, 1LL)))) {
+            for (void *p : o->allocs) cudaFree(p);
+            pool_free(ctx, o->d_filt);
+            delete o;
+            return s;
+        }
+        o->allocs.push_back((void *)p_stack);
+        mwgpu::launch_stack_forms(o->op, p_jobs, (int)jobs.size(), p_stack, ctx->stream);
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        MW_CK(cudaGetLastError());
+        o->op.btc_stack = p_stack;
     }
     *out = o;
     return MWGPU_OK;
@@ -1287,8 +1493,7 @@ mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tr, const doubl
     const size_t nc = 8 * (size_t)tr->mra.kp1_d;
     MW_CK(cudaMemcpyAsync(t.coefs, coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
     launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
-    mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
-    ctx->launches += 1 + (t.tc32 ? 1 : 0);
+    ctx->launches += 1;
     if (norms) {
         MW_CK(cudaMemcpyAsync(t.norms, norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
     } else {
@@ -1297,6 +1502,10 @@ mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tr, const doubl
         if (auto s = ensure_work(ctx, n)) return s;
         MW_CK(cudaMemcpyAsync(ctx->d_work, all.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
         launch_node_norms(tr->mra, t, ctx->d_work, n, ctx->stream);
+        ctx->launches++;
+    }
+    if (t.tc32) {
+        mwgpu::launch_tc_tree_layout(t, 0, n, ctx->stream);
         ctx->launches++;
     }
     MW_CK(cudaStreamSynchronize(ctx->stream));

@@ -78,6 +78,9 @@ struct DevOper {
     // operands of the tensor-core contraction (k_tc.cu), TF32 hi and lo parts,
     // with the blocks outside the band zeroed; null otherwise
     const float *btc;
+    // K = 8: stacked x-step forms of the pencil contraction (k_pencil.cu), per
+    // (depth, term group, x slot); null otherwise
+    const float *btc_stack;
     int n_nodes;
     // derivative operators (DerivativeCalculator::makeOperBand): the band runs
     // along band_dir only, band_dir_w wide; -1: the convolution band box
@@ -198,6 +201,34 @@ struct LevelStats {
     unsigned long long gen_nodes;    // GenNodes created
 };
 
+// One unit of the pencil contraction (k_pencil.cu): output node g (work entry
+// wi), pencil (l_y, l_z), and a group of up to kPencilGroup operator terms: the
+// terms of the depth in descending band width that reach the pencil
+// (w >= max(|l_y|, |l_z|)), from term row q on.  Slot b of the x window is
+// l_x = 0 (b = 0), -k (b = 2k - 1), +k (b = 2k), |l_x| <= xw; ntk[k] of the
+// unit's terms reach |l_x| = k.  The host fills the topology part, the device
+// the f nodes (k_pencil_units).  The pencil path takes the terms whose band
+// width at the depth is at most kPencilMaxW (then every |l_d| <= that); the
+// wider terms stay with the item kernel: at |l| >= 2 they have 1 or 2 terms
+// per pencil, and a tensor-core product of N <= 48 costs as much as one of
+// N = 128.
+constexpr int kPencilMaxW = 1;
+constexpr int kPencilMaxL = kPencilMaxW;
+constexpr int kPencilSlots = 2 * kPencilMaxL + 1;
+struct PencilUnit {
+    long long form[kPencilSlots];   // float offsets of the stacked x-step forms of the slots
+    int fid[kPencilSlots];          // f nodes of the slots (-1: none, outside the world or zero norm)
+    int task;                       // partial slot of the task (work entry, l_z)
+    int wi;                         // work entry of g
+    int flags;                      // bit b: fid[b] is a GenNode
+    short depth, q, nt, xw;         // q: term row of the group's first term at the depth
+    short ntk[kPencilMaxL + 1];     // terms reaching |l_x| = k
+    short nform[kPencilSlots];      // terms of each slot's stacked form (its layout)
+    short wt0, wt1;                 // terms whose products tile 0 / tile 1 of D hold
+    short pflags;                   // bit 0: first group of its pencil, bit 1: last (a pencil's groups are consecutive)
+    signed char ly, lz;
+};
+
 // kernel launchers (k_apply.cu / k_tree.cu)
 void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, const DevTree &g, const int *work, int n_work,
                          NodeKey *pkeys, int *pvals, int phcap, NodeKey *plist, int *pcount, int pcap, int *err, cudaStream_t s);
@@ -244,8 +275,10 @@ void launch_chunk_fill(const long long *g_off, const long long *c_off, int n_wor
 void launch_items(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                   const int4 *chunks, int n_chunks, const WorkItem *items, double *partial, int *err, const int *n_chunks_dev, int *counter,
                   int *tc_counter, cudaStream_t s);
+// pen_begin / pen_partial: task sums of the pencil contraction per work entry (optional)
 void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tree, const int *work, int n_work, const int *chunk_begin,
-                          const double *partial, cudaStream_t s, const int *nw_dev = nullptr);
+                          const double *partial, cudaStream_t s, const int *nw_dev = nullptr, const int *pen_begin = nullptr,
+                          const double *pen_partial = nullptr);
 // CTAs of the contraction kernel of order K resident on one SM (0 if unknown)
 int contract_items_resident(int K);
 long long scan_blocks(long long n);
@@ -317,6 +350,27 @@ void launch_chunk_types(int4 *chunks, int n_chunks, const int *n_chunks_dev, con
 void launch_contract_tc(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                         const int4 *chunks, int n_chunks, const int *n_chunks_dev, const WorkItem *items, double *partial, int *err,
                         int *counter, cudaStream_t s);
+
+// pencil contraction (k_pencil.cu)
+constexpr int kPencilGroup = 5;   // operator terms per tensor-core product (24 columns each)
+bool pencil_supported(int K);
+// stacked form jobs; forms get 128 pad16(24 nt) bytes each
+struct PencilFormJob {
+    int depth, q, lx, nt;   // q: term row of the group's first term
+    long long off;
+};
+void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *forms, cudaStream_t s);
+void launch_pencil_units(const DevMRA &m, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, void *units, int n_units,
+                         int *err, cudaStream_t s);
+// per work entry the number of its items whose term is wider than kPencilMaxW
+// at the entry's depth (those the item kernel keeps), and their compaction
+void launch_keep_items(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
+                       int n_work, const WorkItem *in, int *keep, cudaStream_t s, const int *nw_dev = nullptr);
+void launch_keep_fill(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
+                      const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, const int *nw_dev = nullptr);
+// persistent; counter: a device int (zeroed here); pen_partial: 8 K^3 doubles per task
+void launch_pencil(const DevOper &op, const DevTree *fs, const int *work_tree, const void *units, const int *task_unit, int n_tasks,
+                   double *pen_partial, int *err, int *counter, cudaStream_t s);
 
 // judged adaptive apply (k_judged.cu)
 void launch_keep_counts(const int *flags, int begin, int n, int *cnt, cudaStream_t s);
