@@ -28,10 +28,13 @@
 // legacy mma.sync shares the same tensor pipe).  The 24 columns of a term are
 // its x-step outputs a0 = 0 from b0 = 1 (C block), a0 = 1 (B, A blocks) and
 // a0 = 0 from b0 = 0 (T block), so that the s->s path can be split off (U
-// channel below).  Per term the consumers then apply the y and z steps in FP32
-// (CUDA-core FMA pipe, which runs beside the tensor pipe):
-//     Y[x][y_out][z]  = sum_{y_in} O^y[y_out][y_in] S1[x][y_in][z]
-//     G[x][y][z_out] += sum_{z_in} O^z[z_out][z_in] Y[x][y][z_in]
+// channel below).  Per term the consumers then apply the y and z steps with
+// warp-level tensor-core products (mma.sync m16n8k8, TF32 hi / lo, 3 products):
+//     Y^T[y_out][(x, z)] = O^y[y_out][y_in] S1^T[y_in][(x, z)]
+//     G[(x, y)][z_out]  += Y[(x, y)][z_in] O^z[z_out][z_in]^T
+// the accumulator fragments of the first product are the A fragments of the
+// second (the k index of the z step is permuted to match, and so are the O^z
+// fragments), so Y never leaves the registers.
 // Below the roots the T-block part of S1 on the (b1, b2) = (0, 0) rows is the
 // U channel: it goes through y with the B block (a1 = 1) into Y and with the T
 // block into P, and P goes through z with the B block only (a2 = 1), which
@@ -41,12 +44,13 @@
 // mbarrier-tracked slots (a pencil's f nodes once for all its term groups,
 // stacked operator forms, per-term operator blocks); warp 1 lane 0 issues the
 // tensor-core products and commits into one of two TMEM buffers, so that the
-// products of the next unit overlap the consumers; warps 2-9 (consumers) read
-// TMEM, transpose through shared memory, run the y / z steps and keep the g
-// accumulators (FP32 sums per unit, compensated sums over the units) of the
-// task.  A task is (g, l_z): its pencils x their term groups ("units", made by
-// the host and k_pencil_units); its 8 (k+1)^3 sums go to pen_partial[slot] in
-// FP64, and the chunk reduction adds the tasks of g after its chunk partials.
+// products of the next unit overlap the consumers; warps 2-9 (consumers; warp
+// 2 + w owns x = 2 w, 2 w + 1) read TMEM, transpose S1 through shared memory,
+// run the y / z steps and keep the g accumulators (FP32 sums per unit,
+// compensated sums over the units) of the task.  A task is (g, l_z): its
+// pencils x their term groups ("units", made by the host and
+// k_pencil_units); its 8 (k+1)^3 sums go to pen_partial[slot] in FP64, and the
+// chunk reduction adds the tasks of g after its chunk partials.
 //
 // Every wait is bounded (about a second of cycles); on expiry a thread sets
 // DE_TIMEOUT, its role stops, the others then time out too, and the CTA
@@ -66,20 +70,17 @@ constexpr int FREC = kTcNodeFloats * 4;    // bytes of a staged real node (hi 16
 constexpr int GREC = 8192;                 // bytes of a staged GenNode (hi 4 KB, lo 4 KB; rows 64-127 zero)
 constexpr int BREC = 128 * NMAX;           // bytes of a stacked form (hi s0, hi s1, lo s0, lo s1)
 constexpr int OREC = GT * 2 * 256 * 4;     // bytes of the per-term operator blocks of a unit (O^y, O^z)
-// S1 staging: S1[x][y][z] at x XS + y YS + z; U[x][y][z] at x US + y UYS + z
-// (strides chosen so that the drain stores and the float4 loads avoid bank conflicts)
-constexpr int YS = 20, XS = 336, UYS = 12, US = 112;
+// S1 staging (double-buffered by term): S1[x][y][z] at x XS + y YS + z, U[x][y][z] at
+// x US + y UYS + z (strides chosen so that the fragment loads avoid bank conflicts)
+constexpr int YS = 24, XS = 16 * YS, UYS = 8, US = 64;
 constexpr int S1_FLOATS = 16 * XS + 8 * US;
-// Y / P exchange (per consumer warp): Y[xl][y][z] at xl 336 + y 20 + z, P[xl][y][z] at xl 112 + y 12 + z
-constexpr int YW = 2 * 336, PW = 2 * 112;
 // shared memory map (bytes)
 constexpr int SM_F = 0;                              // NFS real-node slots
 constexpr int SM_G = SM_F + NFS * FREC;              // NFS GenNode slots (a slot's node is real or generated)
 constexpr int SM_B = SM_G + NFS * GREC;              // 2 form slots
 constexpr int SM_O = SM_B + 2 * BREC;                // 2 operator-block slots
 constexpr int SM_S1 = SM_O + 2 * OREC;               // S1 staging
-constexpr int SM_Y = SM_S1 + 4 * S1_FLOATS;          // Y / P exchange
-constexpr int SM_BYTES = SM_Y + 4 * NCW * (YW + PW);
+constexpr int SM_BYTES = SM_S1 + 2 * 4 * S1_FLOATS;
 static_assert(SM_BYTES + 1024 <= 227 * 1024, "pencil kernel shared memory");
 static_assert(SM_F % 1024 == 0 && SM_G % 1024 == 0 && SM_B % 1024 == 0 && SM_O % 16 == 0 && SM_S1 % 16 == 0, "alignment");
 constexpr int TM_COLS = 512;                         // D buffer db at column 256 db, tile t at + 128 t
@@ -161,6 +162,19 @@ __device__ __forceinline__ void split(float x, float &hi, float &lo) {
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
     hi = __uint_as_float(h);
     lo = x - hi;
+}
+
+__device__ __forceinline__ void mma16(float (&d)[4], const float (&a)[4], const float (&b)[2]) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(__float_as_uint(a[0])), "r"(__float_as_uint(a[1])), "r"(__float_as_uint(a[2])), "r"(__float_as_uint(a[3])),
+                   "r"(__float_as_uint(b[0])), "r"(__float_as_uint(b[1])));
+}
+// d += a b in FP32 accuracy from TF32 operands: lo.hi + hi.lo + hi.hi
+__device__ __forceinline__ void mma3x(float (&d)[4], const float (&ah)[4], const float (&al)[4], const float (&bh)[2], const float (&bl)[2]) {
+    mma16(d, al, bh);
+    mma16(d, ah, bl);
+    mma16(d, ah, bh);
 }
 
 // padded N of a tensor-core product with n terms (M = 128 needs N % 16 == 0)
@@ -309,14 +323,10 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
         if (!lbad) atomicOr(err, DE_TIMEOUT);
         lbad = true;
     };
-    const int cw = warp - 2;                       // consumer index 0..7 (x pair 2 cw, 2 cw + 1)
-    float *S1s = reinterpret_cast<float *>(sm + SM_S1);
-    float *Us = S1s + 16 * XS;
-    float *Yw = reinterpret_cast<float *>(sm + SM_Y) + (cw >= 0 ? cw : 0) * (YW + PW);
-    float *Pw = Yw + YW;
-    const int xl = lane >> 4;                      // which of the two x of this warp
-    const int xo = 2 * (cw >= 0 ? cw : 0) + xl;    // x of this lane
-    const int yq = (lane >> 2) & 3, zq = lane & 3; // lane tile: y 4 yq .. +3, z 4 zq .. +3
+    // consumer warp cw owns x = 2 cw, 2 cw + 1; fragment coordinates g (group), tq (thread in group)
+    const int cw = warp >= 2 ? warp - 2 : 0;
+    const int x0 = 2 * cw, fg = lane >> 2, tq = lane & 3;
+    float *S1base = reinterpret_cast<float *>(sm + SM_S1);
     float G[16], Gc[16];
 
     for (;;) {
@@ -449,9 +459,7 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
             const int r = 32 * quarter + lane;              // D row of this thread: b1 64 + q1 + 8 q2
             const int b1 = r >> 6, q1 = r & 7, q2 = (r >> 3) & 7;
             const int yrow = 8 * b1 + q1;
-            const int a1 = yq >> 1, ph1 = yq & 1;           // y_out = 8 a1 + 4 ph1 + (0..3)
-            const int a2 = zq >> 1, ph2 = zq & 1;           // z_out = 8 a2 + 4 ph2 + (0..3)
-            const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            unsigned nterm = 0;   // terms drained (S1 buffer parity)
             for (int u = u0; u < u1; u++) {
                 const Unit &U = units[u];
                 const bool pure = U.depth > 0;   // the s->s path is left out below the roots
@@ -464,10 +472,12 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                 const float *OB = reinterpret_cast<const float *>(sm + SM_O + so * OREC);
                 const int nw = U.wt0;
                 const int ly = U.ly, lz = U.lz;
-                float Gu[16];
+                float Gu[16];   // [xi][a2][v]: unit sums of the z-step fragments
 #pragma unroll
                 for (int i = 0; i < 16; i++) Gu[i] = 0.f;
-                for (int j = 0; j < nw && ok; j++) {
+                for (int j = 0; j < nw && ok; j++, nterm++) {
+                    float *S1s = S1base + (nterm & 1) * S1_FLOATS;
+                    float *Us = S1s + 16 * XS;
                     // ---- drain S1 of term j (both z halves) into shared memory ----
                     const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
                     for (int t = 0; t < 2; t++) {
@@ -487,10 +497,10 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                         const bool u_row = pure && t == 0 && b1 == 0;
 #pragma unroll
                         for (int i = 0; i < 4; i++) {
-                            const int x0 = 4 * half + i;     // a0 = 0
-                            S1s[x0 * XS + yrow * YS + z] = u_row ? cC[i] : cC[i] + cT[i];
-                            S1s[(8 + x0) * XS + yrow * YS + z] = cA[i];
-                            if (u_row) Us[x0 * US + q1 * UYS + q2] = cT[i];
+                            const int xa = 4 * half + i;     // a0 = 0
+                            S1s[xa * XS + yrow * YS + z] = u_row ? cC[i] : cC[i] + cT[i];
+                            S1s[(8 + xa) * XS + yrow * YS + z] = cA[i];
+                            if (u_row) Us[xa * US + q1 * UYS + q2] = cT[i];
                         }
                     }
                     consumers_sync();
@@ -501,119 +511,94 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                         vy |= (abs(ly) <= row.wd[c] ? 1u : 0u) << c;
                         vz |= (abs(lz) <= row.wd[c] ? 1u : 0u) << c;
                     }
-                    const float4 *Oy4 = reinterpret_cast<const float4 *>(OB + j * 512);
-                    const float4 *Oz4 = Oy4 + 64;
-                    // ---- y step: Y[x][y_out][z] (lane tile y 4 yq.., z 4 zq..), P (U channel) ----
-                    float Y[4][4], P[4][4];
+                    const float *Oy = OB + j * 512, *Oz = Oy + 256;
+                    // O^y A fragments per k step s = b1 (block of row half a1: idx 2 a1 + s):
+                    // O^y[y_out = (a1, p1)][y_in = (s, q1)] = blocks32[idx 64 + 8 q1 + p1]
+                    float yah[2][4], yal[2][4];
 #pragma unroll
-                    for (int a = 0; a < 4; a++)
+                    for (int s = 0; s < 2; s++) {
+                        const bool v0 = (vy >> s) & 1u, v1 = (vy >> (2 + s)) & 1u;
+                        const float e[4] = {v0 ? Oy[s * 64 + 8 * tq + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * tq + fg] : 0.f,
+                                            v0 ? Oy[s * 64 + 8 * (tq + 4) + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * (tq + 4) + fg] : 0.f};
 #pragma unroll
-                        for (int c = 0; c < 4; c++) Y[a][c] = P[a][c] = 0.f;
-                    const float4 *S14 = reinterpret_cast<const float4 *>(S1s + xo * XS) + zq;
-#pragma unroll
-                    for (int bb = 0; bb < 2; bb++) {
-                        const int idx = 2 * a1 + bb;
-                        const bool v = (vy >> idx) & 1u;
-#pragma unroll 4
-                        for (int qq = 0; qq < 8; qq++) {
-                            // O^y[y_out][y_in] = block_idx(in q1 -> out p1) = blocks32[idx 64 + 8 q1 + p1]
-                            const float4 w = v ? Oy4[idx * 16 + 2 * qq + ph1] : zero4;
-                            const float4 sv = S14[(8 * bb + qq) * (YS / 4)];
-                            const float wv[4] = {w.x, w.y, w.z, w.w}, s4[4] = {sv.x, sv.y, sv.z, sv.w};
-#pragma unroll
-                            for (int a = 0; a < 4; a++)
-#pragma unroll
-                                for (int c = 0; c < 4; c++) Y[a][c] = fmaf(wv[a], s4[c], Y[a][c]);
-                        }
+                        for (int q = 0; q < 4; q++) split(e[q], yah[s][q], yal[s][q]);
                     }
-                    // U channel: rows x < 8 (a0 = 0), z < 8 (b2 = 0), y_in < 8 (b1 = 0):
-                    // T (a1 = 0) into P, B (a1 = 1) into Y
-                    const bool uch = pure && xo < 8 && zq < 2;
-                    if (uch) {
-                        const int idx = 2 * a1;
-                        const bool v = (vy >> idx) & 1u;
-                        const float4 *U4 = reinterpret_cast<const float4 *>(Us + xo * US) + zq;
-#pragma unroll 4
-                        for (int k = 0; k < 8; k++) {
-                            const float4 w = v ? Oy4[idx * 16 + 2 * k + ph1] : zero4;
-                            const float4 sv = U4[k * (UYS / 4)];
-                            const float wv[4] = {w.x, w.y, w.z, w.w}, s4[4] = {sv.x, sv.y, sv.z, sv.w};
-                            if (a1 == 1) {
+                    // O^z B fragments per (a2, s = b2), k permuted: row k = tq <-> z_in = 8 s + 2 tq,
+                    // row tq + 4 <-> 8 s + 2 tq + 1; O^z[z_out][z_in] = blocks32[idx 64 + 8 (z_in % 8) + z_out % 8]
+                    float zbh[2][2][2], zbl[2][2][2];
 #pragma unroll
-                                for (int a = 0; a < 4; a++)
+                    for (int a2 = 0; a2 < 2; a2++)
 #pragma unroll
-                                    for (int c = 0; c < 4; c++) Y[a][c] = fmaf(wv[a], s4[c], Y[a][c]);
-                            } else {
+                        for (int s = 0; s < 2; s++) {
+                            const int idx = 2 * a2 + s;
+                            const bool v = (vz >> idx) & 1u;
+                            split(v ? Oz[idx * 64 + 8 * (2 * tq) + fg] : 0.f, zbh[a2][s][0], zbl[a2][s][0]);
+                            split(v ? Oz[idx * 64 + 8 * (2 * tq + 1) + fg] : 0.f, zbh[a2][s][1], zbl[a2][s][1]);
+                        }
+                    const bool ys0 = (vy & 5u) != 0, ys1 = (vy & 10u) != 0;   // k step s has a block that takes part
+                    // ---- y step: C[xi][zb] = Y^T fragment (rows y_out g, g + 8; columns z = 8 zb + 2 tq, +1) ----
+                    float C[2][2][4], P[2][2];
 #pragma unroll
-                                for (int a = 0; a < 4; a++)
+                    for (int xi = 0; xi < 2; xi++) {
+                        const int x = x0 + xi;
 #pragma unroll
-                                    for (int c = 0; c < 4; c++) P[a][c] = fmaf(wv[a], s4[c], P[a][c]);
+                        for (int zb = 0; zb < 2; zb++) {
+#pragma unroll
+                            for (int v = 0; v < 4; v++) C[xi][zb][v] = 0.f;
+#pragma unroll
+                            for (int s = 0; s < 2; s++) {
+                                if (!(s == 0 ? ys0 : ys1)) continue;
+                                // B = S1^T: rows k = y_in = 8 s + tq (+4), column n = z = 8 zb + g
+                                float bh[2], bl[2];
+                                split(S1s[x * XS + (8 * s + tq) * YS + 8 * zb + fg], bh[0], bl[0]);
+                                split(S1s[x * XS + (8 * s + tq + 4) * YS + 8 * zb + fg], bh[1], bl[1]);
+                                mma3x(C[xi][zb], yah[s], yal[s], bh, bl);
                             }
                         }
-                    }
-                    // the S1 staging may be overwritten once every consumer has read it
-                    consumers_sync();
-                    // ---- exchange: Y rows (and P) to the lanes of the z step ----
-#pragma unroll
-                    for (int a = 0; a < 4; a++)
-                        *reinterpret_cast<float4 *>(Yw + xl * 336 + (4 * yq + a) * 20 + 4 * zq) = make_float4(Y[a][0], Y[a][1], Y[a][2], Y[a][3]);
-                    if (uch && a1 == 0)
-#pragma unroll
-                        for (int a = 0; a < 4; a++)
-                            *reinterpret_cast<float4 *>(Pw + xl * 112 + (4 * yq + a) * 12 + 4 * zq) = make_float4(P[a][0], P[a][1], P[a][2], P[a][3]);
-                    __syncwarp();
-                    // ---- z step into the unit sums: lane tile y 4 yq .., z_out 4 zq .. ----
-#pragma unroll
-                    for (int bb = 0; bb < 2; bb++) {
-                        const int idx = 2 * a2 + bb;
-                        const bool v = (vz >> idx) & 1u;
-#pragma unroll
-                        for (int q4 = 0; q4 < 8; q4 += 4) {
-                            float yv[4][4];
-#pragma unroll
-                            for (int a = 0; a < 4; a++) {
-                                const float4 t4 = *reinterpret_cast<const float4 *>(Yw + xl * 336 + (4 * yq + a) * 20 + 8 * bb + q4);
-                                yv[a][0] = t4.x;
-                                yv[a][1] = t4.y;
-                                yv[a][2] = t4.z;
-                                yv[a][3] = t4.w;
-                            }
-#pragma unroll
-                            for (int kk = 0; kk < 4; kk++) {
-                                const float4 w = v ? Oz4[idx * 16 + 2 * (q4 + kk) + ph2] : zero4;
-                                const float wv[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-                                for (int a = 0; a < 4; a++)
-#pragma unroll
-                                    for (int c = 0; c < 4; c++) Gu[4 * a + c] = fmaf(yv[a][kk], wv[c], Gu[4 * a + c]);
-                            }
+                        P[xi][0] = P[xi][1] = 0.f;
+                        // U channel (x < 8, z < 8, y_in < 8): O^y's k step 0 applied to U; the a1 = 0 rows
+                        // (T block) are P, the a1 = 1 rows (B block) join Y
+                        if (pure && x < 8 && (vy & 5u)) {
+                            float bh[2], bl[2], cu[4] = {0.f, 0.f, 0.f, 0.f};
+                            split(Us[x * US + tq * UYS + fg], bh[0], bl[0]);
+                            split(Us[x * US + (tq + 4) * UYS + fg], bh[1], bl[1]);
+                            mma3x(cu, yah[0], yal[0], bh, bl);
+                            P[xi][0] = cu[0];
+                            P[xi][1] = cu[1];
+                            C[xi][0][2] += cu[2];
+                            C[xi][0][3] += cu[3];
                         }
                     }
-                    // P through z with the B block only (a2 = 1 from b2 = 0): the T.T.T path is left out
-                    if (pure && xo < 8 && yq < 2 && a2 == 1 && ((vz >> 2) & 1u)) {
+                    // ---- z step: the y-step fragments are the A fragments (k' = tq <-> z = 8 s + 2 tq) ----
 #pragma unroll
-                        for (int q4 = 0; q4 < 8; q4 += 4) {
-                            float pv[4][4];
+                    for (int xi = 0; xi < 2; xi++) {
+                        const int x = x0 + xi;
 #pragma unroll
-                            for (int a = 0; a < 4; a++) {
-                                const float4 t4 = *reinterpret_cast<const float4 *>(Pw + xl * 112 + (4 * yq + a) * 12 + q4);
-                                pv[a][0] = t4.x;
-                                pv[a][1] = t4.y;
-                                pv[a][2] = t4.z;
-                                pv[a][3] = t4.w;
+                        for (int a2 = 0; a2 < 2; a2++) {
+                            float Z[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                            for (int s = 0; s < 2; s++) {
+                                if (!((vz >> (2 * a2 + s)) & 1u)) continue;
+                                float ah[4], al[4];
+                                split(C[xi][s][0], ah[0], al[0]);
+                                split(C[xi][s][2], ah[1], al[1]);
+                                split(C[xi][s][1], ah[2], al[2]);
+                                split(C[xi][s][3], ah[3], al[3]);
+                                mma3x(Z, ah, al, zbh[a2][s], zbl[a2][s]);
+                            }
+                            // P through z with the B block only (a2 = 1 from b2 = 0): the T.T.T path is left out
+                            if (a2 == 1 && pure && x < 8 && (vy & 1u) && ((vz >> 2) & 1u)) {
+                                float ah[4], al[4];
+                                split(P[xi][0], ah[0], al[0]);
+                                ah[1] = al[1] = 0.f;
+                                split(P[xi][1], ah[2], al[2]);
+                                ah[3] = al[3] = 0.f;
+                                mma3x(Z, ah, al, zbh[1][0], zbl[1][0]);
                             }
 #pragma unroll
-                            for (int kk = 0; kk < 4; kk++) {
-                                const float4 w = Oz4[2 * 16 + 2 * (q4 + kk) + ph2];
-                                const float wv[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-                                for (int a = 0; a < 4; a++)
-#pragma unroll
-                                    for (int c = 0; c < 4; c++) Gu[4 * a + c] = fmaf(pv[a][kk], wv[c], Gu[4 * a + c]);
-                            }
+                            for (int v = 0; v < 4; v++) Gu[8 * xi + 4 * a2 + v] += Z[v];
                         }
                     }
-                    __syncwarp();
                 }
                 // compensated sums over the units
 #pragma unroll
@@ -632,18 +617,16 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                 }
                 nu++;
             }
-            // the task's sums (slot of its units; every task has one): g component
+            // the task's sums (slot of its units; every task has one): fragment v of
+            // (x, a2): y_out = fg + 8 (v >> 1), z_out = 8 a2 + 2 tq + (v & 1); g component
             // gt = a0 + 2 a1 + 4 a2, element p0 + 8 p1 + 64 p2
             double *go = pen_partial + (size_t)units[u0].task * 4096;
-            const int a0 = xo >> 3, p0 = xo & 7;
 #pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const int yo = 4 * yq + a, zo = 4 * zq + c;
-                    const int gt = a0 + 2 * (yo >> 3) + 4 * (zo >> 3);
-                    go[gt * 512 + p0 + 8 * (yo & 7) + 64 * (zo & 7)] = (double)G[4 * a + c] - (double)Gc[4 * a + c];
-                }
+            for (int e = 0; e < 16; e++) {
+                const int xi = e >> 3, a2 = (e >> 2) & 1, v = e & 3;
+                const int x = x0 + xi, a0 = x >> 3, p0 = x & 7, a1 = v >> 1, p1 = fg, p2 = 2 * tq + (v & 1);
+                go[(a0 + 2 * a1 + 4 * a2) * 512 + p0 + 8 * p1 + 64 * p2] = (double)G[e] - (double)Gc[e];
+            }
         }
         // the producer / MMA lanes other than 0 did not walk the units: bring their counters along
         if (warp <= 1) {
