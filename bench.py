@@ -25,10 +25,17 @@ screening rules); the count is an integer that equals the oracle's.
   fp64       the plain FP64 form on the same workload
   roofline   the contraction kernel: algorithmic FLOP (96 (k+1)^4 per node-term)
              per launch / kernel time, against the measured bf16 dense peak
-  cpu_baseline  the CPU oracle (port of the reference path) on a bounded sample
+  cpu_baseline  the CPU oracle (port of the reference path) on the whole fixed
+             grid, repeated for about 10 s of CPU work (at most 3 passes);
+             the same leg gives error_vs_oracle (the GPU results against the
+             oracle's coefficients on the same grid)
+  error_vs_potential  the mixed result against the closed-form potential of
+             the Gaussian sum at seeded points
 
 --impl reference times the CPU oracle (the reference itself needs Eigen and
-cannot be built here) with all host threads on the same workload.
+cannot be built here) with all host threads on the same workload.  Its inputs
+(MRA, operator node caches, projected input) are written by a child process;
+the timing process itself loads only the oracle library.
 """
 import argparse
 import json
@@ -68,6 +75,7 @@ def parse():
     p.add_argument("--batch-n", type=int, default=64, help="functions in the batch workload")
     p.add_argument("--learned-n", type=int, default=20, help="held-out densities in the learned-grid workload")
     p.add_argument("--fp64-sample", type=int, default=8, help="batch workload: separate FP64 applies timed (every n/s-th function)")
+    p.add_argument("--write-inputs", default=None, help=argparse.SUPPRESS)
     a = p.parse_args()
     global PREC, NGAUSS, WORKLOAD, ORDER, EXP_RANGE, CENTRE_RANGE, MU, METRIC
     if a.workload == "helmholtz":
@@ -211,35 +219,80 @@ def cpu_oracle_rate(mra, P, f, grid, sample, threads, prepared=None):
     return prepared.node_terms / dt, dt, prepared.node_terms, prepared
 
 
+def write_inputs(path):
+    """The workload's MRA, operator node caches, projected input and root
+    topology as plain arrays (run in a child process of the reference arm)."""
+    import mrcpp_gb300 as mw
+
+    mra, P, f = make_input()
+    d = mra.desc()
+    ex = P.export()
+    fx = f.export()
+    roots = mw.FunctionTree(mra).export()
+    np.savez(path, order=d.order, root_scale=d.root_scale, max_scale=d.max_scale, sf=d.sf, corner=np.array([d.corner[i] for i in range(3)]),
+             nbox=np.array([d.nbox[i] for i in range(3)]), filters=mra._filters, n_terms=P.n_terms, build_prec=float(P.prec),
+             depth=ex["depth"], max_transl=ex["max_transl"], blocks=ex["blocks"], norms=ex["norms"], f_idx=fx["idx"], f_child0=fx["child0"],
+             f_coefs=fx["coefs"], f_norms=fx["norms"], r_idx=roots["idx"], r_child0=roots["child0"])
+
+
 def run_reference(args, rank, world, pg):
     if rank != 0:
         return
-    import mrcpp_gb300 as mw
+    import tempfile
+
     import oracle
 
     threads = os.cpu_count() or 1
-    mra, P, f = make_input()
-    grid = oracle.to_tree(oracle.apply(PREC, mw.FunctionTree(mra), P, f, nthreads=threads, count_terms=False), mra)
-    sample = 1  # the whole fixed grid per step (about 4-5 s on 16 cores)
-    prep = None
+    # inputs from a child process (the product's host mirror projects the
+    # input and builds the operator); this process loads only the oracle
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "inputs.npz")
+        cmd = [sys.executable, os.path.abspath(__file__), "--write-inputs", path, "--workload", args.workload] + (["--small"] if args.small else [])
+        subprocess.run(cmd, check=True)
+        z = dict(np.load(path))
+    mra = {k: z[k] for k in ("order", "root_scale", "max_scale", "sf", "corner", "nbox", "filters")}
+    op = {k: z[k] for k in ("n_terms", "build_prec", "depth", "max_transl", "blocks", "norms")}
+    inp = {"idx": z["f_idx"], "child0": z["f_child0"], "coefs": z["f_coefs"], "norms": z["f_norms"]}
+    adaptive = oracle.Prepared.from_arrays(PREC, mra, op, inp, {"idx": z["r_idx"], "child0": z["r_child0"]}, -1.0, -1).run(threads, False)
+    grid = {"idx": adaptive["idx"], "child0": adaptive["child0"]}
+    prep = oracle.Prepared.from_arrays(PREC, mra, op, inp, grid, -1.0, 0)
+    nt = prep.run(threads, count_terms=True, export=False)["node_terms"]
     for _ in range(args.warmup):
-        _, _, _, prep = cpu_oracle_rate(mra, P, f, grid, sample, threads, prep)
-    rates, times, nts = [], [], []
+        prep.run(threads, count_terms=False, export=False, fast=True)
+    times = []
     for _ in range(args.steps):
-        r, dt, nt, prep = cpu_oracle_rate(mra, P, f, grid, sample, threads, prep)
-        rates.append(r)
-        times.append(dt)
-        nts.append(nt)
-    value = sum(nts) / sum(times)
-    desc = "the whole %d-node fixed grid per step (%d node-terms per step)" % (grid.n_nodes, nts[0])
+        t0 = time.perf_counter()
+        prep.run(threads, count_terms=False, export=False, fast=True)
+        times.append(time.perf_counter() - t0)
+    value = nt * len(times) / sum(times)
+    desc = "the whole %d-node fixed grid per step (%d node-terms per step)" % (len(grid["child0"]), nt)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "out_nodes": grid.n_nodes, "sample": desc},
+            "config": {"workload": WORKLOAD, "out_nodes": len(grid["child0"]), "sample": desc},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": desc + "; CPU oracle restating ConvolutionCalculator (reference needs Eigen 3.4, absent)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def closed_form(gs, x):
+    """Potential of the Gaussian sum sum c exp(-a |r - R|^2) at x: Coulomb
+    (erf) for Poisson, Yukawa for Helmholtz with mu = MU."""
+    import math
+
+    v = 0.0
+    for c, a, R in gs:
+        r = float(np.linalg.norm(x - np.asarray(R)))
+        pre = c * (math.pi / a) ** 1.5
+        if MU is None:
+            v += pre * (math.erf(math.sqrt(a) * r) / r if r > 1e-12 else 2.0 * math.sqrt(a / math.pi))
+        else:
+            sb = math.sqrt(a)
+            al = MU / (2.0 * sb)
+            v += pre * math.exp(MU * MU / (4.0 * a)) / (2.0 * r) * (math.exp(-MU * r) * math.erfc(al - sb * r) -
+                                                                       math.exp(MU * r) * math.erfc(al + sb * r))
+    return v
 
 
 def split_bound(achieved, bf16_peak):
@@ -523,6 +576,9 @@ def main_learned(args, rank, world, local, pg):
 
 def main():
     args = parse()
+    if args.write_inputs:
+        write_inputs(args.write_inputs)
+        return
     rank, world, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world, pg)
@@ -650,14 +706,28 @@ def main():
         ck(L.mwgpu_launch_count(ctx, C.byref(l1)))
         pst = mw.MwgpuLevelStats()
         ck(L.mwgpu_plan_check(ctx, plan, C.byref(pst)))
+        pnt, pms = C.c_ulonglong(), C.c_double()
+        ck(L.mwgpu_plan_pencil_info(plan, C.byref(pnt), C.byref(pms)))
         out = np.zeros((n_out, 8 * K ** 3))
         ck(L.mwgpu_download_tree(ctx, dout, mw._pd(out), None))
         ck(L.mwgpu_plan_destroy(ctx, plan))
         barrier(pg)
-        return ms, pst, cs.summary(), (l1.value - l0.value), out
+        return ms, pst, cs.summary(), (l1.value - l0.value), out, (pnt.value, pms.value)
 
-    ms_plan, st_plan, clk_plan, launches_plan, out_plan = plan_timed(mw.MIXED)
-    ms_plan64, st_plan64, _, _, out_plan64 = plan_timed(mw.FP64)
+    ms_plan, st_plan, clk_plan, launches_plan, out_plan, pencil = plan_timed(mw.MIXED)
+    ms_plan64, st_plan64, _, _, out_plan64, _ = plan_timed(mw.FP64)
+    # the mixed result against the closed-form potential at seeded points
+    from cases import gaussian_sum
+
+    gs = gaussian_sum(SEED, NGAUSS, EXP_RANGE, CENTRE_RANGE)
+    tmix = mw.FunctionTree(mra)
+    tmix.load_flat(gx["idx"], gx["child0"], out_plan)
+    cr = CENTRE_RANGE[1] + 2.0
+    xs = np.random.default_rng(7).uniform(-cr, cr, (200, 3))
+    va = np.array([closed_form(gs, x) for x in xs])
+    vg = np.array([tmix.evalf(x) for x in xs])
+    pot_err = {"rel_l2": float(np.linalg.norm(vg - va) / np.linalg.norm(va)), "points": len(xs), "box": [-cr, cr],
+               "potential": "sum of c (pi/a)^1.5 erf(sqrt(a) r)/r" if MU is None else "Yukawa potential of each Gaussian (mu = %g)" % MU}
     plan_l2 = float(np.linalg.norm(out_plan - out_plan64) / np.linalg.norm(out_plan64))
     plan_node_err = float((np.linalg.norm(out_plan - out_plan64, axis=1) / np.linalg.norm(out_plan64, axis=1).max()).max())
 
@@ -688,20 +758,28 @@ def main():
     t_e2e = reduce_max(pg, statistics.mean(e2e_times))
     e2e_value = total_nt / t_e2e
 
-    # roofline of the contraction kernel (mixed form, last timed launch)
+    # roofline of the dominant kernel (mixed form, last timed plan execution):
+    # the pencil contraction where the level uses it (order 7), else the item kernel
     bf16_peak, hbm_peak, peak_kind = load_peaks()
-    achieved = node_terms * flop_per_nt / (st_plan.contract_ms / 1e3) / 1e12
     tr = load_traffic() if (args.workload == "poisson" and not args.small) else None
+    contraction = {"ms": st_plan.contract_ms, "node_terms": int(node_terms),
+                   "tflops": node_terms * flop_per_nt / (st_plan.contract_ms / 1e3) / 1e12,
+                   "kernels": "chunk setup, k_contract_items (remaining items), k_pencil_units, k_pencil, k_reduce_chunks"}
+    if pencil[0] > 0 and pencil[1] > 0:
+        achieved = pencil[0] * flop_per_nt / (pencil[1] / 1e3) / 1e12
+        kname, kms, knt = "k_pencil (x step tcgen05 kind::tf32, 5 terms per product; y/z steps mma.sync TF32 hi/lo)", pencil[1], pencil[0]
+    else:
+        achieved = contraction["tflops"]
+        kname = "k_contract_items<%d> (mixed form, %s)" % (ORDER + 1, "TF32-split mma.sync" if ORDER == 7 else "FP32 FMA")
+        kms, knt = st_plan.contract_ms, int(node_terms)
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s", "frac": achieved / bf16_peak,
             "traffic": (tr or {}).get("dram_bytes_per_launch"), "peak_kind": peak_kind + " bf16 dense burst",
-            "kernel": ("k_contract_tc (mixed form, tcgen05, MWGPU_TC)" if (ORDER == 7 and os.environ.get("MWGPU_TC")) else
-                       "k_contract_items<%d> (mixed form, %s)" % (ORDER + 1, "TF32-split mma.sync" if ORDER == 7 else "FP32 FMA")),
-            "kernel_ms": st_plan.contract_ms, "kernel_ms_level_path": st_mixed.contract_ms,
-            "flop_per_node_term": flop_per_nt}
-    if ORDER == 7 and not os.environ.get("MWGPU_TC"):
+            "kernel": kname, "kernel_ms": kms, "kernel_node_terms": int(knt), "contraction": contraction,
+            "kernel_ms_level_path": st_mixed.contract_ms, "flop_per_node_term": flop_per_nt}
+    if ORDER == 7:
         roof["split_bound"] = split_bound(achieved, bf16_peak)
 
-    cpu = None
+    cpu, err_oracle = None, None
     if rank == 0 and not args.no_cpu_baseline:
         # the whole fixed grid, repeated until about 10 s of CPU work (at most 3 passes)
         threads = os.cpu_count() or 1
@@ -711,6 +789,17 @@ def main():
             tot_nt, tot_dt, reps = tot_nt + nt, tot_dt + dt, reps + 1
         cpu = {"value": tot_nt / tot_dt, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "the whole %d-node fixed grid, %d pass(es) (%d node-terms, %.1f s)" % (grid.n_nodes, reps, tot_nt, tot_dt)}
+        # the GPU results against the oracle's coefficients on the same grid
+        ref = prep.run(threads, count_terms=False, export=True)
+        key = {tuple(r): i for i, r in enumerate(ref["idx"].tolist())}
+        perm = np.array([key[tuple(r)] for r in gx["idx"].tolist()])
+        rc = ref["coefs"][perm]
+        err_oracle = {"mixed_rel_l2": float(np.linalg.norm(out_plan - rc) / np.linalg.norm(rc)),
+                      "mixed_max_rel": float(np.abs(out_plan - rc).max() / np.abs(rc).max()),
+                      "fp64_rel_l2": float(np.linalg.norm(out_plan64 - rc) / np.linalg.norm(rc)),
+                      "fp64_max_rel": float(np.abs(out_plan64 - rc).max() / np.abs(rc).max())}
+    else:
+        err_oracle = None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warm,
@@ -729,6 +818,7 @@ def main():
                 "level_path": {"value": value_level, "fp64_value": value_level64, "unit": UNIT, "ms_per_step": t_level,
                                "rel_l2_error": rel_l2, "max_node_error": node_err,
                                "note": "the host-driven mwgpu_apply_level + transforms (GenNodes dropped and rebuilt each step)"},
+                "error_vs_oracle": err_oracle, "error_vs_potential": pot_err,
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     barrier(pg)

@@ -248,6 +248,13 @@ mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *oper, int n_tre
                                mwgpu_plan **plan);
 mwgpu_status mwgpu_plan_execute(mwgpu_ctx *ctx, mwgpu_plan *plan, mwgpu_level_stats *stats);
 mwgpu_status mwgpu_plan_check(mwgpu_ctx *ctx, mwgpu_plan *plan, mwgpu_level_stats *stats);
+/* Pencil contraction of the last checked execution of a plan (mwgpu_plan_check):
+ * the node-terms it computed (those of the operator terms of band width <= 1,
+ * on levels without norm screening) and its device time in ms; 0 and 0 when the
+ * plan does not use it.  No reference counterpart (a measurement of the GPU
+ * schedule of calcNodeVector, ConvolutionCalculator.cpp:224-382). */
+mwgpu_status mwgpu_plan_pencil_info(const mwgpu_plan *plan, unsigned long long *node_terms, double *ms);
+
 /* Chunk length and persistent grid in use, the timed candidates (n_candidates:
  * in = room in the arrays, out = number tried) and kernel launches per execution. */
 mwgpu_status mwgpu_plan_info(const mwgpu_plan *plan, long long *chunk_items, int *grid, int *n_candidates, long long *cand_items,

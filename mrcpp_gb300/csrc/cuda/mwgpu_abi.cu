@@ -1721,7 +1721,7 @@ struct mwgpu_plan {
     double *d_partial = nullptr;
     LevelStats *d_stats = nullptr;
     int *d_err = nullptr;
-    unsigned long long *d_stamps = nullptr;  // level start, contraction start / end, level end (ns)
+    unsigned long long *d_stamps = nullptr;  // level start, contraction start / end, level end, pencil kernel start / end (ns)
     std::vector<NodeKey *> d_gkeys;
     std::vector<int> gcount;
     // mixed form: the GenNodes grouped by parent (keys, 8 slots per parent)
@@ -1738,6 +1738,18 @@ struct mwgpu_plan {
     unsigned long long launches_per_exec = 0;
     std::vector<double> tune_ms;  // per candidate, ms per million items
     std::vector<long long> tune_per;
+    // pencil contraction (unscreened order-7 levels): kept items of the item
+    // kernel (their offsets per entry), units and task sums
+    bool pencil = false;
+    int *d_keep = nullptr;
+    long long *d_keep_off = nullptr, *d_kscan = nullptr;
+    long long kscan_n = 0;
+    PencilUnit *d_units = nullptr;
+    int n_units = 0, n_tasks = 0;
+    int *d_task_unit = nullptr, *d_pen_begin = nullptr, *d_pen_counter = nullptr;
+    double *d_pen_partial = nullptr;
+    unsigned long long pen_node_terms = 0;   // last checked execution: node-terms of the pencil kernel
+    double pen_ms = 0.0;                     // and its device time
 };
 
 namespace {
@@ -1762,17 +1774,30 @@ void plan_free(mwgpu_plan *pl) {
 void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
     const mwgpu_oper *o = pl->o;
     cudaStream_t st = ctx->stream;
-    launch_chunk_count(pl->d_goff, pl->n, per, pl->d_ccount, st);
+    // with the pencil contraction the item kernel takes the compacted items of the wider terms
+    const long long *goff = pl->pencil ? pl->d_keep_off : pl->d_goff;
+    const WorkItem *items = pl->pencil ? pl->d_items_cm : pl->d_items;
+    launch_chunk_count(goff, pl->n, per, pl->d_ccount, st);
     launch_scan(pl->d_ccount, pl->d_coff, pl->n, pl->d_cscan, pl->d_cscan + (pl->cscan_n - 1), st);
-    launch_chunk_fill(pl->d_goff, pl->d_coff, pl->n, per, pl->d_chunks, pl->d_chunk_begin, pl->chunks_cap, pl->d_nchunks, pl->d_err, st);
+    launch_chunk_fill(goff, pl->d_coff, pl->n, per, pl->d_chunks, pl->d_chunk_begin, pl->chunks_cap, pl->d_nchunks, pl->d_err, st);
     cudaMemsetAsync(pl->d_counter, 0, sizeof(int), st);
     if (reduce) launch_stamp(pl->d_stamps + 1, st);
     else cudaEventRecord(pl->e1, st);
     bool tc_ok = true;
     for (int t = 0; t < pl->nt; t++) tc_ok = tc_ok && pl->inps[t]->t.tc32 != nullptr;
-    launch_items(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_chunks, pl->grid, pl->d_items, pl->d_partial, pl->d_err,
+    launch_items(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_chunks, pl->grid, items, pl->d_partial, pl->d_err,
                  pl->d_nchunks, pl->d_counter, tc_ok ? pl->d_counter + 1 : nullptr, st);
-    if (reduce) launch_reduce_chunks(o->mra, pl->d_gs, pl->d_wtree, pl->d_work, pl->n, pl->d_chunk_begin, pl->d_partial, st);
+    if (reduce && pl->pencil) {
+        launch_pencil_units(o->mra, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_units, pl->n_units, pl->d_err, st);
+        launch_stamp(pl->d_stamps + 4, st);
+        launch_pencil(o->op, pl->d_fs, pl->d_wtree, pl->d_units, pl->d_task_unit, pl->n_tasks, pl->d_pen_partial, pl->d_err, pl->d_pen_counter,
+                      st);
+        launch_stamp(pl->d_stamps + 5, st);
+        ctx->launches += 5;
+    }
+    if (reduce)
+        launch_reduce_chunks(o->mra, pl->d_gs, pl->d_wtree, pl->d_work, pl->n, pl->d_chunk_begin, pl->d_partial, st, nullptr,
+                             pl->pencil ? pl->d_pen_begin : nullptr, pl->pencil ? pl->d_pen_partial : nullptr);
     ctx->launches += 6 + (reduce ? 2 : 0);
 }
 
@@ -1801,10 +1826,17 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
                            &dst->components, &dst->band_nodes, pl->d_err, st);
         launch_scan(pl->d_pcounts, pl->d_item_off, pl->np, pl->d_scan, pl->d_scan + (pl->scan_n - 1), st);
         launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st);
+        const bool ordered = term_order_supported(o->op.n_terms);
         launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
-                          pl->d_item_off, pl->d_items_cm ? pl->d_items_cm : pl->d_items, pl->items_cap, pl->d_err, st);
-        if (pl->d_items_cm) launch_order_terms(pl->d_goff, pl->n, pl->d_items_cm, pl->d_items, o->op.n_terms, pl->d_err, st);
-        ctx->launches += 6 + (pl->d_items_cm ? 1 : 0);
+                          pl->d_item_off, ordered ? pl->d_items_cm : pl->d_items, pl->items_cap, pl->d_err, st);
+        if (ordered) launch_order_terms(pl->d_goff, pl->n, pl->d_items_cm, pl->d_items, o->op.n_terms, pl->d_err, st);
+        ctx->launches += 6 + (ordered ? 1 : 0);
+        if (pl->pencil) {
+            launch_keep_items(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->n, pl->d_items, pl->d_keep, st);
+            launch_scan(pl->d_keep, pl->d_keep_off, pl->n, pl->d_kscan, pl->d_kscan + (pl->kscan_n - 1), st);
+            launch_keep_fill(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->d_keep_off, pl->n, pl->d_items, pl->d_items_cm, st);
+            ctx->launches += 5;
+        }
         plan_contract(ctx, pl, pl->per, true);
     } else {
         launch_stamp(pl->d_stamps + 1, st);
@@ -1839,13 +1871,19 @@ mwgpu_status plan_check(mwgpu_ctx *ctx, mwgpu_plan *pl, mwgpu_level_stats *stats
     int herr = 0;
     LevelStats hs{};
     long long total = 0;
-    unsigned long long stamps[4] = {0, 0, 0, 0};
+    unsigned long long stamps[6] = {0, 0, 0, 0, 0, 0};
+    long long kept = 0;
     MW_CK(cudaMemcpyAsync(stamps, pl->d_stamps, sizeof(stamps), cudaMemcpyDeviceToHost, ctx->stream));
     MW_CK(cudaMemcpyAsync(&herr, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MW_CK(cudaMemcpyAsync(&hs, pl->d_stats, sizeof(LevelStats), cudaMemcpyDeviceToHost, ctx->stream));
     if (pl->precision == MWGPU_PREC_MIXED)
         MW_CK(cudaMemcpyAsync(&total, pl->d_goff + pl->n, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+    if (pl->pencil) MW_CK(cudaMemcpyAsync(&kept, pl->d_keep_off + pl->n, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
     MW_CK(cudaStreamSynchronize(ctx->stream));
+    if (pl->pencil) {
+        pl->pen_node_terms = (unsigned long long)(total - kept);
+        pl->pen_ms = (double)(stamps[5] - stamps[4]) * 1e-6;
+    }
     if (herr & DE_POOL_FULL) {
         ctx->err = "plan: the work list outgrew the planned capacity (input values changed the screening); create a new plan";
         return MWGPU_ERR_OOM;
@@ -1922,7 +1960,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
     mwgpu_status s;
     if ((s = plan_alloc(ctx, pl, &pl->d_work, n)) || (s = plan_alloc(ctx, pl, &pl->d_wtree, n)) || (s = plan_alloc(ctx, pl, &pl->d_fs, n_trees)) ||
         (s = plan_alloc(ctx, pl, &pl->d_gs, n_trees)) || (s = plan_alloc(ctx, pl, &pl->d_gthr, n_trees)) ||
-        (s = plan_alloc(ctx, pl, &pl->d_stats, 1)) || (s = plan_alloc(ctx, pl, &pl->d_err, 1)) || (s = plan_alloc(ctx, pl, &pl->d_stamps, 4)))
+        (s = plan_alloc(ctx, pl, &pl->d_stats, 1)) || (s = plan_alloc(ctx, pl, &pl->d_err, 1)) || (s = plan_alloc(ctx, pl, &pl->d_stamps, 6)))
         return fail(s);
     if (cudaEventCreate(&pl->e1) != cudaSuccess || cudaEventCreate(&pl->e2) != cudaSuccess) {
         ctx->err = "plan: event creation failed";
@@ -2041,7 +2079,25 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
             (s = plan_alloc(ctx, pl, &pl->d_counter, 2)) ||
             (s = plan_alloc(ctx, pl, &pl->d_partial, (size_t)pl->chunks_cap * 8 * o->mra.kp1_d)))
             return fail(s);
-        if (term_order_supported(o->op.n_terms) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
+        pl->pencil = use_pencil(lv);
+        if ((term_order_supported(o->op.n_terms) || pl->pencil) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
+        if (pl->pencil) {
+            PencilPlan pp;
+            pencil_build(lv, pp);
+            pl->n_units = (int)pp.units.size();
+            pl->n_tasks = pp.n_tasks;
+            pl->kscan_n = scan_blocks(n + 1) + 2;
+            if ((s = plan_alloc(ctx, pl, &pl->d_keep, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_keep_off, n + 1)) ||
+                (s = plan_alloc(ctx, pl, &pl->d_kscan, pl->kscan_n)) || (s = plan_alloc(ctx, pl, &pl->d_units, std::max(pl->n_units, 1))) ||
+                (s = plan_alloc(ctx, pl, &pl->d_task_unit, pp.n_tasks + 1)) || (s = plan_alloc(ctx, pl, &pl->d_pen_begin, n + 1)) ||
+                (s = plan_alloc(ctx, pl, &pl->d_pen_counter, 1)) ||
+                (s = plan_alloc(ctx, pl, &pl->d_pen_partial, (size_t)std::max(pp.n_tasks, 1) * 8 * o->mra.kp1_d)))
+                return fail(s);
+            if (pl->n_units > 0)
+                MW_CK(cudaMemcpyAsync(pl->d_units, pp.units.data(), sizeof(PencilUnit) * pl->n_units, cudaMemcpyHostToDevice, ctx->stream));
+            MW_CK(cudaMemcpyAsync(pl->d_task_unit, pp.task_unit.data(), sizeof(int) * (pp.n_tasks + 1), cudaMemcpyHostToDevice, ctx->stream));
+            MW_CK(cudaMemcpyAsync(pl->d_pen_begin, pp.pen_begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+        }
         MW_CK(cudaMemcpyAsync(pl->d_pair_off, poff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
         MW_CK(cudaStreamSynchronize(ctx->stream));
         // chunk length: candidates around the default, each timed on the full
@@ -2133,6 +2189,13 @@ extern "C" mwgpu_status mwgpu_plan_info(const mwgpu_plan *pl, long long *chunk_i
             for (int i = 0; i < std::min(nc, *n_candidates); i++) cand_ms[i] = pl->tune_ms[i];
         *n_candidates = nc;
     }
+    return MWGPU_OK;
+}
+
+extern "C" mwgpu_status mwgpu_plan_pencil_info(const mwgpu_plan *pl, unsigned long long *node_terms, double *ms) {
+    if (!pl || !node_terms || !ms) return MWGPU_ERR_BAD_ARG;
+    *node_terms = pl->pencil ? pl->pen_node_terms : 0ull;
+    *ms = pl->pencil ? pl->pen_ms : 0.0;
     return MWGPU_OK;
 }
 

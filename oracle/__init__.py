@@ -81,36 +81,58 @@ def _pd(a):
 
 class Prepared:
     """Marshalled inputs of one oracle apply; run() calls the C oracle only
-    (so a timing of run() covers the restated reference path alone)."""
+    (so a timing of run() covers the restated reference path alone).
+
+    Prepared(prec, out, oper, inp) takes mrcpp_gb300 objects; from_arrays()
+    takes plain arrays (so that a process can run the oracle without loading
+    the library under test)."""
 
     def __init__(self, prec, out, oper, inp, max_iter=-1, abs_prec=False):
-        mra = inp.mra
-        self.mra = mra
+        d = inp.mra.desc()
+        mra = {"order": d.order, "root_scale": d.root_scale, "max_scale": d.max_scale, "sf": d.sf, "corner": [d.corner[i] for i in range(3)],
+               "nbox": [d.nbox[i] for i in range(3)], "filters": inp.mra._filters}
+        ex = oper.export()
+        op = {"n_terms": oper.n_terms, "build_prec": float(getattr(oper, "prec", 1.0)), "depth": ex["depth"], "max_transl": ex["max_transl"],
+              "blocks": ex["blocks"], "norms": ex["norms"]}
+        self._setup(prec, mra, op, inp.export(), out.export(), float(out.square_norm), max_iter, abs_prec)
+
+    @classmethod
+    def from_arrays(cls, prec, mra, oper, inp, out, out_sqnorm=-1.0, max_iter=-1, abs_prec=False):
+        """mra: order, root_scale, max_scale, sf, corner[3], nbox[3], filters;
+        oper: n_terms, build_prec, depth, max_transl, blocks, norms; inp: idx,
+        child0, coefs, norms; out: idx, child0 (the starting topology)."""
+        self = cls.__new__(cls)
+        self._setup(prec, mra, oper, inp, out, out_sqnorm, max_iter, abs_prec)
+        return self
+
+    def _setup(self, prec, mra, oper, inp, out, out_sqnorm, max_iter, abs_prec):
         self.prec, self.max_iter, self.abs_prec = float(prec), int(max_iter), int(bool(abs_prec))
-        d = mra.desc()
+        self.kp1 = int(mra["order"]) + 1
         self.keep = []
         m = OracleMra()
-        m.order, m.root_scale, m.max_scale, m.sf = d.order, d.root_scale, d.max_scale, d.sf
+        m.order, m.root_scale, m.max_scale, m.sf = int(mra["order"]), int(mra["root_scale"]), int(mra["max_scale"]), float(mra["sf"])
         for i in range(3):
-            m.corner[i] = d.corner[i]
-            m.nbox[i] = d.nbox[i]
-        filt = np.ascontiguousarray(mra._filters)
+            m.corner[i] = int(mra["corner"][i])
+            m.nbox[i] = int(mra["nbox"][i])
+        filt = np.ascontiguousarray(mra["filters"], dtype=np.float64)
         self.keep.append(filt)
         m.filters = _pd(filt)
-        ex = oper.export()
         o = OracleOper()
-        o.n_terms, o.order, o.build_prec = oper.n_terms, mra.order, float(getattr(oper, "prec", 1.0))
-        self.keep.append(ex)
-        o.depth, o.max_transl = _pi(ex["depth"]), _pi(ex["max_transl"])
-        o.blocks, o.norms = _pd(ex["blocks"]), _pd(ex["norms"])
-        fi = inp.export()
+        o.n_terms, o.order, o.build_prec = int(oper["n_terms"]), int(mra["order"]), float(oper["build_prec"])
+        arrs = {k: np.ascontiguousarray(oper[k], dtype=np.int32 if k in ("depth", "max_transl") else np.float64)
+                for k in ("depth", "max_transl", "blocks", "norms")}
+        self.keep.append(arrs)
+        o.depth, o.max_transl = _pi(arrs["depth"]), _pi(arrs["max_transl"])
+        o.blocks, o.norms = _pd(arrs["blocks"]), _pd(arrs["norms"])
+        fi = {"idx": np.ascontiguousarray(inp["idx"], dtype=np.int32), "child0": np.ascontiguousarray(inp["child0"], dtype=np.int32),
+              "coefs": np.ascontiguousarray(inp["coefs"], dtype=np.float64), "norms": np.ascontiguousarray(inp["norms"], dtype=np.float64)}
         self.keep.append(fi)
         ft = OracleTree(len(fi["child0"]), _pi(fi["idx"]), _pi(fi["child0"]), _pd(fi["coefs"]), _pd(fi["norms"]))
-        go = out.export()
+        go = {"idx": np.ascontiguousarray(out["idx"], dtype=np.int32), "child0": np.ascontiguousarray(out["child0"], dtype=np.int32)}
         self.keep.append(go)
         gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
         self.m, self.o, self.ft, self.gt = m, o, ft, gt
-        self.out_sqnorm = float(out.square_norm)
+        self.out_sqnorm = float(out_sqnorm)
 
     def run(self, nthreads=0, count_terms=True, sample=1, export=True, fast=False, deriv_dir=None):
         L = lib(fast)
@@ -127,7 +149,7 @@ class Prepared:
         L.oracle_result_info(res, C.byref(n), C.byref(sq), C.byref(nt), C.byref(nc), C.byref(it))
         out = {"square_norm": sq.value, "node_terms": nt.value, "components": nc.value, "iterations": it.value, "n_nodes": n.value}
         if export:
-            K3 = self.mra.kp1 ** 3
+            K3 = self.kp1 ** 3
             out["idx"] = np.zeros((n.value, 4), dtype=np.int32)
             out["child0"] = np.zeros(n.value, dtype=np.int32)
             out["coefs"] = np.zeros((n.value, 8 * K3))

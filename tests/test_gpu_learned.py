@@ -18,6 +18,9 @@ from oracle import mlp_oracle as mo
 
 pytestmark = pytest.mark.gpu
 
+# two mixed-form contraction schedules of the same level (largest coefficient difference, relative)
+MIXED_SCHED_TOL = 1e-6
+
 
 def level_order(idx, child0, drop=(), extra=()):
     """Proposal arrays from a tree (idx, child0 of any node order): level by
@@ -228,7 +231,10 @@ def test_learned_apply_equals_plain_and_falls_back(gpu):
     st = mw.apply_learned(1e-5, g1, P, f, always, precision=mw.MIXED)
     same, perm = match(g1.export(), px)
     assert same
-    assert np.array_equal(g1.export()["coefs"], px["coefs"][perm]) or rel_errors(g1.export()["coefs"], px["coefs"][perm])[0] <= 1e-12
+    # mixed form: the host-driven apply computes its first TreeBuilder level (no
+    # norm screening) with the pencil contraction, the judged levels use the item
+    # kernel; both sums are within the mixed-form accuracy of each other
+    assert rel_errors(g1.export()["coefs"], px["coefs"][perm])[0] <= MIXED_SCHED_TOL
     # a network that refines nothing misses at level 0 (when the plain tree refines)
     q = np.zeros(mo.NPARAM, dtype=np.float32)
     q[mo.OFF_B3] = -10.0
@@ -264,7 +270,7 @@ def test_trained_network_against_plain_refinement(gpu):
         same, perm = match(b, a)
         assert same, seed
         mx, _ = rel_errors(b["coefs"], a["coefs"][perm])
-        assert mx <= 1e-12, (seed, mx)
+        assert mx <= MIXED_SCHED_TOL, (seed, mx)
         passes.append(sl["apply"]["iterations"])
         iters.append(sp["iterations"])
     assert np.mean(passes) < np.mean(iters), (passes, iters)
