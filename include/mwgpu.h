@@ -154,6 +154,16 @@ mwgpu_status mwgpu_free_tree(mwgpu_ctx *ctx, mwgpu_tree *tree);
  * NULL) receives the component norms the split test needs. */
 mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n,
                                double prec, double out_sqnorm, double *norms_out, mwgpu_level_stats *stats);
+/* mwgpu_apply_level with the precision scaled per output node: the
+ * calculator's precision function (ConvolutionCalculator::setPrecFunction,
+ * ConvolutionCalculator.h:43, set by the precTrees form of apply,
+ * apply.cpp:214-251) evaluated by the caller, prec_fac[i] for node node_ix[i].
+ * Node i is screened with gThreshold = prec * prec_fac[i] *
+ * sqrt(out_sqnorm / nTerms) (ConvolutionCalculator.cpp:244-245).  Factors
+ * must be >= 0 (+inf allowed: a node whose precision trees are zero there
+ * keeps no component); else MWGPU_ERR_BAD_ARG before any device work. */
+mwgpu_status mwgpu_apply_level_scaled(mwgpu_ctx *ctx, const mwgpu_oper *oper, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n,
+                                      double prec, double out_sqnorm, const double *prec_fac, double *norms_out, mwgpu_level_stats *stats);
 
 /* Whole-tree transform of the output tree: MWGPU_TOPDOWN with overwrite = 0
  * adds the coarse-scale contributions downwards (MWTree::mwTransformDown,

@@ -5,6 +5,7 @@
  * construction and mrcpp::apply.  Names and argument meaning follow the
  * reference API:
  *   mwh_apply          mrcpp::apply(prec, out, oper, inp, maxIter, absPrec)   src/treebuilders/apply.h:41
+ *   mwh_apply_prec     mrcpp::apply(prec, out, oper, inp, precTrees, ...)      src/treebuilders/apply.h:43
  *   mwh_apply_batch    a loop of mrcpp::apply over functions, one device pass
  *   mwh_poisson        mrcpp::PoissonOperator(MRA, prec)                       src/operators/PoissonOperator.h:44
  *   mwh_helmholtz      mrcpp::HelmholtzOperator(MRA, mu, prec)                 src/operators/HelmholtzOperator.h:44
@@ -140,6 +141,20 @@ int mwh_helmholtz_kernel(double mu, double eps, double r_min, double r_max, int 
 
 /* mrcpp::apply on the GPU: precision = MWGPU_PREC_FP64 or MWGPU_PREC_MIXED. */
 int mwh_apply(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int max_iter, int abs_prec, int precision, mwh_apply_stats *stats);
+/* mrcpp::apply(prec, out, oper, inp, precTrees, maxIter, absPrec)
+ * (src/treebuilders/apply.h:43, apply.cpp:214-251): the precision of output
+ * node idx is scaled by precFac(idx) = 1 / max_i sqrt(getMaxSquareNorm) of the
+ * node idx of precision tree i after makeMaxSquareNorms (MWTree.cpp:536-543;
+ * the largest 2^(3n) |node|^2 over the node and its descendants), in the
+ * screening threshold (mwgpu_apply_level_scaled) and in the split test
+ * (WaveletAdaptor.h:51-54).  A node missing from a precision tree is generated
+ * for its norm (the precision trees are not changed).  n_prec = 0 gives
+ * precFac = 1, the plain apply. */
+int mwh_apply_prec(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int n_prec, mwh_tree *const *prec_trees, int max_iter,
+                   int abs_prec, int precision, mwh_apply_stats *stats);
+/* The precision function of that form alone (the lambda of apply.cpp:222-229):
+ * fac[j] = precFac of the node idx[4j..4j+3] = (n, l0, l1, l2). */
+int mwh_prec_factors(int n_prec, mwh_tree *const *prec_trees, int n, const int *idx, double *fac);
 /* apply(out, DerivativeOperator, inp, dir) (src/treebuilders/apply.cpp:379-412):
  * out must hold only its root nodes; its grid becomes the input grid widened
  * by the operator band along dir (CopyAdaptor), the end nodes are computed on

@@ -100,6 +100,7 @@ _SIGS = {
     "mwgpu_tree_size": (C.c_int, [_P, _PI]),
     "mwgpu_free_tree": (C.c_int, [_P, _P]),
     "mwgpu_apply_level": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_double, C.c_double, _PD, C.POINTER(MwgpuLevelStats)]),
+    "mwgpu_apply_level_scaled": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_double, C.c_double, _PD, _PD, C.POINTER(MwgpuLevelStats)]),
     "mwgpu_apply_derivative": (C.c_int, [_P, _P, _P, _P, _PI, C.c_int, C.c_int, C.c_int, C.POINTER(MwgpuLevelStats)]),
     "mwgpu_transform": (C.c_int, [_P, _P, C.c_int, C.c_int]),
     "mwgpu_apply_level_batch": (C.c_int, [_P, _P, C.c_int, C.POINTER(_P), C.POINTER(_P), _PI, _PI, C.c_int, C.c_double, _PD, _PD,
@@ -173,6 +174,8 @@ _SIGS = {
     "mwh_poisson_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
     "mwh_helmholtz_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
     "mwh_apply": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwh_apply_prec": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwh_prec_factors": (C.c_int, [C.c_int, _P, C.c_int, _PI, _PD]),
     "mwh_apply_batch": (C.c_int, [C.c_double, C.c_int, C.POINTER(_P), _P, C.POINTER(_P), C.c_int, C.c_int, C.c_int,
                                   C.POINTER(MwhApplyStats)]),
     "mwh_mlp_create": (C.c_int, [_PF, C.POINTER(_P)]),
@@ -535,17 +538,47 @@ def helmholtz_kernel(mu, eps, r_min, r_max):
 def apply(*args, **kw):
     """mrcpp::apply on the GPU, returning the apply statistics:
     apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64) for a
-    convolution operator, apply(out, oper, inp, dir) for a derivative operator
-    (ABGVOperator; output grid = input grid widened along dir, FP64)."""
+    convolution operator; apply(prec, out, oper, inp, prec_trees, max_iter,
+    abs_prec, precision=FP64), or prec_trees=[...] as a keyword, for the form
+    whose precision is scaled per node by the largest norm of the precision
+    trees (src/treebuilders/apply.h:43); apply(out, oper, inp, dir) for a
+    derivative operator (ABGVOperator; output grid = input grid widened along
+    dir, FP64)."""
     if args and isinstance(args[0], FunctionTree):
         return apply_derivative(*args, **kw)
     return _apply_convolution(*args, **kw)
 
 
-def _apply_convolution(prec, out, oper, inp, max_iter=-1, abs_prec=False, precision=FP64):
+def _apply_convolution(prec, out, oper, inp, *rest, max_iter=-1, abs_prec=False, precision=FP64, prec_trees=None):
+    rest = list(rest)
+    if rest and isinstance(rest[0], (list, tuple)):
+        prec_trees = rest.pop(0)
+    if len(rest) > 3:
+        raise TypeError("apply: too many positional arguments")
+    vals = dict(zip(["max_iter", "abs_prec", "precision"], rest))
+    max_iter = vals.get("max_iter", max_iter)
+    abs_prec = vals.get("abs_prec", abs_prec)
+    precision = vals.get("precision", precision)
     st = MwhApplyStats()
-    _ck(lib().mwh_apply(float(prec), out._h, oper._h, inp._h, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
+    if prec_trees is None:
+        _ck(lib().mwh_apply(float(prec), out._h, oper._h, inp._h, int(max_iter), int(bool(abs_prec)), int(precision), C.byref(st)))
+    else:
+        pts = list(prec_trees)
+        arr = (_P * max(len(pts), 1))(*[t._h for t in pts])
+        _ck(lib().mwh_apply_prec(float(prec), out._h, oper._h, inp._h, len(pts), arr, int(max_iter), int(bool(abs_prec)),
+                                 int(precision), C.byref(st)))
     return st.as_dict()
+
+
+def prec_factors(prec_trees, idx):
+    """precFac of the precTrees form of apply (apply.cpp:222-229) for the nodes
+    idx[j] = (n, l0, l1, l2): 1 / the largest sqrt(maxSquareNorm) over the trees."""
+    idx = np.ascontiguousarray(idx, dtype=np.int32).reshape(-1, 4)
+    pts = list(prec_trees)
+    arr = (_P * max(len(pts), 1))(*[t._h for t in pts])
+    fac = np.zeros(len(idx))
+    _ck(lib().mwh_prec_factors(len(pts), arr, len(idx), _pi(idx), _pd(fac)))
+    return fac
 
 
 def apply_derivative(out, oper, inp, dir):

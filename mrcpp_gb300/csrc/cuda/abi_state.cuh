@@ -53,6 +53,9 @@ struct mwgpu_ctx {
     // per-tree arrays of a batched level
     DevTree *d_fs = nullptr, *d_gs = nullptr;
     double *d_gthr = nullptr;
+    // per work entry thresholds of levels whose precision is scaled per output node
+    double *d_gnode = nullptr;
+    long long gnode_cap = 0;
     int trees_cap = 0;
     double *d_nstage = nullptr;  // norms of the computed nodes, staged for the host
     long long nstage_cap = 0;

@@ -94,11 +94,14 @@ __global__ void k_band_missing(DevMRA m, DevOper op, DevTree f, DevTree g, const
 // accuracy instead of FP32 summation accuracy).
 template <typename TC>
 // With nw_dev / gthr_dev the number of work entries and the threshold come from
-// the device (the grid is then a capacity).
+// the device (the grid is then a capacity); gthr_node holds one threshold per
+// work entry where the precision is scaled per output node (apply.cpp:221-228).
 __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work,
-                                                  double gthr, LevelStats *stats, int *err, const int *nw_dev, const double *gthr_dev) {
+                                                  double gthr, LevelStats *stats, int *err, const int *nw_dev, const double *gthr_dev,
+                                                  const double *gthr_node) {
     if (nw_dev && (int)blockIdx.x >= *nw_dev) return;
     if (gthr_dev) gthr = *gthr_dev;
+    if (gthr_node) gthr = gthr_node[blockIdx.x];
     extern __shared__ double sm[];
     const int K = m.K, K2 = K * K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
     double *gacc = sm;
@@ -343,11 +346,12 @@ void launch_band_missing(const DevMRA &m, const DevOper &op, const DevTree &f, c
 }
 
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
-                          double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev, const double *gthr_dev) {
+                          double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev, const double *gthr_dev,
+                          const double *gthr_node) {
     if (n_work <= 0) return;
     size_t smem = sizeof(double) * 14 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err, nw_dev, gthr_dev);
+    k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err, nw_dev, gthr_dev, gthr_node);
 }
 
 }  // namespace mwgpu

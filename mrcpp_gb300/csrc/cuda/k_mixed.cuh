@@ -1,8 +1,10 @@
-// Mixed-precision contraction over a work list (FP32 products and FP32 partial
-// sums, FP64 accumulation of the partial sums every 16 work items).
+// Mixed-precision contraction over a work list: FP32 products; per output
+// component, a compensated (Kahan) FP32 accumulator in registers for K <= 8,
+// and for K > 8 FP32 partial sums added into FP64 accumulators in shared
+// memory every 16 work items.
 //
-// One CTA (512 threads = 16 warps) per chunk of the work items of one output
-// node g (k_worklist.cu makes the items; the screening of
+// One CTA (256 threads = 8 warps, Shape<K>::NW) per chunk of the work items of
+// one output node g (k_worklist.cu makes the items; the screening of
 // ConvolutionCalculator.cpp:224-329 is already in each item's (ft, gt)
 // mask).  Two schedules produce the same sum of component products as
 // tensorApplyOperComp (ConvolutionCalculator.cpp:333-382):

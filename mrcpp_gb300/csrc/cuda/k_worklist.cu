@@ -246,7 +246,8 @@ template <bool FILL, int GT>
 __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                                                const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts,
                                                const long long *item_off, WorkItem *items, long long items_cap, unsigned long long *ncomp,
-                                               unsigned long long *nband, int *err, const long long *np_dev, const int *nw_dev) {
+                                               unsigned long long *nband, int *err, const long long *np_dev, const int *nw_dev,
+                                               const double *gthr_node) {
     static_assert(GT == 0 || GT == 1 || GT == 4 || GT == 8 || GT == 32, "lane group size");
     const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long n_cap = n_pairs;
@@ -277,7 +278,8 @@ __global__ void __launch_bounds__(256) k_pairs(DevMRA m, DevOper op, const DevTr
     if (ok) {
         band = (j == 0);
         const DevTree &f = fs[pc.tree];
-        gthr = gthrs[pc.tree];
+        // per work entry where the precision is scaled locally (apply.cpp:221-228)
+        gthr = gthr_node ? gthr_node[pc.wi] : gthrs[pc.tree];
         pn.fn = f.norms + (size_t)pc.fid * 8;
         double fmx = 0.0;
 #pragma unroll
@@ -563,15 +565,16 @@ __global__ void k_chunk_fill(const long long *g_off, const long long *c_off, int
 
 void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                         const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts, unsigned long long *ncomp,
-                        unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
+                        unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev,
+                        const double *gthr_node) {
     if (n_pairs <= 0) return;
     auto go = [&](auto kern, int g) {
         kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts, nullptr,
-                                                                  nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
+                                                                  nullptr, 0, ncomp, nband, err, np_dev, nw_dev, gthr_node);
     };
     auto kern_dev_false = [&](long long thr) {
         k_pairs<false, 0><<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts,
-                                                                       nullptr, nullptr, 0, ncomp, nband, err, np_dev, nw_dev);
+                                                                       nullptr, nullptr, 0, ncomp, nband, err, np_dev, nw_dev, gthr_node);
     };
     if (np_dev) {
         // group size from the device count: at least kPairThreads threads
@@ -589,16 +592,17 @@ void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, c
 
 void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                        const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const int *counts_in, const long long *item_off,
-                       WorkItem *items, long long items_cap, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev) {
+                       WorkItem *items, long long items_cap, int *err, cudaStream_t s, const long long *np_dev, const int *nw_dev,
+                       const double *gthr_node) {
     if (n_pairs <= 0) return;
     int *counts = const_cast<int *>(counts_in);  // read only in FILL
     auto go = [&](auto kern, int g) {
         kern<<<(unsigned)((n_pairs * g + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts, item_off,
-                                                                  items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
+                                                                  items, items_cap, nullptr, nullptr, err, np_dev, nw_dev, gthr_node);
     };
     auto kern_dev_true = [&](long long thr) {
         k_pairs<true, 0><<<(unsigned)((thr + 255) / 256), 256, 0, s>>>(m, op, fs, gs, work_tree, work, pair_off, n_work, n_pairs, gthrs, counts,
-                                                                      item_off, items, items_cap, nullptr, nullptr, err, np_dev, nw_dev);
+                                                                      item_off, items, items_cap, nullptr, nullptr, err, np_dev, nw_dev, gthr_node);
     };
     if (np_dev) {
         // group size from the device count: at least kPairThreads threads

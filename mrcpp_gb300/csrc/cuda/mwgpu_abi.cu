@@ -236,6 +236,9 @@ struct Level {
     std::vector<int> node, tree, order;  // grouped entries; order[j] = caller position of entry j
     std::vector<int> seg;
     std::vector<double> gthr;
+    // precision scaled per output node (the precTrees form of apply): one
+    // factor per grouped entry, and the thresholds made from them; empty: 1
+    std::vector<double> pfac, gnode;
     std::vector<DevTree> fs, gs;
     // derivative levels: band direction (-1: convolution), band width, operator order
     int band_dir = -1, band_w = 0, deriv_order = 0;
@@ -281,6 +284,8 @@ bool use_pencil(const Level &lv) {
     const mwgpu_oper *o = lv.o;
     if (!pencil_supported(o->op.K) || !o->op.btc_stack || lv.band_dir >= 0 || std::getenv("MWGPU_NO_PENCIL")) return false;
     for (double g : lv.gthr)
+        if (!(g < 0.0)) return false;
+    for (double g : lv.gnode)
         if (!(g < 0.0)) return false;
     for (int t = 0; t < lv.nt; t++)
         if (!lv.inps[t]->t.tc32) return false;
@@ -389,8 +394,9 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     if (auto s = grow_buf(ctx, &ctx->d_goff, &ctx->goff_cap, n + 1)) return s;
     MW_CK(cudaMemcpyAsync(ctx->d_pair_off, poff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
     LevelStats *dst = ctx->d_stats;
+    const double *gnode = lv.gnode.empty() ? nullptr : ctx->d_gnode;
     launch_pairs_count(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_pcounts,
-                       &dst->components, &dst->band_nodes, ctx->d_err, ctx->stream);
+                       &dst->components, &dst->band_nodes, ctx->d_err, ctx->stream, nullptr, nullptr, gnode);
     long long *d_total = ctx->d_scan + (ctx->scan_cap - 1);
     launch_scan(ctx->d_pcounts, ctx->d_item_off, np, ctx->d_scan, d_total, ctx->stream);
     launch_gather_goff(ctx->d_item_off, ctx->d_pair_off, n, ctx->d_goff, ctx->stream);
@@ -415,7 +421,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     // cell-major items from the builder, then term-major per output node
     const bool order = term_order_supported(o->op.n_terms);
     launch_pairs_fill(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_pair_off, n, np, ctx->d_gthr, ctx->d_pcounts, ctx->d_item_off,
-                      order ? ctx->d_items_cm : ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream);
+                      order ? ctx->d_items_cm : ctx->d_items, ctx->items_cap, ctx->d_err, ctx->stream, nullptr, nullptr, gnode);
     if (order) launch_order_terms(ctx->d_goff, n, ctx->d_items_cm, ctx->d_items, o->op.n_terms, ctx->d_err, ctx->stream);
     ctx->launches += 1 + (order ? 1 : 0);
     // pencil path: the items of the wider terms stay with the item kernel (stable compaction into d_items_cm)
@@ -687,12 +693,25 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
     if (auto s = gen_pass(ctx, lv, pcount, gen_total)) return s;
     tr.mark("gen");
     if (pcount_out) *pcount_out = pcount;
-    // per-tree screening threshold (ConvolutionCalculator.cpp:297-305)
+    // per-tree screening threshold (ConvolutionCalculator.cpp:240-246); with
+    // per-node factors (apply.cpp:221-228) one threshold per work entry,
+    // prec * precFac * sqrt(|g|^2 / nTerms) in the reference's order
     lv.gthr.assign(nt, 0.0);
     for (int t = 0; t < nt; t++) {
         double g = sqnorms[t];
         if (g > 0.0) g = prec * 1.0 * std::sqrt(g / (double)o->op.n_terms);
         lv.gthr[t] = g;
+    }
+    lv.gnode.clear();
+    if (!lv.pfac.empty()) {
+        lv.gnode.resize(n);
+        for (int j = 0; j < n; j++) {
+            double g = sqnorms[lv.tree[j]];
+            if (g > 0.0) g = prec * lv.pfac[j] * std::sqrt(g / (double)o->op.n_terms);
+            lv.gnode[j] = g;
+        }
+        if (auto s = grow_buf(ctx, &ctx->d_gnode, &ctx->gnode_cap, n)) return s;
+        MW_CK(cudaMemcpyAsync(ctx->d_gnode, lv.gnode.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     }
     lv.fs.resize(nt);
     lv.gs.resize(nt);
@@ -716,7 +735,7 @@ mwgpu_status level_run(mwgpu_ctx *ctx, Level &lv, const double *sqnorms, double 
             const int b = lv.seg[t], e = lv.seg[t + 1];
             if (b == e) continue;
             launch_contract_fp64(o->mra, o->op, lv.inps[t]->t, lv.outs[t]->t, ctx->d_work + b, e - b, lv.gthr[t], ctx->d_stats, ctx->d_err,
-                                 ctx->stream);
+                                 ctx->stream, nullptr, nullptr, lv.gnode.empty() ? nullptr : ctx->d_gnode + b);
             ctx->launches++;
         }
     }
@@ -868,9 +887,15 @@ mwgpu_status make_level(mwgpu_ctx *ctx, const mwgpu_oper *o, int nt, mwgpu_tree 
 }
 
 mwgpu_status level_entry(mwgpu_ctx *ctx, const mwgpu_oper *o, int nt, mwgpu_tree *const *inps, mwgpu_tree *const *outs, const int *work_tree,
-                         const int *node_ix, int n, double prec, const double *sqnorms, double *norms_out, mwgpu_level_stats *stats) {
+                         const int *node_ix, int n, double prec, const double *sqnorms, double *norms_out, mwgpu_level_stats *stats,
+                         const double *prec_fac = nullptr) {
     Level lv;
     if (auto s = make_level(ctx, o, nt, inps, outs, work_tree, node_ix, n, lv)) return s;
+    if (prec_fac) {
+        for (int i = 0; i < n; i++) MW_ARG(prec_fac[i] >= 0.0, "precision factors must be >= 0 (1 / the largest norm of the precision trees)");
+        lv.pfac.resize(n);
+        for (int j = 0; j < n; j++) lv.pfac[j] = prec_fac[lv.order[j]];
+    }
     cudaSetDevice(ctx->device);
     if (stats) std::memset(stats, 0, sizeof(*stats));
     if (n == 0) return MWGPU_OK;
@@ -926,7 +951,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
                     (void *)ctx->d_item_off, (void *)ctx->d_scan, (void *)ctx->d_goff, (void *)ctx->d_wtree, (void *)ctx->d_fs,
                     (void *)ctx->d_gs, (void *)ctx->d_gthr, (void *)ctx->d_nstage, (void *)ctx->d_ltree, (void *)ctx->d_units,
                     (void *)ctx->d_task_unit, (void *)ctx->d_pen_partial, (void *)ctx->d_pen_begin, (void *)ctx->d_keep, (void *)ctx->d_keep_off,
-                    (void *)ctx->d_pen_counter})
+                    (void *)ctx->d_pen_counter, (void *)ctx->d_gnode})
         if (p) cudaFree(p);
     pool_trim(ctx);
     for (auto &e : ctx->marks)
@@ -1284,6 +1309,14 @@ mwgpu_status mwgpu_apply_level(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
     return level_entry(ctx, o, 1, inps, outs, nullptr, node_ix, n, prec, &out_sqnorm, norms_out, stats);
+}
+
+mwgpu_status mwgpu_apply_level_scaled(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n,
+                                      double prec, double out_sqnorm, const double *prec_fac, double *norms_out, mwgpu_level_stats *stats) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n == 0 || prec_fac, "null precision factors");
+    mwgpu_tree *inps[1] = {inp}, *outs[1] = {out};
+    return level_entry(ctx, o, 1, inps, outs, nullptr, node_ix, n, prec, &out_sqnorm, norms_out, stats, prec_fac);
 }
 
 mwgpu_status mwgpu_combine_level(mwgpu_ctx *ctx, int op, int n_in, mwgpu_tree *const *inps, const double *c, const double *cv_map, const double *vc_map,
@@ -1705,6 +1738,9 @@ struct mwgpu_plan {
     std::vector<mwgpu_tree *> inps, outs;
     std::vector<int> seg;
     std::vector<double> gthr;
+    // precision scaled per output node (the precTrees form of apply): one
+    // factor per grouped entry, and the thresholds made from them; empty: 1
+    std::vector<double> pfac, gnode;
     std::vector<void *> allocs;
     int *d_work = nullptr, *d_wtree = nullptr;
     DevTree *d_fs = nullptr, *d_gs = nullptr;

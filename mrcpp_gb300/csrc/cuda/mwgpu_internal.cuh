@@ -256,16 +256,18 @@ void launch_deriv(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree 
                   int *err, cudaStream_t s);
 void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, DevTree g, const int *work, int n_work,
                           double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev = nullptr,
-                          const double *gthr_dev = nullptr);
+                          const double *gthr_dev = nullptr, const double *gthr_node = nullptr);
 bool mixed_supported(int K);
 void launch_pairs_count(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                         const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, int *counts, unsigned long long *ncomp,
-                        unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
+                        unsigned long long *nband, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr,
+                        const double *gthr_node = nullptr);
 // FILL: counts are the COUNT pass's per-pair item counts (pairs without items
 // are skipped; may be null)
 void launch_pairs_fill(const DevMRA &m, const DevOper &op, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work,
                        const long long *pair_off, int n_work, long long n_pairs, const double *gthrs, const int *counts, const long long *item_off,
-                       WorkItem *items, long long items_cap, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr);
+                       WorkItem *items, long long items_cap, int *err, cudaStream_t s, const long long *np_dev = nullptr, const int *nw_dev = nullptr,
+                       const double *gthr_node = nullptr);
 // chunking of the work list on the device (graph-capturable levels); per <= 0:
 // the chunk length follows from the item count on the device (kChunkTarget)
 void launch_chunk_count(const long long *g_off, int n_work, long long per, int *counts, cudaStream_t s, const int *nw_dev = nullptr);

@@ -258,13 +258,35 @@ void sync_new(mwgpu_ctx *ctx, BuildState &b, mwh_apply_stats &acc) {
     b.synced = t.nodes.size();
 }
 
+// The precision function of the precTrees form of apply (apply.cpp:221-229):
+// precFac(idx) = 1 / max_i sqrt(getNode(idx).getMaxSquareNorm()) over the
+// precision trees after makeMaxSquareNorms; 1 without precision trees.  A node
+// a precision tree lacks is generated for its norm alone (the tree is read only).
+struct PrecScale {
+    std::vector<const Tree<3> *> trees;
+    std::vector<std::vector<double>> msq;
+    double operator()(int n, const int *l) const {
+        if (trees.empty()) return 1.0;
+        double maxNorm = 0.0;
+        for (size_t i = 0; i < trees.size(); i++) {
+            const int id = trees[i]->find(n, l);
+            const double v = id >= 0 ? msq[i][id] : trees[i]->genScaledSquareNorm(n, l);
+            maxNorm = std::max(maxNorm, std::sqrt(v));
+        }
+        return 1.0 / maxNorm;
+    }
+};
+
 // mrcpp::apply (apply.cpp:68-93) for nt independent (out, inp) pairs with one
 // operator.  Each TreeBuilder iteration of all trees still building is one
 // device level call; the transforms of all trees share their launches.
 // resume (nt = 1 only): continue the TreeBuilder loop of an apply whose
 // earlier iterations ran elsewhere (device trees, work, iteration and norms).
+// scale (nt = 1 only): the precTrees form (apply.cpp:214-251), the precision
+// scaled per output node in the screening and in the split test.
 int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree **inps, int max_iter, int abs_prec, int precision,
-               mwh_apply_stats *stats, const BuildState *resume = nullptr) {
+               mwh_apply_stats *stats, const BuildState *resume = nullptr, const PrecScale *scale = nullptr) {
+    if (scale && nt != 1) return fail(1, "precision trees need a single (out, inp) pair");
     ConvolutionOperator &op = *operp->op;
     for (int t = 0; t < nt; t++) {
         if (!(*outs[t]->t->mra == *inps[t]->t->mra)) return fail(1, "Incompatible MRA");
@@ -319,7 +341,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
         }
         ht.mark("upload");
         std::vector<int> wtree, wnode;
-        std::vector<double> sq(nt), nbuf;
+        std::vector<double> sq(nt), nbuf, pfac;
         std::vector<mwgpu_tree *> dins(nt), douts(nt);
         for (int t = 0; t < nt; t++) {
             dins[t] = bs[t].dinp;
@@ -342,7 +364,16 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
             const int n = (int)wnode.size();
             nbuf.resize((size_t)n * 8);
             mwgpu_level_stats ls{};
-            if (nt == 1)
+            if (scale) {
+                pfac.resize(n);
+                for (int j = 0; j < n; j++) {
+                    const auto &nd = bs[0].tree->nodes[wnode[j]];
+                    pfac[j] = (*scale)(nd.n, nd.l);
+                }
+                ck(mwgpu_apply_level_scaled(ctx, dop, dins[0], douts[0], wnode.data(), n, prec, sq[0], pfac.data(), nbuf.data(), &ls),
+                   "apply level");
+                acc.h2d_bytes += (unsigned long long)n * 8;
+            } else if (nt == 1)
                 ck(mwgpu_apply_level(ctx, dop, dins[0], douts[0], wnode.data(), n, prec, sq[0], nbuf.data(), &ls), "apply level");
             else
                 ck(mwgpu_apply_level_batch(ctx, dop, nt, dins.data(), douts.data(), wtree.data(), wnode.data(), n, prec, sq.data(), nbuf.data(),
@@ -384,10 +415,13 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
                 tree.squareNorm = (b.sNorm < 0.0 || b.wNorm < 0.0) ? -1.0 : b.sNorm + b.wNorm;
                 if (b.iter >= max_iter && max_iter >= 0) b.work.clear();
                 std::vector<int> next;
-                for (int i : b.work) {
+                for (size_t j = 0; j < b.work.size(); j++) {
+                    const int i = b.work[j];
                     if (tree.isBranch(i)) continue;
                     if (tree.nodes[i].n + 2 > mra.maxScale()) continue;
-                    if (split_check(tree, i, prec, 1.0, abs_prec != 0)) {
+                    // WaveletAdaptor::splitNode: prec * precFac (WaveletAdaptor.h:51-54)
+                    const double p = scale ? prec * pfac[j] : prec;
+                    if (split_check(tree, i, p, 1.0, abs_prec != 0)) {
                         tree.createChildren(i, false);
                         int c0 = tree.nodes[i].child0;
                         for (int c = 0; c < Tree<3>::tDim; c++) next.push_back(c0 + c);
@@ -1128,6 +1162,38 @@ int mwh_apply(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int 
         if (!outp || !operp || !inpp) return fail(1, "null argument");
         mwh_tree *outs[1] = {outp}, *inps[1] = {inpp};
         return apply_impl(prec, 1, outs, operp, inps, max_iter, abs_prec, precision, stats);
+    });
+}
+
+int mwh_apply_prec(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int n_prec, mwh_tree *const *prec_trees, int max_iter,
+                   int abs_prec, int precision, mwh_apply_stats *stats) {
+    return guard([&] {
+        if (!outp || !operp || !inpp || n_prec < 0 || (n_prec > 0 && !prec_trees)) return fail(1, "null argument");
+        PrecScale ps;
+        for (int i = 0; i < n_prec; i++) {
+            if (!prec_trees[i]) return fail(1, "null argument");
+            if (prec_trees[i] == outp) return fail(1, "the output tree cannot be a precision tree");
+            if (!(*prec_trees[i]->t->mra == *outp->t->mra)) return fail(1, "Incompatible MRA");
+            ps.trees.push_back(prec_trees[i]->t.get());
+            ps.msq.push_back(prec_trees[i]->t->maxSquareNorms());  // makeMaxSquareNorms (apply.cpp:221)
+        }
+        mwh_tree *outs[1] = {outp}, *inps[1] = {inpp};
+        return apply_impl(prec, 1, outs, operp, inps, max_iter, abs_prec, precision, stats, nullptr, &ps);
+    });
+}
+
+int mwh_prec_factors(int n_prec, mwh_tree *const *prec_trees, int n, const int *idx, double *fac) {
+    return guard([&] {
+        if (n_prec < 0 || (n_prec > 0 && !prec_trees) || n < 0 || (n > 0 && (!idx || !fac))) return fail(1, "null argument");
+        PrecScale ps;
+        for (int i = 0; i < n_prec; i++) {
+            if (!prec_trees[i]) return fail(1, "null argument");
+            if (i > 0 && !(*prec_trees[i]->t->mra == *prec_trees[0]->t->mra)) return fail(1, "Incompatible MRA");
+            ps.trees.push_back(prec_trees[i]->t.get());
+            ps.msq.push_back(prec_trees[i]->t->maxSquareNorms());
+        }
+        for (int j = 0; j < n; j++) fac[j] = ps(idx[4 * j], idx + 4 * j + 1);
+        return 0;
     });
 }
 

@@ -194,6 +194,15 @@ template <int D> struct Tree {
     std::vector<std::vector<int>> nodesByDepth(bool includeGen = false) const;
     std::vector<int> endNodes() const;
     void clearGenerated();
+    // MWNode::getMaxSquareNorm of every node after MWTree::makeMaxSquareNorms
+    // (MWTree.cpp:536-543, MWNode.cpp:1257-1269, MWNode.h:84,212): the largest
+    // 2^(D n) |node|^2 over the node and its real descendants; GenNodes get
+    // their own scaled square norm
+    std::vector<double> maxSquareNorms() const;
+    // the scaled square norm 2^(D n) |s|^2 of the node (n, l) where it is
+    // missing: its scaling block made from the deepest existing ancestor as
+    // getNode would generate it (the tree is not changed)
+    double genScaledSquareNorm(int n, const int *l) const;
     // norm override hook (OperatorNode::calcComponentNorm); nullptr = plain
     std::function<double(const Tree &, int, int)> componentNorm;
 };

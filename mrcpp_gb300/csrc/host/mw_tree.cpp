@@ -139,6 +139,65 @@ template <int D> void Tree<D>::giveChildrenCoefs(int i, bool overwrite) {
     }
 }
 
+template <int D> std::vector<double> Tree<D>::maxSquareNorms() const {
+    std::vector<double> msq(nodes.size(), -1.0);
+    auto scaled = [this](int i) {
+        double sq = 0.0;
+        for (int c = 0; c < tDim; c++) sq += nodes[i].norms[c] * nodes[i].norms[c];
+        return std::ldexp(1.0, D * nodes[i].n) * sq;
+    };
+    // deepest level first, so that every child is done before its parent
+    const auto levels = nodesByDepth(true);
+    for (auto it = levels.rbegin(); it != levels.rend(); ++it)
+        for (int i : *it) {
+            double m = scaled(i);
+            const int c0 = nodes[i].child0;
+            if (!isGen(i) && c0 >= 0 && !isGen(c0))
+                for (int c = 0; c < tDim; c++) m = std::max(m, msq[c0 + c]);
+            msq[i] = m;
+        }
+    return msq;
+}
+
+template <int D> double Tree<D>::genScaledSquareNorm(int n, const int *l) const {
+    int cur = rootIndexOf(n, l);
+    if (cur < 0) throw Error(1, "node index outside the world box");
+    std::vector<double> blk(c(cur), c(cur) + nCoefs), kids((size_t)tDim * nCoefs);
+    bool gen = isGen(cur);
+    int at = nodes[cur].n;
+    while (at < n) {
+        const int shift = n - at - 1;
+        int ci = 0;
+        for (int d = 0; d < D; d++) ci |= ((l[d] >> shift) & 1) << d;
+        const int c0 = (cur >= 0) ? nodes[cur].child0 : -1;
+        if (c0 >= 0) {
+            cur = c0 + ci;
+            blk.assign(c(cur), c(cur) + nCoefs);
+            gen = isGen(cur);
+        } else {
+            // giveChildrenCoefs(overwrite = true) of a leaf: children scaling blocks
+            std::fill(kids.begin(), kids.end(), 0.0);
+            mw_transform<D>(*mra->basis, blk.data(), kids.data(), gen, nCoefs, true);
+            blk.assign(kids.begin() + (size_t)ci * nCoefs, kids.begin() + (size_t)(ci + 1) * nCoefs);
+            gen = true;
+            cur = -1;
+        }
+        at++;
+    }
+    double sq;
+    if (cur >= 0) {
+        sq = 0.0;
+        for (int c = 0; c < tDim; c++) sq += nodes[cur].norms[c] * nodes[cur].norms[c];
+    } else {
+        // calcNorms of a GenNode: the scaling component only
+        double s = 0.0;
+        for (int j = 0; j < kp1_d; j++) s += blk[j] * blk[j];
+        const double nrm = std::sqrt(s);
+        sq = nrm * nrm;
+    }
+    return std::ldexp(1.0, D * n) * sq;
+}
+
 template <int D> void Tree<D>::calcNorms(int i) {
     double sq = 0.0;
     for (int c = 0; c < tDim; c++) {

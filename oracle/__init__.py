@@ -55,6 +55,8 @@ def lib(fast=False):
                                    C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
         L.oracle_apply_sampled.restype = C.c_int
         L.oracle_apply_sampled.argtypes = L.oracle_apply.argtypes[:10] + [C.c_int, C.POINTER(C.c_void_p)]
+        L.oracle_apply_prec.restype = C.c_int
+        L.oracle_apply_prec.argtypes = L.oracle_apply.argtypes[:10] + [C.c_int, C.c_int, C.POINTER(OracleTree), C.POINTER(C.c_void_p)]
         L.oracle_result_info.restype = C.c_int
         L.oracle_result_info.argtypes = [C.c_void_p, _PI, _PD, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), _PI]
         L.oracle_result_export.restype = C.c_int
@@ -87,25 +89,34 @@ class Prepared:
     takes plain arrays (so that a process can run the oracle without loading
     the library under test)."""
 
-    def __init__(self, prec, out, oper, inp, max_iter=-1, abs_prec=False):
+    def __init__(self, prec, out, oper, inp, max_iter=-1, abs_prec=False, prec_trees=None):
         d = inp.mra.desc()
         mra = {"order": d.order, "root_scale": d.root_scale, "max_scale": d.max_scale, "sf": d.sf, "corner": [d.corner[i] for i in range(3)],
                "nbox": [d.nbox[i] for i in range(3)], "filters": inp.mra._filters}
         ex = oper.export()
         op = {"n_terms": oper.n_terms, "build_prec": float(getattr(oper, "prec", 1.0)), "depth": ex["depth"], "max_transl": ex["max_transl"],
               "blocks": ex["blocks"], "norms": ex["norms"]}
-        self._setup(prec, mra, op, inp.export(), out.export(), float(out.square_norm), max_iter, abs_prec)
+        pts = None if prec_trees is None else [t.export() for t in prec_trees]
+        self._setup(prec, mra, op, inp.export(), out.export(), float(out.square_norm), max_iter, abs_prec, pts)
 
     @classmethod
-    def from_arrays(cls, prec, mra, oper, inp, out, out_sqnorm=-1.0, max_iter=-1, abs_prec=False):
+    def from_arrays(cls, prec, mra, oper, inp, out, out_sqnorm=-1.0, max_iter=-1, abs_prec=False, prec_trees=None):
         """mra: order, root_scale, max_scale, sf, corner[3], nbox[3], filters;
         oper: n_terms, build_prec, depth, max_transl, blocks, norms; inp: idx,
-        child0, coefs, norms; out: idx, child0 (the starting topology)."""
+        child0, coefs, norms; out: idx, child0 (the starting topology);
+        prec_trees: trees like inp (the precTrees form of apply)."""
         self = cls.__new__(cls)
-        self._setup(prec, mra, oper, inp, out, out_sqnorm, max_iter, abs_prec)
+        self._setup(prec, mra, oper, inp, out, out_sqnorm, max_iter, abs_prec, prec_trees)
         return self
 
-    def _setup(self, prec, mra, oper, inp, out, out_sqnorm, max_iter, abs_prec):
+    @staticmethod
+    def _tree(t, keep):
+        a = {"idx": np.ascontiguousarray(t["idx"], dtype=np.int32), "child0": np.ascontiguousarray(t["child0"], dtype=np.int32),
+             "coefs": np.ascontiguousarray(t["coefs"], dtype=np.float64), "norms": np.ascontiguousarray(t["norms"], dtype=np.float64)}
+        keep.append(a)
+        return OracleTree(len(a["child0"]), _pi(a["idx"]), _pi(a["child0"]), _pd(a["coefs"]), _pd(a["norms"]))
+
+    def _setup(self, prec, mra, oper, inp, out, out_sqnorm, max_iter, abs_prec, prec_trees=None):
         self.prec, self.max_iter, self.abs_prec = float(prec), int(max_iter), int(bool(abs_prec))
         self.kp1 = int(mra["order"]) + 1
         self.keep = []
@@ -124,10 +135,9 @@ class Prepared:
         self.keep.append(arrs)
         o.depth, o.max_transl = _pi(arrs["depth"]), _pi(arrs["max_transl"])
         o.blocks, o.norms = _pd(arrs["blocks"]), _pd(arrs["norms"])
-        fi = {"idx": np.ascontiguousarray(inp["idx"], dtype=np.int32), "child0": np.ascontiguousarray(inp["child0"], dtype=np.int32),
-              "coefs": np.ascontiguousarray(inp["coefs"], dtype=np.float64), "norms": np.ascontiguousarray(inp["norms"], dtype=np.float64)}
-        self.keep.append(fi)
-        ft = OracleTree(len(fi["child0"]), _pi(fi["idx"]), _pi(fi["child0"]), _pd(fi["coefs"]), _pd(fi["norms"]))
+        ft = self._tree(inp, self.keep)
+        self.n_prec = 0 if prec_trees is None else len(prec_trees)
+        self.pt = (OracleTree * max(self.n_prec, 1))(*[self._tree(t, self.keep) for t in (prec_trees or [])])
         go = {"idx": np.ascontiguousarray(out["idx"], dtype=np.int32), "child0": np.ascontiguousarray(out["child0"], dtype=np.int32)}
         self.keep.append(go)
         gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
@@ -138,8 +148,9 @@ class Prepared:
         L = lib(fast)
         res = C.c_void_p()
         if deriv_dir is None:
-            rc = L.oracle_apply_sampled(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), self.out_sqnorm, self.prec,
-                                        self.max_iter, self.abs_prec, int(nthreads), int(bool(count_terms)), int(sample), C.byref(res))
+            rc = L.oracle_apply_prec(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), self.out_sqnorm, self.prec,
+                                     self.max_iter, self.abs_prec, int(nthreads), int(bool(count_terms)), int(sample), self.n_prec, self.pt,
+                                     C.byref(res))
         else:
             rc = L.oracle_apply_derivative(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), int(deriv_dir), 1,
                                            int(nthreads), C.byref(res))
@@ -159,11 +170,12 @@ class Prepared:
         return out
 
 
-def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, nthreads=0, count_terms=True, sample=1):
+def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, nthreads=0, count_terms=True, sample=1, prec_trees=None):
     """Oracle apply.  `out` (FunctionTree) gives the starting topology and square
-    norm; `oper` a mrcpp_gb300 ConvolutionOperator; `inp` the input FunctionTree.
+    norm; `oper` a mrcpp_gb300 ConvolutionOperator; `inp` the input FunctionTree;
+    `prec_trees` (FunctionTrees) selects the precTrees form of apply.
     Returns a dict with the flat output tree and the counters."""
-    return Prepared(prec, out, oper, inp, max_iter, abs_prec).run(nthreads, count_terms, sample)
+    return Prepared(prec, out, oper, inp, max_iter, abs_prec, prec_trees).run(nthreads, count_terms, sample)
 
 
 def apply_derivative(out, oper, inp, dir, nthreads=0):

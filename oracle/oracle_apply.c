@@ -19,6 +19,9 @@
  *   node norms                src/trees/MWNode.cpp:609-655
  *   TreeBuilder loop          src/treebuilders/TreeBuilder.cpp:38-87, 150-166
  *   split                     src/treebuilders/TreeAdaptor.h:41-52, src/utils/tree_utils.cpp:47-65
+ *   precTrees form of apply   src/treebuilders/apply.cpp:214-251 (precFunc), MWTree.cpp:536-543 and
+ *                             MWNode.cpp:1257-1269 (makeMaxSquareNorms), MWNode.h:84,212,
+ *                             ConvolutionCalculator.cpp:244-245, WaveletAdaptor.h:51-54
  *   TopDown / BottomUp        src/trees/MWTree.cpp:166-216, MWNode.cpp:312-335,
  *                             FunctionNode.cpp:391-409, tree_utils.cpp:229-301
  * Differences from the reference that do not change results: GenNodes needed
@@ -505,8 +508,8 @@ static int band_box(const ooper *o, const otree *f, okey g, int *s, int *e) {
 }
 
 /* ConvolutionCalculator::calcNode for output node gi */
-static void calc_node(const oracle_mra *m, const ooper *o, const otree *f, otree *g, int gi, double prec, double gsq, double *scr,
-                      ostats *st) {
+static void calc_node(const oracle_mra *m, const ooper *o, const otree *f, otree *g, int gi, double prec, double precFac, double gsq,
+                      double *scr, ostats *st) {
     const int K = g->K, K3 = g->K3;
     double *gc = g->coefs + (size_t)gi * g->nc;
     memset(gc, 0, sizeof(double) * g->nc);
@@ -515,7 +518,6 @@ static void calc_node(const oracle_mra *m, const ooper *o, const otree *f, otree
     double gThrs = gsq;
     if (gThrs > 0.0) {
         double nTerms = (double)o->T;
-        double precFac = 1.0;
         gThrs = prec * precFac * sqrt(gThrs / nTerms);
     }
     int s[3], e[3];
@@ -579,11 +581,11 @@ static void calc_node(const oracle_mra *m, const ooper *o, const otree *f, otree
 /* node.term count: (g, f, i) triples with >= 1 contracted component.  Counted by
  * re-running the screening without the contraction (instrumentation only). */
 static unsigned long long count_node_terms(const oracle_mra *m, const ooper *o, const otree *f, const otree *g, int gi, double prec,
-                                           double gsq) {
+                                           double precFac, double gsq) {
     okey gk = g->idx[gi];
     int o_depth = gk.n - m->root_scale;
     double gThrs = gsq;
-    if (gThrs > 0.0) gThrs = prec * 1.0 * sqrt(gThrs / (double)o->T);
+    if (gThrs > 0.0) gThrs = prec * precFac * sqrt(gThrs / (double)o->T);
     int s[3], e[3];
     unsigned long long cnt = 0;
     if (!band_box(o, f, gk, s, e)) return 0;
@@ -675,6 +677,50 @@ static int *bfs(const otree *t, size_t *count, int **lvl_start, int *nlvl) {
     return out;
 }
 
+/* A precision tree of the precTrees form of apply: its nodes' maxSquareNorm
+ * after makeMaxSquareNorms (MWTree.cpp:536-543, MWNode.cpp:1257-1269): the
+ * largest 2^(3n) |node|^2 over the node and its real descendants. */
+typedef struct {
+    otree t;
+    double *msq;
+    size_t n_real;
+} oprec;
+
+static double scaled_sq(const otree *t, int i) { return ldexp(1.0, 3 * t->idx[i].n) * t->sqn[i]; }
+
+static void prec_setup(oprec *p) {
+    size_t cnt;
+    int *lvl, nl;
+    int *order = bfs(&p->t, &cnt, &lvl, &nl);
+    p->n_real = p->t.n;
+    p->msq = (double *)malloc(sizeof(double) * (p->t.n + 1));
+    for (int L = nl - 1; L >= 0; L--)
+        for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+            int i = order[q];
+            double v = scaled_sq(&p->t, i);
+            int c0 = p->t.child0[i];
+            if (c0 >= 0 && !p->t.gen[c0])
+                for (int c = 0; c < 8; c++) v = fmax(v, p->msq[c0 + c]);
+            p->msq[i] = v;
+        }
+    free(order);
+    free(lvl);
+}
+
+/* precFunc (apply.cpp:222-229): 1 / max_i sqrt(getNode(idx).getMaxSquareNorm());
+ * getNode generates missing nodes (their maxSquareNorm is unset, so
+ * getMaxSquareNorm gives their own scaled square norm, MWNode.h:84). */
+static double prec_factor(oprec *pt, int n_prec, const oracle_mra *m, okey k, double *tmp1, double *tmp2) {
+    double maxNorm = n_prec ? 0.0 : 1.0;
+    for (int i = 0; i < n_prec; i++) {
+        int id = get_node(&pt[i].t, m, k, tmp1, tmp2);
+        if (id < 0) continue;
+        double v = ((size_t)id < pt[i].n_real && !pt[i].t.gen[id]) ? pt[i].msq[id] : scaled_sq(&pt[i].t, id);
+        maxNorm = fmax(maxNorm, sqrt(v));
+    }
+    return 1.0 / maxNorm;
+}
+
 struct oracle_result {
     otree g;
     ostats st;
@@ -683,15 +729,23 @@ struct oracle_result {
 
 int oracle_apply(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm, double prec,
                  int max_iter, int abs_prec, int nthreads, int count_terms, oracle_result **res) {
-    return oracle_apply_sampled(m, od, inp, out0, out_sqnorm, prec, max_iter, abs_prec, nthreads, count_terms, 1, res);
+    return oracle_apply_prec(m, od, inp, out0, out_sqnorm, prec, max_iter, abs_prec, nthreads, count_terms, 1, 0, NULL, res);
+}
+
+int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
+                         double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, oracle_result **res) {
+    return oracle_apply_prec(m, od, inp, out0, out_sqnorm, prec, max_iter, abs_prec, nthreads, count_terms, sample, 0, NULL, res);
 }
 
 /* sample > 1 computes only every sample-th node of each work list (a bounded
- * timing sample for the CPU baseline; the tree is then incomplete). */
-int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
-                         double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, oracle_result **res) {
+ * timing sample for the CPU baseline; the tree is then incomplete).  n_prec > 0:
+ * the precTrees form (apply.cpp:214-251), each output node's precision scaled
+ * by precFac in its threshold and in its split test. */
+int oracle_apply_prec(const oracle_mra *m, const oracle_oper *od, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
+                      double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, int n_prec,
+                      const oracle_tree *prec_trees, oracle_result **res) {
     if (sample < 1) sample = 1;
-    if (!m || !od || !inp || !out0 || !res) return 1;
+    if (!m || !od || !inp || !out0 || !res || n_prec < 0 || (n_prec > 0 && !prec_trees)) return 1;
     if (od->order != m->order) return 1;
     ooper o;
     oper_setup(&o, od, prec); /* MWOperator::calcBandWidths(prec) */
@@ -701,6 +755,15 @@ int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracl
     if (tree_load(&R->g, m, out0->n_nodes, out0->idx, out0->child0, NULL, NULL)) return 2;
     otree *g = &R->g;
     g->square_norm = out_sqnorm;
+    /* makeMaxSquareNorms of every precision tree (apply.cpp:221) */
+    oprec *pt = n_prec ? (oprec *)calloc((size_t)n_prec, sizeof(oprec)) : NULL;
+    for (int i = 0; i < n_prec; i++) {
+        const oracle_tree *q = &prec_trees[i];
+        if (tree_load(&pt[i].t, m, q->n_nodes, q->idx, q->child0, q->coefs, q->norms)) return 2;
+        prec_setup(&pt[i]);
+    }
+    double *pf = NULL;
+    size_t pf_cap = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -727,6 +790,12 @@ int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracl
                         get_node(&f, m, fk, tmp1, tmp2);
                     }
         }
+        /* precFunc of every work node (serially: getNode may generate) */
+        if (nwork > pf_cap) {
+            pf_cap = nwork;
+            pf = (double *)realloc(pf, sizeof(double) * pf_cap);
+        }
+        for (size_t w = 0; w < nwork; w++) pf[w] = prec_factor(pt, n_prec, m, g->idx[work[w]], tmp1, tmp2);
         double gsq = g->square_norm;
         unsigned long long comps = 0, nts = 0;
 #pragma omp parallel reduction(+ : comps, nts)
@@ -735,8 +804,8 @@ int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracl
             ostats ls = {0, 0};
 #pragma omp for schedule(dynamic, 1)
             for (long w = 0; w < (long)nwork; w += sample) {
-                calc_node(m, &o, &f, g, work[w], prec, gsq, scr, &ls);
-                if (count_terms) nts += count_node_terms(m, &o, &f, g, work[w], prec, gsq);
+                calc_node(m, &o, &f, g, work[w], prec, pf[w], gsq, scr, &ls);
+                if (count_terms) nts += count_node_terms(m, &o, &f, g, work[w], prec, pf[w], gsq);
             }
             comps += ls.components;
             free(scr);
@@ -760,7 +829,8 @@ int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracl
             int i = work[w];
             if (g->child0[i] >= 0) continue;
             if (g->idx[i].n + 2 > max_scale) continue;
-            if (split_check(g, i, prec, 1.0, abs_prec)) {
+            /* WaveletAdaptor::splitNode: split_check(node, prec * precFac, ...) */
+            if (split_check(g, i, prec * pf[w], 1.0, abs_prec)) {
                 int c0 = create_children(g, i, 0);
                 for (int c = 0; c < 8; c++) next[nn++] = c0 + c;
             }
@@ -771,6 +841,12 @@ int oracle_apply_sampled(const oracle_mra *m, const oracle_oper *od, const oracl
         iter++;
     }
     free(work);
+    free(pf);
+    for (int i = 0; i < n_prec; i++) {
+        tree_free(&pt[i].t);
+        free(pt[i].msq);
+    }
+    free(pt);
     R->iterations = iter;
     /* mwTransform(TopDown, false) */
     size_t cnt;

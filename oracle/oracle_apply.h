@@ -47,6 +47,11 @@ int oracle_apply_sampled(const oracle_mra *mra, const oracle_oper *oper, const o
                          double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, oracle_result **res);
 /* apply(out, DerivativeOperator, inp, dir): out0 holds the output roots; the
  * grid is copy-adapted from inp along dir, end nodes computed, then BottomUp. */
+/* the precTrees form of apply (apply.cpp:214-251): n_prec precision trees
+ * (coefficients and norms); n_prec = 0 is oracle_apply_sampled */
+int oracle_apply_prec(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
+                      double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, int n_prec,
+                      const oracle_tree *prec_trees, oracle_result **res);
 int oracle_apply_derivative(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, int dir, int order,
                             int nthreads, oracle_result **res);
 /* add (op 0) / multiply (op 1): out = sum / product of c[j] inps[j], adaptive

@@ -1,8 +1,8 @@
 """Writes tests/golden/mwfilters_ref.npz from the reference's shipped filter
 tables (share/mwfilters of MRChemSoft/mrcpp), for the orders the tests compare.
 
-Run in a checkout where the reference is available:
-    python tests/golden/make_golden.py /root/reference
+Run with the path of a checkout of the reference as its one argument:
+    python tests/golden/make_golden.py <mrcpp checkout>
 The fixture holds H0 and G0 (K x K, row-major as stored) and the left/right
 cross-correlation matrices (K^2 x 2K) for Legendre (L) and Interpolating (I).
 """
@@ -16,7 +16,9 @@ ORDERS_CC = [1, 3, 5, 7, 9]
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of an mrcpp checkout>")
+    ref = sys.argv[1]
     d = os.path.join(ref, "share", "mwfilters")
     out = {}
     for t in "LI":
