@@ -22,7 +22,10 @@ screening rules); the count is an integer that equals the oracle's.
   e2e        the same metric through mrcpp_gb300.apply (the host mirror of
              mrcpp::apply) with host buffers: input-tree upload, level
              norms and the output-tree download inside the timed region
-  fp64       the plain FP64 form on the same workload
+  fp64       the plain FP64 form on the same workload, on the same block
+             schedule as the mixed form (so mixed_vs_fp64 compares precision,
+             not algorithm); per_component_schedule: the FP64 form in the
+             reference's loop order, for comparison only
   roofline   the contraction kernel: algorithmic FLOP (96 (k+1)^4 per node-term)
              per launch / kernel time, against the measured bf16 dense peak
   cpu_baseline  the CPU oracle (port of the reference path) on the whole fixed
@@ -716,6 +719,12 @@ def main():
 
     ms_plan, st_plan, clk_plan, launches_plan, out_plan, pencil = plan_timed(mw.MIXED)
     ms_plan64, st_plan64, _, _, out_plan64, _ = plan_timed(mw.FP64)
+    # the FP64 form's per-component schedule (the reference's loop order), for comparison only
+    os.environ["MWGPU_FP64_COMPONENTS"] = "1"
+    try:
+        ms_plan64c, st_plan64c, _, _, out_plan64c, _ = plan_timed(mw.FP64)
+    finally:
+        os.environ.pop("MWGPU_FP64_COMPONENTS", None)
     # the mixed result against the closed-form potential at seeded points
     from cases import gaussian_sum
 
@@ -735,6 +744,7 @@ def main():
     t_level = reduce_max(pg, statistics.mean(ms_mixed))
     t_mixed = reduce_max(pg, statistics.mean(ms_plan))
     t_fp64 = reduce_max(pg, statistics.mean(ms_plan64))
+    t_fp64c = reduce_max(pg, statistics.mean(ms_plan64c))
     total_nt = reduce_sum(pg, node_terms)
     value = total_nt / (t_mixed / 1e3)
     value_fp64 = reduce_sum(pg, st_plan64.node_terms) / (t_fp64 / 1e3)
@@ -813,7 +823,13 @@ def main():
                         "ms_per_step": t_e2e * 1e3},
                 "step": "one planned level (mwgpu_plan_execute: GenNode values, work list, persistent contraction, reduction, "
                         "TopDown and BottomUp replayed as one CUDA graph)",
-                "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": t_fp64, "contract_ms": st_plan64.contract_ms},
+                "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": t_fp64, "contract_ms": st_plan64.contract_ms,
+                         "schedule": "block (the same grouped schedule as the mixed form, DFMA)",
+                         "per_component_schedule": {
+                             "value": reduce_sum(pg, st_plan64c.node_terms) / (t_fp64c / 1e3), "unit": UNIT, "ms_per_step": t_fp64c,
+                             "contract_ms": st_plan64c.contract_ms,
+                             "max_rel_diff": float(np.abs(out_plan64c - out_plan64).max() / np.abs(out_plan64).max()),
+                             "note": "the reference's loop order (per f component), for comparison only"}},
                 "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error": plan_l2, "max_node_error": plan_node_err},
                 "level_path": {"value": value_level, "fp64_value": value_level64, "unit": UNIT, "ms_per_step": t_level,
                                "rel_l2_error": rel_l2, "max_node_error": node_err,

@@ -6,6 +6,7 @@
  * reference API:
  *   mwh_apply          mrcpp::apply(prec, out, oper, inp, maxIter, absPrec)   src/treebuilders/apply.h:41
  *   mwh_apply_prec     mrcpp::apply(prec, out, oper, inp, precTrees, ...)      src/treebuilders/apply.h:43
+ *   mwh_ph, mwh_bs     mrcpp::PHOperator / BSOperator(MRA, order)              src/operators/PHOperator.h, BSOperator.h
  *   mwh_apply_batch    a loop of mrcpp::apply over functions, one device pass
  *   mwh_poisson        mrcpp::PoissonOperator(MRA, prec)                       src/operators/PoissonOperator.h:44
  *   mwh_helmholtz      mrcpp::HelmholtzOperator(MRA, mu, prec)                 src/operators/HelmholtzOperator.h:44
@@ -141,6 +142,18 @@ int mwh_helmholtz_kernel(double mu, double eps, double r_min, double r_max, int 
 
 /* mrcpp::apply on the GPU: precision = MWGPU_PREC_FP64 or MWGPU_PREC_MIXED. */
 int mwh_apply(double prec, mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int max_iter, int abs_prec, int precision, mwh_apply_stats *stats);
+/* Derivative operators from tabulated blocks: PHOperator(MRA, order)
+ * (src/operators/PHOperator.cpp:40-68, Holoborodko's smoothing derivative,
+ * order 1 or 2) and BSOperator(MRA, order) (BSOperator.cpp:40-68, B-spline
+ * derivative, order 1, 2 or 3).  Their S_+1, S_0, S_-1 tables are read from
+ * the reference's filter files <L|I>_ph_deriv_<order>.txt /
+ * <L|I>_b-spline-deriv<order>.txt in filter_dir (NULL: the MWFILTERS_DIR
+ * environment variable, as details::find_filters); mwh_deriv_tables takes the
+ * three (k+1) x (k+1) tables directly (row-major, element (i, j) as the
+ * calculators read it).  Apply with mwh_apply_derivative. */
+int mwh_ph(const mwh_mra *mra, int order, const char *filter_dir, mwh_oper **out);
+int mwh_bs(const mwh_mra *mra, int order, const char *filter_dir, mwh_oper **out);
+int mwh_deriv_tables(const mwh_mra *mra, int order, const double *s_p1, const double *s_0, const double *s_m1, mwh_oper **out);
 /* mrcpp::apply(prec, out, oper, inp, precTrees, maxIter, absPrec)
  * (src/treebuilders/apply.h:43, apply.cpp:214-251): the precision of output
  * node idx is scaled by precFac(idx) = 1 / max_i sqrt(getMaxSquareNorm) of the

@@ -174,6 +174,9 @@ _SIGS = {
     "mwh_poisson_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
     "mwh_helmholtz_kernel": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _PD, _PD]),
     "mwh_apply": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwh_ph": (C.c_int, [_P, C.c_int, C.c_char_p, C.POINTER(_P)]),
+    "mwh_bs": (C.c_int, [_P, C.c_int, C.c_char_p, C.POINTER(_P)]),
+    "mwh_deriv_tables": (C.c_int, [_P, C.c_int, _PD, _PD, _PD, C.POINTER(_P)]),
     "mwh_apply_prec": (C.c_int, [C.c_double, _P, _P, _P, C.c_int, _P, C.c_int, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwh_prec_factors": (C.c_int, [C.c_int, _P, C.c_int, _PI, _PD]),
     "mwh_apply_batch": (C.c_int, [C.c_double, C.c_int, C.POINTER(_P), _P, C.POINTER(_P), C.c_int, C.c_int, C.c_int,
@@ -513,6 +516,43 @@ class ABGVOperator(ConvolutionOperator):
         _ck(lib().mwh_abgv(mra._h, float(a), float(b), C.byref(h)))
         super().__init__(mra, h)
         self.a, self.b = a, b
+
+
+class PHOperator(ConvolutionOperator):
+    """PHOperator(MRA, order, filter_dir=None): Holoborodko's smoothing
+    derivative of order 1 or 2 (src/operators/PHOperator.cpp:40-68); its tables
+    are read from the reference's filter files in filter_dir (default: the
+    MWFILTERS_DIR environment variable).  Apply with apply(out, D, inp, dir)."""
+
+    def __init__(self, mra, order, filter_dir=None):
+        h = _P()
+        _ck(lib().mwh_ph(mra._h, int(order), None if filter_dir is None else os.fsencode(filter_dir), C.byref(h)))
+        super().__init__(mra, h)
+        self.order = order
+
+
+class BSOperator(ConvolutionOperator):
+    """BSOperator(MRA, order, filter_dir=None): the B-spline derivative of order
+    1, 2 or 3 (src/operators/BSOperator.cpp:40-68), tables as for PHOperator."""
+
+    def __init__(self, mra, order, filter_dir=None):
+        h = _P()
+        _ck(lib().mwh_bs(mra._h, int(order), None if filter_dir is None else os.fsencode(filter_dir), C.byref(h)))
+        super().__init__(mra, h)
+        self.order = order
+
+
+class TableDerivativeOperator(ConvolutionOperator):
+    """A derivative operator of the given order from the three blocks S_+1, S_0,
+    S_-1 ((k+1) x (k+1), as PHCalculator / BSCalculator read them)."""
+
+    def __init__(self, mra, order, s_p1, s_0, s_m1):
+        K = mra.kp1
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(K, K) for a in (s_p1, s_0, s_m1)]
+        h = _P()
+        _ck(lib().mwh_deriv_tables(mra._h, int(order), _pd(arrs[0]), _pd(arrs[1]), _pd(arrs[2]), C.byref(h)))
+        super().__init__(mra, h)
+        self.order = order
 
 
 def _kernel(fn, *args):

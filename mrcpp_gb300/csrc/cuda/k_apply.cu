@@ -14,6 +14,8 @@
 // the same three 1D applications.
 #include "mwgpu_internal.cuh"
 
+#include <cstdlib>
+
 namespace mwgpu {
 
 namespace {
@@ -31,6 +33,34 @@ __device__ __forceinline__ void tapply(TO *out, const TI *in, const double *F, i
         for (int i = 0; i < K; i++) s = fma((TC)a[i], (TC)__ldg(b + i), s);
         if (ADD) out[c + K2 * j] += (TO)s;
         else out[c + K2 * j] = (TO)s;
+    }
+}
+
+// One stage of the block schedule: up to 5 output blocks, each the sum of up
+// to 3 one-axis applications out[q] (=|+=) sum_p in[q][p]^T O[q][p] (the cyclic
+// axis order of tapply), all outputs in one pass of the CTA.  The operands are
+// listed in shared memory by thread 0.
+struct StageList {
+    const double *in[5][3];
+    const double *O[5][3];
+    double *out[5];
+    int np[5];
+    int nout;
+};
+
+template <bool ADD>
+__device__ __forceinline__ void stage_apply(const StageList &st, int K, int tid, int nthr) {
+    const int K2 = K * K, K3 = K2 * K;
+    for (int e = tid; e < st.nout * K3; e += nthr) {
+        const int q = e / K3, r = e - q * K3, c = r % K2, j = r / K2;
+        double s = 0.0;
+        for (int p = 0; p < st.np[q]; p++) {
+            const double *a = st.in[q][p] + K * c;
+            const double *b = st.O[q][p] + K * j;
+            for (int i = 0; i < K; i++) s = fma(a[i], __ldg(b + i), s);
+        }
+        if (ADD) st.out[q][r] += s;
+        else st.out[q][r] = s;
     }
 }
 
@@ -86,19 +116,36 @@ __global__ void k_band_missing(DevMRA m, DevOper op, DevTree f, DevTree g, const
     }
 }
 
-// One CTA per output node.  Shared memory: g accumulator 8K^3, x-intermediates
-// 2K^3, xy-intermediates 4K^3.
-// TC is the type of the 1D products and of the x / xy intermediates: double
-// for the plain form, float for the mixed form.  The g accumulator is FP64 in
-// both forms (the compensation that keeps the mixed form at FP32 product
-// accuracy instead of FP32 summation accuracy).
+// One CTA per output node.  Shared memory: g accumulator 8K^3, then either
+// the per-component intermediates (x 2K^3, xy 4K^3) or, with `block`, the
+// block schedule's 10K^3.
+//
+// Two schedules give the sum of the kept component products of
+// tensorApplyOperComp:
+// * block schedule, for a (f, term) whose kept components are all the
+//   structural ones (band widths, zero-norm f components, the depth rule;
+//   every item of a level without norm screening): per output x-bit a0,
+//     Y0[b1 b2]    = sum_b0 O^x_{a0 b0} f[b0 b1 b2]
+//     Y1[a1 b2]    = sum_b1 O^y_{a1 b1} Y0[b1 b2]
+//     g[a0 a1 a2] += sum_b2 O^z_{a2 b2} Y1[a1 b2]
+//   (48 K^4 FMA for a full node-term, against 112 K^4 for the per-component
+//   schedule), operator blocks outside their band and zero-norm f
+//   components left out of the sums.  At depth > 0 the (s, s) product
+//   (ft = gt = 0, ConvolutionCalculator.cpp:261) is not in the sums: f[000]'s
+//   x-step into a0 = 0 is kept apart as U0, enters the y step only toward
+//   a1 = 1, U1 = O^y_00 U0 enters the z step only toward a2 = 1, and the
+//   remaining O^z_00 U1 is never formed;
+// * per-component schedule otherwise: for each f component ft the x and xy
+//   intermediates shared by the kept g components.
+// TC is the type of the 1D products and of the x / xy intermediates of the
+// per-component schedule (double: the plain form).
 template <typename TC>
 // With nw_dev / gthr_dev the number of work entries and the threshold come from
 // the device (the grid is then a capacity); gthr_node holds one threshold per
 // work entry where the precision is scaled per output node (apply.cpp:221-228).
 __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree f, DevTree g, const int *work, int n_work,
                                                   double gthr, LevelStats *stats, int *err, const int *nw_dev, const double *gthr_dev,
-                                                  const double *gthr_node) {
+                                                  const double *gthr_node, bool block) {
     if (nw_dev && (int)blockIdx.x >= *nw_dev) return;
     if (gthr_dev) gthr = *gthr_dev;
     if (gthr_node) gthr = gthr_node[blockIdx.x];
@@ -107,10 +154,12 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
     double *gacc = sm;
     TC *X0 = (TC *)(gacc + 8 * K3);
     TC *X1 = X0 + 2 * K3;
+    double *Y0 = gacc + 8 * K3, *Y1 = Y0 + 4 * K3, *U0 = Y1 + 4 * K3, *U1 = U0 + K3;
     __shared__ int s_fid;
     __shared__ double s_fn[8];
-    __shared__ unsigned s_mask[2];
+    __shared__ unsigned s_mask[2], s_smask[2];
     __shared__ unsigned long long s_nt, s_nc;
+    __shared__ StageList s_st;
     const int gi = work[blockIdx.x];
     const int4 gx = g.idx[gi];
     for (int e = tid; e < 8 * K3; e += nthr) gacc[e] = 0.0;
@@ -160,22 +209,121 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
                             oNorm *= op.norms[(size_t)node * 4 + idx];
                         }
                     }
+                    const bool structural = pass;
                     if (pass) {
                         const double fThr = (double)op.band_size[((size_t)i * kMaxDepthRows + depth) * 64 + gt * 8 + ft] * fNorm;
                         const double upper = oNorm * fThr;
                         pass = upper > gthr;
                     }
-                    unsigned bal = __ballot_sync(0xffffffffu, pass);
-                    if ((tid & 31) == 0) s_mask[tid >> 5] = bal;
+                    unsigned bal = __ballot_sync(0xffffffffu, pass), sbal = __ballot_sync(0xffffffffu, structural);
+                    if ((tid & 31) == 0) {
+                        s_mask[tid >> 5] = bal;
+                        s_smask[tid >> 5] = sbal;
+                    }
                 }
                 __syncthreads();
                 const unsigned long long mask = (unsigned long long)s_mask[0] | ((unsigned long long)s_mask[1] << 32);
+                const unsigned long long smask = (unsigned long long)s_smask[0] | ((unsigned long long)s_smask[1] << 32);
                 if (mask == 0ull) { __syncthreads(); continue; }
                 if (tid == 0) { s_nt++; s_nc += __popcll(mask); }
                 const int L0 = op.dep_L[i * op.max_rows + depth];
                 const int off = op.dep_off[i * op.max_rows + depth];
                 const double *ob[3];
                 for (int d = 0; d < 3; d++) ob[d] = op.blocks + (size_t)(off + tl[d] + L0) * 4 * K2;
+                if (block && mask == smask) {
+                    // f components present and operator blocks inside their band
+                    auto fon = [&](int ft) { return !(s_fn[ft] < kMachineZero); };
+                    auto oon = [&](int d, int a, int bb) { return abs(tl[d]) <= bwi[2 * a + bb]; };
+                    const bool excl = depth != 0;
+                    for (int a0 = 0; a0 < 2; a0++) {
+                        // x step: Y0[b1 b2] (+ U0 for the excluded path)
+                        if (tid == 0) {
+                            StageList &st = s_st;
+                            st.nout = 0;
+                            for (int q = 0; q < 4; q++) {
+                                int np = 0;
+                                for (int b0 = 0; b0 < 2; b0++) {
+                                    const int ft = b0 + 2 * q;
+                                    if (!fon(ft) || !oon(0, a0, b0) || (excl && a0 == 0 && ft == 0)) continue;
+                                    st.in[q][np] = fc + (size_t)ft * K3;
+                                    st.O[q][np] = ob[0] + (2 * a0 + b0) * K2;
+                                    np++;
+                                }
+                                st.np[q] = np;
+                                st.out[q] = Y0 + q * K3;
+                            }
+                            st.nout = 4;
+                            if (excl && a0 == 0) {
+                                st.np[4] = (fon(0) && oon(0, 0, 0)) ? 1 : 0;
+                                st.in[4][0] = fc;
+                                st.O[4][0] = ob[0];
+                                st.out[4] = U0;
+                                st.nout = 5;
+                            }
+                        }
+                        __syncthreads();
+                        stage_apply<false>(s_st, K, tid, nthr);
+                        __syncthreads();
+                        // y step: Y1[a1 b2] = sum_b1 O^y_{a1 b1} Y0[b1 b2] (+ U0 toward a1 = 1; U1 = O^y_00 U0)
+                        if (tid == 0) {
+                            StageList &st = s_st;
+                            for (int q = 0; q < 4; q++) {
+                                const int a1 = q & 1, b2 = q >> 1;
+                                int np = 0;
+                                for (int b1 = 0; b1 < 2; b1++) {
+                                    if (!oon(1, a1, b1)) continue;
+                                    st.in[q][np] = Y0 + (b1 + 2 * b2) * K3;
+                                    st.O[q][np] = ob[1] + (2 * a1 + b1) * K2;
+                                    np++;
+                                }
+                                if (excl && a0 == 0 && a1 == 1 && b2 == 0 && oon(1, 1, 0)) {
+                                    st.in[q][np] = U0;
+                                    st.O[q][np] = ob[1] + 2 * K2;
+                                    np++;
+                                }
+                                st.np[q] = np;
+                                st.out[q] = Y1 + q * K3;
+                            }
+                            st.nout = 4;
+                            if (excl && a0 == 0) {
+                                st.np[4] = oon(1, 0, 0) ? 1 : 0;
+                                st.in[4][0] = U0;
+                                st.O[4][0] = ob[1];
+                                st.out[4] = U1;
+                                st.nout = 5;
+                            }
+                        }
+                        __syncthreads();
+                        stage_apply<false>(s_st, K, tid, nthr);
+                        __syncthreads();
+                        // z step: g[a0 a1 a2] += sum_b2 O^z_{a2 b2} Y1[a1 b2] (+ U1 toward a2 = 1)
+                        if (tid == 0) {
+                            StageList &st = s_st;
+                            for (int q = 0; q < 4; q++) {
+                                const int a1 = q & 1, a2 = q >> 1;
+                                int np = 0;
+                                for (int b2 = 0; b2 < 2; b2++) {
+                                    if (!oon(2, a2, b2)) continue;
+                                    st.in[q][np] = Y1 + (a1 + 2 * b2) * K3;
+                                    st.O[q][np] = ob[2] + (2 * a2 + b2) * K2;
+                                    np++;
+                                }
+                                if (excl && a0 == 0 && a1 == 0 && a2 == 1 && oon(2, 1, 0)) {
+                                    st.in[q][np] = U1;
+                                    st.O[q][np] = ob[2] + 2 * K2;
+                                    np++;
+                                }
+                                st.np[q] = np;
+                                st.out[q] = gacc + (a0 + 2 * a1 + 4 * a2) * K3;
+                            }
+                            st.nout = 4;
+                        }
+                        __syncthreads();
+                        stage_apply<true>(s_st, K, tid, nthr);
+                        __syncthreads();
+                    }
+                    continue;
+                }
                 for (int ft = 0; ft < 8; ft++) {
                     const unsigned gm = (unsigned)((mask >> (8 * ft)) & 0xffull);
                     if (gm == 0) continue;
@@ -349,9 +497,11 @@ void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, 
                           double gthr, LevelStats *stats, int *err, cudaStream_t s, const int *nw_dev, const double *gthr_dev,
                           const double *gthr_node) {
     if (n_work <= 0) return;
-    size_t smem = sizeof(double) * 14 * m.kp1_d;
+    // the block schedule where its 18 K^3 doubles fit (orders up to 10)
+    const bool block = sizeof(double) * 18 * (size_t)m.kp1_d <= 227 * 1024 && !std::getenv("MWGPU_FP64_COMPONENTS");
+    size_t smem = sizeof(double) * (block ? 18 : 14) * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err, nw_dev, gthr_dev, gthr_node);
+    k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err, nw_dev, gthr_dev, gthr_node, block);
 }
 
 }  // namespace mwgpu

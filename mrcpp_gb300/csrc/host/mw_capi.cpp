@@ -8,6 +8,8 @@
 // iteration (ConvolutionCalculator::calcNodeVector) runs on the GPU.
 #include <algorithm>
 #include <chrono>
+#include <fstream>
+#include <sstream>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -23,8 +25,17 @@ using namespace mwh;
 struct mwh_mra {
     MRA<3> m;
 };
+// A host tree and the device copy of it as an apply input (NodeAllocator's
+// device mirror, NodeAllocator.cpp:108-113): made by the first apply that
+// reads the tree, reused while `version` is unchanged (every host entry that
+// changes the tree bumps it), freed with the tree.
 struct mwh_tree {
     std::unique_ptr<Tree<3>> t;
+    unsigned long long version = 1;
+    mwgpu_tree *dev = nullptr;
+    unsigned long long dev_version = 0;
+    size_t dev_nodes = 0;
+    const double *dev_data = nullptr;
 };
 struct mwh_oper {
     std::unique_ptr<ConvolutionOperator> op;
@@ -221,6 +232,25 @@ mwgpu_tree *upload_input(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, const Tree<3>
     return dinp;
 }
 
+// the tree changes: its device input copy is stale
+void touch(mwh_tree *t) {
+    if (t) t->version++;
+}
+
+// the device input copy of a host tree: reused while the tree is unchanged,
+// else (re)uploaded; owned by the tree
+mwgpu_tree *resident_input(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwh_tree *inp, mwh_apply_stats &acc) {
+    const Tree<3> &t = *inp->t;
+    if (inp->dev && inp->dev_version == inp->version && inp->dev_nodes == t.nodes.size() && inp->dev_data == t.coefs.data()) return inp->dev;
+    if (inp->dev) mwgpu_free_tree(ctx, inp->dev);
+    inp->dev = nullptr;
+    inp->dev = upload_input(ctx, md, t, acc);
+    inp->dev_version = inp->version;
+    inp->dev_nodes = t.nodes.size();
+    inp->dev_data = t.coefs.data();
+    return inp->dev;
+}
+
 // output tree: the host ids are the device ids (nodes are only appended)
 mwgpu_tree *create_output(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, Tree<3> &out, mwh_apply_stats &acc) {
     out.clearGenerated();
@@ -280,12 +310,10 @@ struct PrecScale {
 // mrcpp::apply (apply.cpp:68-93) for nt independent (out, inp) pairs with one
 // operator.  Each TreeBuilder iteration of all trees still building is one
 // device level call; the transforms of all trees share their launches.
-// resume (nt = 1 only): continue the TreeBuilder loop of an apply whose
-// earlier iterations ran elsewhere (device trees, work, iteration and norms).
 // scale (nt = 1 only): the precTrees form (apply.cpp:214-251), the precision
 // scaled per output node in the screening and in the split test.
 int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree **inps, int max_iter, int abs_prec, int precision,
-               mwh_apply_stats *stats, const BuildState *resume = nullptr, const PrecScale *scale = nullptr) {
+               mwh_apply_stats *stats, const PrecScale *scale = nullptr) {
     if (scale && nt != 1) return fail(1, "precision trees need a single (out, inp) pair");
     ConvolutionOperator &op = *operp->op;
     for (int t = 0; t < nt; t++) {
@@ -307,20 +335,17 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     unsigned long long l0 = 0, l1 = 0;
     mwgpu_launch_count(ctx, &l0);
     std::vector<BuildState> bs(nt);
+    for (int t = 0; t < nt; t++) touch(outs[t]);
+    // the input trees' device copies belong to the trees
     auto release = [&] {
         for (auto &b : bs) {
             if (b.dout) mwgpu_free_tree(ctx, b.dout);
-            if (b.dinp) mwgpu_free_tree(ctx, b.dinp);
             b.dout = b.dinp = nullptr;
         }
     };
     try {
         for (int t = 0; t < nt; t++) {
             BuildState &b = bs[t];
-            if (resume) {
-                b = *resume;
-                continue;
-            }
             b.tree = outs[t]->t.get();
             // room for the refinement without moving the coefficients on every
             // growth step (untouched capacity costs no memory; a fixed grid
@@ -330,7 +355,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
                 b.tree->nodes.reserve(guess);
                 b.tree->coefs.reserve(guess * (size_t)b.tree->nCoefs);
             }
-            b.dinp = upload_input(ctx, md, *inps[t]->t, acc);
+            b.dinp = resident_input(ctx, md, inps[t], acc);
             ht.mark("input");
             b.dout = create_output(ctx, md, *b.tree, acc);
             ht.mark("output");
@@ -788,7 +813,14 @@ int mwh_tree_create(const mwh_mra *m, mwh_tree **out) {
     });
 }
 
-void mwh_tree_free(mwh_tree *t) { delete t; }
+void mwh_tree_free(mwh_tree *t) {
+    if (!t) return;
+    if (t->dev) {
+        std::lock_guard<std::mutex> lk(g_gpu_mu);
+        if (g_ctx) mwgpu_free_tree(g_ctx, t->dev);
+    }
+    delete t;
+}
 
 static GaussExp<3> make_gexp(int n, const double *coef, const double *ex, const double *pos) {
     GaussExp<3> g;
@@ -797,6 +829,7 @@ static GaussExp<3> make_gexp(int n, const double *coef, const double *ex, const 
 }
 
 int mwh_build_grid_gauss(mwh_tree *t, int n, const double *coef, const double *ex, const double *pos) {
+    touch(t);
     return guard([&] {
         if (!t || n < 0 || (n > 0 && (!coef || !ex || !pos))) return fail(1, "invalid Gaussian list");
         build_grid(*t->t, make_gexp(n, coef, ex, pos));
@@ -805,6 +838,7 @@ int mwh_build_grid_gauss(mwh_tree *t, int n, const double *coef, const double *e
 }
 
 int mwh_project_gauss(double prec, mwh_tree *t, int n, const double *coef, const double *ex, const double *pos, int max_iter, int abs_prec) {
+    touch(t);
     return guard([&] {
         if (!t || n < 0 || (n > 0 && (!coef || !ex || !pos))) return fail(1, "invalid Gaussian list");
         auto g = make_gexp(n, coef, ex, pos);
@@ -814,6 +848,7 @@ int mwh_project_gauss(double prec, mwh_tree *t, int n, const double *coef, const
 }
 
 int mwh_project_func(double prec, mwh_tree *t, mwh_func f, void *user, int max_iter, int abs_prec) {
+    touch(t);
     return guard([&] {
         if (!t || !f) return fail(1, "invalid projection arguments");
         project_batched<3>(prec, *t->t, [f, user](long long n, const double *r, double *v) { f(n, r, v, user); }, max_iter, abs_prec != 0);
@@ -823,6 +858,7 @@ int mwh_project_func(double prec, mwh_tree *t, mwh_func f, void *user, int max_i
 
 int mwh_project_gauss_device(double prec, mwh_tree *t, int n, const double *coef, const double *ex, const double *pos, int max_iter, int abs_prec,
                              mwh_apply_stats *stats) {
+    touch(t);
     return guard([&] {
         if (!t || n < 0 || (n > 0 && (!coef || !ex || !pos))) return fail(1, "invalid Gaussian list");
         return project_device_impl(prec, *t->t, n, coef, ex, pos, max_iter, abs_prec != 0, stats);
@@ -830,6 +866,7 @@ int mwh_project_gauss_device(double prec, mwh_tree *t, int n, const double *coef
 }
 
 int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats) {
+    touch(out);
     return guard([&] {
         if (!out || n < 1 || !c || !inps) return fail(1, "invalid sum");
         for (int j = 0; j < n; j++)
@@ -839,6 +876,7 @@ int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const 
 }
 
 int mwh_multiply(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats) {
+    touch(out);
     return guard([&] {
         if (!out || n < 1 || !c || !inps) return fail(1, "invalid product");
         for (int j = 0; j < n; j++)
@@ -848,6 +886,7 @@ int mwh_multiply(double prec, mwh_tree *out, int n, const double *c, mwh_tree *c
 }
 
 int mwh_copy_grid(mwh_tree *out, const mwh_tree *inp) {
+    touch(out);
     return guard([&] {
         if (!out || !inp) return fail(1, "null argument");
         copy_grid(*out->t, *inp->t);
@@ -866,6 +905,7 @@ int mwh_tree_info(const mwh_tree *t, int *n, double *sq) {
 }
 
 int mwh_tree_rescale(mwh_tree *t, double c) {
+    touch(t);
     return guard([&] {
         if (!t) return fail(1, "null tree");
         auto &tr = *t->t;
@@ -898,6 +938,7 @@ int mwh_tree_export(const mwh_tree *t, int *idx, int *child0, double *coefs, dou
 }
 
 int mwh_tree_import(mwh_tree *t, int n, const int *idx, const int *child0, const double *coefs, double square_norm) {
+    touch(t);
     return guard([&] {
         if (!t || n <= 0 || !idx || !child0) return fail(1, "invalid flat tree");
         auto nt = std::make_unique<Tree<3>>(*t->t->mra);
@@ -980,6 +1021,7 @@ int mwh_tree_save(const mwh_tree *t, const char *file) {
 }
 
 int mwh_tree_load(mwh_tree *t, const char *file) {
+    touch(t);
     return guard([&] {
         if (!t || !file) return fail(1, "null argument");
         const std::string path = tree_path(file);
@@ -1081,7 +1123,87 @@ int mwh_abgv(const mwh_mra *m, double a, double b, mwh_oper **out) {
     });
 }
 
+int mwh_deriv_tables(const mwh_mra *m, int order, const double *s_p1, const double *s_0, const double *s_m1, mwh_oper **out) {
+    return guard([&] {
+        if (!m || !out || !s_p1 || !s_0 || !s_m1 || order < 1) return fail(1, "invalid derivative table arguments");
+        const int K = m->m.kp1();
+        Mat a(K, K), b(K, K), c(K, K);
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) {
+                a(i, j) = s_p1[i * K + j];
+                b(i, j) = s_0[i * K + j];
+                c(i, j) = s_m1[i * K + j];
+            }
+        auto *o = new mwh_oper{make_table_derivative(m->m, order, a, b, c), {}, {}, {}, {}};
+        finish_oper(o);
+        *out = o;
+        return 0;
+    });
+}
+
+// PHCalculator::readSMatrix / BSCalculator::readSMatrix (PHCalculator.cpp:44-74,
+// BSCalculator.cpp:44-74): the file holds, for (k+1) = 2, 3, ..., a line with
+// k+1 and then 3(k+1) rows of k+1 numbers: S_+1, S_0, S_-1
+static int read_deriv_tables(const std::string &file, int K, int kp1_end, Mat &s_p1, Mat &s_0, Mat &s_m1) {
+    std::ifstream ifs(file.c_str());
+    if (!ifs) return fail(1, "Failed to open file: " + file);
+    for (int kp1 = 2; kp1 < kp1_end; kp1++) {
+        std::string line;
+        std::getline(ifs, line);
+        std::istringstream head(line);
+        int order = -1;
+        head >> order;
+        if (order != kp1) return fail(1, "Orders do not match in " + file);
+        Mat data(3 * kp1, kp1);
+        for (int i = 0; i < 3 * kp1; i++) {
+            std::getline(ifs, line);
+            std::istringstream row(line);
+            for (int j = 0; j < kp1; j++) row >> data(i, j);
+            if (!row) return fail(1, "Malformed table in " + file);
+        }
+        if (kp1 == K) {
+            s_p1 = Mat(K, K);
+            s_0 = Mat(K, K);
+            s_m1 = Mat(K, K);
+            for (int i = 0; i < K; i++)
+                for (int j = 0; j < K; j++) {
+                    s_p1(i, j) = data(i, j);
+                    s_0(i, j) = data(K + i, j);
+                    s_m1(i, j) = data(2 * K + i, j);
+                }
+            return 0;
+        }
+    }
+    return fail(1, "Scaling order not supported");
+}
+
+static int table_operator(const mwh_mra *m, int order, const char *filter_dir, bool ph, mwh_oper **out) {
+    return guard([&] {
+        if (!m || !out) return fail(1, "null argument");
+        const int max_order = ph ? 2 : 3;
+        if (order < 1 || order > max_order) return fail(1, ph ? "PH derivative order must be 1 or 2" : "B-spline derivative order must be 1, 2 or 3");
+        std::string dir = filter_dir ? filter_dir : "";
+        if (dir.empty()) {
+            const char *env = std::getenv("MWFILTERS_DIR");
+            if (env) dir = env;
+        }
+        if (dir.empty()) return fail(1, "no filter directory (argument or MWFILTERS_DIR)");
+        const char t = m->m.basis->type == Legendre ? 'L' : 'I';
+        const std::string file = dir + "/" + t + (ph ? "_ph_deriv_" : "_b-spline-deriv") + std::to_string(order) + ".txt";
+        Mat a, b, c;
+        if (int rc = read_deriv_tables(file, m->m.kp1(), ph ? 30 : 21, a, b, c)) return rc;
+        auto *o = new mwh_oper{make_table_derivative(m->m, order, a, b, c), {}, {}, {}, {}};
+        finish_oper(o);
+        *out = o;
+        return 0;
+    });
+}
+
+int mwh_ph(const mwh_mra *m, int order, const char *filter_dir, mwh_oper **out) { return table_operator(m, order, filter_dir, true, out); }
+int mwh_bs(const mwh_mra *m, int order, const char *filter_dir, mwh_oper **out) { return table_operator(m, order, filter_dir, false, out); }
+
 int mwh_apply_derivative(mwh_tree *out, mwh_oper *oper, mwh_tree *inp, int dir, mwh_apply_stats *stats) {
+    touch(out);
     return guard([&] {
         if (!out || !oper || !inp) return fail(1, "null argument");
         return apply_derivative_impl(out, oper, inp, dir, stats);
@@ -1178,7 +1300,7 @@ int mwh_apply_prec(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp,
             ps.msq.push_back(prec_trees[i]->t->maxSquareNorms());  // makeMaxSquareNorms (apply.cpp:221)
         }
         mwh_tree *outs[1] = {outp}, *inps[1] = {inpp};
-        return apply_impl(prec, 1, outs, operp, inps, max_iter, abs_prec, precision, stats, nullptr, &ps);
+        return apply_impl(prec, 1, outs, operp, inps, max_iter, abs_prec, precision, stats, &ps);
     });
 }
 
@@ -1267,6 +1389,7 @@ int mwh_grid_features(double prec, mwh_tree *gridp, mwh_oper *operp, mwh_tree *i
 
 int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, const mwh_mlp *mlpc, double threshold, int full_levels,
                       int abs_prec, int precision, mwh_learned_stats *stats) {
+    touch(outp);
     return guard([&] {
         if (!outp || !operp || !inpp || !mlpc) return fail(1, "null argument");
         mwh_mlp *mlp = const_cast<mwh_mlp *>(mlpc);

@@ -300,6 +300,10 @@ std::unique_ptr<ConvolutionOperator> make_poisson(const MRA<3> &mra, double prec
 std::unique_ptr<ConvolutionOperator> make_helmholtz(const MRA<3> &mra, double mu, double prec);
 // ABGVOperator(mra, a, b) (ABGVOperator.cpp:45-71): first derivative, band 0 (a = b = 0) or 1
 std::unique_ptr<ConvolutionOperator> make_abgv(const MRA<3> &mra, double a, double b);
+// PHOperator / BSOperator (PHOperator.cpp:46-68, BSOperator.cpp:46-68): derivative
+// of order `order` from the tables S_+1, S_0, S_-1 ((k+1) x (k+1), element (i, j)
+// as PHCalculator / BSCalculator read it) of the basis
+std::unique_ptr<ConvolutionOperator> make_table_derivative(const MRA<3> &mra, int order, const Mat &s_p1, const Mat &s_0, const Mat &s_m1);
 // ConvolutionOperator(mra, kernel, prec) (ConvolutionOperator.cpp:51-62)
 std::unique_ptr<ConvolutionOperator> make_convolution(const MRA<3> &mra, const std::vector<GaussFunc<1>> &kernel, double prec);
 // ConvolutionOperator::initialize (ConvolutionOperator.cpp:78-108), k_prec/o_prec given

@@ -281,17 +281,53 @@ static double legendre_deriv(int m, double t) {
 // derivative with boundary parameters a, b, node by node from
 // ABGVCalculator::calcNode (ABGVCalculator.cpp:118-170), refined along the
 // diagonal only (BandWidthAdaptor.h:35-52: split where l0 = 0 and 2 |dl| <= bw).
-std::unique_ptr<ConvolutionOperator> make_abgv(const MRA<3> &mra, double a, double b) {
+// A derivative operator from its blocks: the operator tree of
+// DerivativeOperator::initialize (ABGVOperator.cpp:45-71, PHOperator.cpp:46-68,
+// BSOperator.cpp:46-68): nodes with l = l1 - l0 in {-1, 0, 1} get the blocks
+// `fill` writes (component c, element (i, j) at c K^2 + i K + j), scaled by
+// 2^(order (n+1)) and compressed (the calculators' calcNode); the tree is
+// refined by BandWidthAdaptor(bw) (BandWidthAdaptor.h:45-50).
+static std::unique_ptr<ConvolutionOperator> make_derivative(const MRA<3> &mra, int order, int bw,
+                                                            const std::function<void(int, double *)> &fill) {
     auto op = std::make_unique<ConvolutionOperator>();
     op->mra = mra;
     op->operRoot = mra.rootScale();
     op->operReach = 1;
     op->buildPrec = MachineZero;
-    op->derivOrder = 1;
+    op->derivOrder = order;
+    const ScalingBasis &basis = *mra.basis;
+    const double sf = mra.world.sf[0];
+    MRA<2> omra(BoundingBox<2>(op->operRoot, {0, 0}, {op->operReach + 1, op->operReach + 1}, {sf, sf}), basis.type, mra.order());
+    Tree<2> otree(omra);
+    otree.componentNorm = [](const Tree<2> &t, int i, int c) { return oper_component_norm(t, i, c, MachineZero); };
+    auto calc = [&](Tree<2> &t, const std::vector<int> &work) {
+        for (int node : work) {
+            double *coefs = t.c(node);
+            std::fill(coefs, coefs + t.nCoefs, 0.0);
+            const auto &nd = t.nodes[node];
+            const int l = nd.l[1] - nd.l[0];
+            if (l >= -1 && l <= 1) fill(l, coefs);
+            const double two_np1 = std::pow(2.0, order * (nd.n + 1));
+            for (int j = 0; j < t.nCoefs; j++) coefs[j] *= two_np1;
+            t.mwTransformNode(node, Compression);
+            t.nodes[node].flags |= F_HASCOEFS;
+            t.calcNorms(node);
+        }
+    };
+    auto split = [bw](const Tree<2> &t, int i) {
+        const auto &n = t.nodes[i];
+        return n.l[0] == 0 && 2 * std::abs(n.l[0] - n.l[1]) <= bw;
+    };
+    tree_build<2>(otree, otree.endNodes(), calc, split, -1, omra.maxScale());
+    op->terms.push_back(term_from_tree(otree, op->operRoot, mra.kp1()));
+    op->bandPrec = -2.0;
+    return op;
+}
+
+std::unique_ptr<ConvolutionOperator> make_abgv(const MRA<3> &mra, double a, double b) {
     const int bw = (std::fabs(a) > MachineZero || std::fabs(b) > MachineZero) ? 1 : 0;
     const ScalingBasis &basis = *mra.basis;
     const int K = mra.kp1(), type = basis.type;
-    const double sf = mra.world.sf[0];
     // value vectors and K matrix (ABGVCalculator.cpp:48-116)
     std::vector<double> v0(K), v1(K);
     Mat Km(K, K);
@@ -322,54 +358,56 @@ std::unique_ptr<ConvolutionOperator> make_abgv(const MRA<3> &mra, double a, doub
                 Km(i, j) = 2.0 * std::sqrt(basis.weights[j]) * std::sqrt(basis.weights[i]) * d;
             }
     }
-    MRA<2> omra(BoundingBox<2>(op->operRoot, {0, 0}, {op->operReach + 1, op->operReach + 1}, {sf, sf}), type, mra.order());
-    Tree<2> otree(omra);
-    otree.componentNorm = [](const Tree<2> &t, int i, int c) { return oper_component_norm(t, i, c, MachineZero); };
     const int K2 = K * K;
-    auto calc = [&](Tree<2> &t, const std::vector<int> &work) {
-        for (int node : work) {
-            double *coefs = t.c(node);
-            std::fill(coefs, coefs + t.nCoefs, 0.0);
-            const auto &nd = t.nodes[node];
-            const double two_np1 = std::pow(2.0, nd.n + 1);
-            switch (nd.l[1] - nd.l[0]) {
-                case 1:
-                    if (b > MachineZero)
-                        for (int i = 0; i < K; i++)
-                            for (int j = 0; j < K; j++) coefs[1 * K2 + i * K + j] = -b * v0[i] * v1[j];
-                    break;
-                case 0:
+    auto fill = [&](int l, double *coefs) {
+        switch (l) {
+            case 1:
+                if (b > MachineZero)
                     for (int i = 0; i < K; i++)
-                        for (int j = 0; j < K; j++) {
-                            const double diag = (1.0 - a) * v1[i] * v1[j] - (1.0 - b) * v0[i] * v0[j] - Km(i, j);
-                            coefs[0 * K2 + i * K + j] = diag;
-                            coefs[1 * K2 + i * K + j] = a * v1[i] * v0[j];
-                            coefs[2 * K2 + i * K + j] = -b * v0[i] * v1[j];
-                            coefs[3 * K2 + i * K + j] = diag;
-                        }
-                    break;
-                case -1:
-                    if (a > MachineZero)
-                        for (int i = 0; i < K; i++)
-                            for (int j = 0; j < K; j++) coefs[2 * K2 + i * K + j] = a * v1[i] * v0[j];
-                    break;
-                default:
-                    break;
-            }
-            for (int j = 0; j < t.nCoefs; j++) coefs[j] *= two_np1;
-            t.mwTransformNode(node, Compression);
-            t.nodes[node].flags |= F_HASCOEFS;
-            t.calcNorms(node);
+                        for (int j = 0; j < K; j++) coefs[1 * K2 + i * K + j] = -b * v0[i] * v1[j];
+                break;
+            case 0:
+                for (int i = 0; i < K; i++)
+                    for (int j = 0; j < K; j++) {
+                        const double diag = (1.0 - a) * v1[i] * v1[j] - (1.0 - b) * v0[i] * v0[j] - Km(i, j);
+                        coefs[0 * K2 + i * K + j] = diag;
+                        coefs[1 * K2 + i * K + j] = a * v1[i] * v0[j];
+                        coefs[2 * K2 + i * K + j] = -b * v0[i] * v1[j];
+                        coefs[3 * K2 + i * K + j] = diag;
+                    }
+                break;
+            default:  // l = -1
+                if (a > MachineZero)
+                    for (int i = 0; i < K; i++)
+                        for (int j = 0; j < K; j++) coefs[2 * K2 + i * K + j] = a * v1[i] * v0[j];
+                break;
         }
     };
-    auto split = [bw](const Tree<2> &t, int i) {
-        const auto &n = t.nodes[i];
-        return n.l[0] == 0 && 2 * std::abs(n.l[0] - n.l[1]) <= bw;
+    return make_derivative(mra, 1, bw, fill);
+}
+
+std::unique_ptr<ConvolutionOperator> make_table_derivative(const MRA<3> &mra, int order, const Mat &s_p1, const Mat &s_0, const Mat &s_m1) {
+    const int K = mra.kp1(), K2 = K * K;
+    if (s_p1.rows != K || s_p1.cols != K || s_0.rows != K || s_0.cols != K || s_m1.rows != K || s_m1.cols != K)
+        throw Error(1, "derivative tables must be (k+1) x (k+1)");
+    // PHCalculator::calcNode / BSCalculator::calcNode (PHCalculator.cpp:80-127, BSCalculator.cpp:83-127)
+    auto fill = [&](int l, double *coefs) {
+        for (int i = 0; i < K; i++)
+            for (int j = 0; j < K; j++) {
+                const int e = i * K + j;
+                if (l == 1) {
+                    coefs[1 * K2 + e] = s_p1(i, j);
+                } else if (l == 0) {
+                    coefs[0 * K2 + e] = s_0(i, j);
+                    coefs[1 * K2 + e] = s_m1(i, j);
+                    coefs[2 * K2 + e] = s_p1(i, j);
+                    coefs[3 * K2 + e] = s_0(i, j);
+                } else {
+                    coefs[2 * K2 + e] = s_m1(i, j);
+                }
+            }
     };
-    tree_build<2>(otree, otree.endNodes(), calc, split, -1, omra.maxScale());
-    op->terms.push_back(term_from_tree(otree, op->operRoot, K));
-    op->bandPrec = -2.0;
-    return op;
+    return make_derivative(mra, order, 1, fill);
 }
 
 std::unique_ptr<ConvolutionOperator> make_poisson(const MRA<3> &mra, double prec) {

@@ -144,7 +144,7 @@ class Prepared:
         self.m, self.o, self.ft, self.gt = m, o, ft, gt
         self.out_sqnorm = float(out_sqnorm)
 
-    def run(self, nthreads=0, count_terms=True, sample=1, export=True, fast=False, deriv_dir=None):
+    def run(self, nthreads=0, count_terms=True, sample=1, export=True, fast=False, deriv_dir=None, deriv_order=1):
         L = lib(fast)
         res = C.c_void_p()
         if deriv_dir is None:
@@ -152,8 +152,8 @@ class Prepared:
                                      self.max_iter, self.abs_prec, int(nthreads), int(bool(count_terms)), int(sample), self.n_prec, self.pt,
                                      C.byref(res))
         else:
-            rc = L.oracle_apply_derivative(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), int(deriv_dir), 1,
-                                           int(nthreads), C.byref(res))
+            rc = L.oracle_apply_derivative(C.byref(self.m), C.byref(self.o), C.byref(self.ft), C.byref(self.gt), int(deriv_dir),
+                                           int(deriv_order), int(nthreads), C.byref(res))
         if rc != 0:
             raise RuntimeError("oracle_apply failed with code %d" % rc)
         n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()
@@ -179,9 +179,10 @@ def apply(prec, out, oper, inp, max_iter=-1, abs_prec=False, nthreads=0, count_t
 
 
 def apply_derivative(out, oper, inp, dir, nthreads=0):
-    """Oracle apply(out, DerivativeOperator, inp, dir) (first derivative):
-    `out` holds only its roots; returns the flat copy-adapted output tree."""
-    return Prepared(1.0, out, oper, inp).run(nthreads, deriv_dir=dir)
+    """Oracle apply(out, DerivativeOperator, inp, dir), of the operator's order
+    (`oper.order`, 1 when absent): `out` holds only its roots; returns the flat
+    copy-adapted output tree."""
+    return Prepared(1.0, out, oper, inp).run(nthreads, deriv_dir=dir, deriv_order=getattr(oper, "order", 1))
 
 
 def combine(op, prec, out, terms, max_iter=-1, abs_prec=False):

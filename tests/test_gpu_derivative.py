@@ -66,3 +66,47 @@ def test_derivative_after_mixed_apply(gpu):
     assert same
     mx, _ = rel_errors(g.export()["coefs"], ref["coefs"][perm])
     assert mx <= FP64_TOL
+
+
+# PHOperator / BSOperator (src/operators/PHOperator.cpp, BSOperator.cpp) from
+# the reference's tables (tests/golden/deriv_tables_ref.npz, written into a
+# filter directory in the reference's file format)
+def _table_operator(tmp_path, mra, kind, n, t, k):
+    from test_deriv_tables import filter_dir
+
+    d = filter_dir(tmp_path, t, kind, n, k)
+    return (mw.PHOperator if kind == "ph" else mw.BSOperator)(mra, n, d)
+
+
+@pytest.mark.parametrize("kind,n", [("ph", 1), ("ph", 2), ("bs", 1), ("bs", 2), ("bs", 3)])
+@pytest.mark.parametrize("basis,t,k", [(mw.LEGENDRE, "L", 7), (mw.INTERPOLATING, "I", 5)])
+def test_table_derivatives_gpu_vs_oracle(gpu, tmp_path, kind, n, basis, t, k):
+    mra = mw.MRA(box=(-20, 20), order=k, basis=basis)
+    f = project(mra, 1e-4, gaussian_sum(17, 3, (1.0, 30.0), (-2.0, 2.0)))
+    D = _table_operator(tmp_path, mra, kind, n, t, k)
+    for d in (0, 2):
+        g = mw.FunctionTree(mra)
+        st = mw.apply(g, D, f, d)
+        ref = oracle.apply_derivative(mw.FunctionTree(mra), D, f, d)
+        gx = g.export()
+        same, perm = match(gx, ref)
+        assert same, "output grid differs from the oracle"
+        mx, l2 = rel_errors(gx["coefs"], ref["coefs"][perm])
+        assert mx <= FP64_TOL and l2 <= FP64_TOL, (kind, n, d, mx, l2)
+        assert st["node_terms"] == ref["node_terms"] and st["components"] == ref["components"]
+
+
+@pytest.mark.parametrize("n,tol", [(1, 1e-4), (2, 1e-3), (3, 1e-2)])
+def test_bspline_derivative_known_answer(gpu, tmp_path, n, tol):
+    # d^n/dx^n of exp(-r^2) (the B-spline derivative is the one for smooth functions)
+    mra = mw.MRA(box=(-20, 20), order=7, basis=mw.LEGENDRE)
+    f = project(mra, 1e-6, [(1.0, 1.0, (0.0, 0.0, 0.0))])
+    D = _table_operator(tmp_path, mra, "bs", n, "L", 7)
+    g = mw.FunctionTree(mra)
+    mw.apply(g, D, f, 0)
+    rng = np.random.default_rng(3)
+    pts = 0.8 * rng.normal(size=(300, 3))
+    x, e = pts[:, 0], np.exp(-(pts ** 2).sum(-1))
+    exact = {1: -2.0 * x * e, 2: (4.0 * x * x - 2.0) * e, 3: (-8.0 * x ** 3 + 12.0 * x) * e}[n]
+    got = np.array([g.evalf(p) for p in pts])
+    assert np.linalg.norm(got - exact) / np.linalg.norm(exact) < tol
