@@ -93,6 +93,10 @@ int mwh_project_func(double prec, mwh_tree *tree, mwh_func f, void *user, int ma
  * computations and BottomUp on the device (mwgpu_combine_level). */
 int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats);
 int mwh_multiply(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, int abs_prec, mwh_apply_stats *stats);
+/* multiply(..., useMaxNorms = true) (multiply.cpp:104-108): the grid is
+ * refined by MultiplicationAdaptor (MultiplicationAdaptor.h:45-65) from the
+ * two inputs' max norms (makeMaxSquareNorms); n must be 2. */
+int mwh_multiply_max_norms(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, mwh_apply_stats *stats);
 int mwh_copy_grid(mwh_tree *out, const mwh_tree *inp);
 /* FunctionTree::rescale(c) (src/trees/FunctionTree.cpp:651-668): every stored
  * coefficient times c, norms and square norm recomputed. */

@@ -152,6 +152,7 @@ _SIGS = {
     "mwh_copy_grid": (C.c_int, [_P, _P]),
     "mwh_add": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwh_multiply": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwh_multiply_max_norms": (C.c_int, [C.c_double, _P, C.c_int, _PD, C.POINTER(_P), C.c_int, C.POINTER(MwhApplyStats)]),
     "mwgpu_combine_level": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P), _PD, _PD, _PD, _P, _PI, C.c_int, _PD]),
     "mwh_project_gauss_device": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
     "mwgpu_project_level": (C.c_int, [_P, _P, C.c_int, _PD, _PD, _PD, _PI, C.c_int, _PD]),
@@ -411,10 +412,18 @@ def add(prec, out, *args, max_iter=-1, abs_prec=False):
     return _combine(lib().mwh_add, prec, out, terms, max_iter, abs_prec)
 
 
-def multiply(prec, out, *args, max_iter=-1, abs_prec=False):
+def multiply(prec, out, *args, max_iter=-1, abs_prec=False, use_max_norms=False):
     """multiply(prec, out, c, A, B) or multiply(prec, out, [(c, tree), ...]) (src/treebuilders/multiply.cpp):
-    out = product of c_j f_j, built adaptively on the GPU; returns the statistics."""
+    out = product of c_j f_j, built adaptively on the GPU; returns the statistics.
+    use_max_norms: the grid from the two inputs' max norms (MultiplicationAdaptor,
+    two factors, abs_prec not used), else the wavelet adaptor."""
     terms = args[0] if len(args) == 1 else [(args[0], args[1]), (1.0, args[2])]
+    if use_max_norms:
+        c = np.ascontiguousarray([float(t[0]) for t in terms], dtype=np.float64)
+        hs = (_P * len(terms))(*[t[1]._h for t in terms])
+        st = MwhApplyStats()
+        _ck(lib().mwh_multiply_max_norms(float(prec), out._h, len(terms), _pd(c), hs, int(max_iter), C.byref(st)))
+        return st.as_dict()
     return _combine(lib().mwh_multiply, prec, out, terms, max_iter, abs_prec)
 
 

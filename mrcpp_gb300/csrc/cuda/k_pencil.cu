@@ -1,6 +1,7 @@
 // Pencil contraction of the mixed form for order K = 8 (k = 7): the x step
-// on the 5th-generation tensor cores with the operator terms stacked along N,
-// the y and z steps in FP32 on the CUDA cores, concurrently.
+// on the 5th-generation tensor cores (tcgen05) with the operator terms
+// stacked along N, the y and z steps as warp-level tensor-core products
+// (mma.sync) in the consumer warps, concurrently with the next x step.
 //
 // What it computes.  For one output node g, one band cell l = (l_x, l_y, l_z)
 // and one operator term i, the reference adds (ConvolutionCalculator.cpp:

@@ -356,6 +356,10 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
                 b.tree->coefs.reserve(guess * (size_t)b.tree->nCoefs);
             }
             b.dinp = resident_input(ctx, md, inps[t], acc);
+            // each apply makes its own GenNodes, as the reference deletes them at
+            // the end of apply (apply.cpp:86-87): statistics do not depend on
+            // earlier applies
+            ck(mwgpu_tree_clear_generated(ctx, b.dinp), "clear generated nodes");
             ht.mark("input");
             b.dout = create_output(ctx, md, *b.tree, acc);
             ht.mark("output");
@@ -678,10 +682,25 @@ int project_device_impl(double prec, Tree<3> &tree, int n, const double *coef, c
 // the node computations on the device: TreeBuilder + WaveletAdaptor on the
 // host, AdditionCalculator / MultiplicationCalculator::calcNode per iteration
 // through mwgpu_combine_level, BottomUp on the device
+// max_norms: multiply's MultiplicationAdaptor (multiply.cpp:104-108,
+// MultiplicationAdaptor.h:45-65) instead of the wavelet adaptor: a node splits
+// when maxW0 maxS1 + maxW1 maxS0 + maxW0 maxW1 > prec (max norms of the two
+// inputs at the node after makeMaxSquareNorms; a node an input lacks has its
+// generated scaling norm and no wavelet norm) and one input has children
+// there.  (The reference counts an input node with generated children as
+// a branch too; on an output tree that starts from its root nodes no such node
+// is tested, so the rules agree.)
 int combine_device_impl(int op, double prec, Tree<3> &out, int n, const double *c, mwh_tree *const *inps, int max_iter, bool abs_prec,
-                        mwh_apply_stats *stats) {
+                        mwh_apply_stats *stats, bool max_norms = false) {
     for (int j = 0; j < n; j++)
         if (!(*inps[j]->t->mra == *out.mra)) return fail(1, "Incompatible MRA");
+    if (max_norms && (op != MWGPU_COMBINE_MULTIPLY || n != 2)) return fail(1, "Invalid tree vec size: the max-norm adaptor multiplies two functions");
+    std::vector<double> msq[2], mwsq[2];
+    if (max_norms)
+        for (int j = 0; j < 2; j++) {
+            msq[j] = inps[j]->t->maxSquareNorms();
+            mwsq[j] = inps[j]->t->maxWSquareNorms();
+        }
     auto t0 = std::chrono::steady_clock::now();
     const MRA<3> &mra = *out.mra;
     const ScalingBasis &basis = *mra.basis;
@@ -723,7 +742,28 @@ int combine_device_impl(int op, double prec, Tree<3> &out, int n, const double *
             }
             acc.iterations++;
         };
-        auto split = [prec, abs_prec](const Tree<3> &t, int i) { return split_check(t, i, prec, 1.0, abs_prec); };
+        auto split = [&](const Tree<3> &t, int i) {
+            if (!max_norms) return split_check(t, i, prec, 1.0, abs_prec);
+            const auto &nd = t.nodes[i];
+            double S[2], W[2];
+            bool leaf[2];
+            for (int j = 0; j < 2; j++) {
+                const Tree<3> &f = *inps[j]->t;
+                const int id = f.find(nd.n, nd.l);
+                if (id >= 0) {
+                    S[j] = std::sqrt(msq[j][id]);
+                    W[j] = std::sqrt(mwsq[j][id]);
+                    const int c0 = f.nodes[id].child0;
+                    leaf[j] = c0 < 0 || f.isGen(c0);
+                } else {
+                    S[j] = std::sqrt(f.genScaledSquareNorm(nd.n, nd.l));
+                    W[j] = 0.0;
+                    leaf[j] = true;
+                }
+            }
+            const double multNorm = W[0] * S[1] + W[1] * S[0] + W[0] * W[1];
+            return multNorm > prec && !(leaf[0] && leaf[1]);
+        };
         tree_build<3>(out, out.endNodes(), calc, split, max_iter, mra.maxScale());
         sync_new(ctx, b, acc);
         ck(mwgpu_transform(ctx, b.dout, MWGPU_BOTTOMUP, 1), "BottomUp transform");
@@ -872,6 +912,16 @@ int mwh_add(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const 
         for (int j = 0; j < n; j++)
             if (!inps[j]) return fail(1, "null input tree");
         return combine_device_impl(MWGPU_COMBINE_ADD, prec, *out->t, n, c, inps, max_iter, abs_prec != 0, stats);
+    });
+}
+
+int mwh_multiply_max_norms(double prec, mwh_tree *out, int n, const double *c, mwh_tree *const *inps, int max_iter, mwh_apply_stats *stats) {
+    touch(out);
+    return guard([&] {
+        if (!out || n < 1 || !c || !inps) return fail(1, "null argument");
+        for (int j = 0; j < n; j++)
+            if (!inps[j] || inps[j] == out) return fail(1, "invalid input tree");
+        return combine_device_impl(MWGPU_COMBINE_MULTIPLY, prec, *out->t, n, c, inps, max_iter, false, stats, true);
     });
 }
 

@@ -198,7 +198,10 @@ template <int D> struct Tree {
     // (MWTree.cpp:536-543, MWNode.cpp:1257-1269, MWNode.h:84,212): the largest
     // 2^(D n) |node|^2 over the node and its real descendants; GenNodes get
     // their own scaled square norm
-    std::vector<double> maxSquareNorms() const;
+    std::vector<double> maxSquareNorms() const { return maxNorms(false); }
+    // the same over the wavelet part alone (maxWSquareNorm, MWNode.h:85,213)
+    std::vector<double> maxWSquareNorms() const { return maxNorms(true); }
+    std::vector<double> maxNorms(bool wavelet) const;
     // the scaled square norm 2^(D n) |s|^2 of the node (n, l) where it is
     // missing: its scaling block made from the deepest existing ancestor as
     // getNode would generate it (the tree is not changed)

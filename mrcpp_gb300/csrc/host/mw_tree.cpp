@@ -139,11 +139,11 @@ template <int D> void Tree<D>::giveChildrenCoefs(int i, bool overwrite) {
     }
 }
 
-template <int D> std::vector<double> Tree<D>::maxSquareNorms() const {
+template <int D> std::vector<double> Tree<D>::maxNorms(bool wavelet) const {
     std::vector<double> msq(nodes.size(), -1.0);
-    auto scaled = [this](int i) {
+    auto scaled = [this, wavelet](int i) {
         double sq = 0.0;
-        for (int c = 0; c < tDim; c++) sq += nodes[i].norms[c] * nodes[i].norms[c];
+        for (int c = wavelet ? 1 : 0; c < tDim; c++) sq += nodes[i].norms[c] * nodes[i].norms[c];
         return std::ldexp(1.0, D * nodes[i].n) * sq;
     };
     // deepest level first, so that every child is done before its parent

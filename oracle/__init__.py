@@ -67,6 +67,8 @@ def lib(fast=False):
         L.oracle_combine.restype = C.c_int
         L.oracle_combine.argtypes = [C.POINTER(OracleMra), C.c_int, C.c_int, C.POINTER(OracleTree), _PD, _PD, _PD, C.POINTER(OracleTree),
                                      C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        L.oracle_combine_ex.restype = C.c_int
+        L.oracle_combine_ex.argtypes = L.oracle_combine.argtypes[:11] + [C.c_int, C.POINTER(C.c_void_p)]
         L.oracle_result_free.restype = None
         L.oracle_result_free.argtypes = [C.c_void_p]
         _libs[path] = L
@@ -185,9 +187,10 @@ def apply_derivative(out, oper, inp, dir, nthreads=0):
     return Prepared(1.0, out, oper, inp).run(nthreads, deriv_dir=dir, deriv_order=getattr(oper, "order", 1))
 
 
-def combine(op, prec, out, terms, max_iter=-1, abs_prec=False):
+def combine(op, prec, out, terms, max_iter=-1, abs_prec=False, use_max_norms=False):
     """Oracle add (op 0) / multiply (op 1) of terms [(c, FunctionTree), ...] from
-    the grid of `out`; returns the flat result tree."""
+    the grid of `out` (use_max_norms: multiply's max-norm adaptor); returns the
+    flat result tree."""
     mra = out.mra
     d = mra.desc()
     m = OracleMra()
@@ -209,8 +212,8 @@ def combine(op, prec, out, terms, max_iter=-1, abs_prec=False):
     gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
     res = C.c_void_p()
     L = lib()
-    rc = L.oracle_combine(C.byref(m), int(op), len(terms), trees, _pd(c), _pd(cv), _pd(vc), C.byref(gt), float(prec), int(max_iter),
-                          int(bool(abs_prec)), C.byref(res))
+    rc = L.oracle_combine_ex(C.byref(m), int(op), len(terms), trees, _pd(c), _pd(cv), _pd(vc), C.byref(gt), float(prec), int(max_iter),
+                             int(bool(abs_prec)), int(bool(use_max_norms)), C.byref(res))
     if rc != 0:
         raise RuntimeError("oracle_combine failed with code %d" % rc)
     n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()

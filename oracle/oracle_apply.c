@@ -1102,14 +1102,53 @@ static void combine_node(const oracle_mra *m, int op, int n_in, otree *f, const 
     calc_norms(g, gi);
 }
 
+/* makeMaxSquareNorms (MWNode.cpp:1257-1269) of the loaded nodes of t: the
+   largest 2^(3n) |node|^2 (wavelet = 1: wavelet part only) over the node and
+   its descendants */
+static double *max_norms(const otree *t, int wavelet) {
+    size_t cnt;
+    int *lvl, nl;
+    int *order = bfs(t, &cnt, &lvl, &nl);
+    double *mx = (double *)malloc(sizeof(double) * (t->n + 1));
+    for (int L = nl - 1; L >= 0; L--)
+        for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+            int i = order[q];
+            double v = ldexp(1.0, 3 * t->idx[i].n) * (wavelet ? wavelet_norm(t, i) : t->sqn[i]);
+            int c0 = t->child0[i];
+            if (c0 >= 0 && !t->gen[c0])
+                for (int k = 0; k < 8; k++) v = fmax(v, mx[c0 + k]);
+            mx[i] = v;
+        }
+    free(order);
+    free(lvl);
+    return mx;
+}
+
 /* add (add.cpp:58-83) / multiply with the wavelet adaptor (multiply.cpp:70-101):
    TreeBuilder from the end nodes of out0, then BottomUp and the square norm */
 int oracle_combine(const oracle_mra *m, int op, int n_in, const oracle_tree *inps, const double *c, const double *cv_map, const double *vc_map,
                    const oracle_tree *out0, double prec, int max_iter, int abs_prec, oracle_result **res) {
+    return oracle_combine_ex(m, op, n_in, inps, c, cv_map, vc_map, out0, prec, max_iter, abs_prec, 0, res);
+}
+
+/* use_max_norms: multiply(..., useMaxNorms) (multiply.cpp:104-108) with
+   MultiplicationAdaptor::splitNode (MultiplicationAdaptor.h:45-65) */
+int oracle_combine_ex(const oracle_mra *m, int op, int n_in, const oracle_tree *inps, const double *c, const double *cv_map,
+                      const double *vc_map, const oracle_tree *out0, double prec, int max_iter, int abs_prec, int use_max_norms,
+                      oracle_result **res) {
     if (!m || !inps || !c || !cv_map || !vc_map || !out0 || !res || n_in < 1) return 1;
+    if (use_max_norms && (op != 1 || n_in != 2)) return 1;
     otree *f = (otree *)calloc((size_t)n_in, sizeof(otree));
     for (int j = 0; j < n_in; j++)
         if (tree_load(&f[j], m, inps[j].n_nodes, inps[j].idx, inps[j].child0, inps[j].coefs, inps[j].norms)) return 2;
+    double *msq[2] = {NULL, NULL}, *mwsq[2] = {NULL, NULL};
+    size_t n_real[2] = {0, 0};
+    if (use_max_norms)
+        for (int j = 0; j < 2; j++) {
+            msq[j] = max_norms(&f[j], 0);
+            mwsq[j] = max_norms(&f[j], 1);
+            n_real[j] = f[j].n;
+        }
     oracle_result *R = (oracle_result *)calloc(1, sizeof(oracle_result));
     if (tree_load(&R->g, m, out0->n_nodes, out0->idx, out0->child0, NULL, NULL)) return 2;
     otree *g = &R->g;
@@ -1145,7 +1184,30 @@ int oracle_combine(const oracle_mra *m, int op, int n_in, const oracle_tree *inp
         for (size_t w = 0; w < nwork; w++) {
             int i = work[w];
             if (g->child0[i] >= 0 || g->idx[i].n + 2 > m->max_scale) continue;
-            if (split_check(g, i, prec, 1.0, abs_prec)) {
+            int split;
+            if (use_max_norms) {
+                /* getNode (generating) of both inputs; getMaxSquareNorm / getMaxWSquareNorm
+                   (MWNode.h:84-85): a generated node's own scaled norms */
+                double S[2], W[2];
+                int leaf[2];
+                for (int j = 0; j < 2; j++) {
+                    int id = get_node(&f[j], m, g->idx[i], t1, t2);
+                    double sc = ldexp(1.0, 3 * g->idx[i].n);
+                    if ((size_t)id < n_real[j] && !f[j].gen[id]) {
+                        S[j] = sqrt(msq[j][id]);
+                        W[j] = sqrt(mwsq[j][id]);
+                    } else {
+                        S[j] = sqrt(sc * f[j].sqn[id]);
+                        W[j] = sqrt(sc * wavelet_norm(&f[j], id));
+                    }
+                    leaf[j] = f[j].child0[id] < 0; /* isLeafNode: generated children count */
+                }
+                double multNorm = W[0] * S[1] + W[1] * S[0] + W[0] * W[1];
+                split = multNorm > prec && !(leaf[0] && leaf[1]);
+            } else {
+                split = split_check(g, i, prec, 1.0, abs_prec);
+            }
+            if (split) {
                 int c0 = create_children(g, i, 0);
                 for (int q = 0; q < 8; q++) next[nn++] = c0 + q;
             }
@@ -1173,6 +1235,10 @@ int oracle_combine(const oracle_mra *m, int op, int n_in, const oracle_tree *inp
     free(order_);
     free(lvl);
     free(bufs);
+    for (int j = 0; j < 2; j++) {
+        free(msq[j]);
+        free(mwsq[j]);
+    }
     for (int j = 0; j < n_in; j++) tree_free(&f[j]);
     free(f);
     *res = R;

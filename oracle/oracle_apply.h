@@ -58,6 +58,10 @@ int oracle_apply_derivative(const oracle_mra *mra, const oracle_oper *oper, cons
  * from out0's end nodes at prec; cv_map / vc_map the basis's value maps. */
 int oracle_combine(const oracle_mra *mra, int op, int n_in, const oracle_tree *inps, const double *c, const double *cv_map, const double *vc_map,
                    const oracle_tree *out0, double prec, int max_iter, int abs_prec, oracle_result **res);
+/* use_max_norms = 1: multiply of two functions with the max-norm adaptor */
+int oracle_combine_ex(const oracle_mra *mra, int op, int n_in, const oracle_tree *inps, const double *c, const double *cv_map,
+                      const double *vc_map, const oracle_tree *out0, double prec, int max_iter, int abs_prec, int use_max_norms,
+                      oracle_result **res);
 int oracle_result_info(const oracle_result *r, int *n_nodes, double *square_norm, unsigned long long *node_terms,
                        unsigned long long *components, int *iterations);
 int oracle_result_export(const oracle_result *r, int *idx, int *child0, double *coefs, double *norms);
