@@ -298,6 +298,18 @@ def closed_form(gs, x):
     return v
 
 
+def plan_tuning(L, plan):
+    """The plan's autotuning candidates: [chunk items, schedule, ms] and the chosen one."""
+    import ctypes as C
+
+    n = C.c_int(32)
+    items, sched, ms, chosen = (C.c_longlong * 32)(), (C.c_int * 32)(), (C.c_double * 32)(), C.c_int()
+    if L.mwgpu_plan_tuning(plan, C.byref(n), items, sched, ms, C.byref(chosen)) != 0:
+        return None
+    names = {1: "pencil+items", 0: "items"}
+    return {"candidates": [[int(items[i]), names[sched[i]], round(float(ms[i]), 4)] for i in range(n.value)], "chosen": int(chosen.value)}
+
+
 def split_bound(achieved, bf16_peak):
     """The mixed form's own bound: each logical FP32 product is 3 TF32
     tensor-core products (hi*hi, hi*lo, lo*hi), and the TF32 rate is half the
@@ -395,6 +407,7 @@ def main_batch(args, rank, world, local, pg):
     per, grid, ncand, lpe = C.c_longlong(), C.c_int(), C.c_int(8), C.c_ulonglong()
     cand_items, cand_ms = (C.c_longlong * 8)(), (C.c_double * 8)()
     ck(L.mwgpu_plan_info(plan, C.byref(per), C.byref(grid), C.byref(ncand), cand_items, cand_ms, C.byref(lpe)))
+    tune = plan_tuning(L, plan)
     scrub = 256 << 20
 
     def step():
@@ -497,8 +510,7 @@ def main_batch(args, rank, world, local, pg):
                            "node_terms_per_step": int(node_terms), "components_per_step": int(st.components),
                            "l2": "256 MiB scrub between steps", "parallelism": "replicas" if world > 1 else "single",
                            "plan": {"chunk_items": per.value, "persistent_grid": grid.value, "create_s": t_plan,
-                                    "autotune": [[int(cand_items[i]), float(cand_ms[i])] for i in range(ncand.value)],
-                                    "launches_per_step": int(lpe.value)},
+                                    "autotune": tune, "launches_per_step": int(lpe.value)},
                            "setup_s": time.perf_counter() - t_setup},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "ms_per_step": t_e2e * 1e3},
@@ -721,11 +733,12 @@ def main():
         ck(L.mwgpu_plan_check(ctx, plan, C.byref(pst)))
         pnt, pms = C.c_ulonglong(), C.c_double()
         ck(L.mwgpu_plan_pencil_info(plan, C.byref(pnt), C.byref(pms)))
+        tune = plan_tuning(L, plan)
         out = np.zeros((n_out, 8 * K ** 3))
         ck(L.mwgpu_download_tree(ctx, dout, mw._pd(out), None))
         ck(L.mwgpu_plan_destroy(ctx, plan))
         barrier(pg)
-        return ms, pst, cs.summary(), (l1.value - l0.value), out, (pnt.value, pms.value)
+        return ms, pst, cs.summary(), (l1.value - l0.value), out, (pnt.value, pms.value, tune)
 
     ms_plan, st_plan, clk_plan, launches_plan, out_plan, pencil = plan_timed(mw.MIXED)
     ms_plan64, st_plan64, _, _, out_plan64, _ = plan_timed(mw.FP64)
@@ -834,6 +847,7 @@ def main():
                         "ms_per_step": t_e2e * 1e3},
                 "step": "one planned level (mwgpu_plan_execute: GenNode values, work list, persistent contraction, reduction, "
                         "TopDown and BottomUp replayed as one CUDA graph)",
+                "autotune": pencil[2],
                 "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": t_fp64, "contract_ms": st_plan64.contract_ms,
                          "schedule": "block (the same grouped schedule as the mixed form, DFMA)",
                          "per_component_schedule": {

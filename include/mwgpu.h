@@ -196,6 +196,14 @@ mwgpu_status mwgpu_combine_level(mwgpu_ctx *ctx, int op, int n_in, mwgpu_tree *c
  * (project.cpp:47-66). */
 mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *vc_map, const double *roots,
                                  const int *node_ix, int n, double *norms_out);
+/* The same level for any function the caller can evaluate (the
+ * RepresentableFunction of ProjectionCalculator, ProjectionCalculator.cpp:
+ * 40-43, lives on the host): values[8 (k+1)^3 j + (k+1)^3 ct + qx + (k+1) qy
+ * + (k+1)^2 qz] = f at the point of child ct of node node_ix[j], coordinate d
+ * = sf 2^-(n+1) (root[q_d] + 2 l_d + bit_d(ct)) (MWNode::getExpandedChildPts,
+ * MWNode.cpp:854-935). */
+mwgpu_status mwgpu_project_level_values(mwgpu_ctx *ctx, mwgpu_tree *tree, const double *values, const double *vc_map, const double *roots,
+                                        const int *node_ix, int n, double *norms_out);
 
 /* Derivative level: replaces DerivativeCalculator::calcNodeVector
  * (src/treebuilders/DerivativeCalculator.cpp:113-151) for the output end nodes
@@ -233,8 +241,10 @@ mwgpu_status mwgpu_transform_batch(mwgpu_ctx *ctx, int n_trees, mwgpu_tree *cons
  * only on the topology: the input trees' GenNode keys and slots (earlier
  * GenNodes of the input trees are dropped first), the band pair offsets,
  * buffer capacities (work list: 1.25x the planned size) and, with
- * MWGPU_PLAN_AUTOTUNE, the chunk length of the persistent contraction launch,
- * chosen by timing candidates on this level.  The level is then captured as
+ * MWGPU_PLAN_AUTOTUNE, the schedule of the contraction (for order 7 on
+ * levels without norm screening: pencil and item kernels, or the item
+ * kernel alone) and the chunk length of the persistent item kernel, chosen
+ * by timing every combination on the whole contraction of this level.  The level is then captured as
  * one CUDA graph: GenNode values from the current input coefficients,
  * screening and work list, contraction (one persistent launch for all trees),
  * chunk reduction and norms, and with MWGPU_PLAN_TRANSFORMS the TopDown(add)
@@ -269,6 +279,11 @@ mwgpu_status mwgpu_plan_pencil_info(const mwgpu_plan *plan, unsigned long long *
  * in = room in the arrays, out = number tried) and kernel launches per execution. */
 mwgpu_status mwgpu_plan_info(const mwgpu_plan *plan, long long *chunk_items, int *grid, int *n_candidates, long long *cand_items,
                              double *cand_ms, unsigned long long *launches);
+/* The autotuning candidates of a plan: per candidate the chunk length, the
+ * schedule (1: pencil + item kernels, 0: item kernel alone) and the time of
+ * the contraction in ms; chosen = the index in use (-1 without autotuning).
+ * n_candidates: in = room in the arrays (any may be NULL), out = number tried. */
+mwgpu_status mwgpu_plan_tuning(const mwgpu_plan *plan, int *n_candidates, long long *chunk_items, int *schedule, double *ms, int *chosen);
 mwgpu_status mwgpu_plan_destroy(mwgpu_ctx *ctx, mwgpu_plan *plan);
 /* New coefficients (and norms, or NULL to compute them) of all nodes of an
  * input tree with unchanged topology; refreshes the FP32 copy.  GenNodes are

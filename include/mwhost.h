@@ -86,6 +86,11 @@ int mwh_project_gauss_device(double prec, mwh_tree *tree, int n, const double *c
  * (ProjectionCalculator::calcNode) and the final BottomUp run on the host. */
 typedef void (*mwh_func)(long long n, const double *r, double *values, void *user);
 int mwh_project_func(double prec, mwh_tree *tree, mwh_func f, void *user, int max_iter, int abs_prec);
+/* The same with the node computations on the device: per TreeBuilder
+ * iteration f is evaluated on the host at every child quadrature point of the
+ * level (mwgpu_project_level_values), the transforms, norms and the final
+ * BottomUp run on the GPU. */
+int mwh_project_func_device(double prec, mwh_tree *tree, mwh_func f, void *user, int max_iter, int abs_prec, mwh_apply_stats *stats);
 /* add(prec, out, FunctionTreeVector, maxIter, absPrec) (src/treebuilders/add.cpp:58-83)
  * and multiply(prec, out, FunctionTreeVector, maxIter, absPrec) with the
  * wavelet adaptor (multiply.cpp:70-101): out = sum_j c[j] inps[j] or

@@ -112,6 +112,7 @@ _SIGS = {
     "mwgpu_plan_check": (C.c_int, [_P, _P, C.POINTER(MwgpuLevelStats)]),
     "mwgpu_plan_info": (C.c_int, [_P, C.POINTER(C.c_longlong), _PI, _PI, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_ulonglong)]),
     "mwgpu_plan_pencil_info": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _PD]),
+    "mwgpu_plan_tuning": (C.c_int, [_P, _PI, C.POINTER(C.c_longlong), _PI, _PD, _PI]),
     "mwgpu_plan_destroy": (C.c_int, [_P, _P]),
     "mwgpu_tree_update_coefs": (C.c_int, [_P, _P, _PD, _PD]),
     "mwgpu_apply_judged": (C.c_int, [_P, _P, _P, _P, C.c_int, _PI, C.c_double, C.c_int, C.c_int, _PD, C.c_int, _PI, _PI, _PD,
@@ -146,6 +147,8 @@ _SIGS = {
     "mwh_build_grid_gauss": (C.c_int, [_P, C.c_int, _PD, _PD, _PD]),
     "mwh_project_gauss": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int]),
     "mwh_project_func": (C.c_int, [C.c_double, _P, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "mwh_project_func_device": (C.c_int, [C.c_double, _P, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(MwhApplyStats)]),
+    "mwgpu_project_level_values": (C.c_int, [_P, _P, _PD, _PD, _PD, _PI, C.c_int, _PD]),
     "mwh_tree_rescale": (C.c_int, [_P, C.c_double]),
     "mwh_convolution": (C.c_int, [_P, C.c_int, _PD, _PD, C.c_double, C.POINTER(_P)]),
     "mwh_mra_distances": (C.c_int, [_P, C.c_double, _PD, _PD]),
@@ -355,7 +358,7 @@ def build_grid(tree, gaussians):
 _FUNC = C.CFUNCTYPE(None, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
 
 
-def _project_func(prec, tree, func, max_iter, abs_prec):
+def _project_func(prec, tree, func, max_iter, abs_prec, device=False):
     errors = []
 
     def cb(n, r, v, _user):
@@ -367,10 +370,15 @@ def _project_func(prec, tree, func, max_iter, abs_prec):
             errors.append(e)
 
     f = _FUNC(cb)
-    code = lib().mwh_project_func(float(prec), tree._h, C.cast(f, C.c_void_p), None, int(max_iter), int(bool(abs_prec)))
+    st = MwhApplyStats()
+    if device:
+        code = lib().mwh_project_func_device(float(prec), tree._h, C.cast(f, C.c_void_p), None, int(max_iter), int(bool(abs_prec)), C.byref(st))
+    else:
+        code = lib().mwh_project_func(float(prec), tree._h, C.cast(f, C.c_void_p), None, int(max_iter), int(bool(abs_prec)))
     if errors:
         raise errors[0]
     _ck(code)
+    return st.as_dict() if device else None
 
 
 def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True, device=False):
@@ -380,12 +388,11 @@ def project(prec, tree, gaussians, max_iter=-1, abs_prec=False, grid=True, devic
 
     gaussians may also be a function: project(prec, tree, func) with func
     taking an (n, 3) array of points and returning n values is
-    project(prec, tree, std::function) (project.cpp:59-63), projected on the
-    host from the tree's current grid (no grid is built for it)."""
+    project(prec, tree, std::function) (project.cpp:59-63), from the tree's
+    current grid (no grid is built for it); device=True evaluates func on the
+    host per level and computes the nodes on the GPU (mwgpu_project_level_values)."""
     if callable(gaussians):
-        if device:
-            raise ValueError("functions are projected on the host; device=True takes Gaussians")
-        return _project_func(prec, tree, gaussians, max_iter, abs_prec)
+        return _project_func(prec, tree, gaussians, max_iter, abs_prec, device)
     if grid:
         build_grid(tree, gaussians)
     coef, ex, pos = _gauss_arrays(gaussians)

@@ -36,6 +36,9 @@ __device__ __forceinline__ void tapply(TO *out, const TI *in, const double *F, i
     }
 }
 
+// the block schedule runs where its 18 K^3 doubles of shared memory fit: K <= 11
+constexpr int kBlockMaxK = 11;
+
 // One stage of the block schedule: up to 5 output blocks, each the sum of up
 // to 3 one-axis applications out[q] (=|+=) sum_p in[q][p]^T O[q][p] (the cyclic
 // axis order of tapply), all outputs in one pass of the CTA.  The operands are
@@ -48,19 +51,55 @@ struct StageList {
     int nout;
 };
 
-template <bool ADD>
+// Thread t owns output column j = t % K of every block and rows c = t / K +
+// m (nthr / K): the operator column of the current input stays in registers,
+// and the K threads that share a row c read the same shared-memory words (the
+// rows of consecutive threads would be K doubles apart, a 16-way bank
+// conflict for K = 8).  The inputs of an output are added one after the other
+// by the thread that owns the element.
+template <bool ADD, int KM>
 __device__ __forceinline__ void stage_apply(const StageList &st, int K, int tid, int nthr) {
-    const int K2 = K * K, K3 = K2 * K;
-    for (int e = tid; e < st.nout * K3; e += nthr) {
-        const int q = e / K3, r = e - q * K3, c = r % K2, j = r / K2;
-        double s = 0.0;
-        for (int p = 0; p < st.np[q]; p++) {
-            const double *a = st.in[q][p] + K * c;
-            const double *b = st.O[q][p] + K * j;
-            for (int i = 0; i < K; i++) s = fma(a[i], __ldg(b + i), s);
+    const int K2 = K * K;
+    const int groups = nthr / K;  // threads per column
+    const int j = tid % K, c0 = tid / K;
+    if (c0 >= groups) return;
+    for (int q = 0; q < st.nout; q++) {
+        const int np = st.np[q];
+        double *out = st.out[q] + K2 * j;
+        if (np == 0) {
+            if (!ADD)
+                for (int c = c0; c < K2; c += groups) out[c] = 0.0;
+            continue;
         }
-        if (ADD) st.out[q][r] += s;
-        else st.out[q][r] = s;
+        for (int p = 0; p < np; p++) {
+            double b[KM];
+#pragma unroll
+            for (int i = 0; i < KM; i++) b[i] = i < K ? __ldg(st.O[q][p] + K * j + i) : 0.0;
+            const double *in = st.in[q][p];
+            const bool store = !ADD && p == 0;
+            for (int c = c0; c < K2; c += groups) {
+                const double *a = in + K * c;
+                double s = 0.0;
+#pragma unroll
+                for (int i = 0; i < KM; i++)
+                    if (i < K) s = fma(a[i], b[i], s);
+                if (store) out[c] = s;
+                else out[c] += s;
+            }
+        }
+    }
+}
+
+// stage_apply with the operator columns sized for K
+template <bool ADD>
+__device__ __forceinline__ void stage_apply_k(const StageList &st, int K, int tid, int nthr) {
+    switch (K) {
+        case 2: stage_apply<ADD, 2>(st, K, tid, nthr); break;
+        case 4: stage_apply<ADD, 4>(st, K, tid, nthr); break;
+        case 6: stage_apply<ADD, 6>(st, K, tid, nthr); break;
+        case 8: stage_apply<ADD, 8>(st, K, tid, nthr); break;
+        case 10: stage_apply<ADD, 10>(st, K, tid, nthr); break;
+        default: stage_apply<ADD, kBlockMaxK>(st, K, tid, nthr); break;
     }
 }
 
@@ -262,7 +301,7 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
                             }
                         }
                         __syncthreads();
-                        stage_apply<false>(s_st, K, tid, nthr);
+                        stage_apply_k<false>(s_st, K, tid, nthr);
                         __syncthreads();
                         // y step: Y1[a1 b2] = sum_b1 O^y_{a1 b1} Y0[b1 b2] (+ U0 toward a1 = 1; U1 = O^y_00 U0)
                         if (tid == 0) {
@@ -294,7 +333,7 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
                             }
                         }
                         __syncthreads();
-                        stage_apply<false>(s_st, K, tid, nthr);
+                        stage_apply_k<false>(s_st, K, tid, nthr);
                         __syncthreads();
                         // z step: g[a0 a1 a2] += sum_b2 O^z_{a2 b2} Y1[a1 b2] (+ U1 toward a2 = 1)
                         if (tid == 0) {
@@ -319,7 +358,7 @@ __global__ void __launch_bounds__(256) k_contract(DevMRA m, DevOper op, DevTree 
                             st.nout = 4;
                         }
                         __syncthreads();
-                        stage_apply<true>(s_st, K, tid, nthr);
+                        stage_apply_k<true>(s_st, K, tid, nthr);
                         __syncthreads();
                     }
                     continue;
@@ -498,7 +537,7 @@ void launch_contract_fp64(const DevMRA &m, const DevOper &op, const DevTree &f, 
                           const double *gthr_node) {
     if (n_work <= 0) return;
     // the block schedule where its 18 K^3 doubles fit (orders up to 10)
-    const bool block = sizeof(double) * 18 * (size_t)m.kp1_d <= 227 * 1024 && !std::getenv("MWGPU_FP64_COMPONENTS");
+    const bool block = m.K <= kBlockMaxK && sizeof(double) * 18 * (size_t)m.kp1_d <= 227 * 1024 && !std::getenv("MWGPU_FP64_COMPONENTS");
     size_t smem = sizeof(double) * (block ? 18 : 14) * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_contract<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_contract<double><<<n_work, 256, smem, s>>>(m, op, f, g, work, n_work, gthr, stats, err, nw_dev, gthr_dev, gthr_node, block);

@@ -177,6 +177,14 @@ __device__ __forceinline__ void mma3x(float (&d)[4], const float (&ah)[4], const
     mma16(d, ah, bl);
     mma16(d, ah, bh);
 }
+// the same with the two correction products in their own accumulator dl (d + dl
+// is the sum): two dependency chains instead of one
+__device__ __forceinline__ void mma3x2(float (&d)[4], float (&dl)[4], const float (&ah)[4], const float (&al)[4], const float (&bh)[2],
+                                       const float (&bl)[2]) {
+    mma16(dl, al, bh);
+    mma16(d, ah, bh);
+    mma16(dl, ah, bl);
+}
 
 // padded N of a tensor-core product with n terms (M = 128 needs N % 16 == 0)
 __host__ __device__ constexpr int n_pad(int n) { return (CPT * n + 15) / 16 * 16; }
@@ -542,10 +550,11 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
 #pragma unroll
                     for (int xi = 0; xi < 2; xi++) {
                         const int x = x0 + xi;
+                        float Cl[2][4];
 #pragma unroll
                         for (int zb = 0; zb < 2; zb++) {
 #pragma unroll
-                            for (int v = 0; v < 4; v++) C[xi][zb][v] = 0.f;
+                            for (int v = 0; v < 4; v++) C[xi][zb][v] = Cl[zb][v] = 0.f;
 #pragma unroll
                             for (int s = 0; s < 2; s++) {
                                 if (!(s == 0 ? ys0 : ys1)) continue;
@@ -553,9 +562,13 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                                 float bh[2], bl[2];
                                 split(S1s[x * XS + (8 * s + tq) * YS + 8 * zb + fg], bh[0], bl[0]);
                                 split(S1s[x * XS + (8 * s + tq + 4) * YS + 8 * zb + fg], bh[1], bl[1]);
-                                mma3x(C[xi][zb], yah[s], yal[s], bh, bl);
+                                mma3x2(C[xi][zb], Cl[zb], yah[s], yal[s], bh, bl);
                             }
                         }
+#pragma unroll
+                        for (int zb = 0; zb < 2; zb++)
+#pragma unroll
+                            for (int v = 0; v < 4; v++) C[xi][zb][v] += Cl[zb][v];
                         P[xi][0] = P[xi][1] = 0.f;
                         // U channel (x < 8, z < 8, y_in < 8): O^y's k step 0 applied to U; the a1 = 0 rows
                         // (T block) are P, the a1 = 1 rows (B block) join Y
@@ -576,7 +589,7 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                         const int x = x0 + xi;
 #pragma unroll
                         for (int a2 = 0; a2 < 2; a2++) {
-                            float Z[4] = {0.f, 0.f, 0.f, 0.f};
+                            float Z[4] = {0.f, 0.f, 0.f, 0.f}, Zl[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                             for (int s = 0; s < 2; s++) {
                                 if (!((vz >> (2 * a2 + s)) & 1u)) continue;
@@ -585,8 +598,10 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
                                 split(C[xi][s][2], ah[1], al[1]);
                                 split(C[xi][s][1], ah[2], al[2]);
                                 split(C[xi][s][3], ah[3], al[3]);
-                                mma3x(Z, ah, al, zbh[a2][s], zbl[a2][s]);
+                                mma3x2(Z, Zl, ah, al, zbh[a2][s], zbl[a2][s]);
                             }
+#pragma unroll
+                            for (int v = 0; v < 4; v++) Z[v] += Zl[v];
                             // P through z with the B block only (a2 = 1 from b2 = 0): the T.T.T path is left out
                             if (a2 == 1 && pure && x < 8 && (vy & 1u) && ((vz >> 2) & 1u)) {
                                 float ah[4], al[4];

@@ -284,8 +284,10 @@ __global__ void k_mw_up(DevMRA m, DevTree t0, const DevTree *ts, const int *ptre
 // the value-to-coefficient map along each direction, times
 // sqrt(sf^3 2^(-3 (n+1)))), the compression of the 8 child blocks
 // (mwTransform(Compression)) and the node norms.  FP64.  gauss: [n][5] =
-// coefficient, exponent, position.
-__global__ void k_project(DevMRA m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map, const double *roots) {
+// coefficient, exponent, position; or values: the function at those points,
+// 8 (k+1)^3 per node in the same order (evaluated by the caller).
+__global__ void k_project(DevMRA m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map, const double *roots,
+                          const double *values) {
     extern __shared__ double sm[];
     const int K = m.K, K3 = m.kp1_d, tid = threadIdx.x, nthr = blockDim.x;
     double *t1 = sm, *t2 = sm + 8 * K3;
@@ -294,6 +296,10 @@ __global__ void k_project(DevMRA m, DevTree t, const int *nodes, int n, const do
     const double sfac = exp2(-(double)(nd.x + 1));
     const int lq[3] = {nd.y, nd.z, nd.w};
     for (int e = tid; e < 8 * K3; e += nthr) {
+        if (values) {
+            t1[e] = values[(size_t)blockIdx.x * 8 * K3 + e];
+            continue;
+        }
         const int ct = e / K3, p = e % K3;
         double r[3];
         int rem = p;
@@ -984,11 +990,11 @@ void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *pt
 }
 
 void launch_project(const DevMRA &m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map,
-                    const double *roots, cudaStream_t s) {
+                    const double *roots, cudaStream_t s, const double *values) {
     if (n <= 0) return;
     const size_t smem = sizeof(double) * 16 * m.kp1_d;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_project, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_project<<<n, 256, smem, s>>>(m, t, nodes, n, gauss, ng, vc_map, roots);
+    k_project<<<n, 256, smem, s>>>(m, t, nodes, n, gauss, ng, vc_map, roots, values);
 }
 
 void launch_combine(const DevMRA &m, bool mul, const DevTree *ins, const double *c, int n_in, DevTree out, const int *nodes, int n,

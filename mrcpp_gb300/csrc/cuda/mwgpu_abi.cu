@@ -1390,25 +1390,30 @@ mwgpu_status mwgpu_combine_level(mwgpu_ctx *ctx, int op, int n_in, mwgpu_tree *c
     return check_err(ctx, "combine level");
 }
 
-mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *vc_map, const double *roots,
-                                 const int *node_ix, int n, double *norms_out) {
+// The level of a projection: the Gaussians (n_gauss > 0) evaluated on the
+// device, or the function values the caller evaluated (values).
+static mwgpu_status project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *values, const double *vc_map,
+                                  const double *roots, const int *node_ix, int n, double *norms_out) {
     if (!ctx) return MWGPU_ERR_BAD_ARG;
     MW_ARG(tree && !tree->is_input, "projection writes an output tree");
     MW_ARG(n_gauss >= 0 && (n_gauss == 0 || gauss) && vc_map && roots, "invalid Gaussian list or basis tables");
     MW_ARG(n >= 0 && (n == 0 || node_ix), "invalid node list");
+    MW_ARG(n == 0 || !values || n_gauss == 0, "Gaussians or values, not both");
     for (int i = 0; i < n; i++) MW_ARG(node_ix[i] >= 0 && node_ix[i] < tree->t.n_real, "node index out of range");
     cudaSetDevice(ctx->device);
     if (n == 0) return MWGPU_OK;
     const int K = tree->mra.K;
-    const long long need = 5LL * std::max(n_gauss, 1) + (long long)K * K + K;
+    const long long nval = values ? (long long)n * 8 * tree->mra.kp1_d : 0;
+    const long long need = 5LL * std::max(n_gauss, 1) + (long long)K * K + K + nval;
     if (auto s = grow_buf(ctx, &ctx->d_proj, &ctx->proj_cap, need)) return s;
     if (auto s = ensure_work(ctx, n)) return s;
-    double *d_g = ctx->d_proj, *d_vc = d_g + 5 * std::max(n_gauss, 1), *d_roots = d_vc + K * K;
+    double *d_g = ctx->d_proj, *d_vc = d_g + 5 * std::max(n_gauss, 1), *d_roots = d_vc + K * K, *d_val = d_roots + K;
     if (n_gauss > 0) MW_CK(cudaMemcpyAsync(d_g, gauss, sizeof(double) * 5 * n_gauss, cudaMemcpyHostToDevice, ctx->stream));
+    if (values) MW_CK(cudaMemcpyAsync(d_val, values, sizeof(double) * nval, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(d_vc, vc_map, sizeof(double) * K * K, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(d_roots, roots, sizeof(double) * K, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(ctx->d_work, node_ix, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
-    launch_project(tree->mra, tree->t, ctx->d_work, n, d_g, n_gauss, d_vc, d_roots, ctx->stream);
+    launch_project(tree->mra, tree->t, ctx->d_work, n, d_g, n_gauss, d_vc, d_roots, ctx->stream, values ? d_val : nullptr);
     ctx->launches++;
     if (norms_out) {
         if (auto s = grow_buf(ctx, &ctx->d_nstage, &ctx->nstage_cap, 8LL * n)) return s;
@@ -1423,6 +1428,18 @@ mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, 
     MW_CK(cudaGetLastError());
     MW_CK(cudaStreamSynchronize(ctx->stream));
     return MWGPU_OK;
+}
+
+mwgpu_status mwgpu_project_level(mwgpu_ctx *ctx, mwgpu_tree *tree, int n_gauss, const double *gauss, const double *vc_map, const double *roots,
+                                 const int *node_ix, int n, double *norms_out) {
+    return project_level(ctx, tree, n_gauss, gauss, nullptr, vc_map, roots, node_ix, n, norms_out);
+}
+
+mwgpu_status mwgpu_project_level_values(mwgpu_ctx *ctx, mwgpu_tree *tree, const double *values, const double *vc_map, const double *roots,
+                                        const int *node_ix, int n, double *norms_out) {
+    if (!ctx) return MWGPU_ERR_BAD_ARG;
+    MW_ARG(n == 0 || values, "null values");
+    return project_level(ctx, tree, 0, nullptr, values, vc_map, roots, node_ix, n, norms_out);
 }
 
 mwgpu_status mwgpu_apply_derivative(mwgpu_ctx *ctx, const mwgpu_oper *o, mwgpu_tree *inp, mwgpu_tree *out, const int *node_ix, int n, int dir,
@@ -1772,8 +1789,12 @@ struct mwgpu_plan {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long launches_per_exec = 0;
-    std::vector<double> tune_ms;  // per candidate, ms per million items
+    // autotuning candidates: chunk length, schedule (1: pencil + item kernels,
+    // 0: item kernel alone) and the contraction's time
+    std::vector<double> tune_ms;
     std::vector<long long> tune_per;
+    std::vector<int> tune_pencil;
+    int tune_choice = -1;
     // pencil contraction (unscreened order-7 levels): kept items of the item
     // kernel (their offsets per entry), units and task sums
     bool pencil = false;
@@ -1807,6 +1828,8 @@ void plan_free(mwgpu_plan *pl) {
 }
 
 // chunking + contraction + reduction of a planned mixed level (no host sync)
+// reduce: the whole contraction with the reduction (the level); otherwise the
+// contraction alone between the plan's events e1 and e2 (autotuning)
 void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
     const mwgpu_oper *o = pl->o;
     cudaStream_t st = ctx->stream;
@@ -1823,13 +1846,13 @@ void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
     for (int t = 0; t < pl->nt; t++) tc_ok = tc_ok && pl->inps[t]->t.tc32 != nullptr;
     launch_items(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_chunks, pl->grid, items, pl->d_partial, pl->d_err,
                  pl->d_nchunks, pl->d_counter, tc_ok ? pl->d_counter + 1 : nullptr, st);
-    if (reduce && pl->pencil) {
+    if (pl->pencil) {
         launch_pencil_units(o->mra, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_units, pl->n_units, pl->d_err, st);
-        launch_stamp(pl->d_stamps + 4, st);
+        if (reduce) launch_stamp(pl->d_stamps + 4, st);
         launch_pencil(o->op, pl->d_fs, pl->d_wtree, pl->d_units, pl->d_task_unit, pl->n_tasks, pl->d_pen_partial, pl->d_err, pl->d_pen_counter,
                       st);
-        launch_stamp(pl->d_stamps + 5, st);
-        ctx->launches += 5;
+        if (reduce) launch_stamp(pl->d_stamps + 5, st);
+        ctx->launches += reduce ? 5 : 3;
     }
     if (reduce)
         launch_reduce_chunks(o->mra, pl->d_gs, pl->d_wtree, pl->d_work, pl->n, pl->d_chunk_begin, pl->d_partial, st, nullptr,
@@ -2143,29 +2166,51 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         if ((s = plan_check(ctx, pl, nullptr))) return fail(s);
         const bool tune = (flags & MWGPU_PLAN_AUTOTUNE) != 0 && total > 0;
         if (tune) {
+            // the schedule of the contraction (pencil + item kernels where the
+            // level allows the pencil kernel, or the item kernel alone) and the
+            // chunk length of the persistent item kernel (2 to 16 waves of the
+            // grid over its items), each candidate timed on the whole
+            // contraction of this level
+            const bool can_pencil = pl->pencil;
+            const long long kept = can_pencil ? std::max<long long>(1, total - (long long)pl->pen_node_terms) : total;
             double best = 1e300;
             long long best_per = pl->per;
-            for (int waves : {2, 4, 8, 16}) {
-                const long long per = std::max<long long>(per_min, (total + (long long)waves * pl->grid - 1) / ((long long)waves * pl->grid));
-                float ms = 0.f;
-                for (int rep = 0; rep < 2; rep++) {
-                    plan_contract(ctx, pl, per, false);
-                    MW_CK(cudaEventRecord(pl->e2, ctx->stream));
-                    MW_CK(cudaEventSynchronize(pl->e2));
-                    float m1 = 0.f;
-                    MW_CK(cudaEventElapsedTime(&m1, pl->e1, pl->e2));
-                    ms = rep == 0 ? m1 : std::min(ms, m1);
-                    if (m1 > 250.f) break;  // long launches: one timing is enough
-                }
-                pl->tune_per.push_back(per);
-                pl->tune_ms.push_back(ms);
-                if (ms < best) {
-                    best = ms;
-                    best_per = per;
+            bool best_pen = pl->pencil;
+            for (int pen = can_pencil ? 1 : 0; pen >= 0; pen--) {
+                pl->pencil = pen != 0;
+                const long long base = pen ? kept : total;
+                for (int waves : {2, 4, 8, 16}) {
+                    const long long per = std::max<long long>(per_min, (base + (long long)waves * pl->grid - 1) / ((long long)waves * pl->grid));
+                    float ms = 0.f;
+                    for (int rep = 0; rep < 2; rep++) {
+                        plan_contract(ctx, pl, per, false);
+                        MW_CK(cudaEventRecord(pl->e2, ctx->stream));
+                        MW_CK(cudaEventSynchronize(pl->e2));
+                        float m1 = 0.f;
+                        MW_CK(cudaEventElapsedTime(&m1, pl->e1, pl->e2));
+                        ms = rep == 0 ? m1 : std::min(ms, m1);
+                        if (m1 > 250.f) break;  // long launches: one timing is enough
+                    }
+                    int herr = 0;
+                    MW_CK(cudaMemcpy(&herr, pl->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+                    if (herr) {
+                        ctx->err = "plan autotuning: device error flags " + std::to_string(herr);
+                        return fail((herr & DE_TIMEOUT) ? MWGPU_ERR_TIMEOUT : MWGPU_ERR_INTERNAL);
+                    }
+                    pl->tune_per.push_back(per);
+                    pl->tune_pencil.push_back(pen);
+                    pl->tune_ms.push_back(ms);
+                    if (ms < best) {
+                        best = ms;
+                        best_per = per;
+                        best_pen = pen != 0;
+                        pl->tune_choice = (int)pl->tune_ms.size() - 1;
+                    }
                 }
             }
             pl->per = best_per;
-            // the trees hold what every execution leaves (same chunking)
+            pl->pencil = best_pen;
+            // the trees hold what every execution leaves (same schedule and chunking)
             plan_sequence(ctx, pl);
             if ((s = plan_check(ctx, pl, nullptr))) return fail(s);
         }
@@ -2225,6 +2270,20 @@ extern "C" mwgpu_status mwgpu_plan_info(const mwgpu_plan *pl, long long *chunk_i
             for (int i = 0; i < std::min(nc, *n_candidates); i++) cand_ms[i] = pl->tune_ms[i];
         *n_candidates = nc;
     }
+    return MWGPU_OK;
+}
+
+extern "C" mwgpu_status mwgpu_plan_tuning(const mwgpu_plan *pl, int *n_candidates, long long *chunk_items, int *schedule, double *ms,
+                                          int *chosen) {
+    if (!pl || !n_candidates) return MWGPU_ERR_BAD_ARG;
+    const int nc = (int)pl->tune_per.size();
+    for (int i = 0; i < std::min(nc, *n_candidates); i++) {
+        if (chunk_items) chunk_items[i] = pl->tune_per[i];
+        if (schedule) schedule[i] = pl->tune_pencil[i];
+        if (ms) ms[i] = pl->tune_ms[i];
+    }
+    if (chosen) *chosen = pl->tune_choice;
+    *n_candidates = nc;
     return MWGPU_OK;
 }
 

@@ -610,8 +610,12 @@ int apply_derivative_impl(mwh_tree *outp, mwh_oper *operp, mwh_tree *inpp, int d
 // node computations on the device: TreeBuilder + WaveletAdaptor on the host,
 // ProjectionCalculator::calcNode per iteration through mwgpu_project_level,
 // BottomUp on the device, then the coefficients come back
+// func (optional): any function, evaluated on the host at the children's
+// quadrature points of each level (the RepresentableFunction of
+// ProjectionCalculator), in batches of at most kProjectBatch points; the
+// transforms and norms of the level run on the device
 int project_device_impl(double prec, Tree<3> &tree, int n, const double *coef, const double *ex, const double *pos, int max_iter, bool abs_prec,
-                        mwh_apply_stats *stats) {
+                        mwh_apply_stats *stats, const BatchFunc *func = nullptr) {
     auto t0 = std::chrono::steady_clock::now();
     std::vector<double> gauss(5 * (size_t)n);
     for (int j = 0; j < n; j++) {
@@ -633,12 +637,39 @@ int project_device_impl(double prec, Tree<3> &tree, int n, const double *coef, c
     b.dout = create_output(ctx, md, tree, acc);
     b.synced = tree.nodes.size();
     try {
-        std::vector<double> nbuf;
+        std::vector<double> nbuf, pts, vals;
+        const int K = mra.kp1(), K3 = K * K * K;
         auto calc = [&](Tree<3> &t, const std::vector<int> &work) {
             sync_new(ctx, b, acc);
             nbuf.resize(8 * work.size());
-            ck(mwgpu_project_level(ctx, b.dout, n, gauss.data(), basis.vcMap.data(), basis.roots.data(), work.data(), (int)work.size(), nbuf.data()),
-               "projection level");
+            if (func) {
+                // MWNode::getExpandedChildPts (MWNode.cpp:854-935), scaled by the world's factors
+                const size_t np = work.size() * 8 * (size_t)K3;
+                pts.resize(3 * np);
+                vals.resize(np);
+                for (size_t j = 0; j < work.size(); j++) {
+                    const auto &nd = t.nodes[work[j]];
+                    const double h = std::ldexp(1.0, -(nd.n + 1));
+                    for (int e = 0; e < 8 * K3; e++) {
+                        const int ct = e / K3, q = e % K3;
+                        const int qd[3] = {q % K, (q / K) % K, q / (K * K)};
+                        for (int d = 0; d < 3; d++)
+                            pts[3 * (j * 8 * K3 + e) + d] = mra.world.sf[d] * (h * (basis.roots[qd[d]] + 2.0 * nd.l[d] + ((ct >> d) & 1)));
+                    }
+                }
+                for (size_t b0 = 0; b0 < np; b0 += kProjectBatch) {
+                    const size_t nb = std::min(kProjectBatch, np - b0);
+                    (*func)((long long)nb, pts.data() + 3 * b0, vals.data() + b0);
+                }
+                acc.h2d_bytes += np * 8;
+                ck(mwgpu_project_level_values(ctx, b.dout, vals.data(), basis.vcMap.data(), basis.roots.data(), work.data(), (int)work.size(),
+                                              nbuf.data()),
+                   "projection level");
+            } else {
+                ck(mwgpu_project_level(ctx, b.dout, n, gauss.data(), basis.vcMap.data(), basis.roots.data(), work.data(), (int)work.size(),
+                                       nbuf.data()),
+                   "projection level");
+            }
             for (size_t j = 0; j < work.size(); j++) {
                 auto &nd = t.nodes[work[j]];
                 double s2 = 0.0;
@@ -893,6 +924,15 @@ int mwh_project_func(double prec, mwh_tree *t, mwh_func f, void *user, int max_i
         if (!t || !f) return fail(1, "invalid projection arguments");
         project_batched<3>(prec, *t->t, [f, user](long long n, const double *r, double *v) { f(n, r, v, user); }, max_iter, abs_prec != 0);
         return 0;
+    });
+}
+
+int mwh_project_func_device(double prec, mwh_tree *t, mwh_func f, void *user, int max_iter, int abs_prec, mwh_apply_stats *stats) {
+    touch(t);
+    return guard([&] {
+        if (!t || !f) return fail(1, "null argument");
+        BatchFunc bf = [f, user](long long n, const double *r, double *v) { f(n, r, v, user); };
+        return project_device_impl(prec, *t->t, 0, nullptr, nullptr, nullptr, max_iter, abs_prec != 0, stats, &bf);
     });
 }
 
@@ -1479,7 +1519,8 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         std::vector<int> level_begin, flags;
         std::vector<double> norm_levels, norms;
         try {
-            dinp = upload_input(ctx, md, inp, acc);
+            dinp = resident_input(ctx, md, inpp, acc);
+            ck(mwgpu_tree_clear_generated(ctx, dinp), "clear generated nodes");
             ht.mark("upload");
             const double f_norm = std::sqrt(std::max(inp.squareNorm, 0.0));
             const size_t max_nodes = std::max<size_t>(4096, 4 * inp.nodes.size());
@@ -1619,7 +1660,6 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
         } catch (...) {
             if (dprop) mwgpu_free_tree(ctx, dprop);
             if (dold) mwgpu_free_tree(ctx, dold);
-            if (dinp) mwgpu_free_tree(ctx, dinp);
             throw;
         }
         // the judged tree, created in TreeBuilder's order (the host ids of the plain apply)
@@ -1657,13 +1697,11 @@ int mwh_apply_learned(double prec, mwh_tree *outp, mwh_oper *operp, mwh_tree *in
             ck(mwgpu_download_nodes(ctx, dprop, (int)src.size(), src.data(), out.coefs.data(), norms.data()), "download output tree");
         } catch (...) {
             mwgpu_free_tree(ctx, dprop);
-            mwgpu_free_tree(ctx, dinp);
             throw;
         }
         acc.d2h_bytes += (src.size() * (size_t)out.nCoefs + norms.size()) * 8;
         ls.host_round_trips += 1;
-        mwgpu_free_tree(ctx, dprop);
-        mwgpu_free_tree(ctx, dinp);
+        mwgpu_free_tree(ctx, dprop);  // the input tree keeps its device copy
         mwgpu_launch_count(ctx, &l1);
         acc.launches = l1 - l0;
         ht.mark("download");

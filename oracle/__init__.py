@@ -69,6 +69,9 @@ def lib(fast=False):
                                      C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
         L.oracle_combine_ex.restype = C.c_int
         L.oracle_combine_ex.argtypes = L.oracle_combine.argtypes[:11] + [C.c_int, C.POINTER(C.c_void_p)]
+        L.oracle_project.restype = C.c_int
+        L.oracle_project.argtypes = [C.POINTER(OracleMra), _PD, _PD, C.POINTER(OracleTree), C.c_double, C.c_int, C.c_int, _ORACLE_FUNC, C.c_void_p,
+                                     C.POINTER(C.c_void_p)]
         L.oracle_result_free.restype = None
         L.oracle_result_free.argtypes = [C.c_void_p]
         _libs[path] = L
@@ -187,6 +190,67 @@ def apply_derivative(out, oper, inp, dir, nthreads=0):
     return Prepared(1.0, out, oper, inp).run(nthreads, deriv_dir=dir, deriv_order=getattr(oper, "order", 1))
 
 
+_ORACLE_FUNC = C.CFUNCTYPE(None, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
+
+
+def basis_maps(basis, order):
+    """Quadrature roots on [0, 1] and the value-to-coefficient map of the
+    scaling basis, computed here with numpy (LegendreBasis::calcCVMaps,
+    LegendreBasis.cpp:98-109: vcMap(i, k) = phi_k(x_i) w_i with phi_k =
+    sqrt(2k+1) P_k(2x - 1); InterpolatingBasis::calcCVMaps,
+    InterpolatingBasis.cpp:115-123: vcMap(k, k) = sqrt(w_k)); column-major."""
+    from numpy.polynomial import legendre as npleg
+
+    K = order + 1
+    x, w = npleg.leggauss(K)
+    x, w = 0.5 * (x + 1.0), 0.5 * w
+    vc = np.zeros((K, K))
+    if basis == 0:  # Legendre
+        for k in range(K):
+            c = np.zeros(k + 1)
+            c[k] = 1.0
+            vc[:, k] = np.sqrt(2 * k + 1) * npleg.legval(2 * x - 1, c) * w
+    else:
+        vc[np.arange(K), np.arange(K)] = np.sqrt(w)
+    return x, np.ascontiguousarray(vc.T).ravel()  # element (i, k) at i + K k
+
+
+def project(prec, tree, func, max_iter=-1, abs_prec=False):
+    """Oracle project(prec, tree, func) from the current grid of `tree` (a
+    FunctionTree; only its MRA and node indices are read): func takes an (n, 3)
+    array of points and returns n values.  Returns the flat result tree."""
+    mra = tree.mra
+    d = mra.desc()
+    m = OracleMra()
+    m.order, m.root_scale, m.max_scale, m.sf = d.order, d.root_scale, d.max_scale, d.sf
+    for i in range(3):
+        m.corner[i] = d.corner[i]
+        m.nbox[i] = d.nbox[i]
+    filt = np.ascontiguousarray(mra._filters)
+    m.filters = _pd(filt)
+    roots, vc = basis_maps(mra.basis, mra.order)
+    go = tree.export()
+    gt = OracleTree(len(go["child0"]), _pi(go["idx"]), _pi(go["child0"]), None, None)
+    errors = []
+
+    def cb(n, r, v, _user):
+        try:
+            pts = np.ctypeslib.as_array(r, shape=(n, 3))
+            np.ctypeslib.as_array(v, shape=(n,))[:] = np.asarray(func(pts), dtype=np.float64).reshape(n)
+        except BaseException as e:
+            errors.append(e)
+
+    f = _ORACLE_FUNC(cb)
+    res = C.c_void_p()
+    L = lib()
+    rc = L.oracle_project(C.byref(m), _pd(vc), _pd(roots), C.byref(gt), float(prec), int(max_iter), int(bool(abs_prec)), f, None, C.byref(res))
+    if errors:
+        raise errors[0]
+    if rc != 0:
+        raise RuntimeError("oracle_project failed with code %d" % rc)
+    return _export_result(L, res, mra.kp1)
+
+
 def combine(op, prec, out, terms, max_iter=-1, abs_prec=False, use_max_norms=False):
     """Oracle add (op 0) / multiply (op 1) of terms [(c, FunctionTree), ...] from
     the grid of `out` (use_max_norms: multiply's max-norm adaptor); returns the
@@ -216,9 +280,13 @@ def combine(op, prec, out, terms, max_iter=-1, abs_prec=False, use_max_norms=Fal
                              int(bool(abs_prec)), int(bool(use_max_norms)), C.byref(res))
     if rc != 0:
         raise RuntimeError("oracle_combine failed with code %d" % rc)
+    return _export_result(L, res, mra.kp1)
+
+
+def _export_result(L, res, kp1):
     n, sq, nt, nc, it = C.c_int(), C.c_double(), C.c_ulonglong(), C.c_ulonglong(), C.c_int()
     L.oracle_result_info(res, C.byref(n), C.byref(sq), C.byref(nt), C.byref(nc), C.byref(it))
-    K3 = mra.kp1 ** 3
+    K3 = kp1 ** 3
     out_ = {"square_norm": sq.value, "iterations": it.value, "n_nodes": n.value, "idx": np.zeros((n.value, 4), dtype=np.int32),
             "child0": np.zeros(n.value, dtype=np.int32), "coefs": np.zeros((n.value, 8 * K3)), "norms": np.zeros((n.value, 8))}
     L.oracle_result_export(res, _pi(out_["idx"]), _pi(out_["child0"]), _pd(out_["coefs"]), _pd(out_["norms"]))

@@ -19,6 +19,8 @@
  *   node norms                src/trees/MWNode.cpp:609-655
  *   TreeBuilder loop          src/treebuilders/TreeBuilder.cpp:38-87, 150-166
  *   split                     src/treebuilders/TreeAdaptor.h:41-52, src/utils/tree_utils.cpp:47-65
+ *   projection                src/treebuilders/project.cpp:41-66, ProjectionCalculator.cpp:34-51,
+ *                             MWNode.cpp:448-490 (cvTransform), 854-935 (child quadrature points)
  *   precTrees form of apply   src/treebuilders/apply.cpp:214-251 (precFunc), MWTree.cpp:536-543 and
  *                             MWNode.cpp:1257-1269 (makeMaxSquareNorms), MWNode.h:84,212,
  *                             ConvolutionCalculator.cpp:244-245, WaveletAdaptor.h:51-54
@@ -1241,6 +1243,103 @@ int oracle_combine_ex(const oracle_mra *m, int op, int n_in, const oracle_tree *
     }
     for (int j = 0; j < n_in; j++) tree_free(&f[j]);
     free(f);
+    *res = R;
+    return 0;
+}
+
+/* project(prec, tree, func) (project.cpp:41-66): TreeBuilder from the end
+   nodes of out0 with ProjectionCalculator::calcNode (ProjectionCalculator.cpp:
+   34-51: the function at the quadrature points of the 8 children -- child ct,
+   point (qx, qy, qz) at sf 2^-(n+1) (root_q + 2 l + bit_d(ct)), x fastest --,
+   cvTransform(Backward) with vc_map (MWNode.cpp:448-490), mwTransform(
+   Compression), norms), the WaveletAdaptor split, then BottomUp and the
+   square norm.  f is called once per level with every point of the level. */
+int oracle_project(const oracle_mra *m, const double *vc_map, const double *roots, const oracle_tree *out0, double prec, int max_iter, int abs_prec,
+                   oracle_func f, void *user, oracle_result **res) {
+    if (!m || !vc_map || !roots || !out0 || !f || !res) return 1;
+    oracle_result *R = (oracle_result *)calloc(1, sizeof(oracle_result));
+    if (tree_load(&R->g, m, out0->n_nodes, out0->idx, out0->child0, NULL, NULL)) return 2;
+    otree *g = &R->g;
+    const int K = g->K, K3 = g->K3;
+    double *bufs = (double *)malloc(sizeof(double) * 3 * 8 * K3);
+    double *t1 = bufs, *t2 = bufs + 8 * K3, *t3 = bufs + 16 * K3;
+    size_t cnt, nwork = 0;
+    int *lvl, nl;
+    int *all = bfs(g, &cnt, &lvl, &nl);
+    free(lvl);
+    int *work = (int *)malloc(sizeof(int) * (cnt + 1));
+    for (size_t q = 0; q < cnt; q++)
+        if (g->child0[all[q]] < 0) work[nwork++] = all[q];
+    free(all);
+    double sNorm = 0.0, wNorm = 0.0;
+    int iter = 0;
+    while (nwork > 0) {
+        const size_t np = nwork * 8 * (size_t)K3;
+        double *pts = (double *)malloc(sizeof(double) * 3 * np), *val = (double *)malloc(sizeof(double) * np);
+        for (size_t w = 0; w < nwork; w++) {
+            okey k = g->idx[work[w]];
+            const double h = ldexp(1.0, -(k.n + 1));
+            for (int e = 0; e < 8 * K3; e++) {
+                const int ct = e / K3, p = e % K3;
+                const int q[3] = {p % K, (p / K) % K, p / (K * K)};
+                for (int d = 0; d < 3; d++)
+                    pts[3 * (w * 8 * K3 + e) + d] = m->sf * (h * (roots[q[d]] + 2.0 * k.l[d] + ((ct >> d) & 1)));
+            }
+        }
+        f((long long)np, pts, val, user);
+        for (size_t w = 0; w < nwork; w++) {
+            const int gi = work[w];
+            okey k = g->idx[gi];
+            const double fac = sqrt(m->sf * m->sf * m->sf / pow(2.0, 3.0 * (k.n + 1)));
+            memcpy(t1, val + w * 8 * K3, sizeof(double) * 8 * K3);
+            cv_transform(m, vc_map, fac, t1, t2, t3);                 /* cvTransform(Backward) */
+            mw_transform_back(m, t2, g->coefs + (size_t)gi * g->nc, K3, t3); /* mwTransform(Compression) */
+            calc_norms(g, gi);
+        }
+        free(pts);
+        free(val);
+        if (iter == 0) {
+            sNorm = 0.0;
+            for (size_t w = 0; w < nwork; w++)
+                if (g->idx[work[w]].n - m->root_scale >= 0) sNorm += scaling_norm(g, work[w]);
+        }
+        for (size_t w = 0; w < nwork; w++)
+            if (g->idx[work[w]].n - m->root_scale >= 0) wNorm += wavelet_norm(g, work[w]);
+        g->square_norm = (sNorm < 0.0 || wNorm < 0.0) ? -1.0 : sNorm + wNorm;
+        if (iter >= max_iter && max_iter >= 0) nwork = 0;
+        int *next = (int *)malloc(sizeof(int) * (8 * nwork + 1));
+        size_t nn = 0;
+        for (size_t w = 0; w < nwork; w++) {
+            int i = work[w];
+            if (g->child0[i] >= 0 || g->idx[i].n + 2 > m->max_scale) continue;
+            if (split_check(g, i, prec, 1.0, abs_prec)) {
+                int c0 = create_children(g, i, 0);
+                for (int q = 0; q < 8; q++) next[nn++] = c0 + q;
+            }
+        }
+        free(work);
+        work = next;
+        nwork = nn;
+        iter++;
+    }
+    free(work);
+    R->iterations = iter;
+    int *order_ = bfs(g, &cnt, &lvl, &nl);
+    for (int L = nl - 2; L >= 0; L--)
+        for (int q = lvl[L]; q < lvl[L + 1]; q++) {
+            int i = order_[q];
+            int c0 = g->child0[i];
+            if (c0 < 0) continue;
+            mw_transform_back(m, g->coefs + (size_t)c0 * g->nc, g->coefs + (size_t)i * g->nc, g->nc, t1);
+            calc_norms(g, i);
+        }
+    double sq = 0.0;
+    for (size_t q = 0; q < cnt; q++)
+        if (g->child0[order_[q]] < 0) sq += g->sqn[order_[q]];
+    g->square_norm = sq;
+    free(order_);
+    free(lvl);
+    free(bufs);
     *res = R;
     return 0;
 }

@@ -52,6 +52,10 @@ int oracle_apply_sampled(const oracle_mra *mra, const oracle_oper *oper, const o
 int oracle_apply_prec(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, double out_sqnorm,
                       double prec, int max_iter, int abs_prec, int nthreads, int count_terms, int sample, int n_prec,
                       const oracle_tree *prec_trees, oracle_result **res);
+/* project(prec, out0's grid, f): f(n, r[3 n], v[n], user) evaluates the function */
+typedef void (*oracle_func)(long long n, const double *r, double *v, void *user);
+int oracle_project(const oracle_mra *mra, const double *vc_map, const double *roots, const oracle_tree *out0, double prec, int max_iter,
+                   int abs_prec, oracle_func f, void *user, oracle_result **res);
 int oracle_apply_derivative(const oracle_mra *mra, const oracle_oper *oper, const oracle_tree *inp, const oracle_tree *out0, int dir, int order,
                             int nthreads, oracle_result **res);
 /* add (op 0) / multiply (op 1): out = sum / product of c[j] inps[j], adaptive

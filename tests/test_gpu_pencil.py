@@ -1,0 +1,149 @@
+"""The pencil contraction (k_pencil, order 7, terms of band width <= 1 on
+levels without norm screening) against the item kernel alone
+(MWGPU_NO_PENCIL=1) on the same levels: both are the mixed form, so the
+results agree to the mixed form's accuracy (relative L2 <= 2e-6 between them,
+each within 1e-5 of the FP64 form), with identical node-term and component
+counts; the pencil kernel really takes part (its node-term count from
+mwgpu_plan_pencil_info is positive and below the level's).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import mrcpp_gb300 as mw
+from cases import gaussian_sum, project
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case():
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, 1e-4)
+    f = project(mra, 1e-4, gaussian_sum(2026, 6, (1.0, 100.0), (-5.0, 5.0)))
+    grid = mw.FunctionTree(mra)
+    mw.apply(1e-4, grid, P, f, precision=mw.FP64)
+    return mra, P, f, grid
+
+
+def fixed(mra, P, f, grid, form, no_pencil=False):
+    if no_pencil:
+        os.environ["MWGPU_NO_PENCIL"] = "1"
+    try:
+        g = mw.FunctionTree(mra)
+        mw.copy_grid(g, grid)
+        st = mw.apply(1e-4, g, P, f, max_iter=0, precision=form)
+    finally:
+        os.environ.pop("MWGPU_NO_PENCIL", None)
+    return g.export()["coefs"], st
+
+
+def test_level_path(gpu, case):
+    mra, P, f, grid = case
+    a, sa = fixed(mra, P, f, grid, mw.MIXED)
+    b, sb = fixed(mra, P, f, grid, mw.MIXED, no_pencil=True)
+    c, _ = fixed(mra, P, f, grid, mw.FP64)
+    assert sa["node_terms"] == sb["node_terms"] and sa["components"] == sb["components"]
+    rel = lambda x, y: np.linalg.norm(x - y) / np.linalg.norm(y)
+    assert rel(a, b) <= 2e-6
+    assert rel(a, c) <= 1e-5 and rel(b, c) <= 1e-5
+
+
+def test_plan_path(gpu, case):
+    mra, P, f, grid = case
+    L = mw.lib()
+    out = {}
+    for no_pencil in (False, True):
+        if no_pencil:
+            os.environ["MWGPU_NO_PENCIL"] = "1"
+        ctx = C.c_void_p()
+        cfg = mw.MwgpuConfig()
+        cfg.precision = mw.MIXED
+        assert L.mwgpu_init(C.byref(ctx), C.byref(cfg)) == 0
+        try:
+            dop = C.c_void_p()
+            assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
+            fx = f.export()
+            fd = mw.MwgpuTreeDesc(len(fx["child0"]), mw._pi(fx["idx"]), mw._pi(fx["child0"]), mw._pd(fx["coefs"]), mw._pd(fx["norms"]))
+            dinp = C.c_void_p()
+            assert L.mwgpu_upload_tree(ctx, C.byref(mra.desc()), C.byref(fd), C.byref(dinp)) == 0
+            gx = grid.export()
+            gd = mw.MwgpuTreeDesc(len(gx["child0"]), mw._pi(gx["idx"]), mw._pi(gx["child0"]), None, None)
+            dout = C.c_void_p()
+            assert L.mwgpu_create_tree(ctx, C.byref(mra.desc()), C.byref(gd), C.byref(dout)) == 0
+            n = len(gx["child0"])
+            PA1 = C.c_void_p * 1
+            plan = C.c_void_p()
+            sq = np.full(1, -1.0)
+            rc = L.mwgpu_plan_create(ctx, dop, 1, PA1(dinp), PA1(dout), mw._pi(np.zeros(n, dtype=np.int32)), mw._pi(np.arange(n, dtype=np.int32)),
+                                     n, 1e-4, mw._pd(sq), 1, C.byref(plan))
+            assert rc == 0, L.mwgpu_last_error(ctx).decode()
+            for _ in range(2):
+                assert L.mwgpu_plan_execute(ctx, plan, None) == 0
+            st = mw.MwgpuLevelStats()
+            assert L.mwgpu_plan_check(ctx, plan, C.byref(st)) == 0
+            pnt, pms = C.c_ulonglong(), C.c_double()
+            assert L.mwgpu_plan_pencil_info(plan, C.byref(pnt), C.byref(pms)) == 0
+            c = np.zeros((n, 8 * 512))
+            assert L.mwgpu_download_tree(ctx, dout, mw._pd(c), None) == 0
+            assert L.mwgpu_plan_destroy(ctx, plan) == 0
+            out[no_pencil] = (c, st.node_terms, st.components, pnt.value)
+        finally:
+            os.environ.pop("MWGPU_NO_PENCIL", None)
+            L.mwgpu_destroy(ctx)
+    (a, nta, nca, pa), (b, ntb, ncb, pb) = out[False], out[True]
+    assert nta == ntb and nca == ncb
+    assert 0 < pa < nta and pb == 0
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
+
+
+def test_plan_autotuning(gpu, case):
+    # MWGPU_PLAN_AUTOTUNE times both schedules (pencil + item kernels, item
+    # kernel alone) x 4 chunk lengths on the level and keeps the fastest; the
+    # result does not depend on the choice beyond the mixed form's accuracy
+    mra, P, f, grid = case
+    L = mw.lib()
+    ctx = C.c_void_p()
+    cfg = mw.MwgpuConfig()
+    cfg.precision = mw.MIXED
+    assert L.mwgpu_init(C.byref(ctx), C.byref(cfg)) == 0
+    try:
+        dop = C.c_void_p()
+        assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
+        fx = f.export()
+        fd = mw.MwgpuTreeDesc(len(fx["child0"]), mw._pi(fx["idx"]), mw._pi(fx["child0"]), mw._pd(fx["coefs"]), mw._pd(fx["norms"]))
+        dinp = C.c_void_p()
+        assert L.mwgpu_upload_tree(ctx, C.byref(mra.desc()), C.byref(fd), C.byref(dinp)) == 0
+        gx = grid.export()
+        gd = mw.MwgpuTreeDesc(len(gx["child0"]), mw._pi(gx["idx"]), mw._pi(gx["child0"]), None, None)
+        n = len(gx["child0"])
+        PA1 = C.c_void_p * 1
+        res = {}
+        for flags in (1, 3):
+            dout = C.c_void_p()
+            assert L.mwgpu_create_tree(ctx, C.byref(mra.desc()), C.byref(gd), C.byref(dout)) == 0
+            plan = C.c_void_p()
+            sq = np.full(1, -1.0)
+            rc = L.mwgpu_plan_create(ctx, dop, 1, PA1(dinp), PA1(dout), mw._pi(np.zeros(n, dtype=np.int32)), mw._pi(np.arange(n, dtype=np.int32)),
+                                     n, 1e-4, mw._pd(sq), flags, C.byref(plan))
+            assert rc == 0, L.mwgpu_last_error(ctx).decode()
+            nc, chosen = C.c_int(16), C.c_int()
+            items, sched, ms = (C.c_longlong * 16)(), (C.c_int * 16)(), (C.c_double * 16)()
+            assert L.mwgpu_plan_tuning(plan, C.byref(nc), items, sched, ms, C.byref(chosen)) == 0
+            if flags == 3:
+                assert nc.value == 8 and sorted(set(sched[:8])) == [0, 1]
+                assert 0 <= chosen.value < 8 and ms[chosen.value] == min(ms[:8])
+            else:
+                assert nc.value == 0 and chosen.value == -1
+            assert L.mwgpu_plan_execute(ctx, plan, None) == 0
+            assert L.mwgpu_plan_check(ctx, plan, None) == 0
+            c = np.zeros((n, 8 * 512))
+            assert L.mwgpu_download_tree(ctx, dout, mw._pd(c), None) == 0
+            assert L.mwgpu_plan_destroy(ctx, plan) == 0
+            assert L.mwgpu_free_tree(ctx, dout) == 0
+            res[flags] = c
+        assert np.linalg.norm(res[3] - res[1]) / np.linalg.norm(res[1]) <= 2e-6
+    finally:
+        L.mwgpu_destroy(ctx)

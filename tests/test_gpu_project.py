@@ -1,6 +1,7 @@
-"""Projection on the GPU (mwgpu_project_level through the host TreeBuilder
-loop) against the host projection that restates project / ProjectionCalculator
-(CPU): identical grid, FP64 coefficients within 1e-12 of the largest, and the
+"""Projection on the GPU (mwgpu_project_level / mwgpu_project_level_values
+through the host TreeBuilder loop) against the oracle's projection and the
+host mirror's (both restate project / ProjectionCalculator on the CPU):
+identical grid, FP64 coefficients within 1e-12 of the largest, and the
 analytic norm and integral of the projected Gaussians."""
 import math
 
@@ -54,3 +55,35 @@ def test_project_gpu_feeds_apply(gpu):
     assert same
     mx, _ = rel_errors(gb.export()["coefs"], ga.export()["coefs"][perm])
     assert mx <= 1e-11
+
+
+@pytest.mark.parametrize("basis,order", [(mw.LEGENDRE, 7), (mw.INTERPOLATING, 5)])
+def test_device_projection_vs_oracle(gpu, basis, order):
+    # project(prec, tree, func) with the nodes on the GPU: a Slater function
+    # evaluated on the host per level (mwgpu_project_level_values) and a
+    # Gaussian sum evaluated on the device (mwgpu_project_level), both against
+    # the oracle's projection: the same grid, coefficients within 1e-12
+    import oracle
+    from cases import gaussian_sum, match, rel_errors
+
+    mra = mw.MRA(box=(-20, 20), order=order, basis=basis)
+    slater = lambda r: np.exp(-np.linalg.norm(r, axis=1)) / np.sqrt(np.pi)
+    gs = gaussian_sum(31, 3, (1.0, 40.0), (-2.0, 2.0))
+
+    def gsum(r):
+        v = np.zeros(len(r))
+        for c, a, R in gs:
+            v += c * np.exp(-a * ((r - np.asarray(R)) ** 2).sum(axis=1))
+        return v
+
+    for f, dev in ((slater, lambda t: mw.project(1e-5, t, slater, device=True)),
+                   (gsum, lambda t: mw.project(1e-5, t, gs, grid=False, device=True))):
+        ref = oracle.project(1e-5, mw.FunctionTree(mra), f)
+        t = mw.FunctionTree(mra)
+        st = dev(t)
+        tx = t.export()
+        same, perm = match(tx, ref)
+        assert same, "grid differs from the oracle's"
+        mx, l2 = rel_errors(tx["coefs"], ref["coefs"][perm])
+        assert mx <= 1e-12 and l2 <= 1e-12, (mx, l2)
+        assert st["iterations"] == ref["iterations"]
