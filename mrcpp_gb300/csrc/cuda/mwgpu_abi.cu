@@ -401,6 +401,29 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     launch_scan(ctx->d_pcounts, ctx->d_item_off, np, ctx->d_scan, d_total, ctx->stream);
     launch_gather_goff(ctx->d_item_off, ctx->d_pair_off, n, ctx->d_goff, ctx->stream);
     ctx->launches += 5;
+    // the pencil units depend on the topology only: built on the host while the
+    // device counts the work list, uploaded behind it
+    const bool pencil = use_pencil(lv);
+    PencilPlan pp;
+    if (pencil) {
+        pencil_build(lv, pp);
+        const long long nu = (long long)pp.units.size();
+        if (auto s = grow_buf(ctx, &ctx->d_units, &ctx->units_cap, std::max(nu, 1LL))) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_task_unit, &ctx->task_unit_cap, pp.n_tasks + 1)) return s;
+        if (auto s = grow_buf(ctx, &ctx->d_pen_begin, &ctx->pen_begin_cap, n + 1)) return s;
+        const size_t pneed = (size_t)std::max(pp.n_tasks, 1) * 8 * (size_t)o->mra.kp1_d;
+        if (pneed > ctx->pen_partial_cap) {
+            if (ctx->d_pen_partial) cudaFree(ctx->d_pen_partial);
+            ctx->d_pen_partial = nullptr;
+            ctx->pen_partial_cap = std::max(pneed, 2 * ctx->pen_partial_cap);
+            if (auto s = dev_alloc(ctx, &ctx->d_pen_partial, ctx->pen_partial_cap)) return s;
+        }
+        if (!ctx->d_pen_counter)
+            if (auto s = dev_alloc(ctx, &ctx->d_pen_counter, 1)) return s;
+        if (nu > 0) MW_CK(cudaMemcpyAsync(ctx->d_units, pp.units.data(), sizeof(PencilUnit) * nu, cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_task_unit, pp.task_unit.data(), sizeof(int) * (pp.n_tasks + 1), cudaMemcpyHostToDevice, ctx->stream));
+        MW_CK(cudaMemcpyAsync(ctx->d_pen_begin, pp.pen_begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
+    }
     std::vector<long long> offs(n + 1);
     MW_CK(cudaMemcpyAsync(offs.data(), ctx->d_goff, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
     MW_CK(cudaStreamSynchronize(ctx->stream));
@@ -425,9 +448,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     if (order) launch_order_terms(ctx->d_goff, n, ctx->d_items_cm, ctx->d_items, o->op.n_terms, ctx->d_err, ctx->stream);
     ctx->launches += 1 + (order ? 1 : 0);
     // pencil path: the items of the wider terms stay with the item kernel (stable compaction into d_items_cm)
-    const bool pencil = use_pencil(lv);
     const WorkItem *kitems = ctx->d_items;
-    PencilPlan pp;
     if (pencil) {
         if (auto s = grow_buf(ctx, &ctx->d_keep, &ctx->keep_cap, n + 1)) return s;
         if (auto s = grow_buf(ctx, &ctx->d_keep_off, &ctx->keep_off_cap, n + 1)) return s;
@@ -439,23 +460,6 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
         ctx->launches += 5;
         MW_CK(cudaMemcpyAsync(offs.data(), ctx->d_keep_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
         kitems = ctx->d_items_cm;
-        pencil_build(lv, pp);
-        const long long nu = (long long)pp.units.size();
-        if (auto s = grow_buf(ctx, &ctx->d_units, &ctx->units_cap, std::max(nu, 1LL))) return s;
-        if (auto s = grow_buf(ctx, &ctx->d_task_unit, &ctx->task_unit_cap, pp.n_tasks + 1)) return s;
-        if (auto s = grow_buf(ctx, &ctx->d_pen_begin, &ctx->pen_begin_cap, n + 1)) return s;
-        const size_t pneed = (size_t)std::max(pp.n_tasks, 1) * 8 * (size_t)o->mra.kp1_d;
-        if (pneed > ctx->pen_partial_cap) {
-            if (ctx->d_pen_partial) cudaFree(ctx->d_pen_partial);
-            ctx->d_pen_partial = nullptr;
-            ctx->pen_partial_cap = std::max(pneed, 2 * ctx->pen_partial_cap);
-            if (auto s = dev_alloc(ctx, &ctx->d_pen_partial, ctx->pen_partial_cap)) return s;
-        }
-        if (!ctx->d_pen_counter)
-            if (auto s = dev_alloc(ctx, &ctx->d_pen_counter, 1)) return s;
-        if (nu > 0) MW_CK(cudaMemcpyAsync(ctx->d_units, pp.units.data(), sizeof(PencilUnit) * nu, cudaMemcpyHostToDevice, ctx->stream));
-        MW_CK(cudaMemcpyAsync(ctx->d_task_unit, pp.task_unit.data(), sizeof(int) * (pp.n_tasks + 1), cudaMemcpyHostToDevice, ctx->stream));
-        MW_CK(cudaMemcpyAsync(ctx->d_pen_begin, pp.pen_begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
         MW_CK(cudaStreamSynchronize(ctx->stream));
     }
     // chunks of about the same number of items, several waves of CTAs

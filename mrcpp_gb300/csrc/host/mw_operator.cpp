@@ -14,55 +14,62 @@ namespace {
 constexpr double root_pi = 1.7724538509055160273;  // api/constants.h
 }  // namespace
 
+// 1/r and exp(-mu r)/r as sums of Gaussians from a truncated trapezoidal
+// rule in s after the substitution that turns the kernel's integral
+// representation into a sum of Gaussians in r (PoissonKernel.cpp:48-86,
+// HelmholtzKernel.cpp:47-80).  The steps, the operation order and the long
+// double literals are the reference's: the number of terms and every exponent
+// depend on their rounding, and the reference's tests pin the term counts
+// (26 for Poisson at 1e-5, 33 for Helmholtz).  Lengths are in units of
+// r_max; the rule runs over s in [s_lo, s_hi] with step `step`, end points
+// at half weight.
 std::vector<GaussFunc<1>> poisson_kernel(double epsilon, double r_min, double r_max) {
     std::vector<GaussFunc<1>> out;
-    double r0 = r_min / r_max;
-    double r1 = r_max;
-    double t1 = 1.0L;
-    while ((2.0 * t1 * std::exp(-t1)) > epsilon) t1 *= 1.1L;
-    double t2 = 1.0L;
-    while ((std::sqrt(t2) * std::exp(-t2) / r0) > epsilon) t2 *= 1.1L;
-    double s1 = -std::log(2.0 * t1);
-    double s2 = std::log(t2 / (r0 * r0)) / 2.0;
-    double h = 1.0 / (0.2L - 0.47L * std::log10(epsilon));
-    int n_exp = static_cast<int>(std::ceil((s2 - s1) / h) + 1);
-    if (n_exp > MaxSepRank) throw Error(1, "Maximum separation rank exceeded.");
-    for (int i = 0; i < n_exp; i++) {
-        double arg = s1 + h * i;
-        double sinharg = std::sinh(arg);
-        double cosharg = std::cosh(arg);
-        double onepexp = 1.0 + std::exp(-sinharg);
-        double expo = 4.0L * (sinharg + std::log(onepexp)) * (sinharg + std::log(onepexp));
-        double coef = h * (4.0L / root_pi) * cosharg / onepexp;
-        expo *= 1.0 / (r1 * r1);
-        coef *= 1.0 / r1;
-        if (i == 0 || i == (n_exp - 1)) coef *= 1.0 / 2.0;
-        out.push_back(GaussFunc<1>(expo, coef));
+    const double r_rel = r_min / r_max, unit = r_max;
+    // where the integrand has decayed below epsilon at both ends
+    double t_lo = 1.0L;
+    while ((2.0 * t_lo * std::exp(-t_lo)) > epsilon) t_lo *= 1.1L;
+    double t_hi = 1.0L;
+    while ((std::sqrt(t_hi) * std::exp(-t_hi) / r_rel) > epsilon) t_hi *= 1.1L;
+    const double s_lo = -std::log(2.0 * t_lo);
+    const double s_hi = std::log(t_hi / (r_rel * r_rel)) / 2.0;
+    const double step = 1.0 / (0.2L - 0.47L * std::log10(epsilon));
+    const int n_terms = static_cast<int>(std::ceil((s_hi - s_lo) / step) + 1);
+    if (n_terms > MaxSepRank) throw Error(1, "Maximum separation rank exceeded.");
+    for (int k = 0; k < n_terms; k++) {
+        const double s = s_lo + step * k;
+        const double sh = std::sinh(s), ch = std::cosh(s);
+        const double w = 1.0 + std::exp(-sh);
+        double alpha = 4.0L * (sh + std::log(w)) * (sh + std::log(w));
+        double beta = step * (4.0L / root_pi) * ch / w;
+        alpha *= 1.0 / (unit * unit);
+        beta *= 1.0 / unit;
+        if (k == 0 || k == (n_terms - 1)) beta *= 1.0 / 2.0;
+        out.push_back(GaussFunc<1>(alpha, beta));
     }
     return out;
 }
 
 std::vector<GaussFunc<1>> helmholtz_kernel(double mu, double epsilon, double r_min, double r_max) {
     std::vector<GaussFunc<1>> out;
-    double r0 = r_min / r_max;
-    double r1 = r_max;
-    double mu_tilde = mu * r1;
-    double t = std::max((-2.5L * std::log(epsilon)), 5.0L);
-    double s1 = -std::log(4 * t / (mu_tilde * mu_tilde)) / 2;
-    double s2 = std::log(t / (r0 * r0)) / 2;
-    double h = 1.0 / (0.20L - 0.47L * std::log10(epsilon));
-    int n_exp = static_cast<int>(std::ceil((s2 - s1) / h) + 1);
-    if (n_exp > MaxSepRank) throw Error(1, "Maximum separation rank exceeded.");
-    for (int i = 0; i < n_exp; i++) {
-        double arg = s1 + h * i;
-        double temp = -arg * 2.0;
-        double temp2 = -mu_tilde * mu_tilde * std::exp(temp) / 4.0 + arg;
-        double beta = (h * (2.0 / root_pi) * std::exp(temp2));
-        double temp3 = 2.0L * arg;
-        double alpha = std::exp(temp3);
-        alpha *= 1.0 / (r1 * r1);
-        beta *= 1.0 / r1;
-        if (i == 0 || i == (n_exp - 1)) beta *= 1.0 / 2.0;
+    const double r_rel = r_min / r_max, unit = r_max;
+    const double mu_u = mu * unit;  // mu in units of r_max
+    const double t = std::max((-2.5L * std::log(epsilon)), 5.0L);
+    const double s_lo = -std::log(4 * t / (mu_u * mu_u)) / 2;
+    const double s_hi = std::log(t / (r_rel * r_rel)) / 2;
+    const double step = 1.0 / (0.20L - 0.47L * std::log10(epsilon));
+    const int n_terms = static_cast<int>(std::ceil((s_hi - s_lo) / step) + 1);
+    if (n_terms > MaxSepRank) throw Error(1, "Maximum separation rank exceeded.");
+    for (int k = 0; k < n_terms; k++) {
+        const double s = s_lo + step * k;
+        const double two_s_neg = -s * 2.0;
+        const double log_w = -mu_u * mu_u * std::exp(two_s_neg) / 4.0 + s;
+        double beta = (step * (2.0 / root_pi) * std::exp(log_w));
+        const double two_s = 2.0L * s;
+        double alpha = std::exp(two_s);
+        alpha *= 1.0 / (unit * unit);
+        beta *= 1.0 / unit;
+        if (k == 0 || k == (n_terms - 1)) beta *= 1.0 / 2.0;
         out.push_back(GaussFunc<1>(alpha, beta));
     }
     return out;
