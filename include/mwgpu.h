@@ -284,6 +284,12 @@ mwgpu_status mwgpu_plan_info(const mwgpu_plan *plan, long long *chunk_items, int
  * the contraction in ms; chosen = the index in use (-1 without autotuning).
  * n_candidates: in = room in the arrays (any may be NULL), out = number tried. */
 mwgpu_status mwgpu_plan_tuning(const mwgpu_plan *plan, int *n_candidates, long long *chunk_items, int *schedule, double *ms, int *chosen);
+
+/* Peak FP64 rates of this GPU in TFLOP/s, measured with CUDA events: chains of
+ * independent DFMA per thread, and of mma.sync m8n8k4 f64 (DMMA) per warp, 4
+ * CTAs of 256 threads per SM.  No reference counterpart: the measurement
+ * behind the FP64 form's choice of pipe (it runs on DFMA). */
+mwgpu_status mwgpu_fp64_pipe_rates(mwgpu_ctx *ctx, double *dfma_tflops, double *dmma_tflops);
 mwgpu_status mwgpu_plan_destroy(mwgpu_ctx *ctx, mwgpu_plan *plan);
 /* New coefficients (and norms, or NULL to compute them) of all nodes of an
  * input tree with unchanged topology; refreshes the FP32 copy.  GenNodes are

@@ -113,6 +113,7 @@ _SIGS = {
     "mwgpu_plan_info": (C.c_int, [_P, C.POINTER(C.c_longlong), _PI, _PI, C.POINTER(C.c_longlong), _PD, C.POINTER(C.c_ulonglong)]),
     "mwgpu_plan_pencil_info": (C.c_int, [_P, C.POINTER(C.c_ulonglong), _PD]),
     "mwgpu_plan_tuning": (C.c_int, [_P, _PI, C.POINTER(C.c_longlong), _PI, _PD, _PI]),
+    "mwgpu_fp64_pipe_rates": (C.c_int, [_P, _PD, _PD]),
     "mwgpu_plan_destroy": (C.c_int, [_P, _P]),
     "mwgpu_tree_update_coefs": (C.c_int, [_P, _P, _PD, _PD]),
     "mwgpu_apply_judged": (C.c_int, [_P, _P, _P, _P, C.c_int, _PI, C.c_double, C.c_int, C.c_int, _PD, C.c_int, _PI, _PI, _PD,

@@ -2277,6 +2277,46 @@ extern "C" mwgpu_status mwgpu_plan_info(const mwgpu_plan *pl, long long *chunk_i
     return MWGPU_OK;
 }
 
+extern "C" mwgpu_status mwgpu_fp64_pipe_rates(mwgpu_ctx *ctx, double *dfma_tflops, double *dmma_tflops) {
+    if (!ctx || !dfma_tflops || !dmma_tflops) return MWGPU_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int blocks = std::max(1, sms) * 4, iters = 2048;
+    double *out = nullptr;
+    MW_CK(cudaMalloc(&out, sizeof(double) * (size_t)blocks * rate_threads()));
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    auto timed = [&](bool dmma) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(a, ctx->stream);
+            if (dmma) launch_rate_dmma(out, blocks, iters, ctx->stream);
+            else launch_rate_dfma(out, blocks, iters, ctx->stream);
+            cudaEventRecord(b, ctx->stream);
+            cudaEventSynchronize(b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (rep > 0) best = std::min(best, ms);  // the first launch warms up
+        }
+        return best;
+    };
+    const float t_dfma = timed(false), t_dmma = timed(true);
+    const cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    ctx->launches += 6;
+    if (e != cudaSuccess) {
+        ctx->err = std::string("fp64 pipe rates: ") + cudaGetErrorString(e);
+        return MWGPU_ERR_DEVICE;
+    }
+    *dfma_tflops = rate_dfma_flops(blocks, iters) / (t_dfma * 1e-3) / 1e12;
+    *dmma_tflops = rate_dmma_flops(blocks, iters) / (t_dmma * 1e-3) / 1e12;
+    return MWGPU_OK;
+}
+
 extern "C" mwgpu_status mwgpu_plan_tuning(const mwgpu_plan *pl, int *n_candidates, long long *chunk_items, int *schedule, double *ms,
                                           int *chosen) {
     if (!pl || !n_candidates) return MWGPU_ERR_BAD_ARG;

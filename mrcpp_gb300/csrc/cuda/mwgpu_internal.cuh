@@ -311,6 +311,12 @@ void launch_combine(const DevMRA &m, bool mul, const DevTree *ins, const double 
                     const double *cv_map, const double *vc_map, int *err, cudaStream_t s);
 // ProjectionCalculator::calcNode of a Gaussian sum (gauss [ng][5]: coefficient,
 // exponent, position) for the given nodes; vc_map (K x K) and roots (K) of the basis
+// peak-rate probes of the FP64 pipes (k_rates.cu)
+void launch_rate_dfma(double *out, int blocks, int iters, cudaStream_t s);
+void launch_rate_dmma(double *out, int blocks, int iters, cudaStream_t s);
+double rate_dfma_flops(int blocks, int iters);
+double rate_dmma_flops(int blocks, int iters);
+int rate_threads();
 // values: the function at the children's quadrature points (8 (k+1)^3 per node), or null for the Gaussians
 void launch_project(const DevMRA &m, DevTree t, const int *nodes, int n, const double *gauss, int ng, const double *vc_map,
                     const double *roots, cudaStream_t s, const double *values = nullptr);

@@ -64,3 +64,20 @@ def test_block_and_component_schedules(gpu, case):
         out[comp] = gx["coefs"]
     d = np.abs(out[False] - out[True]).max() / np.abs(out[True]).max()
     assert d <= 1e-13, (case, d)
+
+
+def test_fp64_pipe_rates(gpu):
+    # the FP64 form runs on DFMA: measured, DMMA (mma.sync m8n8k4 f64) peaks
+    # lower on this GPU (1.26 against 1.10 TFLOP/s when written)
+    import ctypes as C
+
+    L = mw.lib()
+    ctx = C.c_void_p()
+    assert L.mwgpu_init(C.byref(ctx), C.byref(mw.MwgpuConfig())) == 0
+    try:
+        a, b = C.c_double(), C.c_double()
+        assert L.mwgpu_fp64_pipe_rates(ctx, C.byref(a), C.byref(b)) == 0
+        assert a.value > 0.1 and b.value > 0.1
+        assert a.value >= 0.95 * b.value, (a.value, b.value)
+    finally:
+        L.mwgpu_destroy(ctx)
