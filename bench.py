@@ -559,6 +559,7 @@ def main_learned(args, rank, world, local, pg):
         mw.apply(PREC, mw.FunctionTree(mra), P, fs[0], precision=mw.MIXED)
         mw.apply_learned(PREC, mw.FunctionTree(mra), P, fs[0], net, threshold=thr, full_levels=full, precision=mw.MIXED)
     plain_t, learned_t, nt_p, nt_l, it_p, it_l, rt_l, cont, same, diffs, contract, launches = [], [], 0, 0, [], [], [], 0, 0, [], 0.0, 0
+    fp64_t, nt_64 = [], 0
     with ClockSampler(local) as cs:
         for f in fs:
             # each density REPEATS times, the two methods alternating; the
@@ -575,6 +576,12 @@ def main_learned(args, rank, world, local, pg):
                 tl.append(time.perf_counter() - t0)
             plain_t.append(statistics.median(tp))
             learned_t.append(statistics.median(tl))
+            # the plain FP64 form on the same density (one apply)
+            g2 = mw.FunctionTree(mra)
+            t0 = time.perf_counter()
+            s64 = mw.apply(PREC, g2, P, f, precision=mw.FP64)
+            fp64_t.append(time.perf_counter() - t0)
+            nt_64 += s64["node_terms"]
             nt_p += sp["node_terms"]
             nt_l += sl["apply"]["node_terms"]
             it_p.append(sp["iterations"])
@@ -602,6 +609,11 @@ def main_learned(args, rank, world, local, pg):
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                         "note": "the adaptive apply is end to end by construction (host FunctionTrees)"},
                 "plain": {"value": nt_p / t_p, "unit": UNIT, "ms_per_step": 1e3 * t_p / len(fs), "iterations_mean": float(np.mean(it_p))},
+                "fp64_plain": {"value": nt_64 / sum(fp64_t), "unit": UNIT, "ms_per_step": 1e3 * sum(fp64_t) / len(fs),
+                               "learned_mixed_vs_fp64_wall": sum(fp64_t) / t_l,
+                               "note": "the plain FP64 form, plain refinement, one apply per density (the target "
+                                       "configuration: mixed apply with the learned grid against separate FP64 applies; "
+                                       "the learned apply takes one function per call)"},
                 "learned": {"judged_passes_mean": float(np.mean(it_l)), "host_round_trips_mean": float(np.mean(rt_l)),
                             "densities_with_more_passes": cont, "same_topology": same, "max_rel_diff": max(diffs) if diffs else None,
                             "speedup_wall": t_p / t_l},

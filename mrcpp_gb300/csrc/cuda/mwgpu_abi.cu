@@ -308,11 +308,13 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
     const DevMRA &m = o->mra;
     const int G = o->pen_groups, n = lv.n;
     constexpr int G5 = mwgpu::kPencilGroup, NK = mwgpu::kPencilMaxL + 1, NS = mwgpu::kPencilSlots;
-    std::vector<std::vector<PencilUnit>> tasks;
+    // units in creation order, task t's units at flat[tstart[t] .. tstart[t+1])
+    std::vector<PencilUnit> flat;
+    std::vector<int> tstart;
     std::vector<long long> cost;
     pp.pen_begin.assign(n + 1, 0);
     for (int wi = 0; wi < n; wi++) {
-        pp.pen_begin[wi] = (int)tasks.size();
+        pp.pen_begin[wi] = (int)tstart.size();
         const int4 gx = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]];
         const int depth = gx.x - m.root_scale;
         if (depth < 0 || depth >= o->n_rows || o->band_max[depth] < 0) continue;
@@ -326,7 +328,8 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
         const int gl[3] = {gx.y, gx.z, gx.w};
         for (int lz = -W; lz <= W; lz++) {
             if (!inworld(2, (long long)gl[2] + lz)) continue;
-            std::vector<PencilUnit> us;
+            const size_t first = flat.size();
+            const int task = (int)tstart.size();
             long long c = 0;
             for (int ly = -W; ly <= W; ly++) {
                 if (!inworld(1, (long long)gl[1] + ly)) continue;
@@ -335,7 +338,7 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
                 for (int q = 0; q * G5 < tm; q++) {
                     PencilUnit U{};
                     U.pflags = (short)((q == 0 ? 1 : 0) | ((q + 1) * G5 >= tm ? 2 : 0));
-                    U.task = (int)tasks.size();
+                    U.task = task;
                     U.wi = wi;
                     U.depth = (short)depth;
                     U.ly = (signed char)ly;
@@ -355,27 +358,32 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
                         U.fid[b] = -1;
                         if ((b + 1) / 2 <= xw) c += 2;   // tensor-core products
                     }
-                    us.push_back(U);
+                    flat.push_back(U);
                     c += 3 * U.nt;                       // y / z steps
                 }
             }
-            if (us.empty()) continue;
-            tasks.push_back(std::move(us));
+            if (flat.size() == first) continue;
+            tstart.push_back((int)first);
             cost.push_back(c);
         }
     }
-    pp.pen_begin[n] = (int)tasks.size();
-    pp.n_tasks = (int)tasks.size();
+    tstart.push_back((int)flat.size());
+    pp.n_tasks = (int)cost.size();
+    pp.pen_begin[n] = pp.n_tasks;
+    // tasks in descending cost (the persistent kernel takes them in this order)
     std::vector<int> ord(pp.n_tasks);
     for (int i = 0; i < pp.n_tasks; i++) ord[i] = i;
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-    pp.units.clear();
+    pp.units.resize(flat.size());
     pp.task_unit.assign(pp.n_tasks + 1, 0);
+    size_t pos = 0;
     for (int k = 0; k < pp.n_tasks; k++) {
-        pp.task_unit[k] = (int)pp.units.size();
-        for (auto &U : tasks[ord[k]]) pp.units.push_back(U);
+        pp.task_unit[k] = (int)pos;
+        const int t = ord[k];
+        std::copy(flat.begin() + tstart[t], flat.begin() + tstart[t + 1], pp.units.begin() + pos);
+        pos += (size_t)(tstart[t + 1] - tstart[t]);
     }
-    pp.task_unit[pp.n_tasks] = (int)pp.units.size();
+    pp.task_unit[pp.n_tasks] = (int)pos;
 }
 
 // Mixed form: work list (pair counts, scan, fill) then the contraction over
