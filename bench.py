@@ -65,6 +65,14 @@ EXP_RANGE, CENTRE_RANGE, MU = (1.0, 100.0), (-5.0, 5.0), None
 WORKLOAD = "poisson-apply legendre k=7 box [-32,32]^3, 16 gaussians (exp 1..100, centres [-5,5]^3), prec 1e-5, fixed output grid (maxIter=0)"
 
 
+def host_memory():
+    """How the host trees' coefficients are held (page-locked blocks copy as DMA)."""
+    import mrcpp_gb300 as mw
+
+    st = mw.pinned_stats()
+    return {1: "page-locked", -1: "pageable"}.get(st["state"], "small trees only (C heap)")
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -494,10 +502,10 @@ def main_batch(args, rank, world, local, pg):
                 times.append(dt)
                 h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
         t = reduce_max(pg, statistics.mean(times))
-        return reduce_sum(pg, node_terms) / t, t, h2d, d2h
+        return reduce_sum(pg, node_terms) / t, t, h2d, d2h, [round(x * 1e3, 1) for x in times]
 
-    e2e_value, t_e2e, h2d, d2h = e2e_run(True)
-    e2e_res_value, t_e2e_res, h2d_res, d2h_res = e2e_run(False)
+    e2e_value, t_e2e, h2d, d2h, e2e_steps = e2e_run(True)
+    e2e_res_value, t_e2e_res, h2d_res, d2h_res, e2e_res_steps = e2e_run(False)
     bf16_peak, hbm_peak, peak_kind = load_peaks()
     contraction = {"ms": st.contract_ms, "node_terms": int(node_terms),
                    "tflops": node_terms * flop_per_nt / (st.contract_ms / 1e3) / 1e12,
@@ -525,9 +533,11 @@ def main_batch(args, rank, world, local, pg):
                                     "autotune": tune, "launches_per_step": int(lpe.value)},
                            "setup_s": time.perf_counter() - t_setup},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                        "ms_per_step": t_e2e * 1e3, "inputs": "uploaded every step (pageable host memory)"},
+                        "ms_per_step": t_e2e * 1e3, "ms_steps": e2e_steps, "inputs": "uploaded every step",
+                        "host_memory": host_memory()},
                 "e2e_resident": {"value": e2e_res_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_res), "d2h_bytes_per_step": int(d2h_res),
-                                 "ms_per_step": t_e2e_res * 1e3, "inputs": "unchanged between steps: the device copies are reused"},
+                                 "ms_per_step": t_e2e_res * 1e3, "ms_steps": e2e_res_steps,
+                                 "inputs": "unchanged between steps: the device copies are reused"},
                 "fp64_separate": {"value": value_fp64, "unit": UNIT, "functions_timed": sample, "node_terms": int(fp_nt),
                                   "ms": fp_ms},
                 "mixed_vs_fp64": {"speedup": value / value_fp64, "rel_l2_error_max": max(errs), "rel_l2_errors": errs},
@@ -882,7 +892,7 @@ def main():
                            "band_pairs_per_step": int(st_mixed.band_nodes), "l2": "256 MiB scrub between steps",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                        "ms_per_step": t_e2e * 1e3, "inputs": "uploaded every step (pageable host memory)"},
+                        "ms_per_step": t_e2e * 1e3, "inputs": "uploaded every step", "host_memory": host_memory()},
                 "e2e_resident": {"value": e2e_res_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_res), "d2h_bytes_per_step": int(d2h_res),
                                  "ms_per_step": t_e2e_res * 1e3, "inputs": "unchanged between steps: the device copy is reused"},
                 "step": "one planned level (mwgpu_plan_execute: GenNode values, work list, persistent contraction, reduction, "

@@ -134,7 +134,10 @@ mwgpu_status mwgpu_operator_bandwidths(mwgpu_ctx *ctx, const mwgpu_oper *oper, i
 /* Input tree (the `inp` of apply, compressed s+d form, all nodes).  GenNodes
  * the operator band needs are created on the device from these nodes, like
  * MWTree::getNode (MWTree.cpp:340-352); the host never sees them, matching
- * inp.deleteGenerated() at the end of apply (apply.cpp:86-87). */
+ * inp.deleteGenerated() at the end of apply (apply.cpp:86-87).  The host
+ * arrays may be pageable or page-locked (page-locked ones copy as DMA); either
+ * way they are read in full before the call returns, as in create_tree,
+ * tree_update_coefs, download_tree and download_nodes. */
 mwgpu_status mwgpu_upload_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *tree, mwgpu_tree **out);
 /* Output tree with the given topology and zero coefficients. */
 mwgpu_status mwgpu_create_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tree_desc *tree, mwgpu_tree **out);

@@ -67,6 +67,13 @@ int mwh_mra_maps(const mwh_mra *mra, double *cv_map, double *vc_map, double *roo
 int mwh_mra_distances(const mwh_mra *mra, double eps, double *r_min, double *r_max);
 int mwh_tree_create(const mwh_mra *mra, mwh_tree **out);
 void mwh_tree_free(mwh_tree *tree);
+/* Tree coefficients of 4 MiB and more live in page-locked host memory (so the
+ * device copies of an apply run as DMA), freed blocks in a size-keyed cache;
+ * MWH_PAGEABLE=1 keeps them on the C heap.  Reports the page-locked bytes in
+ * trees and idle in the cache; returns 1 when page-locked memory is in use, -1
+ * when it is declined (no device, or MWH_PAGEABLE=1), 0 before the first
+ * large tree.  No reference counterpart (its trees are pageable). */
+int mwh_pinned_stats(unsigned long long *live_bytes, unsigned long long *idle_bytes);
 /* n Gaussians coef * exp(-exp * |r - pos|^2) (pos: 3n doubles). */
 int mwh_build_grid_gauss(mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos);
 int mwh_project_gauss(double prec, mwh_tree *tree, int n, const double *coef, const double *exp, const double *pos, int max_iter,

@@ -145,6 +145,7 @@ _SIGS = {
     "mwh_mra_maps": (C.c_int, [_P, _PD, _PD, _PD, _PD]),
     "mwh_tree_create": (C.c_int, [_P, C.POINTER(_P)]),
     "mwh_tree_free": (None, [_P]),
+    "mwh_pinned_stats": (C.c_int, [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
     "mwh_build_grid_gauss": (C.c_int, [_P, C.c_int, _PD, _PD, _PD]),
     "mwh_project_gauss": (C.c_int, [C.c_double, _P, C.c_int, _PD, _PD, _PD, C.c_int, C.c_int]),
     "mwh_project_func": (C.c_int, [C.c_double, _P, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
@@ -636,6 +637,16 @@ def prec_factors(prec_trees, idx):
     fac = np.zeros(len(idx))
     _ck(lib().mwh_prec_factors(len(pts), arr, len(idx), _pi(idx), _pd(fac)))
     return fac
+
+
+def pinned_stats():
+    """Host memory of tree coefficients: state 1 when blocks of 4 MiB and more
+    are page-locked (device copies run as DMA), -1 when declined (no device, or
+    MWH_PAGEABLE=1), 0 before the first large tree; with the page-locked bytes
+    held by trees and idle in the cache."""
+    live, idle = C.c_ulonglong(), C.c_ulonglong()
+    state = lib().mwh_pinned_stats(C.byref(live), C.byref(idle))
+    return {"state": int(state), "live_bytes": int(live.value), "idle_bytes": int(idle.value)}
 
 
 def apply_derivative(out, oper, inp, dir):

@@ -586,6 +586,9 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     // ancestors); output trees are addressed by position
     if (input && (s = rebuild_hash(ctx, tr, n))) { free_tree(ctx, tr); return s; }
     trace.mark("hash");
+    // the host arrays may be page-locked, so the copies run asynchronously:
+    // they are read in full before the call returns
+    if (!input) MW_CK(cudaStreamSynchronize(ctx->stream));
     *out = tr;
     return MWGPU_OK;
 }

@@ -37,6 +37,35 @@ constexpr int MaxDepth = 30;
 constexpr int MaxSepRank = 1000;
 constexpr double pi = 3.14159265358979323846;
 
+// Storage of tree coefficients.  Blocks of at least host_block_min() bytes are
+// asked of host_block_alloc first: page-locked host memory kept in a cache
+// (mw_pinned.cpp), so that whole-tree copies between host and device run as
+// direct DMA instead of through the driver's pageable staging buffers.  When
+// page-locked memory cannot be had (no device) the C heap serves.
+size_t host_block_min();
+void *host_block_alloc(size_t bytes);            // nullptr: declined
+bool host_block_release(void *p, size_t bytes);  // false: not a page-locked block
+
+template <class T> struct CoefAllocator {
+    using value_type = T;
+    CoefAllocator() noexcept = default;
+    template <class U> CoefAllocator(const CoefAllocator<U> &) noexcept {}
+    T *allocate(size_t n) {
+        const size_t bytes = n * sizeof(T);
+        if (bytes >= host_block_min())
+            if (void *p = host_block_alloc(bytes)) return static_cast<T *>(p);
+        return std::allocator<T>().allocate(n);
+    }
+    void deallocate(T *p, size_t n) noexcept {
+        const size_t bytes = n * sizeof(T);
+        if (bytes >= host_block_min() && host_block_release(p, bytes)) return;
+        std::allocator<T>().deallocate(p, n);
+    }
+    template <class U> bool operator==(const CoefAllocator<U> &) const noexcept { return true; }
+    template <class U> bool operator!=(const CoefAllocator<U> &) const noexcept { return false; }
+};
+using CoefVector = std::vector<double, CoefAllocator<double>>;
+
 enum BasisType { Legendre = 0, Interpol = 1 };
 enum Operation { Compression = 0, Reconstruction = 1 };
 
@@ -163,7 +192,7 @@ template <int D> struct Tree {
     const MRA<D> *mra;
     int K, kp1_d, nCoefs;
     std::vector<Node> nodes;
-    std::vector<double> coefs;  // nodes.size() * nCoefs
+    CoefVector coefs;  // nodes.size() * nCoefs
     std::unordered_map<NodeKey, int, NodeKeyHash> index;
     std::vector<int> roots;
     double squareNorm = -1.0;

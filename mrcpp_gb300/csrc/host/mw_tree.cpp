@@ -322,7 +322,7 @@ template <int D> void Tree<D>::clearGenerated() {
     if (!any) return;
     std::vector<int> remap(nodes.size(), -1);
     std::vector<Node> nn;
-    std::vector<double> nc;
+    CoefVector nc;
     for (size_t i = 0; i < nodes.size(); i++) {
         if (isGen((int)i)) continue;
         remap[i] = (int)nn.size();
