@@ -22,9 +22,12 @@ screening rules); the count is an integer that equals the oracle's.
   e2e        the same metric through mrcpp_gb300.apply (the host mirror of
              mrcpp::apply) with host buffers: the input tree (marked
              changed before every step) uploaded, level norms and the
-             output-tree download inside the timed region; e2e_resident the
-             same with the input unchanged between steps (its device copy is
-             reused)
+             output-tree download inside the timed region; repeated
+             fixed-grid applies replay the level plan the first apply
+             cached (its cost in first_apply_ms, outside the timed steps);
+             e2e_resident the same with the input unchanged between steps
+             (its device copy is reused); e2e_built with the plan cache off
+             (the level built on every apply, as for a one-off apply)
   fp64       the plain FP64 form on the same workload, on the same block
              schedule as the mixed form (so mixed_vs_fp64 compares precision,
              not algorithm); per_component_schedule: the FP64 form in the
@@ -317,7 +320,7 @@ def plan_tuning(L, plan):
     items, sched, ms, chosen = (C.c_longlong * 32)(), (C.c_int * 32)(), (C.c_double * 32)(), C.c_int()
     if L.mwgpu_plan_tuning(plan, C.byref(n), items, sched, ms, C.byref(chosen)) != 0:
         return None
-    names = {1: "pencil+items", 0: "items"}
+    names = {1: "pencil(8 warps)+items", 2: "pencil(16 warps)+items", 0: "items"}
     return {"candidates": [[int(items[i]), names[sched[i]], round(float(ms[i]), 4)] for i in range(n.value)], "chosen": int(chosen.value)}
 
 
@@ -819,25 +822,38 @@ def main():
     # with new input values every step (the input tree is marked changed before
     # each step, so the step uploads it: e2e), and repeated with the input
     # unchanged (its device copy stays resident: e2e_resident)
-    def e2e_run(touch):
-        times, h2d, d2h = [], 0, 0
-        for i in range(max(args.warmup, 1) + args.steps):
-            g = mw.FunctionTree(mra)
-            mw.copy_grid(g, grid)
-            if touch:
-                f.rescale(1.0)  # exact: the values stay, the tree counts as changed
-            barrier(pg)
-            t0 = time.perf_counter()
-            s = mw.apply(PREC, g, P, f, max_iter=0, precision=mw.MIXED)
-            dt = time.perf_counter() - t0
-            if i >= max(args.warmup, 1):
-                times.append(dt)
-                h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+    # Repeated fixed-grid applies replay the level plan that the first one
+    # cached (planned = 1); e2e_built builds the level every step instead
+    # (MWH_NO_PLAN_CACHE=1, the path of a one-off apply).
+    def e2e_run(touch, cache=True):
+        times, h2d, d2h, planned, first_ms = [], 0, 0, set(), None
+        if not cache:
+            os.environ["MWH_NO_PLAN_CACHE"] = "1"
+        try:
+            for i in range(max(args.warmup, 1) + args.steps):
+                g = mw.FunctionTree(mra)
+                mw.copy_grid(g, grid)
+                if touch:
+                    f.rescale(1.0)  # exact: the values stay, the tree counts as changed
+                barrier(pg)
+                t0 = time.perf_counter()
+                s = mw.apply(PREC, g, P, f, max_iter=0, precision=mw.MIXED)
+                dt = time.perf_counter() - t0
+                if i == 0:
+                    first_ms = dt * 1e3
+                if i >= max(args.warmup, 1):
+                    times.append(dt)
+                    h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+                    planned.add(int(s["planned"]))
+        finally:
+            os.environ.pop("MWH_NO_PLAN_CACHE", None)
         t = reduce_max(pg, statistics.mean(times))
-        return total_nt / t, t, h2d, d2h
+        path = "cached level plan" if planned == {1} else ("built level" if planned == {0} else "mixed: %s" % sorted(planned))
+        return total_nt / t, t, h2d, d2h, path, first_ms
 
-    e2e_value, t_e2e, h2d, d2h = e2e_run(True)
-    e2e_res_value, t_e2e_res, h2d_res, d2h_res = e2e_run(False)
+    e2e_value, t_e2e, h2d, d2h, e2e_path, e2e_first = e2e_run(True)
+    e2e_res_value, t_e2e_res, h2d_res, d2h_res, e2e_res_path, _ = e2e_run(False)
+    e2e_b_value, t_e2e_b, h2d_b, d2h_b, e2e_b_path, _ = e2e_run(True, cache=False)
 
     # roofline of the dominant kernel (mixed form, last timed plan execution):
     # the pencil contraction where the level uses it (order 7), else the item kernel
@@ -892,9 +908,14 @@ def main():
                            "band_pairs_per_step": int(st_mixed.band_nodes), "l2": "256 MiB scrub between steps",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                        "ms_per_step": t_e2e * 1e3, "inputs": "uploaded every step", "host_memory": host_memory()},
+                        "ms_per_step": t_e2e * 1e3, "inputs": "uploaded every step", "host_memory": host_memory(), "path": e2e_path,
+                        "first_apply_ms": e2e_first},
                 "e2e_resident": {"value": e2e_res_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_res), "d2h_bytes_per_step": int(d2h_res),
-                                 "ms_per_step": t_e2e_res * 1e3, "inputs": "unchanged between steps: the device copy is reused"},
+                                 "ms_per_step": t_e2e_res * 1e3, "inputs": "unchanged between steps: the device copy is reused",
+                                 "path": e2e_res_path},
+                "e2e_built": {"value": e2e_b_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_b), "d2h_bytes_per_step": int(d2h_b),
+                              "ms_per_step": t_e2e_b * 1e3, "inputs": "uploaded every step", "path": e2e_b_path,
+                              "note": "plan cache off (MWH_NO_PLAN_CACHE=1): the level built on every apply"},
                 "step": "one planned level (mwgpu_plan_execute: GenNode values, work list, persistent contraction, reduction, "
                         "TopDown and BottomUp replayed as one CUDA graph)",
                 "autotune": pencil[2],

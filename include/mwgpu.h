@@ -283,7 +283,8 @@ mwgpu_status mwgpu_plan_pencil_info(const mwgpu_plan *plan, unsigned long long *
 mwgpu_status mwgpu_plan_info(const mwgpu_plan *plan, long long *chunk_items, int *grid, int *n_candidates, long long *cand_items,
                              double *cand_ms, unsigned long long *launches);
 /* The autotuning candidates of a plan: per candidate the chunk length, the
- * schedule (1: pencil + item kernels, 0: item kernel alone) and the time of
+ * schedule (1: pencil kernel with 8 consumer warps per CTA + item kernel,
+ * 2: the same with 16 consumer warps, 0: item kernel alone) and the time of
  * the contraction in ms; chosen = the index in use (-1 without autotuning).
  * n_candidates: in = room in the arrays (any may be NULL), out = number tried. */
 mwgpu_status mwgpu_plan_tuning(const mwgpu_plan *plan, int *n_candidates, long long *chunk_items, int *schedule, double *ms, int *chosen);

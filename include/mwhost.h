@@ -43,6 +43,8 @@ typedef struct {
     unsigned long long launches;   /* kernels launched by this apply */
     unsigned long long h2d_bytes;  /* host-to-device bytes copied by this apply */
     unsigned long long d2h_bytes;  /* device-to-host bytes copied by this apply */
+    int planned;                   /* 1: a fixed-grid apply replayed a cached level plan,
+                                      2: it created that plan, 0: built the level */
 } mwh_apply_stats;
 
 const char *mwh_last_error(void);

@@ -64,7 +64,7 @@ class MwhApplyStats(C.Structure):
     _fields_ = [("node_terms", C.c_ulonglong), ("components", C.c_ulonglong), ("band_nodes", C.c_ulonglong),
                 ("gen_nodes", C.c_ulonglong), ("iterations", C.c_int), ("out_nodes", C.c_int), ("device_ms", C.c_double),
                 ("contract_ms", C.c_double), ("transform_ms", C.c_double), ("wall_ms", C.c_double),
-                ("launches", C.c_ulonglong), ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong)]
+                ("launches", C.c_ulonglong), ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong), ("planned", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -183,8 +183,10 @@ __device__ __forceinline__ void split_tf32(float x, unsigned &hi, unsigned &lo) 
     lo = __float_as_uint(x - __uint_as_float(hi));
 }
 
+// (not volatile: a pure function of its operands, free to be scheduled
+// between independent products)
 __device__ __forceinline__ void mma_tf32(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3, unsigned b0, unsigned b1) {
-    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                  : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
@@ -207,11 +209,13 @@ __device__ __forceinline__ void task_mma(const float *const (&in)[NS], const flo
     using S = Shape<K>;
     static_assert(K == 8, "tensor-core path for K = 8");
     const int g = lane >> 2, t = lane & 3;
-    float d[4][4];
+    // hi.hi products in d, the two correction products in dl: two dependency
+    // chains per m-tile
+    float d[4][4], dl[4][4];
 #pragma unroll
     for (int mt = 0; mt < 4; mt++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) d[mt][v] = 0.f;
+        for (int v = 0; v < 4; v++) d[mt][v] = dl[mt][v] = 0.f;
 #pragma unroll
     for (int p = 0; p < NS; p++) {
         if (!((valid >> p) & 1u)) continue;
@@ -241,16 +245,16 @@ __device__ __forceinline__ void task_mma(const float *const (&in)[NS], const flo
             for (int q = 0; q < 4; q++) split_tf32(x[q], ah[mt][q], al[mt][q]);
         }
 #pragma unroll
-        for (int mt = 0; mt < 4; mt++) mma_tf32(d[mt], al[mt][0], al[mt][1], al[mt][2], al[mt][3], bh0, bh1);
-#pragma unroll
-        for (int mt = 0; mt < 4; mt++) mma_tf32(d[mt], ah[mt][0], ah[mt][1], ah[mt][2], ah[mt][3], bl0, bl1);
+        for (int mt = 0; mt < 4; mt++) mma_tf32(dl[mt], al[mt][0], al[mt][1], al[mt][2], al[mt][3], bh0, bh1);
 #pragma unroll
         for (int mt = 0; mt < 4; mt++) mma_tf32(d[mt], ah[mt][0], ah[mt][1], ah[mt][2], ah[mt][3], bh0, bh1);
+#pragma unroll
+        for (int mt = 0; mt < 4; mt++) mma_tf32(dl[mt], ah[mt][0], ah[mt][1], ah[mt][2], ah[mt][3], bl0, bl1);
     }
 #pragma unroll
     for (int mt = 0; mt < 4; mt++)
 #pragma unroll
-        for (int v = 0; v < 4; v++) s[mt >> 1][4 * (mt & 1) + v] = d[mt][v];
+        for (int v = 0; v < 4; v++) s[mt >> 1][4 * (mt & 1) + v] = d[mt][v] + dl[mt][v];
 }
 
 // One m-tile (rows 16 mt .. 16 mt + 15) of a one-input task on the tensor cores:

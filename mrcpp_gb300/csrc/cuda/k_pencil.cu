@@ -41,14 +41,16 @@
 // block into P, and P goes through z with the B block only (a2 = 1), which
 // leaves out exactly the T.T.T path from f[0] to g[0].
 //
-// Roles (320 threads): warp 0 lane 0 stages operands with cp.async.bulk into
-// mbarrier-tracked slots (a pencil's f nodes once for all its term groups,
-// stacked operator forms, per-term operator blocks); warp 1 lane 0 issues the
-// tensor-core products and commits into one of two TMEM buffers, so that the
-// products of the next unit overlap the consumers; warps 2-9 (consumers; warp
-// 2 + w owns x = 2 w, 2 w + 1) read TMEM, transpose S1 through shared memory,
-// run the y / z steps and keep the g accumulators (FP32 sums per unit,
-// compensated sums over the units) of the task.  A task is (g, l_z): its
+// Roles (128 + 32 x 8 threads): warp 0 lane 0 stages operands with
+// cp.async.bulk into mbarrier-tracked slots (a pencil's f nodes once for all
+// its term groups, stacked operator forms, per-term operator blocks); warp 1
+// lane 0 issues the tensor-core products and commits into one of two TMEM
+// buffers, so that the products of the next unit overlap the consumers; warps
+// 2 and 3 only give their registers to the consumers (setmaxnreg); warps 4-11
+// (consumers; warp 4 + w owns x = w and w + 8, so that each has one x of the U
+// channel; or warps 4-19 with one x each) read TMEM, transpose S1 through
+// shared memory, run the y / z steps and keep the g accumulators (FP32 sums
+// per unit, compensated sums over the units) of the task.  A task is (g, l_z): its
 // pencils x their term groups ("units", made by the host and
 // k_pencil_units); its 8 (k+1)^3 sums go to pen_partial[slot] in FP64, and the
 // chunk reduction adds the tasks of g after its chunk partials.
@@ -61,9 +63,18 @@
 namespace mwgpu {
 namespace pencil {
 
-constexpr int NT = 320;                    // threads: producer warp, MMA warp, 8 consumer warps
-constexpr int NCW = 8;                     // consumer warps
-constexpr int GT = kPencilGroup;           // terms per group (per product)
+// threads: warpgroup 0 (producer warp, MMA warp, two idle warps), then NCW
+// consumer warps (8 or 16: a tile-shape parameter of the plan autotuner; 16
+// warps own one x each, 8 warps two)
+template <int NCW> __host__ __device__ constexpr int n_threads() { return 128 + 32 * NCW; }
+// register split (setmaxnreg): warpgroup 0 hands registers to the consumer
+// warpgroups.  The shares must fit in what the CTA is launched with (threads x
+// registers per thread): checked on the host before the first launch
+// (pencil_shape_ok), since a setmaxnreg.inc that cannot be served waits.
+template <int NCW> struct Regs;
+template <> struct Regs<8> { static constexpr int prod = 56, cons = 216; };
+template <> struct Regs<16> { static constexpr int prod = 40, cons = 104; };
+constexpr int GT = kPencilGroup;          // terms per group (per product)
 constexpr int CPT = 24;                    // D columns per term
 constexpr int NMAX = (GT * CPT + 15) / 16 * 16;   // 128: two D buffers of two tiles fit the 512 TMEM columns
 constexpr int NFS = kPencilSlots;          // f slots: one per x slot of a pencil
@@ -136,15 +147,15 @@ __device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity) {
 }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+template <int NCW> __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * NCW) : "memory"); }
 // true on every consumer thread iff v is true on all of them (named barrier 1,
 // so that control flow around the consumers' barriers stays uniform)
-__device__ __forceinline__ bool consumers_all(bool v) {
+template <int NCW> __device__ __forceinline__ bool consumers_all(bool v) {
     uint32_t r;
     asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 1, 256, q;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, 1, %2, q;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(r)
-        : "r"((uint32_t)v)
+        : "r"((uint32_t)v), "n"(32 * NCW)
         : "memory");
     return r != 0;
 }
@@ -154,6 +165,17 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4]) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];" : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(taddr));
 #pragma unroll
     for (int i = 0; i < 4; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, float (&v)[2]) {
+    uint32_t r[2];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+    v[0] = __uint_as_float(r[0]);
+    v[1] = __uint_as_float(r[1]);
+}
+// n consecutive TMEM columns of this thread's lane (n = 4 or 2)
+template <int n> __device__ __forceinline__ void tmem_ldn(uint32_t taddr, float (&v)[n]) {
+    if constexpr (n == 4) tmem_ld4(taddr, v);
+    else tmem_ld2(taddr, v);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -165,8 +187,10 @@ __device__ __forceinline__ void split(float x, float &hi, float &lo) {
     lo = x - hi;
 }
 
+// (not volatile: a pure function of its operands, so that independent products
+// can be scheduled between dependent ones)
 __device__ __forceinline__ void mma16(float (&d)[4], const float (&a)[4], const float (&b)[2]) {
-    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                  : "r"(__float_as_uint(a[0])), "r"(__float_as_uint(a[1])), "r"(__float_as_uint(a[2])), "r"(__float_as_uint(a[3])),
                    "r"(__float_as_uint(b[0])), "r"(__float_as_uint(b[1])));
@@ -284,8 +308,13 @@ __global__ void k_pencil_units(DevMRA m, const DevTree *fs, const DevTree *gs, c
 
 // ---------------------------------------------------------------------------
 // The contraction.
-__global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs, const int *work_tree, const Unit *units, const int *task_unit,
-                                                  int n_tasks, double *pen_partial, int *err, int *counter) {
+template <int NCW>
+__global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, const DevTree *fs, const int *work_tree, const Unit *units,
+                                                               const int *task_unit, int n_tasks, double *pen_partial, int *err, int *counter) {
+    static_assert(NCW == 8 || NCW == 16, "consumer warps");
+    constexpr int NT = n_threads<NCW>();
+    constexpr int XPW = 16 / NCW;   // x values per consumer warp
+    constexpr int CPP = 32 / NCW;   // drained columns of each 8-column block per consumer warp
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ __align__(8) uint64_t f_full[NFS], f_empty[NFS], b_full[2], b_empty[2], o_full[2], o_empty[2], d_full[2], d_empty[2], bar_end;
     __shared__ uint32_t s_tmem;
@@ -332,328 +361,406 @@ __global__ void __launch_bounds__(NT, 1) k_pencil(DevOper op, const DevTree *fs,
         if (!lbad) atomicOr(err, DE_TIMEOUT);
         lbad = true;
     };
-    // consumer warp cw owns x = 2 cw, 2 cw + 1; fragment coordinates g (group), tq (thread in group)
-    const int cw = warp >= 2 ? warp - 2 : 0;
-    const int x0 = 2 * cw, fg = lane >> 2, tq = lane & 3;
+    // consumer warp cw owns x = cw + NCW xi (xi < XPW: with 8 warps one x of the
+    // U channel (x < 8) and one without, so that the warps' work per term is
+    // even); fragment coordinates g (group), tq (thread in group)
+    const int cw = warp >= 4 ? warp - 4 : 0;
+    const int fg = lane >> 2, tq = lane & 3;
+    auto xof = [&](int xi) { return cw + NCW * xi; };
     float *S1base = reinterpret_cast<float *>(sm + SM_S1);
-    float G[16], Gc[16];
 
-    for (;;) {
-        if (tid == 0) s_task = atomicAdd(counter, 1);
-        __syncthreads();
-        const int task = s_task;
-        if (task >= n_tasks) break;
-        const int u0 = task_unit[task], u1 = task_unit[task + 1];
-#pragma unroll
-        for (int i = 0; i < 16; i++) G[i] = Gc[i] = 0.f;
-
-        if (warp == 0) {
-            // ---------------- producer ----------------
-            if (lane == 0 && !lbad) {
-                for (int u = u0; u < u1 && !lbad; u++) {
-                    const Unit &U = units[u];
-                    const DevTree &f = fs[work_tree[U.wi]];
-                    if (U.pflags & 1) {
-                        // the pencil's f nodes, once for all its term groups (the first group has the widest window)
+    // each role runs its own task loop after the register split (the CTA
+    // barriers of a task match across the roles: one sync, one reduction)
+    if (warp < 4) {
+        asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(Regs<NCW>::prod));
+        for (;;) {
+            if (tid == 0) s_task = atomicAdd(counter, 1);
+            __syncthreads();
+            const int task = s_task;
+            if (task >= n_tasks) break;
+            const int u0 = task_unit[task], u1 = task_unit[task + 1];
+            if (warp == 0) {
+                // ---------------- producer ----------------
+                if (lane == 0 && !lbad) {
+                    for (int u = u0; u < u1 && !lbad; u++) {
+                        const Unit &U = units[u];
+                        const DevTree &f = fs[work_tree[U.wi]];
+                        if (U.pflags & 1) {
+                            // the pencil's f nodes, once for all its term groups (the first group has the widest window)
+                            for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                                const int fid = U.fid[b];
+                                if (fid < 0) continue;
+                                if (nfs[b] >= 1 && !bar_wait(&f_empty[b], (nfs[b] - 1) & 1)) { fail(); break; }
+                                if (fid < f.cap_real) {
+                                    expect_tx(&f_full[b], FREC);
+                                    bulk(sm + SM_F + b * FREC, f.tc32 + (size_t)fid * kTcNodeFloats, FREC, &f_full[b]);
+                                } else {
+                                    const float *src = f.gtc32 + (size_t)(fid - f.cap_real) * kTcGenFloats;
+                                    unsigned char *dst = sm + SM_G + b * GREC;
+                                    expect_tx(&f_full[b], 4096);
+                                    bulk(dst, src, 1024, &f_full[b]);               // hi, k chunk 0, rows 0-63
+                                    bulk(dst + 2048, src + 256, 1024, &f_full[b]);  // hi, k chunk 1
+                                    bulk(dst + 4096, src + 512, 1024, &f_full[b]);  // lo, k chunk 0
+                                    bulk(dst + 6144, src + 768, 1024, &f_full[b]);  // lo, k chunk 1
+                                }
+                                nfs[b]++;
+                            }
+                        }
+                        for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                            if (U.fid[b] < 0) continue;
+                            const int s = nb & 1;
+                            if (nb >= 2 && !bar_wait(&b_empty[s], ((nb >> 1) - 1) & 1)) { fail(); break; }
+                            const uint32_t bytes = 128u * (uint32_t)n_pad(U.nform[b]);
+                            expect_tx(&b_full[s], bytes);
+                            bulk(sm + SM_B + s * BREC, op.btc_stack + U.form[b], bytes, &b_full[s]);
+                            nb++;
+                        }
+                        if (lbad) break;
+                        // per-term O^y(l_y), O^z(l_z) blocks for the consumers
+                        const int so = nu & 1;
+                        if (nu >= 2 && !bar_wait(&o_empty[so], ((nu >> 1) - 1) & 1)) { fail(); break; }
+                        expect_tx(&o_full[so], (uint32_t)U.nt * 2048u);
+                        for (int j = 0; j < U.nt; j++) {
+                            const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
+                            unsigned char *dst = sm + SM_O + so * OREC + j * 2048;
+                            bulk(dst, op.blocks32 + (size_t)(row.off + U.ly + row.L0) * 256, 1024, &o_full[so]);
+                            bulk(dst + 1024, op.blocks32 + (size_t)(row.off + U.lz + row.L0) * 256, 1024, &o_full[so]);
+                        }
+                        nu++;
+                    }
+                }
+            } else if (warp == 1) {
+                // ---------------- MMA issue ----------------
+                if (lane == 0 && !lbad) {
+                    for (int u = u0; u < u1 && !lbad; u++) {
+                        const Unit &U = units[u];
+                        const DevTree &f = fs[work_tree[U.wi]];
+                        const int db = nu & 1;
+                        if (U.pflags & 1) {
+                            // the pencil's f nodes are staged
+                            pmask = 0;
+                            for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
+                                if (U.fid[b] < 0) continue;
+                                if (!bar_wait(&f_full[b], nfs[b] & 1)) { fail(); break; }
+                                pmask |= 1u << b;
+                            }
+                            if (lbad) break;
+                        }
+                        // the consumers have read this D buffer (unit nu - 2)
+                        if (nu >= 2 && !bar_wait(&d_empty[db], ((nu >> 1) - 1) & 1)) { fail(); break; }
+                        fence_after();
+                        const uint32_t dbase = tmem + 256u * db;
+                        bool first[2] = {true, true};
                         for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
                             const int fid = U.fid[b];
                             if (fid < 0) continue;
-                            if (nfs[b] >= 1 && !bar_wait(&f_empty[b], (nfs[b] - 1) & 1)) { fail(); break; }
-                            if (fid < f.cap_real) {
-                                expect_tx(&f_full[b], FREC);
-                                bulk(sm + SM_F + b * FREC, f.tc32 + (size_t)fid * kTcNodeFloats, FREC, &f_full[b]);
-                            } else {
-                                const float *src = f.gtc32 + (size_t)(fid - f.cap_real) * kTcGenFloats;
-                                unsigned char *dst = sm + SM_G + b * GREC;
-                                expect_tx(&f_full[b], 4096);
-                                bulk(dst, src, 1024, &f_full[b]);               // hi, k chunk 0, rows 0-63
-                                bulk(dst + 2048, src + 256, 1024, &f_full[b]);  // hi, k chunk 1
-                                bulk(dst + 4096, src + 512, 1024, &f_full[b]);  // lo, k chunk 0
-                                bulk(dst + 6144, src + 768, 1024, &f_full[b]);  // lo, k chunk 1
-                            }
-                            nfs[b]++;
+                            const bool gen = fid >= f.cap_real;
+                            const uint32_t a_hi = gen ? su32(sm + SM_G + b * GREC) : su32(sm + SM_F + b * FREC);
+                            const int nt_tiles = gen ? 1 : 2, nks = gen ? 1 : 2;
+                            const int sbix = nb & 1;
+                            if (!bar_wait(&b_full[sbix], (nb >> 1) & 1)) { fail(); break; }
+                            nb++;
+                            fence_after();
+                            const int nt = U.ntk[(b + 1) >> 1];
+                            const int N = n_pad(nt), NF = n_pad(U.nform[b]);   // product N; the form's own N sets its layout
+                            const uint32_t id = idesc(128, N);
+                            const uint32_t b_hi = su32(sm + SM_B + sbix * BREC), b_lo = b_hi + 64u * NF;
+                            // real nodes: region (tile t, k step s) at (2 t + s) 4 KB, lo at +16 KB;
+                            // GenNodes: one region, lo at +4 KB
+                            const uint32_t lo_off = gen ? 4096u : 16384u;
+                            for (int t = 0; t < nt_tiles; t++)
+                                for (int s = 0; s < nks; s++) {
+                                    const uint32_t ao = gen ? 0u : (uint32_t)(2 * t + s) * 4096u, bo = (uint32_t)s * 32u * NF;
+                                    const uint64_t ah = sdesc(a_hi + ao, 2048, 128), al = sdesc(a_hi + lo_off + ao, 2048, 128);
+                                    const uint64_t bh = sdesc(b_hi + bo, 128, 256), bl = sdesc(b_lo + bo, 128, 256);
+                                    const uint32_t d = dbase + 128u * t;
+                                    const uint32_t acc0 = (first[t] && s == 0) ? 0u : 1u;
+                                    mma(d, al, bh, id, acc0);
+                                    mma(d, ah, bl, id, 1u);
+                                    mma(d, ah, bh, id, 1u);
+                                }
+                            for (int t = 0; t < nt_tiles; t++) first[t] = false;
+                            commit(&b_empty[sbix]);    // the form slot is free once these products finish
                         }
+                        commit(&d_full[db]);           // also after a failure, so that the consumers are released
+                        if (U.pflags & 2) {
+                            // last group of the pencil: its f slots are free once the products finish
+                            for (int b = 0; b < NFS; b++)
+                                if ((pmask >> b) & 1u) {
+                                    commit(&f_empty[b]);
+                                    nfs[b]++;
+                                }
+                        }
+                        nu++;
                     }
-                    for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
-                        if (U.fid[b] < 0) continue;
-                        const int s = nb & 1;
-                        if (nb >= 2 && !bar_wait(&b_empty[s], ((nb >> 1) - 1) & 1)) { fail(); break; }
-                        const uint32_t bytes = 128u * (uint32_t)n_pad(U.nform[b]);
-                        expect_tx(&b_full[s], bytes);
-                        bulk(sm + SM_B + s * BREC, op.btc_stack + U.form[b], bytes, &b_full[s]);
-                        nb++;
-                    }
-                    if (lbad) break;
-                    // per-term O^y(l_y), O^z(l_z) blocks for the consumers
-                    const int so = nu & 1;
-                    if (nu >= 2 && !bar_wait(&o_empty[so], ((nu >> 1) - 1) & 1)) { fail(); break; }
-                    expect_tx(&o_full[so], (uint32_t)U.nt * 2048u);
-                    for (int j = 0; j < U.nt; j++) {
-                        const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
-                        unsigned char *dst = sm + SM_O + so * OREC + j * 2048;
-                        bulk(dst, op.blocks32 + (size_t)(row.off + U.ly + row.L0) * 256, 1024, &o_full[so]);
-                        bulk(dst + 1024, op.blocks32 + (size_t)(row.off + U.lz + row.L0) * 256, 1024, &o_full[so]);
-                    }
-                    nu++;
                 }
             }
-        } else if (warp == 1) {
-            // ---------------- MMA issue ----------------
-            if (lane == 0 && !lbad) {
-                for (int u = u0; u < u1 && !lbad; u++) {
-                    const Unit &U = units[u];
-                    const DevTree &f = fs[work_tree[U.wi]];
-                    const int db = nu & 1;
-                    if (U.pflags & 1) {
-                        // the pencil's f nodes are staged
-                        pmask = 0;
-                        for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
-                            if (U.fid[b] < 0) continue;
-                            if (!bar_wait(&f_full[b], nfs[b] & 1)) { fail(); break; }
-                            pmask |= 1u << b;
-                        }
-                        if (lbad) break;
-                    }
-                    // the consumers have read this D buffer (unit nu - 2)
-                    if (nu >= 2 && !bar_wait(&d_empty[db], ((nu >> 1) - 1) & 1)) { fail(); break; }
+            // the producer / MMA lanes other than 0 did not walk the units: bring their counters along
+            if (warp <= 1) {
+                nu = __shfl_sync(0xffffffffu, nu, 0);
+                nb = __shfl_sync(0xffffffffu, nb, 0);
+                for (int i = 0; i < NFS; i++) nfs[i] = __shfl_sync(0xffffffffu, nfs[i], 0);
+            }
+            if (__syncthreads_or(lbad) != 0) {
+                lbad = true;
+                break;
+            }
+        }
+    } else {
+        asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(Regs<NCW>::cons));
+        float G[8 * XPW], Gc[8 * XPW];
+        for (;;) {
+            __syncthreads();
+            const int task = s_task;
+            if (task >= n_tasks) break;
+            const int u0 = task_unit[task], u1 = task_unit[task + 1];
+#pragma unroll
+            for (int i = 0; i < 8 * XPW; i++) G[i] = Gc[i] = 0.f;
+            {
+                // ---------------- consumers ----------------
+                const int quarter = warp & 3, part = cw >> 2;   // TMEM lanes 32 quarter ..; drained columns CPP part ..
+                const int r = 32 * quarter + lane;              // D row of this thread: b1 64 + q1 + 8 q2
+                const int b1 = r >> 6, q1 = r & 7, q2 = (r >> 3) & 7;
+                const int yrow = 8 * b1 + q1;
+                unsigned nterm = 0;   // terms drained (S1 buffer parity)
+                for (int u = u0; u < u1; u++) {
+                    const int so = nu & 1, db = nu & 1;
+                    bool ok = !lbad;
+                    if (ok && !bar_wait(&o_full[so], (nu >> 1) & 1)) { fail(); ok = false; }
+                    if (ok && !bar_wait(&d_full[db], (nu >> 1) & 1)) { fail(); ok = false; }
+                    ok = consumers_all<NCW>(ok);
                     fence_after();
-                    const uint32_t dbase = tmem + 256u * db;
-                    bool first[2] = {true, true};
-                    for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
-                        const int fid = U.fid[b];
-                        if (fid < 0) continue;
-                        const bool gen = fid >= f.cap_real;
-                        const uint32_t a_hi = gen ? su32(sm + SM_G + b * GREC) : su32(sm + SM_F + b * FREC);
-                        const int nt_tiles = gen ? 1 : 2, nks = gen ? 1 : 2;
-                        const int sbix = nb & 1;
-                        if (!bar_wait(&b_full[sbix], (nb >> 1) & 1)) { fail(); break; }
-                        nb++;
-                        fence_after();
-                        const int nt = U.ntk[(b + 1) >> 1];
-                        const int N = n_pad(nt), NF = n_pad(U.nform[b]);   // product N; the form's own N sets its layout
-                        const uint32_t id = idesc(128, N);
-                        const uint32_t b_hi = su32(sm + SM_B + sbix * BREC), b_lo = b_hi + 64u * NF;
-                        // real nodes: region (tile t, k step s) at (2 t + s) 4 KB, lo at +16 KB;
-                        // GenNodes: one region, lo at +4 KB
-                        const uint32_t lo_off = gen ? 4096u : 16384u;
-                        for (int t = 0; t < nt_tiles; t++)
-                            for (int s = 0; s < nks; s++) {
-                                const uint32_t ao = gen ? 0u : (uint32_t)(2 * t + s) * 4096u, bo = (uint32_t)s * 32u * NF;
-                                const uint64_t ah = sdesc(a_hi + ao, 2048, 128), al = sdesc(a_hi + lo_off + ao, 2048, 128);
-                                const uint64_t bh = sdesc(b_hi + bo, 128, 256), bl = sdesc(b_lo + bo, 128, 256);
-                                const uint32_t d = dbase + 128u * t;
-                                const uint32_t acc0 = (first[t] && s == 0) ? 0u : 1u;
-                                mma(d, al, bh, id, acc0);
-                                mma(d, ah, bl, id, 1u);
-                                mma(d, ah, bh, id, 1u);
+                    const float *OB = reinterpret_cast<const float *>(sm + SM_O + so * OREC);
+                    const Unit &U = units[u];
+                    const int nw = ok ? U.wt0 : 0, wt1 = U.wt1;
+                    const bool pure = U.depth > 0;   // the s->s path is left out below the roots
+                    float Gu[8 * XPW];   // [xi][a2][v]: unit sums of the z-step fragments
+#pragma unroll
+                    for (int i = 0; i < 8 * XPW; i++) Gu[i] = 0.f;
+                    // S1 columns of one term (both z halves) from TMEM (loading the next
+                    // term's columns during this term's products measured 6 % slower)
+                    float cC[2][CPP], cA[2][CPP], cT[2][CPP];
+                    auto load_term = [&](int j) {
+#pragma unroll
+                        for (int t = 0; t < 2; t++) {
+                            if (j < (t == 0 ? nw : wt1)) {
+                                const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16) + 256u * db + 128u * t + CPT * j;
+                                tmem_ldn<CPP>(base + CPP * part, cC[t]);
+                                tmem_ldn<CPP>(base + 8 + CPP * part, cA[t]);
+                                tmem_ldn<CPP>(base + 16 + CPP * part, cT[t]);
+                            } else {
+#pragma unroll
+                                for (int i = 0; i < CPP; i++) cC[t][i] = cA[t][i] = cT[t][i] = 0.f;
                             }
-                        for (int t = 0; t < nt_tiles; t++) first[t] = false;
-                        commit(&b_empty[sbix]);    // the form slot is free once these products finish
-                    }
-                    commit(&d_full[db]);           // also after a failure, so that the consumers are released
-                    if (U.pflags & 2) {
-                        // last group of the pencil: its f slots are free once the products finish
-                        for (int b = 0; b < NFS; b++)
-                            if ((pmask >> b) & 1u) {
-                                commit(&f_empty[b]);
-                                nfs[b]++;
+                        }
+                    };
+                    bool d_free = false;   // this warp's arrival on d_empty[db] is made
+                    for (int j = 0; j < nw && ok; j++, nterm++) {
+                        float *S1s = S1base + (nterm & 1) * S1_FLOATS;
+                        float *Us = S1s + 16 * XS;
+                        // ---- S1 of term j (both z halves) into shared memory ----
+                        load_term(j);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int t = 0; t < 2; t++) {
+                            const int z = 8 * t + q2;
+                            const bool u_row = pure && t == 0 && b1 == 0;
+#pragma unroll
+                            for (int i = 0; i < CPP; i++) {
+                                const int xa = CPP * part + i;     // a0 = 0
+                                S1s[xa * XS + yrow * YS + z] = u_row ? cC[t][i] : cC[t][i] + cT[t][i];
+                                S1s[(8 + xa) * XS + yrow * YS + z] = cA[t][i];
+                                if (u_row) Us[xa * US + q1 * UYS + q2] = cT[t][i];
                             }
-                    }
-                    nu++;
-                }
-            }
-        } else {
-            // ---------------- consumers ----------------
-            const int quarter = warp & 3, half = cw >> 2;   // TMEM lanes 32 quarter ..; columns of half
-            const int r = 32 * quarter + lane;              // D row of this thread: b1 64 + q1 + 8 q2
-            const int b1 = r >> 6, q1 = r & 7, q2 = (r >> 3) & 7;
-            const int yrow = 8 * b1 + q1;
-            unsigned nterm = 0;   // terms drained (S1 buffer parity)
-            for (int u = u0; u < u1; u++) {
-                const Unit &U = units[u];
-                const bool pure = U.depth > 0;   // the s->s path is left out below the roots
-                const int so = nu & 1, db = nu & 1;
-                bool ok = !lbad;
-                if (ok && !bar_wait(&o_full[so], (nu >> 1) & 1)) { fail(); ok = false; }
-                if (ok && !bar_wait(&d_full[db], (nu >> 1) & 1)) { fail(); ok = false; }
-                ok = consumers_all(ok);
-                fence_after();
-                const float *OB = reinterpret_cast<const float *>(sm + SM_O + so * OREC);
-                const int nw = U.wt0;
-                const int ly = U.ly, lz = U.lz;
-                float Gu[16];   // [xi][a2][v]: unit sums of the z-step fragments
-#pragma unroll
-                for (int i = 0; i < 16; i++) Gu[i] = 0.f;
-                for (int j = 0; j < nw && ok; j++, nterm++) {
-                    float *S1s = S1base + (nterm & 1) * S1_FLOATS;
-                    float *Us = S1s + 16 * XS;
-                    // ---- drain S1 of term j (both z halves) into shared memory ----
-                    const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
-                    for (int t = 0; t < 2; t++) {
-                        const bool have = j < (t == 0 ? U.wt0 : U.wt1);
-                        float cC[4], cA[4], cT[4];
-                        if (have) {
-                            const uint32_t base = tmem + ((uint32_t)(32 * quarter) << 16) + 256u * db + 128u * t + CPT * j;
-                            tmem_ld4(base + 4 * half, cC);
-                            tmem_ld4(base + 8 + 4 * half, cA);
-                            tmem_ld4(base + 16 + 4 * half, cT);
-                            tmem_wait_ld();
-                        } else {
-#pragma unroll
-                            for (int i = 0; i < 4; i++) cC[i] = cA[i] = cT[i] = 0.f;
                         }
-                        const int z = 8 * t + q2;
-                        const bool u_row = pure && t == 0 && b1 == 0;
-#pragma unroll
-                        for (int i = 0; i < 4; i++) {
-                            const int xa = 4 * half + i;     // a0 = 0
-                            S1s[xa * XS + yrow * YS + z] = u_row ? cC[i] : cC[i] + cT[i];
-                            S1s[(8 + xa) * XS + yrow * YS + z] = cA[i];
-                            if (u_row) Us[xa * US + q1 * UYS + q2] = cT[i];
+                        if (j + 1 == nw) {
+                            // the unit's last TMEM columns are read: the D buffer is free
+                            fence_before();
+                            __syncwarp();
+                            if (lane == 0) bar_arrive(&d_empty[db]);
+                            d_free = true;
                         }
-                    }
-                    consumers_sync();
-                    // blocks (a, b) of a direction take part iff |l| <= bw[2a + b]
-                    unsigned vy = 0, vz = 0;
+                        consumers_sync<NCW>();
+                        // blocks (a, b) of a direction take part iff |l| <= bw[2a + b]
+                        const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
+                        unsigned vy = 0, vz = 0;
 #pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        vy |= (abs(ly) <= row.wd[c] ? 1u : 0u) << c;
-                        vz |= (abs(lz) <= row.wd[c] ? 1u : 0u) << c;
-                    }
-                    const float *Oy = OB + j * 512, *Oz = Oy + 256;
-                    // O^y A fragments per k step s = b1 (block of row half a1: idx 2 a1 + s):
-                    // O^y[y_out = (a1, p1)][y_in = (s, q1)] = blocks32[idx 64 + 8 q1 + p1]
-                    float yah[2][4], yal[2][4];
-#pragma unroll
-                    for (int s = 0; s < 2; s++) {
-                        const bool v0 = (vy >> s) & 1u, v1 = (vy >> (2 + s)) & 1u;
-                        const float e[4] = {v0 ? Oy[s * 64 + 8 * tq + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * tq + fg] : 0.f,
-                                            v0 ? Oy[s * 64 + 8 * (tq + 4) + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * (tq + 4) + fg] : 0.f};
-#pragma unroll
-                        for (int q = 0; q < 4; q++) split(e[q], yah[s][q], yal[s][q]);
-                    }
-                    // O^z B fragments per (a2, s = b2), k permuted: row k = tq <-> z_in = 8 s + 2 tq,
-                    // row tq + 4 <-> 8 s + 2 tq + 1; O^z[z_out][z_in] = blocks32[idx 64 + 8 (z_in % 8) + z_out % 8]
-                    float zbh[2][2][2], zbl[2][2][2];
-#pragma unroll
-                    for (int a2 = 0; a2 < 2; a2++)
+                        for (int c = 0; c < 4; c++) {
+                            vy |= (abs(U.ly) <= row.wd[c] ? 1u : 0u) << c;
+                            vz |= (abs(U.lz) <= row.wd[c] ? 1u : 0u) << c;
+                        }
+                        const float *Oy = OB + j * 512, *Oz = Oy + 256;
+                        // O^y A fragments per k step s = b1 (block of row half a1: idx 2 a1 + s):
+                        // O^y[y_out = (a1, p1)][y_in = (s, q1)] = blocks32[idx 64 + 8 q1 + p1]
+                        float yah[2][4], yal[2][4];
 #pragma unroll
                         for (int s = 0; s < 2; s++) {
-                            const int idx = 2 * a2 + s;
-                            const bool v = (vz >> idx) & 1u;
-                            split(v ? Oz[idx * 64 + 8 * (2 * tq) + fg] : 0.f, zbh[a2][s][0], zbl[a2][s][0]);
-                            split(v ? Oz[idx * 64 + 8 * (2 * tq + 1) + fg] : 0.f, zbh[a2][s][1], zbl[a2][s][1]);
+                            const bool v0 = (vy >> s) & 1u, v1 = (vy >> (2 + s)) & 1u;
+                            const float e[4] = {v0 ? Oy[s * 64 + 8 * tq + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * tq + fg] : 0.f,
+                                                v0 ? Oy[s * 64 + 8 * (tq + 4) + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * (tq + 4) + fg] : 0.f};
+#pragma unroll
+                            for (int q = 0; q < 4; q++) split(e[q], yah[s][q], yal[s][q]);
                         }
-                    const bool ys0 = (vy & 5u) != 0, ys1 = (vy & 10u) != 0;   // k step s has a block that takes part
-                    // ---- y step: C[xi][zb] = Y^T fragment (rows y_out g, g + 8; columns z = 8 zb + 2 tq, +1) ----
-                    float C[2][2][4], P[2][2];
+                        // O^z B fragments per (a2, s = b2), k permuted: row k = tq <-> z_in = 8 s + 2 tq,
+                        // row tq + 4 <-> 8 s + 2 tq + 1; O^z[z_out][z_in] = blocks32[idx 64 + 8 (z_in % 8) + z_out % 8]
+                        float zbh[2][2][2], zbl[2][2][2];
 #pragma unroll
-                    for (int xi = 0; xi < 2; xi++) {
-                        const int x = x0 + xi;
-                        float Cl[2][4];
-#pragma unroll
-                        for (int zb = 0; zb < 2; zb++) {
-#pragma unroll
-                            for (int v = 0; v < 4; v++) C[xi][zb][v] = Cl[zb][v] = 0.f;
+                        for (int a2 = 0; a2 < 2; a2++)
 #pragma unroll
                             for (int s = 0; s < 2; s++) {
-                                if (!(s == 0 ? ys0 : ys1)) continue;
-                                // B = S1^T: rows k = y_in = 8 s + tq (+4), column n = z = 8 zb + g
-                                float bh[2], bl[2];
-                                split(S1s[x * XS + (8 * s + tq) * YS + 8 * zb + fg], bh[0], bl[0]);
-                                split(S1s[x * XS + (8 * s + tq + 4) * YS + 8 * zb + fg], bh[1], bl[1]);
-                                mma3x2(C[xi][zb], Cl[zb], yah[s], yal[s], bh, bl);
+                                const int idx = 2 * a2 + s;
+                                const bool v = (vz >> idx) & 1u;
+                                split(v ? Oz[idx * 64 + 8 * (2 * tq) + fg] : 0.f, zbh[a2][s][0], zbl[a2][s][0]);
+                                split(v ? Oz[idx * 64 + 8 * (2 * tq + 1) + fg] : 0.f, zbh[a2][s][1], zbl[a2][s][1]);
+                            }
+                        const bool ys[2] = {(vy & 5u) != 0, (vy & 10u) != 0};   // k step s has a block that takes part
+                        // ---- y step: C[xi][zb] = Y^T fragment (rows y_out g, g + 8; columns z = 8 zb + 2 tq, +1) ----
+                        // B = S1^T: rows k = y_in = 8 s + tq (+4), column n = z = 8 zb + g; all operands
+                        // first, then the products with the independent accumulators side by side
+                        float C[XPW][2][4], Cl[XPW][2][4], P[XPW][2];
+#pragma unroll
+                        for (int xi = 0; xi < XPW; xi++)
+#pragma unroll
+                            for (int zb = 0; zb < 2; zb++)
+#pragma unroll
+                                for (int v = 0; v < 4; v++) C[xi][zb][v] = Cl[xi][zb][v] = 0.f;
+#pragma unroll
+                        for (int s = 0; s < 2; s++) {
+                            if (!ys[s]) continue;
+                            float bh[XPW][2][2], bl[XPW][2][2];
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++)
+#pragma unroll
+                                for (int zb = 0; zb < 2; zb++) {
+                                    const float *src = S1s + xof(xi) * XS + (8 * s + tq) * YS + 8 * zb + fg;
+                                    split(src[0], bh[xi][zb][0], bl[xi][zb][0]);
+                                    split(src[4 * YS], bh[xi][zb][1], bl[xi][zb][1]);
+                                }
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++)
+#pragma unroll
+                                for (int zb = 0; zb < 2; zb++) mma16(Cl[xi][zb], yal[s], bh[xi][zb]);
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++)
+#pragma unroll
+                                for (int zb = 0; zb < 2; zb++) mma16(C[xi][zb], yah[s], bh[xi][zb]);
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++)
+#pragma unroll
+                                for (int zb = 0; zb < 2; zb++) mma16(Cl[xi][zb], yah[s], bl[xi][zb]);
+                        }
+#pragma unroll
+                        for (int xi = 0; xi < XPW; xi++) {
+                            const int x = xof(xi);
+#pragma unroll
+                            for (int zb = 0; zb < 2; zb++)
+#pragma unroll
+                                for (int v = 0; v < 4; v++) C[xi][zb][v] += Cl[xi][zb][v];
+                            P[xi][0] = P[xi][1] = 0.f;
+                            // U channel (x < 8, z < 8, y_in < 8): O^y's k step 0 applied to U; the a1 = 0 rows
+                            // (T block) are P, the a1 = 1 rows (B block) join Y
+                            if (pure && x < 8 && (vy & 5u)) {
+                                float bh[2], bl[2], cu[4] = {0.f, 0.f, 0.f, 0.f};
+                                split(Us[x * US + tq * UYS + fg], bh[0], bl[0]);
+                                split(Us[x * US + (tq + 4) * UYS + fg], bh[1], bl[1]);
+                                mma3x(cu, yah[0], yal[0], bh, bl);
+                                P[xi][0] = cu[0];
+                                P[xi][1] = cu[1];
+                                C[xi][0][2] += cu[2];
+                                C[xi][0][3] += cu[3];
+                            }
+                        }
+                        // ---- z step: the y-step fragments are the A fragments (k' = tq <-> z = 8 s + 2 tq) ----
+                        // split once per (xi, s) for both a2; the products of the (xi, a2) accumulators side by side
+                        float Z[XPW][2][4], Zl[XPW][2][4];
+#pragma unroll
+                        for (int xi = 0; xi < XPW; xi++)
+#pragma unroll
+                            for (int a2 = 0; a2 < 2; a2++)
+#pragma unroll
+                                for (int v = 0; v < 4; v++) Z[xi][a2][v] = Zl[xi][a2][v] = 0.f;
+#pragma unroll
+                        for (int s = 0; s < 2; s++) {
+                            const bool zs0 = (vz >> s) & 1u, zs1 = (vz >> (2 + s)) & 1u;
+                            if (!zs0 && !zs1) continue;
+                            float ah[XPW][4], al[XPW][4];
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++) {
+                                split(C[xi][s][0], ah[xi][0], al[xi][0]);
+                                split(C[xi][s][2], ah[xi][1], al[xi][1]);
+                                split(C[xi][s][1], ah[xi][2], al[xi][2]);
+                                split(C[xi][s][3], ah[xi][3], al[xi][3]);
+                            }
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++) {
+                                if (zs0) mma16(Zl[xi][0], al[xi], zbh[0][s]);
+                                if (zs1) mma16(Zl[xi][1], al[xi], zbh[1][s]);
+                            }
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++) {
+                                if (zs0) mma16(Z[xi][0], ah[xi], zbh[0][s]);
+                                if (zs1) mma16(Z[xi][1], ah[xi], zbh[1][s]);
+                            }
+#pragma unroll
+                            for (int xi = 0; xi < XPW; xi++) {
+                                if (zs0) mma16(Zl[xi][0], ah[xi], zbl[0][s]);
+                                if (zs1) mma16(Zl[xi][1], ah[xi], zbl[1][s]);
                             }
                         }
 #pragma unroll
-                        for (int zb = 0; zb < 2; zb++)
+                        for (int xi = 0; xi < XPW; xi++) {
+                            const int x = xof(xi);
 #pragma unroll
-                            for (int v = 0; v < 4; v++) C[xi][zb][v] += Cl[zb][v];
-                        P[xi][0] = P[xi][1] = 0.f;
-                        // U channel (x < 8, z < 8, y_in < 8): O^y's k step 0 applied to U; the a1 = 0 rows
-                        // (T block) are P, the a1 = 1 rows (B block) join Y
-                        if (pure && x < 8 && (vy & 5u)) {
-                            float bh[2], bl[2], cu[4] = {0.f, 0.f, 0.f, 0.f};
-                            split(Us[x * US + tq * UYS + fg], bh[0], bl[0]);
-                            split(Us[x * US + (tq + 4) * UYS + fg], bh[1], bl[1]);
-                            mma3x(cu, yah[0], yal[0], bh, bl);
-                            P[xi][0] = cu[0];
-                            P[xi][1] = cu[1];
-                            C[xi][0][2] += cu[2];
-                            C[xi][0][3] += cu[3];
-                        }
-                    }
-                    // ---- z step: the y-step fragments are the A fragments (k' = tq <-> z = 8 s + 2 tq) ----
+                            for (int a2 = 0; a2 < 2; a2++)
 #pragma unroll
-                    for (int xi = 0; xi < 2; xi++) {
-                        const int x = x0 + xi;
-#pragma unroll
-                        for (int a2 = 0; a2 < 2; a2++) {
-                            float Z[4] = {0.f, 0.f, 0.f, 0.f}, Zl[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                            for (int s = 0; s < 2; s++) {
-                                if (!((vz >> (2 * a2 + s)) & 1u)) continue;
-                                float ah[4], al[4];
-                                split(C[xi][s][0], ah[0], al[0]);
-                                split(C[xi][s][2], ah[1], al[1]);
-                                split(C[xi][s][1], ah[2], al[2]);
-                                split(C[xi][s][3], ah[3], al[3]);
-                                mma3x2(Z, Zl, ah, al, zbh[a2][s], zbl[a2][s]);
-                            }
-#pragma unroll
-                            for (int v = 0; v < 4; v++) Z[v] += Zl[v];
+                                for (int v = 0; v < 4; v++) Z[xi][a2][v] += Zl[xi][a2][v];
                             // P through z with the B block only (a2 = 1 from b2 = 0): the T.T.T path is left out
-                            if (a2 == 1 && pure && x < 8 && (vy & 1u) && ((vz >> 2) & 1u)) {
+                            if (pure && x < 8 && (vy & 1u) && ((vz >> 2) & 1u)) {
                                 float ah[4], al[4];
                                 split(P[xi][0], ah[0], al[0]);
                                 ah[1] = al[1] = 0.f;
                                 split(P[xi][1], ah[2], al[2]);
                                 ah[3] = al[3] = 0.f;
-                                mma3x(Z, ah, al, zbh[1][0], zbl[1][0]);
+                                mma3x(Z[xi][1], ah, al, zbh[1][0], zbl[1][0]);
                             }
 #pragma unroll
-                            for (int v = 0; v < 4; v++) Gu[8 * xi + 4 * a2 + v] += Z[v];
+                            for (int a2 = 0; a2 < 2; a2++)
+#pragma unroll
+                                for (int v = 0; v < 4; v++) Gu[8 * xi + 4 * a2 + v] += Z[xi][a2][v];
                         }
                     }
-                }
-                // compensated sums over the units
+                    // compensated sums over the units
 #pragma unroll
-                for (int e = 0; e < 16; e++) {
-                    const float yv = Gu[e] - Gc[e];
-                    const float tv = G[e] + yv;
-                    Gc[e] = (tv - G[e]) - yv;
-                    G[e] = tv;
+                    for (int e = 0; e < 8 * XPW; e++) {
+                        const float yv = Gu[e] - Gc[e];
+                        const float tv = G[e] + yv;
+                        Gc[e] = (tv - G[e]) - yv;
+                        G[e] = tv;
+                    }
+                    // the operator blocks of this unit (and D, if not yet) are free
+                    fence_before();
+                    __syncwarp();
+                    if (lane == 0) {
+                        if (!d_free) bar_arrive(&d_empty[db]);
+                        bar_arrive(&o_empty[so]);
+                    }
+                    nu++;
                 }
-                // D and the operator blocks of this unit are free
-                fence_before();
-                __syncwarp();
-                if (lane == 0) {
-                    bar_arrive(&d_empty[db]);
-                    bar_arrive(&o_empty[so]);
-                }
-                nu++;
-            }
-            // the task's sums (slot of its units; every task has one): fragment v of
-            // (x, a2): y_out = fg + 8 (v >> 1), z_out = 8 a2 + 2 tq + (v & 1); g component
-            // gt = a0 + 2 a1 + 4 a2, element p0 + 8 p1 + 64 p2
-            double *go = pen_partial + (size_t)units[u0].task * 4096;
+                // the task's sums (slot of its units; every task has one): fragment v of
+                // (x, a2): y_out = fg + 8 (v >> 1), z_out = 8 a2 + 2 tq + (v & 1); g component
+                // gt = a0 + 2 a1 + 4 a2, element p0 + 8 p1 + 64 p2
+                double *go = pen_partial + (size_t)units[u0].task * 4096;
 #pragma unroll
-            for (int e = 0; e < 16; e++) {
-                const int xi = e >> 3, a2 = (e >> 2) & 1, v = e & 3;
-                const int x = x0 + xi, a0 = x >> 3, p0 = x & 7, a1 = v >> 1, p1 = fg, p2 = 2 * tq + (v & 1);
-                go[(a0 + 2 * a1 + 4 * a2) * 512 + p0 + 8 * p1 + 64 * p2] = (double)G[e] - (double)Gc[e];
+                for (int e = 0; e < 8 * XPW; e++) {
+                    const int xi = e >> 3, a2 = (e >> 2) & 1, v = e & 3;
+                    const int x = xof(xi), a0 = x >> 3, p0 = x & 7, a1 = v >> 1, p1 = fg, p2 = 2 * tq + (v & 1);
+                    go[(a0 + 2 * a1 + 4 * a2) * 512 + p0 + 8 * p1 + 64 * p2] = (double)G[e] - (double)Gc[e];
+                }
             }
-        }
-        // the producer / MMA lanes other than 0 did not walk the units: bring their counters along
-        if (warp <= 1) {
-            nu = __shfl_sync(0xffffffffu, nu, 0);
-            nb = __shfl_sync(0xffffffffu, nb, 0);
-            for (int i = 0; i < NFS; i++) nfs[i] = __shfl_sync(0xffffffffu, nfs[i], 0);
-        }
-        const bool any_bad = __syncthreads_or(lbad) != 0;
-        if (any_bad) {
-            lbad = true;
-            break;
+            if (__syncthreads_or(lbad) != 0) {
+                lbad = true;
+                break;
+            }
         }
     }
     // wait (bounded) for the tensor-core work in flight, then free TMEM
@@ -719,7 +826,31 @@ __global__ void k_keep_fill(DevMRA m, DevOper op, const DevTree *gs, const int *
 
 }  // namespace pencil
 
-bool pencil_supported(int K) { return K == 8; }
+bool pencil_supported(int K) { return K == 8 && pencil_shape_ok(kPencilWarpsDefault); }
+
+namespace {
+template <int NCW> bool shape_ok_impl() {
+    cudaFuncAttributes a{};
+    if (cudaFuncGetAttributes(&a, pencil::k_pencil<NCW>) != cudaSuccess) return false;
+    return 128 * pencil::Regs<NCW>::prod + 32 * NCW * pencil::Regs<NCW>::cons <= pencil::n_threads<NCW>() * a.numRegs;
+}
+template <int NCW>
+void launch_shape(int grid, const DevOper &op, const DevTree *fs, const int *work_tree, const void *units, const int *task_unit, int n_tasks,
+                  double *pen_partial, int *err, int *counter, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(pencil::k_pencil<NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize, pencil::SM_BYTES);
+        attr = true;
+    }
+    pencil::k_pencil<NCW><<<grid, pencil::n_threads<NCW>(), pencil::SM_BYTES, s>>>(op, fs, work_tree, (const pencil::Unit *)units, task_unit,
+                                                                                  n_tasks, pen_partial, err, counter);
+}
+}  // namespace
+
+bool pencil_shape_ok(int consumer_warps) {
+    static const bool ok8 = shape_ok_impl<8>(), ok16 = shape_ok_impl<16>();
+    return consumer_warps == 16 ? ok16 : consumer_warps == 8 ? ok8 : false;
+}
 
 void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *forms, cudaStream_t s) {
     if (n_jobs <= 0) return;
@@ -745,19 +876,21 @@ void launch_keep_fill(const DevMRA &m, const DevOper &op, const DevTree *gs, con
 }
 
 void launch_pencil(const DevOper &op, const DevTree *fs, const int *work_tree, const void *units, const int *task_unit, int n_tasks,
-                   double *pen_partial, int *err, int *counter, cudaStream_t s) {
+                   double *pen_partial, int *err, int *counter, cudaStream_t s, int consumer_warps) {
     if (n_tasks <= 0) return;
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(pencil::k_pencil, cudaFuncAttributeMaxDynamicSharedMemorySize, pencil::SM_BYTES);
         if (sms <= 0) sms = 1;
     }
     cudaMemsetAsync(counter, 0, sizeof(int), s);
-    pencil::k_pencil<<<std::min(sms, n_tasks), pencil::NT, pencil::SM_BYTES, s>>>(op, fs, work_tree, (const pencil::Unit *)units, task_unit,
-                                                                                   n_tasks, pen_partial, err, counter);
+    const int grid = std::min(sms, n_tasks);
+    if (consumer_warps == 16 && pencil_shape_ok(16))
+        launch_shape<16>(grid, op, fs, work_tree, units, task_unit, n_tasks, pen_partial, err, counter, s);
+    else
+        launch_shape<8>(grid, op, fs, work_tree, units, task_unit, n_tasks, pen_partial, err, counter, s);
 }
 
 }  // namespace mwgpu

@@ -292,6 +292,16 @@ bool use_pencil(const Level &lv) {
     return true;
 }
 
+// Consumer warps of the pencil kernel (its CTA shape) where no autotuning
+// chose them: MWGPU_PENCIL_WARPS = 8 or 16, else the default.
+int pencil_warps() {
+    if (const char *e = std::getenv("MWGPU_PENCIL_WARPS")) {
+        const int w = std::atoi(e);
+        if ((w == 8 || w == 16) && pencil_shape_ok(w)) return w;
+    }
+    return kPencilWarpsDefault;
+}
+
 // Units of the pencil contraction from the topology: per work entry the tasks
 // (l_z in the world) with their pencils (l_y in the world) and term groups;
 // tasks in descending size (the persistent kernel takes them in this order),
@@ -512,7 +522,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
                      nullptr, nullptr, tc_ok ? ctx->d_tc_counter : nullptr, ctx->stream);
         launch_pencil_units(o->mra, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_units, (int)pp.units.size(), ctx->d_err, ctx->stream);
         launch_pencil(o->op, ctx->d_fs, ctx->d_wtree, ctx->d_units, ctx->d_task_unit, pp.n_tasks, ctx->d_pen_partial, ctx->d_err,
-                      ctx->d_pen_counter, ctx->stream);
+                      ctx->d_pen_counter, ctx->stream, pencil_warps());
         launch_reduce_chunks(o->mra, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunk_begin, ctx->d_partial, ctx->stream, nullptr,
                              ctx->d_pen_begin, ctx->d_pen_partial);
         ctx->launches += 4;
@@ -1813,6 +1823,7 @@ struct mwgpu_plan {
     // pencil contraction (unscreened order-7 levels): kept items of the item
     // kernel (their offsets per entry), units and task sums
     bool pencil = false;
+    int pen_warps = kPencilWarpsDefault;     // consumer warps of the pencil kernel
     int *d_keep = nullptr;
     long long *d_keep_off = nullptr, *d_kscan = nullptr;
     long long kscan_n = 0;
@@ -1865,7 +1876,7 @@ void plan_contract(mwgpu_ctx *ctx, mwgpu_plan *pl, long long per, bool reduce) {
         launch_pencil_units(o->mra, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_units, pl->n_units, pl->d_err, st);
         if (reduce) launch_stamp(pl->d_stamps + 4, st);
         launch_pencil(o->op, pl->d_fs, pl->d_wtree, pl->d_units, pl->d_task_unit, pl->n_tasks, pl->d_pen_partial, pl->d_err, pl->d_pen_counter,
-                      st);
+                      st, pl->pen_warps);
         if (reduce) launch_stamp(pl->d_stamps + 5, st);
         ctx->launches += reduce ? 5 : 3;
     }
@@ -2154,6 +2165,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
             (s = plan_alloc(ctx, pl, &pl->d_partial, (size_t)pl->chunks_cap * 8 * o->mra.kp1_d)))
             return fail(s);
         pl->pencil = use_pencil(lv);
+        pl->pen_warps = pencil_warps();
         if ((term_order_supported(o->op.n_terms) || pl->pencil) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
         if (pl->pencil) {
             PencilPlan pp;
@@ -2182,17 +2194,20 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         const bool tune = (flags & MWGPU_PLAN_AUTOTUNE) != 0 && total > 0;
         if (tune) {
             // the schedule of the contraction (pencil + item kernels where the
-            // level allows the pencil kernel, or the item kernel alone) and the
-            // chunk length of the persistent item kernel (2 to 16 waves of the
-            // grid over its items), each candidate timed on the whole
-            // contraction of this level
+            // level allows the pencil kernel, with 8 or 16 consumer warps per
+            // pencil CTA, or the item kernel alone) and the chunk length of the
+            // persistent item kernel (2 to 16 waves of the grid over its
+            // items), each candidate timed on the whole contraction of this level
             const bool can_pencil = pl->pencil;
             const long long kept = can_pencil ? std::max<long long>(1, total - (long long)pl->pen_node_terms) : total;
             double best = 1e300;
             long long best_per = pl->per;
-            bool best_pen = pl->pencil;
-            for (int pen = can_pencil ? 1 : 0; pen >= 0; pen--) {
+            int best_sched = pl->pencil ? (pl->pen_warps == 16 ? 2 : 1) : 0;
+            std::vector<int> scheds{0};
+            if (can_pencil) scheds = pencil_shape_ok(16) ? std::vector<int>{1, 2, 0} : std::vector<int>{1, 0};
+            for (int pen : scheds) {
                 pl->pencil = pen != 0;
+                pl->pen_warps = pen == 2 ? 16 : 8;
                 const long long base = pen ? kept : total;
                 for (int waves : {2, 4, 8, 16}) {
                     const long long per = std::max<long long>(per_min, (base + (long long)waves * pl->grid - 1) / ((long long)waves * pl->grid));
@@ -2218,13 +2233,14 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
                     if (ms < best) {
                         best = ms;
                         best_per = per;
-                        best_pen = pen != 0;
+                        best_sched = pen;
                         pl->tune_choice = (int)pl->tune_ms.size() - 1;
                     }
                 }
             }
             pl->per = best_per;
-            pl->pencil = best_pen;
+            pl->pencil = best_sched != 0;
+            pl->pen_warps = best_sched == 2 ? 16 : 8;
             // the trees hold what every execution leaves (same schedule and chunking)
             plan_sequence(ctx, pl);
             if ((s = plan_check(ctx, pl, nullptr))) return fail(s);

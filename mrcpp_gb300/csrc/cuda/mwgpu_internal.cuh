@@ -377,9 +377,13 @@ void launch_keep_items(const DevMRA &m, const DevOper &op, const DevTree *gs, co
                        int n_work, const WorkItem *in, int *keep, cudaStream_t s, const int *nw_dev = nullptr);
 void launch_keep_fill(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
                       const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, const int *nw_dev = nullptr);
-// persistent; counter: a device int (zeroed here); pen_partial: 8 K^3 doubles per task
+// persistent; counter: a device int (zeroed here); pen_partial: 8 K^3 doubles per task;
+// consumer_warps: 8 or 16 (the CTA shape; kPencilWarpsDefault where nothing was tuned)
+constexpr int kPencilWarpsDefault = 8;
+// the CTA shape's register split fits the registers the kernel is launched with
+bool pencil_shape_ok(int consumer_warps);
 void launch_pencil(const DevOper &op, const DevTree *fs, const int *work_tree, const void *units, const int *task_unit, int n_tasks,
-                   double *pen_partial, int *err, int *counter, cudaStream_t s);
+                   double *pen_partial, int *err, int *counter, cudaStream_t s, int consumer_warps = kPencilWarpsDefault);
 
 // judged adaptive apply (k_judged.cu)
 void launch_keep_counts(const int *flags, int begin, int n, int *cnt, cudaStream_t s);

@@ -7,6 +7,7 @@
 // BottomUp transforms and the final square norm.  The per-node work of each
 // iteration (ConvolutionCalculator::calcNodeVector) runs on the GPU.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <fstream>
 #include <sstream>
@@ -232,9 +233,12 @@ mwgpu_tree *upload_input(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, const Tree<3>
     return dinp;
 }
 
-// the tree changes: its device input copy is stale
+// the tree changes: its device input copy is stale.  Versions come from one
+// counter, so that (tree, version) never repeats, even for a tree allocated
+// where a freed one was.
+std::atomic<unsigned long long> g_version_clock{1};
 void touch(mwh_tree *t) {
-    if (t) t->version++;
+    if (t) t->version = ++g_version_clock;
 }
 
 // the device input copy of a host tree: reused while the tree is unchanged,
@@ -265,6 +269,170 @@ mwgpu_tree *create_output(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, Tree<3> &out
     ck(mwgpu_create_tree(ctx, &md, &gd, &dout), "create output tree");
     acc.h2d_bytes += (oidx.size() + oc0.size()) * 4;
     return dout;
+}
+
+// Fixed-grid applies (maxIter = 0 onto a fresh output grid: no norm
+// screening) that repeat with the same operator, output grid and input
+// topology -- the applies of an SCF loop once its grids have settled -- replay
+// a level plan (mwgpu_plan: GenNode values, work list, contraction, reduction,
+// TopDown and BottomUp as one CUDA graph) instead of building the level again.
+// A plan owns device copies of its input and output trees (the input tree's
+// resident copy moves to a new plan when it is current); new input values go
+// into the plan's input copy (mwgpu_tree_update_coefs).  The first apply of a
+// kind creates the plan (with the autotuner: about 30 timed contractions);
+// up to kPlanCache plans are kept, the least recently used is dropped.
+// MWH_NO_PLAN_CACHE=1 builds every level instead.
+struct PlanEntry {
+    const mwgpu_oper *dop = nullptr;
+    int precision = 0;
+    double prec = 0.0;
+    unsigned long long out_hash = 0, inp_hash = 0;
+    size_t out_n = 0, inp_n = 0;
+    const mwh_tree *inp = nullptr;     // the input whose values the input copy holds
+    unsigned long long inp_version = 0;
+    const double *inp_data = nullptr;
+    mwgpu_tree *dinp = nullptr, *dout = nullptr;
+    mwgpu_plan *plan = nullptr;
+    unsigned long long used = 0;
+};
+constexpr size_t kPlanCache = 4;
+std::vector<PlanEntry> g_plans;
+unsigned long long g_plan_clock = 0;
+
+// FNV-1a over the topology in storage order (node index and first child)
+unsigned long long topo_hash(const Tree<3> &t) {
+    unsigned long long h = 1469598103934665603ull;
+    auto mix = [&](unsigned v) {
+        h ^= v;
+        h *= 1099511628211ull;
+    };
+    for (const auto &nd : t.nodes) {
+        mix((unsigned)nd.n);
+        for (int d = 0; d < 3; d++) mix((unsigned)nd.l[d]);
+        mix((unsigned)nd.child0);
+    }
+    mix((unsigned)t.nodes.size());
+    return h;
+}
+
+void plan_entry_free(mwgpu_ctx *ctx, PlanEntry &e) {
+    if (e.plan) mwgpu_plan_destroy(ctx, e.plan);
+    if (e.dout) mwgpu_free_tree(ctx, e.dout);
+    if (e.dinp) mwgpu_free_tree(ctx, e.dinp);
+    e = PlanEntry{};
+}
+
+// the plans that use a device operator (before it is freed)
+void drop_plans(mwgpu_ctx *ctx, const mwgpu_oper *dop) {
+    for (size_t i = 0; i < g_plans.size();) {
+        if (g_plans[i].dop == dop) {
+            plan_entry_free(ctx, g_plans[i]);
+            g_plans.erase(g_plans.begin() + i);
+        } else {
+            i++;
+        }
+    }
+}
+
+// The fixed-grid apply through a cached plan; false where it does not apply
+// (then the caller builds the level).  Same results as the built level: the
+// plan's level is the level mwgpu_apply_level computes on these nodes.
+bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, double prec, int precision, mwh_tree *outp, mwh_tree *inpp,
+                   mwh_apply_stats &acc) {
+    if (std::getenv("MWH_NO_PLAN_CACHE")) return false;
+    Tree<3> &out = *outp->t;
+    const Tree<3> &inp = *inpp->t;
+    out.clearGenerated();
+    if (!(out.squareNorm < 0.0) || out.nodes.empty()) return false;
+    for (size_t i = 0; i < inp.nodes.size(); i++)
+        if (inp.isGen((int)i)) return false;
+    const unsigned long long oh = topo_hash(out), ih = topo_hash(inp);
+    PlanEntry *e = nullptr;
+    for (auto &x : g_plans)
+        if (x.dop == dop && x.precision == precision && x.prec == prec && x.out_hash == oh && x.out_n == out.nodes.size() && x.inp_hash == ih &&
+            x.inp_n == inp.nodes.size())
+            e = &x;
+    const size_t n_in = inp.nodes.size(), nc = (size_t)inp.nCoefs;
+    acc.planned = 1;
+    if (!e) {
+        if (g_plans.size() >= kPlanCache) {
+            auto lru = std::min_element(g_plans.begin(), g_plans.end(), [](const PlanEntry &a, const PlanEntry &b) { return a.used < b.used; });
+            plan_entry_free(ctx, *lru);
+            g_plans.erase(lru);
+        }
+        PlanEntry ne;
+        ne.dop = dop;
+        ne.precision = precision;
+        ne.prec = prec;
+        ne.out_hash = oh;
+        ne.inp_hash = ih;
+        ne.out_n = out.nodes.size();
+        ne.inp_n = n_in;
+        try {
+            // the tree's current device copy moves to the plan (no second upload);
+            // otherwise the plan uploads its own
+            if (inpp->dev && inpp->dev_version == inpp->version && inpp->dev_nodes == n_in && inpp->dev_data == inp.coefs.data()) {
+                ne.dinp = inpp->dev;
+                inpp->dev = nullptr;
+                inpp->dev_version = 0;
+            } else {
+                ne.dinp = upload_input(ctx, md, inp, acc);
+            }
+            ne.dout = create_output(ctx, md, out, acc);
+            // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
+            std::vector<int> work;
+            for (auto &lvl : out.nodesByDepth(false))
+                for (int i : lvl) work.push_back(i);
+            std::vector<int> wtree(work.size(), 0);
+            const double sq = out.squareNorm;
+            ck(mwgpu_plan_create(ctx, dop, 1, &ne.dinp, &ne.dout, wtree.data(), work.data(), (int)work.size(), prec, &sq,
+                                 MWGPU_PLAN_TRANSFORMS | MWGPU_PLAN_AUTOTUNE, &ne.plan),
+               "create level plan");
+        } catch (...) {
+            plan_entry_free(ctx, ne);
+            throw;
+        }
+        ne.inp = inpp;
+        ne.inp_version = inpp->version;
+        ne.inp_data = inp.coefs.data();
+        g_plans.push_back(ne);
+        e = &g_plans.back();
+        acc.planned = 2;
+    } else if (e->inp != inpp || e->inp_version != inpp->version || e->inp_data != inp.coefs.data()) {
+        // new input values, same topology: into the plan's input copy
+        std::vector<double> norms(8 * n_in);
+        for (size_t i = 0; i < n_in; i++) std::memcpy(&norms[8 * i], inp.nodes[i].norms, sizeof(double) * 8);
+        ck(mwgpu_tree_update_coefs(ctx, e->dinp, inp.coefs.data(), norms.data()), "update input values");
+        acc.h2d_bytes += (unsigned long long)(n_in * nc + norms.size()) * 8;
+        e->inp = inpp;
+        e->inp_version = inpp->version;
+        e->inp_data = inp.coefs.data();
+    }
+    e->used = ++g_plan_clock;
+    mwgpu_level_stats ls{};
+    ck(mwgpu_plan_execute(ctx, e->plan, &ls), "execute level plan");
+    std::vector<double> nn(out.nodes.size() * 8);
+    ck(mwgpu_download_tree(ctx, e->dout, out.coefs.data(), nn.data()), "download output tree");
+    acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
+    for (size_t i = 0; i < out.nodes.size(); i++) {
+        double s2 = 0.0;
+        for (int c = 0; c < 8; c++) {
+            out.nodes[i].norms[c] = nn[i * 8 + c];
+            s2 += nn[i * 8 + c] * nn[i * 8 + c];
+        }
+        out.nodes[i].squareNorm = s2;
+        out.nodes[i].flags |= F_HASCOEFS;
+    }
+    out.calcSquareNorm();
+    acc.node_terms = ls.node_terms;
+    acc.components = ls.components;
+    acc.band_nodes = ls.band_nodes;
+    acc.gen_nodes = ls.gen_nodes;
+    acc.device_ms = ls.device_ms;
+    acc.contract_ms = ls.contract_ms;
+    acc.iterations = 1;
+    acc.out_nodes = (int)out.nodes.size();
+    return true;
 }
 
 // children made by the split step are mirrored to the device before the next
@@ -336,6 +504,14 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     mwgpu_launch_count(ctx, &l0);
     std::vector<BuildState> bs(nt);
     for (int t = 0; t < nt; t++) touch(outs[t]);
+    if (nt == 1 && !scale && max_iter == 0 && apply_planned(ctx, md, dop, prec, precision, outs[0], inps[0], acc)) {
+        ht.mark("planned");
+        mwgpu_launch_count(ctx, &l1);
+        acc.launches = l1 - l0;
+        acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = acc;
+        return 0;
+    }
     // the input trees' device copies belong to the trees
     auto release = [&] {
         for (auto &b : bs) {
@@ -880,6 +1056,7 @@ int mwh_tree_create(const mwh_mra *m, mwh_tree **out) {
     return guard([&] {
         if (!m || !out) return fail(1, "null argument");
         *out = new mwh_tree{std::make_unique<Tree<3>>(m->m)};
+        touch(*out);
         return 0;
     });
 }
@@ -1305,7 +1482,10 @@ void mwh_oper_free(mwh_oper *o) {
     std::lock_guard<std::mutex> lk(g_gpu_mu);
     for (auto it = g_oper_cache.begin(); it != g_oper_cache.end();) {
         if (it->first.op == o) {
-            if (g_ctx) mwgpu_free_operator(g_ctx, it->second);
+            if (g_ctx) {
+                drop_plans(g_ctx, it->second);
+                mwgpu_free_operator(g_ctx, it->second);
+            }
             it = g_oper_cache.erase(it);
         } else {
             ++it;

@@ -28,21 +28,28 @@ def case():
     return mra, P, f, grid
 
 
-def fixed(mra, P, f, grid, form, no_pencil=False):
+def fixed(mra, P, f, grid, form, no_pencil=False, warps=None):
     if no_pencil:
         os.environ["MWGPU_NO_PENCIL"] = "1"
+    if warps:
+        os.environ["MWGPU_PENCIL_WARPS"] = str(warps)
     try:
         g = mw.FunctionTree(mra)
         mw.copy_grid(g, grid)
         st = mw.apply(1e-4, g, P, f, max_iter=0, precision=form)
     finally:
         os.environ.pop("MWGPU_NO_PENCIL", None)
+        os.environ.pop("MWGPU_PENCIL_WARPS", None)
     return g.export()["coefs"], st
 
 
-def test_level_path(gpu, case):
+@pytest.mark.parametrize("warps", [8, 16])
+def test_level_path(gpu, case, warps):
+    # the pencil kernel with 8 consumer warps per CTA (two x values each) and
+    # with 16 (one x value each): the same products, so the same sums up to
+    # the order of FP32 additions
     mra, P, f, grid = case
-    a, sa = fixed(mra, P, f, grid, mw.MIXED)
+    a, sa = fixed(mra, P, f, grid, mw.MIXED, warps=warps)
     b, sb = fixed(mra, P, f, grid, mw.MIXED, no_pencil=True)
     c, _ = fixed(mra, P, f, grid, mw.FP64)
     assert sa["node_terms"] == sb["node_terms"] and sa["components"] == sb["components"]
@@ -100,8 +107,9 @@ def test_plan_path(gpu, case):
 
 
 def test_plan_autotuning(gpu, case):
-    # MWGPU_PLAN_AUTOTUNE times both schedules (pencil + item kernels, item
-    # kernel alone) x 4 chunk lengths on the level and keeps the fastest; the
+    # MWGPU_PLAN_AUTOTUNE times the three schedules (pencil kernel with 8 or
+    # 16 consumer warps + item kernel, item kernel alone) x 4 chunk lengths on
+    # the level and keeps the fastest; the
     # result does not depend on the choice beyond the mixed form's accuracy
     mra, P, f, grid = case
     L = mw.lib()
@@ -133,8 +141,8 @@ def test_plan_autotuning(gpu, case):
             items, sched, ms = (C.c_longlong * 16)(), (C.c_int * 16)(), (C.c_double * 16)()
             assert L.mwgpu_plan_tuning(plan, C.byref(nc), items, sched, ms, C.byref(chosen)) == 0
             if flags == 3:
-                assert nc.value == 8 and sorted(set(sched[:8])) == [0, 1]
-                assert 0 <= chosen.value < 8 and ms[chosen.value] == min(ms[:8])
+                assert nc.value == 12 and sorted(set(sched[:12])) == [0, 1, 2]
+                assert 0 <= chosen.value < 12 and ms[chosen.value] == min(ms[:12])
             else:
                 assert nc.value == 0 and chosen.value == -1
             assert L.mwgpu_plan_execute(ctx, plan, None) == 0
