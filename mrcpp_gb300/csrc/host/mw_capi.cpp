@@ -338,7 +338,7 @@ void drop_plans(mwgpu_ctx *ctx, const mwgpu_oper *dop) {
 // (then the caller builds the level).  Same results as the built level: the
 // plan's level is the level mwgpu_apply_level computes on these nodes.
 bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, double prec, int precision, mwh_tree *outp, mwh_tree *inpp,
-                   mwh_apply_stats &acc) {
+                   mwh_apply_stats &acc, HostTrace &ht) {
     if (std::getenv("MWH_NO_PLAN_CACHE")) return false;
     Tree<3> &out = *outp->t;
     const Tree<3> &inp = *inpp->t;
@@ -347,6 +347,7 @@ bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, do
     for (size_t i = 0; i < inp.nodes.size(); i++)
         if (inp.isGen((int)i)) return false;
     const unsigned long long oh = topo_hash(out), ih = topo_hash(inp);
+    ht.mark("key");
     PlanEntry *e = nullptr;
     for (auto &x : g_plans)
         if (x.dop == dop && x.precision == precision && x.prec == prec && x.out_hash == oh && x.out_n == out.nodes.size() && x.inp_hash == ih &&
@@ -408,11 +409,14 @@ bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, do
         e->inp_version = inpp->version;
         e->inp_data = inp.coefs.data();
     }
+    ht.mark(acc.planned == 2 ? "plan" : "input");
     e->used = ++g_plan_clock;
     mwgpu_level_stats ls{};
     ck(mwgpu_plan_execute(ctx, e->plan, &ls), "execute level plan");
+    ht.mark("level");
     std::vector<double> nn(out.nodes.size() * 8);
     ck(mwgpu_download_tree(ctx, e->dout, out.coefs.data(), nn.data()), "download output tree");
+    ht.mark("download");
     acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
     for (size_t i = 0; i < out.nodes.size(); i++) {
         double s2 = 0.0;
@@ -504,8 +508,8 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     mwgpu_launch_count(ctx, &l0);
     std::vector<BuildState> bs(nt);
     for (int t = 0; t < nt; t++) touch(outs[t]);
-    if (nt == 1 && !scale && max_iter == 0 && apply_planned(ctx, md, dop, prec, precision, outs[0], inps[0], acc)) {
-        ht.mark("planned");
+    if (nt == 1 && !scale && max_iter == 0 && apply_planned(ctx, md, dop, prec, precision, outs[0], inps[0], acc, ht)) {
+        ht.mark("norms");
         mwgpu_launch_count(ctx, &l1);
         acc.launches = l1 - l0;
         acc.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
