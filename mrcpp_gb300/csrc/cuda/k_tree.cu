@@ -11,6 +11,8 @@
 //                   (MWTree.cpp:166-181, FunctionNode.cpp:391-409, tree_utils.cpp:229-301)
 // The 1D step everywhere is math_utils::apply_filter: out(K^2 x K) = in^T (K^2 x K) * F.
 #include <algorithm>
+#include <cstdint>
+#include <cstdlib>
 
 #include "mwgpu_internal.cuh"
 
@@ -834,6 +836,17 @@ __global__ void k_to_float(const double *src, float *dst, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = (float)src[i];
 }
 
+// FP64 node coefficients read straight from page-locked host memory (its
+// device mapping), written as the device FP64 array and its FP32 copy in one
+// pass; n_pairs pairs of doubles
+__global__ void k_host_in(const double2 *__restrict__ src, double2 *__restrict__ dst, float2 *__restrict__ dst32, size_t n_pairs) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n_pairs; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = src[i];
+        dst[i] = v;
+        if (dst32) dst32[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
 __global__ void k_gather_norms_multi(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n * 8) return;
@@ -869,6 +882,23 @@ void launch_stamp(unsigned long long *t, cudaStream_t s) { k_stamp<<<1, 1, 0, s>
 void launch_gather_norms(const DevTree *gs, const int *work_tree, const int *work, int n, double *dst, cudaStream_t s) {
     if (n <= 0) return;
     k_gather_norms_multi<<<(n * 8 + 255) / 256, 256, 0, s>>>(gs, work_tree, work, n, dst);
+}
+
+bool host_in_supported(const double *host, size_t n, const double **dev) {
+    if (std::getenv("MWGPU_H2D_DMA") || n % 2 != 0 || ((uintptr_t)host & 15) != 0) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr || ((uintptr_t)a.devicePointer & 15) != 0) return false;
+    *dev = (const double *)a.devicePointer;
+    return true;
+}
+
+void launch_host_in(const double *src_dev, double *dst, float *dst32, size_t n, cudaStream_t s) {
+    if (n == 0) return;
+    k_host_in<<<4 * 152, 512, 0, s>>>((const double2 *)src_dev, (double2 *)dst, (float2 *)dst32, n / 2);
 }
 
 void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s) {

@@ -563,13 +563,18 @@ mwgpu_status make_tree(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, const mwgpu_tr
     trace.mark("alloc");
     MW_CK(cudaMemcpyAsync(t.idx, tr->h_idx.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->stream));
     MW_CK(cudaMemcpyAsync(t.child0, d->child0, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
-    if (d->coefs) MW_CK(cudaMemcpyAsync(t.coefs, d->coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
-    else MW_CK(cudaMemsetAsync(t.coefs, 0, sizeof(double) * tot * nc, ctx->stream));
+    // page-locked host coefficients of an input tree are read by a kernel that
+    // writes the FP64 array and its FP32 copy in one pass
+    const double *hdev = nullptr;
+    const bool hin = input && d->coefs && host_in_supported(d->coefs, (size_t)n * nc, &hdev);
+    if (d->coefs && !hin) MW_CK(cudaMemcpyAsync(t.coefs, d->coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
+    else if (!d->coefs) MW_CK(cudaMemsetAsync(t.coefs, 0, sizeof(double) * tot * nc, ctx->stream));
     trace.mark("coefs");
     if (input) {
         // FP32 copy read by the mixed form
         if ((s = pool_alloc(ctx, &t.coefs32, (size_t)n * nc))) { free_tree(ctx, tr); return s; }
-        launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
+        if (hin) launch_host_in(hdev, t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
+        else launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
         ctx->launches++;
         // TF32 hi / lo operands of the tensor-core x step (order 7; made below, once the norms are there)
         if (mwgpu::tc_supported(tr->mra.K) && n > 0)
@@ -1563,12 +1568,22 @@ mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tr, const doubl
     if (!ctx || !tr || !coefs) return MWGPU_ERR_BAD_ARG;
     MW_ARG(tr->is_input, "only input trees take new coefficients");
     cudaSetDevice(ctx->device);
+    PhaseTrace trace(ctx, "update_coefs");
     DevTree &t = tr->t;
     const int n = t.n_real;
     const size_t nc = 8 * (size_t)tr->mra.kp1_d;
-    MW_CK(cudaMemcpyAsync(t.coefs, coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
-    launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
-    ctx->launches += 1;
+    // page-locked host arrays are read by a kernel that writes both device copies
+    const double *hdev = nullptr;
+    if (host_in_supported(coefs, (size_t)n * nc, &hdev)) {
+        launch_host_in(hdev, t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
+        ctx->launches += 1;
+        trace.mark("coefs_fp32");
+    } else {
+        MW_CK(cudaMemcpyAsync(t.coefs, coefs, sizeof(double) * n * nc, cudaMemcpyHostToDevice, ctx->stream));
+        trace.mark("coefs");
+        launch_to_float(t.coefs, t.coefs32, (size_t)n * nc, ctx->stream);
+        ctx->launches += 1;
+    }
     if (norms) {
         MW_CK(cudaMemcpyAsync(t.norms, norms, sizeof(double) * n * 8, cudaMemcpyHostToDevice, ctx->stream));
     } else {
@@ -1584,6 +1599,7 @@ mwgpu_status mwgpu_tree_update_coefs(mwgpu_ctx *ctx, mwgpu_tree *tr, const doubl
         ctx->launches++;
     }
     MW_CK(cudaStreamSynchronize(ctx->stream));
+    trace.mark("fp32_tf32_norms");
     // GenNodes hold values of the old coefficients: a plan recomputes its own,
     // otherwise they are dropped and made again by the next level
     if (tr->plans == 0 && t.n_gen > 0) {

@@ -305,6 +305,11 @@ void launch_mw_down(const DevMRA &m, DevTree t, const DevTree *ts, const int *pt
                     bool fp32 = false);
 void launch_mw_up(const DevMRA &m, DevTree t, const DevTree *ts, const int *ptree, const int *parents, int n, cudaStream_t s, bool fp32 = false);
 void launch_to_float(const double *src, float *dst, size_t n, cudaStream_t s);
+// host arrays in page-locked memory that the device can read: their device
+// address (*dev) for launch_host_in (MWGPU_H2D_DMA=1: copy engine instead)
+bool host_in_supported(const double *host, size_t n, const double **dev);
+// n doubles from a device-mapped host array into dst and its FP32 copy dst32 (may be null)
+void launch_host_in(const double *src_dev, double *dst, float *dst32, size_t n, cudaStream_t s);
 // AdditionCalculator / MultiplicationCalculator::calcNode for the given output
 // nodes over the input trees ins[0..n_in) (device array) with factors c (device)
 void launch_combine(const DevMRA &m, bool mul, const DevTree *ins, const double *c, int n_in, DevTree out, const int *nodes, int n,

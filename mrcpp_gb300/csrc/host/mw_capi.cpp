@@ -271,9 +271,10 @@ mwgpu_tree *create_output(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, Tree<3> &out
     return dout;
 }
 
-// Fixed-grid applies (maxIter = 0 onto a fresh output grid: no norm
-// screening) that repeat with the same operator, output grid and input
-// topology -- the applies of an SCF loop once its grids have settled -- replay
+// Fixed-grid applies (maxIter = 0 onto fresh output grids: no norm
+// screening), of one (input, output) pair or a batch of them, that repeat
+// with the same operator, output grids and input topologies -- the applies of
+// an SCF loop once its grids have settled -- replay
 // a level plan (mwgpu_plan: GenNode values, work list, contraction, reduction,
 // TopDown and BottomUp as one CUDA graph) instead of building the level again.
 // A plan owns device copies of its input and output trees (the input tree's
@@ -282,16 +283,19 @@ mwgpu_tree *create_output(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, Tree<3> &out
 // kind creates the plan (with the autotuner: about 30 timed contractions);
 // up to kPlanCache plans are kept, the least recently used is dropped.
 // MWH_NO_PLAN_CACHE=1 builds every level instead.
-struct PlanEntry {
-    const mwgpu_oper *dop = nullptr;
-    int precision = 0;
-    double prec = 0.0;
+struct PlanTree {
     unsigned long long out_hash = 0, inp_hash = 0;
     size_t out_n = 0, inp_n = 0;
     const mwh_tree *inp = nullptr;     // the input whose values the input copy holds
     unsigned long long inp_version = 0;
     const double *inp_data = nullptr;
     mwgpu_tree *dinp = nullptr, *dout = nullptr;
+};
+struct PlanEntry {
+    const mwgpu_oper *dop = nullptr;
+    int precision = 0;
+    double prec = 0.0;
+    std::vector<PlanTree> trees;       // the (input, output) pairs of the batch
     mwgpu_plan *plan = nullptr;
     unsigned long long used = 0;
 };
@@ -317,8 +321,10 @@ unsigned long long topo_hash(const Tree<3> &t) {
 
 void plan_entry_free(mwgpu_ctx *ctx, PlanEntry &e) {
     if (e.plan) mwgpu_plan_destroy(ctx, e.plan);
-    if (e.dout) mwgpu_free_tree(ctx, e.dout);
-    if (e.dinp) mwgpu_free_tree(ctx, e.dinp);
+    for (auto &t : e.trees) {
+        if (t.dout) mwgpu_free_tree(ctx, t.dout);
+        if (t.dinp) mwgpu_free_tree(ctx, t.dinp);
+    }
     e = PlanEntry{};
 }
 
@@ -334,26 +340,38 @@ void drop_plans(mwgpu_ctx *ctx, const mwgpu_oper *dop) {
     }
 }
 
-// The fixed-grid apply through a cached plan; false where it does not apply
-// (then the caller builds the level).  Same results as the built level: the
-// plan's level is the level mwgpu_apply_level computes on these nodes.
-bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, double prec, int precision, mwh_tree *outp, mwh_tree *inpp,
-                   mwh_apply_stats &acc, HostTrace &ht) {
+// The fixed-grid apply of nt (input, output) pairs through a cached plan;
+// false where it does not apply (then the caller builds the levels).  Same
+// results as the built level: the plan's level is the level
+// mwgpu_apply_level_batch computes on these nodes.
+bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, double prec, int precision, int nt, mwh_tree **outs,
+                   mwh_tree **inps, mwh_apply_stats &acc, HostTrace &ht) {
     if (std::getenv("MWH_NO_PLAN_CACHE")) return false;
-    Tree<3> &out = *outp->t;
-    const Tree<3> &inp = *inpp->t;
-    out.clearGenerated();
-    if (!(out.squareNorm < 0.0) || out.nodes.empty()) return false;
-    for (size_t i = 0; i < inp.nodes.size(); i++)
-        if (inp.isGen((int)i)) return false;
-    const unsigned long long oh = topo_hash(out), ih = topo_hash(inp);
+    std::vector<PlanTree> key(nt);
+    for (int t = 0; t < nt; t++) {
+        Tree<3> &out = *outs[t]->t;
+        const Tree<3> &inp = *inps[t]->t;
+        out.clearGenerated();
+        if (!(out.squareNorm < 0.0) || out.nodes.empty()) return false;
+        for (size_t i = 0; i < inp.nodes.size(); i++)
+            if (inp.isGen((int)i)) return false;
+        key[t].out_hash = topo_hash(out);
+        key[t].inp_hash = topo_hash(inp);
+        key[t].out_n = out.nodes.size();
+        key[t].inp_n = inp.nodes.size();
+    }
     ht.mark("key");
+    auto same = [&](const PlanEntry &x) {
+        if (x.dop != dop || x.precision != precision || x.prec != prec || (int)x.trees.size() != nt) return false;
+        for (int t = 0; t < nt; t++)
+            if (x.trees[t].out_hash != key[t].out_hash || x.trees[t].inp_hash != key[t].inp_hash || x.trees[t].out_n != key[t].out_n ||
+                x.trees[t].inp_n != key[t].inp_n)
+                return false;
+        return true;
+    };
     PlanEntry *e = nullptr;
     for (auto &x : g_plans)
-        if (x.dop == dop && x.precision == precision && x.prec == prec && x.out_hash == oh && x.out_n == out.nodes.size() && x.inp_hash == ih &&
-            x.inp_n == inp.nodes.size())
-            e = &x;
-    const size_t n_in = inp.nodes.size(), nc = (size_t)inp.nCoefs;
+        if (same(x)) e = &x;
     acc.planned = 1;
     if (!e) {
         if (g_plans.size() >= kPlanCache) {
@@ -365,69 +383,92 @@ bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, do
         ne.dop = dop;
         ne.precision = precision;
         ne.prec = prec;
-        ne.out_hash = oh;
-        ne.inp_hash = ih;
-        ne.out_n = out.nodes.size();
-        ne.inp_n = n_in;
+        ne.trees = key;
         try {
-            // the tree's current device copy moves to the plan (no second upload);
-            // otherwise the plan uploads its own
-            if (inpp->dev && inpp->dev_version == inpp->version && inpp->dev_nodes == n_in && inpp->dev_data == inp.coefs.data()) {
-                ne.dinp = inpp->dev;
-                inpp->dev = nullptr;
-                inpp->dev_version = 0;
-            } else {
-                ne.dinp = upload_input(ctx, md, inp, acc);
+            std::vector<int> wtree, work;
+            std::vector<double> sq(nt);
+            std::vector<mwgpu_tree *> dins(nt), douts(nt);
+            for (int t = 0; t < nt; t++) {
+                PlanTree &pt = ne.trees[t];
+                mwh_tree *inpp = inps[t];
+                const Tree<3> &inp = *inpp->t;
+                Tree<3> &out = *outs[t]->t;
+                // the tree's current device copy moves to the plan (no second
+                // upload); otherwise the plan uploads its own
+                if (inpp->dev && inpp->dev_version == inpp->version && inpp->dev_nodes == pt.inp_n && inpp->dev_data == inp.coefs.data()) {
+                    pt.dinp = inpp->dev;
+                    inpp->dev = nullptr;
+                    inpp->dev_version = 0;
+                } else {
+                    pt.dinp = upload_input(ctx, md, inp, acc);
+                }
+                pt.dout = create_output(ctx, md, out, acc);
+                pt.inp = inpp;
+                pt.inp_version = inpp->version;
+                pt.inp_data = inp.coefs.data();
+                dins[t] = pt.dinp;
+                douts[t] = pt.dout;
+                sq[t] = out.squareNorm;
+                // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
+                for (auto &lvl : out.nodesByDepth(false))
+                    for (int i : lvl) {
+                        wtree.push_back(t);
+                        work.push_back(i);
+                    }
             }
-            ne.dout = create_output(ctx, md, out, acc);
-            // ConvolutionCalculator::getInitialWorkVector: all nodes of the output tree
-            std::vector<int> work;
-            for (auto &lvl : out.nodesByDepth(false))
-                for (int i : lvl) work.push_back(i);
-            std::vector<int> wtree(work.size(), 0);
-            const double sq = out.squareNorm;
-            ck(mwgpu_plan_create(ctx, dop, 1, &ne.dinp, &ne.dout, wtree.data(), work.data(), (int)work.size(), prec, &sq,
+            ck(mwgpu_plan_create(ctx, dop, nt, dins.data(), douts.data(), wtree.data(), work.data(), (int)work.size(), prec, sq.data(),
                                  MWGPU_PLAN_TRANSFORMS | MWGPU_PLAN_AUTOTUNE, &ne.plan),
                "create level plan");
         } catch (...) {
             plan_entry_free(ctx, ne);
             throw;
         }
-        ne.inp = inpp;
-        ne.inp_version = inpp->version;
-        ne.inp_data = inp.coefs.data();
         g_plans.push_back(ne);
         e = &g_plans.back();
         acc.planned = 2;
-    } else if (e->inp != inpp || e->inp_version != inpp->version || e->inp_data != inp.coefs.data()) {
-        // new input values, same topology: into the plan's input copy
-        std::vector<double> norms(8 * n_in);
-        for (size_t i = 0; i < n_in; i++) std::memcpy(&norms[8 * i], inp.nodes[i].norms, sizeof(double) * 8);
-        ck(mwgpu_tree_update_coefs(ctx, e->dinp, inp.coefs.data(), norms.data()), "update input values");
-        acc.h2d_bytes += (unsigned long long)(n_in * nc + norms.size()) * 8;
-        e->inp = inpp;
-        e->inp_version = inpp->version;
-        e->inp_data = inp.coefs.data();
+    } else {
+        // new input values, same topology: into the plan's input copies
+        std::vector<double> norms;
+        for (int t = 0; t < nt; t++) {
+            PlanTree &pt = e->trees[t];
+            mwh_tree *inpp = inps[t];
+            const Tree<3> &inp = *inpp->t;
+            if (pt.inp == inpp && pt.inp_version == inpp->version && pt.inp_data == inp.coefs.data()) continue;
+            const size_t n_in = inp.nodes.size();
+            norms.resize(8 * n_in);
+            for (size_t i = 0; i < n_in; i++) std::memcpy(&norms[8 * i], inp.nodes[i].norms, sizeof(double) * 8);
+            ck(mwgpu_tree_update_coefs(ctx, pt.dinp, inp.coefs.data(), norms.data()), "update input values");
+            acc.h2d_bytes += (unsigned long long)(n_in * (size_t)inp.nCoefs + norms.size()) * 8;
+            pt.inp = inpp;
+            pt.inp_version = inpp->version;
+            pt.inp_data = inp.coefs.data();
+        }
     }
     ht.mark(acc.planned == 2 ? "plan" : "input");
     e->used = ++g_plan_clock;
     mwgpu_level_stats ls{};
     ck(mwgpu_plan_execute(ctx, e->plan, &ls), "execute level plan");
     ht.mark("level");
-    std::vector<double> nn(out.nodes.size() * 8);
-    ck(mwgpu_download_tree(ctx, e->dout, out.coefs.data(), nn.data()), "download output tree");
-    ht.mark("download");
-    acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
-    for (size_t i = 0; i < out.nodes.size(); i++) {
-        double s2 = 0.0;
-        for (int c = 0; c < 8; c++) {
-            out.nodes[i].norms[c] = nn[i * 8 + c];
-            s2 += nn[i * 8 + c] * nn[i * 8 + c];
+    int out_nodes = 0;
+    std::vector<double> nn;
+    for (int t = 0; t < nt; t++) {
+        Tree<3> &out = *outs[t]->t;
+        nn.resize(out.nodes.size() * 8);
+        ck(mwgpu_download_tree(ctx, e->trees[t].dout, out.coefs.data(), nn.data()), "download output tree");
+        acc.d2h_bytes += (unsigned long long)(out.coefs.size() + nn.size()) * 8;
+        for (size_t i = 0; i < out.nodes.size(); i++) {
+            double s2 = 0.0;
+            for (int c = 0; c < 8; c++) {
+                out.nodes[i].norms[c] = nn[i * 8 + c];
+                s2 += nn[i * 8 + c] * nn[i * 8 + c];
+            }
+            out.nodes[i].squareNorm = s2;
+            out.nodes[i].flags |= F_HASCOEFS;
         }
-        out.nodes[i].squareNorm = s2;
-        out.nodes[i].flags |= F_HASCOEFS;
+        out.calcSquareNorm();
+        out_nodes += (int)out.nodes.size();
     }
-    out.calcSquareNorm();
+    ht.mark("download");
     acc.node_terms = ls.node_terms;
     acc.components = ls.components;
     acc.band_nodes = ls.band_nodes;
@@ -435,7 +476,7 @@ bool apply_planned(mwgpu_ctx *ctx, const mwgpu_mra_desc &md, mwgpu_oper *dop, do
     acc.device_ms = ls.device_ms;
     acc.contract_ms = ls.contract_ms;
     acc.iterations = 1;
-    acc.out_nodes = (int)out.nodes.size();
+    acc.out_nodes = out_nodes;
     return true;
 }
 
@@ -508,7 +549,7 @@ int apply_impl(double prec, int nt, mwh_tree **outs, mwh_oper *operp, mwh_tree *
     mwgpu_launch_count(ctx, &l0);
     std::vector<BuildState> bs(nt);
     for (int t = 0; t < nt; t++) touch(outs[t]);
-    if (nt == 1 && !scale && max_iter == 0 && apply_planned(ctx, md, dop, prec, precision, outs[0], inps[0], acc, ht)) {
+    if (!scale && max_iter == 0 && apply_planned(ctx, md, dop, prec, precision, nt, outs, inps, acc, ht)) {
         ht.mark("norms");
         mwgpu_launch_count(ctx, &l1);
         acc.launches = l1 - l0;

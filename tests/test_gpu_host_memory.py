@@ -51,3 +51,44 @@ def test_page_locked_trees(gpu):
     assert again["idle_bytes"] < after["idle_bytes"]
     assert np.array_equal(g3.export()["coefs"], b["coefs"]) or \
         np.abs(g3.export()["coefs"] - b["coefs"]).max() <= 1e-13 * np.abs(b["coefs"]).max()
+
+
+def test_kernel_read_of_page_locked_inputs_equals_dma(gpu):
+    # a page-locked input is read by a kernel through its device mapping (one
+    # pass writing the FP64 array and the FP32 copy); MWGPU_H2D_DMA=1 takes
+    # the copy engine and a separate conversion instead: the same device copy,
+    # so the same results to the last bit, for fresh uploads and for new
+    # values of a planned fixed-grid apply
+    import os
+
+    mra = mw.MRA(box=(-32, 32), order=7, basis=mw.LEGENDRE)
+    prec = 1e-4
+    f = project(mra, prec, gaussian_sum(77, 5, (1.0, 100.0), (-5.0, 5.0)))
+    assert mw.pinned_stats()["state"] == 1
+    P = mw.PoissonOperator(mra, prec)
+    grid = mw.FunctionTree(mra)
+    mw.apply(prec, grid, P, f, precision=mw.FP64)
+    res = {}
+    for dma in (False, True):
+        if dma:
+            os.environ["MWGPU_H2D_DMA"] = "1"
+        try:
+            for form in (mw.FP64, mw.MIXED):
+                f.rescale(1.0)  # uploaded again: the built level and the plan's update
+                outs = []
+                for cache in (False, True):
+                    if not cache:
+                        os.environ["MWH_NO_PLAN_CACHE"] = "1"
+                    try:
+                        g = mw.FunctionTree(mra)
+                        mw.copy_grid(g, grid)
+                        mw.apply(prec, g, P, f, max_iter=0, precision=form)
+                        outs.append(g.export()["coefs"])
+                    finally:
+                        os.environ.pop("MWH_NO_PLAN_CACHE", None)
+                res[(dma, form)] = outs
+        finally:
+            os.environ.pop("MWGPU_H2D_DMA", None)
+    for form in (mw.FP64, mw.MIXED):
+        for a, b in zip(res[(False, form)], res[(True, form)]):
+            assert np.array_equal(a, b)

@@ -84,3 +84,51 @@ def test_plan_follows_new_input_values(gpu, case):
     assert s1["planned"] in (1, 2) and s2["planned"] == 1
     assert np.linalg.norm(d1 - a) <= 1e-13 * np.linalg.norm(a)
     assert np.linalg.norm(d2 - 3.0 * a) <= 1e-13 * np.linalg.norm(a)
+
+
+def test_batched_fixed_grids_replay_one_plan(gpu, case):
+    # a batch of fixed-grid applies (one output grid per input) goes through
+    # one cached plan for all pairs; each output equals the built level
+    mra, P, _, _ = case
+    fs = [project(mra, 1e-4, gaussian_sum(40 + i, n, (1.0, 100.0), (-5.0, 5.0))) for i, n in enumerate((1, 3, 2))]
+    grids = []
+    for f in fs:
+        g = mw.FunctionTree(mra)
+        mw.apply(1e-4, g, P, f, precision=mw.FP64)
+        grids.append(g)
+
+    def batch(form, cache=True):
+        if not cache:
+            os.environ["MWH_NO_PLAN_CACHE"] = "1"
+        try:
+            outs = []
+            for g in grids:
+                o = mw.FunctionTree(mra)
+                mw.copy_grid(o, g)
+                outs.append(o)
+            st = mw.apply_batch(1e-4, outs, P, fs, max_iter=0, precision=form)
+        finally:
+            os.environ.pop("MWH_NO_PLAN_CACHE", None)
+        return [o.export()["coefs"] for o in outs], st
+
+    for form, tol in ((mw.FP64, 1e-13), (mw.MIXED, 2e-6)):
+        ref, sr = batch(form, cache=False)
+        a, sa = batch(form)
+        b, sb = batch(form)
+        assert sr["planned"] == 0 and sa["planned"] in (1, 2) and sb["planned"] == 1
+        assert sb["h2d_bytes"] == 0
+        for s in (sa, sb):
+            assert s["node_terms"] == sr["node_terms"] and s["components"] == sr["components"]
+        for x, y, r in zip(a, b, ref):
+            assert np.linalg.norm(x - r) <= tol * np.linalg.norm(r)
+            assert np.array_equal(x, y)
+    # new values of one input: only that input goes up again
+    fs[1].rescale(2.0)
+    try:
+        c, sc = batch(mw.FP64)
+    finally:
+        fs[1].rescale(0.5)
+    assert sc["planned"] == 1 and 0 < sc["h2d_bytes"]
+    ref64, _ = batch(mw.FP64, cache=False)
+    assert np.linalg.norm(c[1] - 2.0 * ref64[1]) <= 1e-13 * np.linalg.norm(ref64[1])
+    assert np.array_equal(c[0], ref64[0]) or np.linalg.norm(c[0] - ref64[0]) <= 1e-13 * np.linalg.norm(ref64[0])
