@@ -43,7 +43,7 @@
 //
 // Roles (128 + 32 x 8 threads): warp 0 lane 0 stages operands with
 // cp.async.bulk into mbarrier-tracked slots (a pencil's f nodes once for all
-// its term groups, stacked operator forms, per-term operator blocks); warp 1
+// its term groups, stacked operator forms); warp 1
 // lane 0 issues the tensor-core products and commits into one of two TMEM
 // buffers, so that the products of the next unit overlap the consumers; warps
 // 2 and 3 only give their registers to the consumers (setmaxnreg); warps 4-11
@@ -81,7 +81,6 @@ constexpr int NFS = kPencilSlots;          // f slots: one per x slot of a penci
 constexpr int FREC = kTcNodeFloats * 4;    // bytes of a staged real node (hi 16 KB, lo 16 KB)
 constexpr int GREC = 8192;                 // bytes of a staged GenNode (hi 4 KB, lo 4 KB; rows 64-127 zero)
 constexpr int BREC = 128 * NMAX;           // bytes of a stacked form (hi s0, hi s1, lo s0, lo s1)
-constexpr int OREC = GT * 2 * 256 * 4;     // bytes of the per-term operator blocks of a unit (O^y, O^z)
 // S1 staging (double-buffered by term): S1[x][y][z] at x XS + y YS + z, U[x][y][z] at
 // x US + y UYS + z (strides chosen so that the fragment loads avoid bank conflicts)
 constexpr int YS = 24, XS = 16 * YS, UYS = 8, US = 64;
@@ -90,11 +89,10 @@ constexpr int S1_FLOATS = 16 * XS + 8 * US;
 constexpr int SM_F = 0;                              // NFS real-node slots
 constexpr int SM_G = SM_F + NFS * FREC;              // NFS GenNode slots (a slot's node is real or generated)
 constexpr int SM_B = SM_G + NFS * GREC;              // 2 form slots
-constexpr int SM_O = SM_B + 2 * BREC;                // 2 operator-block slots
-constexpr int SM_S1 = SM_O + 2 * OREC;               // S1 staging
+constexpr int SM_S1 = SM_B + 2 * BREC;               // S1 staging
 constexpr int SM_BYTES = SM_S1 + 2 * 4 * S1_FLOATS;
 static_assert(SM_BYTES + 1024 <= 227 * 1024, "pencil kernel shared memory");
-static_assert(SM_F % 1024 == 0 && SM_G % 1024 == 0 && SM_B % 1024 == 0 && SM_O % 16 == 0 && SM_S1 % 16 == 0, "alignment");
+static_assert(SM_F % 1024 == 0 && SM_G % 1024 == 0 && SM_B % 1024 == 0 && SM_S1 % 16 == 0, "alignment");
 constexpr int TM_COLS = 512;                         // D buffer db at column 256 db, tile t at + 128 t
 constexpr long long kSpin = 1ll << 31;               // about a second at 2 GHz
 
@@ -256,6 +254,46 @@ __global__ void k_stack_forms(DevOper op, const PencilFormJob *jobs, int n_jobs,
 }
 
 // ---------------------------------------------------------------------------
+// The consumers' operator fragments, per (depth, term row r, l = -1, 0, 1) one
+// record of kPencilFragFloats, made at operator upload: the TF32 hi / lo parts
+// of the blocks in the mma.sync fragment order of each lane, the blocks (a, b)
+// outside the band (|l| > bw[2a + b]) zero.  Lane (g, tq), g = lane / 4,
+// tq = lane % 4, of a direction's blocks O (blocks32[idx 64 + 8 i + o] = the
+// K x K block idx, transposed):
+//   y part, per k step s: float4 hi, float4 lo of
+//     {O_s[8 tq + g], O_(2+s)[8 tq + g], O_s[8 (tq+4) + g], O_(2+s)[8 (tq+4) + g]}
+//     at floats 256 s + 8 lane (the A fragments of the y step);
+//   z part, per (a2, s), idx = 2 a2 + s: {hi, hi, lo, lo} of
+//     {O_idx[8 (2 tq) + g], O_idx[8 (2 tq + 1) + g]} at floats 512 + 128 idx + 4 lane
+//     (the B fragments of the z step, k permuted).
+__global__ void k_pencil_frags(DevOper op, float *frags) {
+    const int T = op.n_terms;
+    const int slot = blockIdx.x, l = slot % 3 - 1, tr = slot / 3, r = tr % T, dd = tr / T;
+    const TermRow row = op.term_rows[(size_t)dd * T + r];
+    const bool exists = row.off >= 0 && abs(l) <= row.L0;
+    const float *blk = exists ? op.blocks32 + (size_t)(row.off + l + row.L0) * 256 : nullptr;
+    float *out = frags + (size_t)slot * kPencilFragFloats;
+    for (int e = threadIdx.x; e < kPencilFragFloats; e += blockDim.x) {
+        float v = 0.f;
+        bool lo_part;
+        if (e < 512) {
+            const int s = e >> 8, lane = (e >> 3) & 31, q = e & 7, qq = q & 3, g = lane >> 2, tq = lane & 3;
+            lo_part = q >= 4;
+            const int idx = (qq & 1) ? 2 + s : s;
+            const int i = (qq & 2) ? tq + 4 : tq;
+            if (exists && abs(l) <= row.wd[idx]) v = blk[idx * 64 + 8 * i + g];
+        } else {
+            const int f = e - 512, idx = f >> 7, lane = (f >> 2) & 31, q = f & 3, g = lane >> 2, tq = lane & 3;
+            lo_part = q >= 2;
+            if (exists && abs(l) <= row.wd[idx]) v = blk[idx * 64 + 8 * (2 * tq + (q & 1)) + g];
+        }
+        float hi, lo;
+        split(v, hi, lo);
+        out[e] = lo_part ? lo : hi;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Units (PencilUnit, mwgpu_internal.cuh): made on the host from the topology;
 // k_pencil_units fills the f nodes of the pencil and what the contraction
 // needs to know about them.
@@ -316,7 +354,7 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
     constexpr int XPW = 16 / NCW;   // x values per consumer warp
     constexpr int CPP = 32 / NCW;   // drained columns of each 8-column block per consumer warp
     extern __shared__ __align__(1024) unsigned char sm[];
-    __shared__ __align__(8) uint64_t f_full[NFS], f_empty[NFS], b_full[2], b_empty[2], o_full[2], o_empty[2], d_full[2], d_empty[2], bar_end;
+    __shared__ __align__(8) uint64_t f_full[NFS], f_empty[NFS], b_full[2], b_empty[2], d_full[2], d_empty[2], bar_end;
     __shared__ uint32_t s_tmem;
     __shared__ int s_task;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -334,8 +372,6 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
         for (int i = 0; i < 2; i++) {
             bar_init(&b_full[i], 1);
             bar_init(&b_empty[i], 1);
-            bar_init(&o_full[i], 1);
-            bar_init(&o_empty[i], NCW);
             bar_init(&d_full[i], 1);
             bar_init(&d_empty[i], NCW);
         }
@@ -416,16 +452,6 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                             nb++;
                         }
                         if (lbad) break;
-                        // per-term O^y(l_y), O^z(l_z) blocks for the consumers
-                        const int so = nu & 1;
-                        if (nu >= 2 && !bar_wait(&o_empty[so], ((nu >> 1) - 1) & 1)) { fail(); break; }
-                        expect_tx(&o_full[so], (uint32_t)U.nt * 2048u);
-                        for (int j = 0; j < U.nt; j++) {
-                            const TermRow row = op.term_rows[(size_t)U.depth * T + U.q + j];
-                            unsigned char *dst = sm + SM_O + so * OREC + j * 2048;
-                            bulk(dst, op.blocks32 + (size_t)(row.off + U.ly + row.L0) * 256, 1024, &o_full[so]);
-                            bulk(dst + 1024, op.blocks32 + (size_t)(row.off + U.lz + row.L0) * 256, 1024, &o_full[so]);
-                        }
                         nu++;
                     }
                 }
@@ -524,13 +550,11 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                 const int yrow = 8 * b1 + q1;
                 unsigned nterm = 0;   // terms drained (S1 buffer parity)
                 for (int u = u0; u < u1; u++) {
-                    const int so = nu & 1, db = nu & 1;
+                    const int db = nu & 1;
                     bool ok = !lbad;
-                    if (ok && !bar_wait(&o_full[so], (nu >> 1) & 1)) { fail(); ok = false; }
                     if (ok && !bar_wait(&d_full[db], (nu >> 1) & 1)) { fail(); ok = false; }
                     ok = consumers_all<NCW>(ok);
                     fence_after();
-                    const float *OB = reinterpret_cast<const float *>(sm + SM_O + so * OREC);
                     const Unit &U = units[u];
                     const int nw = ok ? U.wt0 : 0, wt1 = U.wt1;
                     const bool pure = U.depth > 0;   // the s->s path is left out below the roots
@@ -558,6 +582,18 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                     for (int j = 0; j < nw && ok; j++, nterm++) {
                         float *S1s = S1base + (nterm & 1) * S1_FLOATS;
                         float *Us = S1s + 16 * XS;
+                        // this term's operator fragments (in flight during the drain)
+                        const size_t frow = ((size_t)U.depth * T + U.q + j) * 3;
+                        const float4 *py = reinterpret_cast<const float4 *>(op.pfrag + (frow + 1 + U.ly) * kPencilFragFloats);
+                        const float4 *pz = reinterpret_cast<const float4 *>(op.pfrag + (frow + 1 + U.lz) * kPencilFragFloats) + 128;
+                        float4 fy[4], fz[4];
+#pragma unroll
+                        for (int s = 0; s < 2; s++) {
+                            fy[2 * s] = __ldg(py + 64 * s + 2 * lane);
+                            fy[2 * s + 1] = __ldg(py + 64 * s + 2 * lane + 1);
+                        }
+#pragma unroll
+                        for (int idx = 0; idx < 4; idx++) fz[idx] = __ldg(pz + 32 * idx + lane);
                         // ---- S1 of term j (both z halves) into shared memory ----
                         load_term(j);
                         tmem_wait_ld();
@@ -589,30 +625,25 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                             vy |= (abs(U.ly) <= row.wd[c] ? 1u : 0u) << c;
                             vz |= (abs(U.lz) <= row.wd[c] ? 1u : 0u) << c;
                         }
-                        const float *Oy = OB + j * 512, *Oz = Oy + 256;
                         // O^y A fragments per k step s = b1 (block of row half a1: idx 2 a1 + s):
-                        // O^y[y_out = (a1, p1)][y_in = (s, q1)] = blocks32[idx 64 + 8 q1 + p1]
-                        float yah[2][4], yal[2][4];
-#pragma unroll
-                        for (int s = 0; s < 2; s++) {
-                            const bool v0 = (vy >> s) & 1u, v1 = (vy >> (2 + s)) & 1u;
-                            const float e[4] = {v0 ? Oy[s * 64 + 8 * tq + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * tq + fg] : 0.f,
-                                                v0 ? Oy[s * 64 + 8 * (tq + 4) + fg] : 0.f, v1 ? Oy[(2 + s) * 64 + 8 * (tq + 4) + fg] : 0.f};
-#pragma unroll
-                            for (int q = 0; q < 4; q++) split(e[q], yah[s][q], yal[s][q]);
-                        }
+                        // O^y[y_out = (a1, p1)][y_in = (s, q1)] = blocks32[idx 64 + 8 q1 + p1];
                         // O^z B fragments per (a2, s = b2), k permuted: row k = tq <-> z_in = 8 s + 2 tq,
                         // row tq + 4 <-> 8 s + 2 tq + 1; O^z[z_out][z_in] = blocks32[idx 64 + 8 (z_in % 8) + z_out % 8]
-                        float zbh[2][2][2], zbl[2][2][2];
+                        // (split and masked at operator upload, k_pencil_frags; loaded before the drain)
+                        float yah[2][4], yal[2][4], zbh[2][2][2], zbl[2][2][2];
 #pragma unroll
-                        for (int a2 = 0; a2 < 2; a2++)
+                        for (int s = 0; s < 2; s++) {
+                            yah[s][0] = fy[2 * s].x; yah[s][1] = fy[2 * s].y; yah[s][2] = fy[2 * s].z; yah[s][3] = fy[2 * s].w;
+                            yal[s][0] = fy[2 * s + 1].x; yal[s][1] = fy[2 * s + 1].y; yal[s][2] = fy[2 * s + 1].z; yal[s][3] = fy[2 * s + 1].w;
+                        }
 #pragma unroll
-                            for (int s = 0; s < 2; s++) {
-                                const int idx = 2 * a2 + s;
-                                const bool v = (vz >> idx) & 1u;
-                                split(v ? Oz[idx * 64 + 8 * (2 * tq) + fg] : 0.f, zbh[a2][s][0], zbl[a2][s][0]);
-                                split(v ? Oz[idx * 64 + 8 * (2 * tq + 1) + fg] : 0.f, zbh[a2][s][1], zbl[a2][s][1]);
-                            }
+                        for (int idx = 0; idx < 4; idx++) {
+                            const float4 z = fz[idx];
+                            zbh[idx >> 1][idx & 1][0] = z.x;
+                            zbh[idx >> 1][idx & 1][1] = z.y;
+                            zbl[idx >> 1][idx & 1][0] = z.z;
+                            zbl[idx >> 1][idx & 1][1] = z.w;
+                        }
                         const bool ys[2] = {(vy & 5u) != 0, (vy & 10u) != 0};   // k step s has a block that takes part
                         // ---- y step: C[xi][zb] = Y^T fragment (rows y_out g, g + 8; columns z = 8 zb + 2 tq, +1) ----
                         // B = S1^T: rows k = y_in = 8 s + tq (+4), column n = z = 8 zb + g; all operands
@@ -737,13 +768,10 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                         Gc[e] = (tv - G[e]) - yv;
                         G[e] = tv;
                     }
-                    // the operator blocks of this unit (and D, if not yet) are free
+                    // D is free (if not released after the last term's columns)
                     fence_before();
                     __syncwarp();
-                    if (lane == 0) {
-                        if (!d_free) bar_arrive(&d_empty[db]);
-                        bar_arrive(&o_empty[so]);
-                    }
+                    if (lane == 0 && !d_free) bar_arrive(&d_empty[db]);
                     nu++;
                 }
                 // the task's sums (slot of its units; every task has one): fragment v of
@@ -855,6 +883,12 @@ bool pencil_shape_ok(int consumer_warps) {
 void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *forms, cudaStream_t s) {
     if (n_jobs <= 0) return;
     pencil::k_stack_forms<<<n_jobs, 256, 0, s>>>(op, (const PencilFormJob *)jobs, n_jobs, forms);
+}
+
+void launch_pencil_frags(const DevOper &op, int rows, float *frags, cudaStream_t s) {
+    const int n = rows * op.n_terms * 3;
+    if (n <= 0) return;
+    pencil::k_pencil_frags<<<n, 256, 0, s>>>(op, frags);
 }
 
 void launch_pencil_units(const DevMRA &m, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, void *units, int n_units,

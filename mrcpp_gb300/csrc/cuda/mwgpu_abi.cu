@@ -282,7 +282,7 @@ void pair_offsets(const Level &lv, std::vector<long long> &poff) {
 // selects the item kernel for everything (the same sums).
 bool use_pencil(const Level &lv) {
     const mwgpu_oper *o = lv.o;
-    if (!pencil_supported(o->op.K) || !o->op.btc_stack || lv.band_dir >= 0 || std::getenv("MWGPU_NO_PENCIL")) return false;
+    if (!pencil_supported(o->op.K) || !o->op.btc_stack || !o->op.pfrag || lv.band_dir >= 0 || std::getenv("MWGPU_NO_PENCIL")) return false;
     for (double g : lv.gthr)
         if (!(g < 0.0)) return false;
     for (double g : lv.gnode)
@@ -1184,6 +1184,7 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
     o->op.n_nodes = (int)node;
     o->op.btc = nullptr;
     o->op.btc_stack = nullptr;
+    o->op.pfrag = nullptr;
     o->op.band_dir = -1;
     o->op.band_dir_w = 0;
     if (mwgpu::tc_supported(K)) {
@@ -1261,6 +1262,19 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         MW_CK(cudaStreamSynchronize(ctx->stream));
         MW_CK(cudaGetLastError());
         o->op.btc_stack = p_stack;
+        // the y / z operator fragments of the consumers, per (depth, term row, l = -1, 0, 1)
+        float *p_frag = nullptr;
+        if ((s = dev_alloc(ctx, &p_frag, (size_t)rows * T * 3 * mwgpu::kPencilFragFloats))) {
+            for (void *p : o->allocs) cudaFree(p);
+            pool_free(ctx, o->d_filt);
+            delete o;
+            return s;
+        }
+        o->allocs.push_back((void *)p_frag);
+        mwgpu::launch_pencil_frags(o->op, rows, p_frag, ctx->stream);
+        MW_CK(cudaStreamSynchronize(ctx->stream));
+        MW_CK(cudaGetLastError());
+        o->op.pfrag = p_frag;
     }
     *out = o;
     return MWGPU_OK;

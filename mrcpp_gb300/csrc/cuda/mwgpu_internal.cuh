@@ -81,6 +81,9 @@ struct DevOper {
     // K = 8: stacked x-step forms of the pencil contraction (k_pencil.cu), per
     // (depth, term group, x slot); null otherwise
     const float *btc_stack;
+    // K = 8: the y- and z-step operator fragments of the pencil contraction per
+    // (depth, term row, l = -1, 0, 1): 1024 floats each (k_pencil.cu); null otherwise
+    const float *pfrag;
     int n_nodes;
     // derivative operators (DerivativeCalculator::makeOperBand): the band runs
     // along band_dir only, band_dir_w wide; -1: the convolution band box
@@ -374,6 +377,9 @@ struct PencilFormJob {
     long long off;
 };
 void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *forms, cudaStream_t s);
+// the pencil contraction's y / z operator fragments (op.pfrag layout): rows x T x 3 records
+constexpr int kPencilFragFloats = 1024;
+void launch_pencil_frags(const DevOper &op, int rows, float *frags, cudaStream_t s);
 void launch_pencil_units(const DevMRA &m, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, void *units, int n_units,
                          int *err, cudaStream_t s);
 // per work entry the number of its items whose term is wider than kPencilMaxW
