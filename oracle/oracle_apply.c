@@ -221,7 +221,7 @@ static int tree_load(otree *t, const oracle_mra *m, int n, const int *idx, const
 
 /* ---------------------------------------------------------------- 1D filter step */
 /* math_utils::apply_filter: g(K^2 x K) (=|+=) f^T(K^2 x K) * F(K x K), column-major */
-static void apply_filter(double *out, const double *in, const double *F, int K, int add) {
+static void apply_filter_plain(double *out, const double *in, const double *F, int K, int add) {
     const int K2 = K * K;
     for (int j = 0; j < K; j++) {
         const double *Fj = F + (size_t)K * j;
@@ -234,6 +234,41 @@ static void apply_filter(double *out, const double *in, const double *F, int K, 
         }
     }
 }
+#ifndef ORACLE_FAST
+static void apply_filter(double *out, const double *in, const double *F, int K, int add) { apply_filter_plain(out, in, F, K, add); }
+#else
+/* The timing build (liboracle_fast.so, the CPU baseline): the same products
+ * in the order a matrix library runs them, out(:, j) += in^T(:, i) F(i, j)
+ * over contiguous columns of K^2 (the input transposed once per call), so the
+ * compiler vectorises the inner loop (the reference's Eigen products of
+ * ConvolutionCalculator.cpp:366-379 are vectorised the same way). */
+#define ORACLE_KMAX 20
+static void apply_filter(double *out, const double *in, const double *F, int K, int add) {
+    if (K > ORACLE_KMAX) {
+        apply_filter_plain(out, in, F, K, add);
+        return;
+    }
+    const int K2 = K * K;
+    double inT[ORACLE_KMAX * ORACLE_KMAX * ORACLE_KMAX];
+    double acc[ORACLE_KMAX * ORACLE_KMAX];
+    for (int c = 0; c < K2; c++)
+        for (int i = 0; i < K; i++) inT[(size_t)K2 * i + c] = in[(size_t)K * c + i];
+    for (int j = 0; j < K; j++) {
+        const double *Fj = F + (size_t)K * j;
+        for (int c = 0; c < K2; c++) acc[c] = 0.0;
+        for (int i = 0; i < K; i++) {
+            const double f = Fj[i];
+            const double *col = inT + (size_t)K2 * i;
+            for (int c = 0; c < K2; c++) acc[c] += col[c] * f;
+        }
+        double *o = out + (size_t)K2 * j;
+        if (add)
+            for (int c = 0; c < K2; c++) o[c] += acc[c];
+        else
+            for (int c = 0; c < K2; c++) o[c] = acc[c];
+    }
+}
+#endif
 
 static const double *filt(const oracle_mra *m, int op, int fidx) {
     int K = m->order + 1;
