@@ -94,6 +94,9 @@ def test_mixed_adaptive_interpolating_k5(gpu):
     st, gx, ref = run_pair(1e-3, mra, P, f, mw.FunctionTree(mra), mw.FunctionTree(mra), precision=mw.MIXED)
     same, perm = match(gx, ref)
     assert same, "mixed-form adaptive topology differs from the oracle"
+    # the screening decisions of the mixed form (FP32 estimate, FP64 near the
+    # threshold) are the reference's: the same node-term and component counts
+    assert st["node_terms"] == ref["node_terms"] and st["components"] == ref["components"]
     mx, l2 = rel_errors(gx["coefs"], ref["coefs"][perm])
     assert l2 <= MIXED_TOL, l2
 
