@@ -436,10 +436,14 @@ __global__ void k_scan_add(long long *out, long long n, const long long *block_s
 }
 
 // per-g item offsets: g_off[wi] = item_off[pair_off[wi]]
-__global__ void k_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, const int *nw_dev) {
+// per work entry the offset of its first item, clamped to the item capacity:
+// when a list outgrows its buffer (the fill flags DE_POOL_FULL and writes no
+// item beyond it) the passes that read the items stay inside it
+__global__ void k_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, const int *nw_dev,
+                              long long cap) {
     const int wi = blockIdx.x * blockDim.x + threadIdx.x;
     if (nw_dev) n_work = *nw_dev;
-    if (wi <= n_work) g_off[wi] = item_off[pair_off[wi]];
+    if (wi <= n_work) g_off[wi] = min(item_off[pair_off[wi]], cap);
 }
 
 // Term-major order of the work items of each output node: a stable counting
@@ -636,8 +640,9 @@ void launch_scan(const int *in, long long *out, long long n, long long *block_su
     k_scan_add<<<(unsigned)nb, kScanBlock, 0, s>>>(out, n, block_sums, total);
 }
 
-void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev) {
-    k_gather_goff<<<(n_work + 1 + 255) / 256, 256, 0, s>>>(item_off, pair_off, n_work, g_off, nw_dev);
+void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev,
+                        long long cap) {
+    k_gather_goff<<<(n_work + 1 + 255) / 256, 256, 0, s>>>(item_off, pair_off, n_work, g_off, nw_dev, cap);
 }
 
 bool term_order_supported(int n_terms) { return n_terms > 0 && n_terms <= kOrderMaxTerms; }

@@ -1940,7 +1940,7 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
         launch_pairs_count(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
                            &dst->components, &dst->band_nodes, pl->d_err, st);
         launch_scan(pl->d_pcounts, pl->d_item_off, pl->np, pl->d_scan, pl->d_scan + (pl->scan_n - 1), st);
-        launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st);
+        launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st, nullptr, pl->items_cap);
         const bool ordered = term_order_supported(o->op.n_terms);
         launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
                           pl->d_item_off, ordered ? pl->d_items_cm : pl->d_items, pl->items_cap, pl->d_err, st);
@@ -2630,7 +2630,7 @@ extern "C" mwgpu_status mwgpu_apply_judged(mwgpu_ctx *ctx, const mwgpu_oper *o, 
             launch_pairs_count(m, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, b.work, b.pair_off, nl, pc, ctx->d_gthr, b.pcounts, &dst->components,
                                &dst->band_nodes, ctx->d_err, st, np_dev, b.nwork);
             launch_scan(b.pcounts, b.item_off, pc, b.iscan, b.iscan + (scan_blocks(max_pairs + 1) + 1), st);
-            launch_gather_goff(b.item_off, b.pair_off, nl, b.goff, st, b.nwork);
+            launch_gather_goff(b.item_off, b.pair_off, nl, b.goff, st, b.nwork, lvl_items[j]);
             launch_chunk_count(b.goff, nl, lvl_per[j], b.ccnt, st, b.nwork);
             launch_scan(b.ccnt, b.coff, nl, b.cscan, b.cscan + (scan_blocks(max_level + 1) + 1), st);
             const int ccap = (int)((long long)nl + kChunkTarget + 1);

@@ -288,7 +288,9 @@ void launch_reduce_chunks(const DevMRA &m, const DevTree *gs, const int *work_tr
 int contract_items_resident(int K);
 long long scan_blocks(long long n);
 void launch_scan(const int *in, long long *out, long long n, long long *block_sums, long long *total, cudaStream_t s);
-void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev = nullptr);
+// cap: the capacity of the item buffer the offsets index (offsets beyond it are clamped)
+void launch_gather_goff(const long long *item_off, const long long *pair_off, int n_work, long long *g_off, cudaStream_t s, const int *nw_dev = nullptr,
+                        long long cap = 0x7fffffffffffffffLL);
 // term-major order of each output node's items (in -> out, same ranges); only
 // for operators of at most kOrderMaxTerms terms
 bool term_order_supported(int n_terms);

@@ -345,3 +345,54 @@ def test_level_gen_node_families_are_bit_identical(gpu, monkeypatch):
     assert ga == gb > 0
     assert np.array_equal(a["idx"], b["idx"])
     assert np.array_equal(a["coefs"], b["coefs"])
+
+
+def test_plan_work_list_outgrowing_its_capacity_is_reported(gpu):
+    """A mixed plan of a screened level (a positive output square norm) sizes
+    its work list from the screening at plan time.  Input values a million
+    times larger let far more component products pass the same threshold (set
+    1e4 times above the apply's here): the
+    list outgrows its buffer, the fill writes nothing beyond it, the passes
+    that read the items stop at its end, and execute returns MWGPU_ERR_OOM
+    (2); the context stays usable."""
+    L = mw.lib()
+    mra = mw.MRA(box=(-20, 20), order=7, basis=mw.LEGENDRE)
+    P = mw.PoissonOperator(mra, 1e-4)
+    f = _inputs(mra, 1e-4, (3,), 2200)[0]
+    grid = mw.FunctionTree(mra)
+    mw.apply(1e-4, grid, P, f, precision=mw.FP64)
+    ctx = C.c_void_p()
+    cfg = mw.MwgpuConfig()
+    cfg.precision = mw.MIXED
+    assert L.mwgpu_init(C.byref(ctx), C.byref(cfg)) == 0
+    try:
+        dop = C.c_void_p()
+        assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
+        dinp, fx = _upload_input(L, ctx, mra, f)
+        dout, gx = _create_output(L, ctx, mra, grid)
+        n = len(gx["child0"])
+        PA1 = C.c_void_p * 1
+        plan = C.c_void_p()
+        # a square norm 1e8 times that of the result: a screening threshold 1e4
+        # times higher than the apply's, which keeps few products at plan time
+        sq = np.full(1, grid.square_norm * 1e8)
+        assert sq[0] > 0.0
+        rc = L.mwgpu_plan_create(ctx, dop, 1, PA1(dinp), PA1(dout), mw._pi(np.zeros(n, dtype=np.int32)), mw._pi(np.arange(n, dtype=np.int32)),
+                                 n, 1e-4, mw._pd(sq), 1, C.byref(plan))
+        assert rc == 0, L.mwgpu_last_error(ctx).decode()
+        st = mw.MwgpuLevelStats()
+        assert L.mwgpu_plan_execute(ctx, plan, C.byref(st)) == 0
+        screened = st.node_terms
+        big = np.ascontiguousarray(fx["coefs"] * 1e6)
+        assert L.mwgpu_tree_update_coefs(ctx, dinp, mw._pd(big), None) == 0
+        rc = L.mwgpu_plan_execute(ctx, plan, C.byref(st))
+        assert rc == 2, (rc, L.mwgpu_last_error(ctx).decode())
+        assert "outgrew" in L.mwgpu_last_error(ctx).decode()
+        assert L.mwgpu_plan_destroy(ctx, plan) == 0
+        # the context still computes: the same level without the plan
+        assert L.mwgpu_sync(ctx) == 0
+        st2 = mw.MwgpuLevelStats()
+        assert L.mwgpu_apply_level(ctx, dop, dinp, dout, mw._pi(np.arange(n, dtype=np.int32)), n, 1e-4, float(sq[0]), None, C.byref(st2)) == 0
+        assert st2.node_terms > 1.25 * screened
+    finally:
+        L.mwgpu_destroy(ctx)
