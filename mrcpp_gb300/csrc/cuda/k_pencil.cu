@@ -43,14 +43,15 @@
 //
 // Roles (128 + 32 x 8 threads): warp 0 lane 0 stages operands with
 // cp.async.bulk into mbarrier-tracked slots (a pencil's f nodes once for all
-// its term groups, stacked operator forms); warp 1
-// lane 0 issues the tensor-core products and commits into one of two TMEM
-// buffers, so that the products of the next unit overlap the consumers; warps
-// 2 and 3 only give their registers to the consumers (setmaxnreg); warps 4-11
-// (consumers; warp 4 + w owns x = w and w + 8, so that each has one x of the U
-// channel; or warps 4-19 with one x each) read TMEM, transpose S1 through
-// shared memory, run the y / z steps and keep the g accumulators (FP32 sums
-// per unit, compensated sums over the units) of the task.  A task is (g, l_z): its
+// its term groups, stacked operator forms); warp 1 lane 0 issues the
+// tensor-core products and commits into one of two TMEM buffers, so that the
+// products of the next unit overlap the consumers; warps 2 and 3 only give
+// their registers to the consumers (setmaxnreg); warps 4-11 (consumers; warp
+// 4 + w owns x = w and w + 8, so that each has one x of the U channel; or
+// warps 4-19 with one x each) read TMEM, transpose S1 through shared memory,
+// load their y / z operator fragments (op.pfrag, split and masked at operator
+// upload), run the y / z steps and keep the g accumulators (FP32 sums per
+// unit, compensated sums over the units) of the task.  A task is (g, l_z): its
 // pencils x their term groups ("units", made by the host and
 // k_pencil_units); its 8 (k+1)^3 sums go to pen_partial[slot] in FP64, and the
 // chunk reduction adds the tasks of g after its chunk partials.
