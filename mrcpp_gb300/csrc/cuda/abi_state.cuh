@@ -121,16 +121,20 @@ struct mwgpu_oper {
     int n_rows = 0;
     std::vector<int> widths;    // [T * n_rows * 5]
     std::vector<int> band_max;  // [n_rows]
-    // pencil contraction (order 7): per depth and k = 0..kPencilMaxL the number
-    // of terms with band width >= k among those of width <= kPencilMaxW, the
-    // term row of the first such term (the wider ones come first), and per
-    // (depth, group, x slot) the float offset of the stacked form in
-    // op.btc_stack (-1: none) and its number of terms
-    std::vector<int> pen_tk;    // [rows][kPencilMaxL + 1]
-    std::vector<int> pen_r0;    // [rows]
+    // pencil contraction (order 7), per configuration c (terms of band width
+    // <= kPencilCfgW[c] in the pencil kernel): per depth and k = 0..kPencilMaxL
+    // the number of terms with band width >= k among those of width <=
+    // kPencilCfgW[c], the term row of the first such term (the wider ones come
+    // first), and per (depth, group, x slot) the float offset of the stacked
+    // form in op.btc_stack (-1: none) and its number of terms
+    struct PenCfg {
+        std::vector<int> tk;    // [rows][kPencilMaxL + 1]
+        std::vector<int> r0;    // [rows]
+        std::vector<long long> form;
+        std::vector<short> nform;
+    };
+    PenCfg pen[mwgpu::kPencilCfgs];
     int pen_groups = 0;
-    std::vector<long long> pen_form;
-    std::vector<short> pen_nform;
 };
 
 struct mwgpu_tree {

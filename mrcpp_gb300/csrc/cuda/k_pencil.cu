@@ -78,7 +78,7 @@ template <> struct Regs<16> { static constexpr int prod = 40, cons = 104; };
 constexpr int GT = kPencilGroup;          // terms per group (per product)
 constexpr int CPT = 24;                    // D columns per term
 constexpr int NMAX = (GT * CPT + 15) / 16 * 16;   // 128: two D buffers of two tiles fit the 512 TMEM columns
-constexpr int NFS = kPencilSlots;          // f slots: one per x slot of a pencil
+constexpr int NFS = kPencilRing;           // f buffers: a ring through which a unit's x slots pass
 constexpr int FREC = kTcNodeFloats * 4;    // bytes of a staged real node (hi 16 KB, lo 16 KB)
 constexpr int GREC = 8192;                 // bytes of a staged GenNode (hi 4 KB, lo 4 KB; rows 64-127 zero)
 constexpr int BREC = 128 * NMAX;           // bytes of a stacked form (hi s0, hi s1, lo s0, lo s1)
@@ -87,8 +87,8 @@ constexpr int BREC = 128 * NMAX;           // bytes of a stacked form (hi s0, hi
 constexpr int YS = 24, XS = 16 * YS, UYS = 8, US = 64;
 constexpr int S1_FLOATS = 16 * XS + 8 * US;
 // shared memory map (bytes)
-constexpr int SM_F = 0;                              // NFS real-node slots
-constexpr int SM_G = SM_F + NFS * FREC;              // NFS GenNode slots (a slot's node is real or generated)
+constexpr int SM_F = 0;                              // NFS real-node buffers
+constexpr int SM_G = SM_F + NFS * FREC;              // NFS GenNode buffers (a ring entry's node is real or generated)
 constexpr int SM_B = SM_G + NFS * GREC;              // 2 form slots
 constexpr int SM_S1 = SM_B + 2 * BREC;               // S1 staging
 constexpr int SM_BYTES = SM_S1 + 2 * 4 * S1_FLOATS;
@@ -255,7 +255,7 @@ __global__ void k_stack_forms(DevOper op, const PencilFormJob *jobs, int n_jobs,
 }
 
 // ---------------------------------------------------------------------------
-// The consumers' operator fragments, per (depth, term row r, l = -1, 0, 1) one
+// The consumers' operator fragments, per (depth, term row r, |l| <= kPencilMaxL) one
 // record of kPencilFragFloats, made at operator upload: the TF32 hi / lo parts
 // of the blocks in the mma.sync fragment order of each lane, the blocks (a, b)
 // outside the band (|l| > bw[2a + b]) zero.  Lane (g, tq), g = lane / 4,
@@ -269,7 +269,7 @@ __global__ void k_stack_forms(DevOper op, const PencilFormJob *jobs, int n_jobs,
 //     (the B fragments of the z step, k permuted).
 __global__ void k_pencil_frags(DevOper op, float *frags) {
     const int T = op.n_terms;
-    const int slot = blockIdx.x, l = slot % 3 - 1, tr = slot / 3, r = tr % T, dd = tr / T;
+    const int slot = blockIdx.x, l = slot % kPencilFragL - kPencilMaxL, tr = slot / kPencilFragL, r = tr % T, dd = tr / T;
     const TermRow row = op.term_rows[(size_t)dd * T + r];
     const bool exists = row.off >= 0 && abs(l) <= row.L0;
     const float *blk = exists ? op.blocks32 + (size_t)(row.off + l + row.L0) * 256 : nullptr;
@@ -390,9 +390,7 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
     // running counters (the producer and the MMA lane walk the same units and nodes)
     unsigned nu = 0;            // units done
     unsigned nb = 0;            // forms
-    unsigned nfs[NFS];          // pencils staged in (producer) / released from (MMA) each f slot
-    for (int i = 0; i < NFS; i++) nfs[i] = 0;
-    unsigned pmask = 0;         // f slots of the current pencil
+    unsigned nfr = 0;           // f nodes staged (producer) / consumed (MMA) through the ring
     bool lbad = false;
     auto fail = [&]() {
         if (!lbad) atomicOr(err, DE_TIMEOUT);
@@ -422,29 +420,26 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                     for (int u = u0; u < u1 && !lbad; u++) {
                         const Unit &U = units[u];
                         const DevTree &f = fs[work_tree[U.wi]];
-                        if (U.pflags & 1) {
-                            // the pencil's f nodes, once for all its term groups (the first group has the widest window)
-                            for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
-                                const int fid = U.fid[b];
-                                if (fid < 0) continue;
-                                if (nfs[b] >= 1 && !bar_wait(&f_empty[b], (nfs[b] - 1) & 1)) { fail(); break; }
-                                if (fid < f.cap_real) {
-                                    expect_tx(&f_full[b], FREC);
-                                    bulk(sm + SM_F + b * FREC, f.tc32 + (size_t)fid * kTcNodeFloats, FREC, &f_full[b]);
-                                } else {
-                                    const float *src = f.gtc32 + (size_t)(fid - f.cap_real) * kTcGenFloats;
-                                    unsigned char *dst = sm + SM_G + b * GREC;
-                                    expect_tx(&f_full[b], 4096);
-                                    bulk(dst, src, 1024, &f_full[b]);               // hi, k chunk 0, rows 0-63
-                                    bulk(dst + 2048, src + 256, 1024, &f_full[b]);  // hi, k chunk 1
-                                    bulk(dst + 4096, src + 512, 1024, &f_full[b]);  // lo, k chunk 0
-                                    bulk(dst + 6144, src + 768, 1024, &f_full[b]);  // lo, k chunk 1
-                                }
-                                nfs[b]++;
-                            }
-                        }
+                        // slot by slot: the f node into the next ring buffer, then the
+                        // slot's stacked form (the MMA lane takes them in this order)
                         for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
-                            if (U.fid[b] < 0) continue;
+                            const int fid = U.fid[b];
+                            if (fid < 0) continue;
+                            const int r = (int)(nfr % NFS);
+                            if (nfr >= NFS && !bar_wait(&f_empty[r], ((nfr / NFS) - 1) & 1)) { fail(); break; }
+                            if (fid < f.cap_real) {
+                                expect_tx(&f_full[r], FREC);
+                                bulk(sm + SM_F + r * FREC, f.tc32 + (size_t)fid * kTcNodeFloats, FREC, &f_full[r]);
+                            } else {
+                                const float *src = f.gtc32 + (size_t)(fid - f.cap_real) * kTcGenFloats;
+                                unsigned char *dst = sm + SM_G + r * GREC;
+                                expect_tx(&f_full[r], 4096);
+                                bulk(dst, src, 1024, &f_full[r]);               // hi, k chunk 0, rows 0-63
+                                bulk(dst + 2048, src + 256, 1024, &f_full[r]);  // hi, k chunk 1
+                                bulk(dst + 4096, src + 512, 1024, &f_full[r]);  // lo, k chunk 0
+                                bulk(dst + 6144, src + 768, 1024, &f_full[r]);  // lo, k chunk 1
+                            }
+                            nfr++;
                             const int s = nb & 1;
                             if (nb >= 2 && !bar_wait(&b_empty[s], ((nb >> 1) - 1) & 1)) { fail(); break; }
                             const uint32_t bytes = 128u * (uint32_t)n_pad(U.nform[b]);
@@ -463,16 +458,6 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                         const Unit &U = units[u];
                         const DevTree &f = fs[work_tree[U.wi]];
                         const int db = nu & 1;
-                        if (U.pflags & 1) {
-                            // the pencil's f nodes are staged
-                            pmask = 0;
-                            for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
-                                if (U.fid[b] < 0) continue;
-                                if (!bar_wait(&f_full[b], nfs[b] & 1)) { fail(); break; }
-                                pmask |= 1u << b;
-                            }
-                            if (lbad) break;
-                        }
                         // the consumers have read this D buffer (unit nu - 2)
                         if (nu >= 2 && !bar_wait(&d_empty[db], ((nu >> 1) - 1) & 1)) { fail(); break; }
                         fence_after();
@@ -481,8 +466,10 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                         for (int b = 0; b <= 2 * U.xw && !lbad; b++) {
                             const int fid = U.fid[b];
                             if (fid < 0) continue;
+                            const int r = (int)(nfr % NFS);
+                            if (!bar_wait(&f_full[r], (nfr / NFS) & 1)) { fail(); break; }
                             const bool gen = fid >= f.cap_real;
-                            const uint32_t a_hi = gen ? su32(sm + SM_G + b * GREC) : su32(sm + SM_F + b * FREC);
+                            const uint32_t a_hi = gen ? su32(sm + SM_G + r * GREC) : su32(sm + SM_F + r * FREC);
                             const int nt_tiles = gen ? 1 : 2, nks = gen ? 1 : 2;
                             const int sbix = nb & 1;
                             if (!bar_wait(&b_full[sbix], (nb >> 1) & 1)) { fail(); break; }
@@ -507,17 +494,11 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                                     mma(d, ah, bh, id, 1u);
                                 }
                             for (int t = 0; t < nt_tiles; t++) first[t] = false;
-                            commit(&b_empty[sbix]);    // the form slot is free once these products finish
+                            commit(&b_empty[sbix]);    // the form and the f buffer are free once these products finish
+                            commit(&f_empty[r]);
+                            nfr++;
                         }
                         commit(&d_full[db]);           // also after a failure, so that the consumers are released
-                        if (U.pflags & 2) {
-                            // last group of the pencil: its f slots are free once the products finish
-                            for (int b = 0; b < NFS; b++)
-                                if ((pmask >> b) & 1u) {
-                                    commit(&f_empty[b]);
-                                    nfs[b]++;
-                                }
-                        }
                         nu++;
                     }
                 }
@@ -526,7 +507,7 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
             if (warp <= 1) {
                 nu = __shfl_sync(0xffffffffu, nu, 0);
                 nb = __shfl_sync(0xffffffffu, nb, 0);
-                for (int i = 0; i < NFS; i++) nfs[i] = __shfl_sync(0xffffffffu, nfs[i], 0);
+                nfr = __shfl_sync(0xffffffffu, nfr, 0);
             }
             if (__syncthreads_or(lbad) != 0) {
                 lbad = true;
@@ -584,9 +565,9 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
                         float *S1s = S1base + (nterm & 1) * S1_FLOATS;
                         float *Us = S1s + 16 * XS;
                         // this term's operator fragments (in flight during the drain)
-                        const size_t frow = ((size_t)U.depth * T + U.q + j) * 3;
-                        const float4 *py = reinterpret_cast<const float4 *>(op.pfrag + (frow + 1 + U.ly) * kPencilFragFloats);
-                        const float4 *pz = reinterpret_cast<const float4 *>(op.pfrag + (frow + 1 + U.lz) * kPencilFragFloats) + 128;
+                        const size_t frow = ((size_t)U.depth * T + U.q + j) * kPencilFragL + kPencilMaxL;
+                        const float4 *py = reinterpret_cast<const float4 *>(op.pfrag + (frow + U.ly) * kPencilFragFloats);
+                        const float4 *pz = reinterpret_cast<const float4 *>(op.pfrag + (frow + U.lz) * kPencilFragFloats) + 128;
                         float4 fy[4], fz[4];
 #pragma unroll
                         for (int s = 0; s < 2; s++) {
@@ -809,12 +790,12 @@ __global__ void __launch_bounds__(n_threads<NCW>(), 1) k_pencil(DevOper op, cons
 // Work items that the pencil kernel covers (terms of band width <= kPencilMaxW
 // at the depth of g) leave the list of the item kernel: per work entry a
 // stable compaction.
-__device__ __forceinline__ bool kept(const DevOper &op, int depth, const WorkItem &it) {
-    return op.bw[((size_t)it.term * op.max_rows + depth) * 5 + 4] > kPencilMaxW;
+__device__ __forceinline__ bool kept(const DevOper &op, int depth, const WorkItem &it, int maxw) {
+    return op.bw[((size_t)it.term * op.max_rows + depth) * 5 + 4] > maxw;
 }
 
 __global__ void k_keep_count(DevMRA m, DevOper op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off, int n_work,
-                             const WorkItem *items, int *keep, const int *nw_dev) {
+                             const WorkItem *items, int *keep, const int *nw_dev, int maxw) {
     const int wi = blockIdx.x;
     if (nw_dev && wi >= *nw_dev) {
         if (threadIdx.x == 0) keep[wi] = 0;
@@ -823,7 +804,7 @@ __global__ void k_keep_count(DevMRA m, DevOper op, const DevTree *gs, const int 
     if (wi >= n_work) return;
     const int depth = gs[work_tree[wi]].idx[work[wi]].x - m.root_scale;
     int c = 0;
-    for (long long i = g_off[wi] + threadIdx.x; i < g_off[wi + 1]; i += blockDim.x) c += kept(op, depth, items[i]) ? 1 : 0;
+    for (long long i = g_off[wi] + threadIdx.x; i < g_off[wi + 1]; i += blockDim.x) c += kept(op, depth, items[i], maxw) ? 1 : 0;
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
     __shared__ int red[8];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
@@ -836,7 +817,7 @@ __global__ void k_keep_count(DevMRA m, DevOper op, const DevTree *gs, const int 
 }
 
 __global__ void k_keep_fill(DevMRA m, DevOper op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
-                            const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, const int *nw_dev) {
+                            const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, const int *nw_dev, int maxw) {
     const int wi = blockIdx.x;
     if (wi >= n_work || (nw_dev && wi >= *nw_dev)) return;
     const int depth = gs[work_tree[wi]].idx[work[wi]].x - m.root_scale;
@@ -846,7 +827,7 @@ __global__ void k_keep_fill(DevMRA m, DevOper op, const DevTree *gs, const int *
     // one warp keeps the order: ballot prefix per 32 items
     for (long long i0 = b; i0 < e; i0 += 32) {
         const long long i = i0 + lane;
-        const bool k = i < e && kept(op, depth, in[i]);
+        const bool k = i < e && kept(op, depth, in[i], maxw);
         const unsigned mk = __ballot_sync(0xffffffffu, k);
         if (k) out[dst + __popc(mk & ((1u << lane) - 1u))] = in[i];
         dst += __popc(mk);
@@ -887,7 +868,7 @@ void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *
 }
 
 void launch_pencil_frags(const DevOper &op, int rows, float *frags, cudaStream_t s) {
-    const int n = rows * op.n_terms * 3;
+    const int n = rows * op.n_terms * kPencilFragL;
     if (n <= 0) return;
     pencil::k_pencil_frags<<<n, 256, 0, s>>>(op, frags);
 }
@@ -899,15 +880,15 @@ void launch_pencil_units(const DevMRA &m, const DevTree *fs, const DevTree *gs, 
 }
 
 void launch_keep_items(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
-                       int n_work, const WorkItem *in, int *keep, cudaStream_t s, const int *nw_dev) {
+                       int n_work, const WorkItem *in, int *keep, cudaStream_t s, int maxw, const int *nw_dev) {
     if (n_work <= 0) return;
-    pencil::k_keep_count<<<n_work, 256, 0, s>>>(m, op, gs, work_tree, work, g_off, n_work, in, keep, nw_dev);
+    pencil::k_keep_count<<<n_work, 256, 0, s>>>(m, op, gs, work_tree, work, g_off, n_work, in, keep, nw_dev, maxw);
 }
 
 void launch_keep_fill(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
-                      const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, const int *nw_dev) {
+                      const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, int maxw, const int *nw_dev) {
     if (n_work <= 0) return;
-    pencil::k_keep_fill<<<n_work, 32, 0, s>>>(m, op, gs, work_tree, work, g_off, k_off, n_work, in, out, nw_dev);
+    pencil::k_keep_fill<<<n_work, 32, 0, s>>>(m, op, gs, work_tree, work, g_off, k_off, n_work, in, out, nw_dev, maxw);
 }
 
 void launch_pencil(const DevOper &op, const DevTree *fs, const int *work_tree, const void *units, const int *task_unit, int n_tasks,

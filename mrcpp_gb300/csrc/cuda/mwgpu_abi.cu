@@ -313,7 +313,14 @@ struct PencilPlan {
     int n_tasks = 0;
 };
 
-void pencil_build(const Level &lv, PencilPlan &pp) {
+// Pencil configuration of a level: per-call levels take the terms of band
+// width <= 1 (their units are made on the host on every call, and the wider
+// terms would multiply them), plans the terms up to kPencilMaxW (units made
+// once; measured on the bench level: 2.64 ms for the contraction against 3.14
+// ms with the narrow terms only).
+constexpr int kLevelPencilCfg = 0, kPlanPencilCfg = 1;
+
+void pencil_build(const Level &lv, PencilPlan &pp, int cfg) {
     const mwgpu_oper *o = lv.o;
     const DevMRA &m = o->mra;
     const int G = o->pen_groups, n = lv.n;
@@ -328,9 +335,10 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
         const int4 gx = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]];
         const int depth = gx.x - m.root_scale;
         if (depth < 0 || depth >= o->n_rows || o->band_max[depth] < 0) continue;
-        const int *tk = &o->pen_tk[(size_t)depth * NK];
+        const mwgpu_oper::PenCfg &pc = o->pen[cfg];
+        const int *tk = &pc.tk[(size_t)depth * NK];
         if (tk[0] == 0) continue;
-        const int W = std::min(o->band_max[depth], mwgpu::kPencilMaxL);
+        const int W = std::min(o->band_max[depth], mwgpu::kPencilCfgW[cfg]);
         auto inworld = [&](int d, long long l) {
             const long long c = (long long)m.corner[d] << depth, nb = (long long)m.nbox[d] << depth;
             return l >= c && l < c + nb;
@@ -347,13 +355,13 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
                 const int tm = tk[mm];
                 for (int q = 0; q * G5 < tm; q++) {
                     PencilUnit U{};
-                    U.pflags = (short)((q == 0 ? 1 : 0) | ((q + 1) * G5 >= tm ? 2 : 0));
+                    U.pflags = 3;   // the kernel stages every unit's f nodes
                     U.task = task;
                     U.wi = wi;
                     U.depth = (short)depth;
                     U.ly = (signed char)ly;
                     U.lz = (signed char)lz;
-                    U.q = (short)(o->pen_r0[depth] + G5 * q);
+                    U.q = (short)(pc.r0[depth] + G5 * q);
                     U.nt = (short)std::min(G5, tm - G5 * q);
                     int xw = 0;
                     for (int k = 0; k < NK; k++) {
@@ -363,8 +371,8 @@ void pencil_build(const Level &lv, PencilPlan &pp) {
                     U.xw = (short)xw;
                     for (int b = 0; b < NS; b++) {
                         const size_t ix = ((size_t)depth * G + q) * NS + b;
-                        U.form[b] = o->pen_form[ix];
-                        U.nform[b] = o->pen_nform[ix];
+                        U.form[b] = pc.form[ix];
+                        U.nform[b] = pc.nform[ix];
                         U.fid[b] = -1;
                         if ((b + 1) / 2 <= xw) c += 2;   // tensor-core products
                     }
@@ -424,7 +432,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     const bool pencil = use_pencil(lv);
     PencilPlan pp;
     if (pencil) {
-        pencil_build(lv, pp);
+        pencil_build(lv, pp, kLevelPencilCfg);
         const long long nu = (long long)pp.units.size();
         if (auto s = grow_buf(ctx, &ctx->d_units, &ctx->units_cap, std::max(nu, 1LL))) return s;
         if (auto s = grow_buf(ctx, &ctx->d_task_unit, &ctx->task_unit_cap, pp.n_tasks + 1)) return s;
@@ -471,10 +479,11 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
         if (auto s = grow_buf(ctx, &ctx->d_keep, &ctx->keep_cap, n + 1)) return s;
         if (auto s = grow_buf(ctx, &ctx->d_keep_off, &ctx->keep_off_cap, n + 1)) return s;
         if (auto s = grow_buf(ctx, &ctx->d_scan, &ctx->scan_cap, std::max(scan_blocks(np + 1), scan_blocks(n + 1)) + 2)) return s;
-        launch_keep_items(m, o->op, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_goff, n, ctx->d_items, ctx->d_keep, ctx->stream);
+        launch_keep_items(m, o->op, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_goff, n, ctx->d_items, ctx->d_keep, ctx->stream,
+                          mwgpu::kPencilCfgW[kLevelPencilCfg]);
         launch_scan(ctx->d_keep, ctx->d_keep_off, n, ctx->d_scan, ctx->d_scan + (ctx->scan_cap - 1), ctx->stream);
         launch_keep_fill(m, o->op, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_goff, ctx->d_keep_off, n, ctx->d_items, ctx->d_items_cm,
-                         ctx->stream);
+                         ctx->stream, mwgpu::kPencilCfgW[kLevelPencilCfg]);
         ctx->launches += 5;
         MW_CK(cudaMemcpyAsync(offs.data(), ctx->d_keep_off, sizeof(long long) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream));
         kitems = ctx->d_items_cm;
@@ -1210,44 +1219,48 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         o->op.btc = p_btc;
     }
     if (mwgpu::pencil_supported(K)) {
-        // stacked x-step forms of the pencil contraction: per depth the terms of
-        // band width <= kPencilMaxW (after the wider ones in term-row order), in
-        // groups of kPencilGroup, for every x slot (l_x = 0, -k, +k) the group's
-        // terms with band width >= k
+        // stacked x-step forms of the pencil contraction, per configuration c:
+        // per depth the terms of band width <= kPencilCfgW[c] (after the wider
+        // ones in term-row order), in groups of kPencilGroup, for every x slot
+        // (l_x = 0, -k, +k) the group's terms with band width >= k
         constexpr int G5 = mwgpu::kPencilGroup, NK = mwgpu::kPencilMaxL + 1, NS = mwgpu::kPencilSlots;
         const int G = (T + G5 - 1) / G5;
         o->pen_groups = G;
-        o->pen_tk.assign((size_t)rows * NK, 0);
-        o->pen_r0.assign(rows, 0);
-        o->pen_form.assign((size_t)rows * G * NS, -1);
-        o->pen_nform.assign((size_t)rows * G * NS, 0);
         std::vector<mwgpu::PencilFormJob> jobs;
         long long fl = 0;
-        for (int dd = 0; dd < rows; dd++) {
-            int r0 = 0;
-            for (int ti = 0; ti < T; ti++) {
-                const TermRow &tr = trows[(size_t)dd * T + ti];
-                if (tr.off < 0) continue;
-                if (tr.bw_max > mwgpu::kPencilMaxW) {
-                    r0++;
-                    continue;
+        for (int c = 0; c < mwgpu::kPencilCfgs; c++) {
+            mwgpu_oper::PenCfg &pc = o->pen[c];
+            const int maxw = mwgpu::kPencilCfgW[c];
+            pc.tk.assign((size_t)rows * NK, 0);
+            pc.r0.assign(rows, 0);
+            pc.form.assign((size_t)rows * G * NS, -1);
+            pc.nform.assign((size_t)rows * G * NS, 0);
+            for (int dd = 0; dd < rows; dd++) {
+                int r0 = 0;
+                for (int ti = 0; ti < T; ti++) {
+                    const TermRow &tr = trows[(size_t)dd * T + ti];
+                    if (tr.off < 0) continue;
+                    if (tr.bw_max > maxw) {
+                        r0++;
+                        continue;
+                    }
+                    for (int k = 0; k < NK; k++)
+                        if (tr.bw_max >= k) pc.tk[(size_t)dd * NK + k]++;
                 }
-                for (int k = 0; k < NK; k++)
-                    if (tr.bw_max >= k) o->pen_tk[(size_t)dd * NK + k]++;
+                pc.r0[dd] = r0;
+                const int t0 = pc.tk[(size_t)dd * NK];
+                for (int q = 0; q * G5 < t0; q++)
+                    for (int b = 0; b < NS; b++) {
+                        const int k = (b + 1) / 2, lx = b == 0 ? 0 : ((b & 1) ? -k : k);
+                        const int nt = std::max(0, std::min(G5, pc.tk[(size_t)dd * NK + k] - G5 * q));
+                        if (nt <= 0) continue;
+                        const size_t ix = ((size_t)dd * G + q) * NS + b;
+                        pc.form[ix] = fl;
+                        pc.nform[ix] = (short)nt;
+                        jobs.push_back({dd, r0 + G5 * q, lx, nt, fl});
+                        fl += 32LL * ((24 * nt + 15) / 16 * 16);
+                    }
             }
-            o->pen_r0[dd] = r0;
-            const int t0 = o->pen_tk[(size_t)dd * NK];
-            for (int q = 0; q * G5 < t0; q++)
-                for (int b = 0; b < NS; b++) {
-                    const int k = (b + 1) / 2, lx = b == 0 ? 0 : ((b & 1) ? -k : k);
-                    const int nt = std::max(0, std::min(G5, o->pen_tk[(size_t)dd * NK + k] - G5 * q));
-                    if (nt <= 0) continue;
-                    const size_t ix = ((size_t)dd * G + q) * NS + b;
-                    o->pen_form[ix] = fl;
-                    o->pen_nform[ix] = (short)nt;
-                    jobs.push_back({dd, r0 + G5 * q, lx, nt, fl});
-                    fl += 32LL * ((24 * nt + 15) / 16 * 16);
-                }
         }
         mwgpu::PencilFormJob *p_jobs = nullptr;
         float *p_stack = nullptr;
@@ -1262,9 +1275,9 @@ mwgpu_status mwgpu_upload_operator(mwgpu_ctx *ctx, const mwgpu_mra_desc *mra, co
         MW_CK(cudaStreamSynchronize(ctx->stream));
         MW_CK(cudaGetLastError());
         o->op.btc_stack = p_stack;
-        // the y / z operator fragments of the consumers, per (depth, term row, l = -1, 0, 1)
+        // the y / z operator fragments of the consumers, per (depth, term row, l in the pencil band)
         float *p_frag = nullptr;
-        if ((s = dev_alloc(ctx, &p_frag, (size_t)rows * T * 3 * mwgpu::kPencilFragFloats))) {
+        if ((s = dev_alloc(ctx, &p_frag, (size_t)rows * T * mwgpu::kPencilFragL * mwgpu::kPencilFragFloats))) {
             for (void *p : o->allocs) cudaFree(p);
             pool_free(ctx, o->d_filt);
             delete o;
@@ -1947,9 +1960,11 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
         if (ordered) launch_order_terms(pl->d_goff, pl->n, pl->d_items_cm, pl->d_items, o->op.n_terms, pl->d_err, st);
         ctx->launches += 6 + (ordered ? 1 : 0);
         if (pl->pencil) {
-            launch_keep_items(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->n, pl->d_items, pl->d_keep, st);
+            launch_keep_items(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->n, pl->d_items, pl->d_keep, st,
+                              mwgpu::kPencilCfgW[kPlanPencilCfg]);
             launch_scan(pl->d_keep, pl->d_keep_off, pl->n, pl->d_kscan, pl->d_kscan + (pl->kscan_n - 1), st);
-            launch_keep_fill(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->d_keep_off, pl->n, pl->d_items, pl->d_items_cm, st);
+            launch_keep_fill(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->d_keep_off, pl->n, pl->d_items, pl->d_items_cm, st,
+                             mwgpu::kPencilCfgW[kPlanPencilCfg]);
             ctx->launches += 5;
         }
         plan_contract(ctx, pl, pl->per, true);
@@ -2199,7 +2214,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         if ((term_order_supported(o->op.n_terms) || pl->pencil) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
         if (pl->pencil) {
             PencilPlan pp;
-            pencil_build(lv, pp);
+            pencil_build(lv, pp, kPlanPencilCfg);
             pl->n_units = (int)pp.units.size();
             pl->n_tasks = pp.n_tasks;
             pl->kscan_n = scan_blocks(n + 1) + 2;

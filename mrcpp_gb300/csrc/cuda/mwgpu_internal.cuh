@@ -82,7 +82,8 @@ struct DevOper {
     // (depth, term group, x slot); null otherwise
     const float *btc_stack;
     // K = 8: the y- and z-step operator fragments of the pencil contraction per
-    // (depth, term row, l = -1, 0, 1): 1024 floats each (k_pencil.cu); null otherwise
+    // (depth, term row, l = -kPencilMaxL .. kPencilMaxL): 1024 floats each
+    // (k_pencil.cu); null otherwise
     const float *pfrag;
     int n_nodes;
     // derivative operators (DerivativeCalculator::makeOperBand): the band runs
@@ -212,12 +213,20 @@ struct LevelStats {
 // unit's terms reach |l_x| = k.  The host fills the topology part, the device
 // the f nodes (k_pencil_units).  The pencil path takes the terms whose band
 // width at the depth is at most kPencilMaxW (then every |l_d| <= that); the
-// wider terms stay with the item kernel: at |l| >= 2 they have 1 or 2 terms
-// per pencil, and a tensor-core product of N <= 48 costs as much as one of
-// N = 128.
-constexpr int kPencilMaxW = 1;
+// wider terms stay with the item kernel.  The kernel stages a unit's f nodes
+// slot by slot through a ring of kPencilRing buffers (shared memory holds
+// three 32 KB nodes next to the other buffers).
+constexpr int kPencilMaxW = 4;
 constexpr int kPencilMaxL = kPencilMaxW;
+// two configurations of the pencil path: the terms of band width <= 1 (levels
+// built per call: few units, cheap to make on the host) or <= kPencilMaxW
+// (plans: units made once)
+constexpr int kPencilCfgs = 2;
+constexpr int kPencilCfgW[kPencilCfgs] = {1, kPencilMaxW};
 constexpr int kPencilSlots = 2 * kPencilMaxL + 1;
+constexpr int kPencilRing = 3;
+// operator fragment records per (depth, term row): l = -kPencilMaxL .. kPencilMaxL
+constexpr int kPencilFragL = 2 * kPencilMaxL + 1;
 struct PencilUnit {
     long long form[kPencilSlots];   // float offsets of the stacked x-step forms of the slots
     int fid[kPencilSlots];          // f nodes of the slots (-1: none, outside the world or zero norm)
@@ -379,17 +388,18 @@ struct PencilFormJob {
     long long off;
 };
 void launch_stack_forms(const DevOper &op, const void *jobs, int n_jobs, float *forms, cudaStream_t s);
-// the pencil contraction's y / z operator fragments (op.pfrag layout): rows x T x 3 records
+// the pencil contraction's y / z operator fragments (op.pfrag layout): rows x T x kPencilFragL records
 constexpr int kPencilFragFloats = 1024;
 void launch_pencil_frags(const DevOper &op, int rows, float *frags, cudaStream_t s);
 void launch_pencil_units(const DevMRA &m, const DevTree *fs, const DevTree *gs, const int *work_tree, const int *work, void *units, int n_units,
                          int *err, cudaStream_t s);
 // per work entry the number of its items whose term is wider than kPencilMaxW
 // at the entry's depth (those the item kernel keeps), and their compaction
+// (maxw: the widest band the pencil kernel takes, kPencilCfgW of the configuration)
 void launch_keep_items(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
-                       int n_work, const WorkItem *in, int *keep, cudaStream_t s, const int *nw_dev = nullptr);
+                       int n_work, const WorkItem *in, int *keep, cudaStream_t s, int maxw, const int *nw_dev = nullptr);
 void launch_keep_fill(const DevMRA &m, const DevOper &op, const DevTree *gs, const int *work_tree, const int *work, const long long *g_off,
-                      const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, const int *nw_dev = nullptr);
+                      const long long *k_off, int n_work, const WorkItem *in, WorkItem *out, cudaStream_t s, int maxw, const int *nw_dev = nullptr);
 // persistent; counter: a device int (zeroed here); pen_partial: 8 K^3 doubles per task;
 // consumer_warps: 8 or 16 (the CTA shape; kPencilWarpsDefault where nothing was tuned)
 constexpr int kPencilWarpsDefault = 8;
