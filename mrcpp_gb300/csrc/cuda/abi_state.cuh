@@ -94,6 +94,8 @@ struct mwgpu_ctx {
     // pencil contraction (k_pencil.cu): units, task order, task sums, per-entry task ranges
     mwgpu::PencilUnit *d_units = nullptr;
     long long units_cap = 0;
+    mwgpu::PencilUnit *h_units = nullptr;  // page-locked staging of the units of a per-call level
+    size_t h_units_cap = 0;
     int *d_task_unit = nullptr;
     long long task_unit_cap = 0;
     double *d_pen_partial = nullptr;

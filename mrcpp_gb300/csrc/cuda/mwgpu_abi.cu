@@ -307,10 +307,19 @@ int pencil_warps() {
 // tasks in descending size (the persistent kernel takes them in this order),
 // each with its partial slot (slots of a work entry consecutive, pen_begin).
 struct PencilPlan {
-    std::vector<PencilUnit> units;  // in processing order of their tasks
+    std::vector<PencilUnit> flat;   // units in creation order, task t's at flat[tstart[t] .. tstart[t+1])
+    std::vector<int> tstart, ord;   // ord: the tasks in processing order
     std::vector<int> task_unit;     // first unit of every processed task, + total
     std::vector<int> pen_begin;     // per work entry its first slot, + total
     int n_tasks = 0;
+    size_t n_units = 0;
+    // the units in processing order of their tasks into dst[0 .. n_units)
+    void emit(PencilUnit *dst) const {
+        for (int k = 0; k < n_tasks; k++) {
+            const int t = ord[k];
+            std::copy(flat.begin() + tstart[t], flat.begin() + tstart[t + 1], dst + task_unit[k]);
+        }
+    }
 };
 
 // Pencil configuration of a level: per-call levels take the terms of band
@@ -325,10 +334,11 @@ void pencil_build(const Level &lv, PencilPlan &pp, int cfg) {
     const DevMRA &m = o->mra;
     const int G = o->pen_groups, n = lv.n;
     constexpr int G5 = mwgpu::kPencilGroup, NK = mwgpu::kPencilMaxL + 1, NS = mwgpu::kPencilSlots;
-    // units in creation order, task t's units at flat[tstart[t] .. tstart[t+1])
-    std::vector<PencilUnit> flat;
-    std::vector<int> tstart;
+    std::vector<PencilUnit> &flat = pp.flat;
+    std::vector<int> &tstart = pp.tstart;
     std::vector<long long> cost;
+    flat.clear();
+    tstart.clear();
     pp.pen_begin.assign(n + 1, 0);
     for (int wi = 0; wi < n; wi++) {
         pp.pen_begin[wi] = (int)tstart.size();
@@ -389,19 +399,18 @@ void pencil_build(const Level &lv, PencilPlan &pp, int cfg) {
     pp.n_tasks = (int)cost.size();
     pp.pen_begin[n] = pp.n_tasks;
     // tasks in descending cost (the persistent kernel takes them in this order)
-    std::vector<int> ord(pp.n_tasks);
+    std::vector<int> &ord = pp.ord;
+    ord.resize(pp.n_tasks);
     for (int i = 0; i < pp.n_tasks; i++) ord[i] = i;
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-    pp.units.resize(flat.size());
     pp.task_unit.assign(pp.n_tasks + 1, 0);
     size_t pos = 0;
     for (int k = 0; k < pp.n_tasks; k++) {
         pp.task_unit[k] = (int)pos;
-        const int t = ord[k];
-        std::copy(flat.begin() + tstart[t], flat.begin() + tstart[t + 1], pp.units.begin() + pos);
-        pos += (size_t)(tstart[t + 1] - tstart[t]);
+        pos += (size_t)(tstart[ord[k] + 1] - tstart[ord[k]]);
     }
     pp.task_unit[pp.n_tasks] = (int)pos;
+    pp.n_units = pos;
 }
 
 // Mixed form: work list (pair counts, scan, fill) then the contraction over
@@ -430,10 +439,10 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
     // the pencil units depend on the topology only: built on the host while the
     // device counts the work list, uploaded behind it
     const bool pencil = use_pencil(lv);
-    PencilPlan pp;
+    static thread_local PencilPlan pp;  // rebuilt every level, its host vectors kept between levels
     if (pencil) {
         pencil_build(lv, pp, kLevelPencilCfg);
-        const long long nu = (long long)pp.units.size();
+        const long long nu = (long long)pp.n_units;
         if (auto s = grow_buf(ctx, &ctx->d_units, &ctx->units_cap, std::max(nu, 1LL))) return s;
         if (auto s = grow_buf(ctx, &ctx->d_task_unit, &ctx->task_unit_cap, pp.n_tasks + 1)) return s;
         if (auto s = grow_buf(ctx, &ctx->d_pen_begin, &ctx->pen_begin_cap, n + 1)) return s;
@@ -446,7 +455,30 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
         }
         if (!ctx->d_pen_counter)
             if (auto s = dev_alloc(ctx, &ctx->d_pen_counter, 1)) return s;
-        if (nu > 0) MW_CK(cudaMemcpyAsync(ctx->d_units, pp.units.data(), sizeof(PencilUnit) * nu, cudaMemcpyHostToDevice, ctx->stream));
+        if (nu > 0) {
+            // through a page-locked staging buffer (a copy from pageable memory
+            // blocks the host at a fraction of the link's rate); the previous
+            // level's copy out of it ended at that level's stream synchronisation
+            if ((size_t)nu > ctx->h_units_cap) {
+                const size_t cap = std::max((size_t)nu, 2 * ctx->h_units_cap);
+                if (ctx->h_units) cudaFreeHost(ctx->h_units);
+                ctx->h_units = nullptr;
+                ctx->h_units_cap = 0;
+                if (cudaHostAlloc((void **)&ctx->h_units, sizeof(PencilUnit) * cap, cudaHostAllocDefault) == cudaSuccess)
+                    ctx->h_units_cap = cap;
+                else
+                    (void)cudaGetLastError(), ctx->h_units = nullptr;
+            }
+            std::vector<PencilUnit> pageable;
+            PencilUnit *hu = ctx->h_units;
+            if (!hu) {
+                pageable.resize(nu);
+                hu = pageable.data();
+            }
+            pp.emit(hu);
+            MW_CK(cudaMemcpyAsync(ctx->d_units, hu, sizeof(PencilUnit) * nu, cudaMemcpyHostToDevice, ctx->stream));
+            if (!ctx->h_units) MW_CK(cudaStreamSynchronize(ctx->stream));
+        }
         MW_CK(cudaMemcpyAsync(ctx->d_task_unit, pp.task_unit.data(), sizeof(int) * (pp.n_tasks + 1), cudaMemcpyHostToDevice, ctx->stream));
         MW_CK(cudaMemcpyAsync(ctx->d_pen_begin, pp.pen_begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
     }
@@ -529,7 +561,7 @@ mwgpu_status run_mixed(mwgpu_ctx *ctx, const Level &lv, LevelStats *hs) {
         // the wider terms' items (chunks; a chunk of an entry without kept items is empty), the pencils, then both sums
         launch_items(o->mra, o->op, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_chunks, nch, kitems, ctx->d_partial, ctx->d_err,
                      nullptr, nullptr, tc_ok ? ctx->d_tc_counter : nullptr, ctx->stream);
-        launch_pencil_units(o->mra, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_units, (int)pp.units.size(), ctx->d_err, ctx->stream);
+        launch_pencil_units(o->mra, ctx->d_fs, ctx->d_gs, ctx->d_wtree, ctx->d_work, ctx->d_units, (int)pp.n_units, ctx->d_err, ctx->stream);
         launch_pencil(o->op, ctx->d_fs, ctx->d_wtree, ctx->d_units, ctx->d_task_unit, pp.n_tasks, ctx->d_pen_partial, ctx->d_err,
                       ctx->d_pen_counter, ctx->stream, pencil_warps());
         launch_reduce_chunks(o->mra, ctx->d_gs, ctx->d_wtree, ctx->d_work, n, ctx->d_chunk_begin, ctx->d_partial, ctx->stream, nullptr,
@@ -997,6 +1029,7 @@ mwgpu_status mwgpu_destroy(mwgpu_ctx *ctx) {
         if (e) cudaEventDestroy(e);
     if (ctx->d_scrub) cudaFree(ctx->d_scrub);
     if (ctx->d_arena) cudaFree(ctx->d_arena);
+    if (ctx->h_units) cudaFreeHost(ctx->h_units);
     cudaEventDestroy(ctx->ev0);
     cudaEventDestroy(ctx->ev1);
     cudaEventDestroy(ctx->ev2);
@@ -2215,7 +2248,9 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         if (pl->pencil) {
             PencilPlan pp;
             pencil_build(lv, pp, kPlanPencilCfg);
-            pl->n_units = (int)pp.units.size();
+            std::vector<PencilUnit> units(pp.n_units);
+            pp.emit(units.data());
+            pl->n_units = (int)pp.n_units;
             pl->n_tasks = pp.n_tasks;
             pl->kscan_n = scan_blocks(n + 1) + 2;
             if ((s = plan_alloc(ctx, pl, &pl->d_keep, n + 1)) || (s = plan_alloc(ctx, pl, &pl->d_keep_off, n + 1)) ||
@@ -2225,7 +2260,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
                 (s = plan_alloc(ctx, pl, &pl->d_pen_partial, (size_t)std::max(pp.n_tasks, 1) * 8 * o->mra.kp1_d)))
                 return fail(s);
             if (pl->n_units > 0)
-                MW_CK(cudaMemcpyAsync(pl->d_units, pp.units.data(), sizeof(PencilUnit) * pl->n_units, cudaMemcpyHostToDevice, ctx->stream));
+                MW_CK(cudaMemcpyAsync(pl->d_units, units.data(), sizeof(PencilUnit) * pl->n_units, cudaMemcpyHostToDevice, ctx->stream));
             MW_CK(cudaMemcpyAsync(pl->d_task_unit, pp.task_unit.data(), sizeof(int) * (pp.n_tasks + 1), cudaMemcpyHostToDevice, ctx->stream));
             MW_CK(cudaMemcpyAsync(pl->d_pen_begin, pp.pen_begin.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, ctx->stream));
         }
