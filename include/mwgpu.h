@@ -272,7 +272,7 @@ mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *oper, int n_tre
 mwgpu_status mwgpu_plan_execute(mwgpu_ctx *ctx, mwgpu_plan *plan, mwgpu_level_stats *stats);
 mwgpu_status mwgpu_plan_check(mwgpu_ctx *ctx, mwgpu_plan *plan, mwgpu_level_stats *stats);
 /* Pencil contraction of the last checked execution of a plan (mwgpu_plan_check):
- * the node-terms it computed (those of the operator terms of band width <= 1,
+ * the node-terms it computed (those of the operator terms of band width <= 4,
  * on levels without norm screening) and its device time in ms; 0 and 0 when the
  * plan does not use it.  No reference counterpart (a measurement of the GPU
  * schedule of calcNodeVector, ConvolutionCalculator.cpp:224-382). */

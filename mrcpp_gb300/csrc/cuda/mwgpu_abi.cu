@@ -1899,6 +1899,11 @@ struct mwgpu_plan {
     // pencil contraction (unscreened order-7 levels): kept items of the item
     // kernel (their offsets per entry), units and task sums
     bool pencil = false;
+    // the pencil configuration covers every term of every entry (pen_all_ok);
+    // pen_all: the executions leave the item list unfilled.  Set for the
+    // captured graph only: the autotuning candidates of the item kernel alone
+    // read the list that the passes before them fill
+    bool pen_all_ok = false, pen_all = false;
     int pen_warps = kPencilWarpsDefault;     // consumer warps of the pencil kernel
     int *d_keep = nullptr;
     long long *d_keep_off = nullptr, *d_kscan = nullptr;
@@ -1987,18 +1992,25 @@ void plan_sequence(mwgpu_ctx *ctx, mwgpu_plan *pl) {
                            &dst->components, &dst->band_nodes, pl->d_err, st);
         launch_scan(pl->d_pcounts, pl->d_item_off, pl->np, pl->d_scan, pl->d_scan + (pl->scan_n - 1), st);
         launch_gather_goff(pl->d_item_off, pl->d_pair_off, pl->n, pl->d_goff, st, nullptr, pl->items_cap);
+        // the count pass gives the node-terms and the screening statistics; the
+        // items themselves only where the item kernel has terms to take
+        const bool fill = !(pl->pencil && pl->pen_all);
         const bool ordered = term_order_supported(o->op.n_terms);
-        launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr, pl->d_pcounts,
-                          pl->d_item_off, ordered ? pl->d_items_cm : pl->d_items, pl->items_cap, pl->d_err, st);
-        if (ordered) launch_order_terms(pl->d_goff, pl->n, pl->d_items_cm, pl->d_items, o->op.n_terms, pl->d_err, st);
-        ctx->launches += 6 + (ordered ? 1 : 0);
-        if (pl->pencil) {
+        if (fill) {
+            launch_pairs_fill(o->mra, o->op, pl->d_fs, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_pair_off, pl->n, pl->np, pl->d_gthr,
+                              pl->d_pcounts, pl->d_item_off, ordered ? pl->d_items_cm : pl->d_items, pl->items_cap, pl->d_err, st);
+            if (ordered) launch_order_terms(pl->d_goff, pl->n, pl->d_items_cm, pl->d_items, o->op.n_terms, pl->d_err, st);
+        }
+        ctx->launches += 5 + (fill ? 1 + (ordered ? 1 : 0) : 0);
+        if (pl->pencil && fill) {
             launch_keep_items(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->n, pl->d_items, pl->d_keep, st,
                               mwgpu::kPencilCfgW[kPlanPencilCfg]);
             launch_scan(pl->d_keep, pl->d_keep_off, pl->n, pl->d_kscan, pl->d_kscan + (pl->kscan_n - 1), st);
             launch_keep_fill(o->mra, o->op, pl->d_gs, pl->d_wtree, pl->d_work, pl->d_goff, pl->d_keep_off, pl->n, pl->d_items, pl->d_items_cm, st,
                              mwgpu::kPencilCfgW[kPlanPencilCfg]);
             ctx->launches += 5;
+        } else if (pl->pencil) {
+            cudaMemsetAsync(pl->d_keep_off, 0, sizeof(long long) * (pl->n + 1), st);   // no item is left to the item kernel
         }
         plan_contract(ctx, pl, pl->per, true);
     } else {
@@ -2244,6 +2256,15 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
             return fail(s);
         pl->pencil = use_pencil(lv);
         pl->pen_warps = pencil_warps();
+        if (pl->pencil) {
+            // every term at the depth of every entry within the plan configuration's band width
+            pl->pen_all_ok = std::getenv("MWGPU_PLAN_FILL") == nullptr;
+            for (int wi = 0; wi < n && pl->pen_all_ok; wi++) {
+                const int depth = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]].x - o->mra.root_scale;
+                if (depth >= 0 && depth < (int)o->band_max.size() && o->band_max[depth] > mwgpu::kPencilCfgW[kPlanPencilCfg])
+                    pl->pen_all_ok = false;
+            }
+        }
         if ((term_order_supported(o->op.n_terms) || pl->pencil) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
         if (pl->pencil) {
             PencilPlan pp;
@@ -2331,6 +2352,7 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         if ((s = plan_check(ctx, pl, nullptr))) return fail(s);
     }
     // capture the level as one graph
+    pl->pen_all = pl->pen_all_ok;
     unsigned long long l0 = ctx->launches;
     MW_CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
     plan_sequence(ctx, pl);

@@ -58,55 +58,89 @@ def test_level_path(gpu, case, warps):
     assert rel(a, c) <= 1e-5 and rel(b, c) <= 1e-5
 
 
-def test_plan_path(gpu, case):
-    mra, P, f, grid = case
+def _plan_run(mra, P, f, grid, work, env, flags=1):
+    """One planned mixed level over the output nodes `work` with the
+    environment `env` set at plan creation: (coefficients of the work rows,
+    node-terms, components, pencil node-terms, launches per execution, band
+    widths of the operator by depth)."""
     L = mw.lib()
-    out = {}
-    for no_pencil in (False, True):
-        if no_pencil:
-            os.environ["MWGPU_NO_PENCIL"] = "1"
-        ctx = C.c_void_p()
-        cfg = mw.MwgpuConfig()
-        cfg.precision = mw.MIXED
-        assert L.mwgpu_init(C.byref(ctx), C.byref(cfg)) == 0
-        try:
-            dop = C.c_void_p()
-            assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
-            fx = f.export()
-            fd = mw.MwgpuTreeDesc(len(fx["child0"]), mw._pi(fx["idx"]), mw._pi(fx["child0"]), mw._pd(fx["coefs"]), mw._pd(fx["norms"]))
-            dinp = C.c_void_p()
-            assert L.mwgpu_upload_tree(ctx, C.byref(mra.desc()), C.byref(fd), C.byref(dinp)) == 0
-            gx = grid.export()
-            gd = mw.MwgpuTreeDesc(len(gx["child0"]), mw._pi(gx["idx"]), mw._pi(gx["child0"]), None, None)
-            dout = C.c_void_p()
-            assert L.mwgpu_create_tree(ctx, C.byref(mra.desc()), C.byref(gd), C.byref(dout)) == 0
-            n = len(gx["child0"])
-            PA1 = C.c_void_p * 1
-            plan = C.c_void_p()
-            sq = np.full(1, -1.0)
-            rc = L.mwgpu_plan_create(ctx, dop, 1, PA1(dinp), PA1(dout), mw._pi(np.zeros(n, dtype=np.int32)), mw._pi(np.arange(n, dtype=np.int32)),
-                                     n, 1e-4, mw._pd(sq), 1, C.byref(plan))
-            assert rc == 0, L.mwgpu_last_error(ctx).decode()
-            for _ in range(2):
-                assert L.mwgpu_plan_execute(ctx, plan, None) == 0
-            st = mw.MwgpuLevelStats()
-            assert L.mwgpu_plan_check(ctx, plan, C.byref(st)) == 0
-            pnt, pms = C.c_ulonglong(), C.c_double()
-            assert L.mwgpu_plan_pencil_info(plan, C.byref(pnt), C.byref(pms)) == 0
-            c = np.zeros((n, 8 * 512))
-            assert L.mwgpu_download_tree(ctx, dout, mw._pd(c), None) == 0
-            assert L.mwgpu_plan_destroy(ctx, plan) == 0
-            out[no_pencil] = (c, st.node_terms, st.components, pnt.value)
-        finally:
-            os.environ.pop("MWGPU_NO_PENCIL", None)
-            L.mwgpu_destroy(ctx)
-    (a, nta, nca, pa), (b, ntb, ncb, pb) = out[False], out[True]
-    assert nta == ntb and nca == ncb
-    # the pencil kernel takes the terms of band width <= kPencilMaxW (here all)
-    assert 0 < pa <= nta and pb == 0
-    assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
+    os.environ.update(env)
+    ctx = C.c_void_p()
+    cfg = mw.MwgpuConfig()
+    cfg.precision = mw.MIXED
+    assert L.mwgpu_init(C.byref(ctx), C.byref(cfg)) == 0
+    try:
+        dop = C.c_void_p()
+        assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
+        rows = C.c_int()
+        assert L.mwgpu_operator_bandwidths(ctx, dop, C.byref(rows), None, None) == 0
+        band_max = np.zeros(rows.value, dtype=np.int32)
+        assert L.mwgpu_operator_bandwidths(ctx, dop, C.byref(rows), None, mw._pi(band_max)) == 0
+        fx = f.export()
+        fd = mw.MwgpuTreeDesc(len(fx["child0"]), mw._pi(fx["idx"]), mw._pi(fx["child0"]), mw._pd(fx["coefs"]), mw._pd(fx["norms"]))
+        dinp = C.c_void_p()
+        assert L.mwgpu_upload_tree(ctx, C.byref(mra.desc()), C.byref(fd), C.byref(dinp)) == 0
+        gx = grid.export()
+        gd = mw.MwgpuTreeDesc(len(gx["child0"]), mw._pi(gx["idx"]), mw._pi(gx["child0"]), None, None)
+        dout = C.c_void_p()
+        assert L.mwgpu_create_tree(ctx, C.byref(mra.desc()), C.byref(gd), C.byref(dout)) == 0
+        n = len(gx["child0"])
+        work = np.ascontiguousarray(work, dtype=np.int32)
+        PA1 = C.c_void_p * 1
+        plan = C.c_void_p()
+        sq = np.full(1, -1.0)
+        rc = L.mwgpu_plan_create(ctx, dop, 1, PA1(dinp), PA1(dout), mw._pi(np.zeros(len(work), dtype=np.int32)), mw._pi(work),
+                                 len(work), 1e-4, mw._pd(sq), flags, C.byref(plan))
+        assert rc == 0, L.mwgpu_last_error(ctx).decode()
+        for _ in range(2):
+            assert L.mwgpu_plan_execute(ctx, plan, None) == 0
+        st = mw.MwgpuLevelStats()
+        assert L.mwgpu_plan_check(ctx, plan, C.byref(st)) == 0
+        pnt, pms = C.c_ulonglong(), C.c_double()
+        assert L.mwgpu_plan_pencil_info(plan, C.byref(pnt), C.byref(pms)) == 0
+        lpe = C.c_ulonglong()
+        assert L.mwgpu_plan_info(plan, None, None, None, None, None, C.byref(lpe)) == 0
+        c = np.zeros((n, 8 * 512))
+        assert L.mwgpu_download_tree(ctx, dout, mw._pd(c), None) == 0
+        assert L.mwgpu_plan_destroy(ctx, plan) == 0
+        return c[work], st.node_terms, st.components, pnt.value, lpe.value, band_max
+    finally:
+        for k in env:
+            os.environ.pop(k, None)
+        L.mwgpu_destroy(ctx)
 
 
+def test_plan_path(gpu, case):
+    # "pencil": the plan configuration; "fill": the same with the item list
+    # filled and compacted every execution (MWGPU_PLAN_FILL); "items": the
+    # item kernel alone.  Where every term at the depth of every output node
+    # is within the pencil kernel's band width, the plan leaves the item list
+    # unfilled (fewer launches, the same bits); the work list of every node
+    # may leave terms to the item kernel at some depths, that of the nodes at
+    # depths whose band width is within the pencil kernel's none
+    mra, P, f, grid = case
+    gx = grid.export()
+    allw = np.arange(len(gx["child0"]), dtype=np.int32)
+    env = {"pencil": {}, "fill": {"MWGPU_PLAN_FILL": "1"}, "items": {"MWGPU_NO_PENCIL": "1"}}
+    band_max = _plan_run(mra, P, f, grid, allw[:1], {"MWGPU_NO_PENCIL": "1"}, 0)[5]
+    depth = gx["idx"][:, 0] - gx["idx"][:, 0].min()
+    narrow = band_max[depth] <= 4
+    fine = allw[narrow]
+    assert len(fine) > 0
+    # (the nodes of those depths alone without the transforms, which would
+    # mix in the unset coefficients of the other nodes)
+    for work, skips, flags in ((allw, len(fine) == len(allw), 1), (fine, True, 0)):
+        out = {var: _plan_run(mra, P, f, grid, work, env[var], flags) for var in ("pencil", "fill", "items")}
+        (a, nta, nca, pa, la, _), (b, ntb, ncb, pb, _, _) = out["pencil"], out["items"]
+        assert nta == ntb and nca == ncb
+        assert 0 < pa <= nta and pb == 0
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) <= 2e-6
+        fa, fnt, fnc, fpa, fl, _ = out["fill"]
+        assert (fnt, fnc, fpa) == (nta, nca, pa)
+        assert np.array_equal(fa, a)
+        assert (la < fl) == skips
+        if skips:
+            assert pa == nta   # no term is left to the item kernel
 def test_plan_autotuning(gpu, case):
     # MWGPU_PLAN_AUTOTUNE times the three schedules (pencil kernel with 8 or
     # 16 consumer warps + item kernel, item kernel alone) x 4 chunk lengths on
