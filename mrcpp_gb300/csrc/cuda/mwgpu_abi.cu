@@ -2257,7 +2257,8 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         pl->pencil = use_pencil(lv);
         pl->pen_warps = pencil_warps();
         if (pl->pencil) {
-            // every term at the depth of every entry within the plan configuration's band width
+            // every term at the depth of every entry within the plan configuration's band
+            // width (MWGPU_PLAN_FILL=1 keeps the fill, to compare both forms)
             pl->pen_all_ok = std::getenv("MWGPU_PLAN_FILL") == nullptr;
             for (int wi = 0; wi < n && pl->pen_all_ok; wi++) {
                 const int depth = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]].x - o->mra.root_scale;
