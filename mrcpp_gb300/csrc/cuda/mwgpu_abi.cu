@@ -2259,12 +2259,29 @@ extern "C" mwgpu_status mwgpu_plan_create(mwgpu_ctx *ctx, const mwgpu_oper *o, i
         if (pl->pencil) {
             // every term at the depth of every entry within the plan configuration's band
             // width (MWGPU_PLAN_FILL=1 keeps the fill, to compare both forms)
+            // A term wider than that makes no item below the roots when its blocks
+            // other than (s, s) are outside its band at every translation: the
+            // work list leaves the (s, s) block out there, and every other
+            // component pair takes a non-(s, s) block in some direction.
+            const int R = o->n_rows, T = o->op.n_terms;
+            std::vector<signed char> wide(R, -1);   // per depth: -1 unknown, 0 / 1
+            auto depth_wide = [&](int depth) {
+                if (depth < 0 || depth >= R) return false;
+                if (wide[depth] < 0) {
+                    wide[depth] = 0;
+                    for (int t = 0; t < T; t++) {
+                        const int *w = &o->widths[((size_t)t * R + depth) * 5];
+                        if (w[4] <= mwgpu::kPencilCfgW[kPlanPencilCfg]) continue;
+                        if (depth != 0 && std::max(w[1], std::max(w[2], w[3])) < 0) continue;
+                        wide[depth] = 1;
+                        break;
+                    }
+                }
+                return wide[depth] != 0;
+            };
             pl->pen_all_ok = std::getenv("MWGPU_PLAN_FILL") == nullptr;
-            for (int wi = 0; wi < n && pl->pen_all_ok; wi++) {
-                const int depth = lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]].x - o->mra.root_scale;
-                if (depth >= 0 && depth < (int)o->band_max.size() && o->band_max[depth] > mwgpu::kPencilCfgW[kPlanPencilCfg])
-                    pl->pen_all_ok = false;
-            }
+            for (int wi = 0; wi < n && pl->pen_all_ok; wi++)
+                if (depth_wide(lv.outs[lv.tree[wi]]->h_idx[lv.node[wi]].x - o->mra.root_scale)) pl->pen_all_ok = false;
         }
         if ((term_order_supported(o->op.n_terms) || pl->pencil) && (s = plan_alloc(ctx, pl, &pl->d_items_cm, pl->items_cap))) return fail(s);
         if (pl->pencil) {

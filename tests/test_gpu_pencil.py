@@ -74,8 +74,9 @@ def _plan_run(mra, P, f, grid, work, env, flags=1):
         assert L.mwgpu_upload_operator(ctx, C.byref(mra.desc()), C.byref(P.desc()), 1e-4, C.byref(dop)) == 0
         rows = C.c_int()
         assert L.mwgpu_operator_bandwidths(ctx, dop, C.byref(rows), None, None) == 0
-        band_max = np.zeros(rows.value, dtype=np.int32)
-        assert L.mwgpu_operator_bandwidths(ctx, dop, C.byref(rows), None, mw._pi(band_max)) == 0
+        widths = np.zeros(P.desc().n_terms * rows.value * 5, dtype=np.int32)
+        assert L.mwgpu_operator_bandwidths(ctx, dop, C.byref(rows), mw._pi(widths), None) == 0
+        widths = widths.reshape(P.desc().n_terms, rows.value, 5)
         fx = f.export()
         fd = mw.MwgpuTreeDesc(len(fx["child0"]), mw._pi(fx["idx"]), mw._pi(fx["child0"]), mw._pd(fx["coefs"]), mw._pd(fx["norms"]))
         dinp = C.c_void_p()
@@ -103,7 +104,7 @@ def _plan_run(mra, P, f, grid, work, env, flags=1):
         c = np.zeros((n, 8 * 512))
         assert L.mwgpu_download_tree(ctx, dout, mw._pd(c), None) == 0
         assert L.mwgpu_plan_destroy(ctx, plan) == 0
-        return c[work], st.node_terms, st.components, pnt.value, lpe.value, band_max
+        return c[work], st.node_terms, st.components, pnt.value, lpe.value, widths
     finally:
         for k in env:
             os.environ.pop(k, None)
@@ -122,9 +123,13 @@ def test_plan_path(gpu, case):
     gx = grid.export()
     allw = np.arange(len(gx["child0"]), dtype=np.int32)
     env = {"pencil": {}, "fill": {"MWGPU_PLAN_FILL": "1"}, "items": {"MWGPU_NO_PENCIL": "1"}}
-    band_max = _plan_run(mra, P, f, grid, allw[:1], {"MWGPU_NO_PENCIL": "1"}, 0)[5]
+    w = _plan_run(mra, P, f, grid, allw[:1], {"MWGPU_NO_PENCIL": "1"}, 0)[5]
     depth = gx["idx"][:, 0] - gx["idx"][:, 0].min()
-    narrow = band_max[depth] <= 4
+    # a depth leaves nothing to the item kernel when every term there has band
+    # width <= 4, or (below the roots, where the (s, s) block is left out) only
+    # its (s, s) block wider and no other block in its band
+    blocks = (w[:, :, 4] <= 4) | ((np.arange(w.shape[1]) > 0)[None, :] & (w[:, :, 1:4].max(axis=2) < 0))
+    narrow = blocks.all(axis=0)[depth]
     fine = allw[narrow]
     assert len(fine) > 0
     # (the nodes of those depths alone without the transforms, which would
